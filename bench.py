@@ -1,0 +1,313 @@
+"""Benchmark: end-to-end cells/s of CoLoRe's mock-generation path.
+
+One step is the whole driver sequence of src/main.c:66-125 on one
+realisation: Gaussian density and potential (fill + 3-D c2r), physical
+density (1LPT + CIC for the 1024^3 configuration), redshift-bin bias
+normalisation, Poisson sources with their local properties and count map,
+the 64-shell intensity map and the 8 convergence planes.
+
+  value : N^3 * steps / device time, inputs (tables) resident on the GPU;
+  e2e   : the same through the C ABI with host buffers: every step uploads
+          the tables and downloads the catalogue, count map, intensity and
+          convergence maps into pinned host memory inside the timed region.
+
+--impl reference times the CPU restatement of the reference (the oracle,
+FP64, OpenMP on all host cores) on a bounded sample of the same workload.
+Multi-GPU runs are independent replicas (one realisation per rank, seed +
+rank): the path has no exchange step on one node.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BASELINE = json.load(open(os.path.join(ROOT, "BASELINE.json")))
+METRIC = BASELINE["metric"]
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d["hbm_gbs"], "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                self.samples.append(f)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        import numpy as np
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if "Active" in s[5 + i]
+                          and "Not" not in s[5 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def config_spec(name, n):
+    from colore_gb300 import inputs
+    spec = inputs.scaled(name, n) if n else dict(inputs.CONFIGS[name])
+    return spec
+
+
+# Algorithmic HBM bytes per cell of each launch group (FP32 grids; per pass
+# and field one read and one write of 4 bytes per cell; the fill+z pass only
+# writes).  fields: fill+z 2x4 W, y 2x(4R+4W), x 2x(4R+4W) = 40 B/cell.
+ALGO_BYTES_PER_CELL = {"field_fft": 40.0, "lpt_fft": 60.0, "dens_bins": 8.0, "srcs_count": 6.0}
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import colore_gb300 as cg
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        dist = None
+    torch.cuda.set_device(local)
+    spec = config_spec(args.config, args.n)
+    spec["seed"] = spec["seed"] + rank
+    d = tempfile.mkdtemp(prefix="colore_bench_%d_" % rank)
+    from colore_gb300 import inputs
+    prm = cg.Params(inputs.write_inputs(d, spec))
+    cfg = prm.config
+    n = cfg.n_grid
+    ncell = float(n) ** 3
+    m = cg.Mock(prm, device=local)
+    stream = torch.cuda.Stream()
+    m.set_stream(stream.cuda_stream)
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        m.run()
+    m.sync()
+    # device-timed region (inputs resident; grids of 4.3 GB per field >> 129 MB L2)
+    m.set_profiling(True)
+    l0 = m.launches()
+    barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        with torch.cuda.stream(stream):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                m.run()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t0
+    barrier()
+    launches = m.launches() - l0
+    ms = e0.elapsed_time(e1)
+    groups = {}
+    for name, t in m.kernel_times():
+        g = groups.setdefault(name, [0.0, 0])
+        g[0] += t
+        g[1] += 1
+    m.set_profiling(False)
+    nsrc = [m.num_sources(i) for i in range(cfg.n_srcs)]
+    # end-to-end through the C ABI with host buffers
+    outs = {}
+    for i in range(cfg.n_srcs):
+        k = int(nsrc[i] * 1.25) + 1024
+        outs["pos%d" % i] = torch.empty((k, 4), dtype=torch.float32, pin_memory=True).numpy()
+        outs["ipix%d" % i] = torch.empty(k, dtype=torch.int32, pin_memory=True).numpy()
+        outs["src%d" % i] = torch.empty((k, 9), dtype=torch.float32, pin_memory=True).numpy()
+        if cfg.nside_count[i]:
+            outs["cmap%d" % i] = torch.empty(12 * cfg.nside_count[i] ** 2, dtype=torch.int32,
+                                             pin_memory=True).numpy()
+    for i in range(cfg.n_imap):
+        outs["imap%d" % i] = torch.empty((cfg.imap_nr[i], 12 * cfg.nside_imap[i] ** 2), dtype=torch.float32,
+                                         pin_memory=True).numpy()
+    if cfg.do_kappa:
+        outs["kappa"] = torch.empty((cfg.n_kappa, 12 * cfg.nside_kappa ** 2), dtype=torch.float32,
+                                    pin_memory=True).numpy()
+    e2e_steps = max(1, min(args.steps, 3))
+    d2h = 0
+    h2d = 0
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        m.upload_tables()
+        m.run()
+        d2h = 0
+        for i in range(cfg.n_srcs):
+            ns = m.num_sources(i)
+            c = {"pos": outs["pos%d" % i][:ns], "ipix": outs["ipix%d" % i][:ns], "src": outs["src%d" % i][:ns]}
+            m.catalog(i, out=c)
+            d2h += ns * (16 + 4 + 36)
+            if cfg.nside_count[i]:
+                m.count_map(i, out=outs["cmap%d" % i])
+                d2h += outs["cmap%d" % i].nbytes
+        for i in range(cfg.n_imap):
+            m.imap(i, out=outs["imap%d" % i])
+            d2h += outs["imap%d" % i].nbytes
+        if cfg.do_kappa:
+            m.kappa(out=outs["kappa"])
+            d2h += outs["kappa"].nbytes
+    torch.cuda.synchronize()
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    barrier()
+    na = cg.NA
+    h2d = 8 * (9 * na + 2 * na * (cfg.n_srcs + cfg.n_imap) + cfg.numk) // 2  # tables as float
+    t_step = ms / 1e3 / args.steps
+    if dist:
+        tt = torch.tensor([t_step, t_e2e], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step, t_e2e = tt.tolist()
+    hbm, peak_kind = peaks()
+    # roofline of the dominant HBM-bound group
+    rl = None
+    avg = {k: v[0] / max(v[1], 1) for k, v in groups.items()}
+    for name in ("field_fft", "lpt_fft", "dens_bins", "srcs_count"):
+        if name in avg:
+            bytes_launch = ALGO_BYTES_PER_CELL[name] * ncell
+            a = bytes_launch / (avg[name] / 1e3) / 1e9
+            if rl is None or avg[name] > rl["_t"]:
+                rl = {"kernel": name, "bound": "hbm", "achieved": round(a, 1), "peak": hbm, "unit": "GB/s",
+                      "frac": round(a / hbm, 4), "traffic": None, "peak_kind": peak_kind,
+                      "algorithmic_bytes_per_launch": bytes_launch, "avg_launch_ms": round(avg[name], 3),
+                      "_t": avg[name]}
+    if rl:
+        rl.pop("_t")
+    if rank != 0:
+        return
+    out = {
+        "metric": METRIC, "value": world * ncell / t_step, "unit": "cells/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (EH98 no-wiggle P(k), analytic N(z)/b(z)/T(z); random seeds per rank)",
+        "config": {"workload": "%s: %d^3, dens_type %d, %d source pops, %d imap shells nside %s, %d kappa planes"
+                               % (args.config, n, cfg.dens_type, cfg.n_srcs,
+                                  sum(cfg.imap_nr[i] for i in range(cfg.n_imap)),
+                                  [cfg.nside_imap[i] for i in range(cfg.n_imap)], cfg.n_kappa if cfg.do_kappa else 0),
+                   "n_grid": n, "l2": "inputs larger than L2 (4.3 GB per field)", "parallelism": "replicas"},
+        "e2e": {"value": world * ncell / t_e2e, "unit": "cells/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": t_e2e * 1e3},
+        "gpu_launches": int(launches),
+        "kernel_ms": {k: round(v, 3) for k, v in avg.items()},
+        "sources": nsrc,
+        "wall_s_timed": t_wall,
+        "roofline": rl,
+        "clocks": clk.summary(),
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args, quick=True)
+    print(json.dumps(out))
+
+
+def cpu_baseline(args, quick=False):
+    """FP64 oracle (the reference's arithmetic, OpenMP) on a bounded sample:
+    the same configuration at a reduced grid, reported as cells/s."""
+    import colore_gb300 as cg
+    from colore_gb300 import inputs
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    n = args.cpu_n
+    spec = config_spec(args.config, n)
+    d = tempfile.mkdtemp(prefix="colore_cpu_")
+    prm = cg.Params(inputs.write_inputs(d, spec))
+    t0 = time.perf_counter()
+    nsrc, _ = orc.run_mock64(prm.config)
+    t = time.perf_counter() - t0
+    cores = os.cpu_count()
+    return {"value": n ** 3 / t, "unit": "cells/s", "cores": cores, "kind": "port",
+            "sample": "%s at %d^3 (full pipeline, FP64 oracle, %d OpenMP threads), %.1f s" % (args.config, n, cores, t)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    vals = []
+    for _ in range(args.warmup):
+        pass
+    cb = None
+    for _ in range(max(1, args.steps)):
+        cb = cpu_baseline(args)
+        vals.append(cb["value"])
+    v = sum(vals) / len(vals)
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "cells/s", "n_gpus": 0,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "%s (sampled at %d^3 on the host)" % (args.config, args.cpu_n)},
+           "cpu_baseline": dict(cb, value=v),
+           "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c4")
+    ap.add_argument("--n", type=int, default=0, help="override the grid size")
+    ap.add_argument("--cpu-n", type=int, default=128)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

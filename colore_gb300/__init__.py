@@ -1,0 +1,290 @@
+"""colore_gb300: CoLoRe's mock-generation path on one GB300 (sm_103a).
+
+The product is the C library colore_gb300/lib/libcolore_cuda.so (C ABI in
+include/colore_cuda.h and include/colore_host.h).  This module binds it with
+ctypes for Python users, tests and the benchmark:
+
+    from colore_gb300 import Mock
+    m = Mock.from_param_file("run.cfg")
+    m.run()                      # main.c stage sequence on the GPU
+    ra_dec = m.catalog(0)["src"]
+
+There is no CPU fallback: importing works without a GPU, but creating a Mock
+without the built library or without a CUDA device raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "lib", "libcolore_cuda.so")
+
+NPOP_MAX = 10
+NPLANES_MAX = 100
+NA = 5001
+PREC_F32, PREC_F64 = 0, 1
+DENS_LGNR, DENS_1LPT, DENS_CLIP = 0, 1, 3
+ERRORS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "device error flag",
+          5: "stage out of order"}
+
+_dp = C.POINTER(C.c_double)
+
+
+class Config(C.Structure):
+    """Mirror of cg_config (include/colore_cuda.h)."""
+    _fields_ = [
+        ("precision", C.c_int), ("n_grid", C.c_int), ("l_box", C.c_double), ("pos_obs", C.c_double * 3),
+        ("seed", C.c_uint64),
+        ("omega_m", C.c_double), ("hubble_0", C.c_double), ("fgrowth_0", C.c_double),
+        ("prefac_lensing", C.c_double), ("r_max", C.c_double),
+        ("r2_smooth", C.c_double), ("do_smoothing", C.c_int), ("smooth_potential", C.c_int),
+        ("dens_type", C.c_int), ("bias_model", C.c_int),
+        ("numk", C.c_int), ("logkmin", C.c_double), ("logkmax", C.c_double), ("idlogk", C.c_double),
+        ("n_scal", C.c_double), ("pkarr", _dp),
+        ("glob_idr", C.c_double),
+        ("r_arr_r2z", _dp), ("z_arr_r2z", _dp), ("growth_d_arr", _dp), ("growth_d2_arr", _dp),
+        ("growth_v_arr", _dp), ("growth_pd_arr", _dp), ("ihub_arr", _dp), ("a_arr_a2r", _dp), ("r_arr_a2r", _dp),
+        ("n_srcs", C.c_int), ("srcs_nz_arr", _dp * NPOP_MAX), ("srcs_bz_arr", _dp * NPOP_MAX),
+        ("nside_base", C.c_int), ("nside_count", C.c_int * NPOP_MAX),
+        ("n_imap", C.c_int), ("imap_tz_arr", _dp * NPOP_MAX), ("imap_bz_arr", _dp * NPOP_MAX),
+        ("nside_imap", C.c_int * NPOP_MAX), ("imap_nr", C.c_int * NPOP_MAX),
+        ("imap_r0", _dp * NPOP_MAX), ("imap_rf", _dp * NPOP_MAX),
+        ("do_kappa", C.c_int), ("n_kappa", C.c_int), ("nside_kappa", C.c_int),
+        ("kappa_r", C.c_double * NPLANES_MAX),
+        ("need_beaming", C.c_int),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    """The loaded libcolore_cuda.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libcolore_cuda.so is not built: run colore_gb300.build.build() "
+                               "(python -c 'import __graft_entry__ as g; g.build()')")
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        sigs = {
+            "cg_create": (C.c_int, [C.POINTER(vp), C.POINTER(Config), C.c_int]),
+            "cg_destroy": (None, [vp]),
+            "cg_last_error": (C.c_char_p, [vp]),
+            "cg_set_stream": (C.c_int, [vp, vp]),
+            "cg_sync": (C.c_int, [vp]),
+            "cg_memory_estimate": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_ulonglong)]),
+            "cg_upload_tables": (C.c_int, [vp, C.POINTER(Config)]),
+            "cg_create_cartesian_fields": (C.c_int, [vp]),
+            "cg_get_sigma2": (C.c_int, [vp, _dp, _dp]),
+            "cg_compute_physical_density_field": (C.c_int, [vp]),
+            "cg_compute_density_normalization": (C.c_int, [vp]),
+            "cg_collect_density_normalization": (C.c_int, [vp, C.c_int, C.c_double, _dp,
+                                                           C.POINTER(C.c_ulonglong), _dp, _dp]),
+            "cg_set_norm_tables": (C.c_int, [vp, _dp, _dp, _dp, _dp]),
+            "cg_srcs_set_cartesian": (C.c_int, [vp, C.POINTER(C.c_longlong)]),
+            "cg_imap_set_cartesian": (C.c_int, [vp]),
+            "cg_get_beam_properties": (C.c_int, [vp]),
+            "cg_run_mock": (C.c_int, [vp]),
+            "cg_download_grid": (C.c_int, [vp, C.c_int, vp]),
+            "cg_num_sources": (C.c_longlong, [vp, C.c_int]),
+            "cg_download_catalog": (C.c_int, [vp, C.c_int, vp, vp, vp]),
+            "cg_download_count_map": (C.c_int, [vp, C.c_int, vp]),
+            "cg_download_imap": (C.c_int, [vp, C.c_int, vp, vp]),
+            "cg_download_kappa": (C.c_int, [vp, vp]),
+            "cg_download_norm": (C.c_int, [vp, C.c_int, C.c_int, vp, vp]),
+            "cg_kernel_launches": (C.c_longlong, [vp]),
+            "cg_set_profiling": (C.c_int, [vp, C.c_int]),
+            "cg_kernel_times": (C.c_int, [vp, C.c_char_p, C.c_size_t, C.POINTER(C.c_float), C.c_int,
+                                          C.POINTER(C.c_int)]),
+            "cg_read_run_params": (C.c_int, [C.c_char_p, C.POINTER(vp), C.c_char_p, C.c_size_t]),
+            "cg_params_free": (None, [vp]),
+            "cg_params_to_config": (C.c_int, [vp, C.POINTER(Config)]),
+        }
+        for name, (res, args) in sigs.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def exported_symbols():
+    """Names of the C-ABI entry points this binding expects in the library."""
+    return ["cg_create", "cg_destroy", "cg_last_error", "cg_set_stream", "cg_sync", "cg_memory_estimate",
+            "cg_upload_tables", "cg_create_cartesian_fields", "cg_get_sigma2",
+            "cg_compute_physical_density_field", "cg_compute_density_normalization",
+            "cg_collect_density_normalization", "cg_set_norm_tables", "cg_srcs_set_cartesian",
+            "cg_imap_set_cartesian", "cg_get_beam_properties", "cg_run_mock", "cg_download_grid",
+            "cg_num_sources", "cg_download_catalog", "cg_download_count_map", "cg_download_imap",
+            "cg_download_kappa", "cg_download_norm", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_read_run_params",
+            "cg_params_free", "cg_params_to_config"]
+
+
+class CGError(RuntimeError):
+    pass
+
+
+class Params:
+    """Parsed run parameters and FP64 tables (cg_params, C-owned)."""
+
+    def __init__(self, fname):
+        L = lib()
+        self._p = C.c_void_p()
+        err = C.create_string_buffer(1024)
+        rc = L.cg_read_run_params(os.fsencode(fname), C.byref(self._p), err, 1024)
+        if rc:
+            raise CGError("read_run_params(%s): %s" % (fname, err.value.decode()))
+        self.config = Config()
+        L.cg_params_to_config(self._p, C.byref(self.config))
+
+    def __del__(self):
+        if getattr(self, "_p", None) and _lib is not None:
+            _lib.cg_params_free(self._p)
+            self._p = None
+
+
+def grid_shape(n):
+    """Padded real grid shape [z][y][2(N/2+1)] of the in-place layout."""
+    return (n, n, 2 * (n // 2 + 1))
+
+
+class Mock:
+    """One GPU context running CoLoRe's stages (cg_* C ABI)."""
+
+    def __init__(self, params, device=0):
+        self.params = params
+        self.cfg = params.config
+        L = lib()
+        self._c = C.c_void_p()
+        rc = L.cg_create(C.byref(self._c), C.byref(self.cfg), device)
+        if rc:
+            raise CGError("cg_create failed (%s)" % ERRORS.get(rc, rc))
+
+    @classmethod
+    def from_param_file(cls, fname, device=0):
+        return cls(Params(fname), device)
+
+    def close(self):
+        if getattr(self, "_c", None):
+            lib().cg_destroy(self._c)
+            self._c = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc, what):
+        if rc:
+            msg = lib().cg_last_error(self._c)
+            raise CGError("%s: %s (%s)" % (what, ERRORS.get(rc, rc), msg.decode() if msg else ""))
+
+    @property
+    def n(self):
+        return self.cfg.n_grid
+
+    def set_stream(self, stream_handle):
+        self._chk(lib().cg_set_stream(self._c, C.c_void_p(stream_handle)), "cg_set_stream")
+
+    def sync(self):
+        self._chk(lib().cg_sync(self._c), "cg_sync")
+
+    def upload_tables(self):
+        self._chk(lib().cg_upload_tables(self._c, C.byref(self.cfg)), "cg_upload_tables")
+
+    # stages (src/main.c:66-125)
+    def create_cartesian_fields(self):
+        self._chk(lib().cg_create_cartesian_fields(self._c), "create_cartesian_fields")
+
+    def sigma2(self):
+        s, m = C.c_double(), C.c_double()
+        self._chk(lib().cg_get_sigma2(self._c, C.byref(s), C.byref(m)), "get_sigma2")
+        return s.value, m.value
+
+    def compute_physical_density_field(self):
+        self._chk(lib().cg_compute_physical_density_field(self._c), "compute_physical_density_field")
+
+    def compute_density_normalization(self):
+        self._chk(lib().cg_compute_density_normalization(self._c), "compute_density_normalization")
+
+    def srcs_set_cartesian(self):
+        n = (C.c_longlong * NPOP_MAX)()
+        self._chk(lib().cg_srcs_set_cartesian(self._c, n), "srcs_set_cartesian")
+        return [n[i] for i in range(self.cfg.n_srcs)]
+
+    def imap_set_cartesian(self):
+        self._chk(lib().cg_imap_set_cartesian(self._c), "imap_set_cartesian")
+
+    def get_beam_properties(self):
+        self._chk(lib().cg_get_beam_properties(self._c), "get_beam_properties")
+
+    def run(self):
+        self._chk(lib().cg_run_mock(self._c), "run_mock")
+
+    def launches(self):
+        return lib().cg_kernel_launches(self._c)
+
+    def set_profiling(self, on=True):
+        self._chk(lib().cg_set_profiling(self._c, 1 if on else 0), "set_profiling")
+
+    def kernel_times(self):
+        """[(group name, ms)] of the launch groups since the last call."""
+        names = C.create_string_buffer(1 << 16)
+        ms = (C.c_float * 4096)()
+        n = C.c_int()
+        self._chk(lib().cg_kernel_times(self._c, names, 1 << 16, ms, 4096, C.byref(n)), "kernel_times")
+        nm = [s for s in names.value.decode().split(";") if s]
+        return list(zip(nm, [ms[i] for i in range(min(n.value, 4096))]))
+
+    # host mirrors
+    def grid(self, which=0, out=None):
+        a = out if out is not None else np.empty(grid_shape(self.n), np.float32)
+        self._chk(lib().cg_download_grid(self._c, which, a.ctypes.data), "download_grid")
+        return a
+
+    def num_sources(self, ipop):
+        return lib().cg_num_sources(self._c, ipop)
+
+    def catalog(self, ipop, pos=True, ipix=True, src=True, out=None):
+        n = self.num_sources(ipop)
+        d = out or {}
+        if pos and "pos" not in d:
+            d["pos"] = np.empty((n, 4), np.float32)
+        if ipix and "ipix" not in d:
+            d["ipix"] = np.empty(n, np.int32)
+        if src and "src" not in d:
+            d["src"] = np.empty((n, 9), np.float32)
+        ptr = lambda k: d[k].ctypes.data if (k in d and d[k] is not None and n > 0) else None
+        self._chk(lib().cg_download_catalog(self._c, ipop, ptr("pos"), ptr("ipix"), ptr("src")), "download_catalog")
+        return d
+
+    def count_map(self, ipop, out=None):
+        ns = self.cfg.nside_count[ipop]
+        a = out if out is not None else np.empty(12 * ns * ns, np.int32)
+        self._chk(lib().cg_download_count_map(self._c, ipop, a.ctypes.data), "download_count_map")
+        return a
+
+    def imap(self, ipop, with_nadd=False, out=None):
+        ns, nr = self.cfg.nside_imap[ipop], self.cfg.imap_nr[ipop]
+        m = out if out is not None else np.empty((nr, 12 * ns * ns), np.float32)
+        na = np.empty((nr, 12 * ns * ns), np.int32) if with_nadd else None
+        self._chk(lib().cg_download_imap(self._c, ipop, m.ctypes.data, na.ctypes.data if with_nadd else None),
+                  "download_imap")
+        return (m, na) if with_nadd else m
+
+    def kappa(self, out=None):
+        ns = self.cfg.nside_kappa
+        m = out if out is not None else np.empty((self.cfg.n_kappa, 12 * ns * ns), np.float32)
+        self._chk(lib().cg_download_kappa(self._c, m.ctypes.data), "download_kappa")
+        return m
+
+    def norm_table(self, kind, ipop):
+        """Current FP32 normalisation table (kind 0: sources, 1: intensity maps)
+        and its (below, above) edge values, as used by the kernels."""
+        t = np.empty(NA, np.float32)
+        e = np.empty(2, np.float32)
+        self._chk(lib().cg_download_norm(self._c, kind, ipop, t.ctypes.data, e.ctypes.data), "download_norm")
+        return t, e

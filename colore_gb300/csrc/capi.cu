@@ -1,0 +1,1151 @@
+/*
+ * capi.cu -- the C ABI of libcolore_cuda.so (declared in colore_cuda.h):
+ * context, device tables, stage orchestration and host mirrors.
+ *
+ * The host-side parts of the stages (bias-normalisation spline,
+ * density.c:1272-1355; shell sub-sampling factors, imap.c:153-174; kappa
+ * radial kernels, kappa.c:87-116) run here in FP64 on the small tables they
+ * need, exactly as the reference computes them, and are uploaded in FP32.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/colore_cuda.h"
+#include "cg_dev.cuh"
+#include "dens_api.h"
+#include "field_api.h"
+#include "imap_api.h"
+#include "kappa_api.h"
+#include "srcs_api.h"
+
+using namespace cg;
+
+namespace {
+
+struct HostTab { /* double copy of one background table */
+  std::vector<double> v;
+  double f0 = 0, ff = 0;
+};
+
+struct Cat {
+  float4 *pos = nullptr;
+  int *ipix = nullptr;
+  float *src = nullptr;
+  long long n = 0, cap = 0;
+  int *cmap = nullptr;
+  long long cmap_npix = 0;
+};
+
+struct Imap {
+  int nr = 0, nside = 0;
+  long long npix = 0;
+  float *r0 = nullptr, *rf = nullptr;
+  int *nsub = nullptr;
+  int nsub_lo = 0, nsub_hi = 0;
+  float rmin = 0, rmax = 0;
+  float *data = nullptr;
+  int *nadd = nullptr;
+};
+
+} /* namespace */
+
+struct cg_ctx {
+  int device = 0, nsm = 0;
+  cudaStream_t stream = nullptr, own_stream = nullptr;
+  cg_config cfg;
+  int N = 0, NH = 0;
+  size_t grid_floats = 0;
+  /* host double tables */
+  std::vector<double> h_r, h_z, h_d1, h_v1, h_ih, h_a, h_ra;
+  /* device tables */
+  float *d_tabs = nullptr;
+  Grid1 g;
+  Tab zt, d1, d2, v1, pd, ih;
+  const float *a_a2r = nullptr, *r_a2r = nullptr;
+  Tab nz[CG_NPOP_MAX], bz[CG_NPOP_MAX], norm[CG_NPOP_MAX];
+  Tab tz[CG_NPOP_MAX], bzi[CG_NPOP_MAX], normi[CG_NPOP_MAX];
+  float *d_norm = nullptr; /* (n_srcs + n_imap) * NA */
+  float *d_pk = nullptr;
+  float2 *d_twN = nullptr, *d_twH = nullptr;
+  Box box;
+  FillParams fill;
+  /* grids */
+  float *d_dens = nullptr, *d_npot = nullptr, *d_disp[3] = {nullptr, nullptr, nullptr};
+  double2 *d_part = nullptr;
+  size_t npart = 0;
+  double *d_stats = nullptr;
+  float *d_s2f = nullptr;
+  unsigned int *d_err = nullptr;
+  /* normalisation bins */
+  unsigned long long *d_ncount = nullptr;
+  double *d_zsum = nullptr, *d_bsum = nullptr;
+  int pending_mode = CG_DMODE_NONE;
+  /* sources */
+  unsigned short *d_counts = nullptr;
+  long long *d_bsums = nullptr, *d_total = nullptr;
+  Cat cat[CG_NPOP_MAX];
+  /* intensity maps */
+  Imap im[CG_NPOP_MAX];
+  float *d_tmpmap = nullptr;
+  size_t tmpmap_n = 0;
+  /* kappa */
+  float *d_kmap = nullptr, *d_kfac = nullptr, *d_kinv = nullptr;
+  int *d_kir = nullptr;
+  int knr = 0, kpl = 0;
+  float kdr = 0;
+  long long knpix = 0;
+  /* optional per-kernel event log */
+  int profiling = 0;
+  struct Ev {
+    const char *name;
+    cudaEvent_t a, b;
+  };
+  std::vector<Ev> evlog;
+  /* state */
+  int have_fields = 0, have_density = 0, have_norm = 0, have_srcs = 0;
+  long long launches = 0;
+  char err[1024];
+};
+
+/* ------------------------------------------------------------------------ */
+/* errors                                                                   */
+/* ------------------------------------------------------------------------ */
+static int fail(cg_ctx *c, int code, const char *fmt, ...)
+{
+  if (c) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(c->err, sizeof(c->err), fmt, ap);
+    va_end(ap);
+  }
+  return code;
+}
+
+#define CUDA_TRY(c, call)                                                                        \
+  do {                                                                                           \
+    cudaError_t e_ = (call);                                                                     \
+    if (e_ != cudaSuccess) return fail((c), CG_ECUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                                       __FILE__, __LINE__);                                     \
+  } while (0)
+
+template <class T>
+static int dalloc(cg_ctx *c, T **p, size_t n)
+{
+  if (*p) {
+    cudaFree(*p);
+    *p = nullptr;
+  }
+  if (n == 0) return CG_OK;
+  cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return fail(c, CG_ENOMEM, "cudaMalloc of %zu bytes failed: %s", n * sizeof(T), cudaGetErrorString(e));
+  }
+  return CG_OK;
+}
+
+static int check_device_errors(cg_ctx *c)
+{
+  unsigned int h = 0;
+  CUDA_TRY(c, cudaMemcpyAsync(&h, c->d_err, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (h) {
+    CUDA_TRY(c, cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), c->stream));
+    return fail(c, CG_EDEVICE, "device error flags 0x%x (1: >65535 sources in a cell, 2: catalog overflow, "
+                               "4: shell search, 8: imap sub-sampling)", h);
+  }
+  return CG_OK;
+}
+
+/* Event pair around a launch group when profiling is on. */
+struct ProfScope {
+  cg_ctx *c;
+  size_t i;
+  ProfScope(cg_ctx *c_, const char *name) : c(c_), i((size_t)-1)
+  {
+    if (!c->profiling) return;
+    cg_ctx::Ev e;
+    e.name = name;
+    cudaEventCreate(&e.a);
+    cudaEventCreate(&e.b);
+    cudaEventRecord(e.a, c->stream);
+    c->evlog.push_back(e);
+    i = c->evlog.size() - 1;
+  }
+  ~ProfScope()
+  {
+    if (i != (size_t)-1) cudaEventRecord(c->evlog[i].b, c->stream);
+  }
+};
+
+/* get_bg on the host double tables (cosmo.c:30-38) */
+static double host_bg(const cg_ctx *c, const std::vector<double> &f, double f0, double ff, double r)
+{
+  const int na = CG_NA;
+  if (r <= 0) return f0;
+  if (r >= c->h_r[na - 1]) return ff;
+  int ir = (int)(r * c->cfg.glob_idr);
+  return f[ir] + (f[ir + 1] - f[ir]) * (r - c->h_r[ir]) * c->cfg.glob_idr;
+}
+
+static bool size_supported(int n)
+{
+  switch (n) {
+#define X(k) case k:
+    CG_FIELD_SIZES(X)
+#undef X
+    return true;
+    default:
+      return false;
+  }
+}
+
+static cudaError_t run_gauss(int n, const cg_field_launch *L)
+{
+  switch (n) {
+#define X(k) \
+  case k:    \
+    return cg_field_gauss_##k(L);
+    CG_FIELD_SIZES(X)
+#undef X
+  }
+  return cudaErrorInvalidValue;
+}
+
+static cudaError_t run_lpt(int n, const cg_field_launch *L)
+{
+  switch (n) {
+#define X(k) \
+  case k:    \
+    return cg_field_lpt_##k(L);
+    CG_FIELD_SIZES(X)
+#undef X
+  }
+  return cudaErrorInvalidValue;
+}
+
+static size_t npartials(int n)
+{
+  switch (n) {
+#define X(k) \
+  case k:    \
+    return cg_field_npartials_##k();
+    CG_FIELD_SIZES(X)
+#undef X
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* tables                                                                   */
+/* ------------------------------------------------------------------------ */
+static int validate(const cg_config *cfg, char *msg, size_t len)
+{
+  if (!cfg) return snprintf(msg, len, "NULL config"), CG_EINVAL;
+  if (cfg->precision != CG_PREC_F32)
+    return snprintf(msg, len, "precision %d: this library builds the FP32 path only", cfg->precision), CG_EINVAL;
+  if (!size_supported(cfg->n_grid))
+    return snprintf(msg, len, "n_grid=%d unsupported (2^a 3^b sizes 64..2048 in field_api.h)", cfg->n_grid),
+           CG_EINVAL;
+  if (!(cfg->l_box > 0)) return snprintf(msg, len, "l_box must be > 0"), CG_EINVAL;
+  if (cfg->numk < 2 || !cfg->pkarr) return snprintf(msg, len, "P(k) table missing"), CG_EINVAL;
+  if (cfg->n_srcs < 0 || cfg->n_srcs > CG_NPOP_MAX || cfg->n_imap < 0 || cfg->n_imap > CG_NPOP_MAX)
+    return snprintf(msg, len, "population count out of range"), CG_EINVAL;
+  if (cfg->do_kappa && (cfg->n_kappa < 1 || cfg->n_kappa > CG_NPLANES_MAX || cfg->nside_kappa < 1))
+    return snprintf(msg, len, "kappa planes or nside out of range"), CG_EINVAL;
+  if (cfg->dens_type != CG_DENS_LGNR && cfg->dens_type != CG_DENS_1LPT && cfg->dens_type != CG_DENS_CLIP)
+    return snprintf(msg, len, "dens_type %d not supported", cfg->dens_type), CG_EINVAL;
+  const double *req[] = {cfg->r_arr_r2z, cfg->z_arr_r2z, cfg->growth_d_arr, cfg->growth_d2_arr, cfg->growth_v_arr,
+                         cfg->growth_pd_arr, cfg->ihub_arr, cfg->a_arr_a2r, cfg->r_arr_a2r};
+  for (const double *p : req)
+    if (!p) return snprintf(msg, len, "background table missing"), CG_EINVAL;
+  for (int i = 0; i < cfg->n_srcs; i++)
+    if (!cfg->srcs_nz_arr[i] || !cfg->srcs_bz_arr[i]) return snprintf(msg, len, "source table missing"), CG_EINVAL;
+  for (int i = 0; i < cfg->n_imap; i++) {
+    if (!cfg->imap_tz_arr[i] || !cfg->imap_bz_arr[i] || !cfg->imap_r0[i] || !cfg->imap_rf[i] ||
+        cfg->imap_nr[i] < 1 || cfg->nside_imap[i] < 1)
+      return snprintf(msg, len, "intensity-map table missing"), CG_EINVAL;
+  }
+  if (cfg->n_srcs > 0 && cfg->nside_base < 1) return snprintf(msg, len, "nside_base must be >= 1"), CG_EINVAL;
+  return CG_OK;
+}
+
+extern "C" int cg_upload_tables(cg_ctx *c, const cg_config *cfg)
+{
+  if (!c) return CG_EINVAL;
+  if (int rc = validate(cfg, c->err, sizeof(c->err))) return rc;
+  if (cfg->n_grid != c->N) return fail(c, CG_EINVAL, "n_grid differs from the context's");
+  c->cfg = *cfg;
+  const int na = CG_NA;
+  auto cp = [&](std::vector<double> &v, const double *src) { v.assign(src, src + na); };
+  cp(c->h_r, cfg->r_arr_r2z);
+  cp(c->h_z, cfg->z_arr_r2z);
+  cp(c->h_d1, cfg->growth_d_arr);
+  cp(c->h_v1, cfg->growth_v_arr);
+  cp(c->h_ih, cfg->ihub_arr);
+  cp(c->h_a, cfg->a_arr_a2r);
+  cp(c->h_ra, cfg->r_arr_a2r);
+  /* packed float tables: 9 background + 2 per population + 2 per species */
+  const int ntab = 9 + 2 * cfg->n_srcs + 2 * cfg->n_imap;
+  std::vector<float> h((size_t)ntab * na);
+  const double *srcs[9] = {cfg->r_arr_r2z, cfg->z_arr_r2z, cfg->growth_d_arr, cfg->growth_d2_arr, cfg->growth_v_arr,
+                           cfg->growth_pd_arr, cfg->ihub_arr, cfg->a_arr_a2r, cfg->r_arr_a2r};
+  int k = 0;
+  for (int t = 0; t < 9; t++, k++)
+    for (int i = 0; i < na; i++) h[(size_t)k * na + i] = (float)srcs[t][i];
+  for (int p = 0; p < cfg->n_srcs; p++) {
+    for (int i = 0; i < na; i++) h[(size_t)k * na + i] = (float)cfg->srcs_nz_arr[p][i];
+    k++;
+    for (int i = 0; i < na; i++) h[(size_t)k * na + i] = (float)cfg->srcs_bz_arr[p][i];
+    k++;
+  }
+  for (int p = 0; p < cfg->n_imap; p++) {
+    for (int i = 0; i < na; i++) h[(size_t)k * na + i] = (float)cfg->imap_tz_arr[p][i];
+    k++;
+    for (int i = 0; i < na; i++) h[(size_t)k * na + i] = (float)cfg->imap_bz_arr[p][i];
+    k++;
+  }
+  if (int rc = dalloc(c, &c->d_tabs, h.size())) return rc;
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_tabs, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  const float *T = c->d_tabs;
+  auto tab = [&](int i) { return T + (size_t)i * na; };
+  auto last = [&](const double *a) { return (float)a[na - 1]; };
+  c->g.r = tab(0);
+  c->g.r_last = (float)cfg->r_arr_r2z[na - 1];
+  c->g.idr = (float)cfg->glob_idr;
+  /* edge values of get_bg, cosmo.c:42-57 */
+  c->zt = Tab{tab(1), 0.0f, last(cfg->z_arr_r2z)};
+  c->d1 = Tab{tab(2), 1.0f, last(cfg->growth_d_arr)};
+  c->d2 = Tab{tab(3), (float)cfg->growth_d2_arr[0], last(cfg->growth_d2_arr)};
+  c->v1 = Tab{tab(4), (float)cfg->growth_v_arr[0], last(cfg->growth_v_arr)};
+  c->pd = Tab{tab(5), (float)cfg->growth_pd_arr[0], last(cfg->growth_pd_arr)};
+  c->ih = Tab{tab(6), (float)cfg->ihub_arr[0], last(cfg->ihub_arr)};
+  c->a_a2r = tab(7);
+  c->r_a2r = tab(8);
+  k = 9;
+  for (int p = 0; p < cfg->n_srcs; p++) {
+    c->nz[p] = Tab{tab(k), 0.0f, 0.0f};                                  /* cosmo.c:58-59 */
+    c->bz[p] = Tab{tab(k + 1), (float)cfg->srcs_bz_arr[p][0], 1.0f};     /* cosmo.c:60-61 */
+    k += 2;
+  }
+  for (int p = 0; p < cfg->n_imap; p++) {
+    c->tz[p] = Tab{tab(k), 0.0f, 0.0f};                                  /* cosmo.c:66-67 */
+    c->bzi[p] = Tab{tab(k + 1), (float)cfg->imap_bz_arr[p][0], 1.0f};    /* cosmo.c:68-69 */
+    k += 2;
+  }
+  /* normalisation tables start at 1 until compute_density_normalization */
+  const int nnorm = cfg->n_srcs + cfg->n_imap;
+  if (nnorm > 0) {
+    std::vector<float> ones((size_t)nnorm * na, 1.0f);
+    if (int rc = dalloc(c, &c->d_norm, ones.size())) return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_norm, ones.data(), ones.size() * sizeof(float), cudaMemcpyHostToDevice,
+                                c->stream));
+    for (int p = 0; p < cfg->n_srcs; p++) c->norm[p] = Tab{c->d_norm + (size_t)p * na, 1.0f, 1.0f};
+    for (int p = 0; p < cfg->n_imap; p++) c->normi[p] = Tab{c->d_norm + (size_t)(cfg->n_srcs + p) * na, 1.0f, 1.0f};
+  }
+  /* P(k) */
+  std::vector<float> pk(cfg->numk);
+  for (int i = 0; i < cfg->numk; i++) pk[i] = (float)cfg->pkarr[i];
+  if (int rc = dalloc(c, &c->d_pk, pk.size())) return rc;
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_pk, pk.data(), pk.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  /* box and fill parameters */
+  const double L = cfg->l_box;
+  const int N = c->N;
+  c->box.N = N;
+  c->box.dx = (float)(L / N);
+  c->box.idx = (float)(N / L);
+  c->box.L = (float)L;
+  c->box.hL = (float)(0.5 * L);
+  c->box.p0 = (float)cfg->pos_obs[0];
+  c->box.p1 = (float)cfg->pos_obs[1];
+  c->box.p2 = (float)cfg->pos_obs[2];
+  const double dk = 2 * M_PI / L;
+  FillParams &f = c->fill;
+  f.N = N;
+  f.NH = N / 2 + 1;
+  f.dk = (float)dk;
+  f.idk3 = (float)(1.0 / (dk * dk * dk));
+  f.prefac = (float)cfg->prefac_lensing;
+  f.r2s = (float)cfg->r2_smooth;
+  f.do_smooth = cfg->do_smoothing;
+  f.smooth_pot = cfg->smooth_potential;
+  f.pk = c->d_pk;
+  f.numk = cfg->numk;
+  f.logkmin = (float)cfg->logkmin;
+  f.logkmax = (float)cfg->logkmax;
+  f.idlogk = (float)cfg->idlogk;
+  f.n_scal = (float)cfg->n_scal;
+  f.key0 = (uint32_t)cfg->seed;
+  f.key1 = (uint32_t)(cfg->seed >> 32) ^ CG_STREAM_FIELD;
+  f.lpt_norm = (float)std::pow(std::sqrt(2 * M_PI) / L, 3);
+  c->have_fields = c->have_density = c->have_norm = c->have_srcs = 0;
+  return CG_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* lifetime                                                                 */
+/* ------------------------------------------------------------------------ */
+extern "C" const char *cg_last_error(const cg_ctx *c) { return c ? c->err : "NULL context"; }
+
+extern "C" int cg_memory_estimate(const cg_config *cfg, unsigned long long *bytes)
+{
+  char msg[256];
+  if (!bytes) return CG_EINVAL;
+  if (int rc = validate(cfg, msg, sizeof(msg))) return rc;
+  const unsigned long long N = cfg->n_grid, NH = N / 2 + 1;
+  unsigned long long grid = N * N * NH * 8ull;
+  unsigned long long b = 2 * grid;
+  if (cfg->dens_type == CG_DENS_1LPT) b += 3 * grid;
+  if (cfg->n_srcs > 0) b += N * N * N * 2ull;
+  for (int i = 0; i < cfg->n_imap; i++)
+    b += (unsigned long long)cfg->imap_nr[i] * 12ull * cfg->nside_imap[i] * cfg->nside_imap[i] * 8ull;
+  if (cfg->do_kappa) b += (unsigned long long)cfg->n_kappa * 12ull * cfg->nside_kappa * cfg->nside_kappa * 4ull;
+  *bytes = b;
+  return CG_OK;
+}
+
+extern "C" void cg_destroy(cg_ctx *c)
+{
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  void *ptrs[] = {c->d_tabs, c->d_norm, c->d_pk, c->d_twN, c->d_twH, c->d_dens, c->d_npot, c->d_disp[0],
+                  c->d_disp[1], c->d_disp[2], c->d_part, c->d_stats, c->d_s2f, c->d_err, c->d_ncount,
+                  c->d_zsum, c->d_bsum, c->d_counts, c->d_bsums, c->d_total, c->d_tmpmap, c->d_kmap,
+                  c->d_kfac, c->d_kinv, c->d_kir};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  for (int i = 0; i < CG_NPOP_MAX; i++) {
+    void *q[] = {c->cat[i].pos, c->cat[i].ipix, c->cat[i].src, c->cat[i].cmap, c->im[i].r0, c->im[i].rf,
+                 c->im[i].nsub, c->im[i].data, c->im[i].nadd};
+    for (void *p : q)
+      if (p) cudaFree(p);
+  }
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+}
+
+extern "C" int cg_create(cg_ctx **out, const cg_config *cfg, int device)
+{
+  if (!out) return CG_EINVAL;
+  *out = nullptr;
+  cg_ctx *c = new (std::nothrow) cg_ctx();
+  if (!c) return CG_ENOMEM;
+  c->err[0] = 0;
+  int rc = validate(cfg, c->err, sizeof(c->err));
+  if (rc) {
+    fprintf(stderr, "cg_create: %s\n", c->err);
+    delete c;
+    return rc;
+  }
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    fprintf(stderr, "cg_create: no usable CUDA device %d\n", device);
+    cudaGetLastError();
+    delete c;
+    return CG_ECUDA;
+  }
+  c->stream = c->own_stream;
+  cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
+  c->N = cfg->n_grid;
+  c->NH = c->N / 2 + 1;
+  c->grid_floats = (size_t)c->N * c->N * 2 * c->NH;
+  *out = c;
+  /* twiddles in double, rounded once */
+  {
+    const int N = c->N, H = N / 2;
+    std::vector<float2> tw(N), th(H);
+    for (int j = 0; j < N; j++) tw[j] = make_float2((float)cos(2 * M_PI * j / N), (float)sin(2 * M_PI * j / N));
+    for (int j = 0; j < H; j++) th[j] = make_float2((float)cos(2 * M_PI * j / H), (float)sin(2 * M_PI * j / H));
+    if ((rc = dalloc(c, &c->d_twN, (size_t)N)) || (rc = dalloc(c, &c->d_twH, (size_t)H))) return rc;
+    CUDA_TRY(c, cudaMemcpy(c->d_twN, tw.data(), N * sizeof(float2), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->d_twH, th.data(), H * sizeof(float2), cudaMemcpyHostToDevice));
+  }
+  if ((rc = dalloc(c, &c->d_dens, c->grid_floats)) || (rc = dalloc(c, &c->d_npot, c->grid_floats))) return rc;
+  c->npart = npartials(c->N);
+  if ((rc = dalloc(c, &c->d_part, c->npart)) || (rc = dalloc(c, &c->d_stats, (size_t)4)) ||
+      (rc = dalloc(c, &c->d_s2f, (size_t)1)) || (rc = dalloc(c, &c->d_err, (size_t)1)))
+    return rc;
+  CUDA_TRY(c, cudaMemset(c->d_err, 0, sizeof(unsigned int)));
+  if ((rc = cg_upload_tables(c, cfg))) return rc;
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return CG_OK;
+}
+
+extern "C" int cg_set_stream(cg_ctx *c, void *s)
+{
+  if (!c) return CG_EINVAL;
+  c->stream = s ? (cudaStream_t)s : c->own_stream;
+  return CG_OK;
+}
+
+extern "C" int cg_sync(cg_ctx *c)
+{
+  if (!c) return CG_EINVAL;
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return check_device_errors(c);
+}
+
+extern "C" long long cg_kernel_launches(const cg_ctx *c) { return c ? c->launches : 0; }
+
+/* ------------------------------------------------------------------------ */
+/* stages                                                                   */
+/* ------------------------------------------------------------------------ */
+extern "C" int cg_create_cartesian_fields(cg_ctx *c)
+{
+  if (!c) return CG_EINVAL;
+  cudaSetDevice(c->device);
+  cg_field_launch L;
+  L.stream = c->stream;
+  L.f[0] = reinterpret_cast<float2 *>(c->d_dens);
+  L.f[1] = reinterpret_cast<float2 *>(c->d_npot);
+  L.f[2] = nullptr;
+  L.fill = c->fill;
+  L.norm = (float)std::pow(std::sqrt(2 * M_PI) / c->cfg.l_box, 3);
+  L.partials = c->d_part;
+  L.twN = c->d_twN;
+  L.twH = c->d_twH;
+  {
+    ProfScope ps(c, "field_fft");
+    CUDA_TRY(c, run_gauss(c->N, &L));
+    const double ncell = (double)c->N * c->N * c->N;
+    CUDA_TRY(c, cg_moments_final(c->stream, c->d_part, c->npart, 1.0 / ncell, c->d_stats, c->d_s2f));
+  }
+  c->launches += 5;
+  c->have_fields = 1;
+  c->have_density = c->have_norm = c->have_srcs = 0;
+  c->pending_mode = CG_DMODE_NONE;
+  return CG_OK;
+}
+
+extern "C" int cg_get_sigma2(cg_ctx *c, double *sigma2, double *mean)
+{
+  if (!c) return CG_EINVAL;
+  if (!c->have_fields) return fail(c, CG_ESTATE, "fields not created");
+  double h[4];
+  CUDA_TRY(c, cudaMemcpyAsync(h, c->d_stats, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (sigma2) *sigma2 = h[3];
+  if (mean) *mean = h[2];
+  return CG_OK;
+}
+
+extern "C" int cg_compute_physical_density_field(cg_ctx *c)
+{
+  if (!c) return CG_EINVAL;
+  if (!c->have_fields) return fail(c, CG_ESTATE, "create_cartesian_fields first");
+  cudaSetDevice(c->device);
+  if (c->cfg.dens_type == CG_DENS_LGNR) {
+    c->pending_mode = CG_DMODE_LGNR; /* applied in the fused bins pass */
+  } else if (c->cfg.dens_type == CG_DENS_CLIP) {
+    c->pending_mode = CG_DMODE_CLIP;
+  } else {
+    int rc;
+    for (int a = 0; a < 3; a++)
+      if (!c->d_disp[a] && (rc = dalloc(c, &c->d_disp[a], c->grid_floats))) return rc;
+    cg_field_launch L;
+    L.stream = c->stream;
+    for (int a = 0; a < 3; a++) L.f[a] = reinterpret_cast<float2 *>(c->d_disp[a]);
+    L.fill = c->fill;
+    L.norm = 1.0f;
+    L.partials = nullptr;
+    L.twN = c->d_twN;
+    L.twH = c->d_twH;
+    {
+      ProfScope ps(c, "lpt_fft");
+      CUDA_TRY(c, run_lpt(c->N, &L));
+    }
+    ProfScope ps2(c, "lpt_cic");
+    CUDA_TRY(c, cudaMemsetAsync(c->d_dens, 0, c->grid_floats * sizeof(float), c->stream));
+    cg_lpt_params lp;
+    lp.box = c->box;
+    lp.g = c->g;
+    lp.d1 = c->d1;
+    CUDA_TRY(c, cg_lpt_cic(c->stream, c->d_dens, c->d_disp[0], c->d_disp[1], c->d_disp[2], &lp, c->nsm));
+    c->launches += 4;
+    c->pending_mode = CG_DMODE_RHO;
+  }
+  c->have_density = 1;
+  c->have_norm = c->have_srcs = 0;
+  return CG_OK;
+}
+
+/* Launch the bins pass over all tracers (one launch carries up to the
+ * kernel's maximum number of bias tables). */
+static int run_bins(cg_ctx *c, int nz, double idz)
+{
+  const int nts = c->cfg.n_srcs, nti = c->cfg.n_imap, nt = nts + nti;
+  const int MT = cg_dens_bins_max_tracers();
+  if (nt > MT) return fail(c, CG_EINVAL, "%d tracers: at most %d per run are supported", nt, MT);
+  int rc;
+  if ((rc = dalloc(c, &c->d_ncount, (size_t)nz)) || (rc = dalloc(c, &c->d_zsum, (size_t)nz)) ||
+      (rc = dalloc(c, &c->d_bsum, (size_t)std::max(nt, 1) * nz)))
+    return rc;
+  CUDA_TRY(c, cudaMemsetAsync(c->d_ncount, 0, sizeof(unsigned long long) * nz, c->stream));
+  CUDA_TRY(c, cudaMemsetAsync(c->d_zsum, 0, sizeof(double) * nz, c->stream));
+  CUDA_TRY(c, cudaMemsetAsync(c->d_bsum, 0, sizeof(double) * std::max(nt, 1) * nz, c->stream));
+  cg_bins_params p;
+  memset(&p, 0, sizeof(p));
+  p.box = c->box;
+  p.g = c->g;
+  p.zt = c->zt;
+  p.d1 = c->d1;
+  p.mode = c->pending_mode;
+  p.sigma2f = c->d_s2f;
+  p.nz = nz;
+  p.idz = (float)idz;
+  p.bias_model = c->cfg.bias_model;
+  p.nt = nt;
+  for (int t = 0; t < nt; t++) p.bz[t] = t < nts ? c->bz[t] : c->bzi[t - nts];
+  p.ncount = c->d_ncount;
+  p.zsum = c->d_zsum;
+  p.bsum = c->d_bsum;
+  {
+    ProfScope ps(c, "dens_bins");
+    CUDA_TRY(c, cg_dens_bins(c->stream, c->d_dens, &p, c->nsm));
+  }
+  c->launches++;
+  c->pending_mode = CG_DMODE_NONE;
+  return CG_OK;
+}
+
+extern "C" int cg_collect_density_normalization(cg_ctx *c, int nz, double idz, double *zarr,
+                                                unsigned long long *narr, double *norm_srcs, double *norm_imap)
+{
+  if (!c) return CG_EINVAL;
+  if (!c->have_density) return fail(c, CG_ESTATE, "compute_physical_density_field first");
+  if (nz < 2 || nz > 4096) return fail(c, CG_EINVAL, "nz=%d out of range", nz);
+  cudaSetDevice(c->device);
+  if (int rc = run_bins(c, nz, idz)) return rc;
+  const int nts = c->cfg.n_srcs, nti = c->cfg.n_imap;
+  std::vector<double> b((size_t)(nts + nti) * nz);
+  std::vector<unsigned long long> n(nz);
+  std::vector<double> z(nz);
+  CUDA_TRY(c, cudaMemcpyAsync(n.data(), c->d_ncount, nz * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(z.data(), c->d_zsum, nz * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (!b.empty())
+    CUDA_TRY(c, cudaMemcpyAsync(b.data(), c->d_bsum, b.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (narr) memcpy(narr, n.data(), nz * sizeof(unsigned long long));
+  if (zarr) memcpy(zarr, z.data(), nz * sizeof(double));
+  if (norm_srcs && nts) memcpy(norm_srcs, b.data(), (size_t)nts * nz * sizeof(double));
+  if (norm_imap && nti) memcpy(norm_imap, b.data() + (size_t)nts * nz, (size_t)nti * nz * sizeof(double));
+  return CG_OK;
+}
+
+extern "C" int cg_set_norm_tables(cg_ctx *c, const double *srcs_norm, const double *srcs_norm_0f,
+                                  const double *imap_norm, const double *imap_norm_0f)
+{
+  if (!c) return CG_EINVAL;
+  const int na = CG_NA, nts = c->cfg.n_srcs, nti = c->cfg.n_imap;
+  if (nts + nti == 0) return CG_OK;
+  std::vector<float> h((size_t)(nts + nti) * na);
+  for (int p = 0; p < nts; p++)
+    for (int i = 0; i < na; i++) h[(size_t)p * na + i] = (float)srcs_norm[(size_t)p * na + i];
+  for (int p = 0; p < nti; p++)
+    for (int i = 0; i < na; i++) h[(size_t)(nts + p) * na + i] = (float)imap_norm[(size_t)p * na + i];
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_norm, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* h is a local buffer */
+  for (int p = 0; p < nts; p++)
+    c->norm[p] = Tab{c->d_norm + (size_t)p * na, (float)srcs_norm_0f[2 * p], (float)srcs_norm_0f[2 * p + 1]};
+  for (int p = 0; p < nti; p++)
+    c->normi[p] = Tab{c->d_norm + (size_t)(nts + p) * na, (float)imap_norm_0f[2 * p], (float)imap_norm_0f[2 * p + 1]};
+  c->have_norm = 1;
+  return CG_OK;
+}
+
+/* Linear interpolation with GSL's bracketing (largest i with x[i] <= z). */
+static double lin_interp(const std::vector<double> &x, const std::vector<double> &y, double z)
+{
+  size_t lo = 0, hi = x.size() - 1;
+  while (hi > lo + 1) {
+    size_t mid = (lo + hi) / 2;
+    if (x[mid] > z) hi = mid;
+    else lo = mid;
+  }
+  return y[lo] + (z - x[lo]) * (y[hi] - y[lo]) / (x[hi] - x[lo]);
+}
+
+extern "C" int cg_compute_density_normalization(cg_ctx *c)
+{
+  if (!c) return CG_EINVAL;
+  const int nts = c->cfg.n_srcs, nti = c->cfg.n_imap, nt = nts + nti;
+  /* density.c:1233-1245 */
+  const double zmax = host_bg(c, c->h_z, 0, c->h_z[CG_NA - 1], c->cfg.l_box * 0.5);
+  const int nz = (int)(zmax / 0.05) + 2;
+  const double idz = (nz - 2) / zmax;
+  std::vector<double> zarr(nz), b((size_t)std::max(nt, 1) * nz);
+  std::vector<unsigned long long> narr(nz);
+  if (int rc = cg_collect_density_normalization(c, nz, idz, zarr.data(), narr.data(), b.data(),
+                                                 nti ? b.data() + (size_t)nts * nz : nullptr))
+    return rc;
+  /* density.c:1272-1297 */
+  for (int iz = 0; iz < nz; iz++) {
+    if (narr[iz] > 0) {
+      zarr[iz] /= narr[iz];
+      for (int t = 0; t < nt; t++) b[(size_t)t * nz + iz] = narr[iz] / b[(size_t)t * nz + iz];
+    }
+  }
+  zarr[0] = 0;
+  zarr[nz - 1] = host_bg(c, c->h_z, 0, c->h_z[CG_NA - 1], 0.5 * c->cfg.l_box);
+  for (int t = 0; t < nt; t++) {
+    b[(size_t)t * nz + 0] = b[(size_t)t * nz + 1];
+    b[(size_t)t * nz + nz - 1] = b[(size_t)t * nz + nz - 2];
+  }
+  /* density.c:1299-1355: linear spline in z resampled on the r table */
+  const int na = CG_NA;
+  std::vector<double> tabs((size_t)std::max(nt, 1) * na), e0f((size_t)2 * std::max(nt, 1));
+  const double z0n = zarr[0], zfn = zarr[nz - 1];
+  for (int t = 0; t < nt; t++) {
+    std::vector<double> y(b.begin() + (size_t)t * nz, b.begin() + (size_t)(t + 1) * nz);
+    e0f[2 * t] = y[0];
+    e0f[2 * t + 1] = y[nz - 1];
+    for (int i = 0; i < na; i++) {
+      double z = host_bg(c, c->h_z, 0, c->h_z[na - 1], c->h_r[i]);
+      double nm;
+      if (z < z0n) nm = y[0];
+      else if (z >= zfn) nm = y[nz - 1];
+      else nm = lin_interp(zarr, y, z);
+      tabs[(size_t)t * na + i] = nm;
+    }
+  }
+  return cg_set_norm_tables(c, tabs.data(), e0f.data(), nti ? tabs.data() + (size_t)nts * na : nullptr,
+                            nti ? e0f.data() + 2 * nts : nullptr);
+}
+
+static void srcs_params(cg_ctx *c, int ipop, cg_srcs_params &p)
+{
+  memset(&p, 0, sizeof(p));
+  p.box = c->box;
+  p.g = c->g;
+  p.zt = c->zt;
+  p.v1 = c->v1;
+  p.nz = c->nz[ipop];
+  p.bz = c->bz[ipop];
+  p.norm = c->norm[ipop];
+  p.a_a2r = c->a_a2r;
+  p.r_a2r = c->r_a2r;
+  p.na = CG_NA;
+  p.bias_model = c->cfg.bias_model;
+  p.kp0 = (uint32_t)c->cfg.seed;
+  p.kp1 = (uint32_t)(c->cfg.seed >> 32) ^ (CG_STREAM_POIS + (uint32_t)ipop);
+  p.kq0 = (uint32_t)c->cfg.seed;
+  p.kq1 = (uint32_t)(c->cfg.seed >> 32) ^ (CG_STREAM_POS + (uint32_t)ipop);
+  p.rlim = (float)(c->cfg.l_box / 2 + 20.);
+  const double dx = c->cfg.l_box / c->N;
+  p.cell_vol = (float)(dx * dx * dx);
+  p.factor_vel = (float)(-c->cfg.fgrowth_0 / (1.5 * c->cfg.hubble_0 * c->cfg.omega_m));
+  p.need_beaming = c->cfg.need_beaming;
+  p.nside_base = c->cfg.nside_base;
+  p.nside_count = c->cfg.nside_count[ipop];
+  p.cmap = c->cat[ipop].cmap;
+  p.counts = c->d_counts;
+  p.block_sums = c->d_bsums;
+  p.capacity = c->cat[ipop].cap;
+  p.pos = c->cat[ipop].pos;
+  p.ipix = c->cat[ipop].ipix;
+  p.src = c->cat[ipop].src;
+  p.err = c->d_err;
+}
+
+extern "C" int cg_srcs_set_cartesian(cg_ctx *c, long long *nsrc)
+{
+  if (!c) return CG_EINVAL;
+  if (!c->have_density) return fail(c, CG_ESTATE, "density not computed");
+  if (!c->have_norm) return fail(c, CG_ESTATE, "compute_density_normalization first");
+  cudaSetDevice(c->device);
+  const long long ncell = (long long)c->N * c->N * c->N;
+  int rc;
+  if (c->cfg.n_srcs > 0) {
+    if (!c->d_counts && (rc = dalloc(c, &c->d_counts, (size_t)ncell))) return rc;
+    if (!c->d_bsums && (rc = dalloc(c, &c->d_bsums, (size_t)cg_srcs_nblocks(c->N)))) return rc;
+    if (!c->d_total && (rc = dalloc(c, &c->d_total, (size_t)1))) return rc;
+  }
+  for (int ip = 0; ip < c->cfg.n_srcs; ip++) {
+    Cat &K = c->cat[ip];
+    cg_srcs_params p;
+    srcs_params(c, ip, p);
+    {
+      ProfScope ps(c, "srcs_count");
+      CUDA_TRY(c, cg_srcs_count(c->stream, c->d_dens, &p, c->d_total));
+    }
+    long long tot = 0;
+    CUDA_TRY(c, cudaMemcpyAsync(&tot, c->d_total, sizeof(tot), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if ((rc = check_device_errors(c))) return rc;
+    if (tot > K.cap) {
+      long long cap = tot + tot / 8 + 1024;
+      if ((rc = dalloc(c, &K.pos, (size_t)cap)) || (rc = dalloc(c, &K.ipix, (size_t)cap)) ||
+          (rc = dalloc(c, &K.src, (size_t)cap * 9)))
+        return rc;
+      K.cap = cap;
+    }
+    K.n = tot;
+    const int ns = c->cfg.nside_count[ip];
+    if (ns > 0) {
+      long long np = 12LL * ns * ns;
+      if (K.cmap_npix != np) {
+        if ((rc = dalloc(c, &K.cmap, (size_t)np))) return rc;
+        K.cmap_npix = np;
+      }
+      CUDA_TRY(c, cudaMemsetAsync(K.cmap, 0, np * sizeof(int), c->stream));
+    }
+    srcs_params(c, ip, p);
+    {
+      ProfScope ps(c, "srcs_emit");
+      CUDA_TRY(c, cg_srcs_emit(c->stream, c->d_npot, &p));
+    }
+    c->launches += 3;
+    if (nsrc) nsrc[ip] = tot;
+  }
+  c->have_srcs = 1;
+  return CG_OK;
+}
+
+extern "C" long long cg_num_sources(cg_ctx *c, int ipop)
+{
+  if (!c || ipop < 0 || ipop >= c->cfg.n_srcs) return -1;
+  return c->cat[ipop].n;
+}
+
+extern "C" int cg_imap_set_cartesian(cg_ctx *c)
+{
+  if (!c) return CG_EINVAL;
+  if (c->cfg.n_imap == 0) return CG_OK;
+  if (!c->have_norm) return fail(c, CG_ESTATE, "compute_density_normalization first");
+  cudaSetDevice(c->device);
+  int rc;
+  for (int ip = 0; ip < c->cfg.n_imap; ip++) {
+    Imap &M = c->im[ip];
+    const int nr = c->cfg.imap_nr[ip];
+    const int nside = c->cfg.nside_imap[ip];
+    const long long npix = 12LL * nside * nside;
+    /* imap_preproc (imap.c:105-133): sort shells by r0, full-sky maps */
+    std::vector<int> order(nr);
+    for (int i = 0; i < nr; i++) order[i] = i;
+    std::vector<float> r0(nr), rf(nr);
+    for (int i = 0; i < nr; i++) {
+      r0[i] = (float)c->cfg.imap_r0[ip][i];
+      rf[i] = (float)c->cfg.imap_rf[ip][i];
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return r0[a] < r0[b]; });
+    std::vector<float> sr0(nr), srf(nr);
+    for (int i = 0; i < nr; i++) {
+      sr0[i] = r0[order[i]];
+      srf[i] = rf[order[i]];
+    }
+    /* sub-sampling factors, imap.c:153-174 */
+    const double dx = c->cfg.l_box / c->N;
+    const double ps = sqrt(4 * M_PI / (double)npix);
+    std::vector<int> nsub(nr);
+    for (int i = 0; i < nr; i++) {
+      double a = sr0[i], b = srf[i];
+      double vol = (b * b * b - a * a * a) * ps * ps / 3;
+      double sct = a * ps, scr = b - a, scv = pow(vol, 0.333333);
+      double sc0 = fmin(scv, fmin(sct, scr));
+      nsub[i] = (int)(dx / sc0 + 0.5) + 1;
+    }
+    if (M.nr != nr) {
+      if ((rc = dalloc(c, &M.r0, (size_t)nr)) || (rc = dalloc(c, &M.rf, (size_t)nr)) ||
+          (rc = dalloc(c, &M.nsub, (size_t)nr)))
+        return rc;
+    }
+    if (M.nr != nr || M.npix != npix) {
+      if ((rc = dalloc(c, &M.data, (size_t)nr * npix)) || (rc = dalloc(c, &M.nadd, (size_t)nr * npix))) return rc;
+    }
+    M.nr = nr;
+    M.nside = nside;
+    M.npix = npix;
+    CUDA_TRY(c, cudaMemcpyAsync(M.r0, sr0.data(), nr * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(M.rf, srf.data(), nr * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(M.nsub, nsub.data(), nr * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(M.data, 0, (size_t)nr * npix * sizeof(float), c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(M.nadd, 0, (size_t)nr * npix * sizeof(int), c->stream));
+    cg_imap_params p;
+    memset(&p, 0, sizeof(p));
+    p.box = c->box;
+    p.g = c->g;
+    p.tz = c->tz[ip];
+    p.bz = c->bzi[ip];
+    p.norm = c->normi[ip];
+    p.v1 = c->v1;
+    p.ih = c->ih;
+    p.bias_model = c->cfg.bias_model;
+    p.factor_vel = (float)(-c->cfg.fgrowth_0 / (1.5 * c->cfg.hubble_0 * c->cfg.omega_m));
+    p.nr = nr;
+    p.r0 = M.r0;
+    p.rf = M.rf;
+    p.nsub = M.nsub;
+    p.nsub_lo = nsub[0];
+    p.nsub_hi = nsub[nr - 1];
+    p.rmin_here = (float)((double)sr0[0] - 20.);
+    p.rmax_here = (float)((double)srf[nr - 1] + 20.);
+    p.nside = nside;
+    p.npix = npix;
+    p.data = M.data;
+    p.nadd = M.nadd;
+    p.err = c->d_err;
+    {
+      ProfScope ps(c, "imap_paint");
+      CUDA_TRY(c, cg_imap_paint(c->stream, c->d_dens, c->d_npot, &p, c->nsm));
+    }
+    c->launches++;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host vectors above go out of scope */
+  }
+  return CG_OK;
+}
+
+static int kappa_run(cg_ctx *c)
+{
+  const int np = c->cfg.n_kappa;
+  const int nside = c->cfg.nside_kappa;
+  const long long npix = 12LL * nside * nside;
+  const int nr = c->N / 2; /* get_radial_params with NSAMP_RAD = 1 */
+  const double dr = c->cfg.r_max / nr, idr = 1. / dr;
+  /* kappa_beams_preproc: sort planes by distance (stored as flouble) */
+  std::vector<float> rp(np);
+  for (int i = 0; i < np; i++) rp[i] = (float)c->cfg.kappa_r[i];
+  std::stable_sort(rp.begin(), rp.end());
+  std::vector<int> ir(2 * np);
+  std::vector<float> inv(np), fac(2 * (size_t)nr);
+  for (int i = 0; i < np; i++) {
+    int irh = (int)((double)rp[i] * idr + 0.5);
+    inv[i] = (float)(1. / (irh * dr));
+    ir[np + i] = std::min(irh, nr - 1);
+  }
+  ir[0] = 0;
+  for (int i = 1; i < np; i++) ir[i] = ir[np + i - 1] + 1;
+  for (int i = 0; i < nr; i++) {
+    double rm = (i + 0.5) * dr;
+    double pg = host_bg(c, c->h_d1, 1, c->h_d1[CG_NA - 1], rm) * (1 + host_bg(c, c->h_z, 0, c->h_z[CG_NA - 1], rm));
+    fac[i] = (float)(rm * pg * dr);
+    fac[nr + i] = (float)(rm * rm * pg * dr);
+  }
+  int rc;
+  if (c->kpl != np || c->knpix != npix) {
+    if ((rc = dalloc(c, &c->d_kmap, (size_t)np * npix))) return rc;
+  }
+  if (c->knr != nr || c->kpl != np) {
+    if ((rc = dalloc(c, &c->d_kfac, 2 * (size_t)nr)) || (rc = dalloc(c, &c->d_kinv, (size_t)np)) ||
+        (rc = dalloc(c, &c->d_kir, 2 * (size_t)np)))
+      return rc;
+  }
+  c->kpl = np;
+  c->knpix = npix;
+  c->knr = nr;
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_kfac, fac.data(), fac.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_kinv, inv.data(), inv.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_kir, ir.data(), ir.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  cg_kappa_params p;
+  p.box = c->box;
+  p.nside = nside;
+  p.npix = npix;
+  p.nplanes = np;
+  p.ir_min = c->d_kir;
+  p.ir_max = c->d_kir + np;
+  p.inv_r_max = c->d_kinv;
+  p.nr = nr;
+  p.dr = (float)dr;
+  p.fac1 = c->d_kfac;
+  p.fac2 = c->d_kfac + nr;
+  p.map = c->d_kmap;
+  {
+    ProfScope ps(c, "kappa");
+    CUDA_TRY(c, cg_kappa_integrate(c->stream, c->d_npot, &p));
+  }
+  c->launches++;
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host staging vectors */
+  return CG_OK;
+}
+
+extern "C" int cg_get_beam_properties(cg_ctx *c)
+{
+  if (!c) return CG_EINVAL;
+  if (!c->cfg.need_beaming) return CG_OK; /* beaming.c:296-299 */
+  if (!c->have_fields) return fail(c, CG_ESTATE, "fields not created");
+  cudaSetDevice(c->device);
+  if (c->cfg.do_kappa)
+    if (int rc = kappa_run(c)) return rc;
+  if (c->cfg.n_srcs > 0) {
+    if (!c->have_srcs) return fail(c, CG_ESTATE, "srcs_set_cartesian first");
+    for (int ip = 0; ip < c->cfg.n_srcs; ip++) {
+      cg_srcs_params p;
+      srcs_params(c, ip, p);
+      ProfScope ps(c, "srcs_beam_rsd");
+      CUDA_TRY(c, cg_srcs_beam_rsd(c->stream, c->d_npot, &p, c->cat[ip].n, c->nsm));
+      if (c->cat[ip].n > 0) c->launches++;
+    }
+  }
+  return CG_OK;
+}
+
+extern "C" int cg_run_mock(cg_ctx *c)
+{
+  int rc;
+  if ((rc = cg_create_cartesian_fields(c))) return rc;
+  if ((rc = cg_compute_physical_density_field(c))) return rc;
+  if ((rc = cg_compute_density_normalization(c))) return rc;
+  if ((rc = cg_srcs_set_cartesian(c, nullptr))) return rc;
+  if ((rc = cg_imap_set_cartesian(c))) return rc;
+  if ((rc = cg_get_beam_properties(c))) return rc;
+  return CG_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* host mirrors                                                             */
+/* ------------------------------------------------------------------------ */
+static int apply_pending(cg_ctx *c)
+{
+  if (c->pending_mode == CG_DMODE_NONE) return CG_OK;
+  /* the density transform on its own: a bins pass with no bins */
+  cg_bins_params p;
+  memset(&p, 0, sizeof(p));
+  p.box = c->box;
+  p.g = c->g;
+  p.zt = c->zt;
+  p.d1 = c->d1;
+  p.mode = c->pending_mode;
+  p.sigma2f = c->d_s2f;
+  p.nz = 0;
+  p.nt = 0;
+  p.bias_model = c->cfg.bias_model;
+  CUDA_TRY(c, cg_dens_bins(c->stream, c->d_dens, &p, c->nsm));
+  c->launches++;
+  c->pending_mode = CG_DMODE_NONE;
+  return CG_OK;
+}
+
+extern "C" int cg_download_grid(cg_ctx *c, int which, void *dst)
+{
+  if (!c || !dst) return CG_EINVAL;
+  float *src = nullptr;
+  if (which == 0) {
+    if (int rc = apply_pending(c)) return rc;
+    src = c->d_dens;
+  } else if (which == 1) src = c->d_npot;
+  else if (which >= 2 && which <= 4) src = c->d_disp[which - 2];
+  if (!src) return fail(c, CG_ESTATE, "grid %d not available", which);
+  CUDA_TRY(c, cudaMemcpyAsync(dst, src, c->grid_floats * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return check_device_errors(c);
+}
+
+extern "C" int cg_download_catalog(cg_ctx *c, int ipop, float *pos4, int *ipix, float *src9)
+{
+  if (!c || ipop < 0 || ipop >= c->cfg.n_srcs) return CG_EINVAL;
+  const Cat &K = c->cat[ipop];
+  if (K.n > 0) {
+    if (pos4) CUDA_TRY(c, cudaMemcpyAsync(pos4, K.pos, K.n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
+    if (ipix) CUDA_TRY(c, cudaMemcpyAsync(ipix, K.ipix, K.n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    if (src9) CUDA_TRY(c, cudaMemcpyAsync(src9, K.src, K.n * 9 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  }
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return check_device_errors(c);
+}
+
+extern "C" int cg_download_count_map(cg_ctx *c, int ipop, int *counts)
+{
+  if (!c || !counts || ipop < 0 || ipop >= c->cfg.n_srcs) return CG_EINVAL;
+  const Cat &K = c->cat[ipop];
+  if (!K.cmap) return fail(c, CG_ESTATE, "no count map for population %d", ipop);
+  CUDA_TRY(c, cudaMemcpyAsync(counts, K.cmap, K.cmap_npix * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return check_device_errors(c);
+}
+
+__global__ void k_div_nadd(const float *__restrict__ d, const int *__restrict__ n, float *out, long long m)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x) {
+    int k = n[i];
+    out[i] = k > 0 ? d[i] / (float)k : d[i];
+  }
+}
+
+extern "C" int cg_download_imap(cg_ctx *c, int ipop, float *map, int *nadd)
+{
+  if (!c || ipop < 0 || ipop >= c->cfg.n_imap) return CG_EINVAL;
+  const Imap &M = c->im[ipop];
+  if (!M.data) return fail(c, CG_ESTATE, "intensity map %d not painted", ipop);
+  const long long m = (long long)M.nr * M.npix;
+  if (map) {
+    if (c->tmpmap_n < (size_t)m) {
+      if (int rc = dalloc(c, &c->d_tmpmap, (size_t)m)) return rc;
+      c->tmpmap_n = m;
+    }
+    /* write_imap, io.c:738-741: data/nadd where nadd > 0 */
+    k_div_nadd<<<(unsigned)std::min<long long>((m + 255) / 256, (long long)c->nsm * 16), 256, 0, c->stream>>>(
+        M.data, M.nadd, c->d_tmpmap, m);
+    CUDA_TRY(c, cudaGetLastError());
+    c->launches++;
+    CUDA_TRY(c, cudaMemcpyAsync(map, c->d_tmpmap, m * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  }
+  if (nadd) CUDA_TRY(c, cudaMemcpyAsync(nadd, M.nadd, m * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return check_device_errors(c);
+}
+
+extern "C" int cg_download_kappa(cg_ctx *c, float *map)
+{
+  if (!c || !map) return CG_EINVAL;
+  if (!c->d_kmap) return fail(c, CG_ESTATE, "kappa not computed");
+  CUDA_TRY(c, cudaMemcpyAsync(map, c->d_kmap, (size_t)c->kpl * c->knpix * sizeof(float), cudaMemcpyDeviceToHost,
+                              c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return check_device_errors(c);
+}
+
+extern "C" int cg_download_norm(cg_ctx *c, int kind, int ipop, float *tab, float *edges)
+{
+  if (!c || !tab || !edges) return CG_EINVAL;
+  const Tab *t = nullptr;
+  if (kind == 0 && ipop >= 0 && ipop < c->cfg.n_srcs) t = &c->norm[ipop];
+  if (kind == 1 && ipop >= 0 && ipop < c->cfg.n_imap) t = &c->normi[ipop];
+  if (!t || !t->f) return fail(c, CG_EINVAL, "no normalisation table %d/%d", kind, ipop);
+  CUDA_TRY(c, cudaMemcpyAsync(tab, t->f, CG_NA * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  edges[0] = t->f0;
+  edges[1] = t->ff;
+  return CG_OK;
+}
+
+extern "C" int cg_set_profiling(cg_ctx *c, int on)
+{
+  if (!c) return CG_EINVAL;
+  c->profiling = on;
+  return CG_OK;
+}
+
+extern "C" int cg_kernel_times(cg_ctx *c, char *names, size_t names_len, float *ms, int cap, int *n)
+{
+  if (!c || !n) return CG_EINVAL;
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  size_t off = 0;
+  int k = 0;
+  if (names && names_len) names[0] = 0;
+  for (auto &e : c->evlog) {
+    float t = 0;
+    cudaEventElapsedTime(&t, e.a, e.b);
+    if (k < cap) {
+      if (ms) ms[k] = t;
+      if (names) {
+        int w = snprintf(names + off, names_len > off ? names_len - off : 0, "%s;", e.name);
+        if (w > 0) off += (size_t)w;
+      }
+    }
+    k++;
+    cudaEventDestroy(e.a);
+    cudaEventDestroy(e.b);
+  }
+  c->evlog.clear();
+  *n = k;
+  return CG_OK;
+}

@@ -1,0 +1,81 @@
+/*
+ * cg_dev.cuh -- device-side structures shared by the kernels of
+ * libcolore_cuda.so: background/tracer tables, the error word and the
+ * per-pass parameter blocks.
+ */
+#ifndef CG_DEV_CUH
+#define CG_DEV_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cg_cell.h"
+
+namespace cg {
+
+/* Error bits written by kernels (never trapping). */
+enum : unsigned int {
+  ERR_COUNT_OVERFLOW = 1u,  /* more than 65535 sources in one cell     */
+  ERR_CATALOG_OVERFLOW = 2u, /* emit wrote past the allocated catalog  */
+  ERR_SHELL_WALK = 4u,       /* imap shell search did not terminate    */
+  ERR_IMAP_NSUB = 8u,        /* sub-sampling factor out of range       */
+};
+
+/* One background table with the edge values of get_bg (cosmo.c:40-86). */
+struct Tab {
+  const float *f;
+  float f0, ff;
+};
+
+/* r-uniform grid shared by all background and tracer tables. */
+struct Grid1 {
+  const float *r; /* r_i = i / idr, NA entries */
+  float r_last, idr;
+};
+
+__device__ __forceinline__ float bg(const Tab &t, const Grid1 &g, float r)
+{
+  return cg_bg_eval(t.f, g.r, t.f0, t.ff, r, g.r_last, g.idr);
+}
+
+/* r_of_z, cosmo.c:101-112, on the a-uniform table of NA entries. */
+__device__ __forceinline__ float r_of_z(const float *a_arr, const float *r_arr, int na, float z)
+{
+  float a = CG_DIV(1.0f, CG_ADD(1.0f, z));
+  if (a >= 1.0f) return 0.0f;
+  if (a <= 0.0f) return r_arr[0];
+  float nm1 = (float)(na - 1);
+  int ia = (int)CG_MUL(a, nm1);
+  return CG_FMA(CG_SUB(r_arr[ia + 1], r_arr[ia]), CG_MUL(CG_SUB(a, a_arr[ia]), nm1), r_arr[ia]);
+}
+
+/* Padded real index of cell (ix, iy, iz), fourier.c:46-51. */
+__device__ __forceinline__ long long pidx(int ix, int iy, int iz, int N)
+{
+  return (long long)ix + (long long)(2 * (N / 2 + 1)) * ((long long)iy + (long long)N * iz);
+}
+
+__device__ __forceinline__ int wrap(int i, int N) { return i >= N ? i - N : (i < 0 ? i + N : i); }
+
+/* Parameters of the Fourier-space fill (fourier.c:285-359). */
+struct FillParams {
+  int N, NH;
+  float dk, idk3, prefac, r2s;
+  int do_smooth, smooth_pot;
+  const float *pk; /* numk values on logk_i = logkmin + i/idlogk */
+  int numk;
+  float logkmin, logkmax, idlogk, n_scal;
+  uint32_t key0, key1;
+  float lpt_norm; /* (sqrt(2 pi)/L)^3, used by the 1LPT displacement fill */
+};
+
+/* Geometry of the Cartesian box. */
+struct Box {
+  int N;
+  float dx, idx, L, hL;
+  float p0, p1, p2; /* observer */
+};
+
+} /* namespace cg */
+
+#endif /* CG_DEV_CUH */

@@ -1,0 +1,255 @@
+/*
+ * dens.cu -- physical density field (density.c:1034-1126) and the
+ * redshift-bin sums of the bias normalisation (density.c:1128-1211).
+ *
+ *  k_moments_final : fixed-order FP64 sum of the per-block (sum d, sum d^2)
+ *                    partials of the x pass -> <d>, sigma^2 (fourier.c:24-79).
+ *  k_dens_bins     : one streaming pass over the grid that applies the
+ *                    lognormal (or clipped, or 1LPT "rho-1") transform in
+ *                    place and accumulates, per redshift bin, the cell count,
+ *                    the summed redshift and the summed bias_model of every
+ *                    tracer.  A warp owns 64 consecutive cells of a row; lanes
+ *                    sharing a bin are reduced with shuffles, and each warp
+ *                    keeps private FP64 bins in shared memory.
+ *  k_lpt_cic       : 1LPT particle positions (density.c:473-501) and their
+ *                    cloud-in-cell deposit (density.c:64-105).
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cg_dev.cuh"
+#include "dens_api.h"
+
+namespace {
+using namespace cg;
+
+__global__ void k_moments_final(const double2 *__restrict__ part, size_t n, double inv_ncell,
+                                double *stats, float *s2f)
+{
+  __shared__ double sa[1024], sb[1024];
+  double a = 0.0, b = 0.0;
+  for (size_t i = threadIdx.x; i < n; i += blockDim.x) {
+    double2 v = part[i];
+    a += v.x;
+    b += v.y;
+  }
+  sa[threadIdx.x] = a;
+  sb[threadIdx.x] = b;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) {
+      sa[threadIdx.x] += sa[threadIdx.x + s];
+      sb[threadIdx.x] += sb[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double mean = sa[0] * inv_ncell;
+    double s2 = sb[0] * inv_ncell - mean * mean;
+    stats[0] = sa[0];
+    stats[1] = sb[0];
+    stats[2] = mean;
+    stats[3] = s2;
+    *s2f = (float)s2;
+  }
+}
+
+constexpr int MAXT = 8;      /* tracers per bins launch */
+constexpr int BINS_WARPS = 8;
+
+__global__ void __launch_bounds__(BINS_WARPS * 32) k_dens_bins(float *grid, cg_bins_params p)
+{
+  extern __shared__ double sbin[]; /* [warp][nz][2 + nt]; count stored as double-exact integer */
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nz = p.nz, nt = p.nt, W = 2 + nt;
+  double *mybins = sbin + (size_t)wid * nz * W;
+  for (int i = lane; i < nz * W; i += 32) mybins[i] = 0.0;
+  __syncwarp();
+  const int N = p.box.N;
+  const int nseg_row = (N + 63) / 64;
+  const long long nseg = (long long)nseg_row * N * N;
+  const float s2 = p.sigma2f ? *p.sigma2f : 0.0f;
+  const long long gw = (long long)blockIdx.x * BINS_WARPS + wid;
+  const long long nw = (long long)gridDim.x * BINS_WARPS;
+  for (long long seg = gw; seg < nseg; seg += nw) {
+    const int sr = (int)(seg % nseg_row);
+    const long long row = seg / nseg_row;
+    const int iy = (int)(row % N), iz = (int)(row / N);
+    const int ix = sr * 64 + 2 * lane;
+    const bool valid = ix < N;
+    int bin = -1;
+    float cnt = 0.0f, zs = 0.0f, bs[MAXT];
+#pragma unroll
+    for (int t = 0; t < MAXT; t++) bs[t] = 0.0f;
+    if (valid) {
+      float2 *ptr = reinterpret_cast<float2 *>(grid + pidx(ix, iy, iz, N));
+      float2 dv = *ptr;
+      const float y0 = cg_cell_coord(iy, p.box.dx, p.box.p1), z0 = cg_cell_coord(iz, p.box.dx, p.box.p2);
+      float dd[2] = {dv.x, dv.y};
+      int bb[2];
+      float zz[2], rr[2];
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        float x0 = cg_cell_coord(ix + h, p.box.dx, p.box.p0);
+        float r = cg_norm3(x0, y0, z0);
+        rr[h] = r;
+        if (p.mode != CG_DMODE_NONE) dd[h] = cg_dens_transform(p.mode, dd[h], bg(p.d1, p.g, r), s2);
+        float z = bg(p.zt, p.g, r);
+        zz[h] = z;
+        int iz_bin = (int)CG_MUL(z, p.idz) + 1;
+        bb[h] = (iz_bin >= 0 && iz_bin < nz) ? iz_bin : -1; /* nz = 0: transform only */
+      }
+      if (p.mode != CG_DMODE_NONE) *ptr = make_float2(dd[0], dd[1]);
+      /* both cells of a lane normally share a bin; otherwise the second
+       * one is flushed on its own below */
+      bin = bb[0];
+      if (bin >= 0) {
+        cnt = 1.0f;
+        zs = zz[0];
+#pragma unroll
+        for (int t = 0; t < MAXT; t++)
+          if (t < nt) bs[t] = cg_bias_model(dd[0], bg(p.bz[t], p.g, rr[0]), p.bias_model);
+      }
+      if (bb[1] >= 0) {
+        if (bb[1] == bin || bin < 0) {
+          bin = bb[1];
+          cnt += 1.0f;
+          zs += zz[1];
+#pragma unroll
+          for (int t = 0; t < MAXT; t++)
+            if (t < nt) bs[t] += cg_bias_model(dd[1], bg(p.bz[t], p.g, rr[1]), p.bias_model);
+        } else {
+          /* rare: second cell in another bin -> direct FP64 update */
+          double *d = mybins + (size_t)bb[1] * W;
+          atomicAdd(&d[0], 1.0);
+          atomicAdd(&d[1], (double)zz[1]);
+          for (int t = 0; t < nt && t < MAXT; t++)
+            atomicAdd(&d[2 + t], (double)cg_bias_model(dd[1], bg(p.bz[t], p.g, rr[1]), p.bias_model));
+        }
+      }
+    }
+    /* warp-level segmented reduction by bin */
+    unsigned todo = __ballot_sync(0xffffffffu, bin >= 0);
+    while (todo) {
+      int leader = __ffs(todo) - 1;
+      int lb = __shfl_sync(0xffffffffu, bin, leader);
+      bool mine = (bin == lb);
+      float c = mine ? cnt : 0.0f, zsum = mine ? zs : 0.0f;
+      float bsum[MAXT];
+#pragma unroll
+      for (int t = 0; t < MAXT; t++) bsum[t] = mine ? bs[t] : 0.0f;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        c += __shfl_xor_sync(0xffffffffu, c, o);
+        zsum += __shfl_xor_sync(0xffffffffu, zsum, o);
+#pragma unroll
+        for (int t = 0; t < MAXT; t++)
+          if (t < nt) bsum[t] += __shfl_xor_sync(0xffffffffu, bsum[t], o);
+      }
+      if (lane == 0) {
+        double *d = mybins + (size_t)lb * W;
+        atomicAdd(&d[0], (double)c);
+        atomicAdd(&d[1], (double)zsum);
+#pragma unroll
+        for (int t = 0; t < MAXT; t++)
+          if (t < nt) atomicAdd(&d[2 + t], (double)bsum[t]);
+      }
+      todo &= ~__ballot_sync(0xffffffffu, mine);
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  /* combine the warps' bins in fixed order, then one global update per block */
+  for (int i = threadIdx.x; i < nz * W; i += blockDim.x) {
+    double s = 0.0;
+    for (int w = 0; w < BINS_WARPS; w++) s += sbin[(size_t)w * nz * W + i];
+    if (s != 0.0) {
+      int b = i / W, k = i - b * W;
+      if (k == 0) atomicAdd(&p.ncount[b], (unsigned long long)(s + 0.5));
+      else if (k == 1) atomicAdd(&p.zsum[b], s);
+      else atomicAdd(&p.bsum[(size_t)(k - 2) * nz + b], s);
+    }
+  }
+}
+
+/* 1LPT: x = q + D(r) Psi (wrapped into the box), then CIC into grid. */
+__global__ void __launch_bounds__(256) k_lpt_cic(float *grid, const float *__restrict__ dx_,
+                                                 const float *__restrict__ dy_, const float *__restrict__ dz_,
+                                                 cg_lpt_params p)
+{
+  const int N = p.box.N;
+  const long long ncell = (long long)N * N * N;
+  const float iag = CG_DIV((float)N, p.box.L);
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncell;
+       c += (long long)gridDim.x * blockDim.x) {
+    const int ix = (int)(c % N), iy = (int)((c / N) % N), iz = (int)(c / ((long long)N * N));
+    const long long id = pidx(ix, iy, iz, N);
+    float xv[3] = {cg_cell_coord(ix, p.box.dx, p.box.p0), cg_cell_coord(iy, p.box.dx, p.box.p1),
+                   cg_cell_coord(iz, p.box.dx, p.box.p2)};
+    const float po[3] = {p.box.p0, p.box.p1, p.box.p2};
+    float r = cg_norm3(xv[0], xv[1], xv[2]);
+    float dg = bg(p.d1, p.g, r);
+    float dsp[3] = {__ldg(&dx_[id]), __ldg(&dy_[id]), __ldg(&dz_[id])};
+    int i0[3], i1[3];
+    float a0[3], a1[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      float q = CG_ADD(CG_FMA(dg, dsp[a], xv[a]), po[a]);
+      if (q < 0.0f) q = CG_ADD(q, p.box.L);
+      if (q >= p.box.L) q = CG_SUB(q, p.box.L);
+      float u = CG_MUL(q, iag);
+      i0[a] = (int)u;
+      a1[a] = CG_SUB(u, (float)i0[a]);
+      a0[a] = CG_SUB(1.0f, a1[a]);
+      i1[a] = i0[a] + 1;
+      /* full modulo: a cell index stays inside the grid whatever q is */
+      i0[a] %= N;
+      i1[a] %= N;
+      if (i0[a] < 0) i0[a] += N;
+      if (i1[a] < 0) i1[a] += N;
+    }
+    atomicAdd(&grid[pidx(i0[0], i0[1], i0[2], N)], CG_MUL(CG_MUL(a0[0], a0[1]), a0[2]));
+    atomicAdd(&grid[pidx(i1[0], i0[1], i0[2], N)], CG_MUL(CG_MUL(a1[0], a0[1]), a0[2]));
+    atomicAdd(&grid[pidx(i0[0], i1[1], i0[2], N)], CG_MUL(CG_MUL(a0[0], a1[1]), a0[2]));
+    atomicAdd(&grid[pidx(i1[0], i1[1], i0[2], N)], CG_MUL(CG_MUL(a1[0], a1[1]), a0[2]));
+    atomicAdd(&grid[pidx(i0[0], i0[1], i1[2], N)], CG_MUL(CG_MUL(a0[0], a0[1]), a1[2]));
+    atomicAdd(&grid[pidx(i1[0], i0[1], i1[2], N)], CG_MUL(CG_MUL(a1[0], a0[1]), a1[2]));
+    atomicAdd(&grid[pidx(i0[0], i1[1], i1[2], N)], CG_MUL(CG_MUL(a0[0], a1[1]), a1[2]));
+    atomicAdd(&grid[pidx(i1[0], i1[1], i1[2], N)], CG_MUL(CG_MUL(a1[0], a1[1]), a1[2]));
+  }
+}
+
+} /* namespace */
+
+cudaError_t cg_moments_final(cudaStream_t s, const double2 *part, size_t n, double inv_ncell, double *stats,
+                             float *s2f)
+{
+  k_moments_final<<<1, 1024, 0, s>>>(part, n, inv_ncell, stats, s2f);
+  return cudaGetLastError();
+}
+
+cudaError_t cg_dens_bins(cudaStream_t s, float *grid, const cg_bins_params *p, int nsm)
+{
+  size_t smem = (size_t)BINS_WARPS * p->nz * (2 + p->nt) * sizeof(double);
+  cudaError_t e = cudaFuncSetAttribute(k_dens_bins, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  long long nseg = (long long)((p->box.N + 63) / 64) * p->box.N * p->box.N;
+  long long blocks = (nseg + BINS_WARPS - 1) / BINS_WARPS;
+  long long cap = (long long)nsm * 8;
+  if (blocks > cap) blocks = cap;
+  k_dens_bins<<<(unsigned)blocks, BINS_WARPS * 32, smem, s>>>(grid, *p);
+  return cudaGetLastError();
+}
+
+int cg_dens_bins_max_tracers(void) { return MAXT; }
+
+cudaError_t cg_lpt_cic(cudaStream_t s, float *grid, const float *dx, const float *dy, const float *dz,
+                       const cg_lpt_params *p, int nsm)
+{
+  long long ncell = (long long)p->box.N * p->box.N * p->box.N;
+  long long blocks = (ncell + 255) / 256;
+  long long cap = (long long)nsm * 16;
+  if (blocks > cap) blocks = cap;
+  k_lpt_cic<<<(unsigned)blocks, 256, 0, s>>>(grid, dx, dy, dz, *p);
+  return cudaGetLastError();
+}

@@ -1,0 +1,40 @@
+/*
+ * dens_api.h -- launch interface of dens.cu.
+ */
+#ifndef CG_DENS_API_H
+#define CG_DENS_API_H
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "cg_dev.cuh"
+
+struct cg_bins_params {
+  cg::Box box;
+  cg::Grid1 g;
+  cg::Tab zt, d1;
+  int mode;
+  const float *sigma2f;   /* device scalar, lognormal only */
+  int nz;
+  float idz;
+  int nt, bias_model;
+  cg::Tab bz[8];          /* bias tables of the tracers of this launch */
+  unsigned long long *ncount; /* [nz] */
+  double *zsum;               /* [nz] */
+  double *bsum;               /* [nt][nz] */
+};
+
+struct cg_lpt_params {
+  cg::Box box;
+  cg::Grid1 g;
+  cg::Tab d1;
+};
+
+cudaError_t cg_moments_final(cudaStream_t s, const double2 *part, size_t n, double inv_ncell, double *stats,
+                             float *s2f);
+cudaError_t cg_dens_bins(cudaStream_t s, float *grid, const cg_bins_params *p, int nsm);
+int cg_dens_bins_max_tracers(void);
+cudaError_t cg_lpt_cic(cudaStream_t s, float *grid, const float *dx, const float *dy, const float *dz,
+                       const cg_lpt_params *p, int nsm);
+
+#endif

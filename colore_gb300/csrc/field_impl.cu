@@ -1,0 +1,336 @@
+/*
+ * field_impl.cu -- Gaussian field (fourier.c:285-423) and 1LPT displacement
+ * transforms (density.c:376-445) for one grid size N = CG_N.
+ *
+ * This file is compiled once per supported grid size with -DCG_N=<N>; the
+ * dispatcher in capi.cu selects the instantiation.  Three passes make the
+ * 3-D c2r transform of the half spectrum H[kz][ky][kx] (kx in [0, N/2],
+ * fastest) into the padded real grid, in place:
+ *
+ *   1. fill + z : a block owns TX consecutive kx at one ky and all kz.  It
+ *                 generates the modes of every output field from one set of
+ *                 Philox draws (fields after the first are parked in shared
+ *                 memory), transforms along z and writes the result.  The
+ *                 spectrum is never read back from HBM.
+ *   2. y        : the same column transform along y, read-modify-write.
+ *   3. x (c2r)  : a group of threads owns one row of N/2+1 complex values;
+ *                 the Hermitian even/odd split turns the length-N real
+ *                 inverse into a length-N/2 complex one.  The normalisation
+ *                 (sqrt(2 pi)/L)^3 (fourier.c:383-398) and the partial sums
+ *                 of <d> and <d^2> (fourier.c:24-79) are fused here.
+ *
+ * FFTW's c2r semantics for the kx = 0 and kx = N/2 planes (the imaginary
+ * parts of each row's DC and Nyquist terms are ignored after the y and z
+ * transforms) are reproduced by dropping those imaginary parts in pass 3.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cg_dev.cuh"
+#include "fft.cuh"
+#include "field_api.h"
+
+#ifndef CG_N
+#error "compile with -DCG_N=<grid size>"
+#endif
+
+namespace {
+
+using namespace cg;
+
+/* Per-size transform plans: radices of the column (length N) and row
+ * (length N/2) transforms, elements per thread, tile widths. */
+template <int N>
+struct Plan;
+#define CG_PLAN(N_, CR_, C0_, C1_, C2_, TX2_, TX3_, TXY_, RR_, R0_, R1_, R2_, RB_)               \
+  template <>                                                                                \
+  struct Plan<N_> {                                                                          \
+    static constexpr int CR = CR_, C0 = C0_, C1 = C1_, C2 = C2_;                             \
+    static constexpr int TX2 = TX2_, TX3 = TX3_, TXY = TXY_;                                 \
+    static constexpr int RR = RR_, R0 = R0_, R1 = R1_, R2 = R2_, RB = RB_;                   \
+  };
+/*      N    CR  C0  C1 C2 TX2 TX3 TXY  RR  R0  R1 R2 RB */
+CG_PLAN(64, 8, 8, 8, 1, 32, 16, 32, 8, 8, 4, 1, 16)
+CG_PLAN(96, 24, 24, 4, 1, 32, 16, 32, 12, 12, 4, 1, 16)
+CG_PLAN(128, 16, 16, 8, 1, 32, 16, 32, 8, 8, 8, 1, 16)
+CG_PLAN(192, 24, 24, 8, 1, 16, 16, 32, 24, 24, 4, 1, 16)
+CG_PLAN(256, 16, 16, 16, 1, 16, 16, 32, 16, 16, 8, 1, 16)
+CG_PLAN(384, 24, 24, 4, 4, 16, 8, 16, 24, 24, 8, 1, 16)
+CG_PLAN(512, 32, 32, 16, 1, 16, 8, 16, 16, 16, 16, 1, 8)
+CG_PLAN(1024, 32, 32, 32, 1, 8, 4, 16, 32, 32, 16, 1, 8)
+CG_PLAN(2048, 32, 32, 32, 2, 4, 4, 8, 32, 32, 32, 1, 4)
+#undef CG_PLAN
+
+constexpr int N = CG_N;
+constexpr int NH = N / 2 + 1;
+using PL = Plan<N>;
+constexpr int P = N / PL::CR;       /* threads per column transform */
+constexpr int LH = N / 2;           /* row transform length         */
+constexpr int PR = LH / PL::RR;     /* threads per row transform    */
+constexpr int ROWS = (NH > LH + LH / 32 + 1) ? NH : (LH + LH / 32 + 1); /* smem per row */
+
+/* P(k) at log10 k, pk_linear0 (cosmo.c:291-308).  The interpolation branch
+ * stops at numk-2: the reference also takes it for ik = numk-1 and then
+ * reads one element past the table. */
+__device__ __forceinline__ float pk_lin(const FillParams &p, float lgk)
+{
+  int ik = (int)((lgk - p.logkmin) * p.idlogk);
+  if (ik < 0) return __ldg(&p.pk[0]) * exp10f(p.n_scal * (lgk - p.logkmin));
+  if (ik < p.numk - 1) {
+    float lk = p.logkmin + (float)ik / p.idlogk;
+    float a = __ldg(&p.pk[ik]), b = __ldg(&p.pk[ik + 1]);
+    return a + (lgk - lk) * (b - a) * p.idlogk;
+  }
+  return __ldg(&p.pk[p.numk - 1]) * exp10f(-3.0f * (lgk - p.logkmax));
+}
+
+__device__ __forceinline__ float kcomp(int i, int n, float dk) { return (float)(2 * i <= n ? i : i - n) * dk; }
+
+/* Unsmoothed Gaussian mode (rng_delta_gauss, common.c:191-201, with
+ * sigma^2 = P(k)/dk^3, fourier.c:343) and its |k|^2 and smoothing factor. */
+__device__ __forceinline__ float2 gen_mode(const FillParams &p, int kx, int ky, int kz, float &k2, float &sm)
+{
+  float kxf = (float)kx * p.dk, kyf = kcomp(ky, N, p.dk), kzf = kcomp(kz, N, p.dk);
+  k2 = kxf * kxf + kyf * kyf + kzf * kzf;
+  sm = 1.0f;
+  if (!(k2 > 0.0f)) return make_float2(0.0f, 0.0f);
+  float lgk = 0.5f * log10f(k2);
+  float s2 = pk_lin(p, lgk) * p.idk3;
+  uint64_t m = (uint64_t)kx + (uint64_t)NH * ((uint64_t)ky + (uint64_t)N * (uint64_t)kz);
+  cg_u32x4 w = cg_philox4x32_10((uint32_t)m, (uint32_t)(m >> 32), 0u, 0u, p.key0, p.key1);
+  float u1 = cg_u01f(w.v[0]), u2 = cg_u01f(w.v[1]);
+  float s, c;
+  sincospif(2.0f * u1, &s, &c);
+  float mod = sqrtf(-s2 * logf(1.0f - u2));
+  if (p.do_smooth) sm = expf(-0.5f * p.r2s * k2);
+  return make_float2(mod * c, mod * s);
+}
+
+/* Field values of one mode: F = 2 -> (delta_k, phi_k) (fourier.c:337-352);
+ * F = 3 -> 1LPT displacements i k_a delta'_k / (N^3 k^2) (density.c:430-436)
+ * where delta'_k = r2c(delta_G) = N^3 norm H(delta_k) and H is the Hermitian
+ * projection that the c2r applied on the kx = 0 and kx = N/2 planes. */
+template <int F>
+__device__ __forceinline__ void gen_fields(const FillParams &p, int kx, int ky, int kz, float2 *f)
+{
+  float k2, sm;
+  float2 d = gen_mode(p, kx, ky, kz, k2, sm);
+  if (!(k2 > 0.0f)) {
+#pragma unroll
+    for (int j = 0; j < F; j++) f[j] = make_float2(0.0f, 0.0f);
+    return;
+  }
+  if (F == 2) {
+    float g = -p.prefac / k2;
+    float2 phi = make_float2(g * d.x, g * d.y);
+    if (p.do_smooth) {
+      d.x *= sm;
+      d.y *= sm;
+      if (p.smooth_pot) {
+        phi.x *= sm;
+        phi.y *= sm;
+      }
+    }
+    f[0] = d;
+    f[1] = phi;
+  } else {
+    d.x *= sm;
+    d.y *= sm;
+    if (kx == 0 || kx == N / 2) {
+      int ky2 = ky == 0 ? 0 : N - ky, kz2 = kz == 0 ? 0 : N - kz;
+      float k2b, smb;
+      float2 e = gen_mode(p, kx, ky2, kz2, k2b, smb);
+      e.x *= smb;
+      e.y *= smb;
+      d = make_float2(0.5f * (d.x + e.x), 0.5f * (d.y - e.y));
+    }
+    float s = p.lpt_norm / k2;
+    float kv[3] = {(float)kx * p.dk, kcomp(ky, N, p.dk), kcomp(kz, N, p.dk)};
+#pragma unroll
+    for (int a = 0; a < 3; a++) f[a] = make_float2(-kv[a] * s * d.y, kv[a] * s * d.x);
+  }
+}
+
+/* Pass 1: fill + z transform of F fields.  grid = (ceil(NH/TX), N). */
+template <int F, int TX>
+__global__ void __launch_bounds__(TX *P) k_fill_z(float2 *o0, float2 *o1, float2 *o2, FillParams p,
+                                                  const float2 *__restrict__ twN)
+{
+  extern __shared__ float2 smem[];
+  const int c = threadIdx.x % TX, t = threadIdx.x / TX;
+  const int kx = blockIdx.x * TX + c, ky = blockIdx.y;
+  const bool ok = kx < NH;
+  float2 *outs[3] = {o0, o1, o2};
+  auto sm = [&](int pos) -> float2 & { return smem[pos * TX + c]; };
+#pragma unroll
+  for (int j = 0; j < F; j++) {
+    auto ld = [&](int pos) -> float2 {
+      if (j == 0) {
+        float2 f[F];
+        if (ok) gen_fields<F>(p, kx, ky, pos, f);
+        else {
+#pragma unroll
+          for (int q = 0; q < F; q++) f[q] = make_float2(0.0f, 0.0f);
+        }
+#pragma unroll
+        for (int q = 1; q < F; q++) smem[(size_t)q * N * TX + pos * TX + c] = f[q];
+        return f[0];
+      }
+      return smem[(size_t)j * N * TX + pos * TX + c];
+    };
+    float2 *o = outs[j];
+    auto st = [&](int pos, float2 v) {
+      if (ok) o[((size_t)pos * N + ky) * NH + kx] = v;
+    };
+    cgfft::transform<N, PL::CR, PL::C0, PL::C1, PL::C2, 1>(t, twN, ld, st, sm);
+    __syncthreads();
+  }
+}
+
+/* Pass 2: in-place column transform along y.  grid = (ceil(NH/TX), N, nf). */
+template <int TX>
+__global__ void __launch_bounds__(TX *P) k_col_y(float2 *f0, float2 *f1, float2 *f2,
+                                                 const float2 *__restrict__ twN)
+{
+  extern __shared__ float2 smem[];
+  const int c = threadIdx.x % TX, t = threadIdx.x / TX;
+  const int kx = blockIdx.x * TX + c, z = blockIdx.y;
+  const bool ok = kx < NH;
+  float2 *f = blockIdx.z == 0 ? f0 : (blockIdx.z == 1 ? f1 : f2);
+  float2 *base = f + (size_t)z * N * NH + kx;
+  auto sm = [&](int pos) -> float2 & { return smem[pos * TX + c]; };
+  auto ld = [&](int pos) -> float2 { return ok ? base[(size_t)pos * NH] : make_float2(0.0f, 0.0f); };
+  auto st = [&](int pos, float2 v) {
+    if (ok) base[(size_t)pos * NH] = v;
+  };
+  cgfft::transform<N, PL::CR, PL::C0, PL::C1, PL::C2, 1>(t, twN, ld, st, sm);
+}
+
+/* Pass 3: row c2r along x with normalisation and optional moment sums.
+ * grid = (N*N/RB, nf).  partials[blockIdx.x] = (sum d, sum d^2). */
+template <bool STATS>
+__global__ void __launch_bounds__(PL::RB *PR) k_row_c2r(float2 *f0, float2 *f1, float2 *f2, float norm,
+                                                        double2 *partials, const float2 *__restrict__ twN,
+                                                        const float2 *__restrict__ twH)
+{
+  extern __shared__ float2 smem[];
+  const int t = threadIdx.x % PR, rl = threadIdx.x / PR;
+  float2 *f = blockIdx.y == 0 ? f0 : (blockIdx.y == 1 ? f1 : f2);
+  const size_t row0 = (size_t)blockIdx.x * PL::RB;
+  /* stage the block's rows (contiguous in memory) */
+  const float2 *src = f + row0 * NH;
+  for (int i = threadIdx.x; i < PL::RB * NH; i += PL::RB * PR) {
+    int r = i / NH, k = i - r * NH;
+    smem[r * ROWS + k] = src[i];
+  }
+  __syncthreads();
+  float2 *row = smem + rl * ROWS;
+  float2 *dst = f + (row0 + rl) * NH;
+  auto ld = [&](int j) -> float2 {
+    float2 a = row[j], b = row[LH - j];
+    if (j == 0) {
+      a.y = 0.0f;
+      b.y = 0.0f;
+    }
+    float2 e = make_float2(a.x + b.x, a.y - b.y);
+    float2 o = make_float2(a.x - b.x, a.y + b.y);
+    float2 w = __ldg(&twN[j]);
+    float2 ow = make_float2(o.x * w.x - o.y * w.y, o.x * w.y + o.y * w.x);
+    return make_float2(e.x - ow.y, e.y + ow.x);
+  };
+  auto sm = [&](int pos) -> float2 & { return row[pos + (pos >> 5)]; };
+  float s1 = 0.0f, s2 = 0.0f;
+  auto st = [&](int n, float2 v) {
+    float2 r = make_float2(v.x * norm, v.y * norm);
+    dst[n] = r;
+    if (STATS) {
+      s1 += r.x + r.y;
+      s2 += r.x * r.x + r.y * r.y;
+    }
+  };
+  cgfft::transform<LH, PL::RR, PL::R0, PL::R1, PL::R2, 1>(t, twH, ld, st, sm);
+  if (STATS) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    __shared__ double red[2][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) {
+      red[0][wid] = (double)s1;
+      red[1][wid] = (double)s2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double a = 0.0, b = 0.0;
+      for (int w = 0; w < (PL::RB * PR + 31) / 32; w++) {
+        a += red[0][w];
+        b += red[1][w];
+      }
+      partials[blockIdx.x] = make_double2(a, b);
+    }
+  }
+}
+
+template <class K>
+cudaError_t prep(K kern, size_t smem)
+{
+  return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+} /* namespace */
+
+#define CG_CAT2(a, b) a##b
+#define CG_CAT(a, b) CG_CAT2(a, b)
+
+/* Gaussian density and potential: passes 1-3 on both grids. */
+extern "C" cudaError_t CG_CAT(cg_field_gauss_, CG_N)(const cg_field_launch *L)
+{
+  using namespace cg;
+  constexpr int TX2 = PL::TX2, TXY = PL::TXY;
+  size_t sm1 = (size_t)2 * N * TX2 * sizeof(float2);
+  size_t sm2 = (size_t)N * TXY * sizeof(float2);
+  size_t sm3 = (size_t)PL::RB * ROWS * sizeof(float2);
+  cudaError_t e;
+  if ((e = prep(k_fill_z<2, TX2>, sm1)) != cudaSuccess) return e;
+  if ((e = prep(k_col_y<TXY>, sm2)) != cudaSuccess) return e;
+  if ((e = prep(k_row_c2r<true>, sm3)) != cudaSuccess) return e;
+  if ((e = prep(k_row_c2r<false>, sm3)) != cudaSuccess) return e;
+  dim3 g1((NH + TX2 - 1) / TX2, N);
+  k_fill_z<2, TX2><<<g1, TX2 * P, sm1, L->stream>>>(L->f[0], L->f[1], nullptr, L->fill, L->twN);
+  dim3 g2((NH + TXY - 1) / TXY, N, 2);
+  k_col_y<TXY><<<g2, TXY * P, sm2, L->stream>>>(L->f[0], L->f[1], nullptr, L->twN);
+  dim3 g3((unsigned)((size_t)N * N / PL::RB), 1);
+  k_row_c2r<true><<<g3, PL::RB * PR, sm3, L->stream>>>(L->f[0], nullptr, nullptr, L->norm, L->partials,
+                                                        L->twN, L->twH);
+  k_row_c2r<false><<<g3, PL::RB * PR, sm3, L->stream>>>(L->f[1], nullptr, nullptr, L->norm, nullptr,
+                                                         L->twN, L->twH);
+  return cudaGetLastError();
+}
+
+/* 1LPT displacement fields Psi_x,y,z: passes 1-3 on three grids. */
+extern "C" cudaError_t CG_CAT(cg_field_lpt_, CG_N)(const cg_field_launch *L)
+{
+  using namespace cg;
+  constexpr int TX3 = PL::TX3, TXY = PL::TXY;
+  size_t sm1 = (size_t)3 * N * TX3 * sizeof(float2);
+  size_t sm2 = (size_t)N * TXY * sizeof(float2);
+  size_t sm3 = (size_t)PL::RB * ROWS * sizeof(float2);
+  cudaError_t e;
+  if ((e = prep(k_fill_z<3, TX3>, sm1)) != cudaSuccess) return e;
+  if ((e = prep(k_col_y<TXY>, sm2)) != cudaSuccess) return e;
+  if ((e = prep(k_row_c2r<false>, sm3)) != cudaSuccess) return e;
+  dim3 g1((NH + TX3 - 1) / TX3, N);
+  k_fill_z<3, TX3><<<g1, TX3 * P, sm1, L->stream>>>(L->f[0], L->f[1], L->f[2], L->fill, L->twN);
+  dim3 g2((NH + TXY - 1) / TXY, N, 3);
+  k_col_y<TXY><<<g2, TXY * P, sm2, L->stream>>>(L->f[0], L->f[1], L->f[2], L->twN);
+  dim3 g3((unsigned)((size_t)N * N / PL::RB), 3);
+  k_row_c2r<false><<<g3, PL::RB * PR, sm3, L->stream>>>(L->f[0], L->f[1], L->f[2], 1.0f, nullptr, L->twN,
+                                                         L->twH);
+  return cudaGetLastError();
+}
+
+/* Number of blocks of the moment-sum pass (size of the partials array). */
+extern "C" size_t CG_CAT(cg_field_npartials_, CG_N)(void) { return (size_t)N * N / PL::RB; }

@@ -1,0 +1,79 @@
+/*
+ * kappa.cu -- lensing convergence on source planes
+ * (kappa_get_beam_properties, kappa.c:78-175).
+ *
+ * One thread per HEALPix pixel (NEST id, as listed by hp_shell_alloc,
+ * common.c:505-552) marches the N/2 radial steps of the line of sight,
+ * samples the tidal tensor of the potential at the nearest grid cell
+ * (get_element, beaming.c:84-116; interpolate_from_grid NGP branch,
+ * beaming.c:148-182), projects it on the transverse directions and
+ * accumulates the two radial moments.  At each source-plane boundary it
+ * writes kappa_1 - kappa_2 / r_plane straight into RING order (the
+ * nest-to-ring reordering of write_kappa, io.c:826-873).  Threads of a warp
+ * hold neighbouring NEST pixels, so their rays stay close and the 19-point
+ * stencil reads hit L1/L2.  The radial sums use Kahan compensation.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cg_dev.cuh"
+#include "kappa_api.h"
+
+namespace {
+using namespace cg;
+
+__global__ void __launch_bounds__(256) k_kappa(const float *__restrict__ phi, cg_kappa_params p)
+{
+  extern __shared__ float ksh[];
+  float *f1 = ksh, *f2 = ksh + p.nr;
+  for (int i = threadIdx.x; i < p.nr; i += blockDim.x) {
+    f1[i] = p.fac1[i];
+    f2[i] = p.fac2[i];
+  }
+  __syncthreads();
+  const long long ip = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (ip >= p.npix) return;
+  const int N = p.box.N;
+  float u[3], rot[6];
+  cg_pix2vec_nest(p.nside, ip, u);
+  cg_kappa_rot(u, CG_MUL(p.box.idx, p.box.idx), rot);
+  const float po[3] = {p.box.p0, p.box.p1, p.box.p2};
+  const long long ring = cg_nest2ring(p.nside, ip);
+  float k1 = 0.0f, k1c = 0.0f, k2 = 0.0f, k2c = 0.0f;
+  for (int pl = 0; pl < p.nplanes; pl++) {
+    const int irmin = p.ir_min[pl], irmax = p.ir_max[pl];
+    for (int irr = irmin; irr <= irmax; irr++) {
+      const float rm = CG_MUL(CG_ADD((float)irr, 0.5f), p.dr);
+      const int x0 = cg_ngp_cell(rm, u[0], po[0], p.box.idx, N);
+      const int y0 = cg_ngp_cell(rm, u[1], po[1], p.box.idx, N);
+      const int z0 = cg_ngp_cell(rm, u[2], po[2], p.box.idx, N);
+      const int xh = wrap(x0 + 1, N), xl = wrap(x0 - 1, N);
+      const int yh = wrap(y0 + 1, N), yl = wrap(y0 - 1, N);
+      const int zh = wrap(z0 + 1, N), zl = wrap(z0 - 1, N);
+#define PHI(X, Y, Z) __ldg(&phi[pidx((X), (Y), (Z), N)])
+      const float f[19] = {PHI(x0, y0, z0), PHI(xh, y0, z0), PHI(xl, y0, z0), PHI(x0, yh, z0), PHI(x0, yl, z0),
+                           PHI(x0, y0, zh), PHI(x0, y0, zl), PHI(xh, yh, z0), PHI(xl, yl, z0), PHI(xh, yl, z0),
+                           PHI(xl, yh, z0), PHI(xh, y0, zh), PHI(xl, y0, zl), PHI(xh, y0, zl), PHI(xl, y0, zh),
+                           PHI(x0, yh, zh), PHI(x0, yl, zl), PHI(x0, yh, zl), PHI(x0, yl, zh)};
+#undef PHI
+      float t[6];
+      cg_tidal(f, t);
+      const float dot = cg_dot6(rot, t);
+      cg_kahan_add(&k1, &k1c, CG_MUL(dot, f1[irr]));
+      cg_kahan_add(&k2, &k2c, CG_MUL(dot, f2[irr]));
+    }
+    p.map[(long long)pl * p.npix + ring] = CG_SUB(k1, CG_MUL(p.inv_r_max[pl], k2));
+  }
+}
+
+} /* namespace */
+
+cudaError_t cg_kappa_integrate(cudaStream_t s, const float *phi, const cg_kappa_params *p)
+{
+  size_t smem = (size_t)2 * p->nr * sizeof(float);
+  cudaError_t e = cudaFuncSetAttribute(k_kappa, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  long long blocks = (p->npix + 255) / 256;
+  k_kappa<<<(unsigned)blocks, 256, smem, s>>>(phi, *p);
+  return cudaGetLastError();
+}

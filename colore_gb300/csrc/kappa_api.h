@@ -1,0 +1,26 @@
+/*
+ * kappa_api.h -- launch interface of kappa.cu.
+ */
+#ifndef CG_KAPPA_API_H
+#define CG_KAPPA_API_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cg_dev.cuh"
+
+struct cg_kappa_params {
+  cg::Box box;
+  int64_t nside, npix;
+  int nplanes;            /* sorted by distance (kappa_beams_preproc, kappa.c:39-76) */
+  const int *ir_min, *ir_max;
+  const float *inv_r_max;
+  int nr;                 /* radial steps N/2 (get_radial_params, common.c:333-337) */
+  float dr;
+  const float *fac1, *fac2; /* r D (1+z) dr and r^2 D (1+z) dr, kappa.c:109-116 */
+  float *map;             /* nplanes * npix, RING order */
+};
+
+cudaError_t cg_kappa_integrate(cudaStream_t s, const float *phi, const cg_kappa_params *p);
+
+#endif

@@ -1,0 +1,186 @@
+/*
+ * colore_cuda.h -- C ABI of libcolore_cuda.so, the sm_103a implementation
+ * of CoLoRe's mock-generation path (Gaussian field -> lognormal/1LPT density
+ * -> bias normalisation -> Poisson sources -> HEALPix sources, intensity and
+ * convergence maps).
+ *
+ * One cg_ctx owns one GPU's grids, tables, catalogs and maps.  Every call is
+ * enqueued on the context's CUDA stream and returns 0 on success or a
+ * nonzero CG_E* status; cg_last_error() gives the message.  Device work
+ * never traps: bounded loops set an error word that the next host
+ * synchronisation turns into CG_EDEVICE.
+ *
+ * The stage entry points map one-to-one onto the reference's hot-path
+ * functions (paths relative to the CoLoRe source tree):
+ *
+ *   cg_create_cartesian_fields        src/fourier.c:361  create_cartesian_fields
+ *   cg_compute_physical_density_field src/density.c:1105 compute_physical_density_field
+ *   cg_compute_density_normalization  src/density.c:1227 compute_density_normalization
+ *   cg_srcs_set_cartesian             src/srcs.c:285     srcs_set_cartesian
+ *                                     (+ src/srcs.c:375 srcs_distribute, an identity
+ *                                      on one GPU, + src/srcs.c:418
+ *                                      srcs_get_local_properties, fused)
+ *   cg_imap_set_cartesian             src/imap.c:247     imap_set_cartesian
+ *   cg_get_beam_properties            src/beaming.c:293  get_beam_properties
+ *                                     (kappa: src/kappa.c:39,78; source RSD:
+ *                                      src/srcs.c:445,627,739)
+ *   cg_download_*                     host mirrors consumed by src/io.c writers
+ *
+ * Layouts at the boundary are the reference's: padded real grids
+ * index = ix + 2(N/2+1)(iy + N iz) (src/fourier.c:46-51); catalogs as
+ * CatalogCartesian (4 floats + 1 int per source, src/common.h:162-167) and
+ * Src (9 floats, src/common.h:169-179); maps full-sky RING order.
+ */
+#ifndef COLORE_CUDA_H
+#define COLORE_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CG_OK 0
+#define CG_EINVAL 1   /* bad argument or configuration            */
+#define CG_ENOMEM 2   /* device or host allocation failed          */
+#define CG_ECUDA 3    /* CUDA runtime / library error              */
+#define CG_EDEVICE 4  /* a kernel reported an error through its flag */
+#define CG_ESTATE 5   /* stage called out of order                 */
+
+#define CG_PREC_F32 0 /* FP32 fields and per-cell math, FP64 reductions */
+#define CG_PREC_F64 1 /* plain FP64 path: cuFFT Z2D + unfused FP64 kernels */
+
+#define CG_NPOP_MAX 10      /* NPOP_MAX, src/common.h:133    */
+#define CG_NPLANES_MAX 100  /* NPLANES_MAX, src/common.h:134 */
+#define CG_NA 5001          /* NA, src/common.h:132          */
+
+/* dens_type values, src/common.h:115-118 */
+#define CG_DENS_LGNR 0
+#define CG_DENS_1LPT 1
+#define CG_DENS_CLIP 3
+
+/* bias models, src/common.h:414-431 */
+#define CG_BIAS_MODEL_POW 1    /* (1+d)^b, built without flags      */
+#define CG_BIAS_MODEL_EXPLIN 2 /* -D_BIAS_MODEL_2 (Makefile default) */
+#define CG_BIAS_MODEL_LIN 3    /* -D_BIAS_MODEL_3                    */
+
+/*
+ * Everything the hot path reads from ParamCoLoRe (src/common.h:220-381).
+ * Tables are host arrays in double precision, copied by cg_upload_tables.
+ */
+typedef struct {
+  int precision;           /* CG_PREC_*                                    */
+  int n_grid;              /* N                                            */
+  double l_box;            /* box side [Mpc/h], src/cosmo.c:544            */
+  double pos_obs[3];       /* observer, src/cosmo.c:545-547                */
+  uint64_t seed;           /* seed_rng                                     */
+  /* cosmology scalars */
+  double omega_m, hubble_0, fgrowth_0, prefac_lensing, r_max;
+  /* field options */
+  double r2_smooth;        /* squared smoothing length (src/io.c:453-458)  */
+  int do_smoothing, smooth_potential, dens_type, bias_model;
+  /* P(k): uniform in log10 k, already sigma8-normalised (src/cosmo.c:444-495) */
+  int numk;
+  double logkmin, logkmax, idlogk, n_scal;
+  const double *pkarr;
+  /* background on the r-uniform grid r_i = i/glob_idr, CG_NA entries
+   * (src/cosmo.c:668-717), and the a-uniform r(a) table (src/cosmo.c:669-674) */
+  double glob_idr;
+  const double *r_arr_r2z, *z_arr_r2z, *growth_d_arr, *growth_d2_arr, *growth_v_arr,
+      *growth_pd_arr, *ihub_arr;
+  const double *a_arr_a2r, *r_arr_a2r;
+  /* galaxy populations */
+  int n_srcs;
+  const double *srcs_nz_arr[CG_NPOP_MAX];
+  const double *srcs_bz_arr[CG_NPOP_MAX];
+  int nside_base;                  /* src/io.c:224-244 (2 on one GPU)      */
+  int nside_count[CG_NPOP_MAX];    /* source count map resolution, 0 = off */
+  /* intensity-mapping species */
+  int n_imap;
+  const double *imap_tz_arr[CG_NPOP_MAX];
+  const double *imap_bz_arr[CG_NPOP_MAX];
+  int nside_imap[CG_NPOP_MAX];
+  int imap_nr[CG_NPOP_MAX];
+  const double *imap_r0[CG_NPOP_MAX]; /* shell edges, any order (sorted here) */
+  const double *imap_rf[CG_NPOP_MAX];
+  /* convergence */
+  int do_kappa, n_kappa, nside_kappa;
+  double kappa_r[CG_NPLANES_MAX]; /* source-plane comoving distances */
+  /* need_beaming, src/io.c:460-461 */
+  int need_beaming;
+} cg_config;
+
+typedef struct cg_ctx cg_ctx;
+
+/* Lifetime ---------------------------------------------------------------- */
+int cg_create(cg_ctx **out, const cg_config *cfg, int device);
+void cg_destroy(cg_ctx *ctx);
+const char *cg_last_error(const cg_ctx *ctx);
+int cg_set_stream(cg_ctx *ctx, void *cuda_stream); /* NULL = context's own */
+int cg_sync(cg_ctx *ctx);
+/* Bytes of device memory the context would hold for cfg (get_max_memory,
+ * src/common.c:571-750). */
+int cg_memory_estimate(const cg_config *cfg, unsigned long long *bytes);
+
+/* Upload (or re-upload) every table of cfg (same geometry as at create). */
+int cg_upload_tables(cg_ctx *ctx, const cg_config *cfg);
+
+/* Stages ------------------------------------------------------------------ */
+int cg_create_cartesian_fields(cg_ctx *ctx);
+int cg_get_sigma2(cg_ctx *ctx, double *sigma2_gauss, double *mean_gauss);
+int cg_compute_physical_density_field(cg_ctx *ctx);
+int cg_compute_density_normalization(cg_ctx *ctx);
+/* Device half of compute_density_normalization (density.c:1128-1211):
+ * per-redshift-bin cell counts, summed redshifts and summed bias_model per
+ * tracer.  Arrays have nz entries; norm arrays are [n_srcs][nz], [n_imap][nz]. */
+int cg_collect_density_normalization(cg_ctx *ctx, int nz, double idz, double *zarr,
+                                     unsigned long long *narr, double *norm_srcs,
+                                     double *norm_imap);
+/* Replace the NA-point normalisation tables (src/density.c:1323-1355). */
+int cg_set_norm_tables(cg_ctx *ctx, const double *srcs_norm, const double *srcs_norm_0f,
+                       const double *imap_norm, const double *imap_norm_0f);
+int cg_srcs_set_cartesian(cg_ctx *ctx, long long *nsrc_per_pop);
+int cg_imap_set_cartesian(cg_ctx *ctx);
+int cg_get_beam_properties(cg_ctx *ctx);
+/* Run the whole driver sequence of src/main.c:66-125 in one call. */
+int cg_run_mock(cg_ctx *ctx);
+
+/* Host mirrors -------------------------------------------------------------- */
+/* which: 0 = density (grid_dens), 1 = potential (grid_npot), 2..4 = 1LPT
+ * displacement x,y,z.  dst holds N*N*2(N/2+1) values of the context's
+ * precision (float or double), padded layout. */
+int cg_download_grid(cg_ctx *ctx, int which, void *dst);
+long long cg_num_sources(cg_ctx *ctx, int ipop);
+/* pos4: 4 floats per source (x,y,z,dz_rsd) as CatalogCartesian.pos;
+ * ipix: nside_base NEST id; src9: 9 floats per source as Src.  Any may be NULL. */
+int cg_download_catalog(cg_ctx *ctx, int ipop, float *pos4, int *ipix, float *src9);
+/* Counts of sources per RING pixel at nside_count[ipop]. */
+int cg_download_count_map(cg_ctx *ctx, int ipop, int *counts);
+/* Intensity map of species ipop: nr * 12 nside^2 values in RING order,
+ * finalised as data/nadd where nadd > 0 (src/io.c:738-741); nadd may be NULL. */
+int cg_download_imap(cg_ctx *ctx, int ipop, float *map, int *nadd);
+/* Convergence maps: n_kappa * 12 nside^2 values, RING order (src/io.c:826-873). */
+int cg_download_kappa(cg_ctx *ctx, float *map);
+
+/* FP32 normalisation table the kernels use: kind 0 = source population
+ * ipop (srcs_norm_arr, src/common.h:318), 1 = intensity species
+ * (imap_norm_arr, src/common.h:336).  tab: CG_NA floats; edges: the values
+ * below and above the table (norm_*_0 / norm_*_f). */
+int cg_download_norm(cg_ctx *ctx, int kind, int ipop, float *tab, float *edges);
+
+/* Per-kernel timing: when on, every launch group is bracketed by CUDA
+ * events on the context's stream; cg_kernel_times synchronises, returns the
+ * groups in launch order (names ';'-separated, milliseconds) and clears the
+ * log. */
+int cg_set_profiling(cg_ctx *ctx, int on);
+int cg_kernel_times(cg_ctx *ctx, char *names, size_t names_len, float *ms, int cap, int *n);
+
+/* Launch accounting: number of kernels this context has launched. */
+long long cg_kernel_launches(const cg_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COLORE_CUDA_H */

@@ -1,0 +1,104 @@
+/*
+ * colore_host.h -- host side of the GPU path, in C: the run parameters of
+ * CoLoRe (ParamCoLoRe, src/common.h:220-381, hot-path fields only), the
+ * param-file reader (read_run_params, src/io.c:246-563) and the FP64 tables
+ * it builds (cosmo_set, src/cosmo.c:516-816; compute_tracer_cosmo,
+ * src/cosmo.c:818-849), plus their translation into a cg_config.
+ *
+ * GSL, libconfig and FFTW are not needed: the quadratures, the natural cubic
+ * spline and the libconfig-grammar parser are implemented in
+ * colore_gb300/csrc/host/.
+ */
+#ifndef COLORE_HOST_H
+#define COLORE_HOST_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "colore_cuda.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+  /* global */
+  char prefix_out[256], pk_filename[256], output_format[16];
+  double z_min, z_max;
+  int output_density;
+  unsigned long long seed;
+  int write_pred;
+  /* field_par */
+  double r_smooth;          /* as read; r2_smooth = r_smooth^2 (io.c:453-458) */
+  double r2_smooth;
+  int do_smoothing, smooth_potential, n_grid, dens_type, lpt_interp_type, output_lpt;
+  double lpt_buffer_fraction;
+  /* cosmo_par */
+  double omega_m, omega_l, omega_b, h, w, ns, sigma8;
+  /* derived cosmology */
+  double fgrowth_0, hubble_0, prefac_lensing, r_min, r_max, l_box, pos_obs[3];
+  double sigma2_gauss_theory, sigma8_input;
+  /* P(k) */
+  int numk;
+  double logkmin, logkmax, idlogk;
+  double *logkarr, *pkarr;
+  /* background tables */
+  double glob_idr;
+  double a_arr_a2r[CG_NA], r_arr_a2r[CG_NA], z_arr_r2z[CG_NA], r_arr_r2z[CG_NA];
+  double growth_d_arr[CG_NA], growth_d2_arr[CG_NA], growth_v_arr[CG_NA], growth_pd_arr[CG_NA], ihub_arr[CG_NA];
+  /* sources */
+  int n_srcs;
+  char fname_nz_srcs[CG_NPOP_MAX][256], fname_bz_srcs[CG_NPOP_MAX][256];
+  int lensing_srcs[CG_NPOP_MAX], skw_srcs[CG_NPOP_MAX], nside_count[CG_NPOP_MAX];
+  double *srcs_nz_arr[CG_NPOP_MAX], *srcs_bz_arr[CG_NPOP_MAX];
+  /* intensity maps */
+  int n_imap;
+  char fname_tz_imap[CG_NPOP_MAX][256], fname_bz_imap[CG_NPOP_MAX][256], fname_nu_imap[CG_NPOP_MAX][256];
+  double nu0_imap[CG_NPOP_MAX];
+  int nside_imap[CG_NPOP_MAX], imap_nr[CG_NPOP_MAX];
+  double *imap_tz_arr[CG_NPOP_MAX], *imap_bz_arr[CG_NPOP_MAX], *imap_r0[CG_NPOP_MAX], *imap_rf[CG_NPOP_MAX];
+  /* kappa */
+  int do_kappa, n_kappa, nside_kappa;
+  double z_kappa_out[CG_NPLANES_MAX], kappa_r[CG_NPLANES_MAX];
+  /* out-of-scope sections seen in the file (reported, not run) */
+  int n_cstm, do_isw, do_skewers, do_srcs_lensing;
+  int need_beaming, nside_base, bias_model;
+} cg_params;
+
+/* read_run_params: parse the file, read the input tables and build every
+ * FP64 table.  Returns 0 or a CG_E* code with a message in err. */
+int cg_read_run_params(const char *fname, cg_params **out, char *err, size_t errlen);
+void cg_params_free(cg_params *p);
+/* Point cfg at p's tables (p must outlive cfg). */
+int cg_params_to_config(const cg_params *p, cg_config *cfg);
+
+/* Background cosmology of cosmo_mad.c (flat or curved, constant w). */
+typedef struct {
+  double om, ol, ob, ok, h, w0;
+  int ksign, normal_de;
+  double a_eq, phorizon, growth0;
+} cg_cosmo;
+int cg_cosmo_init(cg_cosmo *c, double om, double ol, double ob, double w, double h);
+double cg_cosmo_hubble(const cg_cosmo *c, double a);            /* h/Mpc           */
+double cg_cosmo_chi(const cg_cosmo *c, double a);               /* Mpc/h           */
+double cg_cosmo_growth(const cg_cosmo *c, double a);            /* unnormalised D  */
+double cg_cosmo_fgrowth(const cg_cosmo *c, double a);
+double cg_cosmo_omega_m(const cg_cosmo *c, double a);
+
+/* Natural cubic spline (the gsl_interp_cspline of the reference). */
+typedef struct {
+  int n;
+  double *x, *y, *m; /* m = second derivatives */
+} cg_spline;
+int cg_spline_init(cg_spline *s, const double *x, const double *y, int n);
+double cg_spline_eval(const cg_spline *s, double x); /* NaN outside [x0, x_{n-1}] */
+void cg_spline_free(cg_spline *s);
+
+/* Adaptive Gauss-Legendre quadrature of f on [a, b] to relative tolerance. */
+double cg_integrate(double (*f)(double, void *), void *par, double a, double b, double rtol);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COLORE_HOST_H */

@@ -1,0 +1,37 @@
+"""ORACLE build recipe (test infrastructure only): compiles the CPU
+restatement in oracle/ into oracle/_lib/liboracle.so with OpenMP.
+
+Only tests/, the smoke check and bench.py's CPU-baseline leg load it.
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+OUTDIR = os.path.join(HERE, "_lib")
+LIB = os.path.join(OUTDIR, "liboracle.so")
+SRCS = ["or_fft.c", "or_ref64.c", "or_dev32.c", "or_checks.c"]
+
+
+def build(verbose=False):
+    os.makedirs(OUTDIR, exist_ok=True)
+    srcs = [os.path.join(HERE, s) for s in SRCS]
+    deps = srcs + [os.path.join(HERE, "oracle.h"),
+                   os.path.join(ROOT, "colore_gb300", "csrc", "cg_math.h"),
+                   os.path.join(ROOT, "colore_gb300", "csrc", "cg_cell.h"),
+                   os.path.join(ROOT, "include", "colore_cuda.h")]
+    if os.path.exists(LIB) and all(os.path.getmtime(d) <= os.path.getmtime(LIB) for d in deps):
+        return LIB
+    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-std=gnu11", "-fopenmp", "-ffp-contract=off",
+           "-Wall", "-Wno-unused-function", "-o", LIB] + srcs + ["-lm"]
+    if verbose:
+        print(" ".join(cmd))
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

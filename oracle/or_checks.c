@@ -1,0 +1,46 @@
+/*
+ * or_checks.c -- ORACLE (test infrastructure only).  Array wrappers around
+ * the shared scalar functions of cg_math.h / cg_cell.h so that tests can
+ * check them against libm, numpy and HEALPix identities on the CPU.
+ */
+#include <stdint.h>
+
+#include "../colore_gb300/csrc/cg_cell.h"
+
+void or_vec_expf(const float *x, float *y, long n) { for (long i = 0; i < n; i++) y[i] = cg_expf(x[i]); }
+void or_vec_logf(const float *x, float *y, long n) { for (long i = 0; i < n; i++) y[i] = cg_logf(x[i]); }
+void or_vec_log1pf(const float *x, float *y, long n) { for (long i = 0; i < n; i++) y[i] = cg_log1pf(x[i]); }
+void or_vec_acosf(const float *x, float *y, long n) { for (long i = 0; i < n; i++) y[i] = cg_acosf(x[i]); }
+void or_vec_atan2f(const float *y, const float *x, float *o, long n)
+{
+  for (long i = 0; i < n; i++) o[i] = cg_atan2f(y[i], x[i]);
+}
+void or_vec_sincosf(const float *x, float *s, float *c, long n)
+{
+  for (long i = 0; i < n; i++) cg_sincosf(x[i], &s[i], &c[i]);
+}
+void or_philox(const uint32_t *ctr, const uint32_t *key, uint32_t *out)
+{
+  cg_u32x4 r = cg_philox4x32_10(ctr[0], ctr[1], ctr[2], ctr[3], key[0], key[1]);
+  for (int i = 0; i < 4; i++) out[i] = r.v[i];
+}
+void or_poisson(const float *lam, int *k, long n, uint32_t k0, uint32_t k1)
+{
+  for (long i = 0; i < n; i++) k[i] = cg_poisson(lam[i], k0, k1, (uint32_t)i, (uint32_t)(i >> 32));
+}
+void or_ang2pix(long nside, const float *cth, const float *phi, long long *pix, long n)
+{
+  for (long i = 0; i < n; i++) pix[i] = cg_ang2pix_ring(nside, cth[i], phi[i]);
+}
+void or_nest2ring(long nside, const long long *in, long long *out, long n)
+{
+  for (long i = 0; i < n; i++) out[i] = cg_nest2ring(nside, in[i]);
+}
+void or_ring2nest(long nside, const long long *in, long long *out, long n)
+{
+  for (long i = 0; i < n; i++) out[i] = cg_ring2nest(nside, in[i]);
+}
+void or_pix2vec_nest(long nside, const long long *in, float *v, long n)
+{
+  for (long i = 0; i < n; i++) cg_pix2vec_nest(nside, in[i], v + 3 * i);
+}

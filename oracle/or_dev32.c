@@ -1,0 +1,496 @@
+/*
+ * or_dev32.c -- ORACLE (test infrastructure only).  CPU restatement of the
+ * per-cell stages of CoLoRe evaluated with the single-precision arithmetic
+ * the GPU kernels define (colore_gb300/csrc/cg_cell.h), in the reference's
+ * loop order, so that integer results can be compared bit for bit:
+ *   or_density32  lognormalize / densclip / 1LPT rho-1   density.c:1034-1103, 610-624
+ *   or_bins32     collect_density_normalization_from_grid density.c:1128-1211
+ *   or_counts32   srcs_set_cartesian_single, pass 1       srcs.c:156-184
+ *   or_emit32     srcs_set_cartesian_single, pass 2, and
+ *                 srcs_get_local_properties_single        srcs.c:238-276, 386-416
+ *   or_beam_rsd32 srcs beam RSD (pre/get/postproc)        srcs.c:437-504, 656-662
+ *   or_imap32     imap_set_cartesian_single               imap.c:135-245
+ *   or_kappa32    kappa_get_beam_properties               kappa.c:78-175
+ * Tables are rebuilt from the config with the same double->float roundings
+ * as the GPU upload.  The Poisson and position streams are the Philox
+ * streams of the GPU path (the reference's GSL MT19937 streams depend on the
+ * OpenMP thread count and cannot be reproduced).
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../colore_gb300/csrc/cg_cell.h"
+#include "oracle.h"
+
+typedef struct {
+  const float *f;
+  float f0, ff;
+} T32;
+
+typedef struct {
+  int N;
+  float dx, idx, L, p[3];
+  float *tabs, *r, r_last, idr;
+  T32 zt, d1, v1, ih;
+  float *a_a2r, *r_a2r;
+  T32 nz[CG_NPOP_MAX], bz[CG_NPOP_MAX], tz[CG_NPOP_MAX], bzi[CG_NPOP_MAX];
+} S32;
+
+static void s32_init(S32 *s, const cg_config *c)
+{
+  const int na = CG_NA;
+  const int ntab = 9 + 2 * c->n_srcs + 2 * c->n_imap;
+  s->tabs = malloc((size_t)ntab * na * sizeof(float));
+  const double *src[9] = {c->r_arr_r2z, c->z_arr_r2z, c->growth_d_arr, c->growth_d2_arr, c->growth_v_arr,
+                          c->growth_pd_arr, c->ihub_arr, c->a_arr_a2r, c->r_arr_a2r};
+  int k = 0;
+  for (int t = 0; t < 9; t++, k++)
+    for (int i = 0; i < na; i++) s->tabs[(size_t)k * na + i] = (float)src[t][i];
+  for (int p = 0; p < c->n_srcs; p++) {
+    for (int i = 0; i < na; i++) s->tabs[(size_t)k * na + i] = (float)c->srcs_nz_arr[p][i];
+    for (int i = 0; i < na; i++) s->tabs[(size_t)(k + 1) * na + i] = (float)c->srcs_bz_arr[p][i];
+    s->nz[p] = (T32){s->tabs + (size_t)k * na, 0.0f, 0.0f};
+    s->bz[p] = (T32){s->tabs + (size_t)(k + 1) * na, (float)c->srcs_bz_arr[p][0], 1.0f};
+    k += 2;
+  }
+  for (int p = 0; p < c->n_imap; p++) {
+    for (int i = 0; i < na; i++) s->tabs[(size_t)k * na + i] = (float)c->imap_tz_arr[p][i];
+    for (int i = 0; i < na; i++) s->tabs[(size_t)(k + 1) * na + i] = (float)c->imap_bz_arr[p][i];
+    s->tz[p] = (T32){s->tabs + (size_t)k * na, 0.0f, 0.0f};
+    s->bzi[p] = (T32){s->tabs + (size_t)(k + 1) * na, (float)c->imap_bz_arr[p][0], 1.0f};
+    k += 2;
+  }
+  float *T = s->tabs;
+  s->r = T;
+  s->r_last = (float)c->r_arr_r2z[na - 1];
+  s->idr = (float)c->glob_idr;
+  s->zt = (T32){T + 1 * na, 0.0f, (float)c->z_arr_r2z[na - 1]};
+  s->d1 = (T32){T + 2 * na, 1.0f, (float)c->growth_d_arr[na - 1]};
+  s->v1 = (T32){T + 4 * na, (float)c->growth_v_arr[0], (float)c->growth_v_arr[na - 1]};
+  s->ih = (T32){T + 6 * na, (float)c->ihub_arr[0], (float)c->ihub_arr[na - 1]};
+  s->a_a2r = T + 7 * na;
+  s->r_a2r = T + 8 * na;
+  s->N = c->n_grid;
+  s->dx = (float)(c->l_box / c->n_grid);
+  s->idx = (float)(c->n_grid / c->l_box);
+  s->L = (float)c->l_box;
+  for (int i = 0; i < 3; i++) s->p[i] = (float)c->pos_obs[i];
+}
+
+static void s32_free(S32 *s) { free(s->tabs); }
+
+static float bg32(const S32 *s, T32 t, float r) { return cg_bg_eval(t.f, s->r, t.f0, t.ff, r, s->r_last, s->idr); }
+
+static long long pidx(int ix, int iy, int iz, int N)
+{
+  return (long long)ix + (long long)(2 * (N / 2 + 1)) * ((long long)iy + (long long)N * iz);
+}
+
+static int wrapi(int i, int N) { return i >= N ? i - N : (i < 0 ? i + N : i); }
+
+int or_density32(const cg_config *cfg, float *dens, float s2f, int mode)
+{
+  S32 s;
+  s32_init(&s, cfg);
+  const int N = s.N;
+#pragma omp parallel for schedule(static)
+  for (int iz = 0; iz < N; iz++) {
+    float z0 = cg_cell_coord(iz, s.dx, s.p[2]);
+    for (int iy = 0; iy < N; iy++) {
+      float y0 = cg_cell_coord(iy, s.dx, s.p[1]);
+      for (int ix = 0; ix < N; ix++) {
+        float x0 = cg_cell_coord(ix, s.dx, s.p[0]);
+        float r = cg_norm3(x0, y0, z0);
+        long long id = pidx(ix, iy, iz, N);
+        dens[id] = cg_dens_transform(mode, dens[id], bg32(&s, s.d1, r), s2f);
+      }
+    }
+  }
+  s32_free(&s);
+  return 0;
+}
+
+int or_bins32(const cg_config *cfg, const float *dens, int nz, double idz, unsigned long long *narr, double *zarr,
+              double *bsum)
+{
+  S32 s;
+  s32_init(&s, cfg);
+  const int N = s.N, nts = cfg->n_srcs, nt = nts + cfg->n_imap;
+  const float idzf = (float)idz;
+  memset(narr, 0, nz * sizeof(unsigned long long));
+  memset(zarr, 0, nz * sizeof(double));
+  memset(bsum, 0, (size_t)nt * nz * sizeof(double));
+  for (int iz = 0; iz < N; iz++) {
+    float z0 = cg_cell_coord(iz, s.dx, s.p[2]);
+    for (int iy = 0; iy < N; iy++) {
+      float y0 = cg_cell_coord(iy, s.dx, s.p[1]);
+      for (int ix = 0; ix < N; ix++) {
+        float x0 = cg_cell_coord(ix, s.dx, s.p[0]);
+        float r = cg_norm3(x0, y0, z0);
+        float z = bg32(&s, s.zt, r);
+        int b = (int)CG_MUL(z, idzf) + 1;
+        if (b < 0 || b >= nz) continue;
+        float d = dens[pidx(ix, iy, iz, N)];
+        narr[b]++;
+        zarr[b] += z;
+        for (int t = 0; t < nt; t++) {
+          T32 tb = t < nts ? s.bz[t] : s.bzi[t - nts];
+          bsum[(size_t)t * nz + b] += cg_bias_model(d, bg32(&s, tb, r), cfg->bias_model);
+        }
+      }
+    }
+  }
+  s32_free(&s);
+  return 0;
+}
+
+static void src_keys(const cg_config *c, int ipop, uint32_t *kp0, uint32_t *kp1, uint32_t *kq0, uint32_t *kq1)
+{
+  *kp0 = (uint32_t)c->seed;
+  *kp1 = (uint32_t)(c->seed >> 32) ^ (CG_STREAM_POIS + (uint32_t)ipop);
+  *kq0 = (uint32_t)c->seed;
+  *kq1 = (uint32_t)(c->seed >> 32) ^ (CG_STREAM_POS + (uint32_t)ipop);
+}
+
+static int cell_count(const cg_config *cfg, const S32 *s, int ipop, const float *dens, T32 nrm, int ix, int iy,
+                      int iz, float rlim, float cvol, uint32_t kp0, uint32_t kp1)
+{
+  const int N = s->N;
+  float x0 = cg_cell_coord(ix, s->dx, s->p[0]), y0 = cg_cell_coord(iy, s->dx, s->p[1]),
+        z0 = cg_cell_coord(iz, s->dx, s->p[2]);
+  float r = cg_norm3(x0, y0, z0);
+  if (!(r < rlim)) return 0;
+  float nd = bg32(s, s->nz[ipop], r);
+  if (!(nd > 0.0f)) return 0;
+  float lam = cg_src_lambda(nd, cvol, dens[pidx(ix, iy, iz, N)], bg32(s, s->bz[ipop], r), bg32(s, nrm, r),
+                            cfg->bias_model);
+  if (!(lam > 0.0f)) return 0;
+  long long cid = (long long)ix + (long long)N * ((long long)iy + (long long)N * iz);
+  int n = cg_poisson(lam, kp0, kp1, (uint32_t)cid, (uint32_t)(cid >> 32));
+  return n > 65535 ? 65535 : n;
+}
+
+int or_counts32(const cg_config *cfg, int ipop, const float *dens, const float *normtab, float n0, float nf,
+                unsigned short *counts, long long *total)
+{
+  S32 s;
+  s32_init(&s, cfg);
+  const int N = s.N;
+  T32 nrm = {normtab, n0, nf};
+  uint32_t kp0, kp1, kq0, kq1;
+  src_keys(cfg, ipop, &kp0, &kp1, &kq0, &kq1);
+  const float rlim = (float)(cfg->l_box / 2 + 20.);
+  const double dxd = cfg->l_box / N;
+  const float cvol = (float)(dxd * dxd * dxd);
+  long long tot = 0;
+#pragma omp parallel for schedule(static) reduction(+ : tot)
+  for (int iz = 0; iz < N; iz++)
+    for (int iy = 0; iy < N; iy++)
+      for (int ix = 0; ix < N; ix++) {
+        int n = cell_count(cfg, &s, ipop, dens, nrm, ix, iy, iz, rlim, cvol, kp0, kp1);
+        if (counts) counts[(size_t)ix + (size_t)N * ((size_t)iy + (size_t)N * iz)] = (unsigned short)n;
+        tot += n;
+      }
+  *total = tot;
+  s32_free(&s);
+  return 0;
+}
+
+int or_emit32(const cg_config *cfg, int ipop, const float *dens, const float *npot, const float *normtab, float n0,
+              float nf, long long cap, float *pos4, int *ipix, float *src9, int *cmap, long long *nsrc)
+{
+  S32 s;
+  s32_init(&s, cfg);
+  const int N = s.N;
+  T32 nrm = {normtab, n0, nf};
+  uint32_t kp0, kp1, kq0, kq1;
+  src_keys(cfg, ipop, &kp0, &kp1, &kq0, &kq1);
+  const float rlim = (float)(cfg->l_box / 2 + 20.);
+  const double dxd = cfg->l_box / N;
+  const float cvol = (float)(dxd * dxd * dxd);
+  const float fvel = (float)(-cfg->fgrowth_0 / (1.5 * cfg->hubble_0 * cfg->omega_m));
+  const int64_t nsb = cfg->nside_base, nsc = cfg->nside_count[ipop];
+  long long id = 0;
+  for (int iz = 0; iz < N; iz++) {
+    float z0 = cg_cell_coord(iz, s.dx, s.p[2]);
+    for (int iy = 0; iy < N; iy++) {
+      float y0 = cg_cell_coord(iy, s.dx, s.p[1]);
+      for (int ix = 0; ix < N; ix++) {
+        int n = cell_count(cfg, &s, ipop, dens, nrm, ix, iy, iz, rlim, cvol, kp0, kp1);
+        if (n == 0) continue;
+        float x0 = cg_cell_coord(ix, s.dx, s.p[0]);
+        float rr = cg_norm3(x0, y0, z0);
+        int xh = wrapi(ix + 1, N), xl = wrapi(ix - 1, N), yh = wrapi(iy + 1, N), yl = wrapi(iy - 1, N);
+        int zh = wrapi(iz + 1, N), zl = wrapi(iz - 1, N);
+        float v0 = CG_SUB(npot[pidx(xh, iy, iz, N)], npot[pidx(xl, iy, iz, N)]);
+        float v1 = CG_SUB(npot[pidx(ix, yh, iz, N)], npot[pidx(ix, yl, iz, N)]);
+        float v2 = CG_SUB(npot[pidx(ix, iy, zh, N)], npot[pidx(ix, iy, zl, N)]);
+        float rvel = CG_MUL(fvel, cg_rvel(v0, v1, v2, x0, y0, z0, rr, s.idx));
+        float dz = CG_MUL(rvel, bg32(&s, s.v1, rr));
+        long long cid = (long long)ix + (long long)N * ((long long)iy + (long long)N * iz);
+        for (int j = 0; j < n; j++, id++) {
+          if (id >= cap) {
+            s32_free(&s);
+            return -1;
+          }
+          cg_u32x4 u = cg_philox4x32_10((uint32_t)cid, (uint32_t)(cid >> 32), (uint32_t)j, 0u, kq0, kq1);
+          float px = cg_src_offset(x0, s.dx, u.v[0]);
+          float py = cg_src_offset(y0, s.dx, u.v[1]);
+          float pz = cg_src_offset(z0, s.dx, u.v[2]);
+          if (pos4) {
+            pos4[4 * id + 0] = px;
+            pos4[4 * id + 1] = py;
+            pos4[4 * id + 2] = pz;
+            pos4[4 * id + 3] = dz;
+          }
+          float r, cth, ph;
+          cg_cart2sph(px, py, pz, &r, &cth, &ph);
+          if (ipix) ipix[id] = (int)cg_ring2nest(nsb, cg_ang2pix_ring(nsb, cth, ph));
+          if (src9) {
+            float *q = src9 + 9 * id;
+            cg_radec(cth, ph, &q[0], &q[1]);
+            q[2] = bg32(&s, s.zt, r);
+            q[3] = cfg->need_beaming ? 0.0f : dz;
+            q[4] = cfg->need_beaming ? 0.0f : -1.0f;
+            q[5] = cfg->need_beaming ? 0.0f : -1.0f;
+            q[6] = q[7] = q[8] = 0.0f;
+          }
+          if (cmap && nsc > 0) cmap[cg_ang2pix_ring(nsc, cth, ph)]++;
+        }
+      }
+    }
+  }
+  *nsrc = id;
+  s32_free(&s);
+  return 0;
+}
+
+static void grad32(const float *phi, int ix, int iy, int iz, int N, float v[3])
+{
+  int xh = wrapi(ix + 1, N), xl = wrapi(ix - 1, N), yh = wrapi(iy + 1, N), yl = wrapi(iy - 1, N);
+  int zh = wrapi(iz + 1, N), zl = wrapi(iz - 1, N);
+  v[0] = CG_SUB(phi[pidx(xh, iy, iz, N)], phi[pidx(xl, iy, iz, N)]);
+  v[1] = CG_SUB(phi[pidx(ix, yh, iz, N)], phi[pidx(ix, yl, iz, N)]);
+  v[2] = CG_SUB(phi[pidx(ix, iy, zh, N)], phi[pidx(ix, iy, zl, N)]);
+}
+
+static float r_of_z32(const S32 *s, float z)
+{
+  float a = CG_DIV(1.0f, CG_ADD(1.0f, z));
+  if (a >= 1.0f) return 0.0f;
+  if (a <= 0.0f) return s->r_a2r[0];
+  float nm1 = (float)(CG_NA - 1);
+  int ia = (int)CG_MUL(a, nm1);
+  return CG_FMA(CG_SUB(s->r_a2r[ia + 1], s->r_a2r[ia]), CG_MUL(CG_SUB(a, s->a_a2r[ia]), nm1), s->r_a2r[ia]);
+}
+
+int or_beam_rsd32(const cg_config *cfg, const float *npot, long long n, const float *pos4, float *src9)
+{
+  S32 s;
+  s32_init(&s, cfg);
+  const int N = s.N;
+  const float fvel = (float)(-cfg->fgrowth_0 / (1.5 * cfg->hubble_0 * cfg->omega_m));
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < n; i++) {
+    const float pos[3] = {pos4[4 * i], pos4[4 * i + 1], pos4[4 * i + 2]};
+    float r = cg_norm3(pos[0], pos[1], pos[2]);
+    float ir = CG_DIV(1.0f, r > 0.001f ? r : 0.001f);
+    float u[3], h0[3], h1[3];
+    int i0[3], i1[3];
+    for (int a = 0; a < 3; a++) {
+      float xn = CG_MUL(CG_ADD(pos[a], s.p[a]), s.idx);
+      u[a] = CG_MUL(pos[a], ir);
+      i0[a] = (int)xn;
+      h0[a] = CG_SUB(xn, (float)i0[a]);
+      h1[a] = CG_SUB(1.0f, h0[a]);
+      i1[a] = wrapi(i0[a] + 1, N);
+      i0[a] = wrapi(i0[a], N);
+    }
+    float v[3] = {0.0f, 0.0f, 0.0f};
+    for (int hz = 0; hz < 2; hz++) {
+      const int zc = hz ? i1[2] : i0[2];
+      const float wz = hz ? h0[2] : h1[2];
+      float acc[3] = {0.0f, 0.0f, 0.0f};
+      for (int k = 0; k < 4; k++) {
+        const int yc = (k & 2) ? i1[1] : i0[1], xc = (k & 1) ? i1[0] : i0[0];
+        const float w = CG_MUL(CG_MUL(wz, (k & 2) ? h0[1] : h1[1]), (k & 1) ? h0[0] : h1[0]);
+        float g[3];
+        grad32(npot, xc, yc, zc, N, g);
+        for (int a = 0; a < 3; a++) acc[a] = CG_FMA(g[a], w, acc[a]);
+      }
+      for (int a = 0; a < 3; a++) v[a] = CG_ADD(v[a], acc[a]);
+    }
+    float vr = CG_MUL(CG_MUL(0.5f, s.idx), CG_ADD(CG_ADD(CG_MUL(v[0], u[0]), CG_MUL(v[1], u[1])), CG_MUL(v[2], u[2])));
+    float *q = src9 + 9 * i;
+    float rz = r_of_z32(&s, q[2]);
+    q[3] = CG_MUL(vr, CG_MUL(bg32(&s, s.v1, rz), fvel));
+  }
+  s32_free(&s);
+  return 0;
+}
+
+static int cmp_float_idx(const void *a, const void *b)
+{
+  const float *x = a, *y = b;
+  return (x[0] < y[0]) ? -1 : (x[0] > y[0] ? 1 : (x[1] < y[1] ? -1 : 1));
+}
+
+int or_imap32(const cg_config *cfg, int ipop, const float *dens, const float *npot, const float *normtab, float n0,
+              float nf, float *data, int *nadd)
+{
+  S32 s;
+  s32_init(&s, cfg);
+  const int N = s.N, nr = cfg->imap_nr[ipop], nside = cfg->nside_imap[ipop];
+  const long long npix = 12LL * nside * nside;
+  /* imap_preproc: shells sorted by r0 (stable in the original order) */
+  float *pr = malloc(2 * nr * sizeof(float)), *r0 = malloc(nr * sizeof(float)), *rf = malloc(nr * sizeof(float));
+  for (int i = 0; i < nr; i++) {
+    pr[2 * i] = (float)cfg->imap_r0[ipop][i];
+    pr[2 * i + 1] = (float)i;
+  }
+  qsort(pr, nr, 2 * sizeof(float), cmp_float_idx);
+  for (int i = 0; i < nr; i++) {
+    int o = (int)pr[2 * i + 1];
+    r0[i] = (float)cfg->imap_r0[ipop][o];
+    rf[i] = (float)cfg->imap_rf[ipop][o];
+  }
+  free(pr);
+  const double dx = cfg->l_box / N, ps = sqrt(4 * M_PI / (double)npix);
+  int *nsub = malloc(nr * sizeof(int));
+  for (int i = 0; i < nr; i++) { /* imap.c:158-172 */
+    double a = r0[i], b = rf[i];
+    double vol = (b * b * b - a * a * a) * ps * ps / 3;
+    double sc0 = fmin(pow(vol, 0.333333), fmin(a * ps, b - a));
+    nsub[i] = (int)(dx / sc0 + 0.5) + 1;
+  }
+  const float rmin = (float)((double)r0[0] - 20.), rmax = (float)((double)rf[nr - 1] + 20.);
+  const float fvel = (float)(-cfg->fgrowth_0 / (1.5 * cfg->hubble_0 * cfg->omega_m));
+  T32 nrm = {normtab, n0, nf};
+  memset(data, 0, (size_t)nr * npix * sizeof(float));
+  memset(nadd, 0, (size_t)nr * npix * sizeof(int));
+  for (int iz = 0; iz < N; iz++) {
+    float z0 = cg_cell_coord(iz, s.dx, s.p[2]);
+    for (int iy = 0; iy < N; iy++) {
+      float y0 = cg_cell_coord(iy, s.dx, s.p[1]);
+      for (int ix = 0; ix < N; ix++) {
+        float x0 = cg_cell_coord(ix, s.dx, s.p[0]);
+        float rc = cg_norm3(x0, y0, z0);
+        float tmean = bg32(&s, s.tz[ipop], rc);
+        if (!(rc <= rmax && rc >= rmin && tmean > 0.0f)) continue;
+        float bias = bg32(&s, s.bzi[ipop], rc), dnorm = bg32(&s, nrm, rc);
+        float v[3];
+        grad32(npot, ix, iy, iz, N, v);
+        float rvel = CG_MUL(fvel, cg_rvel(v[0], v[1], v[2], x0, y0, z0, rc, s.idx));
+        float drr = cg_imap_drsd(rvel, bg32(&s, s.v1, rc), bg32(&s, s.ih, rc));
+        float temp = cg_imap_temp(tmean, dens[pidx(ix, iy, iz, N)], bias, dnorm, cfg->bias_model);
+        int ir0 = cg_shell_index(r0, rf, nr, rc, 0);
+        int ns = ir0 < 0 ? nsub[0] : (ir0 >= nr ? nsub[nr - 1] : nsub[ir0]);
+        float dxs = CG_DIV(s.dx, (float)ns);
+        for (int izz = 0; izz < ns; izz++) {
+          float zc = cg_sub_centre(z0, izz, dxs);
+          for (int iyy = 0; iyy < ns; iyy++) {
+            float yc = cg_sub_centre(y0, iyy, dxs);
+            for (int ixx = 0; ixx < ns; ixx++) {
+              float xc = cg_sub_centre(x0, ixx, dxs);
+              float r, cth, ph;
+              cg_cart2sph(xc, yc, zc, &r, &cth, &ph);
+              int ir = cg_shell_index(r0, rf, nr, CG_ADD(r, drr), ir0);
+              if (ir >= 0 && ir < nr) {
+                long long k = (long long)ir * npix + cg_ang2pix_ring(nside, cth, ph);
+                data[k] += temp;
+                nadd[k]++;
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  free(r0);
+  free(rf);
+  free(nsub);
+  s32_free(&s);
+  return 0;
+}
+
+static int cmp_float(const void *a, const void *b)
+{
+  float x = *(const float *)a, y = *(const float *)b;
+  return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+static double bg64(const cg_config *c, const double *f, double f0, double ff, double r)
+{
+  if (r <= 0) return f0;
+  if (r >= c->r_arr_r2z[CG_NA - 1]) return ff;
+  int ir = (int)(r * c->glob_idr);
+  return f[ir] + (f[ir + 1] - f[ir]) * (r - c->r_arr_r2z[ir]) * c->glob_idr;
+}
+
+int or_kappa32(const cg_config *cfg, const float *npot, float *map)
+{
+  S32 s;
+  s32_init(&s, cfg);
+  const int N = s.N, np = cfg->n_kappa, nside = cfg->nside_kappa;
+  const long long npix = 12LL * nside * nside;
+  const int nr = N / 2;
+  const double dr = cfg->r_max / nr, idr = 1. / dr;
+  float *rp = malloc(np * sizeof(float));
+  for (int i = 0; i < np; i++) rp[i] = (float)cfg->kappa_r[i];
+  qsort(rp, np, sizeof(float), cmp_float);
+  int *irmin = malloc(np * sizeof(int)), *irmax = malloc(np * sizeof(int));
+  float *inv = malloc(np * sizeof(float)), *f1 = malloc(nr * sizeof(float)), *f2 = malloc(nr * sizeof(float));
+  for (int i = 0; i < np; i++) {
+    int irh = (int)((double)rp[i] * idr + 0.5);
+    inv[i] = (float)(1. / (irh * dr));
+    irmax[i] = irh < nr - 1 ? irh : nr - 1;
+  }
+  irmin[0] = 0;
+  for (int i = 1; i < np; i++) irmin[i] = irmax[i - 1] + 1;
+  for (int i = 0; i < nr; i++) {
+    double rm = (i + 0.5) * dr;
+    double pg = bg64(cfg, cfg->growth_d_arr, 1, cfg->growth_d_arr[CG_NA - 1], rm) *
+                (1 + bg64(cfg, cfg->z_arr_r2z, 0, cfg->z_arr_r2z[CG_NA - 1], rm));
+    f1[i] = (float)(rm * pg * dr);
+    f2[i] = (float)(rm * rm * pg * dr);
+  }
+  const float drf = (float)dr;
+#pragma omp parallel for schedule(static)
+  for (long long ip = 0; ip < npix; ip++) {
+    float u[3], rot[6];
+    cg_pix2vec_nest(nside, ip, u);
+    cg_kappa_rot(u, CG_MUL(s.idx, s.idx), rot);
+    long long ring = cg_nest2ring(nside, ip);
+    float k1 = 0, k1c = 0, k2 = 0, k2c = 0;
+    for (int pl = 0; pl < np; pl++) {
+      for (int irr = irmin[pl]; irr <= irmax[pl]; irr++) {
+        float rm = CG_MUL(CG_ADD((float)irr, 0.5f), drf);
+        int x0 = cg_ngp_cell(rm, u[0], s.p[0], s.idx, N), y0 = cg_ngp_cell(rm, u[1], s.p[1], s.idx, N),
+            z0 = cg_ngp_cell(rm, u[2], s.p[2], s.idx, N);
+        int xh = wrapi(x0 + 1, N), xl = wrapi(x0 - 1, N), yh = wrapi(y0 + 1, N), yl = wrapi(y0 - 1, N);
+        int zh = wrapi(z0 + 1, N), zl = wrapi(z0 - 1, N);
+#define PHI(X, Y, Z) npot[pidx((X), (Y), (Z), N)]
+        const float f[19] = {PHI(x0, y0, z0), PHI(xh, y0, z0), PHI(xl, y0, z0), PHI(x0, yh, z0), PHI(x0, yl, z0),
+                             PHI(x0, y0, zh), PHI(x0, y0, zl), PHI(xh, yh, z0), PHI(xl, yl, z0), PHI(xh, yl, z0),
+                             PHI(xl, yh, z0), PHI(xh, y0, zh), PHI(xl, y0, zl), PHI(xh, y0, zl), PHI(xl, y0, zh),
+                             PHI(x0, yh, zh), PHI(x0, yl, zl), PHI(x0, yh, zl), PHI(x0, yl, zh)};
+#undef PHI
+        float t[6];
+        cg_tidal(f, t);
+        float dot = cg_dot6(rot, t);
+        cg_kahan_add(&k1, &k1c, CG_MUL(dot, f1[irr]));
+        cg_kahan_add(&k2, &k2c, CG_MUL(dot, f2[irr]));
+      }
+      map[(long long)pl * npix + ring] = CG_SUB(k1, CG_MUL(inv[pl], k2));
+    }
+  }
+  free(rp);
+  free(irmin);
+  free(irmax);
+  free(inv);
+  free(f1);
+  free(f2);
+  s32_free(&s);
+  return 0;
+}

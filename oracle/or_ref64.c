@@ -1,0 +1,615 @@
+/*
+ * or_ref64.c -- ORACLE (test infrastructure only).  The reference's hot path
+ * restated in double precision with libm, loop by loop; the tolerance
+ * oracle for every floating-point output and the timed CPU baseline.
+ *
+ *   or_fill64        create_grids_fourier          fourier.c:285-359
+ *   or_field64       create_cartesian_fields       fourier.c:361-423 (+ compute_sigma_dens 24-79)
+ *   or_density64     lognormalize / densclip       density.c:1034-1103
+ *   or_lpt64         lpt_1 + pos_2_cic             density.c:376-644, 64-105 (literal r2c path)
+ *   or_bins64        collect_density_normalization_from_grid density.c:1128-1211
+ *   or_norm_tables64 compute_density_normalization density.c:1227-1355
+ *   or_lambda64      Poisson mean per cell         srcs.c:156-178
+ *   or_imap64        imap_set_cartesian_single     imap.c:135-245
+ *   or_kappa64       kappa_get_beam_properties     kappa.c:78-175
+ *   or_run_mock64    the driver sequence of main.c:66-125 for timing.
+ * Random numbers: the Philox streams of the GPU path (uniforms identical
+ * bit for bit), since GSL's MT19937 streams cannot be reproduced here.
+ */
+#include <complex.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../colore_gb300/csrc/cg_cell.h"
+#include "oracle.h"
+
+static double bg(const cg_config *c, const double *f, double f0, double ff, double r) /* cosmo.c:30-38 */
+{
+  if (r <= 0) return f0;
+  if (r >= c->r_arr_r2z[CG_NA - 1]) return ff;
+  int ir = (int)(r * c->glob_idr);
+  return f[ir] + (f[ir + 1] - f[ir]) * (r - c->r_arr_r2z[ir]) * c->glob_idr;
+}
+#define BG_Z(c, r) bg((c), (c)->z_arr_r2z, 0, (c)->z_arr_r2z[CG_NA - 1], (r))
+#define BG_D1(c, r) bg((c), (c)->growth_d_arr, 1, (c)->growth_d_arr[CG_NA - 1], (r))
+#define BG_V1(c, r) bg((c), (c)->growth_v_arr, (c)->growth_v_arr[0], (c)->growth_v_arr[CG_NA - 1], (r))
+#define BG_IH(c, r) bg((c), (c)->ihub_arr, (c)->ihub_arr[0], (c)->ihub_arr[CG_NA - 1], (r))
+
+static double bias_model64(double d, double b, int model) /* common.h:414-431 */
+{
+  if (d <= -1) return 0;
+  if (model == CG_BIAS_MODEL_EXPLIN) return d < 0 ? exp(b * d / (1 + d)) : 1 + b * d;
+  if (model == CG_BIAS_MODEL_LIN) return 1 + b * d > 0 ? 1 + b * d : 0;
+  return pow(1 + d, b);
+}
+
+static double pk_lin0(const cg_config *c, double lgk) /* cosmo.c:291-308, guarded at numk-1 */
+{
+  int ik = (int)((lgk - c->logkmin) * c->idlogk);
+  if (ik < 0) return c->pkarr[0] * pow(10, c->n_scal * (lgk - c->logkmin));
+  if (ik < c->numk - 1) {
+    double lk = c->logkmin + ik / c->idlogk;
+    return c->pkarr[ik] + (lgk - lk) * (c->pkarr[ik + 1] - c->pkarr[ik]) * c->idlogk;
+  }
+  return c->pkarr[c->numk - 1] * pow(10, -3 * (lgk - c->logkmax));
+}
+
+static double kc(int i, int n, double dk) { return (2 * i <= n ? i : -(n - i)) * dk; }
+
+int or_fill64(const cg_config *c, double complex *dk, double complex *pk)
+{
+  const int N = c->n_grid, NH = N / 2 + 1;
+  const double dkk = 2 * M_PI / c->l_box, idk3 = 1. / (dkk * dkk * dkk);
+  const uint32_t k0 = (uint32_t)c->seed, k1 = (uint32_t)(c->seed >> 32) ^ CG_STREAM_FIELD;
+#pragma omp parallel for schedule(static)
+  for (int kz = 0; kz < N; kz++) {
+    double z = kc(kz, N, dkk);
+    for (int ky = 0; ky < N; ky++) {
+      double y = kc(ky, N, dkk);
+      for (int kx = 0; kx <= N / 2; kx++) {
+        double x = kx * dkk;
+        size_t idx = kx + (size_t)NH * (ky + (size_t)N * kz);
+        double k2 = x * x + y * y + z * z;
+        if (k2 <= 0) {
+          dk[idx] = 0;
+          if (pk) pk[idx] = 0;
+          continue;
+        }
+        double lgk = 0.5 * log10(k2);
+        double s2 = pk_lin0(c, lgk) * idk3;
+        uint64_t m = (uint64_t)idx;
+        cg_u32x4 w = cg_philox4x32_10((uint32_t)m, (uint32_t)(m >> 32), 0u, 0u, k0, k1);
+        double ph = 2 * M_PI * (double)cg_u01f(w.v[0]);
+        double u = cg_u01f(w.v[1]);
+        double mod = sqrt(-s2 * log(1 - u)); /* rng_delta_gauss, common.c:191-201 */
+        double complex d = mod * cexp(I * ph);
+        double complex p = -c->prefac_lensing * d / k2;
+        if (c->do_smoothing) {
+          double sm = exp(-0.5 * c->r2_smooth * k2);
+          d *= sm;
+          if (c->smooth_potential) p *= sm;
+        }
+        dk[idx] = d;
+        if (pk) pk[idx] = p;
+      }
+    }
+  }
+  return 0;
+}
+
+int or_field64(const cg_config *c, double *dens, double *npot, double stats[4])
+{
+  const int N = c->n_grid, NH = N / 2 + 1;
+  const size_t nh = (size_t)N * N * NH, ncell = (size_t)N * N * N;
+  double complex *dk = malloc(nh * sizeof(double complex)), *pk = malloc(nh * sizeof(double complex));
+  if (!dk || !pk) return -1;
+  or_fill64(c, dk, pk);
+  or_c2r_3d(N, dk, dens);
+  or_c2r_3d(N, pk, npot);
+  free(dk);
+  free(pk);
+  const double norm = pow(sqrt(2 * M_PI) / c->l_box, 3);
+  double s1 = 0, s2 = 0;
+#pragma omp parallel for schedule(static) reduction(+ : s1, s2)
+  for (size_t i = 0; i < ncell; i++) {
+    dens[i] *= norm;
+    npot[i] *= norm;
+    s1 += dens[i];
+    s2 += dens[i] * dens[i];
+  }
+  double mean = s1 / ncell, sig2 = s2 / ncell - mean * mean;
+  stats[0] = s1;
+  stats[1] = s2;
+  stats[2] = mean;
+  stats[3] = sig2;
+  return 0;
+}
+
+int or_density64(const cg_config *c, double *dens, double sigma2)
+{
+  const int N = c->n_grid;
+  const double dx = c->l_box / N;
+#pragma omp parallel for schedule(static)
+  for (int iz = 0; iz < N; iz++) {
+    double z0 = iz * dx - c->pos_obs[2];
+    for (int iy = 0; iy < N; iy++) {
+      double y0 = iy * dx - c->pos_obs[1];
+      for (int ix = 0; ix < N; ix++) {
+        double x0 = ix * dx - c->pos_obs[0];
+        double r = sqrt(x0 * x0 + y0 * y0 + z0 * z0);
+        double dg = BG_D1(c, r);
+        size_t id = ix + (size_t)N * (iy + (size_t)N * iz);
+        double d = dens[id];
+        if (c->dens_type == CG_DENS_CLIP) dens[id] = fmax(1 + dg * d, 0) - 1;
+        else dens[id] = exp(dg * (d - 0.5 * dg * sigma2)) - 1;
+      }
+    }
+  }
+  return 0;
+}
+
+int or_lpt64(const cg_config *c, const double *dg_in, double *dens_out, double *disp)
+{
+  const int N = c->n_grid, NH = N / 2 + 1;
+  const size_t nh = (size_t)N * N * NH, ncell = (size_t)N * N * N;
+  double complex *dk = malloc(nh * sizeof(double complex)), *ck = malloc(nh * sizeof(double complex));
+  if (!dk || !ck) return -1;
+  or_r2c_3d(N, dg_in, dk); /* density.c:392 */
+  const double dkk = 2 * M_PI / c->l_box, fftnorm = (double)N * N * N;
+  for (int ax = 0; ax < 3; ax++) { /* density.c:408-440 */
+#pragma omp parallel for schedule(static)
+    for (int kz = 0; kz < N; kz++)
+      for (int ky = 0; ky < N; ky++)
+        for (int kx = 0; kx <= N / 2; kx++) {
+          double kv[3] = {kx * dkk, kc(ky, N, dkk), kc(kz, N, dkk)};
+          double k2 = fftnorm * (kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2]);
+          size_t idx = kx + (size_t)NH * (ky + (size_t)N * kz);
+          ck[idx] = k2 <= 0 ? 0 : I * kv[ax] * dk[idx] / k2;
+        }
+    or_c2r_3d(N, ck, disp + (size_t)ax * ncell);
+  }
+  free(dk);
+  free(ck);
+  const double dx = c->l_box / N;
+  memset(dens_out, 0, ncell * sizeof(double));
+  /* positions (density.c:473-501) and CIC (density.c:64-105) */
+  const double iag = N / c->l_box;
+  for (int iz = 0; iz < N; iz++)
+    for (int iy = 0; iy < N; iy++)
+      for (int ix = 0; ix < N; ix++) {
+        double xv[3] = {ix * dx - c->pos_obs[0], iy * dx - c->pos_obs[1], iz * dx - c->pos_obs[2]};
+        double r = sqrt(xv[0] * xv[0] + xv[1] * xv[1] + xv[2] * xv[2]);
+        double g = BG_D1(c, r);
+        size_t id = ix + (size_t)N * (iy + (size_t)N * iz);
+        int i0[3], i1[3];
+        double a0[3], a1[3];
+        for (int ax = 0; ax < 3; ax++) {
+          double p = xv[ax] + g * disp[(size_t)ax * ncell + id] + c->pos_obs[ax];
+          if (p < 0) p += c->l_box;
+          if (p >= c->l_box) p -= c->l_box;
+          i0[ax] = (int)(p * iag);
+          a1[ax] = p * iag - i0[ax];
+          a0[ax] = 1 - a1[ax];
+          i1[ax] = i0[ax] + 1;
+          if (i0[ax] >= N) i0[ax] -= N;
+          if (i1[ax] >= N) i1[ax] -= N;
+        }
+#define D(X, Y, Z) dens_out[(X) + (size_t)N * ((Y) + (size_t)N * (Z))]
+        D(i0[0], i0[1], i0[2]) += a0[0] * a0[1] * a0[2];
+        D(i1[0], i0[1], i0[2]) += a1[0] * a0[1] * a0[2];
+        D(i0[0], i1[1], i0[2]) += a0[0] * a1[1] * a0[2];
+        D(i1[0], i1[1], i0[2]) += a1[0] * a1[1] * a0[2];
+        D(i0[0], i0[1], i1[2]) += a0[0] * a0[1] * a1[2];
+        D(i1[0], i0[1], i1[2]) += a1[0] * a0[1] * a1[2];
+        D(i0[0], i1[1], i1[2]) += a0[0] * a1[1] * a1[2];
+        D(i1[0], i1[1], i1[2]) += a1[0] * a1[1] * a1[2];
+#undef D
+      }
+  for (size_t i = 0; i < ncell; i++) dens_out[i] -= 1; /* density.c:621 */
+  return 0;
+}
+
+int or_bins64(const cg_config *c, const double *dens, int nz, double idz, unsigned long long *narr, double *zarr,
+              double *bsum)
+{
+  const int N = c->n_grid, nts = c->n_srcs, nt = nts + c->n_imap;
+  const double dx = c->l_box / N;
+  memset(narr, 0, nz * sizeof(unsigned long long));
+  memset(zarr, 0, nz * sizeof(double));
+  memset(bsum, 0, (size_t)nt * nz * sizeof(double));
+  for (int iz = 0; iz < N; iz++) {
+    double z0 = iz * dx - c->pos_obs[2];
+    for (int iy = 0; iy < N; iy++) {
+      double y0 = iy * dx - c->pos_obs[1];
+      for (int ix = 0; ix < N; ix++) {
+        double x0 = ix * dx - c->pos_obs[0];
+        double r = sqrt(x0 * x0 + y0 * y0 + z0 * z0);
+        double z = BG_Z(c, r);
+        int b = (int)(z * idz) + 1;
+        if (b < 0 || b >= nz) continue;
+        double d = dens[ix + (size_t)N * (iy + (size_t)N * iz)];
+        narr[b]++;
+        zarr[b] += z;
+        for (int t = 0; t < nt; t++) {
+          const double *bt = t < nts ? c->srcs_bz_arr[t] : c->imap_bz_arr[t - nts];
+          bsum[(size_t)t * nz + b] += bias_model64(d, bg(c, bt, bt[0], 1, r), c->bias_model);
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+int or_norm_tables64(const cg_config *c, double *tabs, double *e0f, int *nz_out, unsigned long long *narr,
+                     double *zarr, double *bsum, const double *dens)
+{
+  const int nt = c->n_srcs + c->n_imap;
+  double zmax = BG_Z(c, c->l_box * 0.5);
+  int nz = (int)(zmax / 0.05) + 2;
+  double idz = (nz - 2) / zmax;
+  if (nz_out) *nz_out = nz;
+  if (dens) or_bins64(c, dens, nz, idz, narr, zarr, bsum);
+  double *zz = malloc(nz * sizeof(double)), *y = malloc((size_t)nt * nz * sizeof(double));
+  memcpy(zz, zarr, nz * sizeof(double));
+  memcpy(y, bsum, (size_t)nt * nz * sizeof(double));
+  for (int iz = 0; iz < nz; iz++)
+    if (narr[iz] > 0) {
+      zz[iz] /= narr[iz];
+      for (int t = 0; t < nt; t++) y[(size_t)t * nz + iz] = narr[iz] / y[(size_t)t * nz + iz];
+    }
+  zz[0] = 0;
+  zz[nz - 1] = BG_Z(c, 0.5 * c->l_box);
+  for (int t = 0; t < nt; t++) {
+    y[(size_t)t * nz] = y[(size_t)t * nz + 1];
+    y[(size_t)t * nz + nz - 1] = y[(size_t)t * nz + nz - 2];
+    e0f[2 * t] = y[(size_t)t * nz];
+    e0f[2 * t + 1] = y[(size_t)t * nz + nz - 1];
+    for (int i = 0; i < CG_NA; i++) {
+      double z = BG_Z(c, c->r_arr_r2z[i]), nm;
+      const double *yt = y + (size_t)t * nz;
+      if (z < zz[0]) nm = yt[0];
+      else if (z >= zz[nz - 1]) nm = yt[nz - 1];
+      else {
+        int lo = 0, hi = nz - 1;
+        while (hi > lo + 1) {
+          int mid = (lo + hi) / 2;
+          if (zz[mid] > z) hi = mid;
+          else lo = mid;
+        }
+        nm = yt[lo] + (z - zz[lo]) * (yt[hi] - yt[lo]) / (zz[hi] - zz[lo]);
+      }
+      tabs[(size_t)t * CG_NA + i] = nm;
+    }
+  }
+  free(zz);
+  free(y);
+  return 0;
+}
+
+int or_lambda64(const cg_config *c, int ipop, const double *dens, const double *nt_, double n0, double nf,
+                double *lambda)
+{
+  const int N = c->n_grid;
+  const double dx = c->l_box / N, cv = dx * dx * dx;
+  const double *nzt = c->srcs_nz_arr[ipop], *bzt = c->srcs_bz_arr[ipop];
+#pragma omp parallel for schedule(static)
+  for (int iz = 0; iz < N; iz++) {
+    double z0 = iz * dx - c->pos_obs[2];
+    for (int iy = 0; iy < N; iy++) {
+      double y0 = iy * dx - c->pos_obs[1];
+      for (int ix = 0; ix < N; ix++) {
+        double x0 = ix * dx - c->pos_obs[0];
+        double r = sqrt(x0 * x0 + y0 * y0 + z0 * z0);
+        size_t id = ix + (size_t)N * (iy + (size_t)N * iz);
+        double lam = 0;
+        if (r < c->l_box / 2 + 20.) {
+          double nd = bg(c, nzt, 0, 0, r);
+          if (nd > 0)
+            lam = nd * cv * bias_model64(dens[id], bg(c, bzt, bzt[0], 1, r), c->bias_model) * bg(c, nt_, n0, nf, r);
+        }
+        lambda[id] = lam;
+      }
+    }
+  }
+  return 0;
+}
+
+/* he_ang2pix in double, healpix_extra.c:118-172 */
+static long ang2pix64(long nside, double cth, double phi)
+{
+  double ctha = fabs(cth), tp2 = 2 * M_PI;
+  double ph = phi >= 0 ? (phi < tp2 ? phi : fmod(phi, tp2)) : fmod(phi, tp2) + tp2;
+  if (ph == tp2) ph = 0;
+  double tt = ph * (2 / M_PI);
+  if (ctha <= 2. / 3.) {
+    double t1 = nside * (0.5 + tt), t2 = nside * cth * 0.75;
+    int jp = (int)(t1 - t2), jm = (int)(t1 + t2);
+    int ir = nside + 1 + jp - jm, ks = 1 - (ir & 1);
+    int ip = (jp + jm - nside + ks + 1) / 2;
+    ip %= 4 * nside;
+    if (ip < 0) ip += 4 * nside;
+    return nside * (nside - 1) * 2 + (ir - 1) * 4 * nside + ip;
+  }
+  double tp = tt - (int)tt, tmp = nside * sqrt(3 * (1 - ctha));
+  int jp = (int)(tp * tmp), jm = (int)((1.0 - tp) * tmp), ir = jp + jm + 1;
+  int ip = (int)(tt * ir);
+  ip %= 4 * ir;
+  if (ip < 0) ip += 4 * ir;
+  return cth > 0 ? 2 * ir * (ir - 1) + ip : 12 * nside * nside - 2 * ir * (ir + 1) + ip;
+}
+
+static void cart2sph64(double x, double y, double z, double *r, double *cth, double *phi)
+{
+  *r = sqrt(x * x + y * y + z * z);
+  if (*r == 0) {
+    *cth = 1;
+    *phi = 0;
+    return;
+  }
+  *cth = z / *r;
+  *phi = atan2(y / *r, x / *r);
+  if (*phi < 0) *phi += 2 * M_PI;
+}
+
+static double rvel64(const cg_config *c, const double *p, int ix, int iy, int iz, double x0, double y0, double z0,
+                     double rr)
+{
+  const int N = c->n_grid;
+#define P(X, Y, Z) p[(X) + (size_t)N * ((Y) + (size_t)N * (Z))]
+  int xh = (ix + 1) % N, xl = (ix + N - 1) % N, yh = (iy + 1) % N, yl = (iy + N - 1) % N, zh = (iz + 1) % N,
+      zl = (iz + N - 1) % N;
+  double v0 = P(xh, iy, iz) - P(xl, iy, iz), v1 = P(ix, yh, iz) - P(ix, yl, iz), v2 = P(ix, iy, zh) - P(ix, iy, zl);
+#undef P
+  return 0.5 * (N / c->l_box) * (v0 * x0 / rr + v1 * y0 / rr + v2 * z0 / rr);
+}
+
+int or_imap64(const cg_config *c, int ipop, const double *dens, const double *npot, const double *nrm, double n0,
+              double nf, double *data, int *nadd)
+{
+  const int N = c->n_grid, nr = c->imap_nr[ipop], nside = c->nside_imap[ipop];
+  const long npix = 12L * nside * nside;
+  double *r0 = malloc(nr * sizeof(double)), *rf = malloc(nr * sizeof(double));
+  int *ns = malloc(nr * sizeof(int)), *ord = malloc(nr * sizeof(int));
+  for (int i = 0; i < nr; i++) ord[i] = i;
+  for (int i = 1; i < nr; i++) /* insertion sort by r0 (stable) */
+    for (int j = i; j > 0 && c->imap_r0[ipop][ord[j]] < c->imap_r0[ipop][ord[j - 1]]; j--) {
+      int t = ord[j];
+      ord[j] = ord[j - 1];
+      ord[j - 1] = t;
+    }
+  for (int i = 0; i < nr; i++) {
+    r0[i] = c->imap_r0[ipop][ord[i]];
+    rf[i] = c->imap_rf[ipop][ord[i]];
+  }
+  const double dx = c->l_box / N, ps = sqrt(4 * M_PI / npix);
+  for (int i = 0; i < nr; i++) {
+    double vol = (rf[i] * rf[i] * rf[i] - r0[i] * r0[i] * r0[i]) * ps * ps / 3;
+    ns[i] = (int)(dx / fmin(pow(vol, 0.333333), fmin(r0[i] * ps, rf[i] - r0[i])) + 0.5) + 1;
+  }
+  const double rmin = r0[0] - 20., rmax = rf[nr - 1] + 20.;
+  const double fvel = -c->fgrowth_0 / (1.5 * c->hubble_0 * c->omega_m);
+  memset(data, 0, (size_t)nr * npix * sizeof(double));
+  memset(nadd, 0, (size_t)nr * npix * sizeof(int));
+  const double *tz = c->imap_tz_arr[ipop], *bz = c->imap_bz_arr[ipop];
+  for (int iz = 0; iz < N; iz++) {
+    int irad = 0;
+    double z0 = iz * dx - c->pos_obs[2];
+    for (int iy = 0; iy < N; iy++) {
+      double y0 = iy * dx - c->pos_obs[1];
+      for (int ix = 0; ix < N; ix++) {
+        double x0 = ix * dx - c->pos_obs[0];
+        double rc = sqrt(x0 * x0 + y0 * y0 + z0 * z0);
+        double tm = bg(c, tz, 0, 0, rc);
+        if (!(rc <= rmax && rc >= rmin && tm > 0)) continue;
+        double b = bg(c, bz, bz[0], 1, rc), dn = bg(c, nrm, n0, nf, rc);
+        double rv = fvel * rvel64(c, npot, ix, iy, iz, x0, y0, z0, rc);
+        double drr = rv * BG_V1(c, rc) * BG_IH(c, rc);
+        size_t id = ix + (size_t)N * (iy + (size_t)N * iz);
+        double temp = tm * bias_model64(dens[id], b, c->bias_model) * dn;
+        /* get_r_index_imap walk (imap.c:76-103), bounded */
+#define WALK(R, START)                                                   \
+  ({                                                                     \
+    int q = (START) < 0 ? 0 : ((START) >= nr ? nr - 1 : (START));        \
+    for (int it = 0; it < 2 * nr + 4; it++) {                           \
+      if (q == -1 || q == nr) break;                                     \
+      if ((R) < r0[q]) q--;                                              \
+      else if ((R) >= rf[q]) q++;                                        \
+      else break;                                                        \
+    }                                                                    \
+    q;                                                                   \
+  })
+        irad = WALK(rc, irad);
+        int nsh = irad < 0 ? ns[0] : (irad >= nr ? ns[nr - 1] : ns[irad]);
+        double dxs = dx / nsh;
+        for (int izz = 0; izz < nsh; izz++)
+          for (int iyy = 0; iyy < nsh; iyy++)
+            for (int ixx = 0; ixx < nsh; ixx++) {
+              double r, cth, ph;
+              cart2sph64(x0 + (ixx + 0.5) * dxs, y0 + (iyy + 0.5) * dxs, z0 + (izz + 0.5) * dxs, &r, &cth, &ph);
+              irad = WALK(r + drr, irad);
+              if (irad >= 0 && irad < nr) {
+                long k = irad * npix + ang2pix64(nside, cth, ph);
+                data[k] += temp;
+                nadd[k]++;
+              }
+            }
+#undef WALK
+      }
+    }
+  }
+  free(r0);
+  free(rf);
+  free(ns);
+  free(ord);
+  return 0;
+}
+
+static void pix2vec_nest64(long nside, long ip, double v[3])
+{
+  int64_t jr, jp, nr, ks;
+  cg_nest_ringpos(nside, ip, &jr, &jp, &nr, &ks);
+  double fact2 = 4.0 / (12.0 * nside * nside), z;
+  if (jr < nside) z = 1 - nr * nr * fact2;
+  else if (jr > 3 * nside) z = nr * nr * fact2 - 1;
+  else z = (2 * nside - jr) * 2.0 / (3.0 * nside);
+  double phi = (jp - (ks + 1) * 0.5) * (M_PI / 2) / nr;
+  double sth = sqrt((1 - z) * (1 + z));
+  v[0] = sth * cos(phi);
+  v[1] = sth * sin(phi);
+  v[2] = z;
+}
+
+int or_kappa64(const cg_config *c, const double *p, double *map)
+{
+  const int N = c->n_grid, np = c->n_kappa, nside = c->nside_kappa;
+  const long npix = 12L * nside * nside;
+  const int nr = N / 2;
+  const double dr = c->r_max / nr, idr = 1. / dr, idx = N / c->l_box;
+  double rp[CG_NPLANES_MAX];
+  for (int i = 0; i < np; i++) rp[i] = (float)c->kappa_r[i]; /* stored as flouble */
+  for (int i = 1; i < np; i++)
+    for (int j = i; j > 0 && rp[j] < rp[j - 1]; j--) {
+      double t = rp[j];
+      rp[j] = rp[j - 1];
+      rp[j - 1] = t;
+    }
+  int irmin[CG_NPLANES_MAX], irmax[CG_NPLANES_MAX];
+  double inv[CG_NPLANES_MAX];
+  for (int i = 0; i < np; i++) {
+    int irh = (int)(rp[i] * idr + 0.5);
+    inv[i] = 1. / (irh * dr);
+    irmax[i] = irh < nr - 1 ? irh : nr - 1;
+  }
+  irmin[0] = 0;
+  for (int i = 1; i < np; i++) irmin[i] = irmax[i - 1] + 1;
+  double *f1 = malloc(nr * sizeof(double)), *f2 = malloc(nr * sizeof(double));
+  for (int i = 0; i < nr; i++) {
+    double rm = (i + 0.5) * dr, pg = BG_D1(c, rm) * (1 + BG_Z(c, rm));
+    f1[i] = rm * pg * dr;
+    f2[i] = rm * rm * pg * dr;
+  }
+#pragma omp parallel for schedule(static)
+  for (long ip = 0; ip < npix; ip++) {
+    double u[3];
+    pix2vec_nest64(nside, ip, u);
+    double cth = u[2] > 1 ? 1 : (u[2] < -1 ? -1 : u[2]), sth = sqrt((1 - cth) * (1 + cth)), cph = 1, sph = 0;
+    if (sth != 0) {
+      cph = u[0] / sth;
+      sph = u[1] / sth;
+    }
+    double pf = idx * idx, rot[6] = {(cth * cth * cph * cph + sph * sph) * pf, (2 * cph * sph * (cth * cth - 1)) * pf,
+                                     (-2 * cth * sth * cph) * pf,            (cth * cth * sph * sph + cph * cph) * pf,
+                                     (-2 * cth * sth * sph) * pf,            (sth * sth) * pf};
+    long ring = cg_nest2ring(nside, ip);
+    double k1 = 0, k2 = 0;
+    for (int pl = 0; pl < np; pl++) {
+      for (int irr = irmin[pl]; irr <= irmax[pl]; irr++) {
+        double rm = (irr + 0.5) * dr;
+        int cc[3];
+        for (int a = 0; a < 3; a++) {
+          long q = (long)((rm * u[a] + c->pos_obs[a]) * idx + 0.5);
+          cc[a] = (int)(q >= N ? q - N : (q < 0 ? q + N : q));
+        }
+        int x0 = cc[0], y0 = cc[1], z0 = cc[2];
+        int xh = (x0 + 1) % N, xl = (x0 + N - 1) % N, yh = (y0 + 1) % N, yl = (y0 + N - 1) % N, zh = (z0 + 1) % N,
+            zl = (z0 + N - 1) % N;
+#define P(X, Y, Z) p[(X) + (size_t)N * ((Y) + (size_t)N * (Z))]
+        double t[6];
+        t[0] = P(xh, y0, z0) + P(xl, y0, z0) - 2 * P(x0, y0, z0);
+        t[3] = P(x0, yh, z0) + P(x0, yl, z0) - 2 * P(x0, y0, z0);
+        t[5] = P(x0, y0, zh) + P(x0, y0, zl) - 2 * P(x0, y0, z0);
+        t[1] = 0.25 * (P(xh, yh, z0) + P(xl, yl, z0) - P(xh, yl, z0) - P(xl, yh, z0));
+        t[2] = 0.25 * (P(xh, y0, zh) + P(xl, y0, zl) - P(xh, y0, zl) - P(xl, y0, zh));
+        t[4] = 0.25 * (P(x0, yh, zh) + P(x0, yl, zl) - P(x0, yh, zl) - P(x0, yl, zh));
+#undef P
+        double dot = 0;
+        for (int a = 0; a < 6; a++) dot += rot[a] * t[a];
+        k1 += dot * f1[irr];
+        k2 += dot * f2[irr];
+      }
+      map[(long)pl * npix + ring] = k1 - inv[pl] * k2;
+    }
+  }
+  free(f1);
+  free(f2);
+  return 0;
+}
+
+/* Poisson deviate by inversion in double from the same Philox cell stream. */
+static int poisson64(double lam, uint32_t k0, uint32_t k1, long long cid)
+{
+  if (!(lam > 0)) return 0;
+  cg_u32x4 w = cg_philox4x32_10((uint32_t)cid, (uint32_t)(cid >> 32), 0u, 0u, k0, k1);
+  double u = cg_u01d(w.v[0], w.v[1]), p = exp(-lam), F = p;
+  int k = 0;
+  while (u >= F && k < 100000) {
+    k++;
+    p *= lam / k;
+    F += p;
+    if (p == 0 && F < u) break;
+  }
+  return k;
+}
+
+int or_run_mock64(const cg_config *c, int nthreads_hint, long long *nsrc_total, double *checksum)
+{
+  (void)nthreads_hint;
+  const int N = c->n_grid;
+  const size_t ncell = (size_t)N * N * N;
+  double *dens = malloc(ncell * sizeof(double)), *npot = malloc(ncell * sizeof(double));
+  if (!dens || !npot) return -1;
+  double st[4];
+  or_field64(c, dens, npot, st);
+  if (c->dens_type == CG_DENS_1LPT) {
+    double *d2 = malloc(ncell * sizeof(double)), *disp = malloc(3 * ncell * sizeof(double));
+    or_lpt64(c, dens, d2, disp);
+    memcpy(dens, d2, ncell * sizeof(double));
+    free(d2);
+    free(disp);
+  } else {
+    or_density64(c, dens, st[3]);
+  }
+  const int nt = c->n_srcs + c->n_imap;
+  double *tabs = malloc((size_t)(nt > 0 ? nt : 1) * CG_NA * sizeof(double)), e0f[2 * 2 * CG_NPOP_MAX];
+  unsigned long long narr[4096];
+  double zarr[4096], *bsum = malloc((size_t)(nt > 0 ? nt : 1) * 4096 * sizeof(double));
+  int nz;
+  or_norm_tables64(c, tabs, e0f, &nz, narr, zarr, bsum, dens);
+  double cs = 0;
+  long long tot = 0;
+  double *lam = malloc(ncell * sizeof(double));
+  for (int p = 0; p < c->n_srcs; p++) {
+    or_lambda64(c, p, dens, tabs + (size_t)p * CG_NA, e0f[2 * p], e0f[2 * p + 1], lam);
+    const uint32_t k0 = (uint32_t)c->seed, k1 = (uint32_t)(c->seed >> 32) ^ (CG_STREAM_POIS + (uint32_t)p);
+    long long t = 0;
+#pragma omp parallel for schedule(static) reduction(+ : t)
+    for (size_t i = 0; i < ncell; i++) t += poisson64(lam[i], k0, k1, (long long)i);
+    tot += t;
+  }
+  free(lam);
+  for (int p = 0; p < c->n_imap; p++) {
+    long npix = 12L * c->nside_imap[p] * c->nside_imap[p];
+    double *data = malloc((size_t)c->imap_nr[p] * npix * sizeof(double));
+    int *nadd = malloc((size_t)c->imap_nr[p] * npix * sizeof(int));
+    or_imap64(c, p, dens, npot, tabs + (size_t)(c->n_srcs + p) * CG_NA, e0f[2 * (c->n_srcs + p)],
+              e0f[2 * (c->n_srcs + p) + 1], data, nadd);
+    for (long i = 0; i < (long)c->imap_nr[p] * npix; i++) cs += nadd[i];
+    free(data);
+    free(nadd);
+  }
+  if (c->do_kappa) {
+    long npix = 12L * c->nside_kappa * c->nside_kappa;
+    double *map = malloc((size_t)c->n_kappa * npix * sizeof(double));
+    or_kappa64(c, npot, map);
+    for (long i = 0; i < (long)c->n_kappa * npix; i++) cs += map[i];
+    free(map);
+  }
+  free(tabs);
+  free(bsum);
+  free(dens);
+  free(npot);
+  if (nsrc_total) *nsrc_total = tot;
+  if (checksum) *checksum = cs + st[3];
+  return 0;
+}

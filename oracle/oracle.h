@@ -1,0 +1,66 @@
+/*
+ * oracle.h -- ORACLE: CPU restatement of CoLoRe's mock-generation path.
+ *
+ * Test infrastructure only.  Nothing in the product (colore_gb300/,
+ * include/) links, imports or calls this code; only tests/, the smoke check
+ * of __graft_entry__.py and the CPU-baseline leg of bench.py do, as the
+ * checker and as the timed CPU reference.
+ *
+ * Two restatements live here:
+ *   ref64 (or_ref64.c): the reference's arithmetic in double precision with
+ *         libm, loop by loop (file:line cited per function).  It is the
+ *         tolerance oracle for floating-point outputs and the CPU baseline.
+ *   dev32 (or_dev32.c): the same loops evaluated with the single-precision
+ *         per-cell arithmetic that the GPU kernels define (cg_cell.h), so
+ *         that integer outputs -- Poisson counts, catalogue order, HEALPix
+ *         pixel ids, hit counts -- can be compared bit for bit.
+ * Real grids passed to dev32 functions use the padded in-place layout of
+ * the GPU (index ix + 2(N/2+1)(iy + N iz)); ref64 grids are unpadded N^3.
+ *
+ * Parity against the reference binary itself is unpinned: the reference
+ * cannot be built here (GSL, FFTW, libconfig, cfitsio, chealpix absent) and
+ * ships no tests or fixtures; see the tests for the known-answer values it
+ * does pin (cosmology from the notebook log, Philox vectors).
+ */
+#ifndef CG_ORACLE_H
+#define CG_ORACLE_H
+
+#include <complex.h>
+#include <stdint.h>
+
+#include "../include/colore_cuda.h"
+
+/* ---- FFT (or_fft.c) ---- */
+int or_c2r_3d(int N, const double complex *in, double *out);
+int or_r2c_3d(int N, const double *in, double complex *out);
+
+/* ---- ref64 (or_ref64.c) ---- */
+int or_fill64(const cg_config *cfg, double complex *dk, double complex *pk);
+int or_field64(const cg_config *cfg, double *dens, double *npot, double stats[4]);
+int or_density64(const cg_config *cfg, double *dens, double sigma2);
+int or_lpt64(const cg_config *cfg, const double *dens_gauss, double *dens_out, double *disp);
+int or_bins64(const cg_config *cfg, const double *dens, int nz, double idz, unsigned long long *narr, double *zarr,
+              double *bsum);
+int or_norm_tables64(const cg_config *cfg, double *tabs, double *e0f, int *nz_out, unsigned long long *narr,
+                     double *zarr, double *bsum, const double *dens);
+int or_lambda64(const cg_config *cfg, int ipop, const double *dens, const double *normtab, double n0, double nf,
+                double *lambda);
+int or_kappa64(const cg_config *cfg, const double *npot, double *map);
+int or_imap64(const cg_config *cfg, int ipop, const double *dens, const double *npot, const double *normtab,
+              double n0, double nf, double *data, int *nadd);
+int or_run_mock64(const cg_config *cfg, int nthreads_hint, long long *nsrc_total, double *checksum);
+
+/* ---- dev32 (or_dev32.c) ---- */
+int or_density32(const cg_config *cfg, float *dens, float sigma2f, int mode);
+int or_bins32(const cg_config *cfg, const float *dens, int nz, double idz, unsigned long long *narr, double *zarr,
+              double *bsum);
+int or_counts32(const cg_config *cfg, int ipop, const float *dens, const float *normtab, float n0, float nf,
+                unsigned short *counts, long long *total);
+int or_emit32(const cg_config *cfg, int ipop, const float *dens, const float *npot, const float *normtab, float n0,
+              float nf, long long cap, float *pos4, int *ipix, float *src9, int *cmap, long long *nsrc);
+int or_beam_rsd32(const cg_config *cfg, const float *npot, long long n, const float *pos4, float *src9);
+int or_imap32(const cg_config *cfg, int ipop, const float *dens, const float *npot, const float *normtab, float n0,
+              float nf, float *data, int *nadd);
+int or_kappa32(const cg_config *cfg, const float *npot, float *map);
+
+#endif

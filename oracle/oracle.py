@@ -1,0 +1,264 @@
+"""ORACLE Python binding (test infrastructure only).
+
+ctypes wrappers around oracle/_lib/liboracle.so, the CPU restatement of
+CoLoRe's hot path.  Imported by tests/, the smoke check and the CPU-baseline
+leg of bench.py; never by the product package.
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import build_oracle  # noqa: E402
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_oracle.build()
+        L = C.CDLL(path)
+        vp, d, i, f = C.c_void_p, C.c_double, C.c_int, C.c_float
+        sig = {
+            "or_fill64": [vp, vp, vp], "or_field64": [vp, vp, vp, vp], "or_density64": [vp, vp, d],
+            "or_lpt64": [vp, vp, vp, vp], "or_bins64": [vp, vp, i, d, vp, vp, vp],
+            "or_norm_tables64": [vp, vp, vp, vp, vp, vp, vp, vp],
+            "or_lambda64": [vp, i, vp, vp, d, d, vp], "or_kappa64": [vp, vp, vp],
+            "or_imap64": [vp, i, vp, vp, vp, d, d, vp, vp], "or_run_mock64": [vp, i, vp, vp],
+            "or_density32": [vp, vp, f, i], "or_bins32": [vp, vp, i, d, vp, vp, vp],
+            "or_counts32": [vp, i, vp, vp, f, f, vp, vp],
+            "or_emit32": [vp, i, vp, vp, vp, f, f, C.c_longlong, vp, vp, vp, vp, vp],
+            "or_beam_rsd32": [vp, vp, C.c_longlong, vp, vp], "or_imap32": [vp, i, vp, vp, vp, f, f, vp, vp],
+            "or_kappa32": [vp, vp, vp], "or_c2r_3d": [i, vp, vp], "or_r2c_3d": [i, vp, vp],
+            "or_vec_expf": [vp, vp, C.c_long], "or_vec_logf": [vp, vp, C.c_long],
+            "or_vec_log1pf": [vp, vp, C.c_long], "or_vec_acosf": [vp, vp, C.c_long],
+            "or_vec_atan2f": [vp, vp, vp, C.c_long], "or_vec_sincosf": [vp, vp, vp, C.c_long],
+            "or_philox": [vp, vp, vp], "or_poisson": [vp, vp, C.c_long, C.c_uint32, C.c_uint32],
+            "or_ang2pix": [C.c_long, vp, vp, vp, C.c_long], "or_nest2ring": [C.c_long, vp, vp, C.c_long],
+            "or_ring2nest": [C.c_long, vp, vp, C.c_long], "or_pix2vec_nest": [C.c_long, vp, vp, C.c_long],
+        }
+        for k, a in sig.items():
+            fn = getattr(L, k)
+            fn.argtypes = a
+            fn.restype = None if k.startswith("or_vec") or k in ("or_philox", "or_poisson", "or_ang2pix",
+                                                                   "or_nest2ring", "or_ring2nest",
+                                                                   "or_pix2vec_nest") else C.c_int
+        _lib = L
+    return _lib
+
+
+def P(a):
+    return a.ctypes.data if a is not None else None
+
+
+def cfgp(cfg):
+    return C.cast(C.pointer(cfg), C.c_void_p)
+
+
+def unpad(g):
+    """Padded [N][N][2(N/2+1)] grid -> unpadded [N][N][N] view."""
+    n = g.shape[0]
+    return g[:, :, :n]
+
+
+# ---- ref64 ----
+def field64(cfg):
+    n = cfg.n_grid
+    d = np.empty((n, n, n)), np.empty((n, n, n))
+    st = np.empty(4)
+    assert lib().or_field64(cfgp(cfg), P(d[0]), P(d[1]), P(st)) == 0
+    return d[0], d[1], st
+
+
+def fill64(cfg):
+    n = cfg.n_grid
+    dk = np.empty((n, n, n // 2 + 1), np.complex128)
+    pk = np.empty_like(dk)
+    lib().or_fill64(cfgp(cfg), P(dk), P(pk))
+    return dk, pk
+
+
+def density64(cfg, dens, sigma2):
+    dens = np.ascontiguousarray(dens, np.float64).copy()
+    lib().or_density64(cfgp(cfg), P(dens), sigma2)
+    return dens
+
+
+def lpt64(cfg, dens_gauss):
+    n = cfg.n_grid
+    dg = np.ascontiguousarray(dens_gauss, np.float64)
+    out = np.empty((n, n, n))
+    disp = np.empty((3, n, n, n))
+    assert lib().or_lpt64(cfgp(cfg), P(dg), P(out), P(disp)) == 0
+    return out, disp
+
+
+def norm_tables64(cfg, dens):
+    nt = cfg.n_srcs + cfg.n_imap
+    tabs = np.empty((max(nt, 1), 5001))
+    e0f = np.empty((max(nt, 1), 2))
+    nz = C.c_int()
+    narr = np.empty(4096, np.uint64)
+    zarr = np.empty(4096)
+    bsum = np.empty((max(nt, 1), 4096))
+    dd = np.ascontiguousarray(dens, np.float64)
+    lib().or_norm_tables64(cfgp(cfg), P(tabs), P(e0f), C.byref(nz), P(narr), P(zarr), P(bsum), P(dd))
+    return tabs, e0f, nz.value
+
+
+def bins64(cfg, dens, nz, idz):
+    nt = cfg.n_srcs + cfg.n_imap
+    narr = np.empty(nz, np.uint64)
+    zarr = np.empty(nz)
+    bsum = np.empty((max(nt, 1), nz))
+    dd = np.ascontiguousarray(dens, np.float64)
+    lib().or_bins64(cfgp(cfg), P(dd), nz, idz, P(narr), P(zarr), P(bsum))
+    return narr, zarr, bsum[:nt]
+
+
+def lambda64(cfg, ipop, dens, tab, e):
+    n = cfg.n_grid
+    lam = np.empty((n, n, n))
+    dd = np.ascontiguousarray(dens, np.float64)
+    lib().or_lambda64(cfgp(cfg), ipop, P(dd), P(np.ascontiguousarray(tab, np.float64)), float(e[0]), float(e[1]),
+                      P(lam))
+    return lam
+
+
+def kappa64(cfg, npot):
+    ns = cfg.nside_kappa
+    m = np.empty((cfg.n_kappa, 12 * ns * ns))
+    lib().or_kappa64(cfgp(cfg), P(np.ascontiguousarray(npot, np.float64)), P(m))
+    return m
+
+
+def imap64(cfg, ipop, dens, npot, tab, e):
+    ns, nr = cfg.nside_imap[ipop], cfg.imap_nr[ipop]
+    data = np.empty((nr, 12 * ns * ns))
+    nadd = np.empty((nr, 12 * ns * ns), np.int32)
+    lib().or_imap64(cfgp(cfg), ipop, P(np.ascontiguousarray(dens, np.float64)),
+                    P(np.ascontiguousarray(npot, np.float64)), P(np.ascontiguousarray(tab, np.float64)),
+                    float(e[0]), float(e[1]), P(data), P(nadd))
+    return data, nadd
+
+
+def run_mock64(cfg):
+    n = C.c_longlong()
+    cs = C.c_double()
+    assert lib().or_run_mock64(cfgp(cfg), 0, C.byref(n), C.byref(cs)) == 0
+    return n.value, cs.value
+
+
+# ---- dev32 (padded float32 grids as downloaded from the GPU) ----
+def density32(cfg, dens, s2f, mode):
+    d = np.array(dens, np.float32, copy=True)
+    lib().or_density32(cfgp(cfg), P(d), float(s2f), mode)
+    return d
+
+
+def bins32(cfg, dens, nz, idz):
+    nt = cfg.n_srcs + cfg.n_imap
+    narr = np.empty(nz, np.uint64)
+    zarr = np.empty(nz)
+    bsum = np.empty((max(nt, 1), nz))
+    lib().or_bins32(cfgp(cfg), P(np.ascontiguousarray(dens, np.float32)), nz, idz, P(narr), P(zarr), P(bsum))
+    return narr, zarr, bsum[:nt]
+
+
+def counts32(cfg, ipop, dens, tab, e):
+    n = cfg.n_grid
+    cnt = np.empty((n, n, n), np.uint16)
+    tot = C.c_longlong()
+    lib().or_counts32(cfgp(cfg), ipop, P(dens), P(tab), float(e[0]), float(e[1]), P(cnt), C.byref(tot))
+    return cnt, tot.value
+
+
+def emit32(cfg, ipop, dens, npot, tab, e, cap):
+    pos = np.empty((cap, 4), np.float32)
+    ipix = np.empty(cap, np.int32)
+    src = np.empty((cap, 9), np.float32)
+    ns = cfg.nside_count[ipop]
+    cmap = np.zeros(12 * ns * ns, np.int32) if ns > 0 else None
+    n = C.c_longlong()
+    rc = lib().or_emit32(cfgp(cfg), ipop, P(dens), P(npot), P(tab), float(e[0]), float(e[1]), cap, P(pos), P(ipix),
+                         P(src), P(cmap), C.byref(n))
+    assert rc == 0
+    k = n.value
+    return dict(pos=pos[:k], ipix=ipix[:k], src=src[:k], cmap=cmap)
+
+
+def beam_rsd32(cfg, npot, pos, src):
+    s = np.array(src, np.float32, copy=True)
+    lib().or_beam_rsd32(cfgp(cfg), P(npot), len(pos), P(np.ascontiguousarray(pos, np.float32)), P(s))
+    return s
+
+
+def imap32(cfg, ipop, dens, npot, tab, e):
+    ns, nr = cfg.nside_imap[ipop], cfg.imap_nr[ipop]
+    data = np.empty((nr, 12 * ns * ns), np.float32)
+    nadd = np.empty((nr, 12 * ns * ns), np.int32)
+    lib().or_imap32(cfgp(cfg), ipop, P(dens), P(npot), P(tab), float(e[0]), float(e[1]), P(data), P(nadd))
+    return data, nadd
+
+
+def kappa32(cfg, npot):
+    ns = cfg.nside_kappa
+    m = np.empty((cfg.n_kappa, 12 * ns * ns), np.float32)
+    lib().or_kappa32(cfgp(cfg), P(npot), P(m))
+    return m
+
+
+# ---- scalar checks ----
+def vec(name, *arrs):
+    out = [np.empty_like(arrs[0]) for _ in range(2 if name == "sincosf" else 1)]
+    args = [P(np.ascontiguousarray(a, np.float32)) for a in arrs] + [P(o) for o in out] + [len(arrs[0])]
+    getattr(lib(), "or_vec_" + name)(*args)
+    return out if len(out) > 1 else out[0]
+
+
+def philox(ctr, key):
+    c = np.array(ctr, np.uint32)
+    k = np.array(key, np.uint32)
+    o = np.empty(4, np.uint32)
+    lib().or_philox(P(c), P(k), P(o))
+    return o
+
+
+def poisson(lam, k0=1, k1=2):
+    lam = np.ascontiguousarray(lam, np.float32)
+    k = np.empty(len(lam), np.int32)
+    lib().or_poisson(P(lam), P(k), len(lam), k0, k1)
+    return k
+
+
+def ang2pix(nside, cth, phi):
+    cth = np.ascontiguousarray(cth, np.float32)
+    phi = np.ascontiguousarray(phi, np.float32)
+    p = np.empty(len(cth), np.int64)
+    lib().or_ang2pix(nside, P(cth), P(phi), P(p), len(cth))
+    return p
+
+
+def nest2ring(nside, ip):
+    ip = np.ascontiguousarray(ip, np.int64)
+    o = np.empty_like(ip)
+    lib().or_nest2ring(nside, P(ip), P(o), len(ip))
+    return o
+
+
+def ring2nest(nside, ip):
+    ip = np.ascontiguousarray(ip, np.int64)
+    o = np.empty_like(ip)
+    lib().or_ring2nest(nside, P(ip), P(o), len(ip))
+    return o
+
+
+def pix2vec_nest(nside, ip):
+    ip = np.ascontiguousarray(ip, np.int64)
+    v = np.empty((len(ip), 3), np.float32)
+    lib().or_pix2vec_nest(nside, P(ip), P(v), len(ip))
+    return v

@@ -1,0 +1,48 @@
+"""The CPU oracle checked on its own (no GPU): its FFT against numpy's
+pocketfft, and the Gaussian field against the input power spectrum."""
+import numpy as np
+import pytest
+
+
+@pytest.mark.parametrize("n", [16, 24, 32, 48])
+def test_oracle_c2r_matches_numpy_irfftn(built, n):
+    import oracle as orc
+    rng = np.random.default_rng(n)
+    X = rng.normal(size=(n, n, n // 2 + 1)) + 1j * rng.normal(size=(n, n, n // 2 + 1))
+    out = np.empty((n, n, n))
+    orc.lib().or_c2r_3d(n, orc.P(X), orc.P(out))
+    ref = np.fft.irfftn(X, s=(n, n, n), axes=(0, 1, 2), norm="forward")
+    assert np.abs(out - ref).max() < 1e-9 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("n", [16, 24])
+def test_oracle_r2c_matches_numpy_rfftn(built, n):
+    import oracle as orc
+    x = np.random.default_rng(1).normal(size=(n, n, n))
+    out = np.empty((n, n, n // 2 + 1), np.complex128)
+    orc.lib().or_r2c_3d(n, orc.P(x), orc.P(out))
+    ref = np.fft.rfftn(x, axes=(0, 1, 2))
+    assert np.abs(out - ref).max() < 1e-9 * np.abs(ref).max()
+
+
+def test_oracle_field_power_spectrum(built, tmp_path):
+    """P(k) of the oracle's Gaussian field follows the input P(k) e^{-k^2 R^2}
+    (the statistical check the reference relies on, predictions.c)."""
+    import colore_gb300 as cg
+    from colore_gb300 import inputs
+    import oracle as orc
+    f = inputs.write_inputs(str(tmp_path), inputs.scaled("c1", 64))
+    prm = cg.Params(f)  # owns the tables cfg points at
+    cfg = prm.config
+    dk, _ = orc.fill64(cfg)
+    n = cfg.n_grid
+    kf = 2 * np.pi / cfg.l_box
+    kx = np.arange(n // 2 + 1) * kf
+    ky = np.fft.fftfreq(n, 1.0 / n) * kf
+    kk = np.sqrt(kx[None, None, :] ** 2 + ky[None, :, None] ** 2 + ky[:, None, None] ** 2)
+    sel = (kk > 0) & (kk < 0.5 * n * kf)
+    pk = np.ctypeslib.as_array(cfg.pkarr, (cfg.numk,))
+    lk = cfg.logkmin + np.arange(cfg.numk) / cfg.idlogk
+    model = np.interp(np.log10(kk[sel]), lk, pk) * np.exp(-cfg.r2_smooth * kk[sel] ** 2) / kf ** 3
+    ratio = np.abs(dk[sel]) ** 2 / model
+    assert abs(ratio.mean() - 1) < 0.02
