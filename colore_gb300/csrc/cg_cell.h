@@ -132,7 +132,9 @@ CG_HD int cg_poisson(float lam, uint32_t k0, uint32_t k1, uint32_t c0, uint32_t 
   return (int)cg_floorf(lam);
 }
 
-/* cart2sph, srcs.c:68-85 / imap.c:24-41. */
+/* cart2sph, srcs.c:68-85 / imap.c:24-41.  phi = atan2(y, x): the reference
+ * normalises x and y by r first, which leaves the angle unchanged and costs
+ * two divisions. */
 CG_HD void cg_cart2sph(float x, float y, float z, float *r, float *cth, float *phi)
 {
   float rr = cg_norm3(x, y, z);
@@ -142,16 +144,17 @@ CG_HD void cg_cart2sph(float x, float y, float z, float *r, float *cth, float *p
     *phi = 0.0f;
     return;
   }
-  float xn = CG_DIV(x, rr), yn = CG_DIV(y, rr);
   *cth = CG_DIV(z, rr);
-  float ph = cg_atan2f(yn, xn);
+  float ph = cg_atan2f(y, x);
   if (ph < 0.0f) ph = CG_ADD(ph, CG_TWOPI_F);
   *phi = ph;
 }
 
-/* he_ang2pix (RING), healpix_extra.c:118-172. */
-CG_HD int64_t cg_ang2pix_ring(int64_t nside, float cth, float phi)
+/* he_ang2pix (RING), healpix_extra.c:118-172.  Integer work is 32-bit:
+ * every intermediate fits for nside <= 8192 (NSIDE_MAX_HPX, common.h:94). */
+CG_HD int64_t cg_ang2pix_ring(int64_t nside64, float cth, float phi)
 {
+  const int nside = (int)nside64;
   float ctha = cg_fabsf(cth);
   float ph = phi;
   if (ph >= 0.0f) {
@@ -165,27 +168,27 @@ CG_HD int64_t cg_ang2pix_ring(int64_t nside, float cth, float phi)
   if (ctha <= 0.666666666666666667f) {
     float temp1 = CG_MUL(ns, CG_ADD(0.5f, tt));
     float temp2 = CG_MUL(CG_MUL(ns, cth), 0.75f);
-    int64_t jp = (int64_t)CG_SUB(temp1, temp2);
-    int64_t jm = (int64_t)CG_ADD(temp1, temp2);
-    int64_t ir = nside + 1 + jp - jm;
-    int64_t kshift = 1 - (ir & 1);
-    int64_t ip = (jp + jm - nside + kshift + 1) / 2;
-    int64_t m = 4 * nside;
+    int jp = (int)CG_SUB(temp1, temp2);
+    int jm = (int)CG_ADD(temp1, temp2);
+    int ir = nside + 1 + jp - jm;
+    int kshift = 1 - (ir & 1);
+    int ip = (jp + jm - nside + kshift + 1) / 2;
+    int m = 4 * nside;
     ip = ip % m;
     if (ip < 0) ip += m;
-    return nside * (nside - 1) * 2 + (ir - 1) * 4 * nside + ip;
+    return (int64_t)(nside * (nside - 1) * 2 + (ir - 1) * 4 * nside + ip);
   } else {
     float tp = CG_SUB(tt, (float)(int)tt);
     float tmp = CG_MUL(ns, CG_SQRT(CG_MUL(3.0f, CG_SUB(1.0f, ctha))));
-    int64_t jp = (int64_t)CG_MUL(tp, tmp);
-    int64_t jm = (int64_t)CG_MUL(CG_SUB(1.0f, tp), tmp);
-    int64_t ir = jp + jm + 1;
-    int64_t ip = (int64_t)CG_MUL(tt, (float)ir);
-    int64_t m = 4 * ir;
+    int jp = (int)CG_MUL(tp, tmp);
+    int jm = (int)CG_MUL(CG_SUB(1.0f, tp), tmp);
+    int ir = jp + jm + 1;
+    int ip = (int)CG_MUL(tt, (float)ir);
+    int m = 4 * ir;
     ip = ip % m;
     if (ip < 0) ip += m;
-    if (cth > 0.0f) return 2 * ir * (ir - 1) + ip;
-    return 12 * nside * nside - 2 * ir * (ir + 1) + ip;
+    if (cth > 0.0f) return (int64_t)(2 * ir * (ir - 1) + ip);
+    return (int64_t)(12 * nside * nside - 2 * ir * (ir + 1) + ip);
   }
 }
 

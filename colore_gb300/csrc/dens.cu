@@ -57,9 +57,44 @@ __global__ void k_moments_final(const double2 *__restrict__ part, size_t n, doub
 constexpr int MAXT = 8;      /* tracers per bins launch */
 constexpr int BINS_WARPS = 8;
 
+/* Segmented warp reduction by bin of (count, z, bias sums); lane 0 adds the
+ * totals to the warp's private FP64 bins (no atomics: one writer). */
+__device__ __forceinline__ void warp_bins_add(double *mybins, int W, int nt, int lane, int bin, float cnt, float zs,
+                                              const float *bs)
+{
+  unsigned todo = __ballot_sync(0xffffffffu, bin >= 0);
+  while (todo) {
+    const int leader = __ffs(todo) - 1;
+    const int lb = __shfl_sync(0xffffffffu, bin, leader);
+    const bool mine = (bin == lb);
+    float c = mine ? cnt : 0.0f, zsum = mine ? zs : 0.0f;
+    float bsum[MAXT];
+#pragma unroll
+    for (int t = 0; t < MAXT; t++) bsum[t] = mine ? bs[t] : 0.0f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      c += __shfl_xor_sync(0xffffffffu, c, o);
+      zsum += __shfl_xor_sync(0xffffffffu, zsum, o);
+#pragma unroll
+      for (int t = 0; t < MAXT; t++)
+        if (t < nt) bsum[t] += __shfl_xor_sync(0xffffffffu, bsum[t], o);
+    }
+    if (lane == 0) {
+      double *d = mybins + (size_t)lb * W;
+      d[0] += (double)c;
+      d[1] += (double)zsum;
+#pragma unroll
+      for (int t = 0; t < MAXT; t++)
+        if (t < nt) d[2 + t] += (double)bsum[t];
+    }
+    todo &= ~__ballot_sync(0xffffffffu, mine);
+  }
+  __syncwarp();
+}
+
 __global__ void __launch_bounds__(BINS_WARPS * 32) k_dens_bins(float *grid, cg_bins_params p)
 {
-  extern __shared__ double sbin[]; /* [warp][nz][2 + nt]; count stored as double-exact integer */
+  extern __shared__ double sbin[]; /* [warp][nz][2 + nt]; the count is an exact integer in FP64 */
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nz = p.nz, nt = p.nt, W = 2 + nt;
   double *mybins = sbin + (size_t)wid * nz * W;
@@ -76,86 +111,44 @@ __global__ void __launch_bounds__(BINS_WARPS * 32) k_dens_bins(float *grid, cg_b
     const long long row = seg / nseg_row;
     const int iy = (int)(row % N), iz = (int)(row / N);
     const int ix = sr * 64 + 2 * lane;
-    const bool valid = ix < N;
-    int bin = -1;
-    float cnt = 0.0f, zs = 0.0f, bs[MAXT];
+    int bb[2] = {-1, -1};
+    float zz[2] = {0.0f, 0.0f}, bs[2][MAXT];
 #pragma unroll
-    for (int t = 0; t < MAXT; t++) bs[t] = 0.0f;
-    if (valid) {
+    for (int t = 0; t < MAXT; t++) bs[0][t] = bs[1][t] = 0.0f;
+    if (ix < N) {
       float2 *ptr = reinterpret_cast<float2 *>(grid + pidx(ix, iy, iz, N));
       float2 dv = *ptr;
       const float y0 = cg_cell_coord(iy, p.box.dx, p.box.p1), z0 = cg_cell_coord(iz, p.box.dx, p.box.p2);
       float dd[2] = {dv.x, dv.y};
-      int bb[2];
-      float zz[2], rr[2];
 #pragma unroll
       for (int h = 0; h < 2; h++) {
-        float x0 = cg_cell_coord(ix + h, p.box.dx, p.box.p0);
-        float r = cg_norm3(x0, y0, z0);
-        rr[h] = r;
+        const float x0 = cg_cell_coord(ix + h, p.box.dx, p.box.p0);
+        const float r = cg_norm3(x0, y0, z0);
         if (p.mode != CG_DMODE_NONE) dd[h] = cg_dens_transform(p.mode, dd[h], bg(p.d1, p.g, r), s2);
-        float z = bg(p.zt, p.g, r);
-        zz[h] = z;
-        int iz_bin = (int)CG_MUL(z, p.idz) + 1;
-        bb[h] = (iz_bin >= 0 && iz_bin < nz) ? iz_bin : -1; /* nz = 0: transform only */
-      }
-      if (p.mode != CG_DMODE_NONE) *ptr = make_float2(dd[0], dd[1]);
-      /* both cells of a lane normally share a bin; otherwise the second
-       * one is flushed on its own below */
-      bin = bb[0];
-      if (bin >= 0) {
-        cnt = 1.0f;
-        zs = zz[0];
+        if (nz > 0) {
+          const float z = bg(p.zt, p.g, r);
+          const int b = (int)CG_MUL(z, p.idz) + 1;
+          if (b >= 0 && b < nz) {
+            bb[h] = b;
+            zz[h] = z;
 #pragma unroll
-        for (int t = 0; t < MAXT; t++)
-          if (t < nt) bs[t] = cg_bias_model(dd[0], bg(p.bz[t], p.g, rr[0]), p.bias_model);
-      }
-      if (bb[1] >= 0) {
-        if (bb[1] == bin || bin < 0) {
-          bin = bb[1];
-          cnt += 1.0f;
-          zs += zz[1];
-#pragma unroll
-          for (int t = 0; t < MAXT; t++)
-            if (t < nt) bs[t] += cg_bias_model(dd[1], bg(p.bz[t], p.g, rr[1]), p.bias_model);
-        } else {
-          /* rare: second cell in another bin -> direct FP64 update */
-          double *d = mybins + (size_t)bb[1] * W;
-          atomicAdd(&d[0], 1.0);
-          atomicAdd(&d[1], (double)zz[1]);
-          for (int t = 0; t < nt && t < MAXT; t++)
-            atomicAdd(&d[2 + t], (double)cg_bias_model(dd[1], bg(p.bz[t], p.g, rr[1]), p.bias_model));
+            for (int t = 0; t < MAXT; t++)
+              if (t < nt) bs[h][t] = cg_bias_model(dd[h], bg(p.bz[t], p.g, r), p.bias_model);
+          }
         }
       }
+      if (p.mode != CG_DMODE_NONE) *ptr = make_float2(dd[0], dd[1]);
     }
-    /* warp-level segmented reduction by bin */
-    unsigned todo = __ballot_sync(0xffffffffu, bin >= 0);
-    while (todo) {
-      int leader = __ffs(todo) - 1;
-      int lb = __shfl_sync(0xffffffffu, bin, leader);
-      bool mine = (bin == lb);
-      float c = mine ? cnt : 0.0f, zsum = mine ? zs : 0.0f;
-      float bsum[MAXT];
+    if (nz == 0) continue;
+    /* both cells of a lane share a bin except at bin edges */
+    if (__all_sync(0xffffffffu, bb[0] == bb[1])) {
+      float b2[MAXT];
 #pragma unroll
-      for (int t = 0; t < MAXT; t++) bsum[t] = mine ? bs[t] : 0.0f;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        c += __shfl_xor_sync(0xffffffffu, c, o);
-        zsum += __shfl_xor_sync(0xffffffffu, zsum, o);
-#pragma unroll
-        for (int t = 0; t < MAXT; t++)
-          if (t < nt) bsum[t] += __shfl_xor_sync(0xffffffffu, bsum[t], o);
-      }
-      if (lane == 0) {
-        double *d = mybins + (size_t)lb * W;
-        atomicAdd(&d[0], (double)c);
-        atomicAdd(&d[1], (double)zsum);
-#pragma unroll
-        for (int t = 0; t < MAXT; t++)
-          if (t < nt) atomicAdd(&d[2 + t], (double)bsum[t]);
-      }
-      todo &= ~__ballot_sync(0xffffffffu, mine);
-      __syncwarp();
+      for (int t = 0; t < MAXT; t++) b2[t] = bs[0][t] + bs[1][t];
+      warp_bins_add(mybins, W, nt, lane, bb[0], bb[0] >= 0 ? 2.0f : 0.0f, zz[0] + zz[1], b2);
+    } else {
+      warp_bins_add(mybins, W, nt, lane, bb[0], 1.0f, zz[0], bs[0]);
+      warp_bins_add(mybins, W, nt, lane, bb[1], 1.0f, zz[1], bs[1]);
     }
   }
   __syncthreads();

@@ -25,133 +25,94 @@
 namespace cgfft {
 
 /* exp(+2 pi i j / 96), j = 0..95: every radix used here divides 96. */
-static __constant__ float2 c_tw96[96] = {
-    {1.000000000e+00f, 0.000000000e+00f},
-    {9.978589416e-01f, 6.540312618e-02f},
-    {9.914448857e-01f, 1.305261850e-01f},
-    {9.807852507e-01f, 1.950903237e-01f},
-    {9.659258127e-01f, 2.588190436e-01f},
-    {9.469301105e-01f, 3.214394748e-01f},
-    {9.238795042e-01f, 3.826834261e-01f},
-    {8.968727589e-01f, 4.422886968e-01f},
-    {8.660253882e-01f, 5.000000000e-01f},
-    {8.314695954e-01f, 5.555702448e-01f},
-    {7.933533192e-01f, 6.087614298e-01f},
-    {7.518398166e-01f, 6.593458056e-01f},
-    {7.071067691e-01f, 7.071067691e-01f},
-    {6.593458056e-01f, 7.518398166e-01f},
-    {6.087614298e-01f, 7.933533192e-01f},
-    {5.555702448e-01f, 8.314695954e-01f},
-    {5.000000000e-01f, 8.660253882e-01f},
-    {4.422886968e-01f, 8.968727589e-01f},
-    {3.826834261e-01f, 9.238795042e-01f},
-    {3.214394748e-01f, 9.469301105e-01f},
-    {2.588190436e-01f, 9.659258127e-01f},
-    {1.950903237e-01f, 9.807852507e-01f},
-    {1.305261850e-01f, 9.914448857e-01f},
-    {6.540312618e-02f, 9.978589416e-01f},
-    {0.000000000e+00f, 1.000000000e+00f},
-    {-6.540312618e-02f, 9.978589416e-01f},
-    {-1.305261850e-01f, 9.914448857e-01f},
-    {-1.950903237e-01f, 9.807852507e-01f},
-    {-2.588190436e-01f, 9.659258127e-01f},
-    {-3.214394748e-01f, 9.469301105e-01f},
-    {-3.826834261e-01f, 9.238795042e-01f},
-    {-4.422886968e-01f, 8.968727589e-01f},
-    {-5.000000000e-01f, 8.660253882e-01f},
-    {-5.555702448e-01f, 8.314695954e-01f},
-    {-6.087614298e-01f, 7.933533192e-01f},
-    {-6.593458056e-01f, 7.518398166e-01f},
-    {-7.071067691e-01f, 7.071067691e-01f},
-    {-7.518398166e-01f, 6.593458056e-01f},
-    {-7.933533192e-01f, 6.087614298e-01f},
-    {-8.314695954e-01f, 5.555702448e-01f},
-    {-8.660253882e-01f, 5.000000000e-01f},
-    {-8.968727589e-01f, 4.422886968e-01f},
-    {-9.238795042e-01f, 3.826834261e-01f},
-    {-9.469301105e-01f, 3.214394748e-01f},
-    {-9.659258127e-01f, 2.588190436e-01f},
-    {-9.807852507e-01f, 1.950903237e-01f},
-    {-9.914448857e-01f, 1.305261850e-01f},
-    {-9.978589416e-01f, 6.540312618e-02f},
-    {-1.000000000e+00f, 0.000000000e+00f},
-    {-9.978589416e-01f, -6.540312618e-02f},
-    {-9.914448857e-01f, -1.305261850e-01f},
-    {-9.807852507e-01f, -1.950903237e-01f},
-    {-9.659258127e-01f, -2.588190436e-01f},
-    {-9.469301105e-01f, -3.214394748e-01f},
-    {-9.238795042e-01f, -3.826834261e-01f},
-    {-8.968727589e-01f, -4.422886968e-01f},
-    {-8.660253882e-01f, -5.000000000e-01f},
-    {-8.314695954e-01f, -5.555702448e-01f},
-    {-7.933533192e-01f, -6.087614298e-01f},
-    {-7.518398166e-01f, -6.593458056e-01f},
-    {-7.071067691e-01f, -7.071067691e-01f},
-    {-6.593458056e-01f, -7.518398166e-01f},
-    {-6.087614298e-01f, -7.933533192e-01f},
-    {-5.555702448e-01f, -8.314695954e-01f},
-    {-5.000000000e-01f, -8.660253882e-01f},
-    {-4.422886968e-01f, -8.968727589e-01f},
-    {-3.826834261e-01f, -9.238795042e-01f},
-    {-3.214394748e-01f, -9.469301105e-01f},
-    {-2.588190436e-01f, -9.659258127e-01f},
-    {-1.950903237e-01f, -9.807852507e-01f},
-    {-1.305261850e-01f, -9.914448857e-01f},
-    {-6.540312618e-02f, -9.978589416e-01f},
-    {0.000000000e+00f, -1.000000000e+00f},
-    {6.540312618e-02f, -9.978589416e-01f},
-    {1.305261850e-01f, -9.914448857e-01f},
-    {1.950903237e-01f, -9.807852507e-01f},
-    {2.588190436e-01f, -9.659258127e-01f},
-    {3.214394748e-01f, -9.469301105e-01f},
-    {3.826834261e-01f, -9.238795042e-01f},
-    {4.422886968e-01f, -8.968727589e-01f},
-    {5.000000000e-01f, -8.660253882e-01f},
-    {5.555702448e-01f, -8.314695954e-01f},
-    {6.087614298e-01f, -7.933533192e-01f},
-    {6.593458056e-01f, -7.518398166e-01f},
-    {7.071067691e-01f, -7.071067691e-01f},
-    {7.518398166e-01f, -6.593458056e-01f},
-    {7.933533192e-01f, -6.087614298e-01f},
-    {8.314695954e-01f, -5.555702448e-01f},
-    {8.660253882e-01f, -5.000000000e-01f},
-    {8.968727589e-01f, -4.422886968e-01f},
-    {9.238795042e-01f, -3.826834261e-01f},
-    {9.469301105e-01f, -3.214394748e-01f},
-    {9.659258127e-01f, -2.588190436e-01f},
-    {9.807852507e-01f, -1.950903237e-01f},
-    {9.914448857e-01f, -1.305261850e-01f},
-    {9.978589416e-01f, -6.540312618e-02f}
+#define CG_TW96_VALUES \
+  { \
+    {1.000000000e+00f, 0.000000000e+00f}, {9.978589416e-01f, 6.540312618e-02f}, \
+    {9.914448857e-01f, 1.305261850e-01f}, {9.807852507e-01f, 1.950903237e-01f}, \
+    {9.659258127e-01f, 2.588190436e-01f}, {9.469301105e-01f, 3.214394748e-01f}, \
+    {9.238795042e-01f, 3.826834261e-01f}, {8.968727589e-01f, 4.422886968e-01f}, \
+    {8.660253882e-01f, 5.000000000e-01f}, {8.314695954e-01f, 5.555702448e-01f}, \
+    {7.933533192e-01f, 6.087614298e-01f}, {7.518398166e-01f, 6.593458056e-01f}, \
+    {7.071067691e-01f, 7.071067691e-01f}, {6.593458056e-01f, 7.518398166e-01f}, \
+    {6.087614298e-01f, 7.933533192e-01f}, {5.555702448e-01f, 8.314695954e-01f}, \
+    {5.000000000e-01f, 8.660253882e-01f}, {4.422886968e-01f, 8.968727589e-01f}, \
+    {3.826834261e-01f, 9.238795042e-01f}, {3.214394748e-01f, 9.469301105e-01f}, \
+    {2.588190436e-01f, 9.659258127e-01f}, {1.950903237e-01f, 9.807852507e-01f}, \
+    {1.305261850e-01f, 9.914448857e-01f}, {6.540312618e-02f, 9.978589416e-01f}, \
+    {0.000000000e+00f, 1.000000000e+00f}, {-6.540312618e-02f, 9.978589416e-01f}, \
+    {-1.305261850e-01f, 9.914448857e-01f}, {-1.950903237e-01f, 9.807852507e-01f}, \
+    {-2.588190436e-01f, 9.659258127e-01f}, {-3.214394748e-01f, 9.469301105e-01f}, \
+    {-3.826834261e-01f, 9.238795042e-01f}, {-4.422886968e-01f, 8.968727589e-01f}, \
+    {-5.000000000e-01f, 8.660253882e-01f}, {-5.555702448e-01f, 8.314695954e-01f}, \
+    {-6.087614298e-01f, 7.933533192e-01f}, {-6.593458056e-01f, 7.518398166e-01f}, \
+    {-7.071067691e-01f, 7.071067691e-01f}, {-7.518398166e-01f, 6.593458056e-01f}, \
+    {-7.933533192e-01f, 6.087614298e-01f}, {-8.314695954e-01f, 5.555702448e-01f}, \
+    {-8.660253882e-01f, 5.000000000e-01f}, {-8.968727589e-01f, 4.422886968e-01f}, \
+    {-9.238795042e-01f, 3.826834261e-01f}, {-9.469301105e-01f, 3.214394748e-01f}, \
+    {-9.659258127e-01f, 2.588190436e-01f}, {-9.807852507e-01f, 1.950903237e-01f}, \
+    {-9.914448857e-01f, 1.305261850e-01f}, {-9.978589416e-01f, 6.540312618e-02f}, \
+    {-1.000000000e+00f, 0.000000000e+00f}, {-9.978589416e-01f, -6.540312618e-02f}, \
+    {-9.914448857e-01f, -1.305261850e-01f}, {-9.807852507e-01f, -1.950903237e-01f}, \
+    {-9.659258127e-01f, -2.588190436e-01f}, {-9.469301105e-01f, -3.214394748e-01f}, \
+    {-9.238795042e-01f, -3.826834261e-01f}, {-8.968727589e-01f, -4.422886968e-01f}, \
+    {-8.660253882e-01f, -5.000000000e-01f}, {-8.314695954e-01f, -5.555702448e-01f}, \
+    {-7.933533192e-01f, -6.087614298e-01f}, {-7.518398166e-01f, -6.593458056e-01f}, \
+    {-7.071067691e-01f, -7.071067691e-01f}, {-6.593458056e-01f, -7.518398166e-01f}, \
+    {-6.087614298e-01f, -7.933533192e-01f}, {-5.555702448e-01f, -8.314695954e-01f}, \
+    {-5.000000000e-01f, -8.660253882e-01f}, {-4.422886968e-01f, -8.968727589e-01f}, \
+    {-3.826834261e-01f, -9.238795042e-01f}, {-3.214394748e-01f, -9.469301105e-01f}, \
+    {-2.588190436e-01f, -9.659258127e-01f}, {-1.950903237e-01f, -9.807852507e-01f}, \
+    {-1.305261850e-01f, -9.914448857e-01f}, {-6.540312618e-02f, -9.978589416e-01f}, \
+    {0.000000000e+00f, -1.000000000e+00f}, {6.540312618e-02f, -9.978589416e-01f}, \
+    {1.305261850e-01f, -9.914448857e-01f}, {1.950903237e-01f, -9.807852507e-01f}, \
+    {2.588190436e-01f, -9.659258127e-01f}, {3.214394748e-01f, -9.469301105e-01f}, \
+    {3.826834261e-01f, -9.238795042e-01f}, {4.422886968e-01f, -8.968727589e-01f}, \
+    {5.000000000e-01f, -8.660253882e-01f}, {5.555702448e-01f, -8.314695954e-01f}, \
+    {6.087614298e-01f, -7.933533192e-01f}, {6.593458056e-01f, -7.518398166e-01f}, \
+    {7.071067691e-01f, -7.071067691e-01f}, {7.518398166e-01f, -6.593458056e-01f}, \
+    {7.933533192e-01f, -6.087614298e-01f}, {8.314695954e-01f, -5.555702448e-01f}, \
+    {8.660253882e-01f, -5.000000000e-01f}, {8.968727589e-01f, -4.422886968e-01f}, \
+    {9.238795042e-01f, -3.826834261e-01f}, {9.469301105e-01f, -3.214394748e-01f}, \
+    {9.659258127e-01f, -2.588190436e-01f}, {9.807852507e-01f, -1.950903237e-01f}, \
+    {9.914448857e-01f, -1.305261850e-01f}, {9.978589416e-01f, -6.540312618e-02f} \
+  }
+static __constant__ float2 c_tw96[96] = CG_TW96_VALUES;
+static const float2 h_tw96[96] = CG_TW96_VALUES;
+#ifdef __CUDA_ARCH__
+#define CG_TW96(j) c_tw96[j]
+#define CG_LDG(p) __ldg(p)
+#else
+#define CG_TW96(j) h_tw96[j]
+#define CG_LDG(p) (*(p))
+#endif
 
-};
-
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 /* a * w (S>0) or a * conj(w) (S<0) */
 template <int S>
-__device__ __forceinline__ float2 cmulS(float2 a, float2 w)
+__host__ __device__ __forceinline__ float2 cmulS(float2 a, float2 w)
 {
   if (S > 0) return make_float2(a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x);
   return make_float2(a.x * w.x + a.y * w.y, a.y * w.x - a.x * w.y);
 }
 /* S * i * a */
 template <int S>
-__device__ __forceinline__ float2 mulSi(float2 a)
+__host__ __device__ __forceinline__ float2 mulSi(float2 a)
 {
   return S > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
 }
 
 /* a * exp(S 2 pi i m / R) for a compile-time m once loops are unrolled */
 template <int R, int S>
-__device__ __forceinline__ float2 twc(float2 a, int m)
+__host__ __device__ __forceinline__ float2 twc(float2 a, int m)
 {
   int j = (m * (96 / R)) % 96;
   if (j == 0) return a;
   if (j == 24) return mulSi<S>(a);
   if (j == 48) return make_float2(-a.x, -a.y);
   if (j == 72) return mulSi<-S>(a);
-  return cmulS<S>(a, c_tw96[j]);
+  return cmulS<S>(a, CG_TW96(j));
 }
 
 template <int R, int S>
@@ -159,7 +120,7 @@ struct DFT;
 
 template <int S>
 struct DFT<2, S> {
-  __device__ __forceinline__ static void run(float2 *v)
+  __host__ __device__ __forceinline__ static void run(float2 *v)
   {
     float2 a = v[0], b = v[1];
     v[0] = cadd(a, b);
@@ -169,7 +130,7 @@ struct DFT<2, S> {
 
 template <int S>
 struct DFT<3, S> {
-  __device__ __forceinline__ static void run(float2 *v)
+  __host__ __device__ __forceinline__ static void run(float2 *v)
   {
     const float s3 = 0.866025403784438647f;
     float2 a = v[0], b = v[1], c = v[2];
@@ -184,7 +145,7 @@ struct DFT<3, S> {
 
 template <int S>
 struct DFT<4, S> {
-  __device__ __forceinline__ static void run(float2 *v)
+  __host__ __device__ __forceinline__ static void run(float2 *v)
   {
     float2 a = v[0], b = v[1], c = v[2], d = v[3];
     float2 s0 = cadd(a, c), s1 = csub(a, c), s2 = cadd(b, d), s3 = mulSi<S>(csub(b, d));
@@ -197,7 +158,7 @@ struct DFT<4, S> {
 
 /* Composite radix R = R1 R2 by one Cooley-Tukey split in registers. */
 template <int R1, int R2, int S>
-__device__ __forceinline__ void dft_split(float2 *v)
+__host__ __device__ __forceinline__ void dft_split(float2 *v)
 {
   constexpr int R = R1 * R2;
   float2 t[R];
@@ -224,7 +185,7 @@ __device__ __forceinline__ void dft_split(float2 *v)
 #define CG_DFT_SPLIT(R, R1, R2)                                            \
   template <int S>                                                         \
   struct DFT<R, S> {                                                       \
-    __device__ __forceinline__ static void run(float2 *v) { dft_split<R1, R2, S>(v); } \
+    __host__ __device__ __forceinline__ static void run(float2 *v) { dft_split<R1, R2, S>(v); } \
   };
 CG_DFT_SPLIT(6, 3, 2)
 CG_DFT_SPLIT(8, 4, 2)
@@ -238,13 +199,13 @@ CG_DFT_SPLIT(64, 8, 8)
 
 /* Position read by stage input (i, q) of thread t. */
 template <int L, int R, int r>
-__device__ __forceinline__ int in_pos(int t, int i, int q)
+__host__ __device__ __forceinline__ int in_pos(int t, int i, int q)
 {
   return t + (L / R) * i + q * (L / r);
 }
 /* Position written by stage output (i, q) of thread t. */
 template <int L, int R, int r, int Ns>
-__device__ __forceinline__ int out_pos(int t, int i, int q)
+__host__ __device__ __forceinline__ int out_pos(int t, int i, int q)
 {
   int b = t + (L / R) * i;
   return (b / Ns) * Ns * r + (b % Ns) + q * Ns;
@@ -252,7 +213,7 @@ __device__ __forceinline__ int out_pos(int t, int i, int q)
 
 /* Twiddles and radix-r butterflies of one stage, data in v[i*r + q]. */
 template <int L, int R, int r, int Ns, int S>
-__device__ __forceinline__ void stage(float2 *v, int t, const float2 *__restrict__ twL)
+__host__ __device__ __forceinline__ void stage(float2 *v, int t, const float2 *__restrict__ twL)
 {
   constexpr int NB = R / r;
 #pragma unroll
@@ -262,7 +223,7 @@ __device__ __forceinline__ void stage(float2 *v, int t, const float2 *__restrict
       int k = b % Ns;
 #pragma unroll
       for (int q = 1; q < r; q++) {
-        float2 w = __ldg(&twL[(q * k) * (L / (Ns * r))]);
+        float2 w = CG_LDG(&twL[(q * k) * (L / (Ns * r))]);
         v[i * r + q] = cmulS<S>(v[i * r + q], w);
       }
     }

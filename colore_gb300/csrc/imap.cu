@@ -9,9 +9,13 @@
  *
  * A warp takes 32 consecutive cells of a row (one per lane), computes their
  * per-cell quantities, and then walks the concatenated list of all their
- * sub-samples 32 at a time, so that lanes stay busy whatever nsub is.  Lanes
- * whose samples land on the same (cell, shell, pixel) are merged with
- * __match_any_sync before the atomic updates.
+ * sub-samples 32 at a time, so that lanes stay busy whatever nsub is.  Hits
+ * are first counted in a per-warp shared-memory hash table keyed by
+ * (cell, shell, pixel): at low redshift a cell spans hundreds of pixels and
+ * each pixel receives tens of its sub-samples, so the table turns one global
+ * atomic pair per sub-sample into one per distinct key.  The table is
+ * flushed (data += temp * count, nadd += count) when it fills and at the end
+ * of each group of cells.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -22,21 +26,99 @@
 namespace {
 using namespace cg;
 
-constexpr int IW = 8; /* warps per block */
+constexpr int IW = 4;          /* warps per block            */
+constexpr int HT = 1024;       /* hash slots per warp        */
+constexpr int HFLUSH = 768;    /* flush once this many used  */
+constexpr unsigned long long EMPTY = ~0ull;
+constexpr unsigned long long IDXMASK = (1ull << 58) - 1;
+
+struct CellPar {
+  float x0, temp, drr, dxs, inv_nn, inv_ns;
+  int nsub, irad0;
+};
+
+struct WarpSm {
+  unsigned long long key[HT];
+  unsigned int cnt[HT];
+  unsigned short list[HT];
+  CellPar cell[32];
+  int nused;
+};
+
+__device__ __forceinline__ unsigned int hslot(unsigned long long k)
+{
+  unsigned long long h = k * 0x9E3779B97F4A7C15ull;
+  return (unsigned int)(h >> 54) & (HT - 1);
+}
+
+__device__ __forceinline__ void flush(WarpSm &w, int lane, const cg_imap_params &p)
+{
+  __syncwarp();
+  const int n = *(volatile int *)&w.nused;
+  for (int i = lane; i < n; i += 32) {
+    const int h = w.list[i];
+    const unsigned long long k = w.key[h];
+    const unsigned int c = w.cnt[h];
+    const int j = (int)(k >> 58);
+    const long long idx = (long long)(k & IDXMASK);
+    atomicAdd(&p.data[idx], CG_MUL(w.cell[j].temp, (float)c));
+    atomicAdd(&p.nadd[idx], (int)c);
+    w.key[h] = EMPTY;
+    w.cnt[h] = 0u;
+  }
+  __syncwarp();
+  if (lane == 0) w.nused = 0;
+  __syncwarp();
+}
+
+__device__ __forceinline__ void insert(WarpSm &w, unsigned long long key)
+{
+  unsigned int h = hslot(key);
+  volatile unsigned long long *vk = w.key;
+  for (int probe = 0; probe < HT; probe++) {
+    unsigned long long k = vk[h];
+    if (k == key) {
+      atomicAdd(&w.cnt[h], 1u);
+      return;
+    }
+    if (k == EMPTY) {
+      unsigned long long old = atomicCAS(&w.key[h], EMPTY, key);
+      if (old == EMPTY) {
+        atomicAdd(&w.cnt[h], 1u);
+        int pos = atomicAdd(&w.nused, 1);
+        w.list[pos] = (unsigned short)h;
+        return;
+      }
+      if (old == key) {
+        atomicAdd(&w.cnt[h], 1u);
+        return;
+      }
+    }
+    h = (h + 1) & (HT - 1);
+  }
+}
 
 __global__ void __launch_bounds__(IW * 32) k_imap(const float *__restrict__ dens, const float *__restrict__ phi,
                                                   cg_imap_params p)
 {
-  extern __shared__ float ssh[];
-  float *r0 = ssh, *rf = ssh + p.nr;
-  int *nsa = reinterpret_cast<int *>(ssh + 2 * p.nr);
+  extern __shared__ unsigned char sraw[];
+  WarpSm *ws = reinterpret_cast<WarpSm *>(sraw);
+  float *r0 = reinterpret_cast<float *>(sraw + IW * sizeof(WarpSm));
+  float *rf = r0 + p.nr;
+  int *nsa = reinterpret_cast<int *>(rf + p.nr);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  WarpSm &w = ws[wid];
   for (int i = threadIdx.x; i < p.nr; i += blockDim.x) {
     r0[i] = p.r0[i];
     rf[i] = p.rf[i];
     nsa[i] = p.nsub[i];
   }
+  for (int i = lane; i < HT; i += 32) {
+    w.key[i] = EMPTY;
+    w.cnt[i] = 0u;
+  }
+  if (lane == 0) w.nused = 0;
   __syncthreads();
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int N = p.box.N;
   const int nch = (N + 31) / 32;
   const long long ntask = (long long)nch * N * N;
@@ -48,11 +130,11 @@ __global__ void __launch_bounds__(IW * 32) k_imap(const float *__restrict__ dens
     const int iy = (int)(row % N), iz = (int)(row / N);
     const int ix = ch * 32 + lane;
     const float y0 = cg_cell_coord(iy, dx, p.box.p1), z0 = cg_cell_coord(iz, dx, p.box.p2);
-    float x0 = 0.0f, temp = 0.0f, drr = 0.0f, dxs = 0.0f;
-    int nsub = 0, irad0 = 0, n = 0;
+    CellPar cp = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0, 0};
+    int n = 0;
     if (ix < N) {
-      x0 = cg_cell_coord(ix, dx, p.box.p0);
-      const float rc = cg_norm3(x0, y0, z0);
+      cp.x0 = cg_cell_coord(ix, dx, p.box.p0);
+      const float rc = cg_norm3(cp.x0, y0, z0);
       const float tmean = bg(p.tz, p.g, rc);
       if (rc <= p.rmax_here && rc >= p.rmin_here && tmean > 0.0f) {
         const float bias = bg(p.bz, p.g, rc);
@@ -63,20 +145,26 @@ __global__ void __launch_bounds__(IW * 32) k_imap(const float *__restrict__ dens
         float v0 = CG_SUB(__ldg(&phi[pidx(xh, iy, iz, N)]), __ldg(&phi[pidx(xl, iy, iz, N)]));
         float v1 = CG_SUB(__ldg(&phi[pidx(ix, yh, iz, N)]), __ldg(&phi[pidx(ix, yl, iz, N)]));
         float v2 = CG_SUB(__ldg(&phi[pidx(ix, iy, zh, N)]), __ldg(&phi[pidx(ix, iy, zl, N)]));
-        float rvel = CG_MUL(p.factor_vel, cg_rvel(v0, v1, v2, x0, y0, z0, rc, p.box.idx));
-        drr = cg_imap_drsd(rvel, bg(p.v1, p.g, rc), bg(p.ih, p.g, rc));
+        float rvel = CG_MUL(p.factor_vel, cg_rvel(v0, v1, v2, cp.x0, y0, z0, rc, p.box.idx));
+        cp.drr = cg_imap_drsd(rvel, bg(p.v1, p.g, rc), bg(p.ih, p.g, rc));
         const float d = __ldg(&dens[pidx(ix, iy, iz, N)]);
-        temp = cg_imap_temp(tmean, d, bias, dnorm, p.bias_model);
-        irad0 = cg_shell_index(r0, rf, p.nr, rc, 0);
-        nsub = irad0 < 0 ? p.nsub_lo : (irad0 >= p.nr ? p.nsub_hi : nsa[irad0]);
-        if (nsub < 1 || nsub > 1024) {
+        cp.temp = cg_imap_temp(tmean, d, bias, dnorm, p.bias_model);
+        cp.irad0 = cg_shell_index(r0, rf, p.nr, rc, 0);
+        int ns = cp.irad0 < 0 ? p.nsub_lo : (cp.irad0 >= p.nr ? p.nsub_hi : nsa[cp.irad0]);
+        if (ns < 1 || ns > 1024) {
           atomicOr(p.err, ERR_IMAP_NSUB);
-          nsub = 0;
+          ns = 0;
         }
-        dxs = CG_DIV(dx, (float)nsub);
-        n = nsub * nsub * nsub;
+        cp.nsub = ns;
+        if (ns > 0) {
+          cp.dxs = CG_DIV(dx, (float)ns);
+          cp.inv_nn = 1.0f / (float)(ns * ns);
+          cp.inv_ns = 1.0f / (float)ns;
+          n = ns * ns * ns;
+        }
       }
     }
+    w.cell[lane] = cp;
     /* inclusive scan of the sample counts over the warp */
     int incl = n;
 #pragma unroll
@@ -86,6 +174,7 @@ __global__ void __launch_bounds__(IW * 32) k_imap(const float *__restrict__ dens
     }
     const int excl = incl - n;
     const int total = __shfl_sync(FULL, incl, 31);
+    __syncwarp();
     for (int base = 0; base < total; base += 32) {
       const int s = base + lane;
       /* owning lane j = number of lanes whose inclusive prefix is <= s */
@@ -96,41 +185,35 @@ __global__ void __launch_bounds__(IW * 32) k_imap(const float *__restrict__ dens
         if (v <= s) j += st;
       }
       if (j > 31) j = 31;
-      const int ns = __shfl_sync(FULL, nsub, j);
       const int ex = __shfl_sync(FULL, excl, j);
-      const float cx = __shfl_sync(FULL, x0, j);
-      const float ct = __shfl_sync(FULL, temp, j);
-      const float cd = __shfl_sync(FULL, drr, j);
-      const float cs = __shfl_sync(FULL, dxs, j);
-      const int cr = __shfl_sync(FULL, irad0, j);
-      unsigned long long key = ~0ull;
       if (s < total) {
-        const int l = s - ex;
-        const int nn = ns * ns;
-        const int izz = l / nn, rem = l - izz * nn;
-        const int iyy = rem / ns, ixx = rem - iyy * ns;
-        const float zc = cg_sub_centre(z0, izz, cs);
-        const float yc = cg_sub_centre(y0, iyy, cs);
-        const float xc = cg_sub_centre(cx, ixx, cs);
+        const CellPar c = w.cell[j];
+        const int l = s - ex, ns = c.nsub, nn = ns * ns;
+        int izz, iyy;
+        if (ns <= 128) { /* (l + 1/2)/nn is at least 1/(2nn) from an integer: exact */
+          izz = (int)(((float)l + 0.5f) * c.inv_nn);
+          const int rem = l - izz * nn;
+          iyy = (int)(((float)rem + 0.5f) * c.inv_ns);
+        } else {
+          izz = l / nn;
+          iyy = (l - izz * nn) / ns;
+        }
+        const int ixx = l - izz * nn - iyy * ns;
+        const float zc = cg_sub_centre(z0, izz, c.dxs);
+        const float yc = cg_sub_centre(y0, iyy, c.dxs);
+        const float xc = cg_sub_centre(c.x0, ixx, c.dxs);
         float r, cth, ph;
         cg_cart2sph(xc, yc, zc, &r, &cth, &ph);
-        const int ir = cg_shell_index(r0, rf, p.nr, CG_ADD(r, cd), cr);
+        const int ir = cg_shell_index(r0, rf, p.nr, CG_ADD(r, c.drr), c.irad0);
         if (ir >= 0 && ir < p.nr) {
           const long long pix = cg_ang2pix_ring(p.nside, cth, ph);
-          key = ((unsigned long long)j << 58) | (unsigned long long)((long long)ir * p.npix + pix);
+          insert(w, ((unsigned long long)j << 58) | (unsigned long long)((long long)ir * p.npix + pix));
         }
       }
-      const unsigned act = __ballot_sync(FULL, key != ~0ull);
-      if (key != ~0ull) {
-        const unsigned grp = __match_any_sync(act, key);
-        if (lane == __ffs(grp) - 1) {
-          const int c = __popc(grp);
-          const long long idx = (long long)(key & ((1ull << 58) - 1));
-          atomicAdd(&p.data[idx], CG_MUL(ct, (float)c));
-          atomicAdd(&p.nadd[idx], c);
-        }
-      }
+      __syncwarp();
+      if (*(volatile int *)&w.nused >= HFLUSH) flush(w, lane, p);
     }
+    flush(w, lane, p);
   }
 }
 
@@ -138,7 +221,7 @@ __global__ void __launch_bounds__(IW * 32) k_imap(const float *__restrict__ dens
 
 cudaError_t cg_imap_paint(cudaStream_t s, const float *dens, const float *phi, const cg_imap_params *p, int nsm)
 {
-  size_t smem = (size_t)p->nr * (2 * sizeof(float) + sizeof(int));
+  size_t smem = IW * sizeof(WarpSm) + (size_t)p->nr * (2 * sizeof(float) + sizeof(int));
   cudaError_t e = cudaFuncSetAttribute(k_imap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   long long ntask = (long long)((p->box.N + 31) / 32) * p->box.N * p->box.N;

@@ -364,9 +364,10 @@ static double rvel64(const cg_config *c, const double *p, int ix, int iy, int iz
   return 0.5 * (N / c->l_box) * (v0 * x0 / rr + v1 * y0 / rr + v2 * z0 / rr);
 }
 
-int or_imap64(const cg_config *c, int ipop, const double *dens, const double *npot, const double *nrm, double n0,
-              double nf, double *data, int *nadd)
+int or_imap64_part(const cg_config *c, int ipop, const double *dens, const double *npot, const double *nrm,
+                   double n0, double nf, int iz_stride, double *data, int *nadd, long long *nsamp)
 {
+  long long ns_tot = 0;
   const int N = c->n_grid, nr = c->imap_nr[ipop], nside = c->nside_imap[ipop];
   const long npix = 12L * nside * nside;
   double *r0 = malloc(nr * sizeof(double)), *rf = malloc(nr * sizeof(double));
@@ -392,7 +393,7 @@ int or_imap64(const cg_config *c, int ipop, const double *dens, const double *np
   memset(data, 0, (size_t)nr * npix * sizeof(double));
   memset(nadd, 0, (size_t)nr * npix * sizeof(int));
   const double *tz = c->imap_tz_arr[ipop], *bz = c->imap_bz_arr[ipop];
-  for (int iz = 0; iz < N; iz++) {
+  for (int iz = 0; iz < N; iz += iz_stride) {
     int irad = 0;
     double z0 = iz * dx - c->pos_obs[2];
     for (int iy = 0; iy < N; iy++) {
@@ -421,6 +422,7 @@ int or_imap64(const cg_config *c, int ipop, const double *dens, const double *np
   })
         irad = WALK(rc, irad);
         int nsh = irad < 0 ? ns[0] : (irad >= nr ? ns[nr - 1] : ns[irad]);
+        ns_tot += (long long)nsh * nsh * nsh;
         double dxs = dx / nsh;
         for (int izz = 0; izz < nsh; izz++)
           for (int iyy = 0; iyy < nsh; iyy++)
@@ -442,7 +444,77 @@ int or_imap64(const cg_config *c, int ipop, const double *dens, const double *np
   free(rf);
   free(ns);
   free(ord);
+  if (nsamp) *nsamp = ns_tot;
   return 0;
+}
+
+int or_imap64(const cg_config *c, int ipop, const double *dens, const double *npot, const double *nrm, double n0,
+              double nf, double *data, int *nadd)
+{
+  return or_imap64_part(c, ipop, dens, npot, nrm, n0, nf, 1, data, nadd, NULL);
+}
+
+/* Number of sub-samples imap_set_cartesian_single draws for species ipop at
+ * the configuration's grid size (cells in the shells' range with T > 0,
+ * times nsub^3), from the geometry alone. */
+long long or_imap_samples(const cg_config *c, int ipop)
+{
+  const int N = c->n_grid, nr = c->imap_nr[ipop], nside = c->nside_imap[ipop];
+  const long npix = 12L * nside * nside;
+  double r0min = 1e300, rfmax = -1e300;
+  double *r0 = malloc(nr * sizeof(double)), *rf = malloc(nr * sizeof(double));
+  int *ns = malloc(nr * sizeof(int));
+  int *ord = malloc(nr * sizeof(int));
+  for (int i = 0; i < nr; i++) ord[i] = i;
+  for (int i = 1; i < nr; i++)
+    for (int j = i; j > 0 && c->imap_r0[ipop][ord[j]] < c->imap_r0[ipop][ord[j - 1]]; j--) {
+      int t = ord[j];
+      ord[j] = ord[j - 1];
+      ord[j - 1] = t;
+    }
+  for (int i = 0; i < nr; i++) {
+    r0[i] = c->imap_r0[ipop][ord[i]];
+    rf[i] = c->imap_rf[ipop][ord[i]];
+  }
+  const double dx = c->l_box / N, ps = sqrt(4 * M_PI / npix);
+  for (int i = 0; i < nr; i++) {
+    double vol = (rf[i] * rf[i] * rf[i] - r0[i] * r0[i] * r0[i]) * ps * ps / 3;
+    ns[i] = (int)(dx / fmin(pow(vol, 0.333333), fmin(r0[i] * ps, rf[i] - r0[i])) + 0.5) + 1;
+    if (r0[i] < r0min) r0min = r0[i];
+    if (rf[i] > rfmax) rfmax = rf[i];
+  }
+  const double rmin = r0[0] - 20., rmax = rf[nr - 1] + 20.;
+  const double *tz = c->imap_tz_arr[ipop];
+  long long tot = 0;
+#pragma omp parallel for schedule(dynamic) reduction(+ : tot)
+  for (int iz = 0; iz < N; iz++) {
+    double z0 = iz * dx - c->pos_obs[2];
+    int q = 0;
+    for (int iy = 0; iy < N; iy++) {
+      double y0 = iy * dx - c->pos_obs[1];
+      for (int ix = 0; ix < N; ix++) {
+        double x0 = ix * dx - c->pos_obs[0];
+        double rc = sqrt(x0 * x0 + y0 * y0 + z0 * z0);
+        if (!(rc <= rmax && rc >= rmin)) continue;
+        if (!(bg(c, tz, 0, 0, rc) > 0)) continue;
+        for (int it = 0; it < 2 * nr + 4; it++) {
+          if (q == -1 || q == nr) break;
+          if (rc < r0[q]) q--;
+          else if (rc >= rf[q]) q++;
+          else break;
+        }
+        int nsh = q < 0 ? ns[0] : (q >= nr ? ns[nr - 1] : ns[q]);
+        if (q < 0) q = 0;
+        if (q >= nr) q = nr - 1;
+        tot += (long long)nsh * nsh * nsh;
+      }
+    }
+  }
+  free(r0);
+  free(rf);
+  free(ns);
+  free(ord);
+  return tot;
 }
 
 static void pix2vec_nest64(long nside, long ip, double v[3])
@@ -460,7 +532,7 @@ static void pix2vec_nest64(long nside, long ip, double v[3])
   v[2] = z;
 }
 
-int or_kappa64(const cg_config *c, const double *p, double *map)
+int or_kappa64_part(const cg_config *c, const double *p, int pix_stride, double *map)
 {
   const int N = c->n_grid, np = c->n_kappa, nside = c->nside_kappa;
   const long npix = 12L * nside * nside;
@@ -490,7 +562,7 @@ int or_kappa64(const cg_config *c, const double *p, double *map)
     f2[i] = rm * rm * pg * dr;
   }
 #pragma omp parallel for schedule(static)
-  for (long ip = 0; ip < npix; ip++) {
+  for (long ip = 0; ip < npix; ip += pix_stride) {
     double u[3];
     pix2vec_nest64(nside, ip, u);
     double cth = u[2] > 1 ? 1 : (u[2] < -1 ? -1 : u[2]), sth = sqrt((1 - cth) * (1 + cth)), cph = 1, sph = 0;
@@ -536,6 +608,8 @@ int or_kappa64(const cg_config *c, const double *p, double *map)
   return 0;
 }
 
+int or_kappa64(const cg_config *c, const double *p, double *map) { return or_kappa64_part(c, p, 1, map); }
+
 /* Poisson deviate by inversion in double from the same Philox cell stream. */
 static int poisson64(double lam, uint32_t k0, uint32_t k1, long long cid)
 {
@@ -550,6 +624,16 @@ static int poisson64(double lam, uint32_t k0, uint32_t k1, long long cid)
     if (p == 0 && F < u) break;
   }
   return k;
+}
+
+long long or_poisson_total64(const cg_config *c, int ipop, const double *lam)
+{
+  const size_t ncell = (size_t)c->n_grid * c->n_grid * c->n_grid;
+  const uint32_t k0 = (uint32_t)c->seed, k1 = (uint32_t)(c->seed >> 32) ^ (CG_STREAM_POIS + (uint32_t)ipop);
+  long long t = 0;
+#pragma omp parallel for schedule(static) reduction(+ : t)
+  for (size_t i = 0; i < ncell; i++) t += poisson64(lam[i], k0, k1, (long long)i);
+  return t;
 }
 
 int or_run_mock64(const cg_config *c, int nthreads_hint, long long *nsrc_total, double *checksum)

@@ -48,6 +48,11 @@ int or_lambda64(const cg_config *cfg, int ipop, const double *dens, const double
 int or_kappa64(const cg_config *cfg, const double *npot, double *map);
 int or_imap64(const cg_config *cfg, int ipop, const double *dens, const double *npot, const double *normtab,
               double n0, double nf, double *data, int *nadd);
+int or_imap64_part(const cg_config *cfg, int ipop, const double *dens, const double *npot, const double *normtab,
+                   double n0, double nf, int iz_stride, double *data, int *nadd, long long *nsamp);
+long long or_imap_samples(const cg_config *cfg, int ipop);
+int or_kappa64_part(const cg_config *cfg, const double *npot, int pix_stride, double *map);
+long long or_poisson_total64(const cg_config *cfg, int ipop, const double *lam);
 int or_run_mock64(const cg_config *cfg, int nthreads_hint, long long *nsrc_total, double *checksum);
 
 /* ---- dev32 (or_dev32.c) ---- */
