@@ -18,6 +18,7 @@ rank): the path has no exchange step on one node.
 """
 import argparse
 import json
+import numpy as np
 import os
 import subprocess
 import sys
@@ -252,23 +253,85 @@ def run_ours(args):
     print(json.dumps(out))
 
 
+def _kappa_steps(cfg):
+    """Ray steps of kappa_get_beam_properties (kappa.c:146-162) for cfg."""
+    nr = cfg.n_grid // 2
+    dr = cfg.r_max / nr
+    rmax = max(float(np.float32(cfg.kappa_r[i])) for i in range(cfg.n_kappa))
+    last = min(int(rmax / dr + 0.5), nr - 1)
+    return 12 * cfg.nside_kappa ** 2 * (last + 1)
+
+
 def cpu_baseline(args, quick=False):
-    """FP64 oracle (the reference's arithmetic, OpenMP) on a bounded sample:
-    the same configuration at a reduced grid, reported as cells/s."""
+    """The FP64 oracle (the reference's arithmetic; OpenMP on every host core)
+    timed stage by stage on a sample of the workload and scaled to it:
+      field/1LPT FFT stages at cpu_n^3, scaled by cells x log2 N;
+      density, bins and Poisson stages at cpu_n^3, scaled by cells;
+      intensity maps: every iz_stride-th plane of the cpu_n^3 grid gives the
+        sub-samples/s, times the exact sub-sample count of the full grid;
+      kappa: every pix_stride-th pixel gives the ray steps/s, times the full
+        grid's ray steps."""
+    import numpy as np
     import colore_gb300 as cg
     from colore_gb300 import inputs
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
-    n = args.cpu_n
-    spec = config_spec(args.config, n)
+    full = config_spec(args.config, args.n)
+    ns_ = args.cpu_n
     d = tempfile.mkdtemp(prefix="colore_cpu_")
-    prm = cg.Params(inputs.write_inputs(d, spec))
-    t0 = time.perf_counter()
-    nsrc, _ = orc.run_mock64(prm.config)
-    t = time.perf_counter() - t0
+    prm_f = cg.Params(inputs.write_inputs(os.path.join(d, "full"), full))
+    cf = prm_f.config
+    nf = cf.n_grid
+    prm = cg.Params(inputs.write_inputs(os.path.join(d, "sample"), config_spec(args.config, ns_)))
+    c = prm.config
+    T = {}
+    t = time.perf_counter()
+    dens, npot, st = orc.field64(c)
+    T["field"] = time.perf_counter() - t
+    t = time.perf_counter()
+    if c.dens_type == 1:
+        dens, _ = orc.lpt64(c, dens)
+    else:
+        dens = orc.density64(c, dens, st[3])
+    T["density"] = time.perf_counter() - t
+    t = time.perf_counter()
+    tabs, e0f, nz = orc.norm_tables64(c, dens)
+    T["bins"] = time.perf_counter() - t
+    t = time.perf_counter()
+    nsrc = 0
+    for i in range(c.n_srcs):
+        lam = orc.lambda64(c, i, dens, tabs[i], e0f[i])
+        nsrc += orc.poisson_total64(c, i, lam)
+    T["sources"] = time.perf_counter() - t
+    R = (nf / ns_) ** 3
+    lg = np.log2(nf) / np.log2(ns_)
+    parts = {"field": T["field"] * R * lg, "density": T["density"] * R * (lg if c.dens_type == 1 else 1),
+             "bins": T["bins"] * R, "sources": T["sources"] * R}
+    est = sum(parts.values())
+    if c.n_imap:
+        stride = max(1, ns_ // 16)
+        t = time.perf_counter()
+        done = 0
+        for i in range(c.n_imap):
+            done += orc.imap64_part(c, i, dens, npot, tabs[c.n_srcs + i], e0f[c.n_srcs + i], stride)
+        ti = time.perf_counter() - t
+        need = sum(orc.imap_samples(cf, i) for i in range(cf.n_imap))
+        parts["imap"] = need / max(done, 1) * ti
+        est += parts["imap"]
+    if c.do_kappa:
+        ps = 64
+        t = time.perf_counter()
+        orc.kappa64_part(c, npot, ps)
+        tk = time.perf_counter() - t
+        parts["kappa"] = _kappa_steps(cf) / (_kappa_steps(c) / ps) * tk
+        est += parts["kappa"]
     cores = os.cpu_count()
-    return {"value": n ** 3 / t, "unit": "cells/s", "cores": cores, "kind": "port",
-            "sample": "%s at %d^3 (full pipeline, FP64 oracle, %d OpenMP threads), %.1f s" % (args.config, n, cores, t)}
+    return {"value": nf ** 3 / est, "unit": "cells/s", "cores": cores, "kind": "port",
+            "sample": ("FP64 oracle of the reference path, %d OpenMP threads: stages timed at %d^3 and scaled to "
+                       "%d^3 (FFT by N^3 log N, cell stages by N^3), imap by sub-sample count, kappa by ray steps; "
+                       "estimated %.1f s per full step") % (cores, ns_, nf, est),
+            "stage_s_full_step": {k: round(v, 3) for k, v in parts.items()},
+            "stage_s_sample": {k: round(v, 4) for k, v in T.items()}}
 
 
 def run_reference(args):
@@ -300,7 +363,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c4")
     ap.add_argument("--n", type=int, default=0, help="override the grid size")
-    ap.add_argument("--cpu-n", type=int, default=128)
+    ap.add_argument("--cpu-n", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -174,8 +174,11 @@ CG_HD int64_t cg_ang2pix_ring(int64_t nside64, float cth, float phi)
     int kshift = 1 - (ir & 1);
     int ip = (jp + jm - nside + kshift + 1) / 2;
     int m = 4 * nside;
-    ip = ip % m;
-    if (ip < 0) ip += m;
+    if ((nside & (nside - 1)) == 0) ip &= m - 1; /* same as the modulo below */
+    else {
+      ip = ip % m;
+      if (ip < 0) ip += m;
+    }
     return (int64_t)(nside * (nside - 1) * 2 + (ir - 1) * 4 * nside + ip);
   } else {
     float tp = CG_SUB(tt, (float)(int)tt);
@@ -439,6 +442,26 @@ CG_HD float cg_imap_temp(float tmean, float d, float bias, float dnorm, int mode
   return CG_MUL(CG_MUL(tmean, cg_bias_model(d, bias, model)), dnorm);
 }
 CG_HD float cg_imap_drsd(float rvel, float v1, float ih) { return CG_MUL(CG_MUL(rvel, v1), ih); }
+
+/* One intensity-map sub-sample of imap.c:210-231 at (x, y, z), with
+ * yz2 = y^2 + z^2 shared by the samples of an x-line: returns the shell
+ * index (or -1 / nr outside the shells) and the RING pixel.  The radius is
+ * sqrt(x^2 + yz2); cos(theta) = z/r and phi = atan2(y, x) as in cart2sph. */
+CG_HD int cg_imap_sample(float x, float y, float z, float yz2, float drr, const float *r0, const float *rf, int nr,
+                         int start, int64_t nside, int64_t *pix)
+{
+  const float r = CG_SQRT(CG_ADD(CG_MUL(x, x), yz2));
+  const int ir = cg_shell_index(r0, rf, nr, CG_ADD(r, drr), start);
+  if (ir < 0 || ir >= nr) return ir;
+  float cth = 1.0f, ph = 0.0f;
+  if (r != 0.0f) {
+    cth = CG_DIV(z, r);
+    ph = cg_atan2f(y, x);
+    if (ph < 0.0f) ph = CG_ADD(ph, CG_TWOPI_F);
+  }
+  *pix = cg_ang2pix_ring(nside, cth, ph);
+  return ir;
+}
 
 /* NGP cell along a ray, interpolate_from_grid NGP branch (beaming.c:148-157) */
 CG_HD int cg_ngp_cell(float rm, float u, float po, float idx, int N)

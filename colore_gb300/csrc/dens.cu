@@ -8,9 +8,12 @@
  *                    lognormal (or clipped, or 1LPT "rho-1") transform in
  *                    place and accumulates, per redshift bin, the cell count,
  *                    the summed redshift and the summed bias_model of every
- *                    tracer.  A warp owns 64 consecutive cells of a row; lanes
- *                    sharing a bin are reduced with shuffles, and each warp
- *                    keeps private FP64 bins in shared memory.
+ *                    tracer.  A warp owns 32 consecutive cells of a row;
+ *                    lanes sharing a bin are reduced with shuffles (one pass
+ *                    when the 32 cells share a bin, the common case) and lane
+ *                    0 adds the sums to the warp's private FP64 bins in shared
+ *                    memory, so no atomics are needed until the per-block
+ *                    totals go to global memory.
  *  k_lpt_cic       : 1LPT particle positions (density.c:473-501) and their
  *                    cloud-in-cell deposit (density.c:64-105).
  */
@@ -57,39 +60,13 @@ __global__ void k_moments_final(const double2 *__restrict__ part, size_t n, doub
 constexpr int MAXT = 8;      /* tracers per bins launch */
 constexpr int BINS_WARPS = 8;
 
-/* Segmented warp reduction by bin of (count, z, bias sums); lane 0 adds the
- * totals to the warp's private FP64 bins (no atomics: one writer). */
-__device__ __forceinline__ void warp_bins_add(double *mybins, int W, int nt, int lane, int bin, float cnt, float zs,
-                                              const float *bs)
+/* Warp reduction of v over the lanes whose mask bit is set (others add 0). */
+__device__ __forceinline__ float wsum(float v, bool mine)
 {
-  unsigned todo = __ballot_sync(0xffffffffu, bin >= 0);
-  while (todo) {
-    const int leader = __ffs(todo) - 1;
-    const int lb = __shfl_sync(0xffffffffu, bin, leader);
-    const bool mine = (bin == lb);
-    float c = mine ? cnt : 0.0f, zsum = mine ? zs : 0.0f;
-    float bsum[MAXT];
+  float x = mine ? v : 0.0f;
 #pragma unroll
-    for (int t = 0; t < MAXT; t++) bsum[t] = mine ? bs[t] : 0.0f;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      c += __shfl_xor_sync(0xffffffffu, c, o);
-      zsum += __shfl_xor_sync(0xffffffffu, zsum, o);
-#pragma unroll
-      for (int t = 0; t < MAXT; t++)
-        if (t < nt) bsum[t] += __shfl_xor_sync(0xffffffffu, bsum[t], o);
-    }
-    if (lane == 0) {
-      double *d = mybins + (size_t)lb * W;
-      d[0] += (double)c;
-      d[1] += (double)zsum;
-#pragma unroll
-      for (int t = 0; t < MAXT; t++)
-        if (t < nt) d[2 + t] += (double)bsum[t];
-    }
-    todo &= ~__ballot_sync(0xffffffffu, mine);
-  }
-  __syncwarp();
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
 }
 
 __global__ void __launch_bounds__(BINS_WARPS * 32) k_dens_bins(float *grid, cg_bins_params p)
@@ -101,55 +78,65 @@ __global__ void __launch_bounds__(BINS_WARPS * 32) k_dens_bins(float *grid, cg_b
   for (int i = lane; i < nz * W; i += 32) mybins[i] = 0.0;
   __syncwarp();
   const int N = p.box.N;
-  const int nseg_row = (N + 63) / 64;
+  const int nseg_row = (N + 31) / 32;
   const long long nseg = (long long)nseg_row * N * N;
   const float s2 = p.sigma2f ? *p.sigma2f : 0.0f;
+  const bool need_d1 = (p.mode == CG_DMODE_LGNR || p.mode == CG_DMODE_CLIP);
   const long long gw = (long long)blockIdx.x * BINS_WARPS + wid;
   const long long nw = (long long)gridDim.x * BINS_WARPS;
   for (long long seg = gw; seg < nseg; seg += nw) {
     const int sr = (int)(seg % nseg_row);
     const long long row = seg / nseg_row;
     const int iy = (int)(row % N), iz = (int)(row / N);
-    const int ix = sr * 64 + 2 * lane;
-    int bb[2] = {-1, -1};
-    float zz[2] = {0.0f, 0.0f}, bs[2][MAXT];
+    const int ix = sr * 32 + lane;
+    int bin = -1;
+    float zz = 0.0f, bs[MAXT];
 #pragma unroll
-    for (int t = 0; t < MAXT; t++) bs[0][t] = bs[1][t] = 0.0f;
+    for (int t = 0; t < MAXT; t++) bs[t] = 0.0f;
     if (ix < N) {
-      float2 *ptr = reinterpret_cast<float2 *>(grid + pidx(ix, iy, iz, N));
-      float2 dv = *ptr;
+      float *ptr = grid + pidx(ix, iy, iz, N);
+      float d = *ptr;
+      const float x0 = cg_cell_coord(ix, p.box.dx, p.box.p0);
       const float y0 = cg_cell_coord(iy, p.box.dx, p.box.p1), z0 = cg_cell_coord(iz, p.box.dx, p.box.p2);
-      float dd[2] = {dv.x, dv.y};
+      const float r = cg_norm3(x0, y0, z0);
+      if (p.mode != CG_DMODE_NONE) {
+        d = cg_dens_transform(p.mode, d, need_d1 ? bg(p.d1, p.g, r) : 0.0f, s2);
+        *ptr = d;
+      }
+      if (nz > 0) {
+        const float z = bg(p.zt, p.g, r);
+        const int b = (int)CG_MUL(z, p.idz) + 1;
+        if (b >= 0 && b < nz) {
+          bin = b;
+          zz = z;
 #pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const float x0 = cg_cell_coord(ix + h, p.box.dx, p.box.p0);
-        const float r = cg_norm3(x0, y0, z0);
-        if (p.mode != CG_DMODE_NONE) dd[h] = cg_dens_transform(p.mode, dd[h], bg(p.d1, p.g, r), s2);
-        if (nz > 0) {
-          const float z = bg(p.zt, p.g, r);
-          const int b = (int)CG_MUL(z, p.idz) + 1;
-          if (b >= 0 && b < nz) {
-            bb[h] = b;
-            zz[h] = z;
-#pragma unroll
-            for (int t = 0; t < MAXT; t++)
-              if (t < nt) bs[h][t] = cg_bias_model(dd[h], bg(p.bz[t], p.g, r), p.bias_model);
-          }
+          for (int t = 0; t < MAXT; t++)
+            if (t < nt) bs[t] = cg_bias_model(d, bg(p.bz[t], p.g, r), p.bias_model);
         }
       }
-      if (p.mode != CG_DMODE_NONE) *ptr = make_float2(dd[0], dd[1]);
     }
     if (nz == 0) continue;
-    /* both cells of a lane share a bin except at bin edges */
-    if (__all_sync(0xffffffffu, bb[0] == bb[1])) {
-      float b2[MAXT];
+    /* segmented reduction by bin; one pass when the 32 cells share a bin */
+    unsigned todo = __ballot_sync(0xffffffffu, bin >= 0);
+    while (todo) {
+      const int lb = __shfl_sync(0xffffffffu, bin, __ffs(todo) - 1);
+      const bool mine = (bin == lb);
+      const unsigned grp = __ballot_sync(0xffffffffu, mine);
+      const float zsum = wsum(zz, mine);
+      float bsum[MAXT];
 #pragma unroll
-      for (int t = 0; t < MAXT; t++) b2[t] = bs[0][t] + bs[1][t];
-      warp_bins_add(mybins, W, nt, lane, bb[0], bb[0] >= 0 ? 2.0f : 0.0f, zz[0] + zz[1], b2);
-    } else {
-      warp_bins_add(mybins, W, nt, lane, bb[0], 1.0f, zz[0], bs[0]);
-      warp_bins_add(mybins, W, nt, lane, bb[1], 1.0f, zz[1], bs[1]);
+      for (int t = 0; t < MAXT; t++) bsum[t] = (t < nt) ? wsum(bs[t], mine) : 0.0f;
+      if (lane == 0) {
+        double *dd = mybins + (size_t)lb * W;
+        dd[0] += (double)__popc(grp);
+        dd[1] += (double)zsum;
+#pragma unroll
+        for (int t = 0; t < MAXT; t++)
+          if (t < nt) dd[2 + t] += (double)bsum[t];
+      }
+      todo &= ~grp;
     }
+    __syncwarp();
   }
   __syncthreads();
   /* combine the warps' bins in fixed order, then one global update per block */
@@ -226,7 +213,7 @@ cudaError_t cg_dens_bins(cudaStream_t s, float *grid, const cg_bins_params *p, i
   size_t smem = (size_t)BINS_WARPS * p->nz * (2 + p->nt) * sizeof(double);
   cudaError_t e = cudaFuncSetAttribute(k_dens_bins, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  long long nseg = (long long)((p->box.N + 63) / 64) * p->box.N * p->box.N;
+  long long nseg = (long long)((p->box.N + 31) / 32) * p->box.N * p->box.N;
   long long blocks = (nseg + BINS_WARPS - 1) / BINS_WARPS;
   long long cap = (long long)nsm * 8;
   if (blocks > cap) blocks = cap;

@@ -43,7 +43,8 @@ using namespace cg;
 constexpr int N = CG_N;
 constexpr int NH = N / 2 + 1;
 using PL = Plan<N>;
-constexpr int P = N / PL::CR;       /* threads per column transform */
+constexpr int P = N / PL::CR;       /* threads per column transform (y pass)      */
+constexpr int PF = N / PL::FR;      /* threads per column transform (fill + z)    */
 constexpr int LH = N / 2;           /* row transform length         */
 constexpr int PR = LH / PL::RR;     /* threads per row transform    */
 constexpr int ROWS = (NH > LH + LH / 32 + 1) ? NH : (LH + LH / 32 + 1); /* smem per row */
@@ -132,7 +133,7 @@ __device__ __forceinline__ void gen_fields(const FillParams &p, int kx, int ky, 
 
 /* Pass 1: fill + z transform of F fields.  grid = (ceil(NH/TX), N). */
 template <int F, int TX>
-__global__ void __launch_bounds__(TX *P) k_fill_z(float2 *o0, float2 *o1, float2 *o2, FillParams p,
+__global__ void __launch_bounds__(TX *PF) k_fill_z(float2 *o0, float2 *o1, float2 *o2, FillParams p,
                                                   const float2 *__restrict__ twN)
 {
   extern __shared__ float2 smem[];
@@ -161,7 +162,7 @@ __global__ void __launch_bounds__(TX *P) k_fill_z(float2 *o0, float2 *o1, float2
     auto st = [&](int pos, float2 v) {
       if (ok) o[((size_t)pos * N + ky) * NH + kx] = v;
     };
-    cgfft::transform<N, PL::CR, PL::C0, PL::C1, PL::C2, 1>(t, twN, ld, st, sm);
+    cgfft::transform<N, PL::FR, PL::F0, PL::F1, PL::F2, 1>(t, twN, ld, st, sm);
     __syncthreads();
   }
 }
@@ -278,7 +279,7 @@ extern "C" cudaError_t CG_CAT(cg_field_gauss_, CG_N)(const cg_field_launch *L)
   if ((e = prep(k_row_c2r<true>, sm3)) != cudaSuccess) return e;
   if ((e = prep(k_row_c2r<false>, sm3)) != cudaSuccess) return e;
   dim3 g1((NH + TX2 - 1) / TX2, N);
-  k_fill_z<2, TX2><<<g1, TX2 * P, sm1, L->stream>>>(L->f[0], L->f[1], nullptr, L->fill, L->twN);
+  k_fill_z<2, TX2><<<g1, TX2 * PF, sm1, L->stream>>>(L->f[0], L->f[1], nullptr, L->fill, L->twN);
   dim3 g2((NH + TXY - 1) / TXY, N, 2);
   k_col_y<TXY><<<g2, TXY * P, sm2, L->stream>>>(L->f[0], L->f[1], nullptr, L->twN);
   dim3 g3((unsigned)((size_t)N * N / PL::RB), 1);
@@ -302,7 +303,7 @@ extern "C" cudaError_t CG_CAT(cg_field_lpt_, CG_N)(const cg_field_launch *L)
   if ((e = prep(k_col_y<TXY>, sm2)) != cudaSuccess) return e;
   if ((e = prep(k_row_c2r<false>, sm3)) != cudaSuccess) return e;
   dim3 g1((NH + TX3 - 1) / TX3, N);
-  k_fill_z<3, TX3><<<g1, TX3 * P, sm1, L->stream>>>(L->f[0], L->f[1], L->f[2], L->fill, L->twN);
+  k_fill_z<3, TX3><<<g1, TX3 * PF, sm1, L->stream>>>(L->f[0], L->f[1], L->f[2], L->fill, L->twN);
   dim3 g2((NH + TXY - 1) / TXY, N, 3);
   k_col_y<TXY><<<g2, TXY * P, sm2, L->stream>>>(L->f[0], L->f[1], L->f[2], L->twN);
   dim3 g3((unsigned)((size_t)N * N / PL::RB), 3);

@@ -7,15 +7,18 @@
  * it is split into nsub^3 sub-cells whose centres are placed in a shell (by
  * r + dr_rsd) and a RING pixel, where temp is added and a hit counted.
  *
- * A warp takes 32 consecutive cells of a row (one per lane), computes their
- * per-cell quantities, and then walks the concatenated list of all their
- * sub-samples 32 at a time, so that lanes stay busy whatever nsub is.  Hits
- * are first counted in a per-warp shared-memory hash table keyed by
+ * A warp takes 32 consecutive cells of a row (one per lane) and computes
+ * their per-cell quantities; its lanes then take the x-lines of sub-samples
+ * (nsub^2 per cell, nsub samples each) of all 32 cells, so that lanes stay
+ * busy whatever nsub is.  Along a line y, z and y^2+z^2 are computed once
+ * and consecutive samples landing on the same (shell, pixel) are merged in
+ * registers.  Those runs go to a per-warp shared-memory hash table keyed by
  * (cell, shell, pixel): at low redshift a cell spans hundreds of pixels and
  * each pixel receives tens of its sub-samples, so the table turns one global
  * atomic pair per sub-sample into one per distinct key.  The table is
- * flushed (data += temp * count, nadd += count) when it fills and at the end
- * of each group of cells.
+ * flushed (data += temp * count, nadd += count) when half full and at the
+ * end of each group of cells; runs that find it nearly full go straight to
+ * global memory.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -26,9 +29,10 @@
 namespace {
 using namespace cg;
 
-constexpr int IW = 4;          /* warps per block            */
-constexpr int HT = 1024;       /* hash slots per warp        */
-constexpr int HFLUSH = 768;    /* flush once this many used  */
+constexpr int IW = 4;          /* warps per block                        */
+constexpr int HT = 1024;       /* hash slots per warp                    */
+constexpr int HFLUSH = 512;    /* flush after a step with this many used */
+constexpr int HCAP = 896;      /* no new keys beyond this many           */
 constexpr unsigned long long EMPTY = ~0ull;
 constexpr unsigned long long IDXMASK = (1ull << 58) - 1;
 
@@ -71,31 +75,36 @@ __device__ __forceinline__ void flush(WarpSm &w, int lane, const cg_imap_params 
   __syncwarp();
 }
 
-__device__ __forceinline__ void insert(WarpSm &w, unsigned long long key)
+/* Add c hits of key; new keys go to global memory once the table is full. */
+__device__ __forceinline__ void insert(WarpSm &w, unsigned long long key, unsigned int c, const cg_imap_params &p)
 {
   unsigned int h = hslot(key);
   volatile unsigned long long *vk = w.key;
   for (int probe = 0; probe < HT; probe++) {
     unsigned long long k = vk[h];
     if (k == key) {
-      atomicAdd(&w.cnt[h], 1u);
+      atomicAdd(&w.cnt[h], c);
       return;
     }
     if (k == EMPTY) {
+      if (*(volatile int *)&w.nused >= HCAP) break;
       unsigned long long old = atomicCAS(&w.key[h], EMPTY, key);
       if (old == EMPTY) {
-        atomicAdd(&w.cnt[h], 1u);
+        atomicAdd(&w.cnt[h], c);
         int pos = atomicAdd(&w.nused, 1);
         w.list[pos] = (unsigned short)h;
         return;
       }
       if (old == key) {
-        atomicAdd(&w.cnt[h], 1u);
+        atomicAdd(&w.cnt[h], c);
         return;
       }
     }
     h = (h + 1) & (HT - 1);
   }
+  const long long idx = (long long)(key & IDXMASK);
+  atomicAdd(&p.data[idx], CG_MUL(w.cell[(int)(key >> 58)].temp, (float)c));
+  atomicAdd(&p.nadd[idx], (int)c);
 }
 
 __global__ void __launch_bounds__(IW * 32) k_imap(const float *__restrict__ dens, const float *__restrict__ phi,
@@ -165,14 +174,15 @@ __global__ void __launch_bounds__(IW * 32) k_imap(const float *__restrict__ dens
       }
     }
     w.cell[lane] = cp;
-    /* inclusive scan of the sample counts over the warp */
-    int incl = n;
+    /* inclusive scan of the line counts (nsub^2 per cell) over the warp */
+    const int nl = cp.nsub * cp.nsub;
+    int incl = n > 0 ? nl : 0;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       int t = __shfl_up_sync(FULL, incl, o);
       if (lane >= o) incl += t;
     }
-    const int excl = incl - n;
+    const int excl = incl - (n > 0 ? nl : 0);
     const int total = __shfl_sync(FULL, incl, 31);
     __syncwarp();
     for (int base = 0; base < total; base += 32) {
@@ -188,27 +198,31 @@ __global__ void __launch_bounds__(IW * 32) k_imap(const float *__restrict__ dens
       const int ex = __shfl_sync(FULL, excl, j);
       if (s < total) {
         const CellPar c = w.cell[j];
-        const int l = s - ex, ns = c.nsub, nn = ns * ns;
-        int izz, iyy;
-        if (ns <= 128) { /* (l + 1/2)/nn is at least 1/(2nn) from an integer: exact */
-          izz = (int)(((float)l + 0.5f) * c.inv_nn);
-          const int rem = l - izz * nn;
-          iyy = (int)(((float)rem + 0.5f) * c.inv_ns);
-        } else {
-          izz = l / nn;
-          iyy = (l - izz * nn) / ns;
-        }
-        const int ixx = l - izz * nn - iyy * ns;
+        const int l = s - ex, ns = c.nsub;
+        /* (l + 1/2)/ns is at least 1/(2 ns) from an integer: exact for ns <= 128 */
+        const int izz = ns <= 128 ? (int)(((float)l + 0.5f) * c.inv_ns) : l / ns;
+        const int iyy = l - izz * ns;
         const float zc = cg_sub_centre(z0, izz, c.dxs);
         const float yc = cg_sub_centre(y0, iyy, c.dxs);
-        const float xc = cg_sub_centre(c.x0, ixx, c.dxs);
-        float r, cth, ph;
-        cg_cart2sph(xc, yc, zc, &r, &cth, &ph);
-        const int ir = cg_shell_index(r0, rf, p.nr, CG_ADD(r, c.drr), c.irad0);
-        if (ir >= 0 && ir < p.nr) {
-          const long long pix = cg_ang2pix_ring(p.nside, cth, ph);
-          insert(w, ((unsigned long long)j << 58) | (unsigned long long)((long long)ir * p.npix + pix));
+        const float yz2 = CG_ADD(CG_MUL(yc, yc), CG_MUL(zc, zc));
+        const unsigned long long jk = (unsigned long long)j << 58;
+        unsigned long long cur = EMPTY;
+        unsigned int run = 0;
+        for (int ixx = 0; ixx < ns; ixx++) {
+          const float xc = cg_sub_centre(c.x0, ixx, c.dxs);
+          int64_t pix = 0;
+          const int ir = cg_imap_sample(xc, yc, zc, yz2, c.drr, r0, rf, p.nr, c.irad0, p.nside, &pix);
+          if (ir < 0 || ir >= p.nr) continue;
+          const unsigned long long key = jk | (unsigned long long)((long long)ir * p.npix + pix);
+          if (key == cur) {
+            run++;
+          } else {
+            if (run) insert(w, cur, run, p);
+            cur = key;
+            run = 1;
+          }
         }
+        if (run) insert(w, cur, run, p);
       }
       __syncwarp();
       if (*(volatile int *)&w.nused >= HFLUSH) flush(w, lane, p);

@@ -391,13 +391,13 @@ int or_imap32(const cg_config *cfg, int ipop, const float *dens, const float *np
           float zc = cg_sub_centre(z0, izz, dxs);
           for (int iyy = 0; iyy < ns; iyy++) {
             float yc = cg_sub_centre(y0, iyy, dxs);
+            float yz2 = CG_ADD(CG_MUL(yc, yc), CG_MUL(zc, zc));
             for (int ixx = 0; ixx < ns; ixx++) {
               float xc = cg_sub_centre(x0, ixx, dxs);
-              float r, cth, ph;
-              cg_cart2sph(xc, yc, zc, &r, &cth, &ph);
-              int ir = cg_shell_index(r0, rf, nr, CG_ADD(r, drr), ir0);
+              int64_t pix = 0;
+              int ir = cg_imap_sample(xc, yc, zc, yz2, drr, r0, rf, nr, ir0, nside, &pix);
               if (ir >= 0 && ir < nr) {
-                long long k = (long long)ir * npix + cg_ang2pix_ring(nside, cth, ph);
+                long long k = (long long)ir * npix + pix;
                 data[k] += temp;
                 nadd[k]++;
               }

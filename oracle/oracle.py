@@ -29,6 +29,8 @@ def lib():
             "or_norm_tables64": [vp, vp, vp, vp, vp, vp, vp, vp],
             "or_lambda64": [vp, i, vp, vp, d, d, vp], "or_kappa64": [vp, vp, vp],
             "or_imap64": [vp, i, vp, vp, vp, d, d, vp, vp], "or_run_mock64": [vp, i, vp, vp],
+            "or_imap64_part": [vp, i, vp, vp, vp, d, d, i, vp, vp, vp], "or_imap_samples": [vp, i],
+            "or_kappa64_part": [vp, vp, i, vp], "or_poisson_total64": [vp, i, vp],
             "or_density32": [vp, vp, f, i], "or_bins32": [vp, vp, i, d, vp, vp, vp],
             "or_counts32": [vp, i, vp, vp, f, f, vp, vp],
             "or_emit32": [vp, i, vp, vp, vp, f, f, C.c_longlong, vp, vp, vp, vp, vp],
@@ -41,12 +43,16 @@ def lib():
             "or_ang2pix": [C.c_long, vp, vp, vp, C.c_long], "or_nest2ring": [C.c_long, vp, vp, C.c_long],
             "or_ring2nest": [C.c_long, vp, vp, C.c_long], "or_pix2vec_nest": [C.c_long, vp, vp, C.c_long],
         }
+        void = ("or_philox", "or_poisson", "or_ang2pix", "or_nest2ring", "or_ring2nest", "or_pix2vec_nest")
         for k, a in sig.items():
             fn = getattr(L, k)
             fn.argtypes = a
-            fn.restype = None if k.startswith("or_vec") or k in ("or_philox", "or_poisson", "or_ang2pix",
-                                                                   "or_nest2ring", "or_ring2nest",
-                                                                   "or_pix2vec_nest") else C.c_int
+            if k in ("or_imap_samples", "or_poisson_total64"):
+                fn.restype = C.c_longlong
+            elif k.startswith("or_vec") or k in void:
+                fn.restype = None
+            else:
+                fn.restype = C.c_int
         _lib = L
     return _lib
 
@@ -262,3 +268,29 @@ def pix2vec_nest(nside, ip):
     v = np.empty((len(ip), 3), np.float32)
     lib().or_pix2vec_nest(nside, P(ip), P(v), len(ip))
     return v
+
+
+def imap64_part(cfg, ipop, dens, npot, tab, e, iz_stride):
+    ns, nr = cfg.nside_imap[ipop], cfg.imap_nr[ipop]
+    data = np.empty((nr, 12 * ns * ns))
+    nadd = np.empty((nr, 12 * ns * ns), np.int32)
+    nsamp = C.c_longlong()
+    lib().or_imap64_part(cfgp(cfg), ipop, P(np.ascontiguousarray(dens, np.float64)),
+                         P(np.ascontiguousarray(npot, np.float64)), P(np.ascontiguousarray(tab, np.float64)),
+                         float(e[0]), float(e[1]), iz_stride, P(data), P(nadd), C.byref(nsamp))
+    return nsamp.value
+
+
+def imap_samples(cfg, ipop):
+    return lib().or_imap_samples(cfgp(cfg), ipop)
+
+
+def kappa64_part(cfg, npot, pix_stride):
+    ns = cfg.nside_kappa
+    m = np.zeros((cfg.n_kappa, 12 * ns * ns))
+    lib().or_kappa64_part(cfgp(cfg), P(np.ascontiguousarray(npot, np.float64)), pix_stride, P(m))
+    return m
+
+
+def poisson_total64(cfg, ipop, lam):
+    return lib().or_poisson_total64(cfgp(cfg), ipop, P(np.ascontiguousarray(lam, np.float64)))

@@ -61,8 +61,9 @@ static void check_size()
 {
   using PL = Plan<N>;
   double ec = check_plan<N, PL::CR, PL::C0, PL::C1, PL::C2>(N);
+  double ef = check_plan<N, PL::FR, PL::F0, PL::F1, PL::F2>(N + 2);
   double er = check_plan<N / 2, PL::RR, PL::R0, PL::R1, PL::R2>(N + 1);
-  printf("%d %.3e %.3e\n", N, ec, er);
+  printf("%d %.3e %.3e\n", N, ec > ef ? ec : ef, er);
 }
 
 int main()

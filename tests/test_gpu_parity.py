@@ -92,11 +92,11 @@ class Run:
             self.disp = [m.grid(w).copy() for w in (2, 3, 4)]
         m.compute_density_normalization()
         self.d = m.grid(0).copy()
+        self.norm_s = [m.norm_table(0, i) for i in range(self.cfg.n_srcs)]
+        self.norm_i = [m.norm_table(1, i) for i in range(self.cfg.n_imap)]
         self.nsrc = m.srcs_set_cartesian()
         self.cats = [m.catalog(i) for i in range(self.cfg.n_srcs)]
         self.cmaps = [m.count_map(i) if self.cfg.nside_count[i] > 0 else None for i in range(self.cfg.n_srcs)]
-        self.norm_s = [m.norm_table(0, i) for i in range(self.cfg.n_srcs)]
-        self.norm_i = [m.norm_table(1, i) for i in range(self.cfg.n_imap)]
         m.imap_set_cartesian()
         self.imaps = [m.imap(i, with_nadd=True) for i in range(self.cfg.n_imap)]
         m.get_beam_properties()
@@ -226,6 +226,20 @@ def test_redshift_bin_sums(runs, kind):
     assert np.allclose(zarr[ok], z32[ok], rtol=1e-6)
     gb = np.concatenate([bs, bi[:r.cfg.n_imap]])
     assert np.allclose(gb[:, ok], b32[:, ok], rtol=1e-6)
+
+
+@pytest.mark.parametrize("kind", ["full", "nobeam", "lpt", "n96", "ptrs", "clip"])
+def test_norm_tables_vs_fp64(runs, kind):
+    """compute_density_normalization (density.c:1227-1355): the FP32 tables the
+    kernels use against the FP64 oracle's, from the same physical field."""
+    import oracle as orc
+    r = runs(kind)
+    tabs, e0f, nz = orc.norm_tables64(r.cfg, unpad(r.need('d')).astype(np.float64))
+    got = r.need('norm_s') + r.need('norm_i')
+    for t, (tab, e) in enumerate(got):
+        assert np.all(np.isfinite(tab)), (t, tab[~np.isfinite(tab)][:5])
+        assert np.allclose(tab, tabs[t], rtol=2e-6), (t, np.max(np.abs(tab / tabs[t] - 1)))
+        assert np.allclose(e, e0f[t], rtol=2e-6)
 
 
 @pytest.mark.parametrize("kind", ["full", "nobeam", "lpt", "n96", "ptrs", "clip"])
