@@ -90,12 +90,17 @@ struct cg_ctx {
   int pending_mode = CG_DMODE_NONE;
   /* sources */
   unsigned short *d_counts = nullptr;
-  long long *d_bsums = nullptr, *d_total = nullptr;
+  long long *d_bsums = nullptr, *d_total = nullptr, *d_ovf_cell = nullptr;
+  int *d_ovf_cnt = nullptr, *d_ovf_n = nullptr;
   Cat cat[CG_NPOP_MAX];
   /* intensity maps */
   Imap im[CG_NPOP_MAX];
   float *d_tmpmap = nullptr;
   size_t tmpmap_n = 0;
+  cg_heavy_cell *d_heavy = nullptr;
+  long long *d_heavy_off = nullptr;
+  unsigned long long *d_heavy_ctr = nullptr;
+  long long heavy_cap = 0;
   /* kappa */
   float *d_kmap = nullptr, *d_kfac = nullptr, *d_kinv = nullptr;
   int *d_kir = nullptr;
@@ -160,8 +165,8 @@ static int check_device_errors(cg_ctx *c)
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   if (h) {
     CUDA_TRY(c, cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), c->stream));
-    return fail(c, CG_EDEVICE, "device error flags 0x%x (1: >65535 sources in a cell, 2: catalog overflow, "
-                               "4: shell search, 8: imap sub-sampling)", h);
+    return fail(c, CG_EDEVICE, "device error flags 0x%x (1: source count overflow, 2: catalog overflow, "
+                               "4: shell search, 8: imap sub-sampling, 16: imap heavy-sample count)", h);
   }
   return CG_OK;
 }
@@ -421,7 +426,8 @@ extern "C" void cg_destroy(cg_ctx *c)
   void *ptrs[] = {c->d_tabs, c->d_norm, c->d_pk, c->d_twN, c->d_twH, c->d_dens, c->d_npot, c->d_disp[0],
                   c->d_disp[1], c->d_disp[2], c->d_part, c->d_stats, c->d_s2f, c->d_err, c->d_ncount,
                   c->d_zsum, c->d_bsum, c->d_counts, c->d_bsums, c->d_total, c->d_tmpmap, c->d_kmap,
-                  c->d_kfac, c->d_kinv, c->d_kir};
+                  c->d_kfac, c->d_kinv, c->d_kir, c->d_ovf_cell, c->d_ovf_cnt, c->d_ovf_n,
+                  c->d_heavy, c->d_heavy_off, c->d_heavy_ctr};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < CG_NPOP_MAX; i++) {
@@ -750,6 +756,9 @@ static void srcs_params(cg_ctx *c, int ipop, cg_srcs_params &p)
   p.cmap = c->cat[ipop].cmap;
   p.counts = c->d_counts;
   p.block_sums = c->d_bsums;
+  p.ovf_cell = c->d_ovf_cell;
+  p.ovf_cnt = c->d_ovf_cnt;
+  p.ovf_n = c->d_ovf_n;
   p.capacity = c->cat[ipop].cap;
   p.pos = c->cat[ipop].pos;
   p.ipix = c->cat[ipop].ipix;
@@ -769,6 +778,9 @@ extern "C" int cg_srcs_set_cartesian(cg_ctx *c, long long *nsrc)
     if (!c->d_counts && (rc = dalloc(c, &c->d_counts, (size_t)ncell))) return rc;
     if (!c->d_bsums && (rc = dalloc(c, &c->d_bsums, (size_t)cg_srcs_nblocks(c->N)))) return rc;
     if (!c->d_total && (rc = dalloc(c, &c->d_total, (size_t)1))) return rc;
+    if (!c->d_ovf_n && ((rc = dalloc(c, &c->d_ovf_cell, (size_t)CG_OVF_CAP)) ||
+                        (rc = dalloc(c, &c->d_ovf_cnt, (size_t)CG_OVF_CAP)) || (rc = dalloc(c, &c->d_ovf_n, (size_t)1))))
+      return rc;
   }
   for (int ip = 0; ip < c->cfg.n_srcs; ip++) {
     Cat &K = c->cat[ip];
@@ -894,6 +906,40 @@ extern "C" int cg_imap_set_cartesian(cg_ctx *c)
     p.data = M.data;
     p.nadd = M.nadd;
     p.err = c->d_err;
+    /* Heavy cells: nsub >= CG_NSUB_HEAVY.  Their list is sized for every cell
+     * whose corner lies within the outer radius of the shells that can give
+     * such an nsub (a gap between shells counts as nsub_lo); cells past the
+     * list's capacity are painted by the first kernel. */
+    {
+      const bool gaps = [&] {
+        for (int i = 0; i + 1 < nr; i++)
+          if (sr0[i + 1] > srf[i]) return true;
+        return false;
+      }();
+      double rb = -1;
+      if (nsub[0] >= CG_NSUB_HEAVY) rb = gaps ? (double)p.rmax_here : (double)sr0[0];
+      for (int i = 0; i < nr; i++)
+        if (nsub[i] >= CG_NSUB_HEAVY && srf[i] > rb) rb = srf[i];
+      if (nsub[nr - 1] >= CG_NSUB_HEAVY) rb = p.rmax_here;
+      long long want = 0;
+      if (rb >= 0) {
+        const double rc = rb / dx + 2.0;
+        const double ball = 4.0 / 3.0 * M_PI * rc * rc * rc;
+        const double ncell = (double)c->N * c->N * c->N;
+        want = (long long)fmin(fmin(ball, ncell), (double)CG_HEAVY_MAX) + 1;
+      }
+      if (want > c->heavy_cap) {
+        if ((rc = dalloc(c, &c->d_heavy, (size_t)want)) || (rc = dalloc(c, &c->d_heavy_off, (size_t)want)))
+          return rc;
+        c->heavy_cap = want;
+      }
+      if (!c->d_heavy_ctr && (rc = dalloc(c, &c->d_heavy_ctr, (size_t)1))) return rc;
+      p.nsub_heavy = CG_NSUB_HEAVY;
+      p.heavy_cap = want;
+      p.heavy_ctr = c->d_heavy_ctr;
+      p.heavy_off = c->d_heavy_off;
+      p.heavy = c->d_heavy;
+    }
     {
       ProfScope ps(c, "imap_paint");
       CUDA_TRY(c, cg_imap_paint(c->stream, c->d_dens, c->d_npot, &p, c->nsm));

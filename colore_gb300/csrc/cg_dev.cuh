@@ -15,10 +15,12 @@ namespace cg {
 
 /* Error bits written by kernels (never trapping). */
 enum : unsigned int {
-  ERR_COUNT_OVERFLOW = 1u,  /* more than 65535 sources in one cell     */
+  ERR_COUNT_OVERFLOW = 1u,  /* count overflow list full, lambda > 2^30,
+                               or > 2^31-1 sources in 2048 cells      */
   ERR_CATALOG_OVERFLOW = 2u, /* emit wrote past the allocated catalog  */
   ERR_SHELL_WALK = 4u,       /* imap shell search did not terminate    */
   ERR_IMAP_NSUB = 8u,        /* sub-sampling factor out of range       */
+  ERR_IMAP_HEAVY = 16u,      /* more than 2^40 samples in heavy cells  */
 };
 
 /* One background table with the edge values of get_bg (cosmo.c:40-86). */

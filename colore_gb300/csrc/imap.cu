@@ -7,18 +7,30 @@
  * it is split into nsub^3 sub-cells whose centres are placed in a shell (by
  * r + dr_rsd) and a RING pixel, where temp is added and a hit counted.
  *
- * A warp takes 32 consecutive cells of a row (one per lane) and computes
- * their per-cell quantities; its lanes then take the x-lines of sub-samples
- * (nsub^2 per cell, nsub samples each) of all 32 cells, so that lanes stay
- * busy whatever nsub is.  Along a line y, z and y^2+z^2 are computed once
- * and consecutive samples landing on the same (shell, pixel) are merged in
- * registers.  Those runs go to a per-warp shared-memory hash table keyed by
- * (cell, shell, pixel): at low redshift a cell spans hundreds of pixels and
- * each pixel receives tens of its sub-samples, so the table turns one global
- * atomic pair per sub-sample into one per distinct key.  The table is
- * flushed (data += temp * count, nadd += count) when half full and at the
- * end of each group of cells; runs that find it nearly full go straight to
- * global memory.
+ * The work per cell is nsub^3 and nsub grows as 1/r towards the observer
+ * (the sub-cell follows the pixel size r * sqrt(4 pi / npix)), so a few
+ * cells near the observer hold most of the samples.  Two kernels:
+ *
+ *   k_imap        A warp takes 32 consecutive cells of a row (one per lane)
+ *                 and computes their per-cell quantities.  Cells with at least
+ *                 nsub_heavy sub-samples per side are appended to the heavy
+ *                 list, with their first sample offset from one 64-bit atomic
+ *                 that counts records and samples together, so the offsets
+ *                 are an exclusive prefix in list order.  The warp's lanes
+ *                 then take the x-lines of sub-samples (nsub^2 per cell,
+ *                 nsub samples each) of the remaining cells.
+ *   k_imap_heavy  The heavy samples are cut into one equal range per warp;
+ *                 a warp finds its first cell by binary search on the
+ *                 offsets and paints 32 lines of one cell at a time.
+ *
+ * Along a line y, z and y^2+z^2 are computed once and consecutive samples
+ * landing on the same (shell, pixel) are merged in registers.  Those runs go
+ * to a per-warp shared-memory hash table keyed by (cell, shell, pixel): at
+ * low redshift a cell spans hundreds of pixels and each pixel receives tens
+ * of its sub-samples, so the table turns one global atomic pair per
+ * sub-sample into one per distinct key.  The table is flushed
+ * (data += temp * count, nadd += count) when half full and whenever its
+ * cells change; runs that find it nearly full go straight to global memory.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -107,6 +119,50 @@ __device__ __forceinline__ void insert(WarpSm &w, unsigned long long key, unsign
   atomicAdd(&p.nadd[idx], (int)c);
 }
 
+/* Paint x-line l (l = izz * ns + iyy) of cell c, whose corner is (c.x0, y0, z0);
+ * its samples go to the table under cell slot j. */
+__device__ __forceinline__ void paint_line(WarpSm &w, const cg_imap_params &p, const float *r0, const float *rf,
+                                           const CellPar &c, float y0, float z0, int l, int j)
+{
+  const int ns = c.nsub;
+  /* (l + 1/2)/ns is at least 1/(2 ns) from an integer: exact for ns <= 128 */
+  const int izz = ns <= 128 ? (int)(((float)l + 0.5f) * c.inv_ns) : l / ns;
+  const int iyy = l - izz * ns;
+  const float zc = cg_sub_centre(z0, izz, c.dxs);
+  const float yc = cg_sub_centre(y0, iyy, c.dxs);
+  const float yz2 = CG_ADD(CG_MUL(yc, yc), CG_MUL(zc, zc));
+  const unsigned long long jk = (unsigned long long)j << 58;
+  unsigned long long cur = EMPTY;
+  unsigned int run = 0;
+  for (int ixx = 0; ixx < ns; ixx++) {
+    const float xc = cg_sub_centre(c.x0, ixx, c.dxs);
+    int64_t pix = 0;
+    const int ir = cg_imap_sample(xc, yc, zc, yz2, c.drr, r0, rf, p.nr, c.irad0, p.nside, &pix);
+    if (ir < 0 || ir >= p.nr) continue;
+    const unsigned long long key = jk | (unsigned long long)((long long)ir * p.npix + pix);
+    if (key == cur) {
+      run++;
+    } else {
+      if (run) insert(w, cur, run, p);
+      cur = key;
+      run = 1;
+    }
+  }
+  if (run) insert(w, cur, run, p);
+}
+
+__device__ __forceinline__ void init_tables(WarpSm &w, int lane)
+{
+  for (int i = lane; i < HT; i += 32) {
+    w.key[i] = EMPTY;
+    w.cnt[i] = 0u;
+  }
+  if (lane == 0) w.nused = 0;
+}
+
+constexpr unsigned long long HREC = 1ull << 40;     /* one heavy record    */
+constexpr unsigned long long HSMASK = HREC - 1;     /* heavy sample field  */
+
 __global__ void __launch_bounds__(IW * 32) k_imap(const float *__restrict__ dens, const float *__restrict__ phi,
                                                   cg_imap_params p)
 {
@@ -122,11 +178,7 @@ __global__ void __launch_bounds__(IW * 32) k_imap(const float *__restrict__ dens
     rf[i] = p.rf[i];
     nsa[i] = p.nsub[i];
   }
-  for (int i = lane; i < HT; i += 32) {
-    w.key[i] = EMPTY;
-    w.cnt[i] = 0u;
-  }
-  if (lane == 0) w.nused = 0;
+  init_tables(w, lane);
   __syncthreads();
   const int N = p.box.N;
   const int nch = (N + 31) / 32;
@@ -173,6 +225,43 @@ __global__ void __launch_bounds__(IW * 32) k_imap(const float *__restrict__ dens
         }
       }
     }
+    /* heavy cells go to the list (one atomic per warp); past its capacity
+     * they are painted here */
+    const bool hv = n > 0 && p.nsub_heavy > 0 && cp.nsub >= p.nsub_heavy;
+    if (__ballot_sync(FULL, hv)) {
+      const unsigned long long v = hv ? HREC | (unsigned long long)n : 0ull;
+      unsigned long long inc = v;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long t = __shfl_up_sync(FULL, inc, o);
+        if (lane >= o) inc += t;
+      }
+      const unsigned long long wt = __shfl_sync(FULL, inc, 31);
+      unsigned long long base = 0;
+      int ok = 0;
+      if (lane == 0) {
+        /* stop appending once the list is full or half the sample field is
+         * used, so that neither field can wrap (the overshoot of warps in
+         * flight is at most 32 records and 2^35 samples each) */
+        const unsigned long long cur = *(volatile unsigned long long *)p.heavy_ctr;
+        if ((long long)(cur >> 40) < p.heavy_cap && (cur & HSMASK) < (HSMASK >> 1)) {
+          base = atomicAdd(p.heavy_ctr, wt);
+          ok = 1;
+          if ((base & HSMASK) + (wt & HSMASK) > HSMASK) atomicOr(p.err, ERR_IMAP_HEAVY);
+        }
+      }
+      ok = __shfl_sync(FULL, ok, 0);
+      base = __shfl_sync(FULL, base, 0);
+      const unsigned long long mine = base + inc - v;
+      const long long slot = (long long)(mine >> 40);
+      if (ok && hv && slot < p.heavy_cap) {
+        float4 *q = reinterpret_cast<float4 *>(p.heavy + slot);
+        q[0] = make_float4(cp.x0, y0, z0, cp.temp);
+        q[1] = make_float4(cp.drr, cp.dxs, __int_as_float(cp.nsub), __int_as_float(cp.irad0));
+        p.heavy_off[slot] = (long long)(mine & HSMASK);
+        n = 0;
+      }
+    }
     w.cell[lane] = cp;
     /* inclusive scan of the line counts (nsub^2 per cell) over the warp */
     const int nl = cp.nsub * cp.nsub;
@@ -196,34 +285,68 @@ __global__ void __launch_bounds__(IW * 32) k_imap(const float *__restrict__ dens
       }
       if (j > 31) j = 31;
       const int ex = __shfl_sync(FULL, excl, j);
-      if (s < total) {
-        const CellPar c = w.cell[j];
-        const int l = s - ex, ns = c.nsub;
-        /* (l + 1/2)/ns is at least 1/(2 ns) from an integer: exact for ns <= 128 */
-        const int izz = ns <= 128 ? (int)(((float)l + 0.5f) * c.inv_ns) : l / ns;
-        const int iyy = l - izz * ns;
-        const float zc = cg_sub_centre(z0, izz, c.dxs);
-        const float yc = cg_sub_centre(y0, iyy, c.dxs);
-        const float yz2 = CG_ADD(CG_MUL(yc, yc), CG_MUL(zc, zc));
-        const unsigned long long jk = (unsigned long long)j << 58;
-        unsigned long long cur = EMPTY;
-        unsigned int run = 0;
-        for (int ixx = 0; ixx < ns; ixx++) {
-          const float xc = cg_sub_centre(c.x0, ixx, c.dxs);
-          int64_t pix = 0;
-          const int ir = cg_imap_sample(xc, yc, zc, yz2, c.drr, r0, rf, p.nr, c.irad0, p.nside, &pix);
-          if (ir < 0 || ir >= p.nr) continue;
-          const unsigned long long key = jk | (unsigned long long)((long long)ir * p.npix + pix);
-          if (key == cur) {
-            run++;
-          } else {
-            if (run) insert(w, cur, run, p);
-            cur = key;
-            run = 1;
-          }
-        }
-        if (run) insert(w, cur, run, p);
-      }
+      if (s < total) paint_line(w, p, r0, rf, w.cell[j], y0, z0, s - ex, j);
+      __syncwarp();
+      if (*(volatile int *)&w.nused >= HFLUSH) flush(w, lane, p);
+    }
+    flush(w, lane, p);
+  }
+}
+
+__global__ void __launch_bounds__(IW * 32) k_imap_heavy(cg_imap_params p)
+{
+  extern __shared__ unsigned char sraw[];
+  WarpSm *ws = reinterpret_cast<WarpSm *>(sraw);
+  float *r0 = reinterpret_cast<float *>(sraw + IW * sizeof(WarpSm));
+  float *rf = r0 + p.nr;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  WarpSm &w = ws[wid];
+  for (int i = threadIdx.x; i < p.nr; i += blockDim.x) {
+    r0[i] = p.r0[i];
+    rf[i] = p.rf[i];
+  }
+  init_tables(w, lane);
+  __syncthreads();
+  const unsigned long long ctr = *(volatile unsigned long long *)p.heavy_ctr;
+  long long H = (long long)(ctr >> 40);
+  if (H > p.heavy_cap) H = p.heavy_cap;
+  if (H <= 0) return;
+  const cg_heavy_cell *hl = p.heavy;
+  const long long *off = p.heavy_off;
+  const long long nlast = hl[H - 1].nsub;
+  const unsigned long long S = (unsigned long long)(off[H - 1] + nlast * nlast * nlast);
+  const unsigned long long W = (unsigned long long)gridDim.x * IW, wg = (unsigned long long)blockIdx.x * IW + wid;
+  const long long s0 = (long long)(S * wg / W), s1 = (long long)(S * (wg + 1) / W);
+  if (s0 >= s1) return;
+  /* last record starting at or before s0 */
+  long long lo = 0, hi = H - 1;
+  while (lo < hi) {
+    const long long mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= s0) lo = mid;
+    else hi = mid - 1;
+  }
+  /* a line belongs to the warp whose range holds its first sample */
+  for (long long h = lo; h < H && off[h] < s1; h++) {
+    const float4 qa = __ldg(reinterpret_cast<const float4 *>(hl + h));
+    const float4 qb = __ldg(reinterpret_cast<const float4 *>(hl + h) + 1);
+    const cg_heavy_cell hc = {qa.x, qa.y, qa.z, qa.w, qb.x, qb.y, __float_as_int(qb.z), __float_as_int(qb.w)};
+    const long long ns = hc.nsub, base = off[h];
+    long long la = s0 > base ? (s0 - base + ns - 1) / ns : 0;
+    long long lb = (s1 - base + ns - 1) / ns;
+    if (lb > ns * ns) lb = ns * ns;
+    CellPar c;
+    c.x0 = hc.x0;
+    c.temp = hc.temp;
+    c.drr = hc.drr;
+    c.dxs = hc.dxs;
+    c.inv_nn = 0.0f;
+    c.inv_ns = 1.0f / (float)hc.nsub;
+    c.nsub = hc.nsub;
+    c.irad0 = hc.irad0;
+    if (lane == 0) w.cell[0] = c;
+    __syncwarp();
+    for (long long l = la; l < lb; l += 32) {
+      if (l + lane < lb) paint_line(w, p, r0, rf, c, hc.y0, hc.z0, (int)(l + lane), 0);
       __syncwarp();
       if (*(volatile int *)&w.nused >= HFLUSH) flush(w, lane, p);
     }
@@ -238,9 +361,27 @@ cudaError_t cg_imap_paint(cudaStream_t s, const float *dens, const float *phi, c
   size_t smem = IW * sizeof(WarpSm) + (size_t)p->nr * (2 * sizeof(float) + sizeof(int));
   cudaError_t e = cudaFuncSetAttribute(k_imap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_imap, IW * 32, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  if (p->heavy_ctr) {
+    e = cudaMemsetAsync(p->heavy_ctr, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+  }
   long long ntask = (long long)((p->box.N + 31) / 32) * p->box.N * p->box.N;
   long long blocks = (ntask + IW - 1) / IW;
-  if (blocks > (long long)nsm * 8) blocks = (long long)nsm * 8;
+  if (blocks > (long long)nsm * per_sm * 4) blocks = (long long)nsm * per_sm * 4;
   k_imap<<<(unsigned)blocks, IW * 32, smem, s>>>(dens, phi, *p);
+  e = cudaGetLastError();
+  if (e != cudaSuccess || !p->heavy_ctr || p->heavy_cap <= 0) return e;
+  /* every warp of the heavy pass resident at once: the ranges are static */
+  size_t hsmem = IW * sizeof(WarpSm) + (size_t)p->nr * 2 * sizeof(float);
+  e = cudaFuncSetAttribute(k_imap_heavy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hsmem);
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_imap_heavy, IW * 32, hsmem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  k_imap_heavy<<<(unsigned)(nsm * per_sm), IW * 32, hsmem, s>>>(*p);
   return cudaGetLastError();
 }

@@ -24,7 +24,25 @@ struct cg_imap_params {
   float *data;        /* nr * npix, RING */
   int *nadd;          /* nr * npix       */
   unsigned int *err;
+  /* Cells with at least nsub_heavy sub-samples per side are listed by the
+   * first kernel and painted by the second with their samples split evenly
+   * over all warps.  heavy_ctr packs (records << 40) | samples. */
+  int nsub_heavy;
+  long long heavy_cap;
+  unsigned long long *heavy_ctr;
+  long long *heavy_off;            /* first sample of each record          */
+  struct cg_heavy_cell *heavy;     /* heavy_cap records                    */
 };
+
+struct __align__(16) cg_heavy_cell {
+  float x0, y0, z0, temp, drr, dxs;
+  int nsub, irad0;
+};
+
+/* Sub-samples per side from which a cell is painted by the heavy pass, and
+ * the largest heavy list (records of 40 bytes). */
+#define CG_NSUB_HEAVY 8
+#define CG_HEAVY_MAX (1LL << 23)
 
 cudaError_t cg_imap_paint(cudaStream_t s, const float *dens, const float *phi, const cg_imap_params *p, int nsm);
 

@@ -7,7 +7,9 @@
  *   k_pois_count : one block per 2048 consecutive cells; per cell lambda and
  *                  a Poisson deviate keyed by (seed, population, cell), so the
  *                  result does not depend on the launch shape; counts are kept
- *                  as uint16 and the block totals written out.
+ *                  as uint16 and the block totals written out.  A cell with
+ *                  CG_COUNT_ESC or more sources stores the escape value and
+ *                  appends (cell, count) to a short overflow list.
  *   k_scan       : exclusive scan of the block totals (one block).
  *   k_emit       : re-reads the counts, scans them inside the block and writes
  *                  every source at its final catalog index, in cell order (the
@@ -46,12 +48,22 @@ __device__ __forceinline__ float pois_lambda(const cg_srcs_params &p, float d, f
   return cg_src_lambda(nd, p.cell_vol, d, b, dn, p.bias_model);
 }
 
+/* True count of a cell whose stored count is the escape value. */
+__device__ __forceinline__ int ovf_lookup(const cg_srcs_params &p, long long cid)
+{
+  int n = *p.ovf_n;
+  if (n > CG_OVF_CAP) n = CG_OVF_CAP;
+  for (int k = 0; k < n; k++)
+    if (p.ovf_cell[k] == cid) return p.ovf_cnt[k];
+  return CG_COUNT_ESC;
+}
+
 __global__ void __launch_bounds__(SB) k_pois_count(const float *__restrict__ grid, cg_srcs_params p)
 {
   const int N = p.box.N;
   const long long ncell = (long long)N * N * N;
   const long long c0 = (long long)blockIdx.x * CPB + (long long)threadIdx.x * CPT;
-  int tot = 0;
+  long long tot = 0;
   if (c0 < ncell) {
     int ix, iy, iz;
     cell_of(c0, N, ix, iy, iz);
@@ -68,15 +80,24 @@ __global__ void __launch_bounds__(SB) k_pois_count(const float *__restrict__ gri
         float r = cg_norm3(x0, y0, z0);
         float lam = pois_lambda(p, dd[e], r);
         int n = 0;
-        if (lam > 0.0f) {
-          long long cid = c0 + h + e;
+        const long long cid = c0 + h + e;
+        if (lam > 1073741824.0f) {
+          atomicOr(p.err, ERR_COUNT_OVERFLOW);
+        } else if (lam > 0.0f) {
           n = cg_poisson(lam, p.kp0, p.kp1, (uint32_t)cid, (uint32_t)(cid >> 32));
         }
-        if (n > 65535) {
-          atomicOr(p.err, ERR_COUNT_OVERFLOW);
-          n = 65535;
+        if (n >= CG_COUNT_ESC) {
+          const int k = atomicAdd(p.ovf_n, 1);
+          if (k < CG_OVF_CAP) {
+            p.ovf_cell[k] = cid;
+            p.ovf_cnt[k] = n;
+          } else {
+            atomicOr(p.err, ERR_COUNT_OVERFLOW);
+          }
+          cnt[h + e] = (unsigned short)CG_COUNT_ESC;
+        } else {
+          cnt[h + e] = (unsigned short)n;
         }
-        cnt[h + e] = (unsigned short)n;
         tot += n;
       }
     }
@@ -87,15 +108,16 @@ __global__ void __launch_bounds__(SB) k_pois_count(const float *__restrict__ gri
     pk.w = cnt[6] | ((unsigned)cnt[7] << 16);
     *reinterpret_cast<uint4 *>(p.counts + c0) = pk;
   }
-  /* block total */
+  /* block total; k_emit scans a block in int, so it must stay below 2^31 */
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
-  __shared__ int ws[SB / 32];
+  __shared__ long long ws[SB / 32];
   if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = tot;
   __syncthreads();
   if (threadIdx.x == 0) {
     long long s = 0;
     for (int w = 0; w < SB / 32; w++) s += ws[w];
+    if (s > 0x7fffffffLL) atomicOr(p.err, ERR_COUNT_OVERFLOW);
     p.block_sums[blockIdx.x] = s;
   }
 }
@@ -143,12 +165,24 @@ __global__ void __launch_bounds__(SB) k_emit(const float *__restrict__ phi, cg_s
   const long long c0 = (long long)blockIdx.x * CPB + (long long)threadIdx.x * CPT;
   uint64_t clo = 0, chi = 0; /* 8 packed uint16 counts */
   int tot = 0;
+  bool esc = false;
   if (c0 < ncell) {
     uint4 pk = *reinterpret_cast<const uint4 *>(p.counts + c0);
     clo = (uint64_t)pk.x | ((uint64_t)pk.y << 32);
     chi = (uint64_t)pk.z | ((uint64_t)pk.w << 32);
 #pragma unroll
-    for (int h = 0; h < 4; h++) tot += (int)((clo >> (16 * h)) & 0xffffu) + (int)((chi >> (16 * h)) & 0xffffu);
+    for (int h = 0; h < 4; h++) {
+      const int a = (int)((clo >> (16 * h)) & 0xffffu), b = (int)((chi >> (16 * h)) & 0xffffu);
+      esc |= (a == CG_COUNT_ESC) | (b == CG_COUNT_ESC);
+      tot += a + b;
+    }
+    if (esc) {
+      tot = 0;
+      for (int h = 0; h < CPT; h++) {
+        const int n = (int)(((h < 4 ? clo : chi) >> (16 * (h & 3))) & 0xffffu);
+        tot += n == CG_COUNT_ESC ? ovf_lookup(p, c0 + h) : n;
+      }
+    }
   }
   /* block exclusive scan of per-thread totals */
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -170,8 +204,9 @@ __global__ void __launch_bounds__(SB) k_emit(const float *__restrict__ phi, cg_s
   const float dx = p.box.dx;
   const float y0 = cg_cell_coord(iy, dx, p.box.p1), z0 = cg_cell_coord(iz, dx, p.box.p2);
   for (int h = 0; h < CPT; h++) {
-    const int n = (int)(((h < 4 ? clo : chi) >> (16 * (h & 3))) & 0xffffu);
+    int n = (int)(((h < 4 ? clo : chi) >> (16 * (h & 3))) & 0xffffu);
     if (n == 0) continue;
+    if (esc && n == CG_COUNT_ESC) n = ovf_lookup(p, c0 + h);
     const float x0 = cg_cell_coord(ix + h, dx, p.box.p0);
     const float rr = cg_norm3(x0, y0, z0);
     float v[3];
@@ -268,6 +303,8 @@ long long cg_srcs_nblocks(int N) { return ((long long)N * N * N + CPB - 1) / CPB
 cudaError_t cg_srcs_count(cudaStream_t s, const float *grid, const cg_srcs_params *p, long long *total)
 {
   long long nb = cg_srcs_nblocks(p->box.N);
+  cudaError_t e = cudaMemsetAsync(p->ovf_n, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
   k_pois_count<<<(unsigned)nb, SB, 0, s>>>(grid, *p);
   k_scan<<<1, 1024, 0, s>>>(p->block_sums, nb, total);
   return cudaGetLastError();

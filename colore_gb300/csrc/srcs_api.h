@@ -24,7 +24,10 @@ struct cg_srcs_params {
   int need_beaming;
   int64_t nside_base, nside_count;
   int *cmap;                 /* count map or NULL */
-  unsigned short *counts;    /* N^3 */
+  unsigned short *counts;    /* N^3; CG_COUNT_ESC marks a cell in the overflow list */
+  long long *ovf_cell;       /* cells holding CG_COUNT_ESC or more sources ...     */
+  int *ovf_cnt;              /* ... and their counts                             */
+  int *ovf_n;                /* entries used (zeroed by cg_srcs_count)           */
   long long *block_sums;     /* per block; exclusive offsets after the scan */
   long long capacity;
   float4 *pos;
@@ -32,6 +35,12 @@ struct cg_srcs_params {
   float *src;                /* 9 floats per source (Src) */
   unsigned int *err;
 };
+
+/* Per-cell counts are stored as uint16; the few cells at or above the escape
+ * value (in practice the cells touching the observer, where n(z) ~ 1/r^2)
+ * go to an overflow list of CG_OVF_CAP entries. */
+#define CG_COUNT_ESC 65535
+#define CG_OVF_CAP 4096
 
 long long cg_srcs_nblocks(int N);
 cudaError_t cg_srcs_count(cudaStream_t s, const float *grid, const cg_srcs_params *p, long long *total);

@@ -167,12 +167,11 @@ static int cell_count(const cg_config *cfg, const S32 *s, int ipop, const float 
                             cfg->bias_model);
   if (!(lam > 0.0f)) return 0;
   long long cid = (long long)ix + (long long)N * ((long long)iy + (long long)N * iz);
-  int n = cg_poisson(lam, kp0, kp1, (uint32_t)cid, (uint32_t)(cid >> 32));
-  return n > 65535 ? 65535 : n;
+  return cg_poisson(lam, kp0, kp1, (uint32_t)cid, (uint32_t)(cid >> 32));
 }
 
 int or_counts32(const cg_config *cfg, int ipop, const float *dens, const float *normtab, float n0, float nf,
-                unsigned short *counts, long long *total)
+                int *counts, long long *total)
 {
   S32 s;
   s32_init(&s, cfg);
@@ -189,7 +188,7 @@ int or_counts32(const cg_config *cfg, int ipop, const float *dens, const float *
     for (int iy = 0; iy < N; iy++)
       for (int ix = 0; ix < N; ix++) {
         int n = cell_count(cfg, &s, ipop, dens, nrm, ix, iy, iz, rlim, cvol, kp0, kp1);
-        if (counts) counts[(size_t)ix + (size_t)N * ((size_t)iy + (size_t)N * iz)] = (unsigned short)n;
+        if (counts) counts[(size_t)ix + (size_t)N * ((size_t)iy + (size_t)N * iz)] = n;
         tot += n;
       }
   *total = tot;

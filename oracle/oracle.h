@@ -60,7 +60,7 @@ int or_density32(const cg_config *cfg, float *dens, float sigma2f, int mode);
 int or_bins32(const cg_config *cfg, const float *dens, int nz, double idz, unsigned long long *narr, double *zarr,
               double *bsum);
 int or_counts32(const cg_config *cfg, int ipop, const float *dens, const float *normtab, float n0, float nf,
-                unsigned short *counts, long long *total);
+                int *counts, long long *total);
 int or_emit32(const cg_config *cfg, int ipop, const float *dens, const float *npot, const float *normtab, float n0,
               float nf, long long cap, float *pos4, int *ipix, float *src9, int *cmap, long long *nsrc);
 int or_beam_rsd32(const cg_config *cfg, const float *npot, long long n, const float *pos4, float *src9);

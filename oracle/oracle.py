@@ -177,7 +177,7 @@ def bins32(cfg, dens, nz, idz):
 
 def counts32(cfg, ipop, dens, tab, e):
     n = cfg.n_grid
-    cnt = np.empty((n, n, n), np.uint16)
+    cnt = np.empty((n, n, n), np.int32)
     tot = C.c_longlong()
     lib().or_counts32(cfgp(cfg), ipop, P(dens), P(tab), float(e[0]), float(e[1]), P(cnt), C.byref(tot))
     return cnt, tot.value

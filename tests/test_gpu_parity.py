@@ -13,6 +13,7 @@ restatement of the reference (ref64) within the stated tolerances:
   1LPT displacements            relative rms error <= 2e-5 (literal r2c path)
   1LPT density                  relative rms error <= 1e-4
   redshift-bin sums             cell counts exact, sums relative 1e-6
+  normalisation tables          relative 2e-4 vs FP64 (FP32 bin edges)
   intensity maps                hit counts exact, brightness relative 5e-5
   convergence maps              bit-exact vs dev32; relative rms 1e-3 vs FP64
 """
@@ -50,6 +51,12 @@ def _spec(kind):
         base["seed"] = 19
         base["srcs"] = [dict(nz=("gauss", 0.3, 0.15), density=30.0, bias=("const", 1.3), nside_count=16)]
         base.pop("imap")
+        base.pop("kappa")
+    elif kind == "heavy":
+        # nside 64 from z = 0.05: the inner shells have nsub ~ 21 (heavy-cell
+        # pass), the outer ones nsub ~ 3 (painted in place)
+        base["seed"] = 29
+        base["imap"] = [dict(tz=0.1, bias=("const", 1.0), z_range=(0.05, 0.5), nbands=6, nside=64)]
         base.pop("kappa")
     elif kind == "clip":
         base["dens_type"] = 3
@@ -231,15 +238,21 @@ def test_redshift_bin_sums(runs, kind):
 @pytest.mark.parametrize("kind", ["full", "nobeam", "lpt", "n96", "ptrs", "clip"])
 def test_norm_tables_vs_fp64(runs, kind):
     """compute_density_normalization (density.c:1227-1355): the FP32 tables the
-    kernels use against the FP64 oracle's, from the same physical field."""
+    kernels use against the FP64 oracle's, from the same physical field.
+
+    The GPU places each cell in a redshift bin from its FP32 radius and z(r),
+    so a few cells within ~1e-7 of a bin edge land in the neighbouring bin;
+    with 64^3 cells and bins of a few hundred cells that moves a table entry by
+    up to ~1e-4 relative (5e-5 seen).  The bins themselves are checked exactly
+    against the FP32 restatement in test_redshift_bin_sums."""
     import oracle as orc
     r = runs(kind)
     tabs, e0f, nz = orc.norm_tables64(r.cfg, unpad(r.need('d')).astype(np.float64))
     got = r.need('norm_s') + r.need('norm_i')
     for t, (tab, e) in enumerate(got):
         assert np.all(np.isfinite(tab)), (t, tab[~np.isfinite(tab)][:5])
-        assert np.allclose(tab, tabs[t], rtol=2e-6), (t, np.max(np.abs(tab / tabs[t] - 1)))
-        assert np.allclose(e, e0f[t], rtol=2e-6)
+        assert np.allclose(tab, tabs[t], rtol=2e-4), (t, np.max(np.abs(tab / tabs[t] - 1)))
+        assert np.allclose(e, e0f[t], rtol=2e-4)
 
 
 @pytest.mark.parametrize("kind", ["full", "nobeam", "lpt", "n96", "ptrs", "clip"])
@@ -283,7 +296,7 @@ def test_source_counts_vs_fp64_mean(runs, kind):
         assert abs(r.need('nsrc')[ip] - mu) < 5 * np.sqrt(mu) + 5, (r.need('nsrc')[ip], mu)
 
 
-@pytest.mark.parametrize("kind", ["full", "nobeam", "lpt", "n96"])
+@pytest.mark.parametrize("kind", ["full", "nobeam", "lpt", "n96", "heavy"])
 def test_imap_vs_dev32(runs, kind):
     import oracle as orc
     r = runs(kind)
