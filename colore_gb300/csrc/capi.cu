@@ -99,7 +99,7 @@ struct cg_ctx {
   size_t tmpmap_n = 0;
   cg_heavy_cell *d_heavy = nullptr;
   long long *d_heavy_off = nullptr;
-  unsigned long long *d_heavy_ctr = nullptr;
+  unsigned long long *d_imap_ctr = nullptr;
   long long heavy_cap = 0;
   /* kappa */
   float *d_kmap = nullptr, *d_kfac = nullptr, *d_kinv = nullptr;
@@ -366,6 +366,7 @@ extern "C" int cg_upload_tables(cg_ctx *c, const cg_config *cfg)
   const double L = cfg->l_box;
   const int N = c->N;
   c->box.N = N;
+  c->box.mN = ~0ull / (unsigned long long)N + 1ull;
   c->box.dx = (float)(L / N);
   c->box.idx = (float)(N / L);
   c->box.L = (float)L;
@@ -427,7 +428,7 @@ extern "C" void cg_destroy(cg_ctx *c)
                   c->d_disp[1], c->d_disp[2], c->d_part, c->d_stats, c->d_s2f, c->d_err, c->d_ncount,
                   c->d_zsum, c->d_bsum, c->d_counts, c->d_bsums, c->d_total, c->d_tmpmap, c->d_kmap,
                   c->d_kfac, c->d_kinv, c->d_kir, c->d_ovf_cell, c->d_ovf_cnt, c->d_ovf_n,
-                  c->d_heavy, c->d_heavy_off, c->d_heavy_ctr};
+                  c->d_heavy, c->d_heavy_off, c->d_imap_ctr};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < CG_NPOP_MAX; i++) {
@@ -933,10 +934,10 @@ extern "C" int cg_imap_set_cartesian(cg_ctx *c)
           return rc;
         c->heavy_cap = want;
       }
-      if (!c->d_heavy_ctr && (rc = dalloc(c, &c->d_heavy_ctr, (size_t)1))) return rc;
+      if (!c->d_imap_ctr && (rc = dalloc(c, &c->d_imap_ctr, (size_t)3))) return rc;
       p.nsub_heavy = CG_NSUB_HEAVY;
       p.heavy_cap = want;
-      p.heavy_ctr = c->d_heavy_ctr;
+      p.ctr = c->d_imap_ctr;
       p.heavy_off = c->d_heavy_off;
       p.heavy = c->d_heavy;
     }

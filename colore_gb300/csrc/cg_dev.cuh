@@ -75,8 +75,17 @@ struct FillParams {
 struct Box {
   int N;
   float dx, idx, L, hL;
-  float p0, p1, p2; /* observer */
+  float p0, p1, p2;   /* observer */
+  unsigned long long mN; /* floor((2^64 - 1) / N) + 1, see divN */
 };
+
+/* floor(x / N) for 0 <= x < 2^40 (cell and row indices) and N <= 2^13:
+ * x * mN / 2^64 = x / N + e with 0 <= e < x / 2^64 < 2^-24, and x / N is at
+ * least 1/N >= 2^-13 below the next integer, so the high word is exact. */
+__device__ __forceinline__ long long divN(long long x, const Box &b)
+{
+  return (long long)__umul64hi((unsigned long long)x, b.mN);
+}
 
 } /* namespace cg */
 

@@ -69,7 +69,7 @@ __device__ __forceinline__ float wsum(float v, bool mine)
   return x;
 }
 
-__global__ void __launch_bounds__(BINS_WARPS * 32) k_dens_bins(float *grid, cg_bins_params p)
+__global__ void __launch_bounds__(BINS_WARPS * 32, 2) k_dens_bins(float *grid, cg_bins_params p)
 {
   extern __shared__ double sbin[]; /* [warp][nz][2 + nt]; the count is an exact integer in FP64 */
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -79,15 +79,15 @@ __global__ void __launch_bounds__(BINS_WARPS * 32) k_dens_bins(float *grid, cg_b
   __syncwarp();
   const int N = p.box.N;
   const int nseg_row = (N + 31) / 32;
-  const long long nseg = (long long)nseg_row * N * N;
+  const int nrow = N * N;
   const float s2 = p.sigma2f ? *p.sigma2f : 0.0f;
   const bool need_d1 = (p.mode == CG_DMODE_LGNR || p.mode == CG_DMODE_CLIP);
-  const long long gw = (long long)blockIdx.x * BINS_WARPS + wid;
-  const long long nw = (long long)gridDim.x * BINS_WARPS;
-  for (long long seg = gw; seg < nseg; seg += nw) {
-    const int sr = (int)(seg % nseg_row);
-    const long long row = seg / nseg_row;
-    const int iy = (int)(row % N), iz = (int)(row / N);
+  const int gw = blockIdx.x * BINS_WARPS + wid;
+  const int nw = gridDim.x * BINS_WARPS;
+  /* a warp takes whole rows, 32 cells at a time */
+  for (int row = gw; row < nrow; row += nw)
+  for (int sr = 0; sr < nseg_row; sr++) {
+    const int iz = row / N, iy = row - iz * N;
     const int ix = sr * 32 + lane;
     int bin = -1;
     float zz = 0.0f, bs[MAXT];
@@ -162,7 +162,8 @@ __global__ void __launch_bounds__(256) k_lpt_cic(float *grid, const float *__res
   const float iag = CG_DIV((float)N, p.box.L);
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncell;
        c += (long long)gridDim.x * blockDim.x) {
-    const int ix = (int)(c % N), iy = (int)((c / N) % N), iz = (int)(c / ((long long)N * N));
+    const long long q = divN(c, p.box), qz = divN(q, p.box);
+    const int ix = (int)(c - q * N), iy = (int)(q - qz * N), iz = (int)qz;
     const long long id = pidx(ix, iy, iz, N);
     float xv[3] = {cg_cell_coord(ix, p.box.dx, p.box.p0), cg_cell_coord(iy, p.box.dx, p.box.p1),
                    cg_cell_coord(iz, p.box.dx, p.box.p2)};
@@ -213,8 +214,8 @@ cudaError_t cg_dens_bins(cudaStream_t s, float *grid, const cg_bins_params *p, i
   size_t smem = (size_t)BINS_WARPS * p->nz * (2 + p->nt) * sizeof(double);
   cudaError_t e = cudaFuncSetAttribute(k_dens_bins, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  long long nseg = (long long)((p->box.N + 31) / 32) * p->box.N * p->box.N;
-  long long blocks = (nseg + BINS_WARPS - 1) / BINS_WARPS;
+  long long nrow = (long long)p->box.N * p->box.N;
+  long long blocks = (nrow + BINS_WARPS - 1) / BINS_WARPS;
   long long cap = (long long)nsm * 8;
   if (blocks > cap) blocks = cap;
   k_dens_bins<<<(unsigned)blocks, BINS_WARPS * 32, smem, s>>>(grid, *p);

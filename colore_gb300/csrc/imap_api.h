@@ -26,10 +26,11 @@ struct cg_imap_params {
   unsigned int *err;
   /* Cells with at least nsub_heavy sub-samples per side are listed by the
    * first kernel and painted by the second with their samples split evenly
-   * over all warps.  heavy_ctr packs (records << 40) | samples. */
+   * over all warps.  ctr[0] packs (heavy records << 40) | heavy samples,
+   * ctr[1] counts heavy chunks taken, ctr[2] rows taken (zeroed per launch). */
   int nsub_heavy;
   long long heavy_cap;
-  unsigned long long *heavy_ctr;
+  unsigned long long *ctr;
   long long *heavy_off;            /* first sample of each record          */
   struct cg_heavy_cell *heavy;     /* heavy_cap records                    */
 };

@@ -30,12 +30,12 @@ constexpr int CPT = 8;                 /* cells per thread */
 constexpr int SB = 256;                /* threads per block */
 constexpr int CPB = CPT * SB;          /* cells per block   */
 
-__device__ __forceinline__ void cell_of(long long c, int N, int &ix, int &iy, int &iz)
+__device__ __forceinline__ void cell_of(long long c, const Box &b, int &ix, int &iy, int &iz)
 {
-  ix = (int)(c % N);
-  long long q = c / N;
-  iy = (int)(q % N);
-  iz = (int)(q / N);
+  const long long q = divN(c, b), z = divN(q, b);
+  ix = (int)(c - q * b.N);
+  iy = (int)(q - z * b.N);
+  iz = (int)z;
 }
 
 __device__ __forceinline__ float pois_lambda(const cg_srcs_params &p, float d, float r)
@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(SB) k_pois_count(const float *__restrict__ gri
   long long tot = 0;
   if (c0 < ncell) {
     int ix, iy, iz;
-    cell_of(c0, N, ix, iy, iz);
+    cell_of(c0, p.box, ix, iy, iz);
     const float *row = grid + pidx(ix, iy, iz, N);
     const float y0 = cg_cell_coord(iy, p.box.dx, p.box.p1), z0 = cg_cell_coord(iz, p.box.dx, p.box.p2);
     unsigned short cnt[CPT];
@@ -158,7 +158,7 @@ __device__ __forceinline__ void grad_phi(const float *__restrict__ phi, int ix, 
   v[2] = CG_SUB(__ldg(&phi[pidx(ix, iy, zh, N)]), __ldg(&phi[pidx(ix, iy, zl, N)]));
 }
 
-__global__ void __launch_bounds__(SB) k_emit(const float *__restrict__ phi, cg_srcs_params p)
+__global__ void __launch_bounds__(SB, 3) k_emit(const float *__restrict__ phi, cg_srcs_params p)
 {
   const int N = p.box.N;
   const long long ncell = (long long)N * N * N;
@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(SB) k_emit(const float *__restrict__ phi, cg_s
   long long id = p.block_sums[blockIdx.x] + woff + inc - tot;
   if (tot == 0) return;
   int ix, iy, iz;
-  cell_of(c0, N, ix, iy, iz);
+  cell_of(c0, p.box, ix, iy, iz);
   const float dx = p.box.dx;
   const float y0 = cg_cell_coord(iy, dx, p.box.p1), z0 = cg_cell_coord(iz, dx, p.box.p2);
   for (int h = 0; h < CPT; h++) {
