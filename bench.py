@@ -184,9 +184,12 @@ def run_ours(args):
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    t_dl = 0.0
     for _ in range(e2e_steps):
         m.upload_tables()
         m.run()
+        m.sync()
+        t1 = time.perf_counter()
         d2h = 0
         for i in range(cfg.n_srcs):
             ns = m.num_sources(i)
@@ -202,8 +205,10 @@ def run_ours(args):
         if cfg.do_kappa:
             m.kappa(out=outs["kappa"])
             d2h += outs["kappa"].nbytes
+        t_dl += time.perf_counter() - t1
     torch.cuda.synchronize()
     t_e2e = (time.perf_counter() - t0) / e2e_steps
+    t_dl /= e2e_steps
     barrier()
     na = cg.NA
     h2d = 8 * (9 * na + 2 * na * (cfg.n_srcs + cfg.n_imap) + cfg.numk) // 2  # tables as float
@@ -227,6 +232,23 @@ def run_ours(args):
                       "_t": avg[name]}
     if rl:
         rl.pop("_t")
+    # per group: GB/s of the HBM-bound passes, samples/s where atomics or
+    # gathers bound the kernel (intensity-map sub-samples, kappa ray steps)
+    kern = {}
+    for name, t in avg.items():
+        if name in ALGO_BYTES_PER_CELL:
+            gbs = ALGO_BYTES_PER_CELL[name] * ncell / (t / 1e3) / 1e9
+            kern[name] = {"ms": round(t, 3), "GB/s": round(gbs, 1), "frac_hbm": round(gbs / hbm, 4)}
+        else:
+            kern[name] = {"ms": round(t, 3)}
+    if "imap_paint" in avg:
+        smp = sum(m.imap_samples(i) for i in range(cfg.n_imap))
+        kern["imap_paint"]["samples"] = smp
+        kern["imap_paint"]["samples/s"] = smp / (avg["imap_paint"] / 1e3)
+    if "kappa" in avg and cfg.do_kappa:
+        st = _kappa_steps(cfg)
+        kern["kappa"]["ray_steps"] = st
+        kern["kappa"]["ray_steps/s"] = st / (avg["kappa"] / 1e3)
     if rank != 0:
         return
     out = {
@@ -240,9 +262,11 @@ def run_ours(args):
                                   [cfg.nside_imap[i] for i in range(cfg.n_imap)], cfg.n_kappa if cfg.do_kappa else 0),
                    "n_grid": n, "l2": "inputs larger than L2 (4.3 GB per field)", "parallelism": "replicas"},
         "e2e": {"value": world * ncell / t_e2e, "unit": "cells/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "ms_per_step": t_e2e * 1e3},
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": t_e2e * 1e3,
+                "download_ms_per_step": t_dl * 1e3, "d2h_GB/s": d2h / max(t_dl, 1e-9) / 1e9},
         "gpu_launches": int(launches),
         "kernel_ms": {k: round(v, 3) for k, v in avg.items()},
+        "kernels": kern,
         "sources": nsrc,
         "wall_s_timed": t_wall,
         "roofline": rl,

@@ -53,6 +53,7 @@ struct Imap {
   float rmin = 0, rmax = 0;
   float *data = nullptr;
   int *nadd = nullptr;
+  unsigned long long samples = 0; /* sub-samples painted by the last run */
 };
 
 } /* namespace */
@@ -934,7 +935,7 @@ extern "C" int cg_imap_set_cartesian(cg_ctx *c)
           return rc;
         c->heavy_cap = want;
       }
-      if (!c->d_imap_ctr && (rc = dalloc(c, &c->d_imap_ctr, (size_t)3))) return rc;
+      if (!c->d_imap_ctr && (rc = dalloc(c, &c->d_imap_ctr, (size_t)5))) return rc;
       p.nsub_heavy = CG_NSUB_HEAVY;
       p.heavy_cap = want;
       p.ctr = c->d_imap_ctr;
@@ -945,9 +946,19 @@ extern "C" int cg_imap_set_cartesian(cg_ctx *c)
       ProfScope ps(c, "imap_paint");
       CUDA_TRY(c, cg_imap_paint(c->stream, c->d_dens, c->d_npot, &p, c->nsm));
     }
-    c->launches++;
+    c->launches += p.heavy_cap > 0 ? 2 : 1;
+    unsigned long long ns2[2] = {0, 0};
+    CUDA_TRY(c, cudaMemcpyAsync(ns2, c->d_imap_ctr + 3, sizeof(ns2), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host vectors above go out of scope */
+    M.samples = ns2[0] + ns2[1];
   }
+  return CG_OK;
+}
+
+extern "C" int cg_imap_samples(cg_ctx *c, int ipop, unsigned long long *n)
+{
+  if (!c || !n || ipop < 0 || ipop >= c->cfg.n_imap) return CG_EINVAL;
+  *n = c->im[ipop].samples;
   return CG_OK;
 }
 

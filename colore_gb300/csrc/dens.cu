@@ -11,9 +11,11 @@
  *                    tracer.  A warp owns 32 consecutive cells of a row;
  *                    lanes sharing a bin are reduced with shuffles (one pass
  *                    when the 32 cells share a bin, the common case) and lane
- *                    0 adds the sums to the warp's private FP64 bins in shared
- *                    memory, so no atomics are needed until the per-block
- *                    totals go to global memory.
+ *                    0 adds the sums to the warp's private bins in shared
+ *                    memory: integer counts and compensated (Kahan) FP32
+ *                    sums, since FP64 arithmetic is scarce on this GPU.  Each
+ *                    block combines its warps' bins in FP64 in a fixed order
+ *                    and sends them to global memory with one atomic each.
  *  k_lpt_cic       : 1LPT particle positions (density.c:473-501) and their
  *                    cloud-in-cell deposit (density.c:64-105).
  */
@@ -58,7 +60,7 @@ __global__ void k_moments_final(const double2 *__restrict__ part, size_t n, doub
 }
 
 constexpr int MAXT = 8;      /* tracers per bins launch */
-constexpr int BINS_WARPS = 8;
+constexpr int BINS_WARPS = 8; /* warps per block at most  */
 
 /* Warp reduction of v over the lanes whose mask bit is set (others add 0). */
 __device__ __forceinline__ float wsum(float v, bool mine)
@@ -69,21 +71,37 @@ __device__ __forceinline__ float wsum(float v, bool mine)
   return x;
 }
 
+/* Compensated FP32 accumulation s += v (c holds the running correction). */
+__device__ __forceinline__ void kahan_add(float &s, float &c, float v)
+{
+  const float y = __fsub_rn(v, c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
+  s = t;
+}
+
+/* Shared-memory bytes of one warp's bins: u32 count, then (sum, correction)
+ * for the redshift and every tracer. */
+__host__ __device__ inline size_t bins_warp_bytes(int nz, int nt) { return (size_t)nz * (4 + 8 * (1 + nt)); }
+
 __global__ void __launch_bounds__(BINS_WARPS * 32, 2) k_dens_bins(float *grid, cg_bins_params p)
 {
-  extern __shared__ double sbin[]; /* [warp][nz][2 + nt]; the count is an exact integer in FP64 */
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int nz = p.nz, nt = p.nt, W = 2 + nt;
-  double *mybins = sbin + (size_t)wid * nz * W;
-  for (int i = lane; i < nz * W; i += 32) mybins[i] = 0.0;
+  extern __shared__ unsigned char sbins[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+  const int nz = p.nz, nt = p.nt, W = 1 + nt;
+  unsigned int *cnt = reinterpret_cast<unsigned int *>(sbins + (size_t)wid * bins_warp_bytes(nz, nt));
+  float *acc = reinterpret_cast<float *>(cnt + nz); /* [nz][W] sums, then [nz][W] corrections */
+  float *cor = acc + (size_t)nz * W;
+  for (int i = lane; i < nz; i += 32) cnt[i] = 0u;
+  for (int i = lane; i < 2 * nz * W; i += 32) acc[i] = 0.0f;
   __syncwarp();
   const int N = p.box.N;
   const int nseg_row = (N + 31) / 32;
   const int nrow = N * N;
   const float s2 = p.sigma2f ? *p.sigma2f : 0.0f;
   const bool need_d1 = (p.mode == CG_DMODE_LGNR || p.mode == CG_DMODE_CLIP);
-  const int gw = blockIdx.x * BINS_WARPS + wid;
-  const int nw = gridDim.x * BINS_WARPS;
+  const int gw = blockIdx.x * nwb + wid;
+  const int nw = gridDim.x * nwb;
   /* a warp takes whole rows, 32 cells at a time */
   for (int row = gw; row < nrow; row += nw)
   for (int sr = 0; sr < nseg_row; sr++) {
@@ -127,27 +145,37 @@ __global__ void __launch_bounds__(BINS_WARPS * 32, 2) k_dens_bins(float *grid, c
 #pragma unroll
       for (int t = 0; t < MAXT; t++) bsum[t] = (t < nt) ? wsum(bs[t], mine) : 0.0f;
       if (lane == 0) {
-        double *dd = mybins + (size_t)lb * W;
-        dd[0] += (double)__popc(grp);
-        dd[1] += (double)zsum;
+        float *a = acc + (size_t)lb * W, *c = cor + (size_t)lb * W;
+        cnt[lb] += (unsigned)__popc(grp);
+        kahan_add(a[0], c[0], zsum);
 #pragma unroll
         for (int t = 0; t < MAXT; t++)
-          if (t < nt) dd[2 + t] += (double)bsum[t];
+          if (t < nt) kahan_add(a[1 + t], c[1 + t], bsum[t]);
       }
       todo &= ~grp;
     }
     __syncwarp();
   }
   __syncthreads();
-  /* combine the warps' bins in fixed order, then one global update per block */
-  for (int i = threadIdx.x; i < nz * W; i += blockDim.x) {
-    double s = 0.0;
-    for (int w = 0; w < BINS_WARPS; w++) s += sbin[(size_t)w * nz * W + i];
-    if (s != 0.0) {
-      int b = i / W, k = i - b * W;
-      if (k == 0) atomicAdd(&p.ncount[b], (unsigned long long)(s + 0.5));
-      else if (k == 1) atomicAdd(&p.zsum[b], s);
-      else atomicAdd(&p.bsum[(size_t)(k - 2) * nz + b], s);
+  /* combine the warps' bins in FP64 in fixed order, one global update each */
+  const size_t wb = bins_warp_bytes(nz, nt);
+  for (int i = threadIdx.x; i < nz * (1 + W); i += blockDim.x) {
+    const int b = i / (1 + W), k = i - b * (1 + W);
+    if (k == 0) {
+      unsigned long long n = 0;
+      for (int w = 0; w < nwb; w++) n += reinterpret_cast<const unsigned int *>(sbins + (size_t)w * wb)[b];
+      if (n) atomicAdd(&p.ncount[b], n);
+    } else {
+      double sum = 0.0;
+      for (int w = 0; w < nwb; w++) {
+        const unsigned int *cw = reinterpret_cast<const unsigned int *>(sbins + (size_t)w * wb);
+        const float *aw = reinterpret_cast<const float *>(cw + nz);
+        sum += (double)aw[(size_t)b * W + k - 1] - (double)aw[(size_t)nz * W + (size_t)b * W + k - 1];
+      }
+      if (sum != 0.0) {
+        if (k == 1) atomicAdd(&p.zsum[b], sum);
+        else atomicAdd(&p.bsum[(size_t)(k - 2) * nz + b], sum);
+      }
     }
   }
 }
@@ -211,18 +239,25 @@ cudaError_t cg_moments_final(cudaStream_t s, const double2 *part, size_t n, doub
 
 cudaError_t cg_dens_bins(cudaStream_t s, float *grid, const cg_bins_params *p, int nsm)
 {
-  size_t smem = (size_t)BINS_WARPS * p->nz * (2 + p->nt) * sizeof(double);
+  if (p->nt < 0 || p->nt > MAXT || p->nz < 0) return cudaErrorInvalidValue;
+  /* as many warps per block (up to 8) as the bins of each fit in 200 KiB */
+  const size_t wb = bins_warp_bytes(p->nz, p->nt);
+  int nwb = BINS_WARPS;
+  while (nwb > 1 && (size_t)nwb * wb > 200u * 1024u) nwb--;
+  if ((size_t)nwb * wb > 200u * 1024u) return cudaErrorInvalidValue;
+  const size_t smem = (size_t)nwb * wb;
   cudaError_t e = cudaFuncSetAttribute(k_dens_bins, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   long long nrow = (long long)p->box.N * p->box.N;
-  long long blocks = (nrow + BINS_WARPS - 1) / BINS_WARPS;
+  long long blocks = (nrow + nwb - 1) / nwb;
   long long cap = (long long)nsm * 8;
   if (blocks > cap) blocks = cap;
-  k_dens_bins<<<(unsigned)blocks, BINS_WARPS * 32, smem, s>>>(grid, *p);
+  k_dens_bins<<<(unsigned)blocks, nwb * 32, smem, s>>>(grid, *p);
   return cudaGetLastError();
 }
 
 int cg_dens_bins_max_tracers(void) { return MAXT; }
+
 
 cudaError_t cg_lpt_cic(cudaStream_t s, float *grid, const float *dx, const float *dy, const float *dz,
                        const cg_lpt_params *p, int nsm)

@@ -34,6 +34,7 @@ cudaError_t cg_moments_final(cudaStream_t s, const double2 *part, size_t n, doub
                              float *s2f);
 cudaError_t cg_dens_bins(cudaStream_t s, float *grid, const cg_bins_params *p, int nsm);
 int cg_dens_bins_max_tracers(void);
+
 cudaError_t cg_lpt_cic(cudaStream_t s, float *grid, const float *dx, const float *dy, const float *dz,
                        const cg_lpt_params *p, int nsm);
 

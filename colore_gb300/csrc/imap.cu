@@ -18,16 +18,17 @@
  *                 heavy list, with their first sample offset from one 64-bit
  *                 atomic that counts records and samples together, so the
  *                 offsets are an exclusive prefix in list order.  The lanes
- *                 then take the x-lines of sub-samples (nsub^2 per cell, nsub
- *                 samples each) of the remaining cells.
+ *                 then take the sub-samples of the remaining cells, 32
+ *                 consecutive ones at a time.
  *   k_imap_heavy  The heavy samples are cut into 8 chunks per warp, taken
  *                 from a counter; a warp finds the first cell of its chunk by
- *                 binary search on the offsets and paints 32 lines of one
- *                 cell at a time.
+ *                 binary search on the offsets and paints 32 consecutive
+ *                 samples at a time.
  *
- * Along a line y, z and y^2+z^2 are computed once and consecutive samples
- * landing on the same (shell, pixel) are merged in registers.  Those runs go
- * to a per-warp shared-memory hash table keyed by (shell, pixel) that sums
+ * Consecutive samples (x fastest) of a cell often land on the same (shell,
+ * pixel); each run of equal keys across the lanes is found with one shuffle
+ * and a ballot and added once.  The runs go to a per-warp shared-memory hash
+ * table keyed by (shell, pixel) that sums
  * the brightness (temp * run) and the hits: each pixel receives tens of
  * sub-samples of a cell, and neighbouring cells share pixels, so the table
  * turns one global atomic pair per sub-sample into one per distinct key.
@@ -145,35 +146,51 @@ __device__ __forceinline__ void insert(Table<K> &w, K key, unsigned int c, float
   atomicAdd(&p.nadd[(long long)key], (int)c);
 }
 
-/* Paint x-line l (l = izz * ns + iyy) of cell c, whose corner is (c.x0, y0, z0). */
+/* Key of sample q (0 <= q < ns^3, x fastest, then y, then z) of cell c, whose
+ * corner is (c.x0, y0, z0), or the empty key outside the shells. */
 template <typename K>
-__device__ __forceinline__ void paint_line(Table<K> &w, const cg_imap_params &p, const float *r0, const float *rf,
-                                           const CellPar &c, float y0, float z0, int l)
+__device__ __forceinline__ K sample_key(const cg_imap_params &p, const float *r0, const float *rf, const CellPar &c,
+                                        float y0, float z0, int q)
 {
   const int ns = c.nsub;
-  /* (l + 1/2)/ns is at least 1/(2 ns) from an integer: exact for ns <= 128 */
-  const int izz = ns <= 128 ? (int)(((float)l + 0.5f) * c.inv_ns) : l / ns;
-  const int iyy = l - izz * ns;
+  int line, izz;
+  if (ns <= 128) {
+    /* (q + 1/2)/ns is at least 1/(2 ns) from an integer and the float
+     * product is within ns^2 2^-23 of it: exact while ns^3 < 2^22 */
+    line = (int)(((float)q + 0.5f) * c.inv_ns);
+    izz = (int)(((float)line + 0.5f) * c.inv_ns);
+  } else {
+    line = q / ns;
+    izz = line / ns;
+  }
+  const int ixx = q - line * ns, iyy = line - izz * ns;
   const float zc = cg_sub_centre(z0, izz, c.dxs);
   const float yc = cg_sub_centre(y0, iyy, c.dxs);
   const float yz2 = CG_ADD(CG_MUL(yc, yc), CG_MUL(zc, zc));
-  K cur = empty_key<K>();
-  unsigned int run = 0;
-  for (int ixx = 0; ixx < ns; ixx++) {
-    const float xc = cg_sub_centre(c.x0, ixx, c.dxs);
-    int64_t pix = 0;
-    const int ir = cg_imap_sample(xc, yc, zc, yz2, c.drr, r0, rf, p.nr, c.irad0, p.nside, &pix);
-    if (ir < 0 || ir >= p.nr) continue;
-    const K key = (K)((long long)ir * p.npix + pix);
-    if (key == cur) {
-      run++;
-    } else {
-      if (run) insert(w, cur, run, c.temp, p);
-      cur = key;
-      run = 1;
-    }
+  const float xc = cg_sub_centre(c.x0, ixx, c.dxs);
+  int64_t pix = 0;
+  const int ir = cg_imap_sample(xc, yc, zc, yz2, c.drr, r0, rf, p.nr, c.irad0, p.nside, &pix);
+  if (ir < 0 || ir >= p.nr) return empty_key<K>();
+  return (K)((long long)ir * p.npix + pix);
+}
+
+/* The lanes hold consecutive samples: each run of equal (tag, key) is added
+ * once, by its first lane, with its length.  tag separates cells. */
+template <typename K>
+__device__ __forceinline__ void insert_runs(Table<K> &w, K key, int tag, float temp, int lane,
+                                            const cg_imap_params &p)
+{
+  const unsigned FULL = 0xffffffffu;
+  const K pk = __shfl_up_sync(FULL, key, 1);
+  const int pt = __shfl_up_sync(FULL, tag, 1);
+  const bool valid = key != empty_key<K>();
+  const bool head = valid && (lane == 0 || pk != key || pt != tag);
+  const unsigned bnd = __ballot_sync(FULL, head || !valid);
+  if (head) {
+    const unsigned above = lane == 31 ? 0u : bnd & (FULL << (lane + 1));
+    const int end = above ? __ffs(above) - 1 : 32;
+    insert(w, key, (unsigned int)(end - lane), temp, p);
   }
-  if (run) insert(w, cur, run, c.temp, p);
 }
 
 constexpr unsigned long long HREC = 1ull << 40;     /* one heavy record    */
@@ -204,11 +221,17 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap(const float *__restrict__ d
   const int nrow = N * N;
   const float dx = p.box.dx;
   const unsigned FULL = 0xffffffffu;
+  unsigned long long painted = 0; /* samples of the cells painted by this lane */
   for (;;) {
     int rbeg = 0;
     if (lane == 0) rbeg = (int)atomicAdd(&p.ctr[2], (unsigned long long)ROWS);
     rbeg = __shfl_sync(FULL, rbeg, 0);
-    if (rbeg >= nrow) break;
+    if (rbeg >= nrow) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) painted += __shfl_xor_sync(FULL, painted, o);
+      if (lane == 0 && painted) atomicAdd(&p.ctr[3], painted);
+      break;
+    }
     const int rend = rbeg + ROWS < nrow ? rbeg + ROWS : nrow;
     for (int row = rbeg; row < rend; row++)
     for (int ch = 0; ch < nch; ch++) {
@@ -285,16 +308,21 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap(const float *__restrict__ d
           n = 0;
         }
       }
+      /* cells painted here keep the warp's sample count below 2^26 */
+      if (n > 0 && cp.nsub > 128) {
+        atomicOr(p.err, ERR_IMAP_HEAVY);
+        n = 0;
+      }
       wc[lane] = cp;
-      /* inclusive scan of the line counts (nsub^2 per cell) over the warp */
-      const int nl = cp.nsub * cp.nsub;
-      int incl = n > 0 ? nl : 0;
+      painted += (unsigned long long)n;
+      /* inclusive scan of the sample counts (nsub^3 per cell) over the warp */
+      int incl = n;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         int t = __shfl_up_sync(FULL, incl, o);
         if (lane >= o) incl += t;
       }
-      const int excl = incl - (n > 0 ? nl : 0);
+      const int excl = incl - n;
       const int total = __shfl_sync(FULL, incl, 31);
       __syncwarp();
       for (int base = 0; base < total; base += 32) {
@@ -308,7 +336,14 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap(const float *__restrict__ d
         }
         if (j > 31) j = 31;
         const int ex = __shfl_sync(FULL, excl, j);
-        if (s < total) paint_line(w, p, r0, rf, wc[j], y0, z0, s - ex);
+        K key = empty_key<K>();
+        float temp = 0.0f;
+        if (s < total) {
+          const CellPar c = wc[j];
+          key = sample_key<K>(p, r0, rf, c, y0, z0, s - ex);
+          temp = c.temp;
+        }
+        insert_runs(w, key, j, temp, lane, p);
         __syncwarp();
         if (*(volatile int *)&w.nused >= HFLUSH) flush(w, lane, p);
       }
@@ -341,6 +376,7 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap_heavy(cg_imap_params p)
   const long long *off = p.heavy_off;
   const long long nlast = hl[H - 1].nsub;
   const unsigned long long S = (unsigned long long)(off[H - 1] + nlast * nlast * nlast);
+  if (blockIdx.x == 0 && threadIdx.x == 0) p.ctr[4] = S;
   const unsigned long long NC = (unsigned long long)gridDim.x * IW * CHUNKS;
   const unsigned FULL = 0xffffffffu;
   for (;;) {
@@ -357,7 +393,6 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap_heavy(cg_imap_params p)
       if (off[mid] <= s0) lo = mid;
       else hi = mid - 1;
     }
-    /* a line belongs to the chunk that holds its first sample */
     for (long long h = lo; h < H && off[h] < s1; h++) {
       const float4 qa = __ldg(reinterpret_cast<const float4 *>(hl + h));
       const float4 qb = __ldg(reinterpret_cast<const float4 *>(hl + h) + 1);
@@ -371,11 +406,13 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap_heavy(cg_imap_params p)
       c.inv_ns = 1.0f / (float)c.nsub;
       c.pad = 0;
       const long long ns = c.nsub, base = off[h];
-      const long long la = s0 > base ? (s0 - base + ns - 1) / ns : 0;
-      long long lb = (s1 - base + ns - 1) / ns;
-      if (lb > ns * ns) lb = ns * ns;
-      for (long long l = la; l < lb; l += 32) {
-        if (l + lane < lb) paint_line(w, p, r0, rf, c, qa.y, qa.z, (int)(l + lane));
+      const long long qbeg = s0 > base ? s0 - base : 0;
+      long long qend = s1 - base;
+      if (qend > ns * ns * ns) qend = ns * ns * ns;
+      for (long long q0 = qbeg; q0 < qend; q0 += 32) {
+        const long long q = q0 + lane;
+        const K key = q < qend ? sample_key<K>(p, r0, rf, c, qa.y, qa.z, (int)q) : empty_key<K>();
+        insert_runs(w, key, 0, c.temp, lane, p);
         __syncwarp();
         if (*(volatile int *)&w.nused >= HFLUSH) flush(w, lane, p);
       }
@@ -394,7 +431,7 @@ cudaError_t launch(cudaStream_t s, const float *dens, const float *phi, const cg
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_imap<K>, IW * 32, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
-  e = cudaMemsetAsync(p->ctr, 0, 3 * sizeof(unsigned long long), s);
+  e = cudaMemsetAsync(p->ctr, 0, 5 * sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
   long long nrow = (long long)p->box.N * p->box.N;
   long long blocks = (nrow + IW * ROWS - 1) / (IW * ROWS);

@@ -27,7 +27,8 @@ struct cg_imap_params {
   /* Cells with at least nsub_heavy sub-samples per side are listed by the
    * first kernel and painted by the second with their samples split evenly
    * over all warps.  ctr[0] packs (heavy records << 40) | heavy samples,
-   * ctr[1] counts heavy chunks taken, ctr[2] rows taken (zeroed per launch). */
+   * ctr[1] counts heavy chunks taken, ctr[2] rows taken, ctr[3] and ctr[4]
+   * the samples painted by each kernel (all zeroed per launch). */
   int nsub_heavy;
   long long heavy_cap;
   unsigned long long *ctr;

@@ -13,7 +13,9 @@
  *   k_scan       : exclusive scan of the block totals (one block).
  *   k_emit       : re-reads the counts, scans them inside the block and writes
  *                  every source at its final catalog index, in cell order (the
- *                  order of the reference run with one thread).  Positions,
+ *                  order of the reference run with one thread); the block's
+ *                  sources are spread evenly over its threads, each finding
+ *                  its cell by binary search on the scanned offsets.  Positions,
  *                  the NGP velocity (get_rvel, srcs.c:87-118), ra/dec/z, the
  *                  base-pixel id and the count-map increment are fused.
  */
@@ -158,30 +160,27 @@ __device__ __forceinline__ void grad_phi(const float *__restrict__ phi, int ix, 
   v[2] = CG_SUB(__ldg(&phi[pidx(ix, iy, zh, N)]), __ldg(&phi[pidx(ix, iy, zl, N)]));
 }
 
-__global__ void __launch_bounds__(SB, 3) k_emit(const float *__restrict__ phi, cg_srcs_params p)
+__global__ void __launch_bounds__(SB) k_emit(const float *__restrict__ phi, cg_srcs_params p)
 {
+  __shared__ int coff[CPB + 1]; /* exclusive source offset of each cell in the block */
+  __shared__ int ws[SB / 32];
   const int N = p.box.N;
   const long long ncell = (long long)N * N * N;
-  const long long c0 = (long long)blockIdx.x * CPB + (long long)threadIdx.x * CPT;
-  uint64_t clo = 0, chi = 0; /* 8 packed uint16 counts */
+  const long long cb = (long long)blockIdx.x * CPB;
+  const long long c0 = cb + (long long)threadIdx.x * CPT;
+  int n[CPT];
   int tot = 0;
-  bool esc = false;
-  if (c0 < ncell) {
-    uint4 pk = *reinterpret_cast<const uint4 *>(p.counts + c0);
-    clo = (uint64_t)pk.x | ((uint64_t)pk.y << 32);
-    chi = (uint64_t)pk.z | ((uint64_t)pk.w << 32);
 #pragma unroll
-    for (int h = 0; h < 4; h++) {
-      const int a = (int)((clo >> (16 * h)) & 0xffffu), b = (int)((chi >> (16 * h)) & 0xffffu);
-      esc |= (a == CG_COUNT_ESC) | (b == CG_COUNT_ESC);
-      tot += a + b;
-    }
-    if (esc) {
-      tot = 0;
-      for (int h = 0; h < CPT; h++) {
-        const int n = (int)(((h < 4 ? clo : chi) >> (16 * (h & 3))) & 0xffffu);
-        tot += n == CG_COUNT_ESC ? ovf_lookup(p, c0 + h) : n;
-      }
+  for (int h = 0; h < CPT; h++) n[h] = 0;
+  if (c0 < ncell) {
+    const uint4 pk = *reinterpret_cast<const uint4 *>(p.counts + c0);
+    const unsigned w4[4] = {pk.x, pk.y, pk.z, pk.w};
+#pragma unroll
+    for (int h = 0; h < CPT; h++) {
+      int v = (int)((w4[h >> 1] >> (16 * (h & 1))) & 0xffffu);
+      if (v == CG_COUNT_ESC) v = ovf_lookup(p, c0 + h);
+      n[h] = v;
+      tot += v;
     }
   }
   /* block exclusive scan of per-thread totals */
@@ -192,53 +191,67 @@ __global__ void __launch_bounds__(SB, 3) k_emit(const float *__restrict__ phi, c
     int t = __shfl_up_sync(0xffffffffu, inc, o);
     if (lane >= o) inc += t;
   }
-  __shared__ int ws[SB / 32];
   if (lane == 31) ws[wid] = inc;
   __syncthreads();
   int woff = 0;
   for (int w = 0; w < wid; w++) woff += ws[w];
-  long long id = p.block_sums[blockIdx.x] + woff + inc - tot;
-  if (tot == 0) return;
-  int ix, iy, iz;
-  cell_of(c0, p.box, ix, iy, iz);
-  const float dx = p.box.dx;
-  const float y0 = cg_cell_coord(iy, dx, p.box.p1), z0 = cg_cell_coord(iz, dx, p.box.p2);
+  int run = woff + inc - tot;
+#pragma unroll
   for (int h = 0; h < CPT; h++) {
-    int n = (int)(((h < 4 ? clo : chi) >> (16 * (h & 3))) & 0xffffu);
-    if (n == 0) continue;
-    if (esc && n == CG_COUNT_ESC) n = ovf_lookup(p, c0 + h);
-    const float x0 = cg_cell_coord(ix + h, dx, p.box.p0);
+    coff[threadIdx.x * CPT + h] = run;
+    run += n[h];
+  }
+  if (threadIdx.x == SB - 1) coff[CPB] = run;
+  __syncthreads();
+  /* the block's sources, spread evenly over its threads: consecutive threads
+   * write consecutive catalogue entries */
+  const int T = coff[CPB];
+  const long long base = p.block_sums[blockIdx.x];
+  const float dx = p.box.dx;
+  for (int k = threadIdx.x; k < T; k += SB) {
+    /* the cell holding source k: the last cell whose offset is <= k (cells
+     * without sources share their successor's offset) */
+    int lo = 0, hi = CPB - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (coff[mid] <= k) lo = mid;
+      else hi = mid - 1;
+    }
+    const int j = k - coff[lo];
+    const long long cid = cb + lo;
+    const long long id = base + k;
+    if (id >= p.capacity) {
+      atomicOr(p.err, ERR_CATALOG_OVERFLOW);
+      break;
+    }
+    int ix, iy, iz;
+    cell_of(cid, p.box, ix, iy, iz);
+    const float x0 = cg_cell_coord(ix, dx, p.box.p0);
+    const float y0 = cg_cell_coord(iy, dx, p.box.p1), z0 = cg_cell_coord(iz, dx, p.box.p2);
     const float rr = cg_norm3(x0, y0, z0);
     float v[3];
-    grad_phi(phi, ix + h, iy, iz, N, v);
-    float rvel = CG_MUL(p.factor_vel, cg_rvel(v[0], v[1], v[2], x0, y0, z0, rr, p.box.idx));
-    float dz_rsd = CG_MUL(rvel, bg(p.v1, p.g, rr));
-    const long long cid = c0 + h;
-    for (int j = 0; j < n; j++, id++) {
-      if (id >= p.capacity) {
-        atomicOr(p.err, ERR_CATALOG_OVERFLOW);
-        return;
-      }
-      cg_u32x4 u = cg_philox4x32_10((uint32_t)cid, (uint32_t)(cid >> 32), (uint32_t)j, 0u, p.kq0, p.kq1);
-      float px = cg_src_offset(x0, dx, u.v[0]);
-      float py = cg_src_offset(y0, dx, u.v[1]);
-      float pz = cg_src_offset(z0, dx, u.v[2]);
-      p.pos[id] = make_float4(px, py, pz, dz_rsd);
-      float r, cth, ph;
-      cg_cart2sph(px, py, pz, &r, &cth, &ph);
-      int64_t pr = cg_ang2pix_ring(p.nside_base, cth, ph);
-      p.ipix[id] = (int)cg_ring2nest(p.nside_base, pr);
-      float *s = p.src + (size_t)id * 9;
-      cg_radec(cth, ph, &s[0], &s[1]);                              /* ra, dec */
-      s[2] = bg(p.zt, p.g, r);                                      /* z0  */
-      s[3] = p.need_beaming ? 0.0f : dz_rsd;                        /* dz_rsd */
-      s[4] = p.need_beaming ? 0.0f : -1.0f;                         /* e1  */
-      s[5] = p.need_beaming ? 0.0f : -1.0f;                         /* e2  */
-      s[6] = 0.0f;
-      s[7] = 0.0f;
-      s[8] = 0.0f;
-      if (p.cmap) atomicAdd(&p.cmap[cg_ang2pix_ring(p.nside_count, cth, ph)], 1);
-    }
+    grad_phi(phi, ix, iy, iz, N, v);
+    const float rvel = CG_MUL(p.factor_vel, cg_rvel(v[0], v[1], v[2], x0, y0, z0, rr, p.box.idx));
+    const float dz_rsd = CG_MUL(rvel, bg(p.v1, p.g, rr));
+    cg_u32x4 u = cg_philox4x32_10((uint32_t)cid, (uint32_t)(cid >> 32), (uint32_t)j, 0u, p.kq0, p.kq1);
+    const float px = cg_src_offset(x0, dx, u.v[0]);
+    const float py = cg_src_offset(y0, dx, u.v[1]);
+    const float pz = cg_src_offset(z0, dx, u.v[2]);
+    p.pos[id] = make_float4(px, py, pz, dz_rsd);
+    float r, cth, ph;
+    cg_cart2sph(px, py, pz, &r, &cth, &ph);
+    int64_t pr = cg_ang2pix_ring(p.nside_base, cth, ph);
+    p.ipix[id] = (int)cg_ring2nest(p.nside_base, pr);
+    float *q = p.src + (size_t)id * 9;
+    cg_radec(cth, ph, &q[0], &q[1]);                              /* ra, dec */
+    q[2] = bg(p.zt, p.g, r);                                      /* z0  */
+    q[3] = p.need_beaming ? 0.0f : dz_rsd;                        /* dz_rsd */
+    q[4] = p.need_beaming ? 0.0f : -1.0f;                         /* e1  */
+    q[5] = p.need_beaming ? 0.0f : -1.0f;                         /* e2  */
+    q[6] = 0.0f;
+    q[7] = 0.0f;
+    q[8] = 0.0f;
+    if (p.cmap) atomicAdd(&p.cmap[cg_ang2pix_ring(p.nside_count, cth, ph)], 1);
   }
 }
 

@@ -142,6 +142,9 @@ int cg_set_norm_tables(cg_ctx *ctx, const double *srcs_norm, const double *srcs_
                        const double *imap_norm, const double *imap_norm_0f);
 int cg_srcs_set_cartesian(cg_ctx *ctx, long long *nsrc_per_pop);
 int cg_imap_set_cartesian(cg_ctx *ctx);
+/* Sub-samples (cells x nsub^3, imap.c:158-231) painted for species ipop by
+ * the last cg_imap_set_cartesian. */
+int cg_imap_samples(cg_ctx *ctx, int ipop, unsigned long long *n);
 int cg_get_beam_properties(cg_ctx *ctx);
 /* Run the whole driver sequence of src/main.c:66-125 in one call. */
 int cg_run_mock(cg_ctx *ctx);

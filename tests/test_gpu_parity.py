@@ -310,6 +310,20 @@ def test_imap_vs_dev32(runs, kind):
         assert gn.sum() > 0
 
 
+@pytest.mark.parametrize("kind", ["full", "heavy"])
+def test_imap_sample_count(runs, kind):
+    """Sub-samples painted (cells in range x nsub^3) against the FP64 count;
+    the GPU places cells by their FP32 radius, so a few cells at the range and
+    shell edges may differ."""
+    import oracle as orc
+    r = runs(kind)
+    r.need('imaps')
+    for ip in range(r.cfg.n_imap):
+        want = orc.lib().or_imap_samples(orc.cfgp(r.cfg), ip)
+        got = r.m.imap_samples(ip)
+        assert want > 0 and abs(got - want) <= 1e-3 * want, (got, want)
+
+
 def test_imap_vs_fp64(runs):
     import oracle as orc
     r = runs("nobeam")
