@@ -82,6 +82,8 @@ def lib():
             "cg_compute_density_normalization": (C.c_int, [vp]),
             "cg_collect_density_normalization": (C.c_int, [vp, C.c_int, C.c_double, _dp,
                                                            C.POINTER(C.c_ulonglong), _dp, _dp]),
+            "cg_collect_density_normalization_static": (C.c_int, [vp, C.c_int, C.c_double, _dp,
+                                                                  C.POINTER(C.c_ulonglong), _dp, _dp]),
             "cg_set_norm_tables": (C.c_int, [vp, _dp, _dp, _dp, _dp]),
             "cg_srcs_set_cartesian": (C.c_int, [vp, C.POINTER(C.c_longlong)]),
             "cg_imap_set_cartesian": (C.c_int, [vp]),
@@ -116,7 +118,7 @@ def exported_symbols():
     return ["cg_create", "cg_destroy", "cg_last_error", "cg_set_stream", "cg_sync", "cg_memory_estimate",
             "cg_upload_tables", "cg_create_cartesian_fields", "cg_get_sigma2",
             "cg_compute_physical_density_field", "cg_compute_density_normalization",
-            "cg_collect_density_normalization", "cg_set_norm_tables", "cg_srcs_set_cartesian",
+            "cg_collect_density_normalization", "cg_collect_density_normalization_static", "cg_set_norm_tables", "cg_srcs_set_cartesian",
             "cg_imap_set_cartesian", "cg_imap_samples", "cg_get_beam_properties", "cg_run_mock", "cg_download_grid",
             "cg_num_sources", "cg_download_catalog", "cg_download_count_map", "cg_download_imap",
             "cg_download_kappa", "cg_download_norm", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_read_run_params",

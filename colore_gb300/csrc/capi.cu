@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -647,6 +648,87 @@ extern "C" int cg_collect_density_normalization(cg_ctx *c, int nz, double idz, d
   if (zarr) memcpy(zarr, z.data(), nz * sizeof(double));
   if (norm_srcs && nts) memcpy(norm_srcs, b.data(), (size_t)nts * nz * sizeof(double));
   if (norm_imap && nti) memcpy(norm_imap, b.data() + (size_t)nts * nz, (size_t)nti * nz * sizeof(double));
+  return CG_OK;
+}
+
+/* Device address of the static bins scratch, looked up once per device with
+ * that device current (cudaGetSymbolAddress may load the module, so the
+ * first call on a device must not be inside a stream capture) and kept for
+ * the life of the process. */
+static std::mutex g_bins_scratch_mu;
+static void *g_bins_scratch_ptr[64];
+
+static int bins_static_scratch(cg_ctx *c, void **out)
+{
+  if (c->device < 0 || c->device >= 64) return fail(c, CG_EINVAL, "device %d out of range", c->device);
+  std::lock_guard<std::mutex> lock(g_bins_scratch_mu);
+  if (!g_bins_scratch_ptr[c->device]) {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t e = cg_dens_bins_static_scratch(&ptr, &bytes);
+    if (e != cudaSuccess || !ptr)
+      return fail(c, CG_ECUDA, "cudaGetSymbolAddress(bins scratch): %s", cudaGetErrorString(e));
+    g_bins_scratch_ptr[c->device] = ptr;
+  }
+  *out = g_bins_scratch_ptr[c->device];
+  return CG_OK;
+}
+
+/* cg_collect_density_normalization without any allocation: the per-bin
+ * counts and sums live in a fixed module-scope device array instead of
+ * buffers made with cudaMalloc, and the results are copied straight into the
+ * caller's arrays.  Calls overlapping on the GPU (two contexts on one device,
+ * or two streams) share that array and race. */
+extern "C" int cg_collect_density_normalization_static(cg_ctx *c, int nz, double idz, double *zarr,
+                                                       unsigned long long *narr, double *norm_srcs,
+                                                       double *norm_imap)
+{
+  if (!c) return CG_EINVAL;
+  if (!c->have_density) return fail(c, CG_ESTATE, "compute_physical_density_field first");
+  if (nz < 2 || nz > CG_BINS_STATIC_NZ)
+    return fail(c, CG_EINVAL, "nz=%d: the static bins scratch holds 2 to %d bins", nz, CG_BINS_STATIC_NZ);
+  const int nts = c->cfg.n_srcs, nti = c->cfg.n_imap, nt = nts + nti;
+  if (nt > cg_dens_bins_max_tracers())
+    return fail(c, CG_EINVAL, "%d tracers: at most %d per run are supported", nt, cg_dens_bins_max_tracers());
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  void *scratch = nullptr;
+  if (int rc = bins_static_scratch(c, &scratch)) return rc;
+  unsigned long long *ncount = static_cast<unsigned long long *>(scratch);
+  double *zsum = static_cast<double *>(scratch) + CG_BINS_STATIC_NZ;
+  double *bsum = static_cast<double *>(scratch) + 2 * CG_BINS_STATIC_NZ;
+  /* the sums start at zero on every call */
+  CUDA_TRY(c, cudaMemsetAsync(ncount, 0, sizeof(unsigned long long) * nz, c->stream));
+  CUDA_TRY(c, cudaMemsetAsync(zsum, 0, sizeof(double) * nz, c->stream));
+  if (nt > 0) CUDA_TRY(c, cudaMemsetAsync(bsum, 0, sizeof(double) * nt * nz, c->stream));
+  cg_bins_params p;
+  memset(&p, 0, sizeof(p));
+  p.box = c->box;
+  p.g = c->g;
+  p.zt = c->zt;
+  p.d1 = c->d1;
+  p.mode = c->pending_mode;
+  p.sigma2f = c->d_s2f;
+  p.nz = nz;
+  p.idz = (float)idz;
+  p.bias_model = c->cfg.bias_model;
+  p.nt = nt;
+  for (int t = 0; t < nt; t++) p.bz[t] = t < nts ? c->bz[t] : c->bzi[t - nts];
+  p.ncount = ncount;
+  p.zsum = zsum;
+  p.bsum = bsum;
+  CUDA_TRY(c, cg_dens_bins(c->stream, c->d_dens, &p, c->nsm));
+  c->launches++;
+  c->pending_mode = CG_DMODE_NONE;
+  if (narr)
+    CUDA_TRY(c, cudaMemcpyAsync(narr, ncount, nz * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
+  if (zarr) CUDA_TRY(c, cudaMemcpyAsync(zarr, zsum, nz * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (norm_srcs && nts)
+    CUDA_TRY(c, cudaMemcpyAsync(norm_srcs, bsum, (size_t)nts * nz * sizeof(double), cudaMemcpyDeviceToHost,
+                                c->stream));
+  if (norm_imap && nti)
+    CUDA_TRY(c, cudaMemcpyAsync(norm_imap, bsum + (size_t)nts * nz, (size_t)nti * nz * sizeof(double),
+                                cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return CG_OK;
 }
 

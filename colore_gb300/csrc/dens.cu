@@ -258,6 +258,17 @@ cudaError_t cg_dens_bins(cudaStream_t s, float *grid, const cg_bins_params *p, i
 
 int cg_dens_bins_max_tracers(void) { return MAXT; }
 
+/* Scratch of the allocation-free bins entry: u64 counts [CG_BINS_STATIC_NZ],
+ * redshift sums [CG_BINS_STATIC_NZ], bias sums [MAXT][nz] (doubles).  A
+ * module-scope array costs no allocation call at run time: it exists in
+ * every context that loads this module. */
+static __device__ __align__(256) unsigned char g_bins_scratch[(size_t)CG_BINS_STATIC_NZ * (2 + MAXT) * 8];
+
+cudaError_t cg_dens_bins_static_scratch(void **ptr, size_t *bytes)
+{
+  *bytes = sizeof(g_bins_scratch);
+  return cudaGetSymbolAddress(ptr, g_bins_scratch);
+}
 
 cudaError_t cg_lpt_cic(cudaStream_t s, float *grid, const float *dx, const float *dy, const float *dz,
                        const cg_lpt_params *p, int nsm)

@@ -35,6 +35,13 @@ cudaError_t cg_moments_final(cudaStream_t s, const double2 *part, size_t n, doub
 cudaError_t cg_dens_bins(cudaStream_t s, float *grid, const cg_bins_params *p, int nsm);
 int cg_dens_bins_max_tracers(void);
 
+/* Largest number of redshift bins of the allocation-free bins entry, whose
+ * scratch (per bin: cell count, redshift sum and one bias sum per tracer,
+ * for up to cg_dens_bins_max_tracers() tracers) is a fixed device array of
+ * CG_BINS_STATIC_NZ * 10 * 8 bytes = 80 KiB. */
+#define CG_BINS_STATIC_NZ 1024
+/* Device address and size of that array in the current device's context. */
+cudaError_t cg_dens_bins_static_scratch(void **ptr, size_t *bytes);
 cudaError_t cg_lpt_cic(cudaStream_t s, float *grid, const float *dx, const float *dy, const float *dz,
                        const cg_lpt_params *p, int nsm);
 

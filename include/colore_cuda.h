@@ -137,6 +137,20 @@ int cg_compute_density_normalization(cg_ctx *ctx);
 int cg_collect_density_normalization(cg_ctx *ctx, int nz, double idz, double *zarr,
                                      unsigned long long *narr, double *norm_srcs,
                                      double *norm_imap);
+/* Allocation-free variant of cg_collect_density_normalization (no
+ * counterpart in the reference): same arguments and results, for callers
+ * that may not allocate while the pipeline runs (a fixed memory budget, a
+ * pool that must not grow).  Its per-bin scratch is a fixed 80 KiB
+ * module-scope device array rather than cudaMalloc'd buffers, so
+ *  - nz is limited to 2..1024 bins (CG_EINVAL beyond, with a message);
+ *  - the first call on each device looks up that array's address with the
+ *    device current; make that first call before any stream capture;
+ *  - calls that overlap on the GPU (two contexts on one device, or the
+ *    same context on two streams) share the array and race.
+ * The sums are zeroed on the context's stream at every call. */
+int cg_collect_density_normalization_static(cg_ctx *ctx, int nz, double idz, double *zarr,
+                                            unsigned long long *narr, double *norm_srcs,
+                                            double *norm_imap);
 /* Replace the NA-point normalisation tables (src/density.c:1323-1355). */
 int cg_set_norm_tables(cg_ctx *ctx, const double *srcs_norm, const double *srcs_norm_0f,
                        const double *imap_norm, const double *imap_norm_0f);
