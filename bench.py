@@ -191,19 +191,26 @@ def run_ours(args):
         m.sync()
         t1 = time.perf_counter()
         d2h = 0
+        split = {}
         for i in range(cfg.n_srcs):
             ns = m.num_sources(i)
             c = {"pos": outs["pos%d" % i][:ns], "ipix": outs["ipix%d" % i][:ns], "src": outs["src%d" % i][:ns]}
+            ta = time.perf_counter()
             m.catalog(i, out=c)
+            split["catalog%d" % i] = time.perf_counter() - ta
             d2h += ns * (16 + 4 + 36)
             if cfg.nside_count[i]:
                 m.count_map(i, out=outs["cmap%d" % i])
                 d2h += outs["cmap%d" % i].nbytes
         for i in range(cfg.n_imap):
+            ta = time.perf_counter()
             m.imap(i, out=outs["imap%d" % i])
+            split["imap%d" % i] = time.perf_counter() - ta
             d2h += outs["imap%d" % i].nbytes
         if cfg.do_kappa:
+            ta = time.perf_counter()
             m.kappa(out=outs["kappa"])
+            split["kappa"] = time.perf_counter() - ta
             d2h += outs["kappa"].nbytes
         t_dl += time.perf_counter() - t1
     torch.cuda.synchronize()
@@ -263,7 +270,8 @@ def run_ours(args):
                    "n_grid": n, "l2": "inputs larger than L2 (4.3 GB per field)", "parallelism": "replicas"},
         "e2e": {"value": world * ncell / t_e2e, "unit": "cells/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": t_e2e * 1e3,
-                "download_ms_per_step": t_dl * 1e3, "d2h_GB/s": d2h / max(t_dl, 1e-9) / 1e9},
+                "download_ms_per_step": t_dl * 1e3, "d2h_GB/s": d2h / max(t_dl, 1e-9) / 1e9,
+                "download_split_ms": {k: round(v * 1e3, 2) for k, v in split.items()}},
         "gpu_launches": int(launches),
         "kernel_ms": {k: round(v, 3) for k, v in avg.items()},
         "kernels": kern,
@@ -272,6 +280,17 @@ def run_ours(args):
         "roofline": rl,
         "clocks": clk.summary(),
     }
+    if world == 1 and not args.no_fp64:
+        # the plain FP64 path of the same sequence on the same GPU (first run
+        # allocates; the second is timed with CUDA events)
+        m64 = cg.Mock64(prm, device=local)
+        m64.run()
+        t64 = m64.run()
+        m64.close()
+        v64 = ncell / (t64 / 1e3)
+        out["fp64_gpu"] = {"value": v64, "unit": "cells/s", "ms_per_step": t64,
+                           "speedup_of_value": out["value"] / v64,
+                           "path": "plain FP64 kernels + cuFFT, no fusion, same GPU"}
     if world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, quick=True)
     print(json.dumps(out))
@@ -386,6 +405,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c4")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 baseline path")
     ap.add_argument("--n", type=int, default=0, help="override the grid size")
     ap.add_argument("--cpu-n", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -101,6 +101,12 @@ def lib():
             "cg_set_profiling": (C.c_int, [vp, C.c_int]),
             "cg_kernel_times": (C.c_int, [vp, C.c_char_p, C.c_size_t, C.POINTER(C.c_float), C.c_int,
                                           C.POINTER(C.c_int)]),
+            "cg64_create": (C.c_int, [C.POINTER(vp), C.POINTER(Config), C.c_int]),
+            "cg64_destroy": (None, [vp]),
+            "cg64_last_error": (C.c_char_p, [vp]),
+            "cg64_run_mock": (C.c_int, [vp, C.POINTER(C.c_float)]),
+            "cg64_num_sources": (C.c_longlong, [vp, C.c_int]),
+            "cg64_download": (C.c_int, [vp, C.c_int, C.c_int, vp]),
             "cg_read_run_params": (C.c_int, [C.c_char_p, C.POINTER(vp), C.c_char_p, C.c_size_t]),
             "cg_params_free": (None, [vp]),
             "cg_params_to_config": (C.c_int, [vp, C.POINTER(Config)]),
@@ -122,7 +128,8 @@ def exported_symbols():
             "cg_imap_set_cartesian", "cg_imap_samples", "cg_get_beam_properties", "cg_run_mock", "cg_download_grid",
             "cg_num_sources", "cg_download_catalog", "cg_download_count_map", "cg_download_imap",
             "cg_download_kappa", "cg_download_norm", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_read_run_params",
-            "cg_params_free", "cg_params_to_config"]
+            "cg_params_free", "cg_params_to_config", "cg64_create", "cg64_destroy", "cg64_last_error",
+            "cg64_run_mock", "cg64_num_sources", "cg64_download"]
 
 
 class CGError(RuntimeError):
@@ -297,3 +304,67 @@ class Mock:
         e = np.empty(2, np.float32)
         self._chk(lib().cg_download_norm(self._c, kind, ipop, t.ctypes.data, e.ctypes.data), "download_norm")
         return t, e
+
+
+class Mock64:
+    """The plain FP64 path of the same sequence on the same GPU (cg64_* C ABI):
+    the baseline the FP32 path is measured against."""
+
+    def __init__(self, params, device=0):
+        self.params = params
+        self.cfg = params.config
+        self._c = C.c_void_p()
+        rc = lib().cg64_create(C.byref(self._c), C.byref(self.cfg), device)
+        if rc:
+            raise CGError("cg64_create failed (%s)" % ERRORS.get(rc, rc))
+
+    def close(self):
+        if getattr(self, "_c", None):
+            lib().cg64_destroy(self._c)
+            self._c = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc, what):
+        if rc:
+            msg = lib().cg64_last_error(self._c)
+            raise CGError("%s: %s (%s)" % (what, ERRORS.get(rc, rc), msg.decode() if msg else ""))
+
+    def run(self):
+        """Run the whole sequence; returns its device time in ms."""
+        ms = C.c_float()
+        self._chk(lib().cg64_run_mock(self._c, C.byref(ms)), "cg64_run_mock")
+        return ms.value
+
+    def num_sources(self, ipop):
+        return lib().cg64_num_sources(self._c, ipop)
+
+    def density(self, which=0):
+        n = self.cfg.n_grid
+        a = np.empty((n, n, n), np.float64)
+        self._chk(lib().cg64_download(self._c, which, 0, a.ctypes.data), "cg64_download")
+        return a
+
+    def imap(self, ipop):
+        """(summed temperatures, hit counts), nr x npix in RING order."""
+        ns, nr = self.cfg.nside_imap[ipop], self.cfg.imap_nr[ipop]
+        d = np.empty((nr, 12 * ns * ns), np.float64)
+        k = np.empty((nr, 12 * ns * ns), np.int32)
+        self._chk(lib().cg64_download(self._c, 2, ipop, d.ctypes.data), "cg64_download")
+        self._chk(lib().cg64_download(self._c, 3, ipop, k.ctypes.data), "cg64_download")
+        return d, k
+
+    def kappa(self):
+        ns = self.cfg.nside_kappa
+        m = np.empty((self.cfg.n_kappa, 12 * ns * ns), np.float64)
+        self._chk(lib().cg64_download(self._c, 4, 0, m.ctypes.data), "cg64_download")
+        return m
+
+    def norm_table(self, tracer):
+        t = np.empty(NA, np.float64)
+        self._chk(lib().cg64_download(self._c, 5, tracer, t.ctypes.data), "cg64_download")
+        return t

@@ -70,7 +70,7 @@ def _jobs():
         src = os.path.join(CSRC, "field_impl.cu")
         out = os.path.join(BUILD, "field_%d.o" % n)
         units.append((out, [nvcc()] + NVFLAGS + ["-DCG_N=%d" % n, "-c", src, "-o", out], [src] + hdr))
-    for name in ("dens", "srcs", "imap", "kappa", "capi"):
+    for name in ("dens", "srcs", "imap", "kappa", "capi", "fp64"):
         src = os.path.join(CSRC, name + ".cu")
         out = os.path.join(BUILD, name + ".o")
         units.append((out, [nvcc()] + NVFLAGS + ["-c", src, "-o", out], [src] + hdr))
@@ -92,7 +92,9 @@ def build(verbose=False, jobs=None):
             list(ex.map(lambda u: _run(u[1], verbose), todo))
     objs = [u[0] for u in units]
     if _stale(LIB, objs):
-        _run([nvcc(), "-shared", ARCH, "-o", LIB] + objs + ["-cudart=static", "-lm"], verbose)
+        cudalib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "lib64")
+        _run([nvcc(), "-shared", ARCH, "-o", LIB] + objs +
+             ["-cudart=static", "-L" + cudalib, "-lcufft", "-Xlinker", "-rpath=" + cudalib, "-lm"], verbose)
     drv = os.path.join(HOST, "colore_gpu.c")
     if os.path.exists(drv) and _stale(DRIVER, [drv, LIB] + _headers()):
         _run(["gcc"] + CFLAGS + ["-o", DRIVER, drv, "-L" + LIBDIR, "-lcolore_cuda",

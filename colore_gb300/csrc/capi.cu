@@ -99,10 +99,11 @@ struct cg_ctx {
   Imap im[CG_NPOP_MAX];
   float *d_tmpmap = nullptr;
   size_t tmpmap_n = 0;
-  cg_heavy_cell *d_heavy = nullptr;
-  long long *d_heavy_off = nullptr;
+  cg_imap_cell *d_cells = nullptr;
+  unsigned int *d_cell_n = nullptr;
+  long long *d_cell_off = nullptr, *d_scan_tmp = nullptr;
   unsigned long long *d_imap_ctr = nullptr;
-  long long heavy_cap = 0;
+  long long list_cap = 0;
   /* kappa */
   float *d_kmap = nullptr, *d_kfac = nullptr, *d_kinv = nullptr;
   int *d_kir = nullptr;
@@ -168,7 +169,7 @@ static int check_device_errors(cg_ctx *c)
   if (h) {
     CUDA_TRY(c, cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), c->stream));
     return fail(c, CG_EDEVICE, "device error flags 0x%x (1: source count overflow, 2: catalog overflow, "
-                               "4: shell search, 8: imap sub-sampling, 16: imap heavy-sample count)", h);
+                               "4: shell search, 8: imap sub-sampling, 16: imap cell list)", h);
   }
   return CG_OK;
 }
@@ -430,7 +431,7 @@ extern "C" void cg_destroy(cg_ctx *c)
                   c->d_disp[1], c->d_disp[2], c->d_part, c->d_stats, c->d_s2f, c->d_err, c->d_ncount,
                   c->d_zsum, c->d_bsum, c->d_counts, c->d_bsums, c->d_total, c->d_tmpmap, c->d_kmap,
                   c->d_kfac, c->d_kinv, c->d_kir, c->d_ovf_cell, c->d_ovf_cnt, c->d_ovf_n,
-                  c->d_heavy, c->d_heavy_off, c->d_imap_ctr};
+                  c->d_cells, c->d_cell_n, c->d_cell_off, c->d_scan_tmp, c->d_imap_ctr};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < CG_NPOP_MAX; i++) {
@@ -990,49 +991,42 @@ extern "C" int cg_imap_set_cartesian(cg_ctx *c)
     p.data = M.data;
     p.nadd = M.nadd;
     p.err = c->d_err;
-    /* Heavy cells: nsub >= CG_NSUB_HEAVY.  Their list is sized for every cell
-     * whose corner lies within the outer radius of the shells that can give
-     * such an nsub (a gap between shells counts as nsub_lo); cells past the
-     * list's capacity are painted by the first kernel. */
+    /* The cell list holds every cell within the shells' outer radius (or the
+     * whole box), up to a quarter of the free device memory; cells past its
+     * capacity are painted by the first kernel. */
     {
-      const bool gaps = [&] {
-        for (int i = 0; i + 1 < nr; i++)
-          if (sr0[i + 1] > srf[i]) return true;
-        return false;
-      }();
-      double rb = -1;
-      if (nsub[0] >= CG_NSUB_HEAVY) rb = gaps ? (double)p.rmax_here : (double)sr0[0];
-      for (int i = 0; i < nr; i++)
-        if (nsub[i] >= CG_NSUB_HEAVY && srf[i] > rb) rb = srf[i];
-      if (nsub[nr - 1] >= CG_NSUB_HEAVY) rb = p.rmax_here;
-      long long want = 0;
-      if (rb >= 0) {
-        const double rc = rb / dx + 2.0;
-        const double ball = 4.0 / 3.0 * M_PI * rc * rc * rc;
-        const double ncell = (double)c->N * c->N * c->N;
-        want = (long long)fmin(fmin(ball, ncell), (double)CG_HEAVY_MAX) + 1;
-      }
-      if (want > c->heavy_cap) {
-        if ((rc = dalloc(c, &c->d_heavy, (size_t)want)) || (rc = dalloc(c, &c->d_heavy_off, (size_t)want)))
+      const double rb = (double)p.rmax_here / dx + 2.0;
+      const double ball = 4.0 / 3.0 * M_PI * rb * rb * rb;
+      const double ncell = (double)c->N * c->N * c->N;
+      size_t fr = 0, tot = 0;
+      CUDA_TRY(c, cudaMemGetInfo(&fr, &tot));
+      const double budget = (double)(fr + (size_t)c->list_cap * CG_IMAP_CELL_BYTES) * 0.25 / CG_IMAP_CELL_BYTES;
+      const long long want = (long long)fmin(fmin(ball, ncell), budget) + 1;
+      if (want > c->list_cap) {
+        if ((rc = dalloc(c, &c->d_cells, (size_t)want)) || (rc = dalloc(c, &c->d_cell_n, (size_t)want)) ||
+            (rc = dalloc(c, &c->d_cell_off, (size_t)want)) ||
+            (rc = dalloc(c, &c->d_scan_tmp, (size_t)cg_imap_scan_blocks(want))))
           return rc;
-        c->heavy_cap = want;
+        c->list_cap = want;
       }
       if (!c->d_imap_ctr && (rc = dalloc(c, &c->d_imap_ctr, (size_t)5))) return rc;
-      p.nsub_heavy = CG_NSUB_HEAVY;
-      p.heavy_cap = want;
+      p.list_cap = c->list_cap;
+
       p.ctr = c->d_imap_ctr;
-      p.heavy_off = c->d_heavy_off;
-      p.heavy = c->d_heavy;
+      p.cells = c->d_cells;
+      p.cell_n = c->d_cell_n;
+      p.cell_off = c->d_cell_off;
+      p.scan_tmp = c->d_scan_tmp;
     }
     {
       ProfScope ps(c, "imap_paint");
       CUDA_TRY(c, cg_imap_paint(c->stream, c->d_dens, c->d_npot, &p, c->nsm));
     }
-    c->launches += p.heavy_cap > 0 ? 2 : 1;
-    unsigned long long ns2[2] = {0, 0};
-    CUDA_TRY(c, cudaMemcpyAsync(ns2, c->d_imap_ctr + 3, sizeof(ns2), cudaMemcpyDeviceToHost, c->stream));
+    unsigned long long ctr[5] = {0, 0, 0, 0, 0};
+    CUDA_TRY(c, cudaMemcpyAsync(ctr, c->d_imap_ctr, sizeof(ctr), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host vectors above go out of scope */
-    M.samples = ns2[0] + ns2[1];
+    M.samples = ctr[3] + ctr[4];
+    c->launches += ctr[0] > 0 ? 5 : 1; /* cells, 3 scan passes, paint */
   }
   return CG_OK;
 }

@@ -20,7 +20,7 @@ enum : unsigned int {
   ERR_CATALOG_OVERFLOW = 2u, /* emit wrote past the allocated catalog  */
   ERR_SHELL_WALK = 4u,       /* imap shell search did not terminate    */
   ERR_IMAP_NSUB = 8u,        /* sub-sampling factor out of range       */
-  ERR_IMAP_HEAVY = 16u,      /* more than 2^40 samples in heavy cells  */
+  ERR_IMAP_HEAVY = 16u,      /* nsub > 128 in a cell past the list     */
 };
 
 /* One background table with the edge values of get_bg (cosmo.c:40-86). */

@@ -8,36 +8,34 @@
  * r + dr_rsd) and a RING pixel, where temp is added and a hit counted.
  *
  * The work per cell is nsub^3 and nsub grows as 1/r towards the observer
- * (the sub-cell follows the pixel size r * sqrt(4 pi / npix)), so a few
- * cells near the observer hold most of the samples.  Two kernels:
+ * (the sub-cell follows the pixel size r * sqrt(4 pi / npix)): from 8 samples
+ * per cell at high redshift to thousands near the observer.  So the cells
+ * are first listed and their samples then painted as one even stream:
  *
- *   k_imap        Warps take groups of whole rows from a counter; a warp
- *                 handles 32 consecutive cells of a row at a time (one per
- *                 lane) and computes their per-cell quantities.  Cells with
- *                 at least nsub_heavy sub-samples per side are appended to the
- *                 heavy list, with their first sample offset from one 64-bit
- *                 atomic that counts records and samples together, so the
- *                 offsets are an exclusive prefix in list order.  The lanes
- *                 then take the sub-samples of the remaining cells, 32
- *                 consecutive ones at a time.
- *   k_imap_heavy  The heavy samples are cut into 8 chunks per warp, taken
+ *   k_imap_cells  Warps take groups of whole rows from a counter; a lane
+ *                 computes one cell's brightness, radial shift, shell and
+ *                 nsub and appends the cell to the list (one atomic per warp).
+ *                 Cells past the list's capacity are painted here, 32
+ *                 consecutive samples of the warp's cells at a time.
+ *   k_scan_*      exclusive scan of the listed cells' sample counts: the
+ *                 first sample of every listed cell.
+ *   k_imap_paint  The listed samples are cut into 8 chunks per warp, taken
  *                 from a counter; a warp finds the first cell of its chunk by
  *                 binary search on the offsets and paints 32 consecutive
- *                 samples at a time.
+ *                 samples at a time, each lane walking forward to its cell.
  *
  * Consecutive samples (x fastest) of a cell often land on the same (shell,
  * pixel); each run of equal keys across the lanes is found with one shuffle
- * and a ballot and added once.  The runs go to a per-warp shared-memory hash
- * table keyed by (shell, pixel) that sums
- * the brightness (temp * run) and the hits: each pixel receives tens of
- * sub-samples of a cell, and neighbouring cells share pixels, so the table
- * turns one global atomic pair per sub-sample into one per distinct key.
- * The table is flushed (data += sum, nadd += hits) when half full and at the
- * end of each row group or chunk; runs that find it nearly full go straight
- * to global memory.  Keys are 32-bit when nr * npix < 2^32 - 1.
+ * and a ballot and added to the maps once, with one float and one integer
+ * atomic (data += temp * run, nadd += run).  GB300's L2 sustains these
+ * without staging: a shared-memory hash table that merged the runs of a
+ * warp before the global atomics was measured slower at every nsub.  Keys
+ * (shell * npix + pixel) are 32-bit when nr * npix < 2^32 - 1.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <algorithm>
 
 #include "cg_dev.cuh"
 #include "imap_api.h"
@@ -46,11 +44,10 @@ namespace {
 using namespace cg;
 
 constexpr int IW = 4;          /* warps per block                        */
-constexpr int HT = 512;        /* hash slots per warp                    */
-constexpr int HFLUSH = 256;    /* flush after a step with this many used */
-constexpr int HCAP = 448;      /* no new keys beyond this many           */
 constexpr int ROWS = 4;        /* rows per fetch in k_imap               */
-constexpr int CHUNKS = 8;      /* sample chunks per warp in k_imap_heavy */
+constexpr int CHUNKS = 8;      /* sample chunks per warp in k_imap_paint */
+constexpr int SCAN_T = 256;    /* threads per block of the offset scan    */
+constexpr int SCAN_I = 16;     /* records per thread of the offset scan   */
 
 struct CellPar {
   float x0, temp, drr, dxs, inv_ns;
@@ -58,92 +55,9 @@ struct CellPar {
 };
 
 template <typename K>
-struct Table {
-  K key[HT];
-  float sum[HT];
-  unsigned int cnt[HT];
-  unsigned short list[HT];
-  int nused;
-};
-
-template <typename K>
 __device__ __forceinline__ K empty_key()
 {
   return (K)~(K)0;
-}
-
-template <typename K>
-__device__ __forceinline__ unsigned int hslot(K k)
-{
-  unsigned long long h = (unsigned long long)k * 0x9E3779B97F4A7C15ull;
-  return (unsigned int)(h >> 55) & (HT - 1);
-}
-
-template <typename K>
-__device__ __forceinline__ void init_table(Table<K> &w, int lane)
-{
-  for (int i = lane; i < HT; i += 32) {
-    w.key[i] = empty_key<K>();
-    w.sum[i] = 0.0f;
-    w.cnt[i] = 0u;
-  }
-  if (lane == 0) w.nused = 0;
-}
-
-template <typename K>
-__device__ __forceinline__ void flush(Table<K> &w, int lane, const cg_imap_params &p)
-{
-  __syncwarp();
-  const int n = *(volatile int *)&w.nused;
-  for (int i = lane; i < n; i += 32) {
-    const int h = w.list[i];
-    const long long idx = (long long)w.key[h];
-    atomicAdd(&p.data[idx], w.sum[h]);
-    atomicAdd(&p.nadd[idx], (int)w.cnt[h]);
-    w.key[h] = empty_key<K>();
-    w.sum[h] = 0.0f;
-    w.cnt[h] = 0u;
-  }
-  __syncwarp();
-  if (lane == 0) w.nused = 0;
-  __syncwarp();
-}
-
-/* Add c hits of brightness temp to key; new keys go to global memory once
- * the table is nearly full. */
-template <typename K>
-__device__ __forceinline__ void insert(Table<K> &w, K key, unsigned int c, float temp, const cg_imap_params &p)
-{
-  const float v = CG_MUL(temp, (float)c);
-  unsigned int h = hslot(key);
-  volatile K *vk = w.key;
-  for (int probe = 0; probe < HT; probe++) {
-    const K k = vk[h];
-    if (k == key) {
-      atomicAdd(&w.sum[h], v);
-      atomicAdd(&w.cnt[h], c);
-      return;
-    }
-    if (k == empty_key<K>()) {
-      if (*(volatile int *)&w.nused >= HCAP) break;
-      const K old = atomicCAS(&w.key[h], empty_key<K>(), key);
-      if (old == empty_key<K>()) {
-        atomicAdd(&w.sum[h], v);
-        atomicAdd(&w.cnt[h], c);
-        const int pos = atomicAdd(&w.nused, 1);
-        w.list[pos] = (unsigned short)h;
-        return;
-      }
-      if (old == key) {
-        atomicAdd(&w.sum[h], v);
-        atomicAdd(&w.cnt[h], c);
-        return;
-      }
-    }
-    h = (h + 1) & (HT - 1);
-  }
-  atomicAdd(&p.data[(long long)key], v);
-  atomicAdd(&p.nadd[(long long)key], (int)c);
 }
 
 /* Key of sample q (0 <= q < ns^3, x fastest, then y, then z) of cell c, whose
@@ -175,10 +89,10 @@ __device__ __forceinline__ K sample_key(const cg_imap_params &p, const float *r0
 }
 
 /* The lanes hold consecutive samples: each run of equal (tag, key) is added
- * once, by its first lane, with its length.  tag separates cells. */
+ * to the maps once, by its first lane, with its length (data += temp * run,
+ * nadd += run).  tag separates cells, whose brightness differs. */
 template <typename K>
-__device__ __forceinline__ void insert_runs(Table<K> &w, K key, int tag, float temp, int lane,
-                                            const cg_imap_params &p)
+__device__ __forceinline__ void add_runs(K key, int tag, float temp, int lane, const cg_imap_params &p)
 {
   const unsigned FULL = 0xffffffffu;
   const K pk = __shfl_up_sync(FULL, key, 1);
@@ -189,32 +103,28 @@ __device__ __forceinline__ void insert_runs(Table<K> &w, K key, int tag, float t
   if (head) {
     const unsigned above = lane == 31 ? 0u : bnd & (FULL << (lane + 1));
     const int end = above ? __ffs(above) - 1 : 32;
-    insert(w, key, (unsigned int)(end - lane), temp, p);
+    const unsigned int c = (unsigned int)(end - lane);
+    atomicAdd(&p.data[(long long)key], CG_MUL(temp, (float)c));
+    atomicAdd(&p.nadd[(long long)key], (int)c);
   }
 }
 
-constexpr unsigned long long HREC = 1ull << 40;     /* one heavy record    */
-constexpr unsigned long long HSMASK = HREC - 1;     /* heavy sample field  */
-
 template <typename K>
-__global__ void __launch_bounds__(IW * 32, 1) k_imap(const float *__restrict__ dens, const float *__restrict__ phi,
+__global__ void __launch_bounds__(IW * 32, 1) k_imap_cells(const float *__restrict__ dens, const float *__restrict__ phi,
                                                      cg_imap_params p)
 {
   extern __shared__ unsigned char sraw[];
-  Table<K> *ws = reinterpret_cast<Table<K> *>(sraw);
-  CellPar *cells = reinterpret_cast<CellPar *>(sraw + IW * sizeof(Table<K>));
+  CellPar *cells = reinterpret_cast<CellPar *>(sraw);
   float *r0 = reinterpret_cast<float *>(cells + IW * 32);
   float *rf = r0 + p.nr;
   int *nsa = reinterpret_cast<int *>(rf + p.nr);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  Table<K> &w = ws[wid];
   CellPar *wc = cells + wid * 32;
   for (int i = threadIdx.x; i < p.nr; i += blockDim.x) {
     r0[i] = p.r0[i];
     rf[i] = p.rf[i];
     nsa[i] = p.nsub[i];
   }
-  init_table(w, lane);
   __syncthreads();
   const int N = p.box.N;
   const int nch = (N + 31) / 32;
@@ -271,40 +181,25 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap(const float *__restrict__ d
           }
         }
       }
-      /* heavy cells go to the list (one atomic per warp); past its capacity
-       * they are painted here */
-      const bool hv = n > 0 && p.nsub_heavy > 0 && cp.nsub >= p.nsub_heavy;
-      if (__ballot_sync(FULL, hv)) {
-        const unsigned long long v = hv ? HREC | (unsigned long long)n : 0ull;
-        unsigned long long inc = v;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          unsigned long long t = __shfl_up_sync(FULL, inc, o);
-          if (lane >= o) inc += t;
-        }
-        const unsigned long long wt = __shfl_sync(FULL, inc, 31);
+      /* every cell goes to the list (one atomic per warp); past its
+       * capacity it is painted here */
+      const unsigned lm = __ballot_sync(FULL, n > 0);
+      if (lm) {
         unsigned long long base = 0;
-        int ok = 0;
         if (lane == 0) {
-          /* stop appending once the list is full or half the sample field is
-           * used, so that neither field can wrap (the overshoot of warps in
-           * flight is at most 32 records and 2^35 samples each) */
+          /* stop once the list is full: the counter then overshoots its
+           * capacity by at most 32 per warp in flight */
           const unsigned long long cur = *(volatile unsigned long long *)&p.ctr[0];
-          if ((long long)(cur >> 40) < p.heavy_cap && (cur & HSMASK) < (HSMASK >> 1)) {
-            base = atomicAdd(&p.ctr[0], wt);
-            ok = 1;
-            if ((base & HSMASK) + (wt & HSMASK) > HSMASK) atomicOr(p.err, ERR_IMAP_HEAVY);
-          }
+          base = cur < (unsigned long long)p.list_cap ? atomicAdd(&p.ctr[0], (unsigned long long)__popc(lm))
+                                                      : (unsigned long long)p.list_cap;
         }
-        ok = __shfl_sync(FULL, ok, 0);
         base = __shfl_sync(FULL, base, 0);
-        const unsigned long long mine = base + inc - v;
-        const long long slot = (long long)(mine >> 40);
-        if (ok && hv && slot < p.heavy_cap) {
-          float4 *q = reinterpret_cast<float4 *>(p.heavy + slot);
+        const long long slot = (long long)base + __popc(lm & ((1u << lane) - 1u));
+        if (n > 0 && slot < p.list_cap) {
+          float4 *q = reinterpret_cast<float4 *>(p.cells + slot);
           q[0] = make_float4(cp.x0, y0, z0, cp.temp);
-          q[1] = make_float4(cp.drr, cp.dxs, __int_as_float(cp.nsub), __int_as_float(cp.irad0));
-          p.heavy_off[slot] = (long long)(mine & HSMASK);
+          q[1] = make_float4(cp.drr, cp.dxs, cp.inv_ns, __int_as_float(cp.nsub | ((cp.irad0 + 1) << 11)));
+          p.cell_n[slot] = (unsigned int)n;
           n = 0;
         }
       }
@@ -343,40 +238,108 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap(const float *__restrict__ d
           key = sample_key<K>(p, r0, rf, c, y0, z0, s - ex);
           temp = c.temp;
         }
-        insert_runs(w, key, j, temp, lane, p);
-        __syncwarp();
-        if (*(volatile int *)&w.nused >= HFLUSH) flush(w, lane, p);
+        add_runs(key, j, temp, lane, p);
       }
       __syncwarp();
     }
-    flush(w, lane, p);
+  }
+}
+
+/* Sum of the sample counts of each block of SCAN_T * SCAN_I records. */
+__global__ void __launch_bounds__(SCAN_T) k_scan_sum(const unsigned int *__restrict__ n, long long H, long long *bsum)
+{
+  const long long i0 = ((long long)blockIdx.x * SCAN_T + threadIdx.x) * SCAN_I;
+  long long t = 0;
+#pragma unroll
+  for (int i = 0; i < SCAN_I; i++)
+    if (i0 + i < H) t += n[i0 + i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  __shared__ long long ws[SCAN_T / 32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long b = 0;
+    for (int w = 0; w < SCAN_T / 32; w++) b += ws[w];
+    bsum[blockIdx.x] = b;
+  }
+}
+
+/* Exclusive scan of the nb block sums in place (one block); total -> *total. */
+__global__ void __launch_bounds__(1024) k_scan_top(long long *v, long long nb, unsigned long long *total)
+{
+  __shared__ long long sm[1024];
+  const long long per = (nb + 1023) / 1024;
+  const long long b = (long long)threadIdx.x * per, e = b + per < nb ? b + per : nb;
+  long long acc = 0;
+  for (long long i = b; i < e; i++) acc += v[i];
+  sm[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    const long long t = (int)threadIdx.x >= o ? sm[threadIdx.x - o] : 0;
+    __syncthreads();
+    sm[threadIdx.x] += t;
+    __syncthreads();
+  }
+  long long run = sm[threadIdx.x] - acc;
+  for (long long i = b; i < e; i++) {
+    const long long x = v[i];
+    v[i] = run;
+    run += x;
+  }
+  if (threadIdx.x == 1023) *total = (unsigned long long)sm[1023];
+}
+
+/* First sample of every record: block offset + in-block exclusive scan. */
+__global__ void __launch_bounds__(SCAN_T) k_scan_out(const unsigned int *__restrict__ n, long long H,
+                                                      const long long *__restrict__ bexcl, long long *off)
+{
+  const long long i0 = ((long long)blockIdx.x * SCAN_T + threadIdx.x) * SCAN_I;
+  unsigned int v[SCAN_I];
+  long long t = 0;
+#pragma unroll
+  for (int i = 0; i < SCAN_I; i++) {
+    v[i] = i0 + i < H ? n[i0 + i] : 0u;
+    t += v[i];
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  long long inc = t;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long u = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += u;
+  }
+  __shared__ long long ws[SCAN_T / 32];
+  if (lane == 31) ws[wid] = inc;
+  __syncthreads();
+  long long run = bexcl[blockIdx.x];
+  for (int w = 0; w < wid; w++) run += ws[w];
+  run += inc - t;
+#pragma unroll
+  for (int i = 0; i < SCAN_I; i++) {
+    if (i0 + i < H) off[i0 + i] = run;
+    run += v[i];
   }
 }
 
 template <typename K>
-__global__ void __launch_bounds__(IW * 32, 1) k_imap_heavy(cg_imap_params p)
+__global__ void __launch_bounds__(IW * 32, 1) k_imap_paint(cg_imap_params p)
 {
   extern __shared__ unsigned char sraw[];
-  Table<K> *ws = reinterpret_cast<Table<K> *>(sraw);
-  float *r0 = reinterpret_cast<float *>(sraw + IW * sizeof(Table<K>));
+  float *r0 = reinterpret_cast<float *>(sraw);
   float *rf = r0 + p.nr;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  Table<K> &w = ws[wid];
+  const int lane = threadIdx.x & 31;
   for (int i = threadIdx.x; i < p.nr; i += blockDim.x) {
     r0[i] = p.r0[i];
     rf[i] = p.rf[i];
   }
-  init_table(w, lane);
   __syncthreads();
-  const unsigned long long ctr = *(volatile unsigned long long *)&p.ctr[0];
-  long long H = (long long)(ctr >> 40);
-  if (H > p.heavy_cap) H = p.heavy_cap;
-  if (H <= 0) return;
-  const cg_heavy_cell *hl = p.heavy;
-  const long long *off = p.heavy_off;
-  const long long nlast = hl[H - 1].nsub;
-  const unsigned long long S = (unsigned long long)(off[H - 1] + nlast * nlast * nlast);
-  if (blockIdx.x == 0 && threadIdx.x == 0) p.ctr[4] = S;
+  long long H = (long long)*(volatile unsigned long long *)&p.ctr[0];
+  if (H > p.list_cap) H = p.list_cap;
+  const unsigned long long S = *(volatile unsigned long long *)&p.ctr[4];
+  if (H <= 0 || S == 0) return;
+  const cg_imap_cell *cl = p.cells;
+  const long long *off = p.cell_off;
   const unsigned long long NC = (unsigned long long)gridDim.x * IW * CHUNKS;
   const unsigned FULL = 0xffffffffu;
   for (;;) {
@@ -390,45 +353,47 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap_heavy(cg_imap_params p)
     long long lo = 0, hi = H - 1;
     while (lo < hi) {
       const long long mid = (lo + hi + 1) >> 1;
-      if (off[mid] <= s0) lo = mid;
+      if (__ldg(&off[mid]) <= s0) lo = mid;
       else hi = mid - 1;
     }
-    for (long long h = lo; h < H && off[h] < s1; h++) {
-      const float4 qa = __ldg(reinterpret_cast<const float4 *>(hl + h));
-      const float4 qb = __ldg(reinterpret_cast<const float4 *>(hl + h) + 1);
-      CellPar c;
-      c.x0 = qa.x;
-      c.temp = qa.w;
-      c.drr = qb.x;
-      c.dxs = qb.y;
-      c.nsub = __float_as_int(qb.z);
-      c.irad0 = __float_as_int(qb.w);
-      c.inv_ns = 1.0f / (float)c.nsub;
-      c.pad = 0;
-      const long long ns = c.nsub, base = off[h];
-      const long long qbeg = s0 > base ? s0 - base : 0;
-      long long qend = s1 - base;
-      if (qend > ns * ns * ns) qend = ns * ns * ns;
-      for (long long q0 = qbeg; q0 < qend; q0 += 32) {
-        const long long q = q0 + lane;
-        const K key = q < qend ? sample_key<K>(p, r0, rf, c, qa.y, qa.z, (int)q) : empty_key<K>();
-        insert_runs(w, key, 0, c.temp, lane, p);
-        __syncwarp();
-        if (*(volatile int *)&w.nused >= HFLUSH) flush(w, lane, p);
+    long long hw = lo; /* the warp's current record */
+    for (long long sb = s0; sb < s1; sb += 32) {
+      const long long s = sb + lane;
+      long long h = hw;
+      K key = empty_key<K>();
+      float temp = 0.0f;
+      if (s < s1) {
+        while (h + 1 < H && __ldg(&off[h + 1]) <= s) h++;
+        const float4 qa = __ldg(reinterpret_cast<const float4 *>(cl + h));
+        const float4 qb = __ldg(reinterpret_cast<const float4 *>(cl + h) + 1);
+        const int pk = __float_as_int(qb.w);
+        CellPar c;
+        c.x0 = qa.x;
+        c.temp = qa.w;
+        c.drr = qb.x;
+        c.dxs = qb.y;
+        c.inv_ns = qb.z;
+        c.nsub = pk & 2047;
+        c.irad0 = (pk >> 11) - 1;
+        c.pad = 0;
+        key = sample_key<K>(p, r0, rf, c, qa.y, qa.z, (int)(s - __ldg(&off[h])));
+        temp = c.temp;
       }
+      add_runs(key, (int)h, temp, lane, p);
+      hw = __shfl_sync(FULL, h, 31);
     }
-    flush(w, lane, p);
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0) p.ctr[4] = S; /* listed samples, for the caller */
 }
 
 template <typename K>
 cudaError_t launch(cudaStream_t s, const float *dens, const float *phi, const cg_imap_params *p, int nsm)
 {
-  size_t smem = IW * sizeof(Table<K>) + IW * 32 * sizeof(CellPar) + (size_t)p->nr * (2 * sizeof(float) + sizeof(int));
-  cudaError_t e = cudaFuncSetAttribute(k_imap<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  size_t smem = IW * 32 * sizeof(CellPar) + (size_t)p->nr * (2 * sizeof(float) + sizeof(int));
+  cudaError_t e = cudaFuncSetAttribute(k_imap_cells<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_imap<K>, IW * 32, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_imap_cells<K>, IW * 32, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   e = cudaMemsetAsync(p->ctr, 0, 5 * sizeof(unsigned long long), s);
@@ -436,20 +401,36 @@ cudaError_t launch(cudaStream_t s, const float *dens, const float *phi, const cg
   long long nrow = (long long)p->box.N * p->box.N;
   long long blocks = (nrow + IW * ROWS - 1) / (IW * ROWS);
   if (blocks > (long long)nsm * per_sm) blocks = (long long)nsm * per_sm;
-  k_imap<K><<<(unsigned)blocks, IW * 32, smem, s>>>(dens, phi, *p);
+  k_imap_cells<K><<<(unsigned)blocks, IW * 32, smem, s>>>(dens, phi, *p);
   e = cudaGetLastError();
-  if (e != cudaSuccess || p->heavy_cap <= 0) return e;
-  size_t hsmem = IW * sizeof(Table<K>) + (size_t)p->nr * 2 * sizeof(float);
-  e = cudaFuncSetAttribute(k_imap_heavy<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hsmem);
+  if (e != cudaSuccess || p->list_cap <= 0) return e;
+  /* records listed (the count may overshoot the capacity) */
+  unsigned long long h = 0;
+  e = cudaMemcpyAsync(&h, p->ctr, sizeof(h), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_imap_heavy<K>, IW * 32, hsmem);
+  const long long H = (long long)std::min<unsigned long long>(h, (unsigned long long)p->list_cap);
+  if (H == 0) return cudaSuccess;
+  const long long nb = (H + SCAN_T * SCAN_I - 1) / (SCAN_T * SCAN_I);
+  k_scan_sum<<<(unsigned)nb, SCAN_T, 0, s>>>(p->cell_n, H, p->scan_tmp);
+  k_scan_top<<<1, 1024, 0, s>>>(p->scan_tmp, nb, p->ctr + 4);
+  k_scan_out<<<(unsigned)nb, SCAN_T, 0, s>>>(p->cell_n, H, p->scan_tmp, p->cell_off);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  /* every warp of the painting pass resident at once */
+  const size_t psmem = (size_t)p->nr * 2 * sizeof(float);
+  e = cudaFuncSetAttribute(k_imap_paint<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem);
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_imap_paint<K>, IW * 32, psmem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
-  k_imap_heavy<K><<<(unsigned)(nsm * per_sm), IW * 32, hsmem, s>>>(*p);
+  k_imap_paint<K><<<(unsigned)(nsm * per_sm), IW * 32, psmem, s>>>(*p);
   return cudaGetLastError();
 }
 
 } /* namespace */
+
+long long cg_imap_scan_blocks(long long cap) { return (cap + SCAN_T * SCAN_I - 1) / (SCAN_T * SCAN_I); }
 
 cudaError_t cg_imap_paint(cudaStream_t s, const float *dens, const float *phi, const cg_imap_params *p, int nsm)
 {

@@ -24,28 +24,30 @@ struct cg_imap_params {
   float *data;        /* nr * npix, RING */
   int *nadd;          /* nr * npix       */
   unsigned int *err;
-  /* Cells with at least nsub_heavy sub-samples per side are listed by the
-   * first kernel and painted by the second with their samples split evenly
-   * over all warps.  ctr[0] packs (heavy records << 40) | heavy samples,
-   * ctr[1] counts heavy chunks taken, ctr[2] rows taken, ctr[3] and ctr[4]
-   * the samples painted by each kernel (all zeroed per launch). */
-  int nsub_heavy;
-  long long heavy_cap;
+  /* The first kernel lists every cell it computes (while the list has room)
+   * and the second paints the listed cells' samples, split evenly over all
+   * warps.  ctr[0] counts records, ctr[1] sample chunks taken, ctr[2] rows
+   * taken, ctr[3] and ctr[4] the samples painted by each kernel (all zeroed
+   * per launch). */
+  long long list_cap;
   unsigned long long *ctr;
-  long long *heavy_off;            /* first sample of each record          */
-  struct cg_heavy_cell *heavy;     /* heavy_cap records                    */
+  struct cg_imap_cell *cells;     /* list_cap records                       */
+  unsigned int *cell_n;           /* samples of each record (nsub^3)        */
+  long long *cell_off;            /* first sample of each record (scanned)  */
+  long long *scan_tmp;            /* cg_imap_scan_blocks(list_cap) entries  */
 };
 
-struct __align__(16) cg_heavy_cell {
-  float x0, y0, z0, temp, drr, dxs;
-  int nsub, irad0;
+/* One listed cell: corner, brightness, radial shift, sub-cell size, 1/nsub,
+ * and nsub | (shell index + 1) << 11. */
+struct __align__(16) cg_imap_cell {
+  float x0, y0, z0, temp, drr, dxs, inv_ns;
+  int packed;
 };
 
-/* Sub-samples per side from which a cell is painted by the heavy pass, and
- * the largest heavy list (records of 40 bytes). */
-#define CG_NSUB_HEAVY 8
-#define CG_HEAVY_MAX (1LL << 23)
+/* Bytes per listed cell (record, sample count, offset). */
+#define CG_IMAP_CELL_BYTES (sizeof(struct cg_imap_cell) + sizeof(unsigned int) + sizeof(long long))
 
+long long cg_imap_scan_blocks(long long cap);
 cudaError_t cg_imap_paint(cudaStream_t s, const float *dens, const float *phi, const cg_imap_params *p, int nsm);
 
 #endif

@@ -196,6 +196,24 @@ int cg_kernel_times(cg_ctx *ctx, char *names, size_t names_len, float *ms, int c
 /* Launch accounting: number of kernels this context has launched. */
 long long cg_kernel_launches(const cg_ctx *ctx);
 
+/* FP64 baseline (no counterpart in the reference) -------------------------
+ * The same driver sequence (src/main.c:66-125) with plain double-precision
+ * kernels, one thread per mode / cell / source / pixel, cuFFT transforms and
+ * no fusion: the denominator of the FP32 path's speed-up on the same GPU.
+ * Sources are written in an unspecified order. */
+typedef struct cg64_ctx cg64_ctx;
+int cg64_create(cg64_ctx **out, const cg_config *cfg, int device);
+void cg64_destroy(cg64_ctx *ctx);
+const char *cg64_last_error(const cg64_ctx *ctx);
+/* Whole sequence; *ms (may be NULL) gets its device time from CUDA events. */
+int cg64_run_mock(cg64_ctx *ctx, float *ms);
+long long cg64_num_sources(const cg64_ctx *ctx, int ipop);
+/* what: 0 density, 1 potential (N^3 doubles, [z][y][x]); 2 intensity-map
+ * temperature sums and 3 hit counts (int) of species ipop (nr * npix, RING);
+ * 4 convergence (n_kappa * npix doubles, RING); 5 normalisation table of
+ * tracer ipop (CG_NA doubles; source populations first, then species). */
+int cg64_download(cg64_ctx *ctx, int what, int ipop, void *dst);
+
 #ifdef __cplusplus
 }
 #endif

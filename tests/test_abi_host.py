@@ -15,7 +15,7 @@ def declared_symbols():
     for h in ("colore_cuda.h", "colore_host.h"):
         txt = open(os.path.join(ROOT, "include", h)).read()
         txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-        names.update(re.findall(r"\b(cg_[a-z0-9_]+)\s*\(", txt))
+        names.update(re.findall(r"\b(cg(?:64)?_[a-z0-9_]+)\s*\(", txt))
     return sorted(names)
 
 
