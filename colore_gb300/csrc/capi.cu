@@ -49,8 +49,7 @@ struct Imap {
   int nr = 0, nside = 0;
   long long npix = 0;
   float *r0 = nullptr, *rf = nullptr;
-  int *nsub = nullptr;
-  int nsub_lo = 0, nsub_hi = 0;
+  float4 *shp = nullptr; /* per shell index + 1: nsub, dx/nsub, 1/nsub */
   float rmin = 0, rmax = 0;
   float *data = nullptr;
   int *nadd = nullptr;
@@ -436,7 +435,7 @@ extern "C" void cg_destroy(cg_ctx *c)
     if (p) cudaFree(p);
   for (int i = 0; i < CG_NPOP_MAX; i++) {
     void *q[] = {c->cat[i].pos, c->cat[i].ipix, c->cat[i].src, c->cat[i].cmap, c->im[i].r0, c->im[i].rf,
-                 c->im[i].nsub, c->im[i].data, c->im[i].nadd};
+                 c->im[i].shp, c->im[i].data, c->im[i].nadd};
     for (void *p : q)
       if (p) cudaFree(p);
   }
@@ -953,7 +952,7 @@ extern "C" int cg_imap_set_cartesian(cg_ctx *c)
     }
     if (M.nr != nr) {
       if ((rc = dalloc(c, &M.r0, (size_t)nr)) || (rc = dalloc(c, &M.rf, (size_t)nr)) ||
-          (rc = dalloc(c, &M.nsub, (size_t)nr)))
+          (rc = dalloc(c, &M.shp, (size_t)nr + 2)))
         return rc;
     }
     if (M.nr != nr || M.npix != npix) {
@@ -964,7 +963,17 @@ extern "C" int cg_imap_set_cartesian(cg_ctx *c)
     M.npix = npix;
     CUDA_TRY(c, cudaMemcpyAsync(M.r0, sr0.data(), nr * sizeof(float), cudaMemcpyHostToDevice, c->stream));
     CUDA_TRY(c, cudaMemcpyAsync(M.rf, srf.data(), nr * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-    CUDA_TRY(c, cudaMemcpyAsync(M.nsub, nsub.data(), nr * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    /* get_r_index_imap gives -1 below the shells (nsub_lo) and nr beyond
+     * them (nsub_hi); a gap between shells also gives -1 (imap.c:196-208) */
+    std::vector<float4> shp(nr + 2);
+    for (int i = -1; i <= nr; i++) {
+      const int ns = i < 0 ? nsub[0] : (i >= nr ? nsub[nr - 1] : nsub[i]);
+      if (ns < 1 || ns > 1024) return fail(c, CG_EINVAL, "intensity species %d: nsub %d outside 1..1024", ip, ns);
+      float nsbits;
+      memcpy(&nsbits, &ns, sizeof(nsbits));
+      shp[i + 1] = make_float4(nsbits, c->box.dx / (float)ns, 1.0f / (float)ns, 0.0f);
+    }
+    CUDA_TRY(c, cudaMemcpyAsync(M.shp, shp.data(), (nr + 2) * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
     CUDA_TRY(c, cudaMemsetAsync(M.data, 0, (size_t)nr * npix * sizeof(float), c->stream));
     CUDA_TRY(c, cudaMemsetAsync(M.nadd, 0, (size_t)nr * npix * sizeof(int), c->stream));
     cg_imap_params p;
@@ -981,9 +990,7 @@ extern "C" int cg_imap_set_cartesian(cg_ctx *c)
     p.nr = nr;
     p.r0 = M.r0;
     p.rf = M.rf;
-    p.nsub = M.nsub;
-    p.nsub_lo = nsub[0];
-    p.nsub_hi = nsub[nr - 1];
+    p.shp = M.shp;
     p.rmin_here = (float)((double)sr0[0] - 20.);
     p.rmax_here = (float)((double)srf[nr - 1] + 20.);
     p.nside = nside;

@@ -387,10 +387,11 @@ CG_HD int cg_shell_index(const float *r0, const float *rf, int nr, float r, int 
 }
 
 /* Radial velocity from a centred potential difference (get_rvel,
- * srcs.c:87-118): 0.5*idx*(dphi . u) with u = x/r. */
+ * srcs.c:87-118): 0.5*idx*(dphi . u) with u = x * (1/r). */
 CG_HD float cg_rvel(float vx, float vy, float vz, float x0, float y0, float z0, float rr, float idx)
 {
-  float ux = CG_DIV(x0, rr), uy = CG_DIV(y0, rr), uz = CG_DIV(z0, rr);
+  const float ir = CG_DIV(1.0f, rr);
+  float ux = CG_MUL(x0, ir), uy = CG_MUL(y0, ir), uz = CG_MUL(z0, ir);
   float dot = CG_ADD(CG_ADD(CG_MUL(vx, ux), CG_MUL(vy, uy)), CG_MUL(vz, uz));
   return CG_MUL(CG_MUL(0.5f, idx), dot);
 }
@@ -434,7 +435,10 @@ CG_HD void cg_radec(float cth, float ph, float *ra, float *dec)
 }
 
 /* sub-cell centre c0 + (i + 1/2) dxs, imap.c:212-218 */
-CG_HD float cg_sub_centre(float c0, int i, float dxs) { return CG_ADD(c0, CG_MUL(CG_ADD((float)i, 0.5f), dxs)); }
+CG_HD float cg_sub_centre(float c0, int i, float dxs) { return CG_FMA(CG_ADD((float)i, 0.5f), dxs, c0); }
+
+/* y^2 + z^2 of an x-line of sub-samples */
+CG_HD float cg_yz2(float y, float z) { return CG_FMA(y, y, CG_MUL(z, z)); }
 
 /* imap brightness and radial shift, imap.c:199-201 */
 CG_HD float cg_imap_temp(float tmean, float d, float bias, float dnorm, int model)
@@ -446,12 +450,17 @@ CG_HD float cg_imap_drsd(float rvel, float v1, float ih) { return CG_MUL(CG_MUL(
 /* One intensity-map sub-sample of imap.c:210-231 at (x, y, z), with
  * yz2 = y^2 + z^2 shared by the samples of an x-line: returns the shell
  * index (or -1 / nr outside the shells) and the RING pixel.  The radius is
- * sqrt(x^2 + yz2); cos(theta) = z/r and phi = atan2(y, x) as in cart2sph. */
+ * sqrt(x^2 + yz2) (one fused multiply-add); cos(theta) = z/r and
+ * phi = atan2(y, x) as in cart2sph. */
 CG_HD int cg_imap_sample(float x, float y, float z, float yz2, float drr, const float *r0, const float *rf, int nr,
                          int start, int64_t nside, int64_t *pix)
 {
-  const float r = CG_SQRT(CG_ADD(CG_MUL(x, x), yz2));
-  const int ir = cg_shell_index(r0, rf, nr, CG_ADD(r, drr), start);
+  const float r = CG_SQRT(CG_FMA(x, x, yz2));
+  const float rs = CG_ADD(r, drr);
+  /* most samples stay in the shell of their cell: the walk from there */
+  const int ir = (start >= 0 && start < nr && rs >= r0[start] && rs < rf[start])
+                     ? start
+                     : cg_shell_index(r0, rf, nr, rs, start);
   if (ir < 0 || ir >= nr) return ir;
   float cth = 1.0f, ph = 0.0f;
   if (r != 0.0f) {

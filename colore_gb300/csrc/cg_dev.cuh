@@ -40,6 +40,28 @@ __device__ __forceinline__ float bg(const Tab &t, const Grid1 &g, float r)
   return cg_bg_eval(t.f, g.r, t.f0, t.ff, r, g.r_last, g.idr);
 }
 
+/* One r shared by several table lookups: bg(t, g, r) == bgv(t, bg_at(g, r)). */
+struct BgAt {
+  int ir, where; /* where: 0 inside, -1 at or below r = 0, 1 at or beyond r_last */
+  float t;       /* (r - r_ir) * idr */
+};
+
+__device__ __forceinline__ BgAt bg_at(const Grid1 &g, float r)
+{
+  BgAt a;
+  a.where = r <= 0.0f ? -1 : (r >= g.r_last ? 1 : 0);
+  a.ir = a.where ? 0 : (int)CG_MUL(r, g.idr);
+  a.t = a.where ? 0.0f : CG_MUL(CG_SUB(r, g.r[a.ir]), g.idr);
+  return a;
+}
+
+__device__ __forceinline__ float bgv(const Tab &t, const BgAt &a)
+{
+  if (a.where) return a.where < 0 ? t.f0 : t.ff;
+  const float fi = t.f[a.ir];
+  return CG_FMA(CG_SUB(t.f[a.ir + 1], fi), a.t, fi);
+}
+
 /* r_of_z, cosmo.c:101-112, on the a-uniform table of NA entries. */
 __device__ __forceinline__ float r_of_z(const float *a_arr, const float *r_arr, int na, float z)
 {

@@ -17,7 +17,8 @@
  *                    block combines its warps' bins in FP64 in a fixed order
  *                    and sends them to global memory with one atomic each.
  *  k_lpt_cic       : 1LPT particle positions (density.c:473-501) and their
- *                    cloud-in-cell deposit (density.c:64-105).
+ *                    cloud-in-cell deposit (density.c:64-105), staged per
+ *                    tile of particles in shared memory.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -180,27 +181,42 @@ __global__ void __launch_bounds__(BINS_WARPS * 32, 2) k_dens_bins(float *grid, c
   }
 }
 
-/* 1LPT: x = q + D(r) Psi (wrapped into the box), then CIC into grid. */
+/* 1LPT: x = q + D(r) Psi (wrapped into the box), then CIC into grid.  A block
+ * takes a tile of CT_X x CT_Y x CT_Z particles (lattice cells) and deposits
+ * into a shared-memory box that extends the tile by CT_H cells on every
+ * side; the box is added to the grid at the end with one atomic per
+ * non-zero cell.  Deposits that fall outside the box (particles displaced by
+ * more than CT_H - 1 cells) go straight to the grid. */
+constexpr int CT_X = 32, CT_Y = 8, CT_Z = 8, CT_H = 2;
+constexpr int CB_X = CT_X + 2 * CT_H, CB_Y = CT_Y + 2 * CT_H, CB_Z = CT_Z + 2 * CT_H;
+
 __global__ void __launch_bounds__(256) k_lpt_cic(float *grid, const float *__restrict__ dx_,
                                                  const float *__restrict__ dy_, const float *__restrict__ dz_,
                                                  cg_lpt_params p)
 {
+  __shared__ float box[CB_Z][CB_Y][CB_X];
   const int N = p.box.N;
-  const long long ncell = (long long)N * N * N;
+  const int ntx = (N + CT_X - 1) / CT_X, nty = (N + CT_Y - 1) / CT_Y;
+  const int t = blockIdx.x;
+  const int tx0 = (t % ntx) * CT_X, ty0 = ((t / ntx) % nty) * CT_Y, tz0 = (t / (ntx * nty)) * CT_Z;
+  for (int i = threadIdx.x; i < CB_X * CB_Y * CB_Z; i += blockDim.x) (&box[0][0][0])[i] = 0.0f;
+  __syncthreads();
   const float iag = CG_DIV((float)N, p.box.L);
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncell;
-       c += (long long)gridDim.x * blockDim.x) {
-    const long long q = divN(c, p.box), qz = divN(q, p.box);
-    const int ix = (int)(c - q * N), iy = (int)(q - qz * N), iz = (int)qz;
+  const float po[3] = {p.box.p0, p.box.p1, p.box.p2};
+  const int org[3] = {tx0 - CT_H, ty0 - CT_H, tz0 - CT_H};
+  const int ext[3] = {CB_X, CB_Y, CB_Z};
+  for (int k = threadIdx.x; k < CT_X * CT_Y * CT_Z; k += blockDim.x) {
+    const int ix = tx0 + (k % CT_X), iy = ty0 + (k / CT_X) % CT_Y, iz = tz0 + k / (CT_X * CT_Y);
+    if (ix >= N || iy >= N || iz >= N) continue;
     const long long id = pidx(ix, iy, iz, N);
     float xv[3] = {cg_cell_coord(ix, p.box.dx, p.box.p0), cg_cell_coord(iy, p.box.dx, p.box.p1),
                    cg_cell_coord(iz, p.box.dx, p.box.p2)};
-    const float po[3] = {p.box.p0, p.box.p1, p.box.p2};
-    float r = cg_norm3(xv[0], xv[1], xv[2]);
-    float dg = bg(p.d1, p.g, r);
-    float dsp[3] = {__ldg(&dx_[id]), __ldg(&dy_[id]), __ldg(&dz_[id])};
-    int i0[3], i1[3];
+    const float r = cg_norm3(xv[0], xv[1], xv[2]);
+    const float dg = bg(p.d1, p.g, r);
+    const float dsp[3] = {__ldg(&dx_[id]), __ldg(&dy_[id]), __ldg(&dz_[id])};
+    int i0[3], i1[3], b0[3];
     float a0[3], a1[3];
+    bool inbox = true;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
       float q = CG_ADD(CG_FMA(dg, dsp[a], xv[a]), po[a]);
@@ -216,15 +232,38 @@ __global__ void __launch_bounds__(256) k_lpt_cic(float *grid, const float *__res
       i1[a] %= N;
       if (i0[a] < 0) i0[a] += N;
       if (i1[a] < 0) i1[a] += N;
+      /* position of i0 in the box, the shorter way round the period */
+      int d = i0[a] - org[a];
+      if (d < -N / 2) d += N;
+      if (d >= N / 2) d -= N;
+      b0[a] = d;
+      inbox = inbox && d >= 0 && d + 1 < ext[a];
     }
-    atomicAdd(&grid[pidx(i0[0], i0[1], i0[2], N)], CG_MUL(CG_MUL(a0[0], a0[1]), a0[2]));
-    atomicAdd(&grid[pidx(i1[0], i0[1], i0[2], N)], CG_MUL(CG_MUL(a1[0], a0[1]), a0[2]));
-    atomicAdd(&grid[pidx(i0[0], i1[1], i0[2], N)], CG_MUL(CG_MUL(a0[0], a1[1]), a0[2]));
-    atomicAdd(&grid[pidx(i1[0], i1[1], i0[2], N)], CG_MUL(CG_MUL(a1[0], a1[1]), a0[2]));
-    atomicAdd(&grid[pidx(i0[0], i0[1], i1[2], N)], CG_MUL(CG_MUL(a0[0], a0[1]), a1[2]));
-    atomicAdd(&grid[pidx(i1[0], i0[1], i1[2], N)], CG_MUL(CG_MUL(a1[0], a0[1]), a1[2]));
-    atomicAdd(&grid[pidx(i0[0], i1[1], i1[2], N)], CG_MUL(CG_MUL(a0[0], a1[1]), a1[2]));
-    atomicAdd(&grid[pidx(i1[0], i1[1], i1[2], N)], CG_MUL(CG_MUL(a1[0], a1[1]), a1[2]));
+    const float w[8] = {CG_MUL(CG_MUL(a0[0], a0[1]), a0[2]), CG_MUL(CG_MUL(a1[0], a0[1]), a0[2]),
+                        CG_MUL(CG_MUL(a0[0], a1[1]), a0[2]), CG_MUL(CG_MUL(a1[0], a1[1]), a0[2]),
+                        CG_MUL(CG_MUL(a0[0], a0[1]), a1[2]), CG_MUL(CG_MUL(a1[0], a0[1]), a1[2]),
+                        CG_MUL(CG_MUL(a0[0], a1[1]), a1[2]), CG_MUL(CG_MUL(a1[0], a1[1]), a1[2])};
+    if (inbox) {
+#pragma unroll
+      for (int c = 0; c < 8; c++)
+        atomicAdd(&box[b0[2] + (c >> 2)][b0[1] + ((c >> 1) & 1)][b0[0] + (c & 1)], w[c]);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 8; c++)
+        atomicAdd(&grid[pidx((c & 1) ? i1[0] : i0[0], ((c >> 1) & 1) ? i1[1] : i0[1], (c >> 2) ? i1[2] : i0[2], N)],
+                  w[c]);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < CB_X * CB_Y * CB_Z; i += blockDim.x) {
+    const float v = (&box[0][0][0])[i];
+    if (v == 0.0f) continue;
+    const int bx = i % CB_X, by = (i / CB_X) % CB_Y, bz = i / (CB_X * CB_Y);
+    int gx = (org[0] + bx) % N, gy = (org[1] + by) % N, gz = (org[2] + bz) % N;
+    if (gx < 0) gx += N;
+    if (gy < 0) gy += N;
+    if (gz < 0) gz += N;
+    atomicAdd(&grid[pidx(gx, gy, gz, N)], v);
   }
 }
 
@@ -273,10 +312,9 @@ cudaError_t cg_dens_bins_static_scratch(void **ptr, size_t *bytes)
 cudaError_t cg_lpt_cic(cudaStream_t s, float *grid, const float *dx, const float *dy, const float *dz,
                        const cg_lpt_params *p, int nsm)
 {
-  long long ncell = (long long)p->box.N * p->box.N * p->box.N;
-  long long blocks = (ncell + 255) / 256;
-  long long cap = (long long)nsm * 16;
-  if (blocks > cap) blocks = cap;
-  k_lpt_cic<<<(unsigned)blocks, 256, 0, s>>>(grid, dx, dy, dz, *p);
+  (void)nsm;
+  const long long N = p->box.N;
+  const long long tiles = ((N + CT_X - 1) / CT_X) * ((N + CT_Y - 1) / CT_Y) * ((N + CT_Z - 1) / CT_Z);
+  k_lpt_cic<<<(unsigned)tiles, 256, 0, s>>>(grid, dx, dy, dz, *p);
   return cudaGetLastError();
 }

@@ -80,7 +80,7 @@ __device__ __forceinline__ K sample_key(const cg_imap_params &p, const float *r0
   const int ixx = q - line * ns, iyy = line - izz * ns;
   const float zc = cg_sub_centre(z0, izz, c.dxs);
   const float yc = cg_sub_centre(y0, iyy, c.dxs);
-  const float yz2 = CG_ADD(CG_MUL(yc, yc), CG_MUL(zc, zc));
+  const float yz2 = cg_yz2(yc, zc);
   const float xc = cg_sub_centre(c.x0, ixx, c.dxs);
   int64_t pix = 0;
   const int ir = cg_imap_sample(xc, yc, zc, yz2, c.drr, r0, rf, p.nr, c.irad0, p.nside, &pix);
@@ -115,16 +115,16 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap_cells(const float *__restri
 {
   extern __shared__ unsigned char sraw[];
   CellPar *cells = reinterpret_cast<CellPar *>(sraw);
-  float *r0 = reinterpret_cast<float *>(cells + IW * 32);
+  float4 *shp = reinterpret_cast<float4 *>(cells + IW * 32);
+  float *r0 = reinterpret_cast<float *>(shp + p.nr + 2);
   float *rf = r0 + p.nr;
-  int *nsa = reinterpret_cast<int *>(rf + p.nr);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   CellPar *wc = cells + wid * 32;
   for (int i = threadIdx.x; i < p.nr; i += blockDim.x) {
     r0[i] = p.r0[i];
     rf[i] = p.rf[i];
-    nsa[i] = p.nsub[i];
   }
+  for (int i = threadIdx.x; i < p.nr + 2; i += blockDim.x) shp[i] = p.shp[i];
   __syncthreads();
   const int N = p.box.N;
   const int nch = (N + 31) / 32;
@@ -153,10 +153,11 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap_cells(const float *__restri
       if (ix < N) {
         cp.x0 = cg_cell_coord(ix, dx, p.box.p0);
         const float rc = cg_norm3(cp.x0, y0, z0);
-        const float tmean = bg(p.tz, p.g, rc);
+        const BgAt at = bg_at(p.g, rc);
+        const float tmean = bgv(p.tz, at);
         if (rc <= p.rmax_here && rc >= p.rmin_here && tmean > 0.0f) {
-          const float bias = bg(p.bz, p.g, rc);
-          const float dnorm = bg(p.norm, p.g, rc);
+          const float bias = bgv(p.bz, at);
+          const float dnorm = bgv(p.norm, at);
           const int xh = wrap(ix + 1, N), xl = wrap(ix - 1, N);
           const int yh = wrap(iy + 1, N), yl = wrap(iy - 1, N);
           const int zh = wrap(iz + 1, N), zl = wrap(iz - 1, N);
@@ -164,19 +165,20 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap_cells(const float *__restri
           float v1 = CG_SUB(__ldg(&phi[pidx(ix, yh, iz, N)]), __ldg(&phi[pidx(ix, yl, iz, N)]));
           float v2 = CG_SUB(__ldg(&phi[pidx(ix, iy, zh, N)]), __ldg(&phi[pidx(ix, iy, zl, N)]));
           float rvel = CG_MUL(p.factor_vel, cg_rvel(v0, v1, v2, cp.x0, y0, z0, rc, p.box.idx));
-          cp.drr = cg_imap_drsd(rvel, bg(p.v1, p.g, rc), bg(p.ih, p.g, rc));
+          cp.drr = cg_imap_drsd(rvel, bgv(p.v1, at), bgv(p.ih, at));
           const float d = __ldg(&dens[pidx(ix, iy, iz, N)]);
           cp.temp = cg_imap_temp(tmean, d, bias, dnorm, p.bias_model);
           cp.irad0 = cg_shell_index(r0, rf, p.nr, rc, 0);
-          int ns = cp.irad0 < 0 ? p.nsub_lo : (cp.irad0 >= p.nr ? p.nsub_hi : nsa[cp.irad0]);
+          /* nsub of the cell's shell (the first one below the shells, the
+           * last one beyond or in a gap), with dx / nsub and 1 / nsub */
+          const float4 sp = shp[cp.irad0 + 1];
+          const int ns = __float_as_int(sp.x);
           if (ns < 1 || ns > 1024) {
             atomicOr(p.err, ERR_IMAP_NSUB);
-            ns = 0;
-          }
-          cp.nsub = ns;
-          if (ns > 0) {
-            cp.dxs = CG_DIV(dx, (float)ns);
-            cp.inv_ns = 1.0f / (float)ns;
+          } else {
+            cp.nsub = ns;
+            cp.dxs = sp.y;
+            cp.inv_ns = sp.z;
             n = ns * ns * ns;
           }
         }
@@ -208,6 +210,7 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap_cells(const float *__restri
         atomicOr(p.err, ERR_IMAP_HEAVY);
         n = 0;
       }
+      if (!__any_sync(FULL, n > 0)) continue;
       wc[lane] = cp;
       painted += (unsigned long long)n;
       /* inclusive scan of the sample counts (nsub^3 per cell) over the warp */
@@ -389,7 +392,7 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap_paint(cg_imap_params p)
 template <typename K>
 cudaError_t launch(cudaStream_t s, const float *dens, const float *phi, const cg_imap_params *p, int nsm)
 {
-  size_t smem = IW * 32 * sizeof(CellPar) + (size_t)p->nr * (2 * sizeof(float) + sizeof(int));
+  size_t smem = IW * 32 * sizeof(CellPar) + (size_t)(p->nr + 2) * sizeof(float4) + (size_t)p->nr * 2 * sizeof(float);
   cudaError_t e = cudaFuncSetAttribute(k_imap_cells<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;

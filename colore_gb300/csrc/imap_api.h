@@ -17,8 +17,9 @@ struct cg_imap_params {
   float factor_vel;
   int nr;             /* shells, sorted by r0 (imap_preproc, imap.c:105-133) */
   const float *r0, *rf;
-  const int *nsub;    /* per shell (imap.c:158-172) */
-  int nsub_lo, nsub_hi;
+  /* per shell index + 1 (index -1 below the shells, nr beyond them):
+   * nsub (imap.c:158-174, as int bits), dx / nsub, 1 / nsub */
+  const float4 *shp;
   float rmin_here, rmax_here;
   int64_t nside, npix;
   float *data;        /* nr * npix, RING */

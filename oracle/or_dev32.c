@@ -390,7 +390,7 @@ int or_imap32(const cg_config *cfg, int ipop, const float *dens, const float *np
           float zc = cg_sub_centre(z0, izz, dxs);
           for (int iyy = 0; iyy < ns; iyy++) {
             float yc = cg_sub_centre(y0, iyy, dxs);
-            float yz2 = CG_ADD(CG_MUL(yc, yc), CG_MUL(zc, zc));
+            float yz2 = cg_yz2(yc, zc);
             for (int ixx = 0; ixx < ns; ixx++) {
               float xc = cg_sub_centre(x0, ixx, dxs);
               int64_t pix = 0;
