@@ -107,6 +107,9 @@ def lib():
             "cg64_run_mock": (C.c_int, [vp, C.POINTER(C.c_float)]),
             "cg64_num_sources": (C.c_longlong, [vp, C.c_int]),
             "cg64_download": (C.c_int, [vp, C.c_int, C.c_int, vp]),
+            "cg_write_healpix_map": (C.c_int, [C.c_char_p, vp, C.c_long]),
+            "cg_write_catalog": (C.c_int, [C.c_char_p, C.c_int, C.c_int, vp, C.c_longlong]),
+            "cg_write_density_grid": (C.c_int, [C.c_char_p, C.c_char_p, vp, C.c_int, C.c_double]),
             "cg_read_run_params": (C.c_int, [C.c_char_p, C.POINTER(vp), C.c_char_p, C.c_size_t]),
             "cg_params_free": (None, [vp]),
             "cg_params_to_config": (C.c_int, [vp, C.POINTER(Config)]),
@@ -128,12 +131,39 @@ def exported_symbols():
             "cg_imap_set_cartesian", "cg_imap_samples", "cg_get_beam_properties", "cg_run_mock", "cg_download_grid",
             "cg_num_sources", "cg_download_catalog", "cg_download_count_map", "cg_download_imap",
             "cg_download_kappa", "cg_download_norm", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_read_run_params",
-            "cg_params_free", "cg_params_to_config", "cg64_create", "cg64_destroy", "cg64_last_error",
+            "cg_params_free", "cg_params_to_config", "cg_write_healpix_map", "cg_write_catalog",
+            "cg_write_density_grid", "cg64_create", "cg64_destroy", "cg64_last_error",
             "cg64_run_mock", "cg64_num_sources", "cg64_download"]
 
 
 class CGError(RuntimeError):
     pass
+
+
+OUT_ASCII, OUT_FITS = 0, 1
+
+
+def write_healpix_map(fname, m, nside):
+    """One RING map as a FITS binary table (he_write_healpix_map)."""
+    m = np.ascontiguousarray(m, np.float32)
+    if m.size != 12 * nside * nside:
+        raise ValueError("map has %d pixels, nside %d needs %d" % (m.size, nside, 12 * nside * nside))
+    if lib().cg_write_healpix_map(os.fsencode(fname), m.ctypes.data, nside):
+        raise CGError("cannot write %s" % fname)
+
+
+def write_catalog(prefix, ipop, src, fmt=OUT_FITS):
+    """<prefix>_srcs_s<ipop+1>_0.fits or .txt from Src records (n x 9 floats)."""
+    src = np.ascontiguousarray(src, np.float32).reshape(-1, 9)
+    if lib().cg_write_catalog(os.fsencode(prefix), ipop, fmt, src.ctypes.data, len(src)):
+        raise CGError("cannot write the catalogue of population %d under %s" % (ipop, prefix))
+
+
+def write_density_grid(prefix, tag, grid, l_box):
+    """<prefix>_dens_<tag>_0.dat from a padded [N][N][2(N/2+1)] float grid."""
+    g = np.ascontiguousarray(grid, np.float32)
+    if lib().cg_write_density_grid(os.fsencode(prefix), os.fsencode(tag), g.ctypes.data, g.shape[0], l_box):
+        raise CGError("cannot write the density grid under %s" % prefix)
 
 
 class Params:

@@ -6,10 +6,10 @@
  *   ./colore_gpu params.cfg            run and write outputs
  *   ./colore_gpu --test-memory params  print the memory plan and exit
  *
- * Outputs follow io.c: raw density grids (write_density_grid, io.c:565-595),
- * source catalogues in ASCII (io.c:1210-1236) and HEALPix maps in FITS
- * binary tables (he_write_healpix_map, healpix_extra.c:4-57), written by a
- * minimal FITS writer of this file since cfitsio is not required.
+ * Outputs follow io.c through the writers of host_io.c: raw density grids
+ * (write_density_grid, io.c:565-595), source catalogues in FITS or ASCII
+ * (write_catalog, io.c:1069-1236) and HEALPix maps in FITS binary tables
+ * (he_write_healpix_map, healpix_extra.c:4-57).
  */
 #include <stdint.h>
 #include <stdio.h>
@@ -43,98 +43,21 @@ static void die(cg_ctx *c, int rc, const char *what)
   exit(1);
 }
 
-/* ---- minimal FITS writer: primary HDU + one BINTABLE column of 1E ---- */
-static void fits_card(FILE *f, const char *key, const char *val, const char *cmt)
-{
-  char card[81];
-  if (val) snprintf(card, sizeof(card), "%-8.8s= %20s / %-47.47s", key, val, cmt ? cmt : "");
-  else snprintf(card, sizeof(card), "%-80.80s", key);
-  fprintf(f, "%-80.80s", card);
-}
-
-static void fits_end(FILE *f, long *nbytes)
-{
-  fits_card(f, "END", NULL, NULL);
-  *nbytes += 80;
-  while (*nbytes % 2880) {
-    fputc(' ', f);
-    (*nbytes)++;
-  }
-}
-
-static int write_healpix_fits(const char *fname, const float *map, long nside)
-{
-  FILE *f = fopen(fname, "wb");
-  if (!f) return -1;
-  long nb = 0;
-  char v[32];
-  fits_card(f, "SIMPLE", "T", "conforms to FITS standard");
-  fits_card(f, "BITPIX", "8", "");
-  fits_card(f, "NAXIS", "0", "");
-  fits_card(f, "EXTEND", "T", "");
-  nb = 4 * 80;
-  fits_end(f, &nb);
-  long npix = 12 * nside * nside;
-  nb = 0;
-  fits_card(f, "XTENSION", "'BINTABLE'", "binary table extension");
-  fits_card(f, "BITPIX", "8", "");
-  fits_card(f, "NAXIS", "2", "");
-  fits_card(f, "NAXIS1", "4", "bytes per row");
-  snprintf(v, sizeof(v), "%ld", npix);
-  fits_card(f, "NAXIS2", v, "rows");
-  fits_card(f, "PCOUNT", "0", "");
-  fits_card(f, "GCOUNT", "1", "");
-  fits_card(f, "TFIELDS", "1", "");
-  fits_card(f, "TTYPE1", "'map 1   '", "");
-  fits_card(f, "TFORM1", "'1E      '", "");
-  fits_card(f, "TUNIT1", "'uK      '", "");
-  fits_card(f, "EXTNAME", "'BINTABLE'", "");
-  fits_card(f, "PIXTYPE", "'HEALPIX '", "HEALPIX Pixelisation");
-  fits_card(f, "ORDERING", "'RING    '", "Pixel ordering scheme, either RING or NESTED");
-  snprintf(v, sizeof(v), "%ld", nside);
-  fits_card(f, "NSIDE", v, "Resolution parameter for HEALPIX");
-  fits_card(f, "COORDSYS", "'G       '", "Pixelisation coordinate system");
-  nb = 16 * 80;
-  fits_end(f, &nb);
-  for (long i = 0; i < npix; i++) { /* big-endian IEEE float */
-    uint32_t u;
-    memcpy(&u, &map[i], 4);
-    unsigned char b[4] = {(unsigned char)(u >> 24), (unsigned char)(u >> 16), (unsigned char)(u >> 8),
-                          (unsigned char)u};
-    fwrite(b, 1, 4, f);
-  }
-  long data = npix * 4;
-  while (data % 2880) {
-    fputc(0, f);
-    data++;
-  }
-  fclose(f);
-  return 0;
-}
-
 static void write_density_grid(cg_ctx *c, const cg_params *p, const char *tag)
 {
   const int N = p->n_grid, ngx = 2 * (N / 2 + 1);
-  size_t nf = (size_t)N * N * ngx;
-  float *g = malloc(nf * sizeof(float));
+  float *g = malloc((size_t)N * N * ngx * sizeof(float));
+  if (!g) die(c, CG_ENOMEM, "density grid buffer");
   int rc = cg_download_grid(c, 0, g);
   if (rc) die(c, rc, "download_grid");
-  char fname[512];
-  snprintf(fname, sizeof(fname), "%s_dens_%s_0.dat", p->prefix_out, tag);
-  FILE *f = fopen(fname, "wb");
-  if (!f) die(c, CG_EINVAL, fname);
-  int one = 1, sz = (int)sizeof(float), zero = 0;
-  double lb = p->l_box;
-  fwrite(&one, sizeof(int), 1, f);
-  fwrite(&sz, sizeof(int), 1, f);
-  fwrite(&lb, sizeof(double), 1, f);
-  fwrite(&N, sizeof(int), 1, f);
-  fwrite(&N, sizeof(int), 1, f);
-  fwrite(&zero, sizeof(int), 1, f);
-  for (int iz = 0; iz < N; iz++)
-    for (int iy = 0; iy < N; iy++) fwrite(g + (size_t)ngx * (iy + (size_t)iz * N), sizeof(float), N, f);
-  fclose(f);
+  if ((rc = cg_write_density_grid(p->prefix_out, tag, g, N, p->l_box))) die(c, rc, "write_density_grid");
   free(g);
+}
+
+static void write_map(cg_ctx *c, const char *fname, const float *m, long nside)
+{
+  int rc = cg_write_healpix_map(fname, m, nside);
+  if (rc) die(c, rc, fname);
 }
 
 int main(int argc, char **argv)
@@ -217,21 +140,19 @@ int main(int argc, char **argv)
     if ((rc = cg_download_kappa(c, m))) die(c, rc, "download_kappa");
     for (int i = 0; i < p->n_kappa; i++) {
       snprintf(out, sizeof(out), "%s_kappa_z%03d.fits", p->prefix_out, i);
-      write_healpix_fits(out, m + (size_t)i * npix, p->nside_kappa);
+      write_map(c, out, m + (size_t)i * npix, p->nside_kappa);
     }
     free(m);
   }
+  /* write_catalog (io.c:1069-1236): FITS or ASCII; HDF5 is not built */
+  const int fmt = !strcmp(p->output_format, "FITS") ? CG_OUT_FITS : CG_OUT_ASCII;
+  if (p->n_srcs > 0 && !strcmp(p->output_format, "HDF5")) printf("HDF5 not supported\n");
   for (int ip = 0; ip < p->n_srcs; ip++) {
-    printf("*** Writing source catalogs\n %d-th population (ASCII)\n", ip);
+    printf("*** Writing source catalogs\n %d-th population (%s)\n", ip, fmt == CG_OUT_FITS ? "FITS" : "ASCII");
     float *src = malloc((size_t)(ns[ip] > 0 ? ns[ip] : 1) * 9 * sizeof(float));
+    if (!src) die(c, CG_ENOMEM, "catalogue buffer");
     if ((rc = cg_download_catalog(c, ip, NULL, NULL, src))) die(c, rc, "download_catalog");
-    snprintf(out, sizeof(out), "%s_srcs_s%d_0.txt", p->prefix_out, ip + 1);
-    FILE *f = fopen(out, "w");
-    if (!f) die(c, CG_EINVAL, out);
-    fprintf(f, "#[1]type [2]RA, [3]dec, [4]z0, [5]dz_RSD \n");
-    for (long long j = 0; j < ns[ip]; j++)
-      fprintf(f, "%d %E %E %E %E \n", ip, src[9 * j], src[9 * j + 1], src[9 * j + 2], src[9 * j + 3]);
-    fclose(f);
+    if ((rc = cg_write_catalog(p->prefix_out, ip, fmt, src, ns[ip]))) die(c, rc, "write_catalog");
     free(src);
     if (p->nside_count[ip] > 0) {
       long npix = 12L * p->nside_count[ip] * p->nside_count[ip];
@@ -240,7 +161,7 @@ int main(int argc, char **argv)
       if ((rc = cg_download_count_map(c, ip, cm))) die(c, rc, "download_count_map");
       for (long i = 0; i < npix; i++) fm[i] = (float)cm[i];
       snprintf(out, sizeof(out), "%s_srcs_s%d_counts.fits", p->prefix_out, ip + 1);
-      write_healpix_fits(out, fm, p->nside_count[ip]);
+      write_map(c, out, fm, p->nside_count[ip]);
       free(cm);
       free(fm);
     }
@@ -252,7 +173,7 @@ int main(int argc, char **argv)
     if ((rc = cg_download_imap(c, ip, m, NULL))) die(c, rc, "download_imap");
     for (int ir = 0; ir < p->imap_nr[ip]; ir++) {
       snprintf(out, sizeof(out), "%s_imap_s%d_nu%03d.fits", p->prefix_out, ip + 1, ir);
-      write_healpix_fits(out, m + (size_t)ir * npix, p->nside_imap[ip]);
+      write_map(c, out, m + (size_t)ir * npix, p->nside_imap[ip]);
     }
     free(m);
   }

@@ -143,6 +143,28 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap_cells(const float *__restri
       break;
     }
     const int rend = rbeg + ROWS < nrow ? rbeg + ROWS : nrow;
+    /* whether a cell is listed depends on its radius alone: count the row
+     * group's listed cells first and reserve their slots with one atomic */
+    int nlist = 0;
+    for (int row = rbeg; row < rend; row++) {
+      const int iz = row / N, iy = row - iz * N;
+      const float y0 = cg_cell_coord(iy, dx, p.box.p1), z0 = cg_cell_coord(iz, dx, p.box.p2);
+      for (int ix = lane; ix < N; ix += 32) {
+        const float rc = cg_norm3(cg_cell_coord(ix, dx, p.box.p0), y0, z0);
+        nlist += (rc <= p.rmax_here && rc >= p.rmin_here && bgv(p.tz, bg_at(p.g, rc)) > 0.0f) ? 1 : 0;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nlist += __shfl_xor_sync(FULL, nlist, o);
+    unsigned long long next = 0; /* the warp's next slot */
+    if (lane == 0 && nlist > 0) {
+      /* once the list is full the counter overshoots its capacity by at most
+       * one row group per warp in flight */
+      const unsigned long long cur = *(volatile unsigned long long *)&p.ctr[0];
+      next = cur < (unsigned long long)p.list_cap ? atomicAdd(&p.ctr[0], (unsigned long long)nlist)
+                                                  : (unsigned long long)p.list_cap;
+    }
+    next = __shfl_sync(FULL, next, 0);
     for (int row = rbeg; row < rend; row++)
     for (int ch = 0; ch < nch; ch++) {
       const int iz = row / N, iy = row - iz * N;
@@ -150,12 +172,14 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap_cells(const float *__restri
       const float y0 = cg_cell_coord(iy, dx, p.box.p1), z0 = cg_cell_coord(iz, dx, p.box.p2);
       CellPar cp = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0, 0, 0};
       int n = 0;
+      bool lst = false; /* the condition counted in the first pass */
       if (ix < N) {
         cp.x0 = cg_cell_coord(ix, dx, p.box.p0);
         const float rc = cg_norm3(cp.x0, y0, z0);
         const BgAt at = bg_at(p.g, rc);
         const float tmean = bgv(p.tz, at);
-        if (rc <= p.rmax_here && rc >= p.rmin_here && tmean > 0.0f) {
+        lst = rc <= p.rmax_here && rc >= p.rmin_here && tmean > 0.0f;
+        if (lst) {
           const float bias = bgv(p.bz, at);
           const float dnorm = bgv(p.norm, at);
           const int xh = wrap(ix + 1, N), xl = wrap(ix - 1, N);
@@ -183,21 +207,13 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap_cells(const float *__restri
           }
         }
       }
-      /* every cell goes to the list (one atomic per warp); past its
+      /* every cell goes to the list, in the slots reserved above; past its
        * capacity it is painted here */
-      const unsigned lm = __ballot_sync(FULL, n > 0);
+      const unsigned lm = __ballot_sync(FULL, lst);
       if (lm) {
-        unsigned long long base = 0;
-        if (lane == 0) {
-          /* stop once the list is full: the counter then overshoots its
-           * capacity by at most 32 per warp in flight */
-          const unsigned long long cur = *(volatile unsigned long long *)&p.ctr[0];
-          base = cur < (unsigned long long)p.list_cap ? atomicAdd(&p.ctr[0], (unsigned long long)__popc(lm))
-                                                      : (unsigned long long)p.list_cap;
-        }
-        base = __shfl_sync(FULL, base, 0);
-        const long long slot = (long long)base + __popc(lm & ((1u << lane) - 1u));
-        if (n > 0 && slot < p.list_cap) {
+        const long long slot = (long long)next + __popc(lm & ((1u << lane) - 1u));
+        next += (unsigned long long)__popc(lm);
+        if (lst && slot < p.list_cap) {
           float4 *q = reinterpret_cast<float4 *>(p.cells + slot);
           q[0] = make_float4(cp.x0, y0, z0, cp.temp);
           q[1] = make_float4(cp.drr, cp.dxs, cp.inv_ns, __int_as_float(cp.nsub | ((cp.irad0 + 1) << 11)));

@@ -93,8 +93,9 @@ def write_inputs(dirname, spec, prefix="run"):
     np.savetxt(pkf, np.transpose([k, pk]), fmt="%.10e")
     lines = []
     add = lines.append
-    add("global:\n{\n  prefix_out= \"%s\";\n  output_format= \"ASCII\";\n  output_density= false;" %
-        os.path.join(dirname, prefix))
+    add("global:\n{\n  prefix_out= \"%s\";\n  output_format= \"%s\";\n  output_density= %s;" %
+        (os.path.join(dirname, prefix), spec.get("output_format", "ASCII"),
+         "true" if spec.get("output_density") else "false"))
     add("  pk_filename= \"%s\";\n  z_min= %r;\n  z_max= %r;\n  seed= %d;\n  write_pred= false;" %
         (pkf, float(spec["z_min"]), float(spec["z_max"]), spec["seed"]))
     add("  bias_model= %d;\n}\n" % spec.get("bias_model", 2))

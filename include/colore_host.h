@@ -97,6 +97,20 @@ void cg_spline_free(cg_spline *s);
 /* Adaptive Gauss-Legendre quadrature of f on [a, b] to relative tolerance. */
 double cg_integrate(double (*f)(double, void *), void *par, double a, double b, double rtol);
 
+/* Output writers of io.c (no cfitsio needed) ------------------------------ */
+#define CG_OUT_ASCII 0
+#define CG_OUT_FITS 1
+/* One HEALPix map (RING, 12 nside^2 floats) as a FITS binary table with the
+ * keywords of he_write_healpix_map (src/healpix_extra.c:4-57). */
+int cg_write_healpix_map(const char *fname, const float *map, long nside);
+/* Catalogue of population ipop from Src records (9 floats per source) as
+ * <prefix>_srcs_s<ipop+1>_0.fits (columns TYPE, RA, DEC, Z_COSMO, DZ_RSD) or
+ * .txt, as write_catalog (src/io.c:1069-1236) without lensing columns. */
+int cg_write_catalog(const char *prefix, int ipop, int format, const float *src9, long long n);
+/* <prefix>_dens_<tag>_0.dat from a padded [N][N][2(N/2+1)] float grid, the
+ * layout of write_density_grid (src/io.c:565-595) on one node. */
+int cg_write_density_grid(const char *prefix, const char *tag, const float *grid, int n_grid, double l_box);
+
 #ifdef __cplusplus
 }
 #endif
