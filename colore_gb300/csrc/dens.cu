@@ -118,19 +118,20 @@ __global__ void __launch_bounds__(BINS_WARPS * 32, 2) k_dens_bins(float *grid, c
       const float x0 = cg_cell_coord(ix, p.box.dx, p.box.p0);
       const float y0 = cg_cell_coord(iy, p.box.dx, p.box.p1), z0 = cg_cell_coord(iz, p.box.dx, p.box.p2);
       const float r = cg_norm3(x0, y0, z0);
+      const BgAt at = bg_at(p.g, r);
       if (p.mode != CG_DMODE_NONE) {
-        d = cg_dens_transform(p.mode, d, need_d1 ? bg(p.d1, p.g, r) : 0.0f, s2);
+        d = cg_dens_transform(p.mode, d, need_d1 ? bgv(p.d1, at) : 0.0f, s2);
         *ptr = d;
       }
       if (nz > 0) {
-        const float z = bg(p.zt, p.g, r);
+        const float z = bgv(p.zt, at);
         const int b = (int)CG_MUL(z, p.idz) + 1;
         if (b >= 0 && b < nz) {
           bin = b;
           zz = z;
 #pragma unroll
           for (int t = 0; t < MAXT; t++)
-            if (t < nt) bs[t] = cg_bias_model(d, bg(p.bz[t], p.g, r), p.bias_model);
+            if (t < nt) bs[t] = cg_bias_model(d, bgv(p.bz[t], at), p.bias_model);
         }
       }
     }
@@ -226,12 +227,10 @@ __global__ void __launch_bounds__(256) k_lpt_cic(float *grid, const float *__res
       i0[a] = (int)u;
       a1[a] = CG_SUB(u, (float)i0[a]);
       a0[a] = CG_SUB(1.0f, a1[a]);
-      i1[a] = i0[a] + 1;
-      /* full modulo: a cell index stays inside the grid whatever q is */
-      i0[a] %= N;
-      i1[a] %= N;
-      if (i0[a] < 0) i0[a] += N;
-      if (i1[a] < 0) i1[a] += N;
+      /* q is in [0, L) unless the displacement exceeds the box: then a full
+       * modulo keeps the cell index inside the grid */
+      if ((unsigned)i0[a] >= (unsigned)N) i0[a] = ((i0[a] % N) + N) % N;
+      i1[a] = i0[a] + 1 == N ? 0 : i0[a] + 1;
       /* position of i0 in the box, the shorter way round the period */
       int d = i0[a] - org[a];
       if (d < -N / 2) d += N;
@@ -259,10 +258,11 @@ __global__ void __launch_bounds__(256) k_lpt_cic(float *grid, const float *__res
     const float v = (&box[0][0][0])[i];
     if (v == 0.0f) continue;
     const int bx = i % CB_X, by = (i / CB_X) % CB_Y, bz = i / (CB_X * CB_Y);
-    int gx = (org[0] + bx) % N, gy = (org[1] + by) % N, gz = (org[2] + bz) % N;
-    if (gx < 0) gx += N;
-    if (gy < 0) gy += N;
-    if (gz < 0) gz += N;
+    /* box cells lie within one period of the tile */
+    int gx = org[0] + bx, gy = org[1] + by, gz = org[2] + bz;
+    gx = gx < 0 ? gx + N : (gx >= N ? gx - N : gx);
+    gy = gy < 0 ? gy + N : (gy >= N ? gy - N : gy);
+    gz = gz < 0 ? gz + N : (gz >= N ? gz - N : gz);
     atomicAdd(&grid[pidx(gx, gy, gz, N)], v);
   }
 }

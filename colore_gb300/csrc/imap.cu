@@ -85,6 +85,7 @@ __device__ __forceinline__ K sample_key(const cg_imap_params &p, const float *r0
   int64_t pix = 0;
   const int ir = cg_imap_sample(xc, yc, zc, yz2, c.drr, r0, rf, p.nr, c.irad0, p.nside, &pix);
   if (ir < 0 || ir >= p.nr) return empty_key<K>();
+  if (sizeof(K) == 4) return (K)((unsigned)ir * (unsigned)p.npix + (unsigned)pix);
   return (K)((long long)ir * p.npix + pix);
 }
 
@@ -375,14 +376,19 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap_paint(cg_imap_params p)
       if (__ldg(&off[mid]) <= s0) lo = mid;
       else hi = mid - 1;
     }
-    long long hw = lo; /* the warp's current record */
+    long long hw = lo, ow = __ldg(&off[lo]); /* the warp's current record and its first sample */
     for (long long sb = s0; sb < s1; sb += 32) {
       const long long s = sb + lane;
-      long long h = hw;
+      long long h = hw, oh = ow;
       K key = empty_key<K>();
       float temp = 0.0f;
       if (s < s1) {
-        while (h + 1 < H && __ldg(&off[h + 1]) <= s) h++;
+        while (h + 1 < H) {
+          const long long nx = __ldg(&off[h + 1]);
+          if (nx > s) break;
+          h++;
+          oh = nx;
+        }
         const float4 qa = __ldg(reinterpret_cast<const float4 *>(cl + h));
         const float4 qb = __ldg(reinterpret_cast<const float4 *>(cl + h) + 1);
         const int pk = __float_as_int(qb.w);
@@ -395,11 +401,12 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap_paint(cg_imap_params p)
         c.nsub = pk & 2047;
         c.irad0 = (pk >> 11) - 1;
         c.pad = 0;
-        key = sample_key<K>(p, r0, rf, c, qa.y, qa.z, (int)(s - __ldg(&off[h])));
+        key = sample_key<K>(p, r0, rf, c, qa.y, qa.z, (int)(s - oh));
         temp = c.temp;
       }
       add_runs(key, (int)h, temp, lane, p);
       hw = __shfl_sync(FULL, h, 31);
+      ow = __shfl_sync(FULL, oh, 31);
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) p.ctr[4] = S; /* listed samples, for the caller */

@@ -43,10 +43,11 @@ __device__ __forceinline__ void cell_of(long long c, const Box &b, int &ix, int 
 __device__ __forceinline__ float pois_lambda(const cg_srcs_params &p, float d, float r)
 {
   if (!(r < p.rlim)) return 0.0f;
-  float nd = bg(p.nz, p.g, r);
+  const BgAt at = bg_at(p.g, r);
+  float nd = bgv(p.nz, at);
   if (!(nd > 0.0f)) return 0.0f;
-  float b = bg(p.bz, p.g, r);
-  float dn = bg(p.norm, p.g, r);
+  float b = bgv(p.bz, at);
+  float dn = bgv(p.norm, at);
   return cg_src_lambda(nd, p.cell_vol, d, b, dn, p.bias_model);
 }
 
