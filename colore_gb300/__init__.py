@@ -53,6 +53,8 @@ class Config(C.Structure):
         ("do_kappa", C.c_int), ("n_kappa", C.c_int), ("nside_kappa", C.c_int),
         ("kappa_r", C.c_double * NPLANES_MAX),
         ("need_beaming", C.c_int),
+        ("do_isw", C.c_int), ("n_isw", C.c_int), ("nside_isw", C.c_int),
+        ("isw_r", C.c_double * NPLANES_MAX),
     ]
 
 
@@ -96,6 +98,7 @@ def lib():
             "cg_download_count_map": (C.c_int, [vp, C.c_int, vp]),
             "cg_download_imap": (C.c_int, [vp, C.c_int, vp, vp]),
             "cg_download_kappa": (C.c_int, [vp, vp]),
+            "cg_download_isw": (C.c_int, [vp, vp]),
             "cg_download_norm": (C.c_int, [vp, C.c_int, C.c_int, vp, vp]),
             "cg_kernel_launches": (C.c_longlong, [vp]),
             "cg_set_profiling": (C.c_int, [vp, C.c_int]),
@@ -130,7 +133,7 @@ def exported_symbols():
             "cg_collect_density_normalization", "cg_collect_density_normalization_static", "cg_set_norm_tables", "cg_srcs_set_cartesian",
             "cg_imap_set_cartesian", "cg_imap_samples", "cg_get_beam_properties", "cg_run_mock", "cg_download_grid",
             "cg_num_sources", "cg_download_catalog", "cg_download_count_map", "cg_download_imap",
-            "cg_download_kappa", "cg_download_norm", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_read_run_params",
+            "cg_download_kappa", "cg_download_isw", "cg_download_norm", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_read_run_params",
             "cg_params_free", "cg_params_to_config", "cg_write_healpix_map", "cg_write_catalog",
             "cg_write_density_grid", "cg64_create", "cg64_destroy", "cg64_last_error",
             "cg64_run_mock", "cg64_num_sources", "cg64_download"]
@@ -178,6 +181,9 @@ class Params:
             raise CGError("read_run_params(%s): %s" % (fname, err.value.decode()))
         self.config = Config()
         L.cg_params_to_config(self._p, C.byref(self.config))
+        # the config's table pointers live in this object: keep it alive as
+        # long as the config is referenced
+        self.config._owner = self
 
     def __del__(self):
         if getattr(self, "_p", None) and _lib is not None:
@@ -320,6 +326,13 @@ class Mock:
         self._chk(lib().cg_download_imap(self._c, ipop, m.ctypes.data, na.ctypes.data if with_nadd else None),
                   "download_imap")
         return (m, na) if with_nadd else m
+
+    def isw(self, out=None):
+        """ISW maps, n_isw x 12 nside_isw^2, RING order."""
+        ns = self.cfg.nside_isw
+        m = out if out is not None else np.empty((self.cfg.n_isw, 12 * ns * ns), np.float32)
+        self._chk(lib().cg_download_isw(self._c, m.ctypes.data), "download_isw")
+        return m
 
     def kappa(self, out=None):
         ns = self.cfg.nside_kappa

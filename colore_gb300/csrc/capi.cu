@@ -65,7 +65,7 @@ struct cg_ctx {
   int N = 0, NH = 0;
   size_t grid_floats = 0;
   /* host double tables */
-  std::vector<double> h_r, h_z, h_d1, h_v1, h_ih, h_a, h_ra;
+  std::vector<double> h_r, h_z, h_d1, h_v1, h_ih, h_a, h_ra, h_pd;
   /* device tables */
   float *d_tabs = nullptr;
   Grid1 g;
@@ -105,6 +105,11 @@ struct cg_ctx {
   long long list_cap = 0;
   /* kappa */
   float *d_kmap = nullptr, *d_kfac = nullptr, *d_kinv = nullptr;
+  /* ISW */
+  float *d_imap_isw = nullptr, *d_ifac = nullptr;
+  int *d_iir = nullptr;
+  int ipl = 0, inr = 0;
+  long long inpix = 0;
   int *d_kir = nullptr;
   int knr = 0, kpl = 0;
   float kdr = 0;
@@ -269,6 +274,8 @@ static int validate(const cg_config *cfg, char *msg, size_t len)
     return snprintf(msg, len, "population count out of range"), CG_EINVAL;
   if (cfg->do_kappa && (cfg->n_kappa < 1 || cfg->n_kappa > CG_NPLANES_MAX || cfg->nside_kappa < 1))
     return snprintf(msg, len, "kappa planes or nside out of range"), CG_EINVAL;
+  if (cfg->do_isw && (cfg->n_isw < 1 || cfg->n_isw > CG_NPLANES_MAX || cfg->nside_isw < 1))
+    return snprintf(msg, len, "ISW planes or nside out of range"), CG_EINVAL;
   if (cfg->dens_type != CG_DENS_LGNR && cfg->dens_type != CG_DENS_1LPT && cfg->dens_type != CG_DENS_CLIP)
     return snprintf(msg, len, "dens_type %d not supported", cfg->dens_type), CG_EINVAL;
   const double *req[] = {cfg->r_arr_r2z, cfg->z_arr_r2z, cfg->growth_d_arr, cfg->growth_d2_arr, cfg->growth_v_arr,
@@ -299,6 +306,7 @@ extern "C" int cg_upload_tables(cg_ctx *c, const cg_config *cfg)
   cp(c->h_d1, cfg->growth_d_arr);
   cp(c->h_v1, cfg->growth_v_arr);
   cp(c->h_ih, cfg->ihub_arr);
+  cp(c->h_pd, cfg->growth_pd_arr);
   cp(c->h_a, cfg->a_arr_a2r);
   cp(c->h_ra, cfg->r_arr_a2r);
   /* packed float tables: 9 background + 2 per population + 2 per species */
@@ -417,6 +425,7 @@ extern "C" int cg_memory_estimate(const cg_config *cfg, unsigned long long *byte
   for (int i = 0; i < cfg->n_imap; i++)
     b += (unsigned long long)cfg->imap_nr[i] * 12ull * cfg->nside_imap[i] * cfg->nside_imap[i] * 8ull;
   if (cfg->do_kappa) b += (unsigned long long)cfg->n_kappa * 12ull * cfg->nside_kappa * cfg->nside_kappa * 4ull;
+  if (cfg->do_isw) b += (unsigned long long)cfg->n_isw * 12ull * cfg->nside_isw * cfg->nside_isw * 4ull;
   *bytes = b;
   return CG_OK;
 }
@@ -430,7 +439,8 @@ extern "C" void cg_destroy(cg_ctx *c)
                   c->d_disp[1], c->d_disp[2], c->d_part, c->d_stats, c->d_s2f, c->d_err, c->d_ncount,
                   c->d_zsum, c->d_bsum, c->d_counts, c->d_bsums, c->d_total, c->d_tmpmap, c->d_kmap,
                   c->d_kfac, c->d_kinv, c->d_kir, c->d_ovf_cell, c->d_ovf_cnt, c->d_ovf_n,
-                  c->d_cells, c->d_cell_n, c->d_cell_off, c->d_scan_tmp, c->d_imap_ctr};
+                  c->d_cells, c->d_cell_n, c->d_cell_off, c->d_scan_tmp, c->d_imap_ctr,
+                  c->d_imap_isw, c->d_ifac, c->d_iir};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < CG_NPOP_MAX; i++) {
@@ -1108,6 +1118,57 @@ static int kappa_run(cg_ctx *c)
   return CG_OK;
 }
 
+/* isw_beams_preproc + isw_get_beam_properties (isw.c:38-147) */
+static int isw_run(cg_ctx *c)
+{
+  const int np = c->cfg.n_isw;
+  const int nside = c->cfg.nside_isw;
+  const long long npix = 12LL * nside * nside;
+  const int nr = c->N / 2; /* get_radial_params with NSAMP_RAD = 1 */
+  const double dr = c->cfg.r_max / nr, idr = 1. / dr;
+  std::vector<float> rp(np); /* plane distances, stored as flouble and sorted */
+  for (int i = 0; i < np; i++) rp[i] = (float)c->cfg.isw_r[i];
+  std::stable_sort(rp.begin(), rp.end());
+  std::vector<int> ir(2 * np);
+  for (int i = 0; i < np; i++) ir[np + i] = std::min((int)((double)rp[i] * idr + 0.5), nr - 1);
+  ir[0] = 0;
+  for (int i = 1; i < np; i++) ir[i] = ir[np + i - 1] + 1;
+  std::vector<float> fac(nr);
+  for (int i = 0; i < nr; i++) {
+    const double rm = (i + 0.5) * dr;
+    fac[i] = (float)(2 * host_bg(c, c->h_pd, c->h_pd[0], c->h_pd[CG_NA - 1], rm) * dr);
+  }
+  int rc;
+  if (c->ipl != np || c->inpix != npix)
+    if ((rc = dalloc(c, &c->d_imap_isw, (size_t)np * npix))) return rc;
+  if (c->inr != nr || c->ipl != np)
+    if ((rc = dalloc(c, &c->d_ifac, (size_t)nr)) || (rc = dalloc(c, &c->d_iir, 2 * (size_t)np))) return rc;
+  c->ipl = np;
+  c->inpix = npix;
+  c->inr = nr;
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_ifac, fac.data(), fac.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_iir, ir.data(), ir.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  cg_kappa_params p;
+  memset(&p, 0, sizeof(p));
+  p.box = c->box;
+  p.nside = nside;
+  p.npix = npix;
+  p.nplanes = np;
+  p.ir_min = c->d_iir;
+  p.ir_max = c->d_iir + np;
+  p.nr = nr;
+  p.dr = (float)dr;
+  p.fac1 = c->d_ifac;
+  p.map = c->d_imap_isw;
+  {
+    ProfScope ps(c, "isw");
+    CUDA_TRY(c, cg_isw_integrate(c->stream, c->d_npot, &p));
+  }
+  c->launches++;
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host staging vectors */
+  return CG_OK;
+}
+
 extern "C" int cg_get_beam_properties(cg_ctx *c)
 {
   if (!c) return CG_EINVAL;
@@ -1116,6 +1177,8 @@ extern "C" int cg_get_beam_properties(cg_ctx *c)
   cudaSetDevice(c->device);
   if (c->cfg.do_kappa)
     if (int rc = kappa_run(c)) return rc;
+  if (c->cfg.do_isw)
+    if (int rc = isw_run(c)) return rc;
   if (c->cfg.n_srcs > 0) {
     if (!c->have_srcs) return fail(c, CG_ESTATE, "srcs_set_cartesian first");
     for (int ip = 0; ip < c->cfg.n_srcs; ip++) {
@@ -1230,6 +1293,16 @@ extern "C" int cg_download_imap(cg_ctx *c, int ipop, float *map, int *nadd)
     CUDA_TRY(c, cudaMemcpyAsync(map, c->d_tmpmap, m * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
   }
   if (nadd) CUDA_TRY(c, cudaMemcpyAsync(nadd, M.nadd, m * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return check_device_errors(c);
+}
+
+extern "C" int cg_download_isw(cg_ctx *c, float *map)
+{
+  if (!c || !map) return CG_EINVAL;
+  if (!c->d_imap_isw) return fail(c, CG_ESTATE, "ISW maps not computed");
+  CUDA_TRY(c, cudaMemcpyAsync(map, c->d_imap_isw, (size_t)c->ipl * c->inpix * sizeof(float), cudaMemcpyDeviceToHost,
+                              c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return check_device_errors(c);
 }

@@ -91,8 +91,8 @@ int main(int argc, char **argv)
   printf("  Real-space resolution: dx = %.3lE Mpc/h\n", p->l_box / p->n_grid);
   printf("  Original sigma8=%lf, Sigma_Gauss should be %lf\n", p->sigma8_input, p->sigma2_gauss_theory > 0 ? sqrt(p->sigma2_gauss_theory) : 0.0);
   printf("  GPU memory plan: %.3f GB\n", mem / 1e9);
-  if (p->n_cstm || p->do_isw || p->do_skewers || p->do_srcs_lensing)
-    fprintf(stderr, "Warning: custom maps, ISW, skewers and source lensing are not produced by this build\n");
+  if (p->n_cstm || p->do_skewers || p->do_srcs_lensing)
+    fprintf(stderr, "Warning: custom maps, skewers and source lensing are not produced by this build\n");
   if (test_memory) {
     cg_params_free(p);
     return 0;
@@ -147,6 +147,18 @@ int main(int argc, char **argv)
   /* write_catalog (io.c:1069-1236): FITS or ASCII; HDF5 is not built */
   const int fmt = !strcmp(p->output_format, "FITS") ? CG_OUT_FITS : CG_OUT_ASCII;
   if (p->n_srcs > 0 && !strcmp(p->output_format, "HDF5")) printf("HDF5 not supported\n");
+  if (p->do_isw) {
+    printf("*** Writing isw source maps\n");
+    long npix = 12L * p->nside_isw * p->nside_isw;
+    float *m = malloc((size_t)p->n_isw * npix * sizeof(float));
+    if (!m) die(c, CG_ENOMEM, "ISW buffer");
+    if ((rc = cg_download_isw(c, m))) die(c, rc, "download_isw");
+    for (int i = 0; i < p->n_isw; i++) {
+      snprintf(out, sizeof(out), "%s_isw_z%03d.fits", p->prefix_out, i);
+      write_map(c, out, m + (size_t)i * npix, p->nside_isw);
+    }
+    free(m);
+  }
   for (int ip = 0; ip < p->n_srcs; ip++) {
     printf("*** Writing source catalogs\n %d-th population (%s)\n", ip, fmt == CG_OUT_FITS ? "FITS" : "ASCII");
     float *src = malloc((size_t)(ns[ip] > 0 ? ns[ip] : 1) * 9 * sizeof(float));

@@ -429,5 +429,10 @@ int cg_host_cosmo_set(cg_params *p, char *err, size_t el)
       return snprintf(err, el, "Source plane %d outside redshift range", i + 1), CG_EINVAL;
     p->kappa_r[i] = cg_cosmo_chi(&c, 1. / (1 + p->z_kappa_out[i]));
   }
+  for (int i = 0; i < p->n_isw; i++) {
+    if (p->z_isw_out[i] > p->z_max)
+      return snprintf(err, el, "Source plane %d outside redshift range", i + 1), CG_EINVAL;
+    p->isw_r[i] = cg_cosmo_chi(&c, 1. / (1 + p->z_isw_out[i]));
+  }
   return CG_OK;
 }

@@ -431,7 +431,11 @@ int cg_read_run_params(const char *fname, cg_params **out, char *err, size_t el)
     rd_double_array(&r, "kappa", "z_out", p->z_kappa_out, &p->n_kappa, CG_NPLANES_MAX);
     rd_int(&r, "kappa", "nside", &p->nside_kappa);
   }
-  if (lookup(root, "isw")) p->do_isw = 1;
+  if (lookup(root, "isw")) {
+    p->do_isw = 1;
+    rd_double_array(&r, "isw", "z_out", p->z_isw_out, &p->n_isw, CG_NPLANES_MAX);
+    rd_int(&r, "isw", "nside", &p->nside_isw);
+  }
   node_free(root);
   if (r.rc) {
     free(p);
@@ -514,5 +518,9 @@ int cg_params_to_config(const cg_params *p, cg_config *c)
   c->nside_kappa = p->nside_kappa;
   for (int i = 0; i < p->n_kappa; i++) c->kappa_r[i] = p->kappa_r[i];
   c->need_beaming = p->need_beaming;
+  c->do_isw = p->do_isw;
+  c->n_isw = p->n_isw;
+  c->nside_isw = p->nside_isw;
+  for (int i = 0; i < p->n_isw; i++) c->isw_r[i] = p->isw_r[i];
   return CG_OK;
 }

@@ -12,6 +12,7 @@
  * nest-to-ring reordering of write_kappa, io.c:826-873).  Threads of a warp
  * hold neighbouring NEST pixels, so their rays stay close and the 19-point
  * stencil reads hit L1/L2.  The radial sums use Kahan compensation.
+ * k_isw integrates the ISW maps along the same rays.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -71,7 +72,50 @@ __global__ void __launch_bounds__(256) k_kappa(const float *__restrict__ phi, cg
   }
 }
 
+/* isw_get_beam_properties (isw.c:78-147): the same rays, the potential at the
+ * nearest cell (RETURN_PDOT, beaming.c:81-82, 145-180) weighted by
+ * fac1 = 2 PD(r) dr, cumulative over the sorted planes. */
+__global__ void __launch_bounds__(256) k_isw(const float *__restrict__ phi, cg_kappa_params p)
+{
+  extern __shared__ float ksh[];
+  float *f1 = ksh;
+  for (int i = threadIdx.x; i < p.nr; i += blockDim.x) f1[i] = p.fac1[i];
+  __syncthreads();
+  const long long ip = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (ip >= p.npix) return;
+  const int N = p.box.N;
+  const int ngx = 2 * (N / 2 + 1);
+  const size_t plane = (size_t)ngx * N;
+  float u[3];
+  cg_pix2vec_nest(p.nside, ip, u);
+  const float po[3] = {p.box.p0, p.box.p1, p.box.p2};
+  const long long ring = cg_nest2ring(p.nside, ip);
+  float acc = 0.0f, cmp = 0.0f;
+  for (int pl = 0; pl < p.nplanes; pl++) {
+    const int irmin = p.ir_min[pl], irmax = p.ir_max[pl];
+    for (int irr = irmin; irr <= irmax; irr++) {
+      const float rm = CG_MUL(CG_ADD((float)irr, 0.5f), p.dr);
+      const int x0 = cg_ngp_cell(rm, u[0], po[0], p.box.idx, N);
+      const int y0 = cg_ngp_cell(rm, u[1], po[1], p.box.idx, N);
+      const int z0 = cg_ngp_cell(rm, u[2], po[2], p.box.idx, N);
+      const float pd = __ldg(phi + (size_t)z0 * plane + y0 * ngx + x0);
+      cg_kahan_add(&acc, &cmp, CG_MUL(pd, f1[irr]));
+    }
+    p.map[(long long)pl * p.npix + ring] = acc;
+  }
+}
+
 } /* namespace */
+
+cudaError_t cg_isw_integrate(cudaStream_t s, const float *phi, const cg_kappa_params *p)
+{
+  size_t smem = (size_t)p->nr * sizeof(float);
+  cudaError_t e = cudaFuncSetAttribute(k_isw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  long long blocks = (p->npix + 255) / 256;
+  k_isw<<<(unsigned)blocks, 256, smem, s>>>(phi, *p);
+  return cudaGetLastError();
+}
 
 cudaError_t cg_kappa_integrate(cudaStream_t s, const float *phi, const cg_kappa_params *p)
 {

@@ -22,5 +22,7 @@ struct cg_kappa_params {
 };
 
 cudaError_t cg_kappa_integrate(cudaStream_t s, const float *phi, const cg_kappa_params *p);
+/* ISW: fac1 = 2 PD(r) dr (isw.c:105-111); fac2 and inv_r_max unused. */
+cudaError_t cg_isw_integrate(cudaStream_t s, const float *phi, const cg_kappa_params *p);
 
 #endif

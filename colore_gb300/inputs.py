@@ -127,6 +127,9 @@ def write_inputs(dirname, spec, prefix="run"):
     if "kappa" in spec:
         kz = ", ".join("%r" % float(z) for z in spec["kappa"]["z_out"])
         add("kappa:\n{\n  z_out= [%s];\n  nside= %d;\n}\n" % (kz, spec["kappa"]["nside"]))
+    if "isw" in spec:
+        iz = ", ".join("%r" % float(z) for z in spec["isw"]["z_out"])
+        add("isw:\n{\n  z_out= [%s];\n  nside= %d;\n}\n" % (iz, spec["isw"]["nside"]))
     fcfg = os.path.join(dirname, prefix + ".cfg")
     with open(fcfg, "w") as f:
         f.write("\n".join(lines))

@@ -109,6 +109,9 @@ typedef struct {
   double kappa_r[CG_NPLANES_MAX]; /* source-plane comoving distances */
   /* need_beaming, src/io.c:460-461 */
   int need_beaming;
+  /* integrated Sachs-Wolfe maps (isw.c:78-147), planes as kappa's */
+  int do_isw, n_isw, nside_isw;
+  double isw_r[CG_NPLANES_MAX]; /* plane comoving distances (cosmo.c:839-845) */
 } cg_config;
 
 typedef struct cg_ctx cg_ctx;
@@ -179,6 +182,8 @@ int cg_download_count_map(cg_ctx *ctx, int ipop, int *counts);
 int cg_download_imap(cg_ctx *ctx, int ipop, float *map, int *nadd);
 /* Convergence maps: n_kappa * 12 nside^2 values, RING order (src/io.c:826-873). */
 int cg_download_kappa(cg_ctx *ctx, float *map);
+/* ISW maps: n_isw * 12 nside_isw^2 values, RING order (write_isw, src/io.c:946-1010). */
+int cg_download_isw(cg_ctx *ctx, float *map);
 
 /* FP32 normalisation table the kernels use: kind 0 = source population
  * ipop (srcs_norm_arr, src/common.h:318), 1 = intensity species

@@ -60,8 +60,11 @@ typedef struct {
   /* kappa */
   int do_kappa, n_kappa, nside_kappa;
   double z_kappa_out[CG_NPLANES_MAX], kappa_r[CG_NPLANES_MAX];
+  /* isw (io.c:421-426) */
+  int do_isw, n_isw, nside_isw;
+  double z_isw_out[CG_NPLANES_MAX], isw_r[CG_NPLANES_MAX];
   /* out-of-scope sections seen in the file (reported, not run) */
-  int n_cstm, do_isw, do_skewers, do_srcs_lensing;
+  int n_cstm, do_skewers, do_srcs_lensing;
   int need_beaming, nside_base, bias_model;
 } cg_params;
 

@@ -11,6 +11,7 @@
  *   or_beam_rsd32 srcs beam RSD (pre/get/postproc)        srcs.c:437-504, 656-662
  *   or_imap32     imap_set_cartesian_single               imap.c:135-245
  *   or_kappa32    kappa_get_beam_properties               kappa.c:78-175
+ *   or_isw32      isw_get_beam_properties                 isw.c:78-147
  * Tables are rebuilt from the config with the same double->float roundings
  * as the GPU upload.  The Poisson and position streams are the Philox
  * streams of the GPU path (the reference's GSL MT19937 streams depend on the
@@ -490,6 +491,56 @@ int or_kappa32(const cg_config *cfg, const float *npot, float *map)
   free(inv);
   free(f1);
   free(f2);
+  s32_free(&s);
+  return 0;
+}
+
+
+/* isw_get_beam_properties (isw.c:78-147) in the GPU's FP32 arithmetic:
+ * FP64-built weights 2 PD(r) dr rounded to float, the cell of cg_ngp_cell,
+ * compensated sum. */
+int or_isw32(const cg_config *cfg, const float *npot, float *map)
+{
+  S32 s;
+  s32_init(&s, cfg);
+  const int N = s.N, np = cfg->n_isw, nside = cfg->nside_isw;
+  const long long npix = 12LL * nside * nside;
+  const int nr = N / 2;
+  const double dr = cfg->r_max / nr, idr = 1. / dr;
+  float *rp = malloc(np * sizeof(float));
+  for (int i = 0; i < np; i++) rp[i] = (float)cfg->isw_r[i];
+  qsort(rp, np, sizeof(float), cmp_float);
+  int *irmin = malloc(np * sizeof(int)), *irmax = malloc(np * sizeof(int));
+  float *f1 = malloc(nr * sizeof(float));
+  for (int i = 0; i < np; i++) {
+    int irh = (int)((double)rp[i] * idr + 0.5);
+    irmax[i] = irh < nr - 1 ? irh : nr - 1;
+  }
+  irmin[0] = 0;
+  for (int i = 1; i < np; i++) irmin[i] = irmax[i - 1] + 1;
+  const double *pd = cfg->growth_pd_arr;
+  for (int i = 0; i < nr; i++) f1[i] = (float)(2 * bg64(cfg, pd, pd[0], pd[CG_NA - 1], (i + 0.5) * dr) * dr);
+  const float drf = (float)dr;
+#pragma omp parallel for schedule(static)
+  for (long long ip = 0; ip < npix; ip++) {
+    float u[3];
+    cg_pix2vec_nest(nside, ip, u);
+    long long ring = cg_nest2ring(nside, ip);
+    float acc = 0, cmp = 0;
+    for (int pl = 0; pl < np; pl++) {
+      for (int irr = irmin[pl]; irr <= irmax[pl]; irr++) {
+        float rm = CG_MUL(CG_ADD((float)irr, 0.5f), drf);
+        int x0 = cg_ngp_cell(rm, u[0], s.p[0], s.idx, N), y0 = cg_ngp_cell(rm, u[1], s.p[1], s.idx, N),
+            z0 = cg_ngp_cell(rm, u[2], s.p[2], s.idx, N);
+        cg_kahan_add(&acc, &cmp, CG_MUL(npot[pidx(x0, y0, z0, N)], f1[irr]));
+      }
+      map[(long long)pl * npix + ring] = acc;
+    }
+  }
+  free(rp);
+  free(irmin);
+  free(irmax);
+  free(f1);
   s32_free(&s);
   return 0;
 }

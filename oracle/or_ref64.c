@@ -12,6 +12,7 @@
  *   or_lambda64      Poisson mean per cell         srcs.c:156-178
  *   or_imap64        imap_set_cartesian_single     imap.c:135-245
  *   or_kappa64       kappa_get_beam_properties     kappa.c:78-175
+ *   or_isw64         isw_get_beam_properties       isw.c:78-147
  *   or_run_mock64    the driver sequence of main.c:66-125 for timing.
  * Random numbers: the Philox streams of the GPU path (uniforms identical
  * bit for bit), since GSL's MT19937 streams cannot be reproduced here.
@@ -609,6 +610,58 @@ int or_kappa64_part(const cg_config *c, const double *p, int pix_stride, double 
 }
 
 int or_kappa64(const cg_config *c, const double *p, double *map) { return or_kappa64_part(c, p, 1, map); }
+
+/* isw_beams_preproc + isw_get_beam_properties, isw.c:38-147: per NEST pixel,
+ * the potential at the nearest cell (RETURN_PDOT with the NGP lensing
+ * interpolation, beaming.c:81-82,145-180) times 2 PD(r) dr, summed along the
+ * ray and written at each plane (cumulative), in RING order (write_isw,
+ * io.c:946-1010). */
+int or_isw64(const cg_config *c, const double *p, double *map)
+{
+  const int N = c->n_grid, np = c->n_isw, nside = c->nside_isw;
+  const long npix = 12L * nside * nside;
+  const int nr = N / 2;
+  const double dr = c->r_max / nr, idr = 1. / dr, idx = N / c->l_box;
+  double rp[CG_NPLANES_MAX];
+  for (int i = 0; i < np; i++) rp[i] = (float)c->isw_r[i]; /* stored as flouble */
+  for (int i = 1; i < np; i++)
+    for (int j = i; j > 0 && rp[j] < rp[j - 1]; j--) {
+      double t = rp[j];
+      rp[j] = rp[j - 1];
+      rp[j - 1] = t;
+    }
+  int irmin[CG_NPLANES_MAX], irmax[CG_NPLANES_MAX];
+  for (int i = 0; i < np; i++) {
+    int irh = (int)(rp[i] * idr + 0.5);
+    irmax[i] = irh < nr - 1 ? irh : nr - 1;
+  }
+  irmin[0] = 0;
+  for (int i = 1; i < np; i++) irmin[i] = irmax[i - 1] + 1;
+  double *fac = malloc(nr * sizeof(double));
+  const double *pd = c->growth_pd_arr;
+  for (int i = 0; i < nr; i++) fac[i] = 2 * bg(c, pd, pd[0], pd[CG_NA - 1], (i + 0.5) * dr) * dr;
+#pragma omp parallel for schedule(static)
+  for (long ip = 0; ip < npix; ip++) {
+    double u[3];
+    pix2vec_nest64(nside, ip, u);
+    long ring = cg_nest2ring(nside, ip);
+    double isw = 0;
+    for (int pl = 0; pl < np; pl++) {
+      for (int irr = irmin[pl]; irr <= irmax[pl]; irr++) {
+        double rm = (irr + 0.5) * dr;
+        int cc[3];
+        for (int a = 0; a < 3; a++) {
+          long q = (long)((rm * u[a] + c->pos_obs[a]) * idx + 0.5);
+          cc[a] = (int)(q >= N ? q - N : (q < 0 ? q + N : q));
+        }
+        isw += p[cc[0] + (size_t)N * (cc[1] + (size_t)N * cc[2])] * fac[irr];
+      }
+      map[(long)pl * npix + ring] = isw;
+    }
+  }
+  free(fac);
+  return 0;
+}
 
 /* Poisson deviate by inversion in double from the same Philox cell stream. */
 static int poisson64(double lam, uint32_t k0, uint32_t k1, long long cid)

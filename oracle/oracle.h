@@ -46,6 +46,7 @@ int or_norm_tables64(const cg_config *cfg, double *tabs, double *e0f, int *nz_ou
 int or_lambda64(const cg_config *cfg, int ipop, const double *dens, const double *normtab, double n0, double nf,
                 double *lambda);
 int or_kappa64(const cg_config *cfg, const double *npot, double *map);
+int or_isw64(const cg_config *cfg, const double *npot, double *map);
 int or_imap64(const cg_config *cfg, int ipop, const double *dens, const double *npot, const double *normtab,
               double n0, double nf, double *data, int *nadd);
 int or_imap64_part(const cg_config *cfg, int ipop, const double *dens, const double *npot, const double *normtab,
@@ -67,5 +68,6 @@ int or_beam_rsd32(const cg_config *cfg, const float *npot, long long n, const fl
 int or_imap32(const cg_config *cfg, int ipop, const float *dens, const float *npot, const float *normtab, float n0,
               float nf, float *data, int *nadd);
 int or_kappa32(const cg_config *cfg, const float *npot, float *map);
+int or_isw32(const cg_config *cfg, const float *npot, float *map);
 
 #endif

@@ -35,7 +35,7 @@ def lib():
             "or_counts32": [vp, i, vp, vp, f, f, vp, vp],
             "or_emit32": [vp, i, vp, vp, vp, f, f, C.c_longlong, vp, vp, vp, vp, vp],
             "or_beam_rsd32": [vp, vp, C.c_longlong, vp, vp], "or_imap32": [vp, i, vp, vp, vp, f, f, vp, vp],
-            "or_kappa32": [vp, vp, vp], "or_c2r_3d": [i, vp, vp], "or_r2c_3d": [i, vp, vp],
+            "or_kappa32": [vp, vp, vp], "or_isw32": [vp, vp, vp], "or_isw64": [vp, vp, vp], "or_c2r_3d": [i, vp, vp], "or_r2c_3d": [i, vp, vp],
             "or_vec_expf": [vp, vp, C.c_long], "or_vec_logf": [vp, vp, C.c_long],
             "or_vec_log1pf": [vp, vp, C.c_long], "or_vec_acosf": [vp, vp, C.c_long],
             "or_vec_atan2f": [vp, vp, vp, C.c_long], "or_vec_sincosf": [vp, vp, vp, C.c_long],
@@ -209,6 +209,20 @@ def imap32(cfg, ipop, dens, npot, tab, e):
     nadd = np.empty((nr, 12 * ns * ns), np.int32)
     lib().or_imap32(cfgp(cfg), ipop, P(dens), P(npot), P(tab), float(e[0]), float(e[1]), P(data), P(nadd))
     return data, nadd
+
+
+def isw64(cfg, npot):
+    ns = cfg.nside_isw
+    m = np.empty((cfg.n_isw, 12 * ns * ns))
+    lib().or_isw64(cfgp(cfg), P(np.ascontiguousarray(npot, np.float64)), P(m))
+    return m
+
+
+def isw32(cfg, npot):
+    ns = cfg.nside_isw
+    m = np.empty((cfg.n_isw, 12 * ns * ns), np.float32)
+    lib().or_isw32(cfgp(cfg), P(npot), P(m))
+    return m
 
 
 def kappa32(cfg, npot):

@@ -33,7 +33,8 @@ def _spec(kind):
                 srcs=[dict(nz=("gauss", 0.3, 0.1), density=200.0, bias=("1+z",), nside_count=16),
                       dict(nz=("flat", 0.1, 0.5), density=4.0, bias=("const", 2.0), nside_count=8)],
                 imap=[dict(tz=0.1, bias=("const", 1.0), z_range=(0.1, 0.5), nbands=6, nside=16)],
-                kappa=dict(z_out=[0.2, 0.4, 0.55], nside=16))
+                kappa=dict(z_out=[0.2, 0.4, 0.55], nside=16),
+                isw=dict(z_out=[0.55, 0.3], nside=16))
     if kind == "nobeam":
         base.pop("kappa")
         base["bias_model"] = 1
@@ -109,6 +110,7 @@ class Run:
         m.get_beam_properties()
         self.cats_beam = [m.catalog(i, pos=False, ipix=False) for i in range(self.cfg.n_srcs)]
         self.kappa = m.kappa() if self.cfg.do_kappa else None
+        self.isw = m.isw() if self.cfg.do_isw else None
 
 
 _RUNS = {}
@@ -346,6 +348,23 @@ def test_kappa_bitexact_and_fp64(runs, kind):
     assert np.array_equal(ref32.view(np.uint32), r.need('kappa').view(np.uint32))
     ref64 = orc.kappa64(r.cfg, unpad(r.phi).astype(np.float64))
     assert rel_rms(r.need('kappa'), ref64) < 1e-3
+
+
+def test_isw_bitexact_and_fp64(runs):
+    """ISW maps (isw.c:78-147): bit-exact against the FP32 restatement fed the
+    GPU potential; against the FP64 reference within 1e-3 rms (the nearest
+    cell of a ray step can differ between FP32 and FP64 positions)."""
+    import oracle as orc
+    r = runs("full")
+    got = r.need('isw')
+    assert got.shape == (2, 12 * 16 * 16) and np.all(np.isfinite(got))
+    ref32 = orc.isw32(r.cfg, r.phi)
+    assert np.array_equal(ref32.view(np.uint32), got.view(np.uint32))
+    ref64 = orc.isw64(r.cfg, unpad(r.phi).astype(np.float64))
+    assert rel_rms(got, ref64) < 1e-3
+    # maps come in order of distance (isw_beams_preproc sorts the planes) and
+    # are cumulative along the ray, so the two differ
+    assert not np.allclose(got[0], got[1])
 
 
 def test_rerun_is_deterministic(runs, tmp_path):

@@ -67,3 +67,51 @@ def test_syntax_error_reports_line(built):
     open(f, "w").write("global:\n{\n  z_min = ;\n}\n")
     with pytest.raises(cg.CGError, match="line 3"):
         cg.Params(f)
+
+
+def test_isw_section(built):
+    """isw { z_out; nside } (io.c:421-426): plane distances from the
+    cosmology, as the kappa planes (cosmo.c:831-845); planes beyond z_max are
+    rejected with the reference's message."""
+    import colore_gb300 as cg
+    from colore_gb300 import inputs
+    d = tempfile.mkdtemp()
+    spec = inputs.scaled("c1", 64)
+    spec["kappa"] = dict(z_out=[0.3, 0.45], nside=16)
+    spec["isw"] = dict(z_out=[0.45, 0.3], nside=8)
+    prm = cg.Params(inputs.write_inputs(d, spec))  # owns the tables the config points to
+    c = prm.config
+    assert (c.do_isw, c.n_isw, c.nside_isw) == (1, 2, 8) and c.need_beaming > 0
+    assert c.isw_r[0] == c.kappa_r[1] and c.isw_r[1] == c.kappa_r[0]
+    spec["isw"] = dict(z_out=[0.9], nside=8)
+    with pytest.raises(cg.CGError, match="Source plane 1 outside redshift range"):
+        cg.Params(inputs.write_inputs(tempfile.mkdtemp(), spec))
+
+
+def test_isw_oracles_on_a_constant_potential(built):
+    """For a uniform potential c the ISW map of plane p is c * sum of
+    2 PD(r) dr over the steps up to that plane, in both restatements."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(HERE), "oracle"))
+    import oracle as orc
+    import colore_gb300 as cg
+    from colore_gb300 import inputs
+    spec = inputs.scaled("c1", 64)
+    spec["isw"] = dict(z_out=[0.2, 0.45], nside=4)
+    prm = cg.Params(inputs.write_inputs(tempfile.mkdtemp(), spec))  # owns the tables
+    c = prm.config
+    n = c.n_grid
+    nr = n // 2
+    dr = c.r_max / nr
+    pd = np.array([c.growth_pd_arr[i] for i in range(cg.NA)])
+    r_arr = np.array([c.r_arr_r2z[i] for i in range(cg.NA)])
+    rm = (np.arange(nr) + 0.5) * dr
+    fac = 2 * np.interp(rm, r_arr, pd) * dr
+    rp = sorted(np.float32(c.isw_r[i]) for i in range(c.n_isw))
+    irmax = [min(int(r / dr + 0.5), nr - 1) for r in rp]
+    want = [3.0 * fac[:k + 1].sum() for k in irmax]
+    m64 = orc.isw64(c, np.full((n, n, n), 3.0))
+    m32 = orc.isw32(c, np.full((n, n, 2 * (n // 2 + 1)), 3.0, np.float32))
+    for pl in range(c.n_isw):
+        np.testing.assert_allclose(m64[pl], want[pl], rtol=1e-12)
+        np.testing.assert_allclose(m32[pl], want[pl], rtol=2e-6)
