@@ -100,6 +100,11 @@ def config_spec(name, n):
 # and field one read and one write of 4 bytes per cell; the fill+z pass only
 # writes).  fields: fill+z 2x4 W, y 2x(4R+4W), x 2x(4R+4W) = 40 B/cell.
 ALGO_BYTES_PER_CELL = {"field_fft": 40.0, "lpt_fft": 60.0, "dens_bins": 8.0, "srcs_count": 6.0}
+# DRAM bytes (read + write) per cell of the same groups measured by ncu on the
+# 512^3 case of config c4 (grids larger than L2); traffic grows with the cell
+# count, so a launch at N^3 moves N^3 times these (profiles/fft_passes_c4_512.md,
+# profiles/k_dens_bins_c4_512.md).
+MEASURED_DRAM_BYTES_PER_CELL = {"field_fft": 38.5, "lpt_fft": 59.8, "dens_bins": 7.6}
 
 
 def run_ours(args):
@@ -233,8 +238,11 @@ def run_ours(args):
             bytes_launch = ALGO_BYTES_PER_CELL[name] * ncell
             a = bytes_launch / (avg[name] / 1e3) / 1e9
             if rl is None or avg[name] > rl["_t"]:
+                tr = MEASURED_DRAM_BYTES_PER_CELL.get(name)
                 rl = {"kernel": name, "bound": "hbm", "achieved": round(a, 1), "peak": hbm, "unit": "GB/s",
-                      "frac": round(a / hbm, 4), "traffic": None, "peak_kind": peak_kind,
+                      "frac": round(a / hbm, 4), "traffic": tr * ncell if tr else None,
+                      "traffic_source": "ncu DRAM bytes per cell at 512^3 x cells" if tr else None,
+                      "peak_kind": peak_kind,
                       "algorithmic_bytes_per_launch": bytes_launch, "avg_launch_ms": round(avg[name], 3),
                       "_t": avg[name]}
     if rl:

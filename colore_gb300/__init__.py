@@ -55,6 +55,7 @@ class Config(C.Structure):
         ("need_beaming", C.c_int),
         ("do_isw", C.c_int), ("n_isw", C.c_int), ("nside_isw", C.c_int),
         ("isw_r", C.c_double * NPLANES_MAX),
+        ("lpt_interp_type", C.c_int),
     ]
 
 

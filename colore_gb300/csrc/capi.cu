@@ -276,6 +276,8 @@ static int validate(const cg_config *cfg, char *msg, size_t len)
     return snprintf(msg, len, "kappa planes or nside out of range"), CG_EINVAL;
   if (cfg->do_isw && (cfg->n_isw < 1 || cfg->n_isw > CG_NPLANES_MAX || cfg->nside_isw < 1))
     return snprintf(msg, len, "ISW planes or nside out of range"), CG_EINVAL;
+  if (cfg->dens_type == CG_DENS_1LPT && (cfg->lpt_interp_type < 0 || cfg->lpt_interp_type > 2))
+    return snprintf(msg, len, "lpt_interp_type %d: 0 (NGP), 1 (CIC) or 2 (TSC)", cfg->lpt_interp_type), CG_EINVAL;
   if (cfg->dens_type != CG_DENS_LGNR && cfg->dens_type != CG_DENS_1LPT && cfg->dens_type != CG_DENS_CLIP)
     return snprintf(msg, len, "dens_type %d not supported", cfg->dens_type), CG_EINVAL;
   const double *req[] = {cfg->r_arr_r2z, cfg->z_arr_r2z, cfg->growth_d_arr, cfg->growth_d2_arr, cfg->growth_v_arr,
@@ -589,6 +591,7 @@ extern "C" int cg_compute_physical_density_field(cg_ctx *c)
     lp.box = c->box;
     lp.g = c->g;
     lp.d1 = c->d1;
+    lp.interp = c->cfg.lpt_interp_type;
     CUDA_TRY(c, cg_lpt_cic(c->stream, c->d_dens, c->d_disp[0], c->d_disp[1], c->d_disp[2], &lp, c->nsm));
     c->launches += 4;
     c->pending_mode = CG_DMODE_RHO;

@@ -16,8 +16,8 @@
  *                    sums, since FP64 arithmetic is scarce on this GPU.  Each
  *                    block combines its warps' bins in FP64 in a fixed order
  *                    and sends them to global memory with one atomic each.
- *  k_lpt_cic       : 1LPT particle positions (density.c:473-501) and their
- *                    cloud-in-cell deposit (density.c:64-105), staged per
+ *  k_lpt_deposit   : 1LPT particle positions (density.c:473-501) and their
+ *                    NGP, CIC or TSC deposit (density.c:37-187), staged per
  *                    tile of particles in shared memory.
  */
 #include <cuda_runtime.h>
@@ -182,19 +182,23 @@ __global__ void __launch_bounds__(BINS_WARPS * 32, 2) k_dens_bins(float *grid, c
   }
 }
 
-/* 1LPT: x = q + D(r) Psi (wrapped into the box), then CIC into grid.  A block
- * takes a tile of CT_X x CT_Y x CT_Z particles (lattice cells) and deposits
- * into a shared-memory box that extends the tile by CT_H cells on every
- * side; the box is added to the grid at the end with one atomic per
- * non-zero cell.  Deposits that fall outside the box (particles displaced by
- * more than CT_H - 1 cells) go straight to the grid. */
+/* 1LPT: x = q + D(r) Psi (wrapped into the box), then the mass assignment of
+ * pos_2_dens (density.c:178-187): NGP (S = 0, density.c:37-62), CIC (S = 1,
+ * density.c:64-105) or TSC (S = 2, density.c:107-176).  A block takes a tile
+ * of CT_X x CT_Y x CT_Z particles (lattice cells) and deposits into a
+ * shared-memory box that extends the tile by CT_H cells on every side; the
+ * box is added to the grid at the end with one atomic per non-zero cell.
+ * Deposits that fall outside the box (particles displaced by more than about
+ * CT_H - 1 cells) go straight to the grid. */
 constexpr int CT_X = 32, CT_Y = 8, CT_Z = 8, CT_H = 2;
 constexpr int CB_X = CT_X + 2 * CT_H, CB_Y = CT_Y + 2 * CT_H, CB_Z = CT_Z + 2 * CT_H;
 
-__global__ void __launch_bounds__(256) k_lpt_cic(float *grid, const float *__restrict__ dx_,
-                                                 const float *__restrict__ dy_, const float *__restrict__ dz_,
-                                                 cg_lpt_params p)
+template <int S>
+__global__ void __launch_bounds__(256) k_lpt_deposit(float *grid, const float *__restrict__ dx_,
+                                                     const float *__restrict__ dy_, const float *__restrict__ dz_,
+                                                     cg_lpt_params p)
 {
+  constexpr int K = S + 1; /* cells per axis of the stencil */
   __shared__ float box[CB_Z][CB_Y][CB_X];
   const int N = p.box.N;
   const int ntx = (N + CT_X - 1) / CT_X, nty = (N + CT_Y - 1) / CT_Y;
@@ -215,43 +219,60 @@ __global__ void __launch_bounds__(256) k_lpt_cic(float *grid, const float *__res
     const float r = cg_norm3(xv[0], xv[1], xv[2]);
     const float dg = bg(p.d1, p.g, r);
     const float dsp[3] = {__ldg(&dx_[id]), __ldg(&dy_[id]), __ldg(&dz_[id])};
-    int i0[3], i1[3], b0[3];
-    float a0[3], a1[3];
+    int ib[3], bb[3]; /* first stencil cell of each axis, in the grid and in the box */
+    float w[3][K];
     bool inbox = true;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
       float q = CG_ADD(CG_FMA(dg, dsp[a], xv[a]), po[a]);
       if (q < 0.0f) q = CG_ADD(q, p.box.L);
       if (q >= p.box.L) q = CG_SUB(q, p.box.L);
-      float u = CG_MUL(q, iag);
-      i0[a] = (int)u;
-      a1[a] = CG_SUB(u, (float)i0[a]);
-      a0[a] = CG_SUB(1.0f, a1[a]);
+      const float u = CG_MUL(q, iag);
+      int i0;
+      if (S == 0) {
+        i0 = (int)CG_ADD(u, 0.5f);
+        w[a][0] = 1.0f;
+      } else if (S == 1) {
+        i0 = (int)u;
+        const float a1 = CG_SUB(u, (float)i0);
+        w[a][0] = CG_SUB(1.0f, a1);
+        w[a][K - 1] = a1;
+      } else {
+        i0 = (int)floorf(CG_ADD(u, 0.5f));
+        const float a0 = CG_SUB(u, (float)i0);
+        const float hm = CG_SUB(0.5f, a0), hp = CG_ADD(0.5f, a0);
+        w[a][0] = CG_MUL(0.5f, CG_MUL(hm, hm));
+        w[a][1] = CG_SUB(0.75f, CG_MUL(a0, a0));
+        w[a][K - 1] = CG_MUL(0.5f, CG_MUL(hp, hp));
+        i0 -= 1; /* the stencil starts one cell below the nearest */
+      }
       /* q is in [0, L) unless the displacement exceeds the box: then a full
        * modulo keeps the cell index inside the grid */
-      if ((unsigned)i0[a] >= (unsigned)N) i0[a] = ((i0[a] % N) + N) % N;
-      i1[a] = i0[a] + 1 == N ? 0 : i0[a] + 1;
-      /* position of i0 in the box, the shorter way round the period */
-      int d = i0[a] - org[a];
+      if ((unsigned)i0 >= (unsigned)N) i0 = ((i0 % N) + N) % N;
+      ib[a] = i0;
+      /* position of the first stencil cell in the box, the shorter way round */
+      int d = i0 - org[a];
       if (d < -N / 2) d += N;
       if (d >= N / 2) d -= N;
-      b0[a] = d;
-      inbox = inbox && d >= 0 && d + 1 < ext[a];
+      bb[a] = d;
+      inbox = inbox && d >= 0 && d + K - 1 < ext[a];
     }
-    const float w[8] = {CG_MUL(CG_MUL(a0[0], a0[1]), a0[2]), CG_MUL(CG_MUL(a1[0], a0[1]), a0[2]),
-                        CG_MUL(CG_MUL(a0[0], a1[1]), a0[2]), CG_MUL(CG_MUL(a1[0], a1[1]), a0[2]),
-                        CG_MUL(CG_MUL(a0[0], a0[1]), a1[2]), CG_MUL(CG_MUL(a1[0], a0[1]), a1[2]),
-                        CG_MUL(CG_MUL(a0[0], a1[1]), a1[2]), CG_MUL(CG_MUL(a1[0], a1[1]), a1[2])};
-    if (inbox) {
 #pragma unroll
-      for (int c = 0; c < 8; c++)
-        atomicAdd(&box[b0[2] + (c >> 2)][b0[1] + ((c >> 1) & 1)][b0[0] + (c & 1)], w[c]);
-    } else {
+    for (int cz = 0; cz < K; cz++)
 #pragma unroll
-      for (int c = 0; c < 8; c++)
-        atomicAdd(&grid[pidx((c & 1) ? i1[0] : i0[0], ((c >> 1) & 1) ? i1[1] : i0[1], (c >> 2) ? i1[2] : i0[2], N)],
-                  w[c]);
-    }
+      for (int cy = 0; cy < K; cy++)
+#pragma unroll
+        for (int cx = 0; cx < K; cx++) {
+          const float v = CG_MUL(CG_MUL(w[0][cx], w[1][cy]), w[2][cz]);
+          if (inbox) {
+            atomicAdd(&box[bb[2] + cz][bb[1] + cy][bb[0] + cx], v);
+          } else {
+            const int gx = ib[0] + cx >= N ? ib[0] + cx - N : ib[0] + cx;
+            const int gy = ib[1] + cy >= N ? ib[1] + cy - N : ib[1] + cy;
+            const int gz = ib[2] + cz >= N ? ib[2] + cz - N : ib[2] + cz;
+            atomicAdd(&grid[pidx(gx, gy, gz, N)], v);
+          }
+        }
   }
   __syncthreads();
   for (int i = threadIdx.x; i < CB_X * CB_Y * CB_Z; i += blockDim.x) {
@@ -315,6 +336,8 @@ cudaError_t cg_lpt_cic(cudaStream_t s, float *grid, const float *dx, const float
   (void)nsm;
   const long long N = p->box.N;
   const long long tiles = ((N + CT_X - 1) / CT_X) * ((N + CT_Y - 1) / CT_Y) * ((N + CT_Z - 1) / CT_Z);
-  k_lpt_cic<<<(unsigned)tiles, 256, 0, s>>>(grid, dx, dy, dz, *p);
+  if (p->interp == 0) k_lpt_deposit<0><<<(unsigned)tiles, 256, 0, s>>>(grid, dx, dy, dz, *p);
+  else if (p->interp == 2) k_lpt_deposit<2><<<(unsigned)tiles, 256, 0, s>>>(grid, dx, dy, dz, *p);
+  else k_lpt_deposit<1><<<(unsigned)tiles, 256, 0, s>>>(grid, dx, dy, dz, *p);
   return cudaGetLastError();
 }

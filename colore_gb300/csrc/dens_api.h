@@ -28,6 +28,7 @@ struct cg_lpt_params {
   cg::Box box;
   cg::Grid1 g;
   cg::Tab d1;
+  int interp; /* 0 NGP, 1 CIC, 2 TSC (pos_2_dens, density.c:178-187) */
 };
 
 cudaError_t cg_moments_final(cudaStream_t s, const double2 *part, size_t n, double inv_ncell, double *stats,

@@ -1043,6 +1043,8 @@ extern "C" const char *cg64_last_error(const cg64_ctx *c) { return c ? c->err : 
 extern "C" int cg64_run_mock(cg64_ctx *c, float *ms)
 {
   if (!c) return CG_EINVAL;
+  if (c->cfg.dens_type == CG_DENS_1LPT && c->cfg.lpt_interp_type != 1)
+    return fail(c, CG_EINVAL, "the FP64 baseline deposits 1LPT particles with CIC only");
   if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, CG_ECUDA, "cudaSetDevice");
   cudaEvent_t a, b;
   CU(c, cudaEventCreate(&a));

@@ -370,6 +370,7 @@ int cg_read_run_params(const char *fname, cg_params **out, char *err, size_t el)
   reader r = {root, err, el, 0};
   /* defaults of param_colore_new, io.c:24-158 */
   p->dens_type = CG_DENS_LGNR;
+  p->lpt_interp_type = 1; /* INTERP_CIC, io.c:66 */
   p->nside_base = 2; /* choose_nside_base with one task, io.c:224-244 */
   rd_string(&r, "global", "prefix_out", p->prefix_out, sizeof(p->prefix_out));
   rd_string(&r, "global", "pk_filename", p->pk_filename, sizeof(p->pk_filename));
@@ -480,6 +481,7 @@ int cg_params_to_config(const cg_params *p, cg_config *c)
   c->do_smoothing = p->do_smoothing;
   c->smooth_potential = p->smooth_potential;
   c->dens_type = p->dens_type;
+  c->lpt_interp_type = p->lpt_interp_type;
   c->bias_model = p->bias_model;
   c->numk = p->numk;
   c->logkmin = p->logkmin;

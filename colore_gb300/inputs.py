@@ -101,7 +101,7 @@ def write_inputs(dirname, spec, prefix="run"):
     add("  bias_model= %d;\n}\n" % spec.get("bias_model", 2))
     add("field_par:\n{\n  r_smooth= %r;\n  smooth_potential= true;\n  n_grid= %d;\n  dens_type= %d;" %
         (float(spec["r_smooth"]), spec["n_grid"], spec.get("dens_type", 0)))
-    add("  lpt_buffer_fraction= 0.6;\n  lpt_interp_type= 1;\n  output_lpt= 0;\n}\n")
+    add("  lpt_buffer_fraction= 0.6;\n  lpt_interp_type= %d;\n  output_lpt= 0;\n}\n" % spec.get("lpt_interp_type", 1))
     add("cosmo_par:\n{\n" + "".join("  %s= %r;\n" % (kk, float(v)) for kk, v in cos.items()) + "}\n")
     for i, s in enumerate(spec.get("srcs", [])):
         nz = _nz_shape(zs, s["nz"])

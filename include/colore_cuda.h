@@ -112,6 +112,9 @@ typedef struct {
   /* integrated Sachs-Wolfe maps (isw.c:78-147), planes as kappa's */
   int do_isw, n_isw, nside_isw;
   double isw_r[CG_NPLANES_MAX]; /* plane comoving distances (cosmo.c:839-845) */
+  /* mass assignment of the 1LPT particles (density.c:178-187): 0 NGP,
+   * 1 CIC (the reference's default, io.c:66), 2 TSC */
+  int lpt_interp_type;
 } cg_config;
 
 typedef struct cg_ctx cg_ctx;

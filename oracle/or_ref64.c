@@ -6,7 +6,7 @@
  *   or_fill64        create_grids_fourier          fourier.c:285-359
  *   or_field64       create_cartesian_fields       fourier.c:361-423 (+ compute_sigma_dens 24-79)
  *   or_density64     lognormalize / densclip       density.c:1034-1103
- *   or_lpt64         lpt_1 + pos_2_cic             density.c:376-644, 64-105 (literal r2c path)
+ *   or_lpt64         lpt_1 + pos_2_dens            density.c:376-644, 37-187 (literal r2c path)
  *   or_bins64        collect_density_normalization_from_grid density.c:1128-1211
  *   or_norm_tables64 compute_density_normalization density.c:1227-1355
  *   or_lambda64      Poisson mean per cell         srcs.c:156-178
@@ -174,8 +174,10 @@ int or_lpt64(const cg_config *c, const double *dg_in, double *dens_out, double *
   free(ck);
   const double dx = c->l_box / N;
   memset(dens_out, 0, ncell * sizeof(double));
-  /* positions (density.c:473-501) and CIC (density.c:64-105) */
+  /* positions (density.c:473-501) and the deposit of pos_2_dens
+   * (density.c:178-187): NGP (37-62), CIC (64-105) or TSC (107-176) */
   const double iag = N / c->l_box;
+  const int S = c->lpt_interp_type;
   for (int iz = 0; iz < N; iz++)
     for (int iy = 0; iy < N; iy++)
       for (int ix = 0; ix < N; ix++) {
@@ -183,29 +185,37 @@ int or_lpt64(const cg_config *c, const double *dg_in, double *dens_out, double *
         double r = sqrt(xv[0] * xv[0] + xv[1] * xv[1] + xv[2] * xv[2]);
         double g = BG_D1(c, r);
         size_t id = ix + (size_t)N * (iy + (size_t)N * iz);
-        int i0[3], i1[3];
-        double a0[3], a1[3];
+        int ib[3], K = S + 1;
+        double w[3][3];
         for (int ax = 0; ax < 3; ax++) {
-          double p = xv[ax] + g * disp[(size_t)ax * ncell + id] + c->pos_obs[ax];
-          if (p < 0) p += c->l_box;
-          if (p >= c->l_box) p -= c->l_box;
-          i0[ax] = (int)(p * iag);
-          a1[ax] = p * iag - i0[ax];
-          a0[ax] = 1 - a1[ax];
-          i1[ax] = i0[ax] + 1;
-          if (i0[ax] >= N) i0[ax] -= N;
-          if (i1[ax] >= N) i1[ax] -= N;
+          double q = xv[ax] + g * disp[(size_t)ax * ncell + id] + c->pos_obs[ax];
+          if (q < 0) q += c->l_box;
+          if (q >= c->l_box) q -= c->l_box;
+          double u = q * iag;
+          int i0;
+          if (S == 0) {
+            i0 = (int)(u + 0.5);
+            w[ax][0] = 1;
+          } else if (S == 1) {
+            i0 = (int)u;
+            w[ax][1] = u - i0;
+            w[ax][0] = 1 - w[ax][1];
+          } else {
+            i0 = (int)floor(u + 0.5);
+            double a0 = u - i0;
+            w[ax][0] = 0.5 * (0.5 - a0) * (0.5 - a0);
+            w[ax][1] = 0.75 - a0 * a0;
+            w[ax][2] = 0.5 * (0.5 + a0) * (0.5 + a0);
+            i0 -= 1;
+          }
+          ib[ax] = ((i0 % N) + N) % N;
         }
-#define D(X, Y, Z) dens_out[(X) + (size_t)N * ((Y) + (size_t)N * (Z))]
-        D(i0[0], i0[1], i0[2]) += a0[0] * a0[1] * a0[2];
-        D(i1[0], i0[1], i0[2]) += a1[0] * a0[1] * a0[2];
-        D(i0[0], i1[1], i0[2]) += a0[0] * a1[1] * a0[2];
-        D(i1[0], i1[1], i0[2]) += a1[0] * a1[1] * a0[2];
-        D(i0[0], i0[1], i1[2]) += a0[0] * a0[1] * a1[2];
-        D(i1[0], i0[1], i1[2]) += a1[0] * a0[1] * a1[2];
-        D(i0[0], i1[1], i1[2]) += a0[0] * a1[1] * a1[2];
-        D(i1[0], i1[1], i1[2]) += a1[0] * a1[1] * a1[2];
-#undef D
+        for (int cz = 0; cz < K; cz++)
+          for (int cy = 0; cy < K; cy++)
+            for (int cx = 0; cx < K; cx++) {
+              int gx = (ib[0] + cx) % N, gy = (ib[1] + cy) % N, gz = (ib[2] + cz) % N;
+              dens_out[gx + (size_t)N * (gy + (size_t)N * gz)] += w[0][cx] * w[1][cy] * w[2][cz];
+            }
       }
   for (size_t i = 0; i < ncell; i++) dens_out[i] -= 1; /* density.c:621 */
   return 0;

@@ -46,3 +46,24 @@ def test_oracle_field_power_spectrum(built, tmp_path):
     model = np.interp(np.log10(kk[sel]), lk, pk) * np.exp(-cfg.r2_smooth * kk[sel] ** 2) / kf ** 3
     ratio = np.abs(dk[sel]) ** 2 / model
     assert abs(ratio.mean() - 1) < 0.02
+
+
+@pytest.mark.parametrize("scheme", [0, 1, 2])
+def test_oracle_lpt_deposits_conserve_mass(built, tmp_path, scheme):
+    """pos_2_ngp / pos_2_cic / pos_2_tsc (density.c:37-176): the weights of
+    each particle sum to one, so the mean of 1 + delta is exactly 1; NGP puts
+    whole particles in cells."""
+    import oracle as orc
+    import colore_gb300 as cg
+    from colore_gb300 import inputs
+    spec = inputs.scaled("c1", 32)
+    spec.update(dens_type=1, lpt_interp_type=scheme)
+    prm = cg.Params(inputs.write_inputs(str(tmp_path), spec))
+    c = prm.config
+    assert c.lpt_interp_type == scheme
+    d, _, _ = orc.field64(c)
+    out, disp = orc.lpt64(c, d)
+    assert abs(np.mean(out + 1) - 1) < 1e-12
+    assert np.all(out >= -1 - 1e-12)
+    if scheme == 0:
+        assert np.allclose(out + 1, np.round(out + 1), atol=1e-12)
