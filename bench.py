@@ -271,11 +271,7 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (EH98 no-wiggle P(k), analytic N(z)/b(z)/T(z); random seeds per rank)",
-        "config": {"workload": "%s: %d^3, dens_type %d, %d source pops, %d imap shells nside %s, %d kappa planes"
-                               % (args.config, n, cfg.dens_type, cfg.n_srcs,
-                                  sum(cfg.imap_nr[i] for i in range(cfg.n_imap)),
-                                  [cfg.nside_imap[i] for i in range(cfg.n_imap)], cfg.n_kappa if cfg.do_kappa else 0),
-                   "n_grid": n, "l2": "inputs larger than L2 (4.3 GB per field)", "parallelism": "replicas"},
+        "config": workload_config(args, cfg),
         "e2e": {"value": world * ncell / t_e2e, "unit": "cells/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": t_e2e * 1e3,
                 "download_ms_per_step": t_dl * 1e3, "d2h_GB/s": d2h / max(t_dl, 1e-9) / 1e9,
@@ -385,10 +381,23 @@ def cpu_baseline(args, quick=False):
             "stage_s_sample": {k: round(v, 4) for k, v in T.items()}}
 
 
+def workload_config(args, cfg):
+    """The `config` object of both arms: the workload and its sizes."""
+    n = cfg.n_grid
+    gb = (n * n * 2 * (n // 2 + 1) * 4) / 1e9
+    return {"workload": "%s: %d^3, dens_type %d, %d source pops, %d imap shells nside %s, %d kappa planes"
+                        % (args.config, n, cfg.dens_type, cfg.n_srcs, sum(cfg.imap_nr[i] for i in range(cfg.n_imap)),
+                           [cfg.nside_imap[i] for i in range(cfg.n_imap)], cfg.n_kappa if cfg.do_kappa else 0),
+            "n_grid": n, "l2": "inputs larger than L2 (%.1f GB per field)" % gb, "parallelism": "replicas"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    import colore_gb300 as cg
+    from colore_gb300 import inputs
+    prm = cg.Params(inputs.write_inputs(tempfile.mkdtemp(prefix="colore_ref_"), config_spec(args.config, args.n)))
     vals = []
     for _ in range(args.warmup):
         pass
@@ -400,7 +409,7 @@ def run_reference(args):
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "cells/s", "n_gpus": 0,
            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": "%s (sampled at %d^3 on the host)" % (args.config, args.cpu_n)},
+           "config": workload_config(args, prm.config),
            "cpu_baseline": dict(cb, value=v),
            "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))

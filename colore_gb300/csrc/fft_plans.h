@@ -29,8 +29,8 @@ CG_PLAN(128, 16, 16, 8, 1, 8, 8, 8, 2, 32, 16, 32, 8, 8, 8, 1, 16)
 CG_PLAN(192, 24, 24, 8, 1, 12, 12, 4, 4, 16, 16, 32, 24, 24, 4, 1, 16)
 CG_PLAN(256, 16, 16, 16, 1, 16, 16, 16, 1, 16, 16, 32, 16, 16, 8, 1, 16)
 CG_PLAN(384, 24, 24, 4, 4, 24, 24, 4, 4, 16, 8, 16, 24, 24, 8, 1, 16)
-CG_PLAN(512, 32, 32, 16, 1, 16, 16, 16, 2, 4, 4, 8, 16, 16, 16, 1, 8)
-CG_PLAN(1024, 32, 32, 32, 1, 16, 16, 16, 4, 2, 2, 8, 32, 32, 16, 1, 8)
+CG_PLAN(512, 32, 32, 16, 1, 16, 16, 16, 2, 8, 8, 8, 16, 16, 16, 1, 8)
+CG_PLAN(1024, 32, 32, 32, 1, 16, 16, 16, 4, 4, 4, 8, 32, 32, 16, 1, 8)
 CG_PLAN(2048, 32, 32, 32, 2, 16, 16, 16, 8, 4, 2, 8, 32, 32, 32, 1, 4)
 #undef CG_PLAN
 
