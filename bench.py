@@ -107,6 +107,27 @@ ALGO_BYTES_PER_CELL = {"field_fft": 40.0, "lpt_fft": 60.0, "dens_bins": 8.0, "sr
 MEASURED_DRAM_BYTES_PER_CELL = {"field_fft": 38.5, "lpt_fft": 59.8, "dens_bins": 7.6}
 
 
+# ---- replicas: one realisation per rank, no exchange on the data path ----
+def rank_seed(seed, rank):
+    """Each rank runs its own realisation."""
+    return seed + rank
+
+
+def max_over_ranks(times, dist, device):
+    """The slowest rank bounds the job: max of each timing over the ranks."""
+    if dist is None:
+        return [float(t) for t in times]
+    import torch
+    tt = torch.tensor([float(t) for t in times], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return tt.tolist()
+
+
+def job_cells_per_s(ncell, world, t_step):
+    """Whole-job throughput: the cells of all ranks over the slowest rank's time."""
+    return world * ncell / t_step
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -123,7 +144,7 @@ def run_ours(args):
         dist = None
     torch.cuda.set_device(local)
     spec = config_spec(args.config, args.n)
-    spec["seed"] = spec["seed"] + rank
+    spec["seed"] = rank_seed(spec["seed"], rank)
     d = tempfile.mkdtemp(prefix="colore_bench_%d_" % rank)
     from colore_gb300 import inputs
     prm = cg.Params(inputs.write_inputs(d, spec))
@@ -226,9 +247,7 @@ def run_ours(args):
     h2d = 8 * (9 * na + 2 * na * (cfg.n_srcs + cfg.n_imap) + cfg.numk) // 2  # tables as float
     t_step = ms / 1e3 / args.steps
     if dist:
-        tt = torch.tensor([t_step, t_e2e], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step, t_e2e = tt.tolist()
+        t_step, t_e2e = max_over_ranks([t_step, t_e2e], dist, "cuda")
     hbm, peak_kind = peaks()
     # roofline of the dominant HBM-bound group
     rl = None
@@ -267,12 +286,12 @@ def run_ours(args):
     if rank != 0:
         return
     out = {
-        "metric": METRIC, "value": world * ncell / t_step, "unit": "cells/s", "n_gpus": world,
+        "metric": METRIC, "value": job_cells_per_s(ncell, world, t_step), "unit": "cells/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (EH98 no-wiggle P(k), analytic N(z)/b(z)/T(z); random seeds per rank)",
         "config": workload_config(args, cfg),
-        "e2e": {"value": world * ncell / t_e2e, "unit": "cells/s", "h2d_bytes_per_step": int(h2d),
+        "e2e": {"value": job_cells_per_s(ncell, world, t_e2e), "unit": "cells/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": t_e2e * 1e3,
                 "download_ms_per_step": t_dl * 1e3, "d2h_GB/s": d2h / max(t_dl, 1e-9) / 1e9,
                 "download_split_ms": {k: round(v * 1e3, 2) for k, v in split.items()}},
