@@ -56,6 +56,10 @@ class Config(C.Structure):
         ("do_isw", C.c_int), ("n_isw", C.c_int), ("nside_isw", C.c_int),
         ("isw_r", C.c_double * NPLANES_MAX),
         ("lpt_interp_type", C.c_int),
+        ("n_cstm", C.c_int),
+        ("cstm_kz_arr", _dp * NPOP_MAX),
+        ("cstm_bz_arr", _dp * NPOP_MAX),
+        ("nside_cstm", C.c_int * NPOP_MAX),
     ]
 
 
@@ -100,6 +104,7 @@ def lib():
             "cg_download_imap": (C.c_int, [vp, C.c_int, vp, vp]),
             "cg_download_kappa": (C.c_int, [vp, vp]),
             "cg_download_isw": (C.c_int, [vp, vp]),
+            "cg_download_custom": (C.c_int, [vp, C.c_int, vp]),
             "cg_download_norm": (C.c_int, [vp, C.c_int, C.c_int, vp, vp]),
             "cg_kernel_launches": (C.c_longlong, [vp]),
             "cg_set_profiling": (C.c_int, [vp, C.c_int]),
@@ -134,7 +139,7 @@ def exported_symbols():
             "cg_collect_density_normalization", "cg_collect_density_normalization_static", "cg_set_norm_tables", "cg_srcs_set_cartesian",
             "cg_imap_set_cartesian", "cg_imap_samples", "cg_get_beam_properties", "cg_run_mock", "cg_download_grid",
             "cg_num_sources", "cg_download_catalog", "cg_download_count_map", "cg_download_imap",
-            "cg_download_kappa", "cg_download_isw", "cg_download_norm", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_read_run_params",
+            "cg_download_kappa", "cg_download_isw", "cg_download_custom", "cg_download_norm", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_read_run_params",
             "cg_params_free", "cg_params_to_config", "cg_write_healpix_map", "cg_write_catalog",
             "cg_write_density_grid", "cg64_create", "cg64_destroy", "cg64_last_error",
             "cg64_run_mock", "cg64_num_sources", "cg64_download"]
@@ -333,6 +338,14 @@ class Mock:
         ns = self.cfg.nside_isw
         m = out if out is not None else np.empty((self.cfg.n_isw, 12 * ns * ns), np.float32)
         self._chk(lib().cg_download_isw(self._c, m.ctypes.data), "download_isw")
+        return m
+
+    def custom(self, ipop, out=None):
+        """Custom map ipop, 12 nside_cstm^2 values in NEST order (the order the
+        reference's custom-map writer stores)."""
+        ns = self.cfg.nside_cstm[ipop]
+        m = out if out is not None else np.empty(12 * ns * ns, np.float32)
+        self._chk(lib().cg_download_custom(self._c, ipop, m.ctypes.data), "download_custom")
         return m
 
     def kappa(self, out=None):

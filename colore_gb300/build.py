@@ -32,7 +32,7 @@ def nvcc():
     return "nvcc"
 
 
-NVFLAGS = ["-std=c++17", "-O3", ARCH, "-lineinfo", "-Xcompiler", "-fPIC", "-diag-suppress", "177",
+NVFLAGS = ["-std=c++17", "-O3", ARCH, "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-diag-suppress", "177",
            "-I" + CSRC, "-I" + os.path.join(ROOT, "include")]
 CFLAGS = ["-O2", "-fPIC", "-std=gnu11", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
           "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]

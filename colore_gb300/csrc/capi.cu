@@ -73,7 +73,8 @@ struct cg_ctx {
   const float *a_a2r = nullptr, *r_a2r = nullptr;
   Tab nz[CG_NPOP_MAX], bz[CG_NPOP_MAX], norm[CG_NPOP_MAX];
   Tab tz[CG_NPOP_MAX], bzi[CG_NPOP_MAX], normi[CG_NPOP_MAX];
-  float *d_norm = nullptr; /* (n_srcs + n_imap) * NA */
+  Tab kzc[CG_NPOP_MAX], bzc[CG_NPOP_MAX], normc[CG_NPOP_MAX]; /* custom maps */
+  float *d_norm = nullptr; /* (n_srcs + n_imap + n_cstm) * NA */
   float *d_pk = nullptr;
   float2 *d_twN = nullptr, *d_twH = nullptr;
   Box box;
@@ -107,6 +108,11 @@ struct cg_ctx {
   float *d_kmap = nullptr, *d_kfac = nullptr, *d_kinv = nullptr;
   /* ISW */
   float *d_imap_isw = nullptr, *d_ifac = nullptr;
+  /* custom maps: host copies of K(z) and b(z), device maps and step tables */
+  std::vector<double> h_kzc[CG_NPOP_MAX], h_bzc[CG_NPOP_MAX];
+  float *d_cmap[CG_NPOP_MAX] = {nullptr}, *d_cfac = nullptr;
+  long long cnpix[CG_NPOP_MAX] = {0};
+  int cnr = 0;
   int *d_iir = nullptr;
   int ipl = 0, inr = 0;
   long long inpix = 0;
@@ -276,6 +282,11 @@ static int validate(const cg_config *cfg, char *msg, size_t len)
     return snprintf(msg, len, "kappa planes or nside out of range"), CG_EINVAL;
   if (cfg->do_isw && (cfg->n_isw < 1 || cfg->n_isw > CG_NPLANES_MAX || cfg->nside_isw < 1))
     return snprintf(msg, len, "ISW planes or nside out of range"), CG_EINVAL;
+  if (cfg->n_cstm < 0 || cfg->n_cstm > CG_NPOP_MAX)
+    return snprintf(msg, len, "custom-map count out of range"), CG_EINVAL;
+  for (int i = 0; i < cfg->n_cstm; i++)
+    if (!cfg->cstm_kz_arr[i] || !cfg->cstm_bz_arr[i] || cfg->nside_cstm[i] < 1)
+      return snprintf(msg, len, "custom-map table missing or nside < 1"), CG_EINVAL;
   if (cfg->dens_type == CG_DENS_1LPT && (cfg->lpt_interp_type < 0 || cfg->lpt_interp_type > 2))
     return snprintf(msg, len, "lpt_interp_type %d: 0 (NGP), 1 (CIC) or 2 (TSC)", cfg->lpt_interp_type), CG_EINVAL;
   if (cfg->dens_type != CG_DENS_LGNR && cfg->dens_type != CG_DENS_1LPT && cfg->dens_type != CG_DENS_CLIP)
@@ -311,8 +322,12 @@ extern "C" int cg_upload_tables(cg_ctx *c, const cg_config *cfg)
   cp(c->h_pd, cfg->growth_pd_arr);
   cp(c->h_a, cfg->a_arr_a2r);
   cp(c->h_ra, cfg->r_arr_a2r);
-  /* packed float tables: 9 background + 2 per population + 2 per species */
-  const int ntab = 9 + 2 * cfg->n_srcs + 2 * cfg->n_imap;
+  for (int p = 0; p < cfg->n_cstm; p++) {
+    cp(c->h_kzc[p], cfg->cstm_kz_arr[p]);
+    cp(c->h_bzc[p], cfg->cstm_bz_arr[p]);
+  }
+  /* packed float tables: 9 background + 2 per population, species and custom map */
+  const int ntab = 9 + 2 * cfg->n_srcs + 2 * cfg->n_imap + 2 * cfg->n_cstm;
   std::vector<float> h((size_t)ntab * na);
   const double *srcs[9] = {cfg->r_arr_r2z, cfg->z_arr_r2z, cfg->growth_d_arr, cfg->growth_d2_arr, cfg->growth_v_arr,
                            cfg->growth_pd_arr, cfg->ihub_arr, cfg->a_arr_a2r, cfg->r_arr_a2r};
@@ -329,6 +344,12 @@ extern "C" int cg_upload_tables(cg_ctx *c, const cg_config *cfg)
     for (int i = 0; i < na; i++) h[(size_t)k * na + i] = (float)cfg->imap_tz_arr[p][i];
     k++;
     for (int i = 0; i < na; i++) h[(size_t)k * na + i] = (float)cfg->imap_bz_arr[p][i];
+    k++;
+  }
+  for (int p = 0; p < cfg->n_cstm; p++) {
+    for (int i = 0; i < na; i++) h[(size_t)k * na + i] = (float)cfg->cstm_kz_arr[p][i];
+    k++;
+    for (int i = 0; i < na; i++) h[(size_t)k * na + i] = (float)cfg->cstm_bz_arr[p][i];
     k++;
   }
   if (int rc = dalloc(c, &c->d_tabs, h.size())) return rc;
@@ -359,8 +380,13 @@ extern "C" int cg_upload_tables(cg_ctx *c, const cg_config *cfg)
     c->bzi[p] = Tab{tab(k + 1), (float)cfg->imap_bz_arr[p][0], 1.0f};    /* cosmo.c:68-69 */
     k += 2;
   }
+  for (int p = 0; p < cfg->n_cstm; p++) {
+    c->kzc[p] = Tab{tab(k), 0.0f, 0.0f};                                 /* cosmo.c:74-75 */
+    c->bzc[p] = Tab{tab(k + 1), (float)cfg->cstm_bz_arr[p][0], 1.0f};    /* cosmo.c:76-77 */
+    k += 2;
+  }
   /* normalisation tables start at 1 until compute_density_normalization */
-  const int nnorm = cfg->n_srcs + cfg->n_imap;
+  const int nnorm = cfg->n_srcs + cfg->n_imap + cfg->n_cstm;
   if (nnorm > 0) {
     std::vector<float> ones((size_t)nnorm * na, 1.0f);
     if (int rc = dalloc(c, &c->d_norm, ones.size())) return rc;
@@ -368,6 +394,8 @@ extern "C" int cg_upload_tables(cg_ctx *c, const cg_config *cfg)
                                 c->stream));
     for (int p = 0; p < cfg->n_srcs; p++) c->norm[p] = Tab{c->d_norm + (size_t)p * na, 1.0f, 1.0f};
     for (int p = 0; p < cfg->n_imap; p++) c->normi[p] = Tab{c->d_norm + (size_t)(cfg->n_srcs + p) * na, 1.0f, 1.0f};
+    for (int p = 0; p < cfg->n_cstm; p++)
+      c->normc[p] = Tab{c->d_norm + (size_t)(cfg->n_srcs + cfg->n_imap + p) * na, 1.0f, 1.0f};
   }
   /* P(k) */
   std::vector<float> pk(cfg->numk);
@@ -428,6 +456,7 @@ extern "C" int cg_memory_estimate(const cg_config *cfg, unsigned long long *byte
     b += (unsigned long long)cfg->imap_nr[i] * 12ull * cfg->nside_imap[i] * cfg->nside_imap[i] * 8ull;
   if (cfg->do_kappa) b += (unsigned long long)cfg->n_kappa * 12ull * cfg->nside_kappa * cfg->nside_kappa * 4ull;
   if (cfg->do_isw) b += (unsigned long long)cfg->n_isw * 12ull * cfg->nside_isw * cfg->nside_isw * 4ull;
+  for (int i = 0; i < cfg->n_cstm; i++) b += 12ull * cfg->nside_cstm[i] * cfg->nside_cstm[i] * 4ull;
   *bytes = b;
   return CG_OK;
 }
@@ -442,12 +471,12 @@ extern "C" void cg_destroy(cg_ctx *c)
                   c->d_zsum, c->d_bsum, c->d_counts, c->d_bsums, c->d_total, c->d_tmpmap, c->d_kmap,
                   c->d_kfac, c->d_kinv, c->d_kir, c->d_ovf_cell, c->d_ovf_cnt, c->d_ovf_n,
                   c->d_cells, c->d_cell_n, c->d_cell_off, c->d_scan_tmp, c->d_imap_ctr,
-                  c->d_imap_isw, c->d_ifac, c->d_iir};
+                  c->d_imap_isw, c->d_ifac, c->d_iir, c->d_cfac};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < CG_NPOP_MAX; i++) {
     void *q[] = {c->cat[i].pos, c->cat[i].ipix, c->cat[i].src, c->cat[i].cmap, c->im[i].r0, c->im[i].rf,
-                 c->im[i].shp, c->im[i].data, c->im[i].nadd};
+                 c->im[i].shp, c->im[i].data, c->im[i].nadd, c->d_cmap[i]};
     for (void *p : q)
       if (p) cudaFree(p);
   }
@@ -601,11 +630,21 @@ extern "C" int cg_compute_physical_density_field(cg_ctx *c)
   return CG_OK;
 }
 
+/* Tracers of the normalisation: source populations, then intensity species,
+ * then custom maps (collect_density_normalization_from_grid, density.c:1128-1211). */
+static int n_imap_block(const cg_ctx *c) { return c->cfg.n_imap + c->cfg.n_cstm; }
+
+static Tab tracer_bias(const cg_ctx *c, int t)
+{
+  const int nts = c->cfg.n_srcs, nti = c->cfg.n_imap;
+  return t < nts ? c->bz[t] : (t < nts + nti ? c->bzi[t - nts] : c->bzc[t - nts - nti]);
+}
+
 /* Launch the bins pass over all tracers (one launch carries up to the
  * kernel's maximum number of bias tables). */
 static int run_bins(cg_ctx *c, int nz, double idz)
 {
-  const int nts = c->cfg.n_srcs, nti = c->cfg.n_imap, nt = nts + nti;
+  const int nts = c->cfg.n_srcs, nti = n_imap_block(c), nt = nts + nti;
   const int MT = cg_dens_bins_max_tracers();
   if (nt > MT) return fail(c, CG_EINVAL, "%d tracers: at most %d per run are supported", nt, MT);
   int rc;
@@ -627,7 +666,7 @@ static int run_bins(cg_ctx *c, int nz, double idz)
   p.idz = (float)idz;
   p.bias_model = c->cfg.bias_model;
   p.nt = nt;
-  for (int t = 0; t < nt; t++) p.bz[t] = t < nts ? c->bz[t] : c->bzi[t - nts];
+  for (int t = 0; t < nt; t++) p.bz[t] = tracer_bias(c, t);
   p.ncount = c->d_ncount;
   p.zsum = c->d_zsum;
   p.bsum = c->d_bsum;
@@ -648,7 +687,7 @@ extern "C" int cg_collect_density_normalization(cg_ctx *c, int nz, double idz, d
   if (nz < 2 || nz > 4096) return fail(c, CG_EINVAL, "nz=%d out of range", nz);
   cudaSetDevice(c->device);
   if (int rc = run_bins(c, nz, idz)) return rc;
-  const int nts = c->cfg.n_srcs, nti = c->cfg.n_imap;
+  const int nts = c->cfg.n_srcs, nti = n_imap_block(c);
   std::vector<double> b((size_t)(nts + nti) * nz);
   std::vector<unsigned long long> n(nz);
   std::vector<double> z(nz);
@@ -700,7 +739,7 @@ extern "C" int cg_collect_density_normalization_static(cg_ctx *c, int nz, double
   if (!c->have_density) return fail(c, CG_ESTATE, "compute_physical_density_field first");
   if (nz < 2 || nz > CG_BINS_STATIC_NZ)
     return fail(c, CG_EINVAL, "nz=%d: the static bins scratch holds 2 to %d bins", nz, CG_BINS_STATIC_NZ);
-  const int nts = c->cfg.n_srcs, nti = c->cfg.n_imap, nt = nts + nti;
+  const int nts = c->cfg.n_srcs, nti = n_imap_block(c), nt = nts + nti;
   if (nt > cg_dens_bins_max_tracers())
     return fail(c, CG_EINVAL, "%d tracers: at most %d per run are supported", nt, cg_dens_bins_max_tracers());
   CUDA_TRY(c, cudaSetDevice(c->device));
@@ -725,7 +764,7 @@ extern "C" int cg_collect_density_normalization_static(cg_ctx *c, int nz, double
   p.idz = (float)idz;
   p.bias_model = c->cfg.bias_model;
   p.nt = nt;
-  for (int t = 0; t < nt; t++) p.bz[t] = t < nts ? c->bz[t] : c->bzi[t - nts];
+  for (int t = 0; t < nt; t++) p.bz[t] = tracer_bias(c, t);
   p.ncount = ncount;
   p.zsum = zsum;
   p.bsum = bsum;
@@ -749,7 +788,7 @@ extern "C" int cg_set_norm_tables(cg_ctx *c, const double *srcs_norm, const doub
                                   const double *imap_norm, const double *imap_norm_0f)
 {
   if (!c) return CG_EINVAL;
-  const int na = CG_NA, nts = c->cfg.n_srcs, nti = c->cfg.n_imap;
+  const int na = CG_NA, nts = c->cfg.n_srcs, nti = n_imap_block(c), nsp = c->cfg.n_imap;
   if (nts + nti == 0) return CG_OK;
   std::vector<float> h((size_t)(nts + nti) * na);
   for (int p = 0; p < nts; p++)
@@ -760,8 +799,11 @@ extern "C" int cg_set_norm_tables(cg_ctx *c, const double *srcs_norm, const doub
   CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* h is a local buffer */
   for (int p = 0; p < nts; p++)
     c->norm[p] = Tab{c->d_norm + (size_t)p * na, (float)srcs_norm_0f[2 * p], (float)srcs_norm_0f[2 * p + 1]};
-  for (int p = 0; p < nti; p++)
-    c->normi[p] = Tab{c->d_norm + (size_t)(nts + p) * na, (float)imap_norm_0f[2 * p], (float)imap_norm_0f[2 * p + 1]};
+  for (int p = 0; p < nti; p++) {
+    const Tab t = Tab{c->d_norm + (size_t)(nts + p) * na, (float)imap_norm_0f[2 * p], (float)imap_norm_0f[2 * p + 1]};
+    if (p < nsp) c->normi[p] = t;
+    else c->normc[p - nsp] = t;
+  }
   c->have_norm = 1;
   return CG_OK;
 }
@@ -781,7 +823,7 @@ static double lin_interp(const std::vector<double> &x, const std::vector<double>
 extern "C" int cg_compute_density_normalization(cg_ctx *c)
 {
   if (!c) return CG_EINVAL;
-  const int nts = c->cfg.n_srcs, nti = c->cfg.n_imap, nt = nts + nti;
+  const int nts = c->cfg.n_srcs, nti = n_imap_block(c), nt = nts + nti;
   /* density.c:1233-1245 */
   const double zmax = host_bg(c, c->h_z, 0, c->h_z[CG_NA - 1], c->cfg.l_box * 0.5);
   const int nz = (int)(zmax / 0.05) + 2;
@@ -1172,6 +1214,77 @@ static int isw_run(cg_ctx *c)
   return CG_OK;
 }
 
+/* cstm_beams_preproc + cstm_get_beam_properties (cstm.c:39-145): the step
+ * tables kz = K(r)/IH(r) and bz on the N/2 radial step centres from the
+ * FP64 tables, the integration range where |kz| > 1e-4 max|kz|, then one ray
+ * per pixel (the kernel evaluates the FP32 normalisation table itself, as
+ * every other tracer kernel does). */
+static int cstm_run(cg_ctx *c)
+{
+  if (!c->have_norm) return fail(c, CG_ESTATE, "custom maps need the density normalisation");
+  const int nr = c->N / 2, nc = c->cfg.n_cstm; /* get_radial_params with NSAMP_RAD = 1 */
+  const double dr = c->cfg.r_max / nr;
+  int rc;
+  if (c->cnr != nr)
+    if ((rc = dalloc(c, &c->d_cfac, 2 * (size_t)nr * CG_NPOP_MAX))) return rc;
+  c->cnr = nr;
+  std::vector<float> tab(2 * (size_t)nr * nc);
+  std::vector<int> irange(2 * nc);
+  for (int p = 0; p < nc; p++) {
+    float *kz = tab.data() + 2 * (size_t)nr * p, *bz = kz + nr;
+    double kmax = -1e100;
+    std::vector<double> kzd(nr);
+    for (int i = 0; i < nr; i++) {
+      const double rm = (i + 0.5) * dr;
+      kzd[i] = host_bg(c, c->h_kzc[p], 0, 0, rm) / host_bg(c, c->h_ih, c->h_ih[0], c->h_ih[CG_NA - 1], rm);
+      kz[i] = (float)kzd[i];
+      bz[i] = (float)host_bg(c, c->h_bzc[p], c->h_bzc[p][0], 1, rm);
+      kmax = std::max(kmax, fabs(kzd[i]));
+    }
+    int lo = 0, hi = nr - 1;
+    for (int i = 0; i < nr; i++)
+      if (fabs(kzd[i]) > 1e-4 * kmax) {
+        lo = i;
+        break;
+      }
+    for (int i = nr - 1; i >= 0; i--)
+      if (fabs(kzd[i]) > 1e-4 * kmax) {
+        hi = i;
+        break;
+      }
+    if (hi < lo) return fail(c, CG_EINVAL, "Custom kernel %d has no support", p);
+    irange[2 * p] = lo;
+    irange[2 * p + 1] = hi;
+    const long long npix = 12LL * c->cfg.nside_cstm[p] * c->cfg.nside_cstm[p];
+    if (c->cnpix[p] != npix) {
+      if ((rc = dalloc(c, &c->d_cmap[p], (size_t)npix))) return rc;
+      c->cnpix[p] = npix;
+    }
+  }
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_cfac, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  for (int p = 0; p < nc; p++) {
+    cg_cstm_params q;
+    memset(&q, 0, sizeof(q));
+    q.box = c->box;
+    q.g = c->g;
+    q.norm = c->normc[p];
+    q.nside = c->cfg.nside_cstm[p];
+    q.npix = c->cnpix[p];
+    q.ir_min = irange[2 * p];
+    q.ir_max = irange[2 * p + 1];
+    q.bias_model = c->cfg.bias_model;
+    q.dr = (float)dr;
+    q.kz = c->d_cfac + 2 * (size_t)nr * p;
+    q.bz = q.kz + nr;
+    q.map = c->d_cmap[p];
+    ProfScope ps(c, "cstm");
+    CUDA_TRY(c, cg_cstm_integrate(c->stream, c->d_dens, &q));
+    c->launches++;
+  }
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host staging vector */
+  return CG_OK;
+}
+
 extern "C" int cg_get_beam_properties(cg_ctx *c)
 {
   if (!c) return CG_EINVAL;
@@ -1182,6 +1295,8 @@ extern "C" int cg_get_beam_properties(cg_ctx *c)
     if (int rc = kappa_run(c)) return rc;
   if (c->cfg.do_isw)
     if (int rc = isw_run(c)) return rc;
+  if (c->cfg.n_cstm > 0)
+    if (int rc = cstm_run(c)) return rc;
   if (c->cfg.n_srcs > 0) {
     if (!c->have_srcs) return fail(c, CG_ESTATE, "srcs_set_cartesian first");
     for (int ip = 0; ip < c->cfg.n_srcs; ip++) {
@@ -1300,6 +1415,16 @@ extern "C" int cg_download_imap(cg_ctx *c, int ipop, float *map, int *nadd)
   return check_device_errors(c);
 }
 
+extern "C" int cg_download_custom(cg_ctx *c, int ipop, float *map)
+{
+  if (!c || !map || ipop < 0 || ipop >= c->cfg.n_cstm) return CG_EINVAL;
+  if (!c->d_cmap[ipop]) return fail(c, CG_ESTATE, "custom map %d not computed", ipop);
+  CUDA_TRY(c, cudaMemcpyAsync(map, c->d_cmap[ipop], (size_t)c->cnpix[ipop] * sizeof(float), cudaMemcpyDeviceToHost,
+                              c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return check_device_errors(c);
+}
+
 extern "C" int cg_download_isw(cg_ctx *c, float *map)
 {
   if (!c || !map) return CG_EINVAL;
@@ -1326,6 +1451,7 @@ extern "C" int cg_download_norm(cg_ctx *c, int kind, int ipop, float *tab, float
   const Tab *t = nullptr;
   if (kind == 0 && ipop >= 0 && ipop < c->cfg.n_srcs) t = &c->norm[ipop];
   if (kind == 1 && ipop >= 0 && ipop < c->cfg.n_imap) t = &c->normi[ipop];
+  if (kind == 2 && ipop >= 0 && ipop < c->cfg.n_cstm) t = &c->normc[ipop];
   if (!t || !t->f) return fail(c, CG_EINVAL, "no normalisation table %d/%d", kind, ipop);
   CUDA_TRY(c, cudaMemcpyAsync(tab, t->f, CG_NA * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));

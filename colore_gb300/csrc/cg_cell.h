@@ -472,6 +472,43 @@ CG_HD int cg_imap_sample(float x, float y, float z, float yz2, float drr, const 
   return ir;
 }
 
+/* CIC cell and weights along a ray, interpolate_from_grid trilinear branch
+ * (beaming.c:183-204): x = (rm u + po) idx, i0 = (int)x, h0 = x - i0. */
+CG_HD void cg_cic_axis(float rm, float u, float po, float idx, int N, int *i0, int *i1, float *h0, float *h1)
+{
+  const float x = CG_MUL(CG_ADD(CG_MUL(rm, u), po), idx);
+  int a = (int)x;
+  *h0 = CG_SUB(x, (float)a);
+  *h1 = CG_SUB(1.0f, *h0);
+  int b = a + 1;
+  a = a >= N ? a - N : (a < 0 ? a + N : a);
+  b = b >= N ? b - N : (b < 0 ? b + N : b);
+  *i0 = a;
+  *i1 = b;
+}
+
+/* Trilinear density from the padded grid (row stride 2(N/2+1)): the four
+ * terms of the i0[2] plane, then the four of the i1[2] plane, in the order of
+ * interpolate_from_grid (beaming.c:205-262), chained with FMAs. */
+CG_HD float cg_cic_value(const float *g, const int i0[3], const int i1[3], const float h0[3], const float h1[3], int N)
+{
+  const long long ngx = 2 * (N / 2 + 1);
+  const float *pa = g + (long long)i0[2] * ngx * N, *pb = g + (long long)i1[2] * ngx * N;
+  const long long ya = (long long)i0[1] * ngx, yb = (long long)i1[1] * ngx;
+  const float wa = h1[2], wb = h0[2];
+  const float w00 = CG_MUL(h1[1], h1[0]), w01 = CG_MUL(h1[1], h0[0]);
+  const float w10 = CG_MUL(h0[1], h1[0]), w11 = CG_MUL(h0[1], h0[0]);
+  float d = CG_MUL(pa[ya + i0[0]], CG_MUL(wa, w00));
+  d = CG_FMA(pa[ya + i1[0]], CG_MUL(wa, w01), d);
+  d = CG_FMA(pa[yb + i0[0]], CG_MUL(wa, w10), d);
+  d = CG_FMA(pa[yb + i1[0]], CG_MUL(wa, w11), d);
+  d = CG_FMA(pb[ya + i0[0]], CG_MUL(wb, w00), d);
+  d = CG_FMA(pb[ya + i1[0]], CG_MUL(wb, w01), d);
+  d = CG_FMA(pb[yb + i0[0]], CG_MUL(wb, w10), d);
+  d = CG_FMA(pb[yb + i1[0]], CG_MUL(wb, w11), d);
+  return d;
+}
+
 /* NGP cell along a ray, interpolate_from_grid NGP branch (beaming.c:148-157) */
 CG_HD int cg_ngp_cell(float rm, float u, float po, float idx, int N)
 {

@@ -189,6 +189,17 @@ int main(int argc, char **argv)
     }
     free(m);
   }
+  /* write_cstm (io.c:754-800): one map per custom kernel, NEST order */
+  if (p->n_cstm > 0) printf("*** Writing custom maps\n");
+  for (int ip = 0; ip < p->n_cstm; ip++) {
+    long npix = 12L * p->nside_cstm[ip] * p->nside_cstm[ip];
+    float *m = malloc(npix * sizeof(float));
+    if (!m) die(c, CG_ENOMEM, "custom map buffer");
+    if ((rc = cg_download_custom(c, ip, m))) die(c, rc, "download_custom");
+    snprintf(out, sizeof(out), "%s_custom_s%d.fits", p->prefix_out, ip + 1);
+    write_map(c, out, m, p->nside_cstm[ip]);
+    free(m);
+  }
   printf("\n|-------------------------------------------------|\n\n");
   cg_destroy(c);
   cg_params_free(p);

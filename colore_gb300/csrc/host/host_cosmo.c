@@ -346,7 +346,8 @@ int cg_host_cosmo_set(cg_params *p, char *err, size_t el)
   p->l_box = 2 * p->r_max * (1 + 2. / p->n_grid);
   p->pos_obs[0] = p->pos_obs[1] = p->pos_obs[2] = 0.5 * p->l_box;
   int rc;
-  cg_spline snz[CG_NPOP_MAX], sbz[CG_NPOP_MAX], stz[CG_NPOP_MAX], sbi[CG_NPOP_MAX];
+  cg_spline snz[CG_NPOP_MAX], sbz[CG_NPOP_MAX], stz[CG_NPOP_MAX], sbi[CG_NPOP_MAX], skc[CG_NPOP_MAX],
+      sbc[CG_NPOP_MAX];
   for (int i = 0; i < p->n_srcs; i++) {
     if ((rc = tracer_spline(p->fname_bz_srcs[i], &c, 0, p->z_min, p->z_max, &sbz[i], "Bias", err, el))) return rc;
     if ((rc = tracer_spline(p->fname_nz_srcs[i], &c, 1, p->z_min, p->z_max, &snz[i], "N(z)", err, el))) return rc;
@@ -358,6 +359,12 @@ int cg_host_cosmo_set(cg_params *p, char *err, size_t el)
     if ((rc = tracer_spline(p->fname_tz_imap[i], &c, 0, p->z_min, p->z_max, &stz[i], "T(z)", err, el))) return rc;
     p->imap_tz_arr[i] = malloc(CG_NA * sizeof(double));
     p->imap_bz_arr[i] = malloc(CG_NA * sizeof(double));
+  }
+  for (int i = 0; i < p->n_cstm; i++) { /* cosmo.c:631-662 */
+    if ((rc = tracer_spline(p->fname_bz_cstm[i], &c, 0, p->z_min, p->z_max, &sbc[i], "Bias", err, el))) return rc;
+    if ((rc = tracer_spline(p->fname_kz_cstm[i], &c, 0, p->z_min, p->z_max, &skc[i], "K(z)", err, el))) return rc;
+    p->cstm_kz_arr[i] = malloc(CG_NA * sizeof(double));
+    p->cstm_bz_arr[i] = malloc(CG_NA * sizeof(double));
   }
   for (int i = 0; i < CG_NA; i++) {
     double a = ((double)i) / (CG_NA - 1);
@@ -398,6 +405,14 @@ int cg_host_cosmo_set(cg_params *p, char *err, size_t el)
       p->imap_tz_arr[k][i] = cg_spline_eval(&stz[k], z);
       p->imap_bz_arr[k][i] = cg_spline_eval(&sbi[k], z);
     }
+    for (int k = 0; k < p->n_cstm; k++) {
+      p->cstm_kz_arr[k][i] = cg_spline_eval(&skc[k], z);
+      p->cstm_bz_arr[k][i] = cg_spline_eval(&sbc[k], z);
+    }
+  }
+  for (int k = 0; k < p->n_cstm; k++) {
+    cg_spline_free(&skc[k]);
+    cg_spline_free(&sbc[k]);
   }
   for (int k = 0; k < p->n_srcs; k++) {
     cg_spline_free(&snz[k]);

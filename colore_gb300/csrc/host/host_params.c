@@ -335,6 +335,8 @@ void cg_params_free(cg_params *p)
     free(p->srcs_bz_arr[i]);
     free(p->imap_tz_arr[i]);
     free(p->imap_bz_arr[i]);
+    free(p->cstm_kz_arr[i]);
+    free(p->cstm_bz_arr[i]);
     free(p->imap_r0[i]);
     free(p->imap_rf[i]);
   }
@@ -416,6 +418,14 @@ int cg_read_run_params(const char *fname, cg_params **out, char *err, size_t el)
     p->nside_count[i] = opt_int(&r, path, 0);
   }
   p->n_cstm = count_sections(root, "custom");
+  if (p->n_cstm > CG_NPOP_MAX) rfail(&r, "You're asking for too many populations %d! Enlarge NPOP_MAX", p->n_cstm);
+  for (int i = 0; i < p->n_cstm && !r.rc; i++) {
+    char sec[32];
+    snprintf(sec, sizeof(sec), "custom%d", i + 1);
+    rd_string(&r, sec, "kz_filename", p->fname_kz_cstm[i], 256);
+    rd_string(&r, sec, "bias_filename", p->fname_bz_cstm[i], 256);
+    rd_int(&r, sec, "nside", &p->nside_cstm[i]);
+  }
   p->n_imap = count_sections(root, "imap");
   if (p->n_imap > CG_NPOP_MAX) rfail(&r, "You're asking for too many populations %d! Enlarge NPOP_MAX", p->n_imap);
   for (int i = 0; i < p->n_imap && !r.rc; i++) {
@@ -482,6 +492,12 @@ int cg_params_to_config(const cg_params *p, cg_config *c)
   c->smooth_potential = p->smooth_potential;
   c->dens_type = p->dens_type;
   c->lpt_interp_type = p->lpt_interp_type;
+  c->n_cstm = p->n_cstm;
+  for (int i = 0; i < p->n_cstm; i++) {
+    c->cstm_kz_arr[i] = p->cstm_kz_arr[i];
+    c->cstm_bz_arr[i] = p->cstm_bz_arr[i];
+    c->nside_cstm[i] = p->nside_cstm[i];
+  }
   c->bias_model = p->bias_model;
   c->numk = p->numk;
   c->logkmin = p->logkmin;

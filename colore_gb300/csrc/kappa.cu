@@ -12,7 +12,7 @@
  * nest-to-ring reordering of write_kappa, io.c:826-873).  Threads of a warp
  * hold neighbouring NEST pixels, so their rays stay close and the 19-point
  * stencil reads hit L1/L2.  The radial sums use Kahan compensation.
- * k_isw integrates the ISW maps along the same rays.
+ * k_isw integrates the ISW maps along the same rays, k_cstm the custom maps.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -105,7 +105,50 @@ __global__ void __launch_bounds__(256) k_isw(const float *__restrict__ phi, cg_k
   }
 }
 
+/* cstm_get_beam_properties (cstm.c:68-145): one NEST pixel per thread, the
+ * density interpolated trilinearly at each step centre of the kernel's
+ * support, written back in NEST order as write_cstm stores it
+ * (io.c:754-800 copies the shell data without reordering). */
+__global__ void __launch_bounds__(256) k_cstm(const float *__restrict__ dens, cg_cstm_params p)
+{
+  extern __shared__ float csh[];
+  const int ns = p.ir_max - p.ir_min + 1;
+  float *kz = csh, *bz = csh + ns, *nm = csh + 2 * ns;
+  for (int i = threadIdx.x; i < ns; i += blockDim.x) {
+    const int irr = p.ir_min + i;
+    kz[i] = p.kz[irr];
+    bz[i] = p.bz[irr];
+    nm[i] = bg(p.norm, p.g, CG_MUL(CG_ADD((float)irr, 0.5f), p.dr));
+  }
+  __syncthreads();
+  const long long ip = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (ip >= p.npix) return;
+  const int N = p.box.N;
+  float u[3];
+  cg_pix2vec_nest(p.nside, ip, u);
+  const float po[3] = {p.box.p0, p.box.p1, p.box.p2};
+  float acc = 0.0f, cmp = 0.0f;
+  for (int i = 0; i < ns; i++) {
+    const float rm = CG_MUL(CG_ADD((float)(p.ir_min + i), 0.5f), p.dr);
+    int i0[3], i1[3];
+    float h0[3], h1[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) cg_cic_axis(rm, u[a], po[a], p.box.idx, N, &i0[a], &i1[a], &h0[a], &h1[a]);
+    const float d = cg_cic_value(dens, i0, i1, h0, h1, N);
+    cg_kahan_add(&acc, &cmp, CG_MUL(kz[i], CG_SUB(CG_MUL(cg_bias_model(d, bz[i], p.bias_model), nm[i]), 1.0f)));
+  }
+  p.map[ip] = CG_MUL(acc, p.dr);
+}
+
 } /* namespace */
+
+cudaError_t cg_cstm_integrate(cudaStream_t s, const float *dens, const cg_cstm_params *p)
+{
+  long long blocks = (p->npix + 255) / 256;
+  const size_t smem = 3 * sizeof(float) * (size_t)(p->ir_max - p->ir_min + 1);
+  k_cstm<<<(unsigned)blocks, 256, smem, s>>>(dens, *p);
+  return cudaGetLastError();
+}
 
 cudaError_t cg_isw_integrate(cudaStream_t s, const float *phi, const cg_kappa_params *p)
 {

@@ -124,6 +124,13 @@ def write_inputs(dirname, spec, prefix="run"):
         np.savetxt(fnu, np.transpose([edges[:-1], edges[1:]]), fmt="%.10f")
         add("imap%d:\n{\n  tbak_filename= \"%s\";\n  bias_filename= \"%s\";\n  freq_list= \"%s\";\n"
             "  freq_rest= %r;\n  nside= %d;\n}\n" % (i + 1, ftz, fbz, fnu, nu_rest, m["nside"]))
+    for i, m in enumerate(spec.get("custom", [])):
+        fkz = os.path.join(dirname, "kzc_%d.txt" % (i + 1))
+        fbz = os.path.join(dirname, "bzc_%d.txt" % (i + 1))
+        np.savetxt(fkz, np.transpose([zs, m.get("amp", 1.0) * _nz_shape(zs, m["kz"])]), fmt="%.10e")
+        np.savetxt(fbz, np.transpose([zs, _bias(zs, m["bias"])]), fmt="%.10e")
+        add("custom%d:\n{\n  kz_filename= \"%s\";\n  bias_filename= \"%s\";\n  nside= %d;\n}\n" %
+            (i + 1, fkz, fbz, m["nside"]))
     if "kappa" in spec:
         kz = ", ".join("%r" % float(z) for z in spec["kappa"]["z_out"])
         add("kappa:\n{\n  z_out= [%s];\n  nside= %d;\n}\n" % (kz, spec["kappa"]["nside"]))

@@ -115,6 +115,12 @@ typedef struct {
   /* mass assignment of the 1LPT particles (density.c:178-187): 0 NGP,
    * 1 CIC (the reference's default, io.c:66), 2 TSC */
   int lpt_interp_type;
+  /* custom maps (cstm.c:68-145): kernel K(z) and bias b(z) on the r grid
+   * (cosmo.c:631-716), HEALPix resolution */
+  int n_cstm;
+  const double *cstm_kz_arr[CG_NPOP_MAX];
+  const double *cstm_bz_arr[CG_NPOP_MAX];
+  int nside_cstm[CG_NPOP_MAX];
 } cg_config;
 
 typedef struct cg_ctx cg_ctx;
@@ -139,7 +145,9 @@ int cg_compute_physical_density_field(cg_ctx *ctx);
 int cg_compute_density_normalization(cg_ctx *ctx);
 /* Device half of compute_density_normalization (density.c:1128-1211):
  * per-redshift-bin cell counts, summed redshifts and summed bias_model per
- * tracer.  Arrays have nz entries; norm arrays are [n_srcs][nz], [n_imap][nz]. */
+ * tracer.  Arrays have nz entries; norm arrays are [n_srcs][nz] and
+ * [n_imap + n_cstm][nz]: the intensity species, then the custom maps
+ * (norm_cstm_arr, src/density.c:1178), in one block. */
 int cg_collect_density_normalization(cg_ctx *ctx, int nz, double idz, double *zarr,
                                      unsigned long long *narr, double *norm_srcs,
                                      double *norm_imap);
@@ -157,7 +165,9 @@ int cg_collect_density_normalization(cg_ctx *ctx, int nz, double idz, double *za
 int cg_collect_density_normalization_static(cg_ctx *ctx, int nz, double idz, double *zarr,
                                             unsigned long long *narr, double *norm_srcs,
                                             double *norm_imap);
-/* Replace the NA-point normalisation tables (src/density.c:1323-1355). */
+/* Replace the NA-point normalisation tables (src/density.c:1323-1355).
+ * srcs_*: [n_srcs] tables; imap_*: [n_imap + n_cstm] tables, the intensity
+ * species then the custom maps; *_0f: (below, above) edge pairs. */
 int cg_set_norm_tables(cg_ctx *ctx, const double *srcs_norm, const double *srcs_norm_0f,
                        const double *imap_norm, const double *imap_norm_0f);
 int cg_srcs_set_cartesian(cg_ctx *ctx, long long *nsrc_per_pop);
@@ -187,10 +197,16 @@ int cg_download_imap(cg_ctx *ctx, int ipop, float *map, int *nadd);
 int cg_download_kappa(cg_ctx *ctx, float *map);
 /* ISW maps: n_isw * 12 nside_isw^2 values, RING order (write_isw, src/io.c:946-1010). */
 int cg_download_isw(cg_ctx *ctx, float *map);
+/* Custom map ipop: 12 nside_cstm[ipop]^2 values in NEST order, the layout
+ * write_cstm (src/io.c:754-800) puts in its file (it copies the shell data,
+ * listed in NEST order by hp_shell_alloc, src/common.c:505-552, without
+ * the nest-to-ring step of the kappa and ISW writers). */
+int cg_download_custom(cg_ctx *ctx, int ipop, float *map);
 
 /* FP32 normalisation table the kernels use: kind 0 = source population
  * ipop (srcs_norm_arr, src/common.h:318), 1 = intensity species
- * (imap_norm_arr, src/common.h:336).  tab: CG_NA floats; edges: the values
+ * (imap_norm_arr, src/common.h:336), 2 = custom map (cstm_norm_arr,
+ * src/cosmo.c:78-81).  tab: CG_NA floats; edges: the values
  * below and above the table (norm_*_0 / norm_*_f). */
 int cg_download_norm(cg_ctx *ctx, int kind, int ipop, float *tab, float *edges);
 

@@ -63,8 +63,13 @@ typedef struct {
   /* isw (io.c:421-426) */
   int do_isw, n_isw, nside_isw;
   double z_isw_out[CG_NPLANES_MAX], isw_r[CG_NPLANES_MAX];
+  /* custom maps custom1, custom2, ... (io.c:344-364) */
+  int n_cstm;
+  char fname_kz_cstm[CG_NPOP_MAX][256], fname_bz_cstm[CG_NPOP_MAX][256];
+  int nside_cstm[CG_NPOP_MAX];
+  double *cstm_kz_arr[CG_NPOP_MAX], *cstm_bz_arr[CG_NPOP_MAX];
   /* out-of-scope sections seen in the file (reported, not run) */
-  int n_cstm, do_skewers, do_srcs_lensing;
+  int do_skewers, do_srcs_lensing;
   int need_beaming, nside_base, bias_model;
 } cg_params;
 

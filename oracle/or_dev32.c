@@ -12,6 +12,7 @@
  *   or_imap32     imap_set_cartesian_single               imap.c:135-245
  *   or_kappa32    kappa_get_beam_properties               kappa.c:78-175
  *   or_isw32      isw_get_beam_properties                 isw.c:78-147
+ *   or_cstm32     cstm_get_beam_properties                cstm.c:68-145
  * Tables are rebuilt from the config with the same double->float roundings
  * as the GPU upload.  The Poisson and position streams are the Philox
  * streams of the GPU path (the reference's GSL MT19937 streams depend on the
@@ -35,13 +36,13 @@ typedef struct {
   float *tabs, *r, r_last, idr;
   T32 zt, d1, v1, ih;
   float *a_a2r, *r_a2r;
-  T32 nz[CG_NPOP_MAX], bz[CG_NPOP_MAX], tz[CG_NPOP_MAX], bzi[CG_NPOP_MAX];
+  T32 nz[CG_NPOP_MAX], bz[CG_NPOP_MAX], tz[CG_NPOP_MAX], bzi[CG_NPOP_MAX], bzc[CG_NPOP_MAX];
 } S32;
 
 static void s32_init(S32 *s, const cg_config *c)
 {
   const int na = CG_NA;
-  const int ntab = 9 + 2 * c->n_srcs + 2 * c->n_imap;
+  const int ntab = 9 + 2 * c->n_srcs + 2 * c->n_imap + c->n_cstm;
   s->tabs = malloc((size_t)ntab * na * sizeof(float));
   const double *src[9] = {c->r_arr_r2z, c->z_arr_r2z, c->growth_d_arr, c->growth_d2_arr, c->growth_v_arr,
                           c->growth_pd_arr, c->ihub_arr, c->a_arr_a2r, c->r_arr_a2r};
@@ -61,6 +62,10 @@ static void s32_init(S32 *s, const cg_config *c)
     s->tz[p] = (T32){s->tabs + (size_t)k * na, 0.0f, 0.0f};
     s->bzi[p] = (T32){s->tabs + (size_t)(k + 1) * na, (float)c->imap_bz_arr[p][0], 1.0f};
     k += 2;
+  }
+  for (int p = 0; p < c->n_cstm; p++, k++) {
+    for (int i = 0; i < na; i++) s->tabs[(size_t)k * na + i] = (float)c->cstm_bz_arr[p][i];
+    s->bzc[p] = (T32){s->tabs + (size_t)k * na, (float)c->cstm_bz_arr[p][0], 1.0f};
   }
   float *T = s->tabs;
   s->r = T;
@@ -117,7 +122,7 @@ int or_bins32(const cg_config *cfg, const float *dens, int nz, double idz, unsig
 {
   S32 s;
   s32_init(&s, cfg);
-  const int N = s.N, nts = cfg->n_srcs, nt = nts + cfg->n_imap;
+  const int N = s.N, nts = cfg->n_srcs, nti = cfg->n_imap, nt = nts + nti + cfg->n_cstm;
   const float idzf = (float)idz;
   memset(narr, 0, nz * sizeof(unsigned long long));
   memset(zarr, 0, nz * sizeof(double));
@@ -136,7 +141,7 @@ int or_bins32(const cg_config *cfg, const float *dens, int nz, double idz, unsig
         narr[b]++;
         zarr[b] += z;
         for (int t = 0; t < nt; t++) {
-          T32 tb = t < nts ? s.bz[t] : s.bzi[t - nts];
+          T32 tb = t < nts ? s.bz[t] : (t < nts + nti ? s.bzi[t - nts] : s.bzc[t - nts - nti]);
           bsum[(size_t)t * nz + b] += cg_bias_model(d, bg32(&s, tb, r), cfg->bias_model);
         }
       }
@@ -541,6 +546,52 @@ int or_isw32(const cg_config *cfg, const float *npot, float *map)
   free(irmin);
   free(irmax);
   free(f1);
+  s32_free(&s);
+  return 0;
+}
+
+/* k_cstm: step tables kz, bz from the FP64 tables rounded to float, the
+ * FP32 normalisation table evaluated at the float step centre, trilinear
+ * density and Kahan sum along the ray; NEST order. */
+int or_cstm32(const cg_config *cfg, int ipop, const float *dens, const float *normtab, float n0, float nf,
+              float *map)
+{
+  S32 s;
+  s32_init(&s, cfg);
+  const int N = s.N, nr = N / 2, nside = cfg->nside_cstm[ipop];
+  const long long npix = 12LL * nside * nside;
+  double *kzd = malloc(2 * (size_t)nr * sizeof(double)), *bzd = kzd + nr;
+  int lo, hi;
+  if (or_cstm_steps(cfg, ipop, kzd, bzd, &lo, &hi)) {
+    free(kzd);
+    s32_free(&s);
+    return -1;
+  }
+  const float drf = (float)(cfg->r_max / nr);
+  float *kz = malloc(3 * (size_t)nr * sizeof(float)), *bz = kz + nr, *nm = bz + nr;
+  const T32 nt = {normtab, n0, nf};
+  for (int i = 0; i < nr; i++) {
+    kz[i] = (float)kzd[i];
+    bz[i] = (float)bzd[i];
+    nm[i] = bg32(&s, nt, CG_MUL(CG_ADD((float)i, 0.5f), drf));
+  }
+#pragma omp parallel for schedule(static)
+  for (long long ip = 0; ip < npix; ip++) {
+    float u[3];
+    cg_pix2vec_nest(nside, ip, u);
+    float acc = 0, cmp = 0;
+    for (int irr = lo; irr <= hi; irr++) {
+      const float rm = CG_MUL(CG_ADD((float)irr, 0.5f), drf);
+      int i0[3], i1[3];
+      float h0[3], h1[3];
+      for (int a = 0; a < 3; a++) cg_cic_axis(rm, u[a], s.p[a], s.idx, N, &i0[a], &i1[a], &h0[a], &h1[a]);
+      const float d = cg_cic_value(dens, i0, i1, h0, h1, N);
+      cg_kahan_add(&acc, &cmp, CG_MUL(kz[irr], CG_SUB(CG_MUL(cg_bias_model(d, bz[irr], cfg->bias_model), nm[irr]), 1.0f)));
+    }
+    map[ip] = CG_MUL(acc, drf);
+  }
+  free(kzd);
+  free(kz);
   s32_free(&s);
   return 0;
 }

@@ -13,6 +13,8 @@
  *   or_imap64        imap_set_cartesian_single     imap.c:135-245
  *   or_kappa64       kappa_get_beam_properties     kappa.c:78-175
  *   or_isw64         isw_get_beam_properties       isw.c:78-147
+ *   or_cstm_steps    custom-map step tables        cstm.c:81-116
+ *   or_cstm64        cstm_get_beam_properties      cstm.c:68-145
  *   or_run_mock64    the driver sequence of main.c:66-125 for timing.
  * Random numbers: the Philox streams of the GPU path (uniforms identical
  * bit for bit), since GSL's MT19937 streams cannot be reproduced here.
@@ -224,7 +226,7 @@ int or_lpt64(const cg_config *c, const double *dg_in, double *dens_out, double *
 int or_bins64(const cg_config *c, const double *dens, int nz, double idz, unsigned long long *narr, double *zarr,
               double *bsum)
 {
-  const int N = c->n_grid, nts = c->n_srcs, nt = nts + c->n_imap;
+  const int N = c->n_grid, nts = c->n_srcs, nti = c->n_imap, nt = nts + nti + c->n_cstm;
   const double dx = c->l_box / N;
   memset(narr, 0, nz * sizeof(unsigned long long));
   memset(zarr, 0, nz * sizeof(double));
@@ -243,7 +245,8 @@ int or_bins64(const cg_config *c, const double *dens, int nz, double idz, unsign
         narr[b]++;
         zarr[b] += z;
         for (int t = 0; t < nt; t++) {
-          const double *bt = t < nts ? c->srcs_bz_arr[t] : c->imap_bz_arr[t - nts];
+          const double *bt = t < nts ? c->srcs_bz_arr[t]
+                                     : (t < nts + nti ? c->imap_bz_arr[t - nts] : c->cstm_bz_arr[t - nts - nti]);
           bsum[(size_t)t * nz + b] += bias_model64(d, bg(c, bt, bt[0], 1, r), c->bias_model);
         }
       }
@@ -255,7 +258,7 @@ int or_bins64(const cg_config *c, const double *dens, int nz, double idz, unsign
 int or_norm_tables64(const cg_config *c, double *tabs, double *e0f, int *nz_out, unsigned long long *narr,
                      double *zarr, double *bsum, const double *dens)
 {
-  const int nt = c->n_srcs + c->n_imap;
+  const int nt = c->n_srcs + c->n_imap + c->n_cstm;
   double zmax = BG_Z(c, c->l_box * 0.5);
   int nz = (int)(zmax / 0.05) + 2;
   double idz = (nz - 2) / zmax;
@@ -717,8 +720,8 @@ int or_run_mock64(const cg_config *c, int nthreads_hint, long long *nsrc_total, 
   } else {
     or_density64(c, dens, st[3]);
   }
-  const int nt = c->n_srcs + c->n_imap;
-  double *tabs = malloc((size_t)(nt > 0 ? nt : 1) * CG_NA * sizeof(double)), e0f[2 * 2 * CG_NPOP_MAX];
+  const int nt = c->n_srcs + c->n_imap + c->n_cstm;
+  double *tabs = malloc((size_t)(nt > 0 ? nt : 1) * CG_NA * sizeof(double)), e0f[2 * 3 * CG_NPOP_MAX];
   unsigned long long narr[4096];
   double zarr[4096], *bsum = malloc((size_t)(nt > 0 ? nt : 1) * 4096 * sizeof(double));
   int nz;
@@ -758,5 +761,86 @@ int or_run_mock64(const cg_config *c, int nthreads_hint, long long *nsrc_total, 
   free(npot);
   if (nsrc_total) *nsrc_total = tot;
   if (checksum) *checksum = cs + st[3];
+  return 0;
+}
+
+/* Step tables of cstm_get_beam_properties (cstm.c:81-116): kz = K(r)/IH(r)
+ * and b(r) at the N/2 step centres, and the integration range where
+ * |kz| > 1e-4 max|kz|.  Returns -1 when the kernel has no support. */
+int or_cstm_steps(const cg_config *c, int ipop, double *kz, double *bz, int *ir_min, int *ir_max)
+{
+  const int nr = c->n_grid / 2;
+  const double dr = c->r_max / nr;
+  const double *kt = c->cstm_kz_arr[ipop], *bt = c->cstm_bz_arr[ipop];
+  double kmax = -1e100;
+  for (int i = 0; i < nr; i++) {
+    const double rm = (i + 0.5) * dr;
+    kz[i] = bg(c, kt, 0, 0, rm) / BG_IH(c, rm);
+    bz[i] = bg(c, bt, bt[0], 1, rm);
+    if (fabs(kz[i]) > kmax) kmax = fabs(kz[i]);
+  }
+  *ir_min = 0;
+  *ir_max = nr - 1;
+  for (int i = 0; i < nr; i++)
+    if (fabs(kz[i]) > 1e-4 * kmax) {
+      *ir_min = i;
+      break;
+    }
+  for (int i = nr - 1; i >= 0; i--)
+    if (fabs(kz[i]) > 1e-4 * kmax) {
+      *ir_max = i;
+      break;
+    }
+  return *ir_max < *ir_min ? -1 : 0;
+}
+
+/* cstm_get_beam_properties (cstm.c:68-145) in double precision: per NEST
+ * pixel, dr * sum over the support of kz (bias_model(d, bz) norm - 1), d the
+ * trilinear density at (rm u + pos_obs) idx (interpolate_from_grid,
+ * beaming.c:183-262).  dens: N^3 unpadded; map: NEST order (write_cstm,
+ * io.c:754-800, writes the shell data without reordering). */
+int or_cstm64(const cg_config *c, int ipop, const double *dens, const double *normtab, double n0, double nf,
+              double *map)
+{
+  const int N = c->n_grid, nr = N / 2, nside = c->nside_cstm[ipop];
+  const long npix = 12L * nside * nside;
+  const double dr = c->r_max / nr, idx = N / c->l_box;
+  double *kz = malloc(3 * (size_t)nr * sizeof(double)), *bz = kz + nr, *nm = bz + nr;
+  int lo, hi;
+  if (or_cstm_steps(c, ipop, kz, bz, &lo, &hi)) {
+    free(kz);
+    return -1;
+  }
+  for (int i = 0; i < nr; i++) nm[i] = bg(c, normtab, n0, nf, (i + 0.5) * dr);
+#pragma omp parallel for schedule(static)
+  for (long ip = 0; ip < npix; ip++) {
+    double u[3], cval = 0;
+    pix2vec_nest64(nside, ip, u);
+    for (int irr = lo; irr <= hi; irr++) {
+      const double rm = (irr + 0.5) * dr;
+      long i0[3], i1[3];
+      double h0[3], h1[3];
+      for (int a = 0; a < 3; a++) {
+        const double x = (rm * u[a] + c->pos_obs[a]) * idx;
+        i0[a] = (long)x;
+        h0[a] = x - i0[a];
+        h1[a] = 1 - h0[a];
+        i1[a] = i0[a] + 1;
+        if (i0[a] >= N) i0[a] -= N;
+        else if (i0[a] < 0) i0[a] += N;
+        if (i1[a] >= N) i1[a] -= N;
+        else if (i1[a] < 0) i1[a] += N;
+      }
+#define D(X, Y, Z) dens[(X) + (size_t)N * ((Y) + (size_t)N * (Z))]
+      const double d = (D(i0[0], i0[1], i0[2]) * h1[2] * h1[1] * h1[0] + D(i1[0], i0[1], i0[2]) * h1[2] * h1[1] * h0[0] +
+                        D(i0[0], i1[1], i0[2]) * h1[2] * h0[1] * h1[0] + D(i1[0], i1[1], i0[2]) * h1[2] * h0[1] * h0[0]) +
+                       (D(i0[0], i0[1], i1[2]) * h0[2] * h1[1] * h1[0] + D(i1[0], i0[1], i1[2]) * h0[2] * h1[1] * h0[0] +
+                        D(i0[0], i1[1], i1[2]) * h0[2] * h0[1] * h1[0] + D(i1[0], i1[1], i1[2]) * h0[2] * h0[1] * h0[0]);
+#undef D
+      cval += kz[irr] * (bias_model64(d, bz[irr], c->bias_model) * nm[irr] - 1);
+    }
+    map[ip] = cval * dr;
+  }
+  free(kz);
   return 0;
 }

@@ -47,6 +47,9 @@ int or_lambda64(const cg_config *cfg, int ipop, const double *dens, const double
                 double *lambda);
 int or_kappa64(const cg_config *cfg, const double *npot, double *map);
 int or_isw64(const cg_config *cfg, const double *npot, double *map);
+int or_cstm_steps(const cg_config *cfg, int ipop, double *kz, double *bz, int *ir_min, int *ir_max);
+int or_cstm64(const cg_config *cfg, int ipop, const double *dens, const double *normtab, double n0, double nf,
+              double *map);
 int or_imap64(const cg_config *cfg, int ipop, const double *dens, const double *npot, const double *normtab,
               double n0, double nf, double *data, int *nadd);
 int or_imap64_part(const cg_config *cfg, int ipop, const double *dens, const double *npot, const double *normtab,
@@ -69,5 +72,7 @@ int or_imap32(const cg_config *cfg, int ipop, const float *dens, const float *np
               float nf, float *data, int *nadd);
 int or_kappa32(const cg_config *cfg, const float *npot, float *map);
 int or_isw32(const cg_config *cfg, const float *npot, float *map);
+int or_cstm32(const cg_config *cfg, int ipop, const float *dens, const float *normtab, float n0, float nf,
+              float *map);
 
 #endif

@@ -35,7 +35,9 @@ def lib():
             "or_counts32": [vp, i, vp, vp, f, f, vp, vp],
             "or_emit32": [vp, i, vp, vp, vp, f, f, C.c_longlong, vp, vp, vp, vp, vp],
             "or_beam_rsd32": [vp, vp, C.c_longlong, vp, vp], "or_imap32": [vp, i, vp, vp, vp, f, f, vp, vp],
-            "or_kappa32": [vp, vp, vp], "or_isw32": [vp, vp, vp], "or_isw64": [vp, vp, vp], "or_c2r_3d": [i, vp, vp], "or_r2c_3d": [i, vp, vp],
+            "or_kappa32": [vp, vp, vp], "or_isw32": [vp, vp, vp], "or_isw64": [vp, vp, vp],
+            "or_cstm_steps": [vp, i, vp, vp, vp, vp], "or_cstm64": [vp, i, vp, vp, d, d, vp],
+            "or_cstm32": [vp, i, vp, vp, f, f, vp], "or_c2r_3d": [i, vp, vp], "or_r2c_3d": [i, vp, vp],
             "or_vec_expf": [vp, vp, C.c_long], "or_vec_logf": [vp, vp, C.c_long],
             "or_vec_log1pf": [vp, vp, C.c_long], "or_vec_acosf": [vp, vp, C.c_long],
             "or_vec_atan2f": [vp, vp, vp, C.c_long], "or_vec_sincosf": [vp, vp, vp, C.c_long],
@@ -104,7 +106,7 @@ def lpt64(cfg, dens_gauss):
 
 
 def norm_tables64(cfg, dens):
-    nt = cfg.n_srcs + cfg.n_imap
+    nt = cfg.n_srcs + cfg.n_imap + cfg.n_cstm
     tabs = np.empty((max(nt, 1), 5001))
     e0f = np.empty((max(nt, 1), 2))
     nz = C.c_int()
@@ -117,7 +119,7 @@ def norm_tables64(cfg, dens):
 
 
 def bins64(cfg, dens, nz, idz):
-    nt = cfg.n_srcs + cfg.n_imap
+    nt = cfg.n_srcs + cfg.n_imap + cfg.n_cstm
     narr = np.empty(nz, np.uint64)
     zarr = np.empty(nz)
     bsum = np.empty((max(nt, 1), nz))
@@ -167,7 +169,7 @@ def density32(cfg, dens, s2f, mode):
 
 
 def bins32(cfg, dens, nz, idz):
-    nt = cfg.n_srcs + cfg.n_imap
+    nt = cfg.n_srcs + cfg.n_imap + cfg.n_cstm
     narr = np.empty(nz, np.uint64)
     zarr = np.empty(nz)
     bsum = np.empty((max(nt, 1), nz))
@@ -222,6 +224,32 @@ def isw32(cfg, npot):
     ns = cfg.nside_isw
     m = np.empty((cfg.n_isw, 12 * ns * ns), np.float32)
     lib().or_isw32(cfgp(cfg), P(npot), P(m))
+    return m
+
+
+def cstm_steps(cfg, ipop):
+    """(kz, bz, ir_min, ir_max): the custom-map step tables in double."""
+    nr = cfg.n_grid // 2
+    kz = np.empty(nr)
+    bz = np.empty(nr)
+    lo, hi = C.c_int(), C.c_int()
+    rc = lib().or_cstm_steps(cfgp(cfg), ipop, P(kz), P(bz), C.byref(lo), C.byref(hi))
+    return kz, bz, lo.value, hi.value, rc
+
+
+def cstm64(cfg, ipop, dens, tab, e):
+    ns = cfg.nside_cstm[ipop]
+    m = np.empty(12 * ns * ns)
+    assert lib().or_cstm64(cfgp(cfg), ipop, P(np.ascontiguousarray(dens, np.float64)),
+                           P(np.ascontiguousarray(tab, np.float64)), float(e[0]), float(e[1]), P(m)) == 0
+    return m
+
+
+def cstm32(cfg, ipop, dens, tab, e):
+    ns = cfg.nside_cstm[ipop]
+    m = np.empty(12 * ns * ns, np.float32)
+    assert lib().or_cstm32(cfgp(cfg), ipop, P(dens), P(np.ascontiguousarray(tab, np.float32)), float(e[0]),
+                           float(e[1]), P(m)) == 0
     return m
 
 

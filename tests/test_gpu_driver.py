@@ -20,7 +20,8 @@ def _spec(fmt):
                 srcs=[dict(nz=("gauss", 0.3, 0.1), density=50.0, bias=("1+z",), nside_count=8)],
                 imap=[dict(tz=0.1, bias=("const", 1.0), z_range=(0.1, 0.5), nbands=3, nside=8)],
                 kappa=dict(z_out=[0.3, 0.5], nside=8),
-                isw=dict(z_out=[0.4], nside=8))
+                isw=dict(z_out=[0.4], nside=8),
+                custom=[dict(kz=("gauss", 0.3, 0.1), bias=("const", 1.2), nside=8)])
 
 
 @pytest.mark.parametrize("fmt", ["FITS", "ASCII"])
@@ -71,4 +72,7 @@ def test_driver_outputs_match_library(built, tmp_path, fmt):
         assert np.array_equal(np.frombuffer(d, ">f4"), k[ir])
     (_, _), (h, d) = read_fits("%s_isw_z000.fits" % prefix)
     assert np.array_equal(np.frombuffer(d, ">f4"), m.isw()[0])
+    (_, _), (h, d) = read_fits("%s_custom_s1.fits" % prefix)
+    assert h["NSIDE"] == 8 and h["NAXIS2"] == 12 * 64
+    assert np.array_equal(np.frombuffer(d, ">f4"), m.custom(0))
     m.close()

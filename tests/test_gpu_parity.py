@@ -16,6 +16,7 @@ restatement of the reference (ref64) within the stated tolerances:
   normalisation tables          relative 2e-4 vs FP64 (FP32 bin edges)
   intensity maps                hit counts exact, brightness relative 5e-5
   convergence maps              bit-exact vs dev32; relative rms 1e-3 vs FP64
+  custom maps                   bit-exact vs dev32; relative rms 1e-4 vs FP64
 """
 import os
 
@@ -34,7 +35,9 @@ def _spec(kind):
                       dict(nz=("flat", 0.1, 0.5), density=4.0, bias=("const", 2.0), nside_count=8)],
                 imap=[dict(tz=0.1, bias=("const", 1.0), z_range=(0.1, 0.5), nbands=6, nside=16)],
                 kappa=dict(z_out=[0.2, 0.4, 0.55], nside=16),
-                isw=dict(z_out=[0.55, 0.3], nside=16))
+                isw=dict(z_out=[0.55, 0.3], nside=16),
+                custom=[dict(kz=("gauss", 0.3, 0.08), bias=("const", 1.5), nside=16),
+                        dict(kz=("flat", 0.2, 0.45), bias=("1+z",), nside=8, amp=-2.0)])
     if kind == "nobeam":
         base.pop("kappa")
         base["bias_model"] = 1
@@ -108,6 +111,7 @@ class Run:
         self.d = m.grid(0).copy()
         self.norm_s = [m.norm_table(0, i) for i in range(self.cfg.n_srcs)]
         self.norm_i = [m.norm_table(1, i) for i in range(self.cfg.n_imap)]
+        self.norm_c = [m.norm_table(2, i) for i in range(self.cfg.n_cstm)]
         self.nsrc = m.srcs_set_cartesian()
         self.cats = [m.catalog(i) for i in range(self.cfg.n_srcs)]
         self.cmaps = [m.count_map(i) if self.cfg.nside_count[i] > 0 else None for i in range(self.cfg.n_srcs)]
@@ -117,6 +121,7 @@ class Run:
         self.cats_beam = [m.catalog(i, pos=False, ipix=False) for i in range(self.cfg.n_srcs)]
         self.kappa = m.kappa() if self.cfg.do_kappa else None
         self.isw = m.isw() if self.cfg.do_isw else None
+        self.cstm = [m.custom(i) for i in range(self.cfg.n_cstm)]
 
 
 _RUNS = {}
@@ -250,7 +255,7 @@ def test_redshift_bin_sums(runs, kind):
     narr = np.empty(nz, np.uint64)
     zarr = np.empty(nz)
     bs = np.empty((r.cfg.n_srcs, nz))
-    bi = np.empty((max(r.cfg.n_imap, 1), nz))
+    bi = np.empty((max(r.cfg.n_imap + r.cfg.n_cstm, 1), nz))
     rc = cg.lib().cg_collect_density_normalization(
         r.m._c, nz, idz, zarr.ctypes.data_as(C.POINTER(C.c_double)),
         narr.ctypes.data_as(C.POINTER(C.c_ulonglong)), bs.ctypes.data_as(C.POINTER(C.c_double)),
@@ -260,7 +265,7 @@ def test_redshift_bin_sums(runs, kind):
     assert np.array_equal(n32, narr)
     ok = narr > 0
     assert np.allclose(zarr[ok], z32[ok], rtol=1e-6)
-    gb = np.concatenate([bs, bi[:r.cfg.n_imap]])
+    gb = np.concatenate([bs, bi[:r.cfg.n_imap + r.cfg.n_cstm]])
     assert np.allclose(gb[:, ok], b32[:, ok], rtol=1e-6)
 
 
@@ -277,7 +282,8 @@ def test_norm_tables_vs_fp64(runs, kind):
     import oracle as orc
     r = runs(kind)
     tabs, e0f, nz = orc.norm_tables64(r.cfg, unpad(r.need('d')).astype(np.float64))
-    got = r.need('norm_s') + r.need('norm_i')
+    got = r.need('norm_s') + r.need('norm_i') + r.need('norm_c')
+    assert len(got) == r.cfg.n_srcs + r.cfg.n_imap + r.cfg.n_cstm
     for t, (tab, e) in enumerate(got):
         assert np.all(np.isfinite(tab)), (t, tab[~np.isfinite(tab)][:5])
         assert np.allclose(tab, tabs[t], rtol=2e-4), (t, np.max(np.abs(tab / tabs[t] - 1)))
@@ -392,6 +398,28 @@ def test_isw_bitexact_and_fp64(runs):
     # maps come in order of distance (isw_beams_preproc sorts the planes) and
     # are cumulative along the ray, so the two differ
     assert not np.allclose(got[0], got[1])
+
+
+def test_custom_maps_bitexact_and_fp64(runs):
+    """Custom maps (cstm.c:68-145): bit-exact against the FP32 restatement fed
+    the GPU density and normalisation table; against the FP64 restatement of
+    the reference fed the same density within 1e-4 rms (FP32 positions and
+    step tables).  Maps are in NEST order, as the reference writes them."""
+    import oracle as orc
+    r = runs("full")
+    assert r.cfg.n_cstm == 2
+    for ip in range(2):
+        got = r.need('cstm')[ip]
+        ns = r.cfg.nside_cstm[ip]
+        assert got.shape == (12 * ns * ns,) and np.all(np.isfinite(got)) and np.any(got != 0)
+        tab, e = r.norm_c[ip]
+        ref32 = orc.cstm32(r.cfg, ip, r.need('d'), tab, e)
+        assert np.array_equal(ref32.view(np.uint32), got.view(np.uint32)), ip
+        ref64 = orc.cstm64(r.cfg, ip, unpad(r.need('d')).astype(np.float64), tab.astype(np.float64),
+                           e.astype(np.float64))
+        assert rel_rms(got, ref64) < 1e-4, ip
+    # kernel 2 has the opposite sign and another support
+    assert np.corrcoef(r.cstm[0], np.repeat(r.cstm[1], 4))[0, 1] < 0.5
 
 
 def test_rerun_is_deterministic(runs, tmp_path):
