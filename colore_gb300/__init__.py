@@ -60,6 +60,9 @@ class Config(C.Structure):
         ("cstm_kz_arr", _dp * NPOP_MAX),
         ("cstm_bz_arr", _dp * NPOP_MAX),
         ("nside_cstm", C.c_int * NPOP_MAX),
+        ("lensing_srcs", C.c_int * NPOP_MAX),
+        ("skw_srcs", C.c_int * NPOP_MAX),
+        ("skw_gauss", C.c_int * NPOP_MAX),
     ]
 
 
@@ -117,7 +120,8 @@ def lib():
             "cg64_num_sources": (C.c_longlong, [vp, C.c_int]),
             "cg64_download": (C.c_int, [vp, C.c_int, C.c_int, vp]),
             "cg_write_healpix_map": (C.c_int, [C.c_char_p, vp, C.c_long]),
-            "cg_write_catalog": (C.c_int, [C.c_char_p, C.c_int, C.c_int, vp, C.c_longlong]),
+            "cg_write_catalog": (C.c_int, [C.c_char_p, C.c_int, C.c_int, vp, C.c_longlong, C.c_int, vp]),
+            "cg_download_skewers": (C.c_int, [vp, C.c_int, vp, vp]),
             "cg_write_density_grid": (C.c_int, [C.c_char_p, C.c_char_p, vp, C.c_int, C.c_double]),
             "cg_read_run_params": (C.c_int, [C.c_char_p, C.POINTER(vp), C.c_char_p, C.c_size_t]),
             "cg_params_free": (None, [vp]),
@@ -139,7 +143,7 @@ def exported_symbols():
             "cg_collect_density_normalization", "cg_collect_density_normalization_static", "cg_set_norm_tables", "cg_srcs_set_cartesian",
             "cg_imap_set_cartesian", "cg_imap_samples", "cg_get_beam_properties", "cg_run_mock", "cg_download_grid",
             "cg_num_sources", "cg_download_catalog", "cg_download_count_map", "cg_download_imap",
-            "cg_download_kappa", "cg_download_isw", "cg_download_custom", "cg_download_norm", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_read_run_params",
+            "cg_download_kappa", "cg_download_isw", "cg_download_custom", "cg_download_skewers", "cg_download_norm", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_read_run_params",
             "cg_params_free", "cg_params_to_config", "cg_write_healpix_map", "cg_write_catalog",
             "cg_write_density_grid", "cg64_create", "cg64_destroy", "cg64_last_error",
             "cg64_run_mock", "cg64_num_sources", "cg64_download"]
@@ -161,10 +165,28 @@ def write_healpix_map(fname, m, nside):
         raise CGError("cannot write %s" % fname)
 
 
-def write_catalog(prefix, ipop, src, fmt=OUT_FITS):
-    """<prefix>_srcs_s<ipop+1>_0.fits or .txt from Src records (n x 9 floats)."""
+class SkewerSet(C.Structure):
+    """Mirror of cg_skewer_set (include/colore_host.h)."""
+    _fields_ = [("nr", C.c_int), ("gauss", C.c_int), ("dens", C.c_void_p), ("vel", C.c_void_p),
+                ("r", C.c_void_p), ("z", C.c_void_p), ("d1", C.c_void_p), ("v1", C.c_void_p),
+                ("sigma_g", C.c_float)]
+
+
+def write_catalog(prefix, ipop, src, fmt=OUT_FITS, lensing=False, skewers=None):
+    """<prefix>_srcs_s<ipop+1>_0.fits or .txt from Src records (n x 9 floats).
+    lensing adds the E1 E2 KAPPA DRA DDEC columns; skewers (FITS only) is a
+    dict with dens, vel (n x nr), r, z, d1, v1 (nr), sigma_g and gauss."""
     src = np.ascontiguousarray(src, np.float32).reshape(-1, 9)
-    if lib().cg_write_catalog(os.fsencode(prefix), ipop, fmt, src.ctypes.data, len(src)):
+    keep, ps = [], None
+    if skewers is not None:
+        arr = {k: np.ascontiguousarray(skewers[k], np.float32) for k in ("dens", "vel", "r", "z", "d1", "v1")}
+        keep.append(arr)
+        nr = arr["r"].size
+        ps = SkewerSet(nr, int(bool(skewers.get("gauss", False))), arr["dens"].ctypes.data, arr["vel"].ctypes.data,
+                       arr["r"].ctypes.data, arr["z"].ctypes.data, arr["d1"].ctypes.data, arr["v1"].ctypes.data,
+                       float(skewers["sigma_g"]))
+    if lib().cg_write_catalog(os.fsencode(prefix), ipop, fmt, src.ctypes.data, len(src), int(bool(lensing)),
+                              C.byref(ps) if ps is not None else None):
         raise CGError("cannot write the catalogue of population %d under %s" % (ipop, prefix))
 
 
@@ -339,6 +361,15 @@ class Mock:
         m = out if out is not None else np.empty((self.cfg.n_isw, 12 * ns * ns), np.float32)
         self._chk(lib().cg_download_isw(self._c, m.ctypes.data), "download_isw")
         return m
+
+    def skewers(self, ipop):
+        """(dens, vel) skewers of population ipop, n_sources x n_grid/2 each."""
+        n = self.num_sources(ipop)
+        nr = self.cfg.n_grid // 2
+        d = np.empty((n, nr), np.float32)
+        v = np.empty((n, nr), np.float32)
+        self._chk(lib().cg_download_skewers(self._c, ipop, d.ctypes.data, v.ctypes.data), "download_skewers")
+        return d, v
 
     def custom(self, ipop, out=None):
         """Custom map ipop, 12 nside_cstm^2 values in NEST order (the order the

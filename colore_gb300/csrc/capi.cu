@@ -43,6 +43,9 @@ struct Cat {
   long long n = 0, cap = 0;
   int *cmap = nullptr;
   long long cmap_npix = 0;
+  float *skw_d = nullptr, *skw_v = nullptr; /* skewers: n x nr each */
+  long long skw_cap = 0;                   /* sources the skewer buffers hold */
+  long long skw_n = -1;                    /* sources of the last skewer pass */
 };
 
 struct Imap {
@@ -111,6 +114,9 @@ struct cg_ctx {
   /* custom maps: host copies of K(z) and b(z), device maps and step tables */
   std::vector<double> h_kzc[CG_NPOP_MAX], h_bzc[CG_NPOP_MAX];
   float *d_cmap[CG_NPOP_MAX] = {nullptr}, *d_cfac = nullptr;
+  /* source lensing and skewer step tables (2 nr + nr floats) */
+  float *d_losfac = nullptr;
+  int losnr = 0;
   long long cnpix[CG_NPOP_MAX] = {0};
   int cnr = 0;
   int *d_iir = nullptr;
@@ -303,6 +309,9 @@ static int validate(const cg_config *cfg, char *msg, size_t len)
       return snprintf(msg, len, "intensity-map table missing"), CG_EINVAL;
   }
   if (cfg->n_srcs > 0 && cfg->nside_base < 1) return snprintf(msg, len, "nside_base must be >= 1"), CG_EINVAL;
+  for (int i = 0; i < cfg->n_srcs; i++) /* get_element, beaming.c:56-57 */
+    if (cfg->skw_srcs[i] && cfg->skw_gauss[i] && cfg->dens_type != CG_DENS_LGNR)
+      return snprintf(msg, len, "Cannot write Gaussian skewers with density type %d", cfg->dens_type), CG_EINVAL;
   return CG_OK;
 }
 
@@ -471,12 +480,12 @@ extern "C" void cg_destroy(cg_ctx *c)
                   c->d_zsum, c->d_bsum, c->d_counts, c->d_bsums, c->d_total, c->d_tmpmap, c->d_kmap,
                   c->d_kfac, c->d_kinv, c->d_kir, c->d_ovf_cell, c->d_ovf_cnt, c->d_ovf_n,
                   c->d_cells, c->d_cell_n, c->d_cell_off, c->d_scan_tmp, c->d_imap_ctr,
-                  c->d_imap_isw, c->d_ifac, c->d_iir, c->d_cfac};
+                  c->d_imap_isw, c->d_ifac, c->d_iir, c->d_cfac, c->d_losfac};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < CG_NPOP_MAX; i++) {
     void *q[] = {c->cat[i].pos, c->cat[i].ipix, c->cat[i].src, c->cat[i].cmap, c->im[i].r0, c->im[i].rf,
-                 c->im[i].shp, c->im[i].data, c->im[i].nadd, c->d_cmap[i]};
+                 c->im[i].shp, c->im[i].data, c->im[i].nadd, c->d_cmap[i], c->cat[i].skw_d, c->cat[i].skw_v};
     for (void *p : q)
       if (p) cudaFree(p);
   }
@@ -1285,6 +1294,80 @@ static int cstm_run(cg_ctx *c)
   return CG_OK;
 }
 
+/* Step tables of srcs_get_beam_properties_single and
+ * srcs_beams_postproc_single (srcs.c:465-478, 725-733) on the N/2 steps of
+ * the catalogue's radial grid (catalog_alloc, common.c:377-379):
+ * 2 pg dr and rm pg dr with pg = D(rm) (1 + z(rm)), then V1(rm) factor_vel. */
+static int los_tables(cg_ctx *c)
+{
+  const int nr = c->N / 2;
+  const double dr = c->cfg.r_max / nr;
+  if (c->losnr == nr) return CG_OK;
+  if (int rc = dalloc(c, &c->d_losfac, 3 * (size_t)nr)) return rc;
+  const double fv = -c->cfg.fgrowth_0 / (1.5 * c->cfg.hubble_0 * c->cfg.omega_m);
+  std::vector<float> t(3 * (size_t)nr);
+  for (int i = 0; i < nr; i++) {
+    const double rm = (i + 0.5) * dr;
+    const double pg = host_bg(c, c->h_d1, 1, c->h_d1[CG_NA - 1], rm) * (1 + host_bg(c, c->h_z, 0, c->h_z[CG_NA - 1], rm));
+    t[i] = (float)(2 * pg * dr);
+    t[nr + i] = (float)(rm * pg * dr);
+    t[2 * nr + i] = (float)(host_bg(c, c->h_v1, c->h_v1[0], c->h_v1[CG_NA - 1], rm) * fv);
+  }
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_losfac, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host staging vector */
+  c->losnr = nr;
+  return CG_OK;
+}
+
+static int srcs_los_run(cg_ctx *c, int ip)
+{
+  Cat &K = c->cat[ip];
+  const bool lens = c->cfg.lensing_srcs[ip] != 0, skw = c->cfg.skw_srcs[ip] != 0;
+  if (!lens && !skw) return CG_OK;
+  int rc;
+  if ((rc = los_tables(c))) return rc;
+  const int nr = c->losnr;
+  cg_los_params q;
+  memset(&q, 0, sizeof(q));
+  q.box = c->box;
+  q.g = c->g;
+  q.d1 = c->d1;
+  q.pos = K.pos;
+  q.src = K.src;
+  q.nsrc = K.n;
+  q.nr = nr;
+  q.dr = (float)(c->cfg.r_max / nr);
+  q.idr = (float)(nr / c->cfg.r_max);
+  q.lfac = c->d_losfac;
+  q.vfac = c->d_losfac + 2 * (size_t)nr;
+  q.skw_gauss = c->cfg.skw_gauss[ip];
+  q.sigma2 = c->d_s2f;
+  if (lens && K.n > 0) {
+    ProfScope ps(c, "srcs_lensing");
+    CUDA_TRY(c, cg_srcs_lensing(c->stream, c->d_npot, &q, c->nsm));
+    c->launches++;
+  }
+  if (skw) {
+    if (K.n > K.skw_cap) {
+      const long long cap = K.n + K.n / 8 + 64;
+      if ((rc = dalloc(c, &K.skw_d, (size_t)cap * nr)) || (rc = dalloc(c, &K.skw_v, (size_t)cap * nr))) {
+        K.skw_cap = 0;
+        return rc;
+      }
+      K.skw_cap = cap;
+    }
+    q.skw_d = K.skw_d;
+    q.skw_v = K.skw_v;
+    if (K.n > 0) {
+      ProfScope ps(c, "srcs_skewers");
+      CUDA_TRY(c, cg_srcs_skewers(c->stream, c->d_dens, c->d_npot, &q, c->nsm));
+      c->launches++;
+    }
+    K.skw_n = K.n;
+  }
+  return CG_OK;
+}
+
 extern "C" int cg_get_beam_properties(cg_ctx *c)
 {
   if (!c) return CG_EINVAL;
@@ -1305,6 +1388,7 @@ extern "C" int cg_get_beam_properties(cg_ctx *c)
       ProfScope ps(c, "srcs_beam_rsd");
       CUDA_TRY(c, cg_srcs_beam_rsd(c->stream, c->d_npot, &p, c->cat[ip].n, c->nsm));
       if (c->cat[ip].n > 0) c->launches++;
+      if (int rc = srcs_los_run(c, ip)) return rc;
     }
   }
   return CG_OK;
@@ -1369,6 +1453,21 @@ extern "C" int cg_download_catalog(cg_ctx *c, int ipop, float *pos4, int *ipix, 
     if (pos4) CUDA_TRY(c, cudaMemcpyAsync(pos4, K.pos, K.n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
     if (ipix) CUDA_TRY(c, cudaMemcpyAsync(ipix, K.ipix, K.n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     if (src9) CUDA_TRY(c, cudaMemcpyAsync(src9, K.src, K.n * 9 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  }
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return check_device_errors(c);
+}
+
+extern "C" int cg_download_skewers(cg_ctx *c, int ipop, float *dens, float *vel)
+{
+  if (!c || ipop < 0 || ipop >= c->cfg.n_srcs) return CG_EINVAL;
+  const Cat &K = c->cat[ipop];
+  if (!c->cfg.skw_srcs[ipop]) return fail(c, CG_ESTATE, "population %d stores no skewers", ipop);
+  if (K.skw_n != K.n) return fail(c, CG_ESTATE, "skewers of population %d not computed", ipop);
+  const size_t m = (size_t)K.n * c->losnr;
+  if (m) {
+    if (dens) CUDA_TRY(c, cudaMemcpyAsync(dens, K.skw_d, m * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    if (vel) CUDA_TRY(c, cudaMemcpyAsync(vel, K.skw_v, m * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
   }
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return check_device_errors(c);

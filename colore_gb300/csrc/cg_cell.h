@@ -487,26 +487,43 @@ CG_HD void cg_cic_axis(float rm, float u, float po, float idx, int N, int *i0, i
   *i1 = b;
 }
 
-/* Trilinear density from the padded grid (row stride 2(N/2+1)): the four
- * terms of the i0[2] plane, then the four of the i1[2] plane, in the order of
+/* Trilinear combination of the eight corner values v[bx + 2 by + 4 bz]
+ * (b = 0 for the i0 cell, 1 for the i1 cell of each axis): the four terms
+ * of the i0[2] plane, then the four of the i1[2] plane, in the order of
  * interpolate_from_grid (beaming.c:205-262), chained with FMAs. */
+CG_HD float cg_cic_combine(const float v[8], const float h0[3], const float h1[3])
+{
+  const float wa = h1[2], wb = h0[2];
+  const float w00 = CG_MUL(h1[1], h1[0]), w01 = CG_MUL(h1[1], h0[0]);
+  const float w10 = CG_MUL(h0[1], h1[0]), w11 = CG_MUL(h0[1], h0[0]);
+  float d = CG_MUL(v[0], CG_MUL(wa, w00));
+  d = CG_FMA(v[1], CG_MUL(wa, w01), d);
+  d = CG_FMA(v[2], CG_MUL(wa, w10), d);
+  d = CG_FMA(v[3], CG_MUL(wa, w11), d);
+  d = CG_FMA(v[4], CG_MUL(wb, w00), d);
+  d = CG_FMA(v[5], CG_MUL(wb, w01), d);
+  d = CG_FMA(v[6], CG_MUL(wb, w10), d);
+  d = CG_FMA(v[7], CG_MUL(wb, w11), d);
+  return d;
+}
+
+/* Trilinear value of a padded grid (row stride 2(N/2+1)) */
 CG_HD float cg_cic_value(const float *g, const int i0[3], const int i1[3], const float h0[3], const float h1[3], int N)
 {
   const long long ngx = 2 * (N / 2 + 1);
   const float *pa = g + (long long)i0[2] * ngx * N, *pb = g + (long long)i1[2] * ngx * N;
   const long long ya = (long long)i0[1] * ngx, yb = (long long)i1[1] * ngx;
-  const float wa = h1[2], wb = h0[2];
-  const float w00 = CG_MUL(h1[1], h1[0]), w01 = CG_MUL(h1[1], h0[0]);
-  const float w10 = CG_MUL(h0[1], h1[0]), w11 = CG_MUL(h0[1], h0[0]);
-  float d = CG_MUL(pa[ya + i0[0]], CG_MUL(wa, w00));
-  d = CG_FMA(pa[ya + i1[0]], CG_MUL(wa, w01), d);
-  d = CG_FMA(pa[yb + i0[0]], CG_MUL(wa, w10), d);
-  d = CG_FMA(pa[yb + i1[0]], CG_MUL(wa, w11), d);
-  d = CG_FMA(pb[ya + i0[0]], CG_MUL(wb, w00), d);
-  d = CG_FMA(pb[ya + i1[0]], CG_MUL(wb, w01), d);
-  d = CG_FMA(pb[yb + i0[0]], CG_MUL(wb, w10), d);
-  d = CG_FMA(pb[yb + i1[0]], CG_MUL(wb, w11), d);
-  return d;
+  const float v[8] = {pa[ya + i0[0]], pa[ya + i1[0]], pa[yb + i0[0]], pa[yb + i1[0]],
+                      pb[ya + i0[0]], pb[ya + i1[0]], pb[yb + i0[0]], pb[yb + i1[0]]};
+  return cg_cic_combine(v, h0, h1);
+}
+
+/* Gaussian field of a physical (lognormal) density cell, get_element
+ * RETURN_GAUSS (beaming.c:54-66): log(1 + d) / D(r) + D(r) sigma^2 / 2 with
+ * D the growth factor at the cell's own radius. */
+CG_HD float cg_gauss_of_dens(float d, float dg, float sigma2)
+{
+  return CG_ADD(CG_DIV(cg_log1pf(d), dg), CG_MUL(CG_MUL(dg, sigma2), 0.5f));
 }
 
 /* NGP cell along a ray, interpolate_from_grid NGP branch (beaming.c:148-157) */
@@ -538,6 +555,50 @@ CG_HD void cg_kappa_rot(const float u[3], float prefac, float rot[6])
   rot[5] = CG_MUL(CG_MUL(sth, sth), prefac);
 }
 
+/* Projections of srcs_get_beam_properties_single (srcs.c:536-581) for one
+ * source direction: ux, uy take the potential gradient to the deflection
+ * (prefac_m = idx / (2 r)); rk, re1, re2 take the tidal tensor to the
+ * convergence and the two shear components (prefac = idx^2 / r). */
+CG_HD void cg_lens_rot(const float u[3], float prefac, float prefac_m, float ux[3], float uy[3], float rk[6],
+                       float re1[6], float re2[6])
+{
+  float cth = u[2];
+  if (cth >= 1.0f) cth = 1.0f;
+  if (cth <= -1.0f) cth = -1.0f;
+  const float sth = CG_SQRT(CG_MUL(CG_SUB(1.0f, cth), CG_ADD(1.0f, cth)));
+  float cph = 1.0f, sph = 0.0f;
+  if (sth != 0.0f) {
+    cph = CG_DIV(u[0], sth);
+    sph = CG_DIV(u[1], sth);
+  }
+  ux[0] = CG_MUL(CG_MUL(cth, cph), prefac_m);
+  ux[1] = CG_MUL(CG_MUL(cth, sph), prefac_m);
+  ux[2] = CG_MUL(-sth, prefac_m);
+  uy[0] = CG_MUL(-sph, prefac_m);
+  uy[1] = CG_MUL(cph, prefac_m);
+  uy[2] = 0.0f;
+  const float c2 = CG_MUL(cth, cth);
+  const float cc = CG_MUL(cph, cph), ss = CG_MUL(sph, sph), cs = CG_MUL(cph, sph);
+  rk[0] = CG_MUL(CG_ADD(CG_MUL(c2, cc), ss), prefac);
+  rk[1] = CG_MUL(CG_MUL(CG_MUL(2.0f, cs), CG_SUB(c2, 1.0f)), prefac);
+  rk[2] = CG_MUL(CG_MUL(CG_MUL(CG_MUL(-2.0f, cth), sth), cph), prefac);
+  rk[3] = CG_MUL(CG_ADD(CG_MUL(c2, ss), cc), prefac);
+  rk[4] = CG_MUL(CG_MUL(CG_MUL(CG_MUL(-2.0f, cth), sth), sph), prefac);
+  rk[5] = CG_MUL(CG_MUL(sth, sth), prefac);
+  re1[0] = CG_MUL(CG_SUB(CG_MUL(c2, cc), ss), prefac);
+  re1[1] = CG_MUL(CG_MUL(CG_MUL(2.0f, cs), CG_ADD(c2, 1.0f)), prefac);
+  re1[2] = rk[2];
+  re1[3] = CG_MUL(CG_SUB(CG_MUL(c2, ss), cc), prefac);
+  re1[4] = rk[4];
+  re1[5] = rk[5];
+  re2[0] = CG_MUL(CG_MUL(CG_MUL(-2.0f, cth), cs), prefac);
+  re2[1] = CG_MUL(CG_MUL(CG_MUL(2.0f, cth), CG_SUB(cc, ss)), prefac);
+  re2[2] = CG_MUL(CG_MUL(CG_MUL(2.0f, sth), sph), prefac);
+  re2[3] = CG_MUL(CG_MUL(CG_MUL(2.0f, cth), cs), prefac);
+  re2[4] = CG_MUL(CG_MUL(CG_MUL(-2.0f, sth), cph), prefac);
+  re2[5] = 0.0f;
+}
+
 /* tidal tensor from the 19-point stencil, get_element (beaming.c:84-116);
  * order XX, XY, XZ, YY, YZ, ZZ.  f[] = {000, x+, x-, y+, y-, z+, z-,
  * x+y+, x-y-, x+y-, x-y+, x+z+, x-z-, x+z-, x-z+, y+z+, y-z-, y+z-, y-z+} */
@@ -550,6 +611,11 @@ CG_HD void cg_tidal(const float f[19], float t[6])
   t[1] = CG_MUL(0.25f, CG_SUB(CG_SUB(CG_ADD(f[7], f[8]), f[9]), f[10]));
   t[2] = CG_MUL(0.25f, CG_SUB(CG_SUB(CG_ADD(f[11], f[12]), f[13]), f[14]));
   t[4] = CG_MUL(0.25f, CG_SUB(CG_SUB(CG_ADD(f[15], f[16]), f[17]), f[18]));
+}
+
+CG_HD float cg_dot3(const float a[3], const float b[3])
+{
+  return CG_FMA(a[2], b[2], CG_FMA(a[1], b[1], CG_MUL(a[0], b[0])));
 }
 
 CG_HD float cg_dot6(const float a[6], const float b[6])

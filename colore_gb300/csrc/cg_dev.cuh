@@ -81,6 +81,40 @@ __device__ __forceinline__ long long pidx(int ix, int iy, int iz, int N)
 
 __device__ __forceinline__ int wrap(int i, int N) { return i >= N ? i - N : (i < 0 ? i + N : i); }
 
+/* The 19 potential values of get_element's tidal stencil (beaming.c:84-116)
+ * around cell (x0, y0, z0), in the order cg_tidal takes them. */
+__device__ __forceinline__ void stencil19(const float *__restrict__ phi, int x0, int y0, int z0, int N, float f[19])
+{
+  const int ngx = 2 * (N / 2 + 1);
+  const size_t plane = (size_t)ngx * N;
+  const int xh = wrap(x0 + 1, N), xl = wrap(x0 - 1, N);
+  const int yh = wrap(y0 + 1, N), yl = wrap(y0 - 1, N);
+  const int zh = wrap(z0 + 1, N), zl = wrap(z0 - 1, N);
+  const float *P0 = phi + (size_t)z0 * plane, *Ph = phi + (size_t)zh * plane, *Pl = phi + (size_t)zl * plane;
+  const int o0 = y0 * ngx, oh = yh * ngx, ol = yl * ngx;
+#define CG_PHI(X, OY, PZ) __ldg((PZ) + (OY) + (X))
+  f[0] = CG_PHI(x0, o0, P0);
+  f[1] = CG_PHI(xh, o0, P0);
+  f[2] = CG_PHI(xl, o0, P0);
+  f[3] = CG_PHI(x0, oh, P0);
+  f[4] = CG_PHI(x0, ol, P0);
+  f[5] = CG_PHI(x0, o0, Ph);
+  f[6] = CG_PHI(x0, o0, Pl);
+  f[7] = CG_PHI(xh, oh, P0);
+  f[8] = CG_PHI(xl, ol, P0);
+  f[9] = CG_PHI(xh, ol, P0);
+  f[10] = CG_PHI(xl, oh, P0);
+  f[11] = CG_PHI(xh, o0, Ph);
+  f[12] = CG_PHI(xl, o0, Pl);
+  f[13] = CG_PHI(xh, o0, Pl);
+  f[14] = CG_PHI(xl, o0, Ph);
+  f[15] = CG_PHI(x0, oh, Ph);
+  f[16] = CG_PHI(x0, ol, Pl);
+  f[17] = CG_PHI(x0, oh, Pl);
+  f[18] = CG_PHI(x0, ol, Ph);
+#undef CG_PHI
+}
+
 /* Parameters of the Fourier-space fill (fourier.c:285-359). */
 struct FillParams {
   int N, NH;

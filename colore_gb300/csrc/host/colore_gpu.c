@@ -91,8 +91,6 @@ int main(int argc, char **argv)
   printf("  Real-space resolution: dx = %.3lE Mpc/h\n", p->l_box / p->n_grid);
   printf("  Original sigma8=%lf, Sigma_Gauss should be %lf\n", p->sigma8_input, p->sigma2_gauss_theory > 0 ? sqrt(p->sigma2_gauss_theory) : 0.0);
   printf("  GPU memory plan: %.3f GB\n", mem / 1e9);
-  if (p->n_cstm || p->do_skewers || p->do_srcs_lensing)
-    fprintf(stderr, "Warning: custom maps, skewers and source lensing are not produced by this build\n");
   if (test_memory) {
     cg_params_free(p);
     return 0;
@@ -164,7 +162,23 @@ int main(int argc, char **argv)
     float *src = malloc((size_t)(ns[ip] > 0 ? ns[ip] : 1) * 9 * sizeof(float));
     if (!src) die(c, CG_ENOMEM, "catalogue buffer");
     if ((rc = cg_download_catalog(c, ip, NULL, NULL, src))) die(c, rc, "download_catalog");
-    if ((rc = cg_write_catalog(p->prefix_out, ip, fmt, src, ns[ip]))) die(c, rc, "write_catalog");
+    cg_skewer_set skw, *pskw = NULL;
+    float *skw_buf = NULL;
+    if (p->skw_srcs[ip] && fmt == CG_OUT_FITS) { /* io.c:1140-1189 */
+      const int nr = p->n_grid / 2;
+      const size_t m = (size_t)(ns[ip] > 0 ? ns[ip] : 0) * nr;
+      skw_buf = malloc((2 * m + 4 * (size_t)nr) * sizeof(float));
+      if (!skw_buf) die(c, CG_ENOMEM, "skewer buffer");
+      float *bgr = skw_buf + 2 * m;
+      if ((rc = cg_download_skewers(c, ip, skw_buf, skw_buf + m))) die(c, rc, "download_skewers");
+      cg_skewer_background(p, nr, bgr, bgr + nr, bgr + 2 * nr, bgr + 3 * nr);
+      skw = (cg_skewer_set){nr, p->skw_gauss[ip], skw_buf, skw_buf + m, bgr, bgr + nr, bgr + 2 * nr, bgr + 3 * nr,
+                            (float)sqrt(s2)};
+      pskw = &skw;
+    }
+    if ((rc = cg_write_catalog(p->prefix_out, ip, fmt, src, ns[ip], p->lensing_srcs[ip], pskw)))
+      die(c, rc, "write_catalog");
+    free(skw_buf);
     free(src);
     if (p->nside_count[ip] > 0) {
       long npix = 12L * p->nside_count[ip] * p->nside_count[ip];

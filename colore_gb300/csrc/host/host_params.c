@@ -296,6 +296,12 @@ static void rd_bool(reader *r, const char *sec, const char *var, int *out)
   *out = n->bval;
 }
 
+static int opt_bool(reader *r, const char *path, int def)
+{
+  node *n = lookup(r->root, path);
+  return (n && n->type == T_BOOL) ? n->bval : def;
+}
+
 static int opt_int(reader *r, const char *path, int def)
 {
   node *n = lookup(r->root, path);
@@ -412,7 +418,12 @@ int cg_read_run_params(const char *fname, cg_params **out, char *err, size_t el)
     rd_bool(&r, sec, "include_lensing", &p->lensing_srcs[i]);
     if (p->lensing_srcs[i]) p->do_srcs_lensing = 1;
     rd_bool(&r, sec, "store_skewers", &p->skw_srcs[i]);
-    if (p->skw_srcs[i]) p->do_skewers = 1;
+    if (p->skw_srcs[i]) {
+      p->do_skewers = 1;
+      char gpath[64];
+      snprintf(gpath, sizeof(gpath), "%s.gaussian_skewers", sec);
+      p->skw_gauss[i] = opt_bool(&r, gpath, 0);
+    }
     char path[64];
     snprintf(path, sizeof(path), "%s.nside_count", sec);
     p->nside_count[i] = opt_int(&r, path, 0);
@@ -520,6 +531,9 @@ int cg_params_to_config(const cg_params *p, cg_config *c)
     c->srcs_nz_arr[i] = p->srcs_nz_arr[i];
     c->srcs_bz_arr[i] = p->srcs_bz_arr[i];
     c->nside_count[i] = p->nside_count[i];
+    c->lensing_srcs[i] = p->lensing_srcs[i];
+    c->skw_srcs[i] = p->skw_srcs[i];
+    c->skw_gauss[i] = p->skw_gauss[i];
   }
   c->nside_base = p->nside_base;
   c->n_imap = p->n_imap;

@@ -18,6 +18,13 @@
  *                  its cell by binary search on the scanned offsets.  Positions,
  *                  the NGP velocity (get_rvel, srcs.c:87-118), ra/dec/z, the
  *                  base-pixel id and the count-map increment are fused.
+ *
+ * Along the line of sight to each source (one thread per source):
+ *   k_beam_rsd    : trilinear RSD at the source.
+ *   k_src_lensing : shear, convergence and deflection from the nearest-cell
+ *                   tidal tensor and potential gradient at N/2 radial steps.
+ *   k_src_skewers : trilinear density (or Gaussian field) and radial velocity
+ *                   at every step up to the source.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -256,6 +263,39 @@ __global__ void __launch_bounds__(SB) k_emit(const float *__restrict__ phi, cg_s
   }
 }
 
+/* Trilinear potential gradient at a point with corner cells i0/i1 and
+ * weights h0/h1 (interpolate_from_grid RETURN_VEL, beaming.c:183-265): per z
+ * plane the four corners' central differences weighted and summed with FMAs,
+ * then the two planes added. */
+__device__ __forceinline__ void cic_grad(const float *__restrict__ phi, const int i0[3], const int i1[3],
+                                         const float h0[3], const float h1[3], int N, float v[3])
+{
+  v[0] = v[1] = v[2] = 0.0f;
+#pragma unroll
+  for (int hz = 0; hz < 2; hz++) {
+    const int zc = hz ? i1[2] : i0[2];
+    const float wz = hz ? h0[2] : h1[2];
+    float acc[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int yc = (k & 2) ? i1[1] : i0[1], xc = (k & 1) ? i1[0] : i0[0];
+      const float w = CG_MUL(CG_MUL(wz, (k & 2) ? h0[1] : h1[1]), (k & 1) ? h0[0] : h1[0]);
+      float g[3];
+      grad_phi(phi, xc, yc, zc, N, g);
+#pragma unroll
+      for (int a = 0; a < 3; a++) acc[a] = CG_FMA(g[a], w, acc[a]);
+    }
+#pragma unroll
+    for (int a = 0; a < 3; a++) v[a] = CG_ADD(v[a], acc[a]);
+  }
+}
+
+/* radial projection 0.5 idx (v . u), srcs.c:503 */
+__device__ __forceinline__ float los_vel(const float v[3], const float u[3], float idx)
+{
+  return CG_MUL(CG_MUL(0.5f, idx), CG_ADD(CG_ADD(CG_MUL(v[0], u[0]), CG_MUL(v[1], u[1])), CG_MUL(v[2], u[2])));
+}
+
 /* Line-of-sight RSD at each source: trilinear gradient of the potential
  * (interpolate_from_grid CIC branch, beaming.c:183-265) projected on the
  * line of sight (srcs.c:500-504), then scaled by V1(r(z0)) * factor_vel
@@ -283,30 +323,125 @@ __global__ void __launch_bounds__(256) k_beam_rsd(const float *__restrict__ phi,
       i1[a] = wrap(i0[a] + 1, N);
       i0[a] = wrap(i0[a], N);
     }
-    float v[3] = {0.0f, 0.0f, 0.0f};
-#pragma unroll
-    for (int hz = 0; hz < 2; hz++) {
-      const int zc = hz ? i1[2] : i0[2];
-      const float wz = hz ? h0[2] : h1[2];
-      float acc[3] = {0.0f, 0.0f, 0.0f};
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        const int yc = (k & 2) ? i1[1] : i0[1], xc = (k & 1) ? i1[0] : i0[0];
-        const float w = CG_MUL(CG_MUL(wz, (k & 2) ? h0[1] : h1[1]), (k & 1) ? h0[0] : h1[0]);
-        float g[3];
-        grad_phi(phi, xc, yc, zc, N, g);
-#pragma unroll
-        for (int a = 0; a < 3; a++) acc[a] = CG_FMA(g[a], w, acc[a]);
-      }
-#pragma unroll
-      for (int a = 0; a < 3; a++) v[a] = CG_ADD(v[a], acc[a]);
-    }
-    float vr = CG_MUL(CG_MUL(0.5f, p.box.idx),
-                      CG_ADD(CG_ADD(CG_MUL(v[0], u[0]), CG_MUL(v[1], u[1])), CG_MUL(v[2], u[2])));
+    float v[3];
+    cic_grad(phi, i0, i1, h0, h1, N, v);
+    const float vr = los_vel(v, u, p.box.idx);
     float *s = p.src + (size_t)i * 9;
     float z0 = s[2];
     float rz = r_of_z(p.a_a2r, p.r_a2r, p.na, z0);
     s[3] = CG_MUL(vr, CG_MUL(bg(p.v1, p.g, rz), p.factor_vel));
+  }
+}
+
+/* Direction, distance and last radial step of a source (srcs.c:485-493,
+ * 583): r = |pos|, u = pos / max(r, 0.001), i_r_max = min((int)(r/dr + 0.5), nr - 1). */
+__device__ __forceinline__ int los_setup(float4 q, const cg_los_params &p, float *r, float u[3])
+{
+  *r = cg_norm3(q.x, q.y, q.z);
+  const float ir = CG_DIV(1.0f, *r > 0.001f ? *r : 0.001f);
+  u[0] = CG_MUL(q.x, ir);
+  u[1] = CG_MUL(q.y, ir);
+  u[2] = CG_MUL(q.z, ir);
+  const int k = (int)CG_ADD(CG_MUL(*r, p.idr), 0.5f);
+  return k < p.nr - 1 ? k : p.nr - 1;
+}
+
+/* Lensing at each source (srcs.c:536-625 without _USE_FAST_LENSING): at
+ * each step up to the source the nearest cell's tidal tensor and potential
+ * gradient, projected with the source's rotation, weighted by
+ * rm pg dr (r - rm) (shear, convergence) and 2 pg dr (r - rm) (deflection),
+ * summed with Kahan compensation; the deflections are turned to degrees
+ * (srcs.c:721-722). */
+__global__ void __launch_bounds__(256) k_src_lensing(const float *__restrict__ phi, cg_los_params p)
+{
+  extern __shared__ float lsh[];
+  for (int i = threadIdx.x; i < 2 * p.nr; i += blockDim.x) lsh[i] = p.lfac[i];
+  __syncthreads();
+  const float *f0 = lsh, *f1 = lsh + p.nr;
+  const int N = p.box.N;
+  const float po[3] = {p.box.p0, p.box.p1, p.box.p2};
+  const float idx = p.box.idx;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.nsrc;
+       i += (long long)gridDim.x * blockDim.x) {
+    float r, u[3];
+    const int kmax = los_setup(p.pos[i], p, &r, u);
+    const float ir = CG_DIV(1.0f, r > 0.001f ? r : 0.001f);
+    float ux[3], uy[3], rk[6], re1[6], re2[6];
+    cg_lens_rot(u, CG_MUL(CG_MUL(idx, idx), ir), CG_MUL(CG_MUL(0.5f, idx), ir), ux, uy, rk, re1, re2);
+    float a[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, c[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    for (int k = 0; k <= kmax; k++) {
+      const float rm = CG_MUL(CG_ADD((float)k, 0.5f), p.dr);
+      const int x0 = cg_ngp_cell(rm, u[0], po[0], idx, N);
+      const int y0 = cg_ngp_cell(rm, u[1], po[1], idx, N);
+      const int z0 = cg_ngp_cell(rm, u[2], po[2], idx, N);
+      float f[19], t[6];
+      stencil19(phi, x0, y0, z0, N, f);
+      cg_tidal(f, t);
+      const float v[3] = {CG_SUB(f[1], f[2]), CG_SUB(f[3], f[4]), CG_SUB(f[5], f[6])};
+      const float dd = CG_SUB(r, rm);
+      const float fr = CG_MUL(f1[k], dd), frm = CG_MUL(f0[k], dd);
+      cg_kahan_add(&a[0], &c[0], CG_MUL(cg_dot6(re1, t), fr));
+      cg_kahan_add(&a[1], &c[1], CG_MUL(cg_dot6(re2, t), fr));
+      cg_kahan_add(&a[2], &c[2], CG_MUL(cg_dot6(rk, t), fr));
+      cg_kahan_add(&a[3], &c[3], CG_MUL(cg_dot3(ux, v), frm));
+      cg_kahan_add(&a[4], &c[4], CG_MUL(cg_dot3(uy, v), frm));
+    }
+    float *s = p.src + (size_t)i * 9;
+    s[4] = a[0];
+    s[5] = a[1];
+    s[6] = a[2];
+    s[7] = CG_MUL(a[4], 57.2957795f); /* dra  = RTOD * dty */
+    s[8] = CG_MUL(a[3], 57.2957795f); /* ddec = RTOD * dtx */
+  }
+}
+
+/* Skewers (srcs.c:509-536, 725-733): at each step up to the source the
+ * trilinear density, or the Gaussian field of the eight corner cells, and
+ * the trilinear radial velocity times V1(rm) factor_vel; 0 beyond. */
+__global__ void __launch_bounds__(256) k_src_skewers(const float *__restrict__ dens, const float *__restrict__ phi,
+                                                      cg_los_params p)
+{
+  extern __shared__ float ssh[];
+  for (int i = threadIdx.x; i < p.nr; i += blockDim.x) ssh[i] = p.vfac[i];
+  __syncthreads();
+  const int N = p.box.N;
+  const float po[3] = {p.box.p0, p.box.p1, p.box.p2};
+  const float idx = p.box.idx;
+  const float s2 = p.skw_gauss ? *p.sigma2 : 0.0f;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.nsrc;
+       i += (long long)gridDim.x * blockDim.x) {
+    float r, u[3];
+    const int kmax = los_setup(p.pos[i], p, &r, u);
+    float *sd = p.skw_d + (size_t)i * p.nr, *sv = p.skw_v + (size_t)i * p.nr;
+    for (int k = 0; k <= kmax; k++) {
+      const float rm = CG_MUL(CG_ADD((float)k, 0.5f), p.dr);
+      int i0[3], i1[3];
+      float h0[3], h1[3];
+#pragma unroll
+      for (int a = 0; a < 3; a++) cg_cic_axis(rm, u[a], po[a], idx, N, &i0[a], &i1[a], &h0[a], &h1[a]);
+      float d;
+      if (p.skw_gauss) {
+        float gv[8];
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+          const int ix = (b & 1) ? i1[0] : i0[0], iy = (b & 2) ? i1[1] : i0[1], iz = (b & 4) ? i1[2] : i0[2];
+          const float rc = cg_norm3(cg_cell_coord(ix, p.box.dx, p.box.p0), cg_cell_coord(iy, p.box.dx, p.box.p1),
+                                    cg_cell_coord(iz, p.box.dx, p.box.p2));
+          gv[b] = cg_gauss_of_dens(__ldg(&dens[pidx(ix, iy, iz, N)]), bg(p.d1, p.g, rc), s2);
+        }
+        d = cg_cic_combine(gv, h0, h1);
+      } else {
+        d = cg_cic_value(dens, i0, i1, h0, h1, N);
+      }
+      float v[3];
+      cic_grad(phi, i0, i1, h0, h1, N, v);
+      sd[k] = d;
+      sv[k] = CG_MUL(los_vel(v, u, idx), ssh[k]);
+    }
+    for (int k = kmax + 1; k < p.nr; k++) {
+      sd[k] = 0.0f;
+      sv[k] = 0.0f;
+    }
   }
 }
 
@@ -328,6 +463,24 @@ cudaError_t cg_srcs_emit(cudaStream_t s, const float *phi, const cg_srcs_params 
 {
   long long nb = cg_srcs_nblocks(p->box.N);
   k_emit<<<(unsigned)nb, SB, 0, s>>>(phi, *p);
+  return cudaGetLastError();
+}
+
+cudaError_t cg_srcs_lensing(cudaStream_t s, const float *phi, const cg_los_params *p, int nsm)
+{
+  if (p->nsrc <= 0) return cudaSuccess;
+  long long blocks = (p->nsrc + 255) / 256;
+  if (blocks > (long long)nsm * 8) blocks = (long long)nsm * 8;
+  k_src_lensing<<<(unsigned)blocks, 256, 2 * p->nr * sizeof(float), s>>>(phi, *p);
+  return cudaGetLastError();
+}
+
+cudaError_t cg_srcs_skewers(cudaStream_t s, const float *dens, const float *phi, const cg_los_params *p, int nsm)
+{
+  if (p->nsrc <= 0) return cudaSuccess;
+  long long blocks = (p->nsrc + 255) / 256;
+  if (blocks > (long long)nsm * 8) blocks = (long long)nsm * 8;
+  k_src_skewers<<<(unsigned)blocks, 256, p->nr * sizeof(float), s>>>(dens, phi, *p);
   return cudaGetLastError();
 }
 

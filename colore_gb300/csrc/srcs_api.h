@@ -42,9 +42,32 @@ struct cg_srcs_params {
 #define CG_COUNT_ESC 65535
 #define CG_OVF_CAP 4096
 
+/* Line-of-sight quantities at the sources of one population
+ * (srcs_get_beam_properties_single and srcs_beams_postproc_single,
+ * srcs.c:452-733): lensing (shear, convergence, deflection) integrated with
+ * the nearest-cell tidal tensor, and skewers sampled with trilinear
+ * interpolation, on nr = N/2 radial steps of dr up to each source. */
+struct cg_los_params {
+  cg::Box box;
+  cg::Grid1 g;
+  cg::Tab d1;            /* growth factor, for Gaussian skewers */
+  const float4 *pos;     /* catalogue positions */
+  float *src;            /* 9 floats per source; lensing writes e1 e2 kappa dra ddec */
+  long long nsrc;
+  int nr;
+  float dr, idr;
+  const float *lfac;     /* 2 nr: 2 pg dr, then rm pg dr, pg = D(rm) (1 + z(rm)) */
+  const float *vfac;     /* nr: V1(rm) factor_vel */
+  float *skw_d, *skw_v;  /* nsrc x nr each */
+  int skw_gauss;
+  const float *sigma2;   /* device sigma^2 of the Gaussian field */
+};
+
 long long cg_srcs_nblocks(int N);
 cudaError_t cg_srcs_count(cudaStream_t s, const float *grid, const cg_srcs_params *p, long long *total);
 cudaError_t cg_srcs_emit(cudaStream_t s, const float *phi, const cg_srcs_params *p);
 cudaError_t cg_srcs_beam_rsd(cudaStream_t s, const float *phi, const cg_srcs_params *p, long long nsrc, int nsm);
+cudaError_t cg_srcs_lensing(cudaStream_t s, const float *phi, const cg_los_params *p, int nsm);
+cudaError_t cg_srcs_skewers(cudaStream_t s, const float *dens, const float *phi, const cg_los_params *p, int nsm);
 
 #endif

@@ -110,8 +110,11 @@ def write_inputs(dirname, spec, prefix="run"):
         fbz = os.path.join(dirname, "bz_%d.txt" % (i + 1))
         np.savetxt(fnz, np.transpose([zs, nz]), fmt="%.10e")
         np.savetxt(fbz, np.transpose([zs, _bias(zs, s["bias"])]), fmt="%.10e")
-        add("srcs%d:\n{\n  nz_filename= \"%s\";\n  bias_filename= \"%s\";\n  include_lensing= false;\n"
-            "  store_skewers= false;\n  nside_count= %d;\n}\n" % (i + 1, fnz, fbz, s.get("nside_count", 0)))
+        tf = lambda b: "true" if b else "false"  # noqa: E731
+        gs = "  gaussian_skewers= %s;\n" % tf(s["gaussian_skewers"]) if "gaussian_skewers" in s else ""
+        add("srcs%d:\n{\n  nz_filename= \"%s\";\n  bias_filename= \"%s\";\n  include_lensing= %s;\n"
+            "  store_skewers= %s;\n%s  nside_count= %d;\n}\n" %
+            (i + 1, fnz, fbz, tf(s.get("lensing")), tf(s.get("skewers")), gs, s.get("nside_count", 0)))
     for i, m in enumerate(spec.get("imap", [])):
         ftz = os.path.join(dirname, "tz_%d.txt" % (i + 1))
         fbz = os.path.join(dirname, "bzi_%d.txt" % (i + 1))

@@ -121,6 +121,12 @@ typedef struct {
   const double *cstm_kz_arr[CG_NPOP_MAX];
   const double *cstm_bz_arr[CG_NPOP_MAX];
   int nside_cstm[CG_NPOP_MAX];
+  /* per source population: line-of-sight lensing (include_lensing), skewers
+   * (store_skewers) and Gaussian rather than density skewers
+   * (gaussian_skewers), src/io.c:331-339 */
+  int lensing_srcs[CG_NPOP_MAX];
+  int skw_srcs[CG_NPOP_MAX];
+  int skw_gauss[CG_NPOP_MAX];
 } cg_config;
 
 typedef struct cg_ctx cg_ctx;
@@ -202,6 +208,13 @@ int cg_download_isw(cg_ctx *ctx, float *map);
  * listed in NEST order by hp_shell_alloc, src/common.c:505-552, without
  * the nest-to-ring step of the kappa and ISW writers). */
 int cg_download_custom(cg_ctx *ctx, int ipop, float *map);
+/* Skewers of source population ipop (store_skewers; srcs.c:509-536 and the
+ * velocity scaling of srcs_beams_postproc, srcs.c:725-733): nsrc x nr floats
+ * each, catalogue order, nr = n_grid/2 steps of r_max/nr.  dens holds the
+ * density contrast, or the Gaussian field with gaussian_skewers; vel the
+ * radial velocity in units of redshift.  Steps beyond a source are 0.
+ * Either pointer may be NULL. */
+int cg_download_skewers(cg_ctx *ctx, int ipop, float *dens, float *vel);
 
 /* FP32 normalisation table the kernels use: kind 0 = source population
  * ipop (srcs_norm_arr, src/common.h:318), 1 = intensity species

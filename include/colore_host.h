@@ -49,7 +49,7 @@ typedef struct {
   /* sources */
   int n_srcs;
   char fname_nz_srcs[CG_NPOP_MAX][256], fname_bz_srcs[CG_NPOP_MAX][256];
-  int lensing_srcs[CG_NPOP_MAX], skw_srcs[CG_NPOP_MAX], nside_count[CG_NPOP_MAX];
+  int lensing_srcs[CG_NPOP_MAX], skw_srcs[CG_NPOP_MAX], skw_gauss[CG_NPOP_MAX], nside_count[CG_NPOP_MAX];
   double *srcs_nz_arr[CG_NPOP_MAX], *srcs_bz_arr[CG_NPOP_MAX];
   /* intensity maps */
   int n_imap;
@@ -111,10 +111,26 @@ double cg_integrate(double (*f)(double, void *), void *par, double a, double b, 
 /* One HEALPix map (RING, 12 nside^2 floats) as a FITS binary table with the
  * keywords of he_write_healpix_map (src/healpix_extra.c:4-57). */
 int cg_write_healpix_map(const char *fname, const float *map, long nside);
+/* Skewers appended to a FITS catalogue (write_catalog, src/io.c:1140-1189):
+ * dens and vel hold nsrc x nr values; r, z, d1, v1 the background at the nr
+ * step centres; sigma_g the standard deviation of the Gaussian field. */
+typedef struct {
+  int nr, gauss;
+  const float *dens, *vel;
+  const float *r, *z, *d1, *v1;
+  float sigma_g;
+} cg_skewer_set;
 /* Catalogue of population ipop from Src records (9 floats per source) as
- * <prefix>_srcs_s<ipop+1>_0.fits (columns TYPE, RA, DEC, Z_COSMO, DZ_RSD) or
- * .txt, as write_catalog (src/io.c:1069-1236) without lensing columns. */
-int cg_write_catalog(const char *prefix, int ipop, int format, const float *src9, long long n);
+ * <prefix>_srcs_s<ipop+1>_0.fits (columns TYPE, RA, DEC, Z_COSMO, DZ_RSD,
+ * and E1, E2, KAPPA, DRA, DDEC with has_lensing) or .txt, as write_catalog
+ * (src/io.c:1069-1236).  skw (FITS only, may be NULL) appends the skewer
+ * images and the background table. */
+int cg_write_catalog(const char *prefix, int ipop, int format, const float *src9, long long n, int has_lensing,
+                     const cg_skewer_set *skw);
+/* Background at the skewer step centres r_i = (i + 0.5) r_max / nr: z, the
+ * growth factor and the velocity growth (get_bg, src/cosmo.c:40-86), as
+ * write_catalog tabulates them (src/io.c:1166-1176). */
+int cg_skewer_background(const cg_params *p, int nr, float *r, float *z, float *d1, float *v1);
 /* <prefix>_dens_<tag>_0.dat from a padded [N][N][2(N/2+1)] float grid, the
  * layout of write_density_grid (src/io.c:565-595) on one node. */
 int cg_write_density_grid(const char *prefix, const char *tag, const float *grid, int n_grid, double l_box);

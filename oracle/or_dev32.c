@@ -13,6 +13,8 @@
  *   or_kappa32    kappa_get_beam_properties               kappa.c:78-175
  *   or_isw32      isw_get_beam_properties                 isw.c:78-147
  *   or_cstm32     cstm_get_beam_properties                cstm.c:68-145
+ *   or_lens32     source lensing along the line of sight  srcs.c:452-625, 715-723
+ *   or_skw32      source skewers                          srcs.c:509-536, 725-733
  * Tables are rebuilt from the config with the same double->float roundings
  * as the GPU upload.  The Poisson and position streams are the Philox
  * streams of the GPU path (the reference's GSL MT19937 streams depend on the
@@ -592,6 +594,141 @@ int or_cstm32(const cg_config *cfg, int ipop, const float *dens, const float *no
   }
   free(kzd);
   free(kz);
+  s32_free(&s);
+  return 0;
+}
+
+/* direction and last step, as los_setup in srcs.cu */
+static int los32_setup(const S32 *s, const float *pos, int nr, float idr, float *r, float u[3])
+{
+  *r = cg_norm3(pos[0], pos[1], pos[2]);
+  const float ir = CG_DIV(1.0f, *r > 0.001f ? *r : 0.001f);
+  for (int a = 0; a < 3; a++) u[a] = CG_MUL(pos[a], ir);
+  const int k = (int)CG_ADD(CG_MUL(*r, idr), 0.5f);
+  (void)s;
+  return k < nr - 1 ? k : nr - 1;
+}
+
+/* k_src_lensing: writes e1 e2 kappa dra ddec (src9[4..8]) of each source */
+int or_lens32(const cg_config *cfg, const float *npot, long long n, const float *pos4, float *src9)
+{
+  S32 s;
+  s32_init(&s, cfg);
+  const int N = s.N, nr = N / 2;
+  const double dr = cfg->r_max / nr;
+  float *f0 = malloc(2 * (size_t)nr * sizeof(float)), *f1 = f0 + nr;
+  for (int i = 0; i < nr; i++) {
+    const double rm = (i + 0.5) * dr;
+    const double pg = bg64(cfg, cfg->growth_d_arr, 1, cfg->growth_d_arr[CG_NA - 1], rm) *
+                      (1 + bg64(cfg, cfg->z_arr_r2z, 0, cfg->z_arr_r2z[CG_NA - 1], rm));
+    f0[i] = (float)(2 * pg * dr);
+    f1[i] = (float)(rm * pg * dr);
+  }
+  const float drf = (float)dr, idrf = (float)(nr / cfg->r_max);
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < n; i++) {
+    float r, u[3];
+    const int kmax = los32_setup(&s, pos4 + 4 * i, nr, idrf, &r, u);
+    const float ir = CG_DIV(1.0f, r > 0.001f ? r : 0.001f);
+    float ux[3], uy[3], rk[6], re1[6], re2[6];
+    cg_lens_rot(u, CG_MUL(CG_MUL(s.idx, s.idx), ir), CG_MUL(CG_MUL(0.5f, s.idx), ir), ux, uy, rk, re1, re2);
+    float a[5] = {0, 0, 0, 0, 0}, c[5] = {0, 0, 0, 0, 0};
+    for (int k = 0; k <= kmax; k++) {
+      const float rm = CG_MUL(CG_ADD((float)k, 0.5f), drf);
+      const int x0 = cg_ngp_cell(rm, u[0], s.p[0], s.idx, N), y0 = cg_ngp_cell(rm, u[1], s.p[1], s.idx, N),
+                z0 = cg_ngp_cell(rm, u[2], s.p[2], s.idx, N);
+      const int xh = wrapi(x0 + 1, N), xl = wrapi(x0 - 1, N), yh = wrapi(y0 + 1, N), yl = wrapi(y0 - 1, N);
+      const int zh = wrapi(z0 + 1, N), zl = wrapi(z0 - 1, N);
+#define PHI(X, Y, Z) npot[pidx((X), (Y), (Z), N)]
+      const float f[19] = {PHI(x0, y0, z0), PHI(xh, y0, z0), PHI(xl, y0, z0), PHI(x0, yh, z0), PHI(x0, yl, z0),
+                           PHI(x0, y0, zh), PHI(x0, y0, zl), PHI(xh, yh, z0), PHI(xl, yl, z0), PHI(xh, yl, z0),
+                           PHI(xl, yh, z0), PHI(xh, y0, zh), PHI(xl, y0, zl), PHI(xh, y0, zl), PHI(xl, y0, zh),
+                           PHI(x0, yh, zh), PHI(x0, yl, zl), PHI(x0, yh, zl), PHI(x0, yl, zh)};
+#undef PHI
+      float t[6];
+      cg_tidal(f, t);
+      const float v[3] = {CG_SUB(f[1], f[2]), CG_SUB(f[3], f[4]), CG_SUB(f[5], f[6])};
+      const float dd = CG_SUB(r, rm);
+      const float fr = CG_MUL(f1[k], dd), frm = CG_MUL(f0[k], dd);
+      cg_kahan_add(&a[0], &c[0], CG_MUL(cg_dot6(re1, t), fr));
+      cg_kahan_add(&a[1], &c[1], CG_MUL(cg_dot6(re2, t), fr));
+      cg_kahan_add(&a[2], &c[2], CG_MUL(cg_dot6(rk, t), fr));
+      cg_kahan_add(&a[3], &c[3], CG_MUL(cg_dot3(ux, v), frm));
+      cg_kahan_add(&a[4], &c[4], CG_MUL(cg_dot3(uy, v), frm));
+    }
+    float *q = src9 + 9 * i;
+    q[4] = a[0];
+    q[5] = a[1];
+    q[6] = a[2];
+    q[7] = CG_MUL(a[4], 57.2957795f);
+    q[8] = CG_MUL(a[3], 57.2957795f);
+  }
+  free(f0);
+  s32_free(&s);
+  return 0;
+}
+
+/* k_src_skewers: nr values per source of the density (or Gaussian field)
+ * and the scaled radial velocity, 0 beyond the source's last step */
+int or_skw32(const cg_config *cfg, const float *dens, const float *npot, int gauss, float sigma2f, long long n,
+             const float *pos4, float *dout, float *vout)
+{
+  S32 s;
+  s32_init(&s, cfg);
+  const int N = s.N, nr = N / 2;
+  const double dr = cfg->r_max / nr;
+  const double fv = -cfg->fgrowth_0 / (1.5 * cfg->hubble_0 * cfg->omega_m);
+  float *vf = malloc((size_t)nr * sizeof(float));
+  for (int i = 0; i < nr; i++)
+    vf[i] = (float)(bg64(cfg, cfg->growth_v_arr, cfg->growth_v_arr[0], cfg->growth_v_arr[CG_NA - 1], (i + 0.5) * dr) *
+                    fv);
+  const float drf = (float)dr, idrf = (float)(nr / cfg->r_max);
+  const T32 d1 = s.d1;
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < n; i++) {
+    float r, u[3];
+    const int kmax = los32_setup(&s, pos4 + 4 * i, nr, idrf, &r, u);
+    float *od = dout + (size_t)i * nr, *ov = vout + (size_t)i * nr;
+    for (int k = 0; k <= kmax; k++) {
+      const float rm = CG_MUL(CG_ADD((float)k, 0.5f), drf);
+      int i0[3], i1[3];
+      float h0[3], h1[3];
+      for (int a = 0; a < 3; a++) cg_cic_axis(rm, u[a], s.p[a], s.idx, N, &i0[a], &i1[a], &h0[a], &h1[a]);
+      float d;
+      if (gauss) {
+        float gv[8];
+        for (int b = 0; b < 8; b++) {
+          const int ix = (b & 1) ? i1[0] : i0[0], iy = (b & 2) ? i1[1] : i0[1], iz = (b & 4) ? i1[2] : i0[2];
+          const float rc = cg_norm3(cg_cell_coord(ix, s.dx, s.p[0]), cg_cell_coord(iy, s.dx, s.p[1]),
+                                    cg_cell_coord(iz, s.dx, s.p[2]));
+          gv[b] = cg_gauss_of_dens(dens[pidx(ix, iy, iz, N)], bg32(&s, d1, rc), sigma2f);
+        }
+        d = cg_cic_combine(gv, h0, h1);
+      } else {
+        d = cg_cic_value(dens, i0, i1, h0, h1, N);
+      }
+      float v[3] = {0.0f, 0.0f, 0.0f};
+      for (int hz = 0; hz < 2; hz++) {
+        const int zc = hz ? i1[2] : i0[2];
+        const float wz = hz ? h0[2] : h1[2];
+        float acc[3] = {0.0f, 0.0f, 0.0f};
+        for (int k2 = 0; k2 < 4; k2++) {
+          const int yc = (k2 & 2) ? i1[1] : i0[1], xc = (k2 & 1) ? i1[0] : i0[0];
+          const float w = CG_MUL(CG_MUL(wz, (k2 & 2) ? h0[1] : h1[1]), (k2 & 1) ? h0[0] : h1[0]);
+          float g[3];
+          grad32(npot, xc, yc, zc, N, g);
+          for (int a = 0; a < 3; a++) acc[a] = CG_FMA(g[a], w, acc[a]);
+        }
+        for (int a = 0; a < 3; a++) v[a] = CG_ADD(v[a], acc[a]);
+      }
+      const float vr =
+          CG_MUL(CG_MUL(0.5f, s.idx), CG_ADD(CG_ADD(CG_MUL(v[0], u[0]), CG_MUL(v[1], u[1])), CG_MUL(v[2], u[2])));
+      od[k] = d;
+      ov[k] = CG_MUL(vr, vf[k]);
+    }
+    for (int k = kmax + 1; k < nr; k++) od[k] = ov[k] = 0.0f;
+  }
+  free(vf);
   s32_free(&s);
   return 0;
 }

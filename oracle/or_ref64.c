@@ -15,6 +15,8 @@
  *   or_isw64         isw_get_beam_properties       isw.c:78-147
  *   or_cstm_steps    custom-map step tables        cstm.c:81-116
  *   or_cstm64        cstm_get_beam_properties      cstm.c:68-145
+ *   or_lens64        source lensing along the LOS  srcs.c:452-625, 715-723
+ *   or_skw64         source skewers                srcs.c:509-536, 725-733
  *   or_run_mock64    the driver sequence of main.c:66-125 for timing.
  * Random numbers: the Philox streams of the GPU path (uniforms identical
  * bit for bit), since GSL's MT19937 streams cannot be reproduced here.
@@ -844,3 +846,160 @@ int or_cstm64(const cg_config *c, int ipop, const double *dens, const double *no
   free(kz);
   return 0;
 }
+
+/* per-source direction and last step of srcs_get_beam_properties_single
+ * (srcs.c:485-493, 583): r from the float position, u = pos / max(r, 0.001) */
+static int los64_setup(const cg_config *c, const float *pos, double *r, double u[3])
+{
+  const int nr = c->n_grid / 2;
+  const double idr = nr / c->r_max;
+  *r = sqrt((double)pos[0] * pos[0] + (double)pos[1] * pos[1] + (double)pos[2] * pos[2]);
+  const double ir = 1. / (*r > 0.001 ? *r : 0.001);
+  for (int a = 0; a < 3; a++) u[a] = pos[a] * ir;
+  const int k = (int)(*r * idr + 0.5);
+  return k < nr - 1 ? k : nr - 1;
+}
+
+#define P64(G, X, Y, Z) (G)[(X) + (size_t)N * ((Y) + (size_t)N * (Z))]
+
+/* srcs_get_beam_properties_single, lensing branch without _USE_FAST_LENSING
+ * (srcs.c:465-478, 536-625), and the degree conversion of the deflections in
+ * srcs_beams_postproc_single (srcs.c:721-722).  npot: N^3 unpadded;
+ * pos4: 4 floats per source; out: 5 per source (e1, e2, kappa, dra, ddec). */
+int or_lens64(const cg_config *c, const double *p, long long n, const float *pos4, double *out)
+{
+  const int N = c->n_grid, nr = N / 2;
+  const double dr = c->r_max / nr, idx = N / c->l_box;
+  double *f0 = malloc(3 * (size_t)nr * sizeof(double)), *f1 = f0 + nr, *f2 = f1 + nr;
+  for (int i = 0; i < nr; i++) {
+    const double rm = (i + 0.5) * dr, pg = BG_D1(c, rm) * (1 + BG_Z(c, rm));
+    f0[i] = pg * dr;
+    f1[i] = rm * pg * dr;
+    f2[i] = rm * rm * pg * dr;
+  }
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < n; i++) {
+    double r, u[3];
+    const int kmax = los64_setup(c, pos4 + 4 * i, &r, u);
+    const double ir = 1. / (r > 0.001 ? r : 0.001);
+    double cth = u[2] >= 1 ? 1 : (u[2] <= -1 ? -1 : u[2]), sth = sqrt((1 - cth) * (1 + cth)), cph = 1, sph = 0;
+    if (sth != 0) {
+      cph = u[0] / sth;
+      sph = u[1] / sth;
+    }
+    const double pf = idx * idx * ir, pm = 0.5 * idx * ir;
+    const double ux[3] = {cth * cph * pm, cth * sph * pm, -sth * pm}, uy[3] = {-sph * pm, cph * pm, 0};
+    const double rk[6] = {(cth * cth * cph * cph + sph * sph) * pf, (2 * cph * sph * (cth * cth - 1)) * pf,
+                          (-2 * cth * sth * cph) * pf,            (cth * cth * sph * sph + cph * cph) * pf,
+                          (-2 * cth * sth * sph) * pf,            (sth * sth) * pf};
+    const double re1[6] = {(cth * cth * cph * cph - sph * sph) * pf, (2 * cph * sph * (cth * cth + 1)) * pf,
+                           (-2 * cth * sth * cph) * pf,            (cth * cth * sph * sph - cph * cph) * pf,
+                           (-2 * cth * sth * sph) * pf,            (sth * sth) * pf};
+    const double re2[6] = {(-2 * cth * cph * sph) * pf, (2 * cth * (cph * cph - sph * sph)) * pf,
+                           (2 * sth * sph) * pf,        (2 * cth * sph * cph) * pf,
+                           (-2 * sth * cph) * pf,       0};
+    double e1 = 0, e2 = 0, kp = 0, dtx = 0, dty = 0;
+    for (int k = 0; k <= kmax; k++) {
+      const double rm = (k + 0.5) * dr;
+      int cc[3];
+      for (int a = 0; a < 3; a++) {
+        long q = (long)((rm * u[a] + c->pos_obs[a]) * idx + 0.5);
+        cc[a] = (int)(q >= N ? q - N : (q < 0 ? q + N : q));
+      }
+      const int x0 = cc[0], y0 = cc[1], z0 = cc[2];
+      const int xh = (x0 + 1) % N, xl = (x0 + N - 1) % N, yh = (y0 + 1) % N, yl = (y0 + N - 1) % N,
+                zh = (z0 + 1) % N, zl = (z0 + N - 1) % N;
+      double t[6], v[3];
+      v[0] = P64(p, xh, y0, z0) - P64(p, xl, y0, z0);
+      v[1] = P64(p, x0, yh, z0) - P64(p, x0, yl, z0);
+      v[2] = P64(p, x0, y0, zh) - P64(p, x0, y0, zl);
+      t[0] = P64(p, xh, y0, z0) + P64(p, xl, y0, z0) - 2 * P64(p, x0, y0, z0);
+      t[3] = P64(p, x0, yh, z0) + P64(p, x0, yl, z0) - 2 * P64(p, x0, y0, z0);
+      t[5] = P64(p, x0, y0, zh) + P64(p, x0, y0, zl) - 2 * P64(p, x0, y0, z0);
+      t[1] = 0.25 * (P64(p, xh, yh, z0) + P64(p, xl, yl, z0) - P64(p, xh, yl, z0) - P64(p, xl, yh, z0));
+      t[2] = 0.25 * (P64(p, xh, y0, zh) + P64(p, xl, y0, zl) - P64(p, xh, y0, zl) - P64(p, xl, y0, zh));
+      t[4] = 0.25 * (P64(p, x0, yh, zh) + P64(p, x0, yl, zl) - P64(p, x0, yh, zl) - P64(p, x0, yl, zh));
+      const double fr = f1[k] * r - f2[k], frm = 2 * (f0[k] * r - f1[k]);
+      double d1 = 0, d2 = 0, dk = 0, dvx = 0, dvy = 0;
+      for (int a = 0; a < 6; a++) {
+        d1 += re1[a] * t[a];
+        d2 += re2[a] * t[a];
+        dk += rk[a] * t[a];
+      }
+      for (int a = 0; a < 3; a++) {
+        dvx += ux[a] * v[a];
+        dvy += uy[a] * v[a];
+      }
+      e1 += d1 * fr;
+      e2 += d2 * fr;
+      kp += dk * fr;
+      dtx += dvx * frm;
+      dty += dvy * frm;
+    }
+    double *o = out + 5 * i;
+    o[0] = e1;
+    o[1] = e2;
+    o[2] = kp;
+    o[3] = dty * (180. / M_PI);
+    o[4] = dtx * (180. / M_PI);
+  }
+  free(f0);
+  return 0;
+}
+
+/* Skewers (srcs.c:509-536 with INTERP_TYPE_SKW = CIC, beaming.c:183-265; the
+ * velocity scaling of srcs.c:725-733): density (or, with gauss, the
+ * Gaussian field log(1 + d)/D(r_cell) + D(r_cell) sigma^2/2 of each corner
+ * cell, beaming.c:54-66) and the radial velocity times V1(rm) factor_vel at
+ * every step up to the source, 0 beyond.  dens, npot: N^3 unpadded. */
+int or_skw64(const cg_config *c, const double *dens, const double *p, int gauss, double sigma2, long long n,
+             const float *pos4, double *dout, double *vout)
+{
+  const int N = c->n_grid, nr = N / 2;
+  const double dr = c->r_max / nr, idx = N / c->l_box, dx = c->l_box / N;
+  const double fv = -c->fgrowth_0 / (1.5 * c->hubble_0 * c->omega_m);
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < n; i++) {
+    double r, u[3];
+    const int kmax = los64_setup(c, pos4 + 4 * i, &r, u);
+    double *od = dout + (size_t)i * nr, *ov = vout + (size_t)i * nr;
+    for (int k = 0; k < nr; k++) od[k] = ov[k] = 0;
+    for (int k = 0; k <= kmax; k++) {
+      const double rm = (k + 0.5) * dr;
+      long i0[3], i1[3];
+      double h0[3], h1[3];
+      for (int a = 0; a < 3; a++) {
+        const double x = (rm * u[a] + c->pos_obs[a]) * idx;
+        i0[a] = (long)x;
+        h0[a] = x - i0[a];
+        h1[a] = 1 - h0[a];
+        i1[a] = i0[a] + 1;
+        if (i0[a] >= N) i0[a] -= N;
+        else if (i0[a] < 0) i0[a] += N;
+        if (i1[a] >= N) i1[a] -= N;
+        else if (i1[a] < 0) i1[a] += N;
+      }
+      double d = 0, v[3] = {0, 0, 0};
+      for (int b = 0; b < 8; b++) {
+        const long ix = (b & 1) ? i1[0] : i0[0], iy = (b & 2) ? i1[1] : i0[1], iz = (b & 4) ? i1[2] : i0[2];
+        const double w = ((b & 4) ? h0[2] : h1[2]) * ((b & 2) ? h0[1] : h1[1]) * ((b & 1) ? h0[0] : h1[0]);
+        double val = P64(dens, ix, iy, iz);
+        if (gauss) {
+          const double x0 = ix * dx - c->pos_obs[0], y0 = iy * dx - c->pos_obs[1], z0 = iz * dx - c->pos_obs[2];
+          const double dg = BG_D1(c, sqrt(x0 * x0 + y0 * y0 + z0 * z0));
+          val = log(1 + val) / dg + dg * sigma2 * 0.5;
+        }
+        d += val * w;
+        const long xh = (ix + 1) % N, xl = (ix + N - 1) % N, yh = (iy + 1) % N, yl = (iy + N - 1) % N,
+                   zh = (iz + 1) % N, zl = (iz + N - 1) % N;
+        v[0] += (P64(p, xh, iy, iz) - P64(p, xl, iy, iz)) * w;
+        v[1] += (P64(p, ix, yh, iz) - P64(p, ix, yl, iz)) * w;
+        v[2] += (P64(p, ix, iy, zh) - P64(p, ix, iy, zl)) * w;
+      }
+      od[k] = d;
+      ov[k] = 0.5 * idx * (v[0] * u[0] + v[1] * u[1] + v[2] * u[2]) * BG_V1(c, rm) * fv;
+    }
+  }
+  return 0;
+}
+#undef P64

@@ -50,6 +50,9 @@ int or_isw64(const cg_config *cfg, const double *npot, double *map);
 int or_cstm_steps(const cg_config *cfg, int ipop, double *kz, double *bz, int *ir_min, int *ir_max);
 int or_cstm64(const cg_config *cfg, int ipop, const double *dens, const double *normtab, double n0, double nf,
               double *map);
+int or_lens64(const cg_config *cfg, const double *npot, long long n, const float *pos4, double *out);
+int or_skw64(const cg_config *cfg, const double *dens, const double *npot, int gauss, double sigma2, long long n,
+             const float *pos4, double *dout, double *vout);
 int or_imap64(const cg_config *cfg, int ipop, const double *dens, const double *npot, const double *normtab,
               double n0, double nf, double *data, int *nadd);
 int or_imap64_part(const cg_config *cfg, int ipop, const double *dens, const double *npot, const double *normtab,
@@ -74,5 +77,8 @@ int or_kappa32(const cg_config *cfg, const float *npot, float *map);
 int or_isw32(const cg_config *cfg, const float *npot, float *map);
 int or_cstm32(const cg_config *cfg, int ipop, const float *dens, const float *normtab, float n0, float nf,
               float *map);
+int or_lens32(const cg_config *cfg, const float *npot, long long n, const float *pos4, float *src9);
+int or_skw32(const cg_config *cfg, const float *dens, const float *npot, int gauss, float sigma2f, long long n,
+             const float *pos4, float *dout, float *vout);
 
 #endif

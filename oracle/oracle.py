@@ -37,7 +37,10 @@ def lib():
             "or_beam_rsd32": [vp, vp, C.c_longlong, vp, vp], "or_imap32": [vp, i, vp, vp, vp, f, f, vp, vp],
             "or_kappa32": [vp, vp, vp], "or_isw32": [vp, vp, vp], "or_isw64": [vp, vp, vp],
             "or_cstm_steps": [vp, i, vp, vp, vp, vp], "or_cstm64": [vp, i, vp, vp, d, d, vp],
-            "or_cstm32": [vp, i, vp, vp, f, f, vp], "or_c2r_3d": [i, vp, vp], "or_r2c_3d": [i, vp, vp],
+            "or_cstm32": [vp, i, vp, vp, f, f, vp],
+            "or_lens64": [vp, vp, C.c_longlong, vp, vp], "or_lens32": [vp, vp, C.c_longlong, vp, vp],
+            "or_skw64": [vp, vp, vp, i, d, C.c_longlong, vp, vp, vp],
+            "or_skw32": [vp, vp, vp, i, f, C.c_longlong, vp, vp, vp], "or_c2r_3d": [i, vp, vp], "or_r2c_3d": [i, vp, vp],
             "or_vec_expf": [vp, vp, C.c_long], "or_vec_logf": [vp, vp, C.c_long],
             "or_vec_log1pf": [vp, vp, C.c_long], "or_vec_acosf": [vp, vp, C.c_long],
             "or_vec_atan2f": [vp, vp, vp, C.c_long], "or_vec_sincosf": [vp, vp, vp, C.c_long],
@@ -251,6 +254,42 @@ def cstm32(cfg, ipop, dens, tab, e):
     assert lib().or_cstm32(cfgp(cfg), ipop, P(dens), P(np.ascontiguousarray(tab, np.float32)), float(e[0]),
                            float(e[1]), P(m)) == 0
     return m
+
+
+def lens64(cfg, npot, pos4):
+    """(n, 5): e1, e2, kappa, dra, ddec of each source in double precision."""
+    pos4 = np.ascontiguousarray(pos4, np.float32).reshape(-1, 4)
+    out = np.empty((len(pos4), 5))
+    assert lib().or_lens64(cfgp(cfg), P(np.ascontiguousarray(npot, np.float64)), len(pos4), P(pos4), P(out)) == 0
+    return out
+
+
+def lens32(cfg, npot, pos4, src9):
+    """src9 with columns 4..8 replaced by the FP32 lensing restatement."""
+    pos4 = np.ascontiguousarray(pos4, np.float32).reshape(-1, 4)
+    out = np.array(src9, np.float32, copy=True).reshape(-1, 9)
+    assert lib().or_lens32(cfgp(cfg), P(npot), len(pos4), P(pos4), P(out)) == 0
+    return out
+
+
+def skw64(cfg, dens, npot, gauss, sigma2, pos4):
+    pos4 = np.ascontiguousarray(pos4, np.float32).reshape(-1, 4)
+    nr = cfg.n_grid // 2
+    d = np.empty((len(pos4), nr))
+    v = np.empty((len(pos4), nr))
+    assert lib().or_skw64(cfgp(cfg), P(np.ascontiguousarray(dens, np.float64)), P(np.ascontiguousarray(npot, np.float64)),
+                          int(gauss), float(sigma2), len(pos4), P(pos4), P(d), P(v)) == 0
+    return d, v
+
+
+def skw32(cfg, dens, npot, gauss, sigma2f, pos4):
+    pos4 = np.ascontiguousarray(pos4, np.float32).reshape(-1, 4)
+    nr = cfg.n_grid // 2
+    d = np.empty((len(pos4), nr), np.float32)
+    v = np.empty((len(pos4), nr), np.float32)
+    assert lib().or_skw32(cfgp(cfg), P(dens), P(npot), int(gauss), float(sigma2f), len(pos4), P(pos4), P(d),
+                          P(v)) == 0
+    return d, v
 
 
 def kappa32(cfg, npot):

@@ -31,7 +31,8 @@ N_SMALL = 64
 def _spec(kind):
     from colore_gb300 import inputs
     base = dict(n_grid=N_SMALL, z_min=0.05, z_max=0.6, r_smooth=2.0, seed=7, dens_type=0, bias_model=2,
-                srcs=[dict(nz=("gauss", 0.3, 0.1), density=200.0, bias=("1+z",), nside_count=16),
+                srcs=[dict(nz=("gauss", 0.3, 0.1), density=200.0, bias=("1+z",), nside_count=16, lensing=True,
+                           skewers=True),
                       dict(nz=("flat", 0.1, 0.5), density=4.0, bias=("const", 2.0), nside_count=8)],
                 imap=[dict(tz=0.1, bias=("const", 1.0), z_range=(0.1, 0.5), nbands=6, nside=16)],
                 kappa=dict(z_out=[0.2, 0.4, 0.55], nside=16),
@@ -67,6 +68,12 @@ def _spec(kind):
         # pass), the outer ones nsub ~ 3 (painted in place)
         base["seed"] = 29
         base["imap"] = [dict(tz=0.1, bias=("const", 1.0), z_range=(0.05, 0.5), nbands=6, nside=64)]
+        base.pop("kappa")
+    elif kind == "skwg":
+        # Gaussian skewers and lensing on the second population
+        base["seed"] = 31
+        base["srcs"] = [base["srcs"][1]]
+        base["srcs"][0].update(lensing=True, skewers=True, gaussian_skewers=True, density=30.0)
         base.pop("kappa")
     elif kind == "clip":
         base["dens_type"] = 3
@@ -122,6 +129,7 @@ class Run:
         self.kappa = m.kappa() if self.cfg.do_kappa else None
         self.isw = m.isw() if self.cfg.do_isw else None
         self.cstm = [m.custom(i) for i in range(self.cfg.n_cstm)]
+        self.skw = [m.skewers(i) if self.cfg.skw_srcs[i] else None for i in range(self.cfg.n_srcs)]
 
 
 _RUNS = {}
@@ -309,14 +317,54 @@ def test_sources_bitexact(runs, kind):
             assert r.need('cmaps')[ip].sum() == r.need('nsrc')[ip]
 
 
-@pytest.mark.parametrize("kind", ["full", "lpt"])
+@pytest.mark.parametrize("kind", ["full", "lpt", "skwg"])
 def test_beam_rsd_bitexact(runs, kind):
+    """RSD at the sources, and with include_lensing the shear, convergence and
+    deflection integrated to each source, bit for bit."""
     import oracle as orc
     r = runs(kind)
     assert r.cfg.need_beaming
     for ip in range(r.cfg.n_srcs):
-        s = orc.beam_rsd32(r.cfg, r.phi, r.need('cats')[ip]["pos"], r.need('cats')[ip]["src"])
+        pos = r.need('cats')[ip]["pos"]
+        s = orc.beam_rsd32(r.cfg, r.phi, pos, r.need('cats')[ip]["src"])
+        if r.cfg.lensing_srcs[ip]:
+            s = orc.lens32(r.cfg, r.phi, pos, s)
         assert np.array_equal(s.view(np.uint32), r.need('cats_beam')[ip]["src"].view(np.uint32))
+
+
+@pytest.mark.parametrize("kind", ["full", "skwg"])
+def test_source_lensing_vs_fp64(runs, kind):
+    """Source lensing (srcs.c:536-625) against the FP64 restatement of the
+    reference on the same potential: relative rms 2e-3 per quantity (the
+    nearest cell of a step can differ between FP32 and FP64 positions)."""
+    import oracle as orc
+    r = runs(kind)
+    ip = [i for i in range(r.cfg.n_srcs) if r.cfg.lensing_srcs[i]][0]
+    got = r.need('cats_beam')[ip]["src"][:, 4:9].astype(np.float64)
+    assert len(got) > 100
+    ref = orc.lens64(r.cfg, unpad(r.phi).astype(np.float64), r.need('cats')[ip]["pos"])
+    for j in range(5):
+        assert rel_rms(got[:, j], ref[:, j]) < 2e-3, (j, rel_rms(got[:, j], ref[:, j]))
+
+
+@pytest.mark.parametrize("kind", ["full", "skwg"])
+def test_skewers_bitexact_and_fp64(runs, kind):
+    """Density (or Gaussian) and velocity skewers (srcs.c:509-536, 725-733):
+    bit-exact against the FP32 restatement, relative rms 1e-4 against FP64."""
+    import oracle as orc
+    r = runs(kind)
+    ip = [i for i in range(r.cfg.n_srcs) if r.cfg.skw_srcs[i]][0]
+    gauss = r.cfg.skw_gauss[ip]
+    assert gauss == (kind == "skwg")
+    d, v = r.need('skw')[ip]
+    pos = r.need('cats')[ip]["pos"]
+    assert d.shape == (len(pos), r.cfg.n_grid // 2) and np.all(np.isfinite(d))
+    d32, v32 = orc.skw32(r.cfg, r.need('d'), r.phi, gauss, np.float32(r.s2), pos)
+    assert np.array_equal(d32.view(np.uint32), d.view(np.uint32))
+    assert np.array_equal(v32.view(np.uint32), v.view(np.uint32))
+    d64, v64 = orc.skw64(r.cfg, unpad(r.need('d')).astype(np.float64), unpad(r.phi).astype(np.float64), gauss,
+                         r.s2, pos)
+    assert rel_rms(d, d64) < 1e-4 and rel_rms(v, v64) < 1e-4
 
 
 @pytest.mark.parametrize("kind", ["full", "nobeam", "lpt", "ptrs"])

@@ -37,7 +37,7 @@ def read_fits(fname):
         pos = (pos + 2879) // 2880 * 2880
         nbytes = 0
         if hdr.get("NAXIS", 0) > 0:
-            nbytes = hdr["NAXIS1"] * hdr["NAXIS2"]
+            nbytes = abs(hdr["BITPIX"]) // 8 * hdr["NAXIS1"] * hdr["NAXIS2"]
         hdr["_order"] = order
         hdus.append((hdr, raw[pos:pos + nbytes]))
         pos += (nbytes + 2879) // 2880 * 2880
