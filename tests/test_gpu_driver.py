@@ -17,7 +17,8 @@ pytestmark = pytest.mark.gpu
 def _spec(fmt):
     return dict(n_grid=64, z_min=0.05, z_max=0.6, r_smooth=2.0, seed=53, dens_type=0, bias_model=2,
                 output_format=fmt, output_density=True,
-                srcs=[dict(nz=("gauss", 0.3, 0.1), density=50.0, bias=("1+z",), nside_count=8)],
+                srcs=[dict(nz=("gauss", 0.3, 0.1), density=50.0, bias=("1+z",), nside_count=8, lensing=True,
+                           skewers=True)],
                 imap=[dict(tz=0.1, bias=("const", 1.0), z_range=(0.1, 0.5), nbands=3, nside=8)],
                 kappa=dict(z_out=[0.3, 0.5], nside=8),
                 isw=dict(z_out=[0.4], nside=8),
@@ -51,14 +52,20 @@ def test_driver_outputs_match_library(built, tmp_path, fmt):
             assert np.array_equal(body, g1[:, :, :n])
     src = m.catalog(0, pos=False, ipix=False)["src"]
     if fmt == "FITS":
-        (_, _), (h, d) = read_fits(prefix + "_srcs_s1_0.fits")
-        rows = np.frombuffer(d, np.dtype([("t", ">i4"), ("c", ">f4", (4,))]))
-        assert h["NAXIS2"] == len(src)
-        assert np.array_equal(rows["c"], src[:, :4])
+        hdus = read_fits(prefix + "_srcs_s1_0.fits")
+        (h, d) = hdus[1]
+        rows = np.frombuffer(d, np.dtype([("t", ">i4"), ("c", ">f4", (9,))]))
+        assert h["NAXIS2"] == len(src) and h["TFIELDS"] == 10
+        assert np.array_equal(rows["c"], src)
+        sd, sv = m.skewers(0)
+        assert hdus[2][0]["CONTENTS"] == "density skewers" and hdus[3][0]["CONTENTS"] == "velocity skewers"
+        assert np.array_equal(np.frombuffer(hdus[2][1], ">f4").reshape(sd.shape), sd)
+        assert np.array_equal(np.frombuffer(hdus[3][1], ">f4").reshape(sv.shape), sv)
+        assert hdus[4][0]["NAXIS2"] == n // 2
     else:
         a = np.loadtxt(prefix + "_srcs_s1_0.txt", ndmin=2)
         assert a.shape[0] == len(src)
-        np.testing.assert_allclose(a[:, 1:5], src[:, :4], rtol=1e-6, atol=1e-12)
+        np.testing.assert_allclose(a[:, 1:10], src, rtol=1e-6, atol=1e-12)
     (_, _), (h, d) = read_fits(prefix + "_srcs_s1_counts.fits")
     assert np.array_equal(np.frombuffer(d, ">f4"), m.count_map(0).astype(np.float32))
     im = m.imap(0)

@@ -350,7 +350,9 @@ def test_source_lensing_vs_fp64(runs, kind):
 @pytest.mark.parametrize("kind", ["full", "skwg"])
 def test_skewers_bitexact_and_fp64(runs, kind):
     """Density (or Gaussian) and velocity skewers (srcs.c:509-536, 725-733):
-    bit-exact against the FP32 restatement, relative rms 1e-4 against FP64."""
+    bit-exact against the FP32 restatement.  Against FP64, a source whose
+    r/dr + 1/2 lies within rounding of an integer ends one step earlier or
+    later (a few in 1e6); the others agree to relative rms 2e-5."""
     import oracle as orc
     r = runs(kind)
     ip = [i for i in range(r.cfg.n_srcs) if r.cfg.skw_srcs[i]][0]
@@ -364,7 +366,9 @@ def test_skewers_bitexact_and_fp64(runs, kind):
     assert np.array_equal(v32.view(np.uint32), v.view(np.uint32))
     d64, v64 = orc.skw64(r.cfg, unpad(r.need('d')).astype(np.float64), unpad(r.phi).astype(np.float64), gauss,
                          r.s2, pos)
-    assert rel_rms(d, d64) < 1e-4 and rel_rms(v, v64) < 1e-4
+    same_end = np.all((d != 0) == (d64 != 0), axis=1)
+    assert (~same_end).sum() <= 1e-5 * len(pos) + 4, (~same_end).sum()
+    assert rel_rms(d[same_end], d64[same_end]) < 2e-5 and rel_rms(v[same_end], v64[same_end]) < 2e-5
 
 
 @pytest.mark.parametrize("kind", ["full", "nobeam", "lpt", "ptrs"])
