@@ -84,6 +84,15 @@ def lib():
             "cg_last_error": (C.c_char_p, [vp]),
             "cg_set_stream": (C.c_int, [vp, vp]),
             "cg_sync": (C.c_int, [vp]),
+            "cg_graph_capture": (C.c_int, [vp]),
+            "cg_graph_launch": (C.c_int, [vp, vp]),
+            "cg_batch_create": (C.c_int, [C.POINTER(vp), C.c_int, vp, C.c_int, C.c_int]),
+            "cg_batch_run": (C.c_int, [vp, C.POINTER(C.c_float)]),
+            "cg_batch_streams": (C.c_int, [vp]),
+            "cg_batch_tuning": (C.c_int, [vp, C.POINTER(C.c_float), C.c_int]),
+            "cg_batch_context": (vp, [vp, C.c_int]),
+            "cg_batch_last_error": (C.c_char_p, [vp]),
+            "cg_batch_destroy": (None, [vp]),
             "cg_memory_estimate": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_ulonglong)]),
             "cg_upload_tables": (C.c_int, [vp, C.POINTER(Config)]),
             "cg_create_cartesian_fields": (C.c_int, [vp]),
@@ -145,7 +154,9 @@ def exported_symbols():
             "cg_num_sources", "cg_download_catalog", "cg_download_count_map", "cg_download_imap",
             "cg_download_kappa", "cg_download_isw", "cg_download_custom", "cg_download_skewers", "cg_download_norm", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_read_run_params",
             "cg_params_free", "cg_params_to_config", "cg_write_healpix_map", "cg_write_catalog",
-            "cg_write_density_grid", "cg64_create", "cg64_destroy", "cg64_last_error",
+            "cg_write_density_grid", "cg_graph_capture", "cg_graph_launch", "cg_batch_create", "cg_batch_run",
+            "cg_batch_streams", "cg_batch_tuning", "cg_batch_context", "cg_batch_last_error", "cg_batch_destroy",
+            "cg_skewer_background", "cg64_create", "cg64_destroy", "cg64_last_error",
             "cg64_run_mock", "cg64_num_sources", "cg64_download"]
 
 
@@ -227,10 +238,14 @@ def grid_shape(n):
 class Mock:
     """One GPU context running CoLoRe's stages (cg_* C ABI)."""
 
-    def __init__(self, params, device=0):
+    def __init__(self, params, device=0, _handle=None):
         self.params = params
         self.cfg = params.config
         L = lib()
+        self._owned = _handle is None
+        if _handle is not None:  # a context owned by a Batch
+            self._c = C.c_void_p(_handle)
+            return
         self._c = C.c_void_p()
         rc = L.cg_create(C.byref(self._c), C.byref(self.cfg), device)
         if rc:
@@ -242,8 +257,17 @@ class Mock:
 
     def close(self):
         if getattr(self, "_c", None):
-            lib().cg_destroy(self._c)
+            if self._owned:
+                lib().cg_destroy(self._c)
             self._c = None
+
+    def graph_capture(self):
+        """Capture fields, density, normalisation and sources into a CUDA graph."""
+        self._chk(lib().cg_graph_capture(self._c), "cg_graph_capture")
+
+    def graph_launch(self, stream_handle=None):
+        self._chk(lib().cg_graph_launch(self._c, C.c_void_p(stream_handle) if stream_handle else None),
+                  "cg_graph_launch")
 
     def __del__(self):
         try:
@@ -392,6 +416,55 @@ class Mock:
         e = np.empty(2, np.float32)
         self._chk(lib().cg_download_norm(self._c, kind, ipop, t.ctypes.data, e.ctypes.data), "download_norm")
         return t, e
+
+
+class Batch:
+    """Independent realisations run as graph replays over several streams
+    (cg_batch_* C ABI).  nstreams = 0 autotunes the stream count."""
+
+    def __init__(self, params_list, device=0, nstreams=0):
+        self.params = list(params_list)
+        n = len(self.params)
+        self._cfgs = (Config * n)(*[p.config for p in self.params])
+        self._b = C.c_void_p()
+        L = lib()
+        rc = L.cg_batch_create(C.byref(self._b), n, C.cast(self._cfgs, C.c_void_p), device, nstreams)
+        if rc:
+            msg = L.cg_batch_last_error(self._b) if self._b else b""
+            self.close()
+            raise CGError("cg_batch_create: %s (%s)" % (ERRORS.get(rc, rc), msg.decode() if msg else ""))
+        self.mocks = [Mock(self.params[i], _handle=L.cg_batch_context(self._b, i)) for i in range(n)]
+
+    def run(self):
+        """Every realisation once; returns the device time of the pass in ms."""
+        ms = C.c_float()
+        rc = lib().cg_batch_run(self._b, C.byref(ms))
+        if rc:
+            raise CGError("cg_batch_run: %s (%s)" % (ERRORS.get(rc, rc), lib().cg_batch_last_error(self._b).decode()))
+        return ms.value
+
+    @property
+    def streams(self):
+        return lib().cg_batch_streams(self._b)
+
+    def tuning(self):
+        buf = (C.c_float * 16)()
+        k = lib().cg_batch_tuning(self._b, buf, 16)
+        return list(buf[:k])
+
+    def close(self):
+        if getattr(self, "mocks", None):
+            for m in self.mocks:
+                m.close()
+        if getattr(self, "_b", None):
+            lib().cg_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Mock64:

@@ -77,7 +77,13 @@ struct cg_ctx {
   Tab nz[CG_NPOP_MAX], bz[CG_NPOP_MAX], norm[CG_NPOP_MAX];
   Tab tz[CG_NPOP_MAX], bzi[CG_NPOP_MAX], normi[CG_NPOP_MAX];
   Tab kzc[CG_NPOP_MAX], bzc[CG_NPOP_MAX], normc[CG_NPOP_MAX]; /* custom maps */
-  float *d_norm = nullptr; /* (n_srcs + n_imap + n_cstm) * NA */
+  float *d_norm = nullptr; /* (n_srcs + n_imap + n_cstm) tables of NA values and their 2 edge values */
+  /* normalisation bins (density.c:1233-1245): z(r_i) of the table radii,
+   * z(L/2), the bin count and width; bin buffers keep their capacity */
+  double *d_zr = nullptr;
+  double norm_zlast = 0, norm_idz = 0;
+  int norm_nz = 0;
+  int bins_nz_cap = 0, bins_nt_cap = 0;
   float *d_pk = nullptr;
   float2 *d_twN = nullptr, *d_twH = nullptr;
   Box box;
@@ -136,6 +142,11 @@ struct cg_ctx {
   /* state */
   int have_fields = 0, have_density = 0, have_norm = 0, have_srcs = 0;
   long long launches = 0;
+  /* graph of the whole sequence (cg_graph_capture) */
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  cudaEvent_t graph_done = nullptr;
+  long long graph_launches = 0; /* kernels per replay */
   char err[1024];
 };
 
@@ -160,9 +171,15 @@ static int fail(cg_ctx *c, int code, const char *fmt, ...)
                                        __FILE__, __LINE__);                                     \
   } while (0)
 
+static void graph_free(cg_ctx *c);
+
+/* (Re)allocate a device buffer.  A captured graph holds the old addresses,
+ * so any reallocation drops the graph: replaying it would touch freed
+ * memory. */
 template <class T>
 static int dalloc(cg_ctx *c, T **p, size_t n)
 {
+  graph_free(c);
   if (*p) {
     cudaFree(*p);
     *p = nullptr;
@@ -394,17 +411,30 @@ extern "C" int cg_upload_tables(cg_ctx *c, const cg_config *cfg)
     c->bzc[p] = Tab{tab(k + 1), (float)cfg->cstm_bz_arr[p][0], 1.0f};    /* cosmo.c:76-77 */
     k += 2;
   }
-  /* normalisation tables start at 1 until compute_density_normalization */
-  const int nnorm = cfg->n_srcs + cfg->n_imap + cfg->n_cstm;
+  /* normalisation tables (NA values, then the two edges) start at 1 until
+   * compute_density_normalization */
+  const int nnorm = cfg->n_srcs + cfg->n_imap + cfg->n_cstm, nas = na + 2;
   if (nnorm > 0) {
-    std::vector<float> ones((size_t)nnorm * na, 1.0f);
+    std::vector<float> ones((size_t)nnorm * nas, 1.0f);
     if (int rc = dalloc(c, &c->d_norm, ones.size())) return rc;
     CUDA_TRY(c, cudaMemcpyAsync(c->d_norm, ones.data(), ones.size() * sizeof(float), cudaMemcpyHostToDevice,
                                 c->stream));
-    for (int p = 0; p < cfg->n_srcs; p++) c->norm[p] = Tab{c->d_norm + (size_t)p * na, 1.0f, 1.0f};
-    for (int p = 0; p < cfg->n_imap; p++) c->normi[p] = Tab{c->d_norm + (size_t)(cfg->n_srcs + p) * na, 1.0f, 1.0f};
+    for (int p = 0; p < cfg->n_srcs; p++) c->norm[p] = Tab{c->d_norm + (size_t)p * nas, 1.0f, 1.0f};
+    for (int p = 0; p < cfg->n_imap; p++) c->normi[p] = Tab{c->d_norm + (size_t)(cfg->n_srcs + p) * nas, 1.0f, 1.0f};
     for (int p = 0; p < cfg->n_cstm; p++)
-      c->normc[p] = Tab{c->d_norm + (size_t)(cfg->n_srcs + cfg->n_imap + p) * na, 1.0f, 1.0f};
+      c->normc[p] = Tab{c->d_norm + (size_t)(cfg->n_srcs + cfg->n_imap + p) * nas, 1.0f, 1.0f};
+  }
+  /* redshift bins of compute_density_normalization (density.c:1233-1245) and
+   * z at the table radii, for the device-side tables */
+  {
+    c->norm_zlast = host_bg(c, c->h_z, 0, c->h_z[na - 1], 0.5 * cfg->l_box);
+    c->norm_nz = (int)(c->norm_zlast / 0.05) + 2;
+    c->norm_idz = (c->norm_nz - 2) / c->norm_zlast;
+    std::vector<double> zr(na);
+    for (int i = 0; i < na; i++) zr[i] = host_bg(c, c->h_z, 0, c->h_z[na - 1], c->h_r[i]);
+    if (int rc = dalloc(c, &c->d_zr, (size_t)na)) return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_zr, zr.data(), na * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host staging vectors */
   }
   /* P(k) */
   std::vector<float> pk(cfg->numk);
@@ -470,12 +500,27 @@ extern "C" int cg_memory_estimate(const cg_config *cfg, unsigned long long *byte
   return CG_OK;
 }
 
+static void graph_free(cg_ctx *c)
+{
+  if (!c->gexec && !c->graph) return;
+  if (c->graph_done) cudaEventSynchronize(c->graph_done);
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->gexec = nullptr;
+  c->graph = nullptr;
+}
+
 extern "C" void cg_destroy(cg_ctx *c)
 {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  void *ptrs[] = {c->d_tabs, c->d_norm, c->d_pk, c->d_twN, c->d_twH, c->d_dens, c->d_npot, c->d_disp[0],
+  graph_free(c); /* waits for a replay still running */
+  if (c->graph_done) {
+    cudaEventDestroy(c->graph_done);
+    c->graph_done = nullptr;
+  }
+  void *ptrs[] = {c->d_tabs, c->d_norm, c->d_zr, c->d_pk, c->d_twN, c->d_twH, c->d_dens, c->d_npot, c->d_disp[0],
                   c->d_disp[1], c->d_disp[2], c->d_part, c->d_stats, c->d_s2f, c->d_err, c->d_ncount,
                   c->d_zsum, c->d_bsum, c->d_counts, c->d_bsums, c->d_total, c->d_tmpmap, c->d_kmap,
                   c->d_kfac, c->d_kinv, c->d_kir, c->d_ovf_cell, c->d_ovf_cnt, c->d_ovf_n,
@@ -657,9 +702,14 @@ static int run_bins(cg_ctx *c, int nz, double idz)
   const int MT = cg_dens_bins_max_tracers();
   if (nt > MT) return fail(c, CG_EINVAL, "%d tracers: at most %d per run are supported", nt, MT);
   int rc;
-  if ((rc = dalloc(c, &c->d_ncount, (size_t)nz)) || (rc = dalloc(c, &c->d_zsum, (size_t)nz)) ||
-      (rc = dalloc(c, &c->d_bsum, (size_t)std::max(nt, 1) * nz)))
-    return rc;
+  if (nz > c->bins_nz_cap || std::max(nt, 1) > c->bins_nt_cap) { /* grow only */
+    c->bins_nz_cap = c->bins_nt_cap = 0;
+    if ((rc = dalloc(c, &c->d_ncount, (size_t)nz)) || (rc = dalloc(c, &c->d_zsum, (size_t)nz)) ||
+        (rc = dalloc(c, &c->d_bsum, (size_t)std::max(nt, 1) * nz)))
+      return rc;
+    c->bins_nz_cap = nz;
+    c->bins_nt_cap = std::max(nt, 1);
+  }
   CUDA_TRY(c, cudaMemsetAsync(c->d_ncount, 0, sizeof(unsigned long long) * nz, c->stream));
   CUDA_TRY(c, cudaMemsetAsync(c->d_zsum, 0, sizeof(double) * nz, c->stream));
   CUDA_TRY(c, cudaMemsetAsync(c->d_bsum, 0, sizeof(double) * std::max(nt, 1) * nz, c->stream));
@@ -797,83 +847,57 @@ extern "C" int cg_set_norm_tables(cg_ctx *c, const double *srcs_norm, const doub
                                   const double *imap_norm, const double *imap_norm_0f)
 {
   if (!c) return CG_EINVAL;
-  const int na = CG_NA, nts = c->cfg.n_srcs, nti = n_imap_block(c), nsp = c->cfg.n_imap;
+  const int na = CG_NA, nas = CG_NA + 2, nts = c->cfg.n_srcs, nti = n_imap_block(c), nsp = c->cfg.n_imap;
   if (nts + nti == 0) return CG_OK;
-  std::vector<float> h((size_t)(nts + nti) * na);
-  for (int p = 0; p < nts; p++)
-    for (int i = 0; i < na; i++) h[(size_t)p * na + i] = (float)srcs_norm[(size_t)p * na + i];
-  for (int p = 0; p < nti; p++)
-    for (int i = 0; i < na; i++) h[(size_t)(nts + p) * na + i] = (float)imap_norm[(size_t)p * na + i];
+  std::vector<float> h((size_t)(nts + nti) * nas);
+  for (int p = 0; p < nts + nti; p++) {
+    const double *src = p < nts ? srcs_norm + (size_t)p * na : imap_norm + (size_t)(p - nts) * na;
+    const double *e = p < nts ? srcs_norm_0f + 2 * p : imap_norm_0f + 2 * (p - nts);
+    for (int i = 0; i < na; i++) h[(size_t)p * nas + i] = (float)src[i];
+    h[(size_t)p * nas + na] = (float)e[0];
+    h[(size_t)p * nas + na + 1] = (float)e[1];
+  }
   CUDA_TRY(c, cudaMemcpyAsync(c->d_norm, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* h is a local buffer */
-  for (int p = 0; p < nts; p++)
-    c->norm[p] = Tab{c->d_norm + (size_t)p * na, (float)srcs_norm_0f[2 * p], (float)srcs_norm_0f[2 * p + 1]};
-  for (int p = 0; p < nti; p++) {
-    const Tab t = Tab{c->d_norm + (size_t)(nts + p) * na, (float)imap_norm_0f[2 * p], (float)imap_norm_0f[2 * p + 1]};
-    if (p < nsp) c->normi[p] = t;
-    else c->normc[p - nsp] = t;
+  for (int p = 0; p < nts + nti; p++) {
+    const Tab t = Tab{c->d_norm + (size_t)p * nas, h[(size_t)p * nas + na], h[(size_t)p * nas + na + 1]};
+    if (p < nts) c->norm[p] = t;
+    else if (p - nts < nsp) c->normi[p - nts] = t;
+    else c->normc[p - nts - nsp] = t;
   }
   c->have_norm = 1;
   return CG_OK;
 }
 
-/* Linear interpolation with GSL's bracketing (largest i with x[i] <= z). */
-static double lin_interp(const std::vector<double> &x, const std::vector<double> &y, double z)
-{
-  size_t lo = 0, hi = x.size() - 1;
-  while (hi > lo + 1) {
-    size_t mid = (lo + hi) / 2;
-    if (x[mid] > z) hi = mid;
-    else lo = mid;
-  }
-  return y[lo] + (z - x[lo]) * (y[hi] - y[lo]) / (x[hi] - x[lo]);
-}
-
+/* compute_density_normalization (density.c:1227-1393): the bin sums of the
+ * fused density pass, then the tables built on the device (k_norm_tables,
+ * the double-precision steps of density.c:1272-1355), with no host round
+ * trip; the edge values travel inside the tables. */
 extern "C" int cg_compute_density_normalization(cg_ctx *c)
 {
   if (!c) return CG_EINVAL;
-  const int nts = c->cfg.n_srcs, nti = n_imap_block(c), nt = nts + nti;
-  /* density.c:1233-1245 */
-  const double zmax = host_bg(c, c->h_z, 0, c->h_z[CG_NA - 1], c->cfg.l_box * 0.5);
-  const int nz = (int)(zmax / 0.05) + 2;
-  const double idz = (nz - 2) / zmax;
-  std::vector<double> zarr(nz), b((size_t)std::max(nt, 1) * nz);
-  std::vector<unsigned long long> narr(nz);
-  if (int rc = cg_collect_density_normalization(c, nz, idz, zarr.data(), narr.data(), b.data(),
-                                                 nti ? b.data() + (size_t)nts * nz : nullptr))
-    return rc;
-  /* density.c:1272-1297 */
-  for (int iz = 0; iz < nz; iz++) {
-    if (narr[iz] > 0) {
-      zarr[iz] /= narr[iz];
-      for (int t = 0; t < nt; t++) b[(size_t)t * nz + iz] = narr[iz] / b[(size_t)t * nz + iz];
-    }
+  if (!c->have_density) return fail(c, CG_ESTATE, "compute_physical_density_field first");
+  const int nts = c->cfg.n_srcs, nti = n_imap_block(c), nt = nts + nti, nz = c->norm_nz;
+  if (nz < 2 || nz > CG_NORM_NZ_MAX)
+    return fail(c, CG_EINVAL, "%d redshift bins: the device tables take 2 to %d", nz, CG_NORM_NZ_MAX);
+  cudaSetDevice(c->device);
+  if (int rc = run_bins(c, nz, c->norm_idz)) return rc;
+  if (nt > 0) {
+    ProfScope ps(c, "norm_tables");
+    CUDA_TRY(c, cg_norm_tables(c->stream, c->d_ncount, c->d_zsum, c->d_bsum, nz, nt, c->norm_zlast, c->d_zr,
+                               c->d_norm));
+    c->launches++;
   }
-  zarr[0] = 0;
-  zarr[nz - 1] = host_bg(c, c->h_z, 0, c->h_z[CG_NA - 1], 0.5 * c->cfg.l_box);
-  for (int t = 0; t < nt; t++) {
-    b[(size_t)t * nz + 0] = b[(size_t)t * nz + 1];
-    b[(size_t)t * nz + nz - 1] = b[(size_t)t * nz + nz - 2];
+  const int nas = CG_NA + 2, nsp = c->cfg.n_imap;
+  for (int p = 0; p < nt; p++) { /* edges are read from the tables by the kernels */
+    const Tab t = Tab{c->d_norm + (size_t)p * nas, 0.0f, 0.0f};
+    if (p < nts) c->norm[p] = t;
+    else if (p - nts < nsp) c->normi[p - nts] = t;
+    else c->normc[p - nts - nsp] = t;
   }
-  /* density.c:1299-1355: linear spline in z resampled on the r table */
-  const int na = CG_NA;
-  std::vector<double> tabs((size_t)std::max(nt, 1) * na), e0f((size_t)2 * std::max(nt, 1));
-  const double z0n = zarr[0], zfn = zarr[nz - 1];
-  for (int t = 0; t < nt; t++) {
-    std::vector<double> y(b.begin() + (size_t)t * nz, b.begin() + (size_t)(t + 1) * nz);
-    e0f[2 * t] = y[0];
-    e0f[2 * t + 1] = y[nz - 1];
-    for (int i = 0; i < na; i++) {
-      double z = host_bg(c, c->h_z, 0, c->h_z[na - 1], c->h_r[i]);
-      double nm;
-      if (z < z0n) nm = y[0];
-      else if (z >= zfn) nm = y[nz - 1];
-      else nm = lin_interp(zarr, y, z);
-      tabs[(size_t)t * na + i] = nm;
-    }
-  }
-  return cg_set_norm_tables(c, tabs.data(), e0f.data(), nti ? tabs.data() + (size_t)nts * na : nullptr,
-                            nti ? e0f.data() + 2 * nts : nullptr);
+  c->have_norm = 1;
+  c->have_srcs = 0;
+  return CG_OK;
 }
 
 static void srcs_params(cg_ctx *c, int ipop, cg_srcs_params &p)
@@ -914,9 +938,13 @@ static void srcs_params(cg_ctx *c, int ipop, cg_srcs_params &p)
   p.err = c->d_err;
 }
 
-extern "C" int cg_srcs_set_cartesian(cg_ctx *c, long long *nsrc)
+/* srcs_set_cartesian for every population: count -> scan -> emit.  With
+ * readback the total is read after the count to size the catalogue (the
+ * public entry point); without it the catalogue keeps its capacity, emit
+ * drops what does not fit and flags the overflow, and the totals stay on
+ * the device until read (the graph-captured sequence). */
+static int srcs_run(cg_ctx *c, long long *nsrc, bool readback)
 {
-  if (!c) return CG_EINVAL;
   if (!c->have_density) return fail(c, CG_ESTATE, "density not computed");
   if (!c->have_norm) return fail(c, CG_ESTATE, "compute_density_normalization first");
   cudaSetDevice(c->device);
@@ -925,7 +953,7 @@ extern "C" int cg_srcs_set_cartesian(cg_ctx *c, long long *nsrc)
   if (c->cfg.n_srcs > 0) {
     if (!c->d_counts && (rc = dalloc(c, &c->d_counts, (size_t)ncell))) return rc;
     if (!c->d_bsums && (rc = dalloc(c, &c->d_bsums, (size_t)cg_srcs_nblocks(c->N)))) return rc;
-    if (!c->d_total && (rc = dalloc(c, &c->d_total, (size_t)1))) return rc;
+    if (!c->d_total && (rc = dalloc(c, &c->d_total, (size_t)CG_NPOP_MAX))) return rc;
     if (!c->d_ovf_n && ((rc = dalloc(c, &c->d_ovf_cell, (size_t)CG_OVF_CAP)) ||
                         (rc = dalloc(c, &c->d_ovf_cnt, (size_t)CG_OVF_CAP)) || (rc = dalloc(c, &c->d_ovf_n, (size_t)1))))
       return rc;
@@ -936,20 +964,25 @@ extern "C" int cg_srcs_set_cartesian(cg_ctx *c, long long *nsrc)
     srcs_params(c, ip, p);
     {
       ProfScope ps(c, "srcs_count");
-      CUDA_TRY(c, cg_srcs_count(c->stream, c->d_dens, &p, c->d_total));
+      CUDA_TRY(c, cg_srcs_count(c->stream, c->d_dens, &p, c->d_total + ip));
     }
-    long long tot = 0;
-    CUDA_TRY(c, cudaMemcpyAsync(&tot, c->d_total, sizeof(tot), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-    if ((rc = check_device_errors(c))) return rc;
-    if (tot > K.cap) {
-      long long cap = tot + tot / 8 + 1024;
-      if ((rc = dalloc(c, &K.pos, (size_t)cap)) || (rc = dalloc(c, &K.ipix, (size_t)cap)) ||
-          (rc = dalloc(c, &K.src, (size_t)cap * 9)))
-        return rc;
-      K.cap = cap;
+    if (readback) {
+      long long tot = 0;
+      CUDA_TRY(c, cudaMemcpyAsync(&tot, c->d_total + ip, sizeof(tot), cudaMemcpyDeviceToHost, c->stream));
+      CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+      if ((rc = check_device_errors(c))) return rc;
+      if (tot > K.cap) {
+        long long cap = tot + tot / 8 + 1024;
+        if ((rc = dalloc(c, &K.pos, (size_t)cap)) || (rc = dalloc(c, &K.ipix, (size_t)cap)) ||
+            (rc = dalloc(c, &K.src, (size_t)cap * 9)))
+          return rc;
+        K.cap = cap;
+      }
+      K.n = tot;
+      if (nsrc) nsrc[ip] = tot;
+    } else {
+      K.n = -1; /* on the device until refresh_counts */
     }
-    K.n = tot;
     const int ns = c->cfg.nside_count[ip];
     if (ns > 0) {
       long long np = 12LL * ns * ns;
@@ -965,15 +998,41 @@ extern "C" int cg_srcs_set_cartesian(cg_ctx *c, long long *nsrc)
       CUDA_TRY(c, cg_srcs_emit(c->stream, c->d_npot, &p));
     }
     c->launches += 3;
-    if (nsrc) nsrc[ip] = tot;
   }
   c->have_srcs = 1;
+  return CG_OK;
+}
+
+extern "C" int cg_srcs_set_cartesian(cg_ctx *c, long long *nsrc)
+{
+  if (!c) return CG_EINVAL;
+  return srcs_run(c, nsrc, true);
+}
+
+/* Source totals left on the device by a graph launch: wait for it, read
+ * them and check the catalogues held every source. */
+static int refresh_counts(cg_ctx *c)
+{
+  bool stale = false;
+  for (int ip = 0; ip < c->cfg.n_srcs; ip++) stale |= c->cat[ip].n < 0;
+  if (!stale) return CG_OK;
+  if (c->graph_done) CUDA_TRY(c, cudaEventSynchronize(c->graph_done));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  long long tot[CG_NPOP_MAX];
+  CUDA_TRY(c, cudaMemcpy(tot, c->d_total, c->cfg.n_srcs * sizeof(long long), cudaMemcpyDeviceToHost));
+  for (int ip = 0; ip < c->cfg.n_srcs; ip++) c->cat[ip].n = tot[ip];
+  if (int rc = check_device_errors(c)) return rc;
+  for (int ip = 0; ip < c->cfg.n_srcs; ip++)
+    if (c->cat[ip].n > c->cat[ip].cap)
+      return fail(c, CG_EDEVICE, "population %d: %lld sources, catalogue holds %lld", ip, c->cat[ip].n,
+                  c->cat[ip].cap);
   return CG_OK;
 }
 
 extern "C" long long cg_num_sources(cg_ctx *c, int ipop)
 {
   if (!c || ipop < 0 || ipop >= c->cfg.n_srcs) return -1;
+  if (refresh_counts(c)) return -1;
   return c->cat[ipop].n;
 }
 
@@ -1371,6 +1430,7 @@ static int srcs_los_run(cg_ctx *c, int ip)
 extern "C" int cg_get_beam_properties(cg_ctx *c)
 {
   if (!c) return CG_EINVAL;
+  if (int rc = refresh_counts(c)) return rc;
   if (!c->cfg.need_beaming) return CG_OK; /* beaming.c:296-299 */
   if (!c->have_fields) return fail(c, CG_ESTATE, "fields not created");
   cudaSetDevice(c->device);
@@ -1404,6 +1464,204 @@ extern "C" int cg_run_mock(cg_ctx *c)
   if ((rc = cg_imap_set_cartesian(c))) return rc;
   if ((rc = cg_get_beam_properties(c))) return rc;
   return CG_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* graph-captured sequence and batches of realisations                      */
+/* ------------------------------------------------------------------------ */
+/* The stages without host round trips: fields, density, normalisation
+ * tables and sources, totals left on the device. */
+static int run_mock_async(cg_ctx *c)
+{
+  int rc;
+  if ((rc = cg_create_cartesian_fields(c))) return rc;
+  if ((rc = cg_compute_physical_density_field(c))) return rc;
+  if ((rc = cg_compute_density_normalization(c))) return rc;
+  return srcs_run(c, nullptr, false);
+}
+
+extern "C" int cg_graph_capture(cg_ctx *c)
+{
+  if (!c) return CG_EINVAL;
+  if (c->cfg.n_imap > 0 || c->cfg.need_beaming)
+    return fail(c, CG_EINVAL, "graph capture covers fields, density, normalisation and sources; "
+                              "intensity maps and line-of-sight quantities keep their host steps");
+  if (c->profiling) return fail(c, CG_EINVAL, "switch profiling off before capturing");
+  cudaSetDevice(c->device);
+  graph_free(c);
+  /* one plain run sizes every buffer (the catalogue with slack); the
+   * captured sequence allocates nothing */
+  int rc = cg_run_mock(c);
+  if (!rc) rc = cg_sync(c);
+  if (rc) return rc;
+  const long long l0 = c->launches;
+  CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  rc = run_mock_async(c);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  if (rc || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    for (int ip = 0; ip < c->cfg.n_srcs; ip++) c->cat[ip].n = -1;
+    return rc ? rc : fail(c, CG_ECUDA, "stream capture: %s", cudaGetErrorString(e));
+  }
+  c->graph_launches = c->launches - l0;
+  c->launches = l0;
+  c->graph = g;
+  CUDA_TRY(c, cudaGraphInstantiate(&c->gexec, g, 0));
+  if (!c->graph_done) CUDA_TRY(c, cudaEventCreateWithFlags(&c->graph_done, cudaEventDisableTiming));
+  /* nothing ran during the capture: the totals on the device are the plain
+   * run's, read again on demand */
+  return CG_OK;
+}
+
+extern "C" int cg_graph_launch(cg_ctx *c, void *stream)
+{
+  if (!c) return CG_EINVAL;
+  if (!c->gexec) return fail(c, CG_ESTATE, "cg_graph_capture first");
+  cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+  CUDA_TRY(c, cudaGraphLaunch(c->gexec, s));
+  CUDA_TRY(c, cudaEventRecord(c->graph_done, s));
+  if (s != c->stream) CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->graph_done, 0));
+  c->launches += c->graph_launches;
+  for (int ip = 0; ip < c->cfg.n_srcs; ip++) c->cat[ip].n = -1;
+  c->have_fields = c->have_density = c->have_norm = c->have_srcs = 1;
+  c->pending_mode = CG_DMODE_NONE;
+  return CG_OK;
+}
+
+struct cg_batch {
+  int device = 0, n = 0, nstreams = 0;
+  std::vector<cg_ctx *> ctx;
+  std::vector<int> order; /* largest grids first */
+  std::vector<cudaStream_t> streams;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  std::vector<cudaEvent_t> joins;
+  std::vector<float> tune_ms; /* autotuner: time per stream count tried */
+  char err[1024] = {0};
+};
+
+static int batch_fail(cg_batch *b, int code, const char *fmt, ...)
+{
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(b->err, sizeof(b->err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+static int batch_set_streams(cg_batch *b, int ns)
+{
+  for (cudaStream_t s : b->streams) cudaStreamDestroy(s);
+  for (cudaEvent_t e : b->joins) cudaEventDestroy(e);
+  b->streams.assign(ns, nullptr);
+  b->joins.assign(ns, nullptr);
+  for (int k = 0; k < ns; k++) {
+    if (cudaStreamCreateWithFlags(&b->streams[k], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->joins[k], cudaEventDisableTiming) != cudaSuccess)
+      return batch_fail(b, CG_ECUDA, "stream or event creation failed");
+  }
+  b->nstreams = ns;
+  return CG_OK;
+}
+
+/* One pass over every realisation: graph launches dealt round-robin, largest
+ * grid first, over the batch's streams, joined on the first. */
+static int batch_pass(cg_batch *b, float *ms)
+{
+  cudaStream_t s0 = b->streams[0];
+  if (cudaEventRecord(b->t0, s0) != cudaSuccess) return batch_fail(b, CG_ECUDA, "event record");
+  for (int k = 1; k < b->nstreams; k++) cudaStreamWaitEvent(b->streams[k], b->t0, 0);
+  for (size_t j = 0; j < b->order.size(); j++) {
+    cg_ctx *c = b->ctx[b->order[j]];
+    if (int rc = cg_graph_launch(c, b->streams[j % b->nstreams]))
+      return batch_fail(b, rc, "realisation %d: %s", b->order[j], c->err);
+  }
+  for (int k = 1; k < b->nstreams; k++) {
+    cudaEventRecord(b->joins[k], b->streams[k]);
+    cudaStreamWaitEvent(s0, b->joins[k], 0);
+  }
+  cudaEventRecord(b->t1, s0);
+  if (cudaEventSynchronize(b->t1) != cudaSuccess) return batch_fail(b, CG_ECUDA, "batch synchronisation");
+  if (ms) cudaEventElapsedTime(ms, b->t0, b->t1);
+  return CG_OK;
+}
+
+extern "C" int cg_batch_create(cg_batch **out, int n, const cg_config *cfgs, int device, int nstreams)
+{
+  if (!out || n < 1 || !cfgs || nstreams < 0 || nstreams > 64) return CG_EINVAL;
+  *out = nullptr;
+  cg_batch *b = new cg_batch;
+  b->device = device;
+  b->n = n;
+  *out = b;
+  if (cudaSetDevice(device) != cudaSuccess) return batch_fail(b, CG_ECUDA, "cudaSetDevice(%d)", device);
+  b->ctx.assign(n, nullptr);
+  for (int i = 0; i < n; i++) {
+    int rc = cg_create(&b->ctx[i], &cfgs[i], device);
+    if (!rc) rc = cg_graph_capture(b->ctx[i]);
+    if (rc) return batch_fail(b, rc, "realisation %d: %s", i, b->ctx[i] ? b->ctx[i]->err : "cg_create failed");
+  }
+  b->order.resize(n);
+  for (int i = 0; i < n; i++) b->order[i] = i;
+  std::stable_sort(b->order.begin(), b->order.end(), [&](int a, int c) { return b->ctx[a]->N > b->ctx[c]->N; });
+  if (cudaEventCreate(&b->t0) != cudaSuccess || cudaEventCreate(&b->t1) != cudaSuccess)
+    return batch_fail(b, CG_ECUDA, "event creation");
+  if (nstreams > 0) return batch_set_streams(b, nstreams);
+  /* autotune the stream count: one warm pass, then the best of two timed
+   * passes per candidate */
+  const int cand[] = {1, 2, 4, 8, 16};
+  int best = 1;
+  float best_ms = 1e30f;
+  for (int ns : cand) {
+    if (int rc = batch_set_streams(b, ns)) return rc;
+    float t = 0, tmin = 1e30f;
+    for (int rep = 0; rep < 3; rep++) {
+      if (int rc = batch_pass(b, &t)) return rc;
+      if (rep > 0) tmin = std::min(tmin, t);
+    }
+    b->tune_ms.push_back(tmin);
+    if (tmin < best_ms) {
+      best_ms = tmin;
+      best = ns;
+    }
+  }
+  return batch_set_streams(b, best);
+}
+
+extern "C" int cg_batch_run(cg_batch *b, float *ms)
+{
+  if (!b || b->nstreams < 1) return CG_EINVAL;
+  cudaSetDevice(b->device);
+  return batch_pass(b, ms);
+}
+
+extern "C" int cg_batch_streams(const cg_batch *b) { return b ? b->nstreams : -1; }
+
+extern "C" int cg_batch_tuning(const cg_batch *b, float *ms, int cap)
+{
+  if (!b) return -1;
+  const int k = (int)b->tune_ms.size();
+  for (int i = 0; i < k && i < cap && ms; i++) ms[i] = b->tune_ms[i];
+  return k;
+}
+
+extern "C" cg_ctx *cg_batch_context(cg_batch *b, int i) { return (b && i >= 0 && i < b->n) ? b->ctx[i] : nullptr; }
+
+extern "C" const char *cg_batch_last_error(const cg_batch *b) { return b ? b->err : "null batch"; }
+
+extern "C" void cg_batch_destroy(cg_batch *b)
+{
+  if (!b) return;
+  cudaSetDevice(b->device);
+  for (cudaStream_t s : b->streams) {
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+  }
+  for (cudaEvent_t e : b->joins) cudaEventDestroy(e);
+  if (b->t0) cudaEventDestroy(b->t0);
+  if (b->t1) cudaEventDestroy(b->t1);
+  for (cg_ctx *c : b->ctx) cg_destroy(c);
+  delete b;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1448,6 +1706,7 @@ extern "C" int cg_download_grid(cg_ctx *c, int which, void *dst)
 extern "C" int cg_download_catalog(cg_ctx *c, int ipop, float *pos4, int *ipix, float *src9)
 {
   if (!c || ipop < 0 || ipop >= c->cfg.n_srcs) return CG_EINVAL;
+  if (int rc = refresh_counts(c)) return rc;
   const Cat &K = c->cat[ipop];
   if (K.n > 0) {
     if (pos4) CUDA_TRY(c, cudaMemcpyAsync(pos4, K.pos, K.n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
@@ -1461,6 +1720,7 @@ extern "C" int cg_download_catalog(cg_ctx *c, int ipop, float *pos4, int *ipix, 
 extern "C" int cg_download_skewers(cg_ctx *c, int ipop, float *dens, float *vel)
 {
   if (!c || ipop < 0 || ipop >= c->cfg.n_srcs) return CG_EINVAL;
+  if (int rc = refresh_counts(c)) return rc;
   const Cat &K = c->cat[ipop];
   if (!c->cfg.skw_srcs[ipop]) return fail(c, CG_ESTATE, "population %d stores no skewers", ipop);
   if (K.skw_n != K.n) return fail(c, CG_ESTATE, "skewers of population %d not computed", ipop);
@@ -1476,6 +1736,7 @@ extern "C" int cg_download_skewers(cg_ctx *c, int ipop, float *dens, float *vel)
 extern "C" int cg_download_count_map(cg_ctx *c, int ipop, int *counts)
 {
   if (!c || !counts || ipop < 0 || ipop >= c->cfg.n_srcs) return CG_EINVAL;
+  if (int rc = refresh_counts(c)) return rc;
   const Cat &K = c->cat[ipop];
   if (!K.cmap) return fail(c, CG_ESTATE, "no count map for population %d", ipop);
   CUDA_TRY(c, cudaMemcpyAsync(counts, K.cmap, K.cmap_npix * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -1552,10 +1813,12 @@ extern "C" int cg_download_norm(cg_ctx *c, int kind, int ipop, float *tab, float
   if (kind == 1 && ipop >= 0 && ipop < c->cfg.n_imap) t = &c->normi[ipop];
   if (kind == 2 && ipop >= 0 && ipop < c->cfg.n_cstm) t = &c->normc[ipop];
   if (!t || !t->f) return fail(c, CG_EINVAL, "no normalisation table %d/%d", kind, ipop);
+  float e[2];
   CUDA_TRY(c, cudaMemcpyAsync(tab, t->f, CG_NA * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(e, t->f + CG_NA, 2 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-  edges[0] = t->f0;
-  edges[1] = t->ff;
+  edges[0] = e[0];
+  edges[1] = e[1];
   return CG_OK;
 }
 

@@ -10,6 +10,7 @@
 #include <stdint.h>
 
 #include "cg_cell.h"
+#include "colore_cuda.h"
 
 namespace cg {
 
@@ -61,6 +62,18 @@ __device__ __forceinline__ float bgv(const Tab &t, const BgAt &a)
   const float fi = t.f[a.ir];
   return CG_FMA(CG_SUB(t.f[a.ir + 1], fi), a.t, fi);
 }
+
+/* Normalisation tables hold CG_NA values followed by their two edge values
+ * (below r = 0, then at or beyond r_last), so that a table built on the
+ * device needs no host round trip: bgvn and bgn read the edges from it. */
+__device__ __forceinline__ float bgvn(const Tab &t, const BgAt &a)
+{
+  if (a.where) return __ldg(t.f + (a.where < 0 ? CG_NA : CG_NA + 1));
+  const float fi = t.f[a.ir];
+  return CG_FMA(CG_SUB(t.f[a.ir + 1], fi), a.t, fi);
+}
+
+__device__ __forceinline__ float bgn(const Tab &t, const Grid1 &g, float r) { return bgvn(t, bg_at(g, r)); }
 
 /* r_of_z, cosmo.c:101-112, on the a-uniform table of NA entries. */
 __device__ __forceinline__ float r_of_z(const float *a_arr, const float *r_arr, int na, float z)

@@ -288,7 +288,81 @@ __global__ void __launch_bounds__(256) k_lpt_deposit(float *grid, const float *_
   }
 }
 
+/* compute_density_normalization after the bin sums (density.c:1272-1355):
+ * mean redshift and count / sum(bias) per bin, the first and last bins
+ * copied from their neighbours, then the linear spline in z evaluated at
+ * z(r_i) with GSL's bracketing (largest bin centre <= z).  One block per
+ * tracer; every double operation is an explicitly rounded one, in the order
+ * of the host restatement, so the tables do not depend on contraction. */
+__global__ void __launch_bounds__(256) k_norm_tables(const unsigned long long *__restrict__ ncount,
+                                                     const double *__restrict__ zsum,
+                                                     const double *__restrict__ bsum, int nz, double zlast,
+                                                     const double *__restrict__ zr, float *out)
+{
+  extern __shared__ double nsh[];
+  double *zz = nsh, *y = nsh + nz;
+  const int t = blockIdx.x;
+  for (int iz = threadIdx.x; iz < nz; iz += blockDim.x) {
+    const unsigned long long n = ncount[iz];
+    const double b = bsum[(size_t)t * nz + iz];
+    zz[iz] = n > 0 ? __ddiv_rn(zsum[iz], __ull2double_rn(n)) : zsum[iz];
+    y[iz] = n > 0 ? __ddiv_rn(__ull2double_rn(n), b) : b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    zz[0] = 0;
+    zz[nz - 1] = zlast;
+    y[0] = y[1];
+    y[nz - 1] = y[nz - 2];
+  }
+  __syncthreads();
+  float *o = out + (size_t)t * (CG_NA + 2);
+  for (int i = threadIdx.x; i < CG_NA; i += blockDim.x) {
+    const double z = zr[i];
+    double nm;
+    if (z < zz[0]) {
+      nm = y[0];
+    } else if (z >= zz[nz - 1]) {
+      nm = y[nz - 1];
+    } else {
+      int lo = 0, hi = nz - 1;
+      while (hi > lo + 1) {
+        const int mid = (lo + hi) / 2;
+        if (zz[mid] > z) hi = mid;
+        else lo = mid;
+      }
+      nm = __dadd_rn(y[lo], __ddiv_rn(__dmul_rn(__dsub_rn(z, zz[lo]), __dsub_rn(y[hi], y[lo])), __dsub_rn(zz[hi], zz[lo])));
+    }
+    o[i] = (float)nm;
+  }
+  if (threadIdx.x == 0) {
+    o[CG_NA] = (float)y[0];
+    o[CG_NA + 1] = (float)y[nz - 1];
+  }
+}
+
 } /* namespace */
+
+cudaError_t cg_norm_tables(cudaStream_t s, const unsigned long long *ncount, const double *zsum, const double *bsum,
+                           int nz, int nt, double zlast, const double *zr, float *out)
+{
+  if (nz < 2 || nz > CG_NORM_NZ_MAX || nt < 1) return cudaErrorInvalidValue;
+  const size_t smem = 2 * sizeof(double) * (size_t)nz;
+  if (smem > 48 * 1024) {
+    static bool set[CG_MAX_DEVICES]; /* opt-in above 48 KiB, once per device */
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= CG_MAX_DEVICES) return cudaErrorInvalidDevice;
+    if (!set[dev]) {
+      cudaError_t e = cudaFuncSetAttribute(k_norm_tables, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           2 * (int)sizeof(double) * CG_NORM_NZ_MAX);
+      if (e != cudaSuccess) return e;
+      set[dev] = true;
+    }
+  }
+  k_norm_tables<<<nt, 256, smem, s>>>(ncount, zsum, bsum, nz, zlast, zr, out);
+  return cudaGetLastError();
+}
 
 cudaError_t cg_moments_final(cudaStream_t s, const double2 *part, size_t n, double inv_ncell, double *stats,
                              float *s2f)
@@ -306,8 +380,17 @@ cudaError_t cg_dens_bins(cudaStream_t s, float *grid, const cg_bins_params *p, i
   while (nwb > 1 && (size_t)nwb * wb > 200u * 1024u) nwb--;
   if ((size_t)nwb * wb > 200u * 1024u) return cudaErrorInvalidValue;
   const size_t smem = (size_t)nwb * wb;
-  cudaError_t e = cudaFuncSetAttribute(k_dens_bins, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
+  if (smem > 48u * 1024u) {
+    static bool set[CG_MAX_DEVICES]; /* raised once per device to the largest size a launch asks for */
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= CG_MAX_DEVICES) return cudaErrorInvalidDevice;
+    if (!set[dev]) {
+      cudaError_t e = cudaFuncSetAttribute(k_dens_bins, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      if (e != cudaSuccess) return e;
+      set[dev] = true;
+    }
+  }
   long long nrow = (long long)p->box.N * p->box.N;
   long long blocks = (nrow + nwb - 1) / nwb;
   long long cap = (long long)nsm * 8;

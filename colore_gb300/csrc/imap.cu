@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap_cells(const float *__restri
         lst = rc <= p.rmax_here && rc >= p.rmin_here && tmean > 0.0f;
         if (lst) {
           const float bias = bgv(p.bz, at);
-          const float dnorm = bgv(p.norm, at);
+          const float dnorm = bgvn(p.norm, at);
           const int xh = wrap(ix + 1, N), xl = wrap(ix - 1, N);
           const int yh = wrap(iy + 1, N), yl = wrap(iy - 1, N);
           const int zh = wrap(iz + 1, N), zl = wrap(iz - 1, N);

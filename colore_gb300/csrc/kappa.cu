@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(256) k_cstm(const float *__restrict__ dens, cg
     const int irr = p.ir_min + i;
     kz[i] = p.kz[irr];
     bz[i] = p.bz[irr];
-    nm[i] = bg(p.norm, p.g, CG_MUL(CG_ADD((float)irr, 0.5f), p.dr));
+    nm[i] = bgn(p.norm, p.g, CG_MUL(CG_ADD((float)irr, 0.5f), p.dr));
   }
   __syncthreads();
   const long long ip = (long long)blockIdx.x * blockDim.x + threadIdx.x;

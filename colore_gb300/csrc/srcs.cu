@@ -54,7 +54,7 @@ __device__ __forceinline__ float pois_lambda(const cg_srcs_params &p, float d, f
   float nd = bgv(p.nz, at);
   if (!(nd > 0.0f)) return 0.0f;
   float b = bgv(p.bz, at);
-  float dn = bgv(p.norm, at);
+  float dn = bgvn(p.norm, at);
   return cg_src_lambda(nd, p.cell_vol, d, b, dn, p.bias_model);
 }
 

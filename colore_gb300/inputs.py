@@ -73,6 +73,23 @@ CONFIGS = {
 }
 
 
+def batch_specs(n=48, seed=3000):
+    """The batched workload: n independent realisations, a third each at
+    128^3, 256^3 and 384^3, seeds 3001 + i, z_min 0.05 and z_max drawn
+    uniformly in [0.1, 1.2] from `seed`; one population with b = 1.5 and a
+    flat dN/dz of 200 per deg^2 between z_min and z_max."""
+    rng = np.random.default_rng(seed)
+    zmax = rng.uniform(0.1, 1.2, n)
+    grids = [128, 256, 384]
+    out = []
+    for i in range(n):
+        out.append(dict(n_grid=grids[min(3 * i // n, 2)], z_min=0.05, z_max=float(zmax[i]), r_smooth=2.0,
+                        seed=3001 + i, dens_type=0, bias_model=2,
+                        srcs=[dict(nz=("flat", 0.05, float(zmax[i])), density=200.0, bias=("const", 1.5),
+                                   nside_count=0)]))
+    return out
+
+
 def scaled(name, n_grid, **over):
     """A configuration with another grid size (and optional overrides)."""
     spec = dict(CONFIGS[name])

@@ -185,6 +185,37 @@ int cg_get_beam_properties(cg_ctx *ctx);
 /* Run the whole driver sequence of src/main.c:66-125 in one call. */
 int cg_run_mock(cg_ctx *ctx);
 
+/* Graph-captured sequence (no counterpart in the reference; the batching
+ * pattern of the GPU path).  cg_graph_capture runs the sequence once to size
+ * every buffer, then captures fields, density, normalisation and sources
+ * into a CUDA graph; configurations with intensity maps or line-of-sight
+ * quantities are refused (those stages keep host steps).  cg_graph_launch
+ * replays it on a stream (NULL: the context's); the source totals stay on
+ * the device until a download or cg_num_sources reads them, and a total
+ * that outgrew the catalogue is reported there (CG_EDEVICE).  Replays
+ * repeat the captured realisation: change the seed with cg_upload_tables
+ * and capture again. */
+int cg_graph_capture(cg_ctx *ctx);
+int cg_graph_launch(cg_ctx *ctx, void *cuda_stream);
+
+/* Batches of independent realisations (no counterpart in the reference):
+ * one context and captured graph per configuration, the graphs dealt over
+ * nstreams streams (largest grids first) so that small grids run side by
+ * side.  nstreams = 0 autotunes the stream count (1, 2, 4, 8 or 16) by
+ * timing whole passes.  cg_batch_run runs every realisation once and
+ * reports the device time of the pass; cg_batch_context gives the context
+ * of realisation i for the download calls.  The configurations' tables must
+ * outlive the batch. */
+typedef struct cg_batch cg_batch;
+int cg_batch_create(cg_batch **out, int n, const cg_config *cfgs, int device, int nstreams);
+int cg_batch_run(cg_batch *b, float *ms);
+int cg_batch_streams(const cg_batch *b);
+/* stream-count autotuning: the pass time of each candidate, in order */
+int cg_batch_tuning(const cg_batch *b, float *ms, int cap);
+cg_ctx *cg_batch_context(cg_batch *b, int i);
+const char *cg_batch_last_error(const cg_batch *b);
+void cg_batch_destroy(cg_batch *b);
+
 /* Host mirrors -------------------------------------------------------------- */
 /* which: 0 = density (grid_dens), 1 = potential (grid_npot), 2..4 = 1LPT
  * displacement x,y,z.  dst holds N*N*2(N/2+1) values of the context's
