@@ -78,22 +78,10 @@ CG_HD float cg_logfact_small(int k)
  *              and log1p so that single precision keeps ~1e-6 absolute
  *              accuracy in the acceptance test.
  * Iterations are bounded; the bound is never reached for finite lam. */
-CG_HD int cg_poisson(float lam, uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1)
+/* PTRS branch of cg_poisson (lam >= 10), out of line: the per-cell loops
+ * that sample counts stay small enough for the instruction cache. */
+CG_HD_COLD int cg_poisson_ptrs(float lam, uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1)
 {
-  if (!(lam > 0.0f)) return 0;
-  if (lam < 10.0f) {
-    cg_u32x4 w = cg_philox4x32_10(c0, c1, 0u, 0u, k0, k1);
-    float u = cg_u01f(w.v[0]);
-    float p = cg_expf(-lam);
-    float F = p;
-    int k = 0;
-    while (u >= F && k < 200) {
-      k++;
-      p = CG_MUL(p, CG_DIV(lam, (float)k));
-      F = CG_ADD(F, p);
-    }
-    return k;
-  }
   float slam = CG_SQRT(lam);
   float b = CG_FMA(2.53f, slam, 0.931f);
   float a = CG_FMA(0.02483f, b, -0.059f);
@@ -130,6 +118,26 @@ CG_HD int cg_poisson(float lam, uint32_t k0, uint32_t k1, uint32_t c0, uint32_t 
     if (lhs <= rhs) return k;
   }
   return (int)cg_floorf(lam);
+}
+
+
+CG_HD int cg_poisson(float lam, uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1)
+{
+  if (!(lam > 0.0f)) return 0;
+  if (lam < 10.0f) {
+    cg_u32x4 w = cg_philox4x32_10(c0, c1, 0u, 0u, k0, k1);
+    float u = cg_u01f(w.v[0]);
+    float p = cg_expf(-lam);
+    float F = p;
+    int k = 0;
+    while (u >= F && k < 200) {
+      k++;
+      p = CG_MUL(p, CG_DIV(lam, (float)k));
+      F = CG_ADD(F, p);
+    }
+    return k;
+  }
+  return cg_poisson_ptrs(lam, k0, k1, c0, c1);
 }
 
 /* cart2sph, srcs.c:68-85 / imap.c:24-41.  phi = atan2(y, x): the reference

@@ -28,8 +28,11 @@
 
 #if defined(__CUDACC__)
 #define CG_HD __host__ __device__ __forceinline__
+/* rarely taken paths: one out-of-line copy instead of one per call site */
+#define CG_HD_COLD static __host__ __device__ __noinline__
 #else
 #define CG_HD static inline
+#define CG_HD_COLD static
 #include <math.h>
 #include <string.h>
 #endif

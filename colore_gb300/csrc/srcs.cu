@@ -68,7 +68,14 @@ __device__ __forceinline__ int ovf_lookup(const cg_srcs_params &p, long long cid
   return CG_COUNT_ESC;
 }
 
-__global__ void __launch_bounds__(SB) k_pois_count(const float *__restrict__ grid, cg_srcs_params p)
+/* Counts of CPT consecutive cells of one row per thread.  The cell loop is
+ * not unrolled and the PTRS branch of the sampler is out of line, so the
+ * loop stays small in the instruction cache (unrolled, the loop ran
+ * instruction-fetch bound where the mean count per cell is a few); the
+ * counts are packed in two 64-bit registers.  Each warp adds its total to
+ * the block's entry (zeroed before the launch), so warps that finish early
+ * do not wait for the block's slowest. */
+__global__ void __launch_bounds__(SB, 4) k_pois_count(const float *__restrict__ grid, cg_srcs_params p)
 {
   const int N = p.box.N;
   const long long ncell = (long long)N * N * N;
@@ -79,67 +86,55 @@ __global__ void __launch_bounds__(SB) k_pois_count(const float *__restrict__ gri
     cell_of(c0, p.box, ix, iy, iz);
     const float *row = grid + pidx(ix, iy, iz, N);
     const float y0 = cg_cell_coord(iy, p.box.dx, p.box.p1), z0 = cg_cell_coord(iz, p.box.dx, p.box.p2);
-    unsigned short cnt[CPT];
-#pragma unroll
-    for (int h = 0; h < CPT; h += 2) {
-      float2 dv = *reinterpret_cast<const float2 *>(row + h);
-      float dd[2] = {dv.x, dv.y};
-#pragma unroll
-      for (int e = 0; e < 2; e++) {
-        float x0 = cg_cell_coord(ix + h + e, p.box.dx, p.box.p0);
-        float r = cg_norm3(x0, y0, z0);
-        float lam = pois_lambda(p, dd[e], r);
-        int n = 0;
-        const long long cid = c0 + h + e;
-        if (lam > 1073741824.0f) {
-          atomicOr(p.err, ERR_COUNT_OVERFLOW);
-        } else if (lam > 0.0f) {
-          n = cg_poisson(lam, p.kp0, p.kp1, (uint32_t)cid, (uint32_t)(cid >> 32));
-        }
-        if (n >= CG_COUNT_ESC) {
-          const int k = atomicAdd(p.ovf_n, 1);
-          if (k < CG_OVF_CAP) {
-            p.ovf_cell[k] = cid;
-            p.ovf_cnt[k] = n;
-          } else {
-            atomicOr(p.err, ERR_COUNT_OVERFLOW);
-          }
-          cnt[h + e] = (unsigned short)CG_COUNT_ESC;
-        } else {
-          cnt[h + e] = (unsigned short)n;
-        }
-        tot += n;
+    unsigned long long lo = 0, hi = 0;
+#pragma unroll 1
+    for (int h = 0; h < CPT; h++) {
+      const float x0 = cg_cell_coord(ix + h, p.box.dx, p.box.p0);
+      const float r = cg_norm3(x0, y0, z0);
+      const float lam = pois_lambda(p, __ldg(row + h), r);
+      int n = 0;
+      const long long cid = c0 + h;
+      if (lam > 1073741824.0f) {
+        atomicOr(p.err, ERR_COUNT_OVERFLOW);
+      } else if (lam > 0.0f) {
+        n = cg_poisson(lam, p.kp0, p.kp1, (uint32_t)cid, (uint32_t)(cid >> 32));
       }
+      unsigned long long v = (unsigned long long)n;
+      if (n >= CG_COUNT_ESC) {
+        const int k = atomicAdd(p.ovf_n, 1);
+        if (k < CG_OVF_CAP) {
+          p.ovf_cell[k] = cid;
+          p.ovf_cnt[k] = n;
+        } else {
+          atomicOr(p.err, ERR_COUNT_OVERFLOW);
+        }
+        v = CG_COUNT_ESC;
+      }
+      if (h < 4) lo |= v << (16 * h);
+      else hi |= v << (16 * (h - 4));
+      tot += n;
     }
-    uint4 pk;
-    pk.x = cnt[0] | ((unsigned)cnt[1] << 16);
-    pk.y = cnt[2] | ((unsigned)cnt[3] << 16);
-    pk.z = cnt[4] | ((unsigned)cnt[5] << 16);
-    pk.w = cnt[6] | ((unsigned)cnt[7] << 16);
-    *reinterpret_cast<uint4 *>(p.counts + c0) = pk;
+    *reinterpret_cast<uint4 *>(p.counts + c0) =
+        make_uint4((unsigned)lo, (unsigned)(lo >> 32), (unsigned)hi, (unsigned)(hi >> 32));
   }
-  /* block total; k_emit scans a block in int, so it must stay below 2^31 */
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
-  __shared__ long long ws[SB / 32];
-  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = tot;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    long long s = 0;
-    for (int w = 0; w < SB / 32; w++) s += ws[w];
-    if (s > 0x7fffffffLL) atomicOr(p.err, ERR_COUNT_OVERFLOW);
-    p.block_sums[blockIdx.x] = s;
-  }
+  if ((threadIdx.x & 31) == 0 && tot)
+    atomicAdd(reinterpret_cast<unsigned long long *>(&p.block_sums[blockIdx.x]), (unsigned long long)tot);
 }
 
 /* Exclusive scan of n block totals in place; total into *total. */
-__global__ void __launch_bounds__(1024) k_scan(long long *v, long long n, long long *total)
+__global__ void __launch_bounds__(1024) k_scan(long long *v, long long n, long long *total, unsigned int *err)
 {
   __shared__ long long s[1024];
   const long long per = (n + 1023) / 1024;
   const long long b = (long long)threadIdx.x * per, e = (b + per < n) ? b + per : n;
   long long acc = 0;
-  for (long long i = b; i < e; i++) acc += v[i];
+  for (long long i = b; i < e; i++) {
+    const long long x = v[i];
+    if (x > 0x7fffffffLL) atomicOr(err, ERR_COUNT_OVERFLOW); /* k_emit scans a block in int */
+    acc += x;
+  }
   s[threadIdx.x] = acc;
   __syncthreads();
   for (int o = 1; o < 1024; o <<= 1) {
@@ -453,9 +448,10 @@ cudaError_t cg_srcs_count(cudaStream_t s, const float *grid, const cg_srcs_param
 {
   long long nb = cg_srcs_nblocks(p->box.N);
   cudaError_t e = cudaMemsetAsync(p->ovf_n, 0, sizeof(int), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(p->block_sums, 0, nb * sizeof(long long), s);
   if (e != cudaSuccess) return e;
   k_pois_count<<<(unsigned)nb, SB, 0, s>>>(grid, *p);
-  k_scan<<<1, 1024, 0, s>>>(p->block_sums, nb, total);
+  k_scan<<<1, 1024, 0, s>>>(p->block_sums, nb, total, p->err);
   return cudaGetLastError();
 }
 
