@@ -81,6 +81,7 @@ struct cg_ctx {
   /* normalisation bins (density.c:1233-1245): z(r_i) of the table radii,
    * z(L/2), the bin count and width; bin buffers keep their capacity */
   double *d_zr = nullptr;
+  int *d_r2n = nullptr; /* RING -> NEST ids at nside_base (base pixels of the sources) */
   double norm_zlast = 0, norm_idz = 0;
   int norm_nz = 0;
   int bins_nz_cap = 0, bins_nt_cap = 0;
@@ -424,6 +425,15 @@ extern "C" int cg_upload_tables(cg_ctx *c, const cg_config *cfg)
     for (int p = 0; p < cfg->n_cstm; p++)
       c->normc[p] = Tab{c->d_norm + (size_t)(cfg->n_srcs + cfg->n_imap + p) * nas, 1.0f, 1.0f};
   }
+  /* RING -> NEST table of the base pixels (srcs.c:268-270) */
+  if (cfg->n_srcs > 0 && cfg->nside_base <= 1024) {
+    const long long nb = 12LL * cfg->nside_base * cfg->nside_base;
+    std::vector<int> t((size_t)nb);
+    for (long long i = 0; i < nb; i++) t[(size_t)i] = (int)cg_ring2nest(cfg->nside_base, i);
+    if (int rc = dalloc(c, &c->d_r2n, (size_t)nb)) return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_r2n, t.data(), nb * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host staging vector */
+  }
   /* redshift bins of compute_density_normalization (density.c:1233-1245) and
    * z at the table radii, for the device-side tables */
   {
@@ -520,7 +530,7 @@ extern "C" void cg_destroy(cg_ctx *c)
     cudaEventDestroy(c->graph_done);
     c->graph_done = nullptr;
   }
-  void *ptrs[] = {c->d_tabs, c->d_norm, c->d_zr, c->d_pk, c->d_twN, c->d_twH, c->d_dens, c->d_npot, c->d_disp[0],
+  void *ptrs[] = {c->d_tabs, c->d_norm, c->d_zr, c->d_r2n, c->d_pk, c->d_twN, c->d_twH, c->d_dens, c->d_npot, c->d_disp[0],
                   c->d_disp[1], c->d_disp[2], c->d_part, c->d_stats, c->d_s2f, c->d_err, c->d_ncount,
                   c->d_zsum, c->d_bsum, c->d_counts, c->d_bsums, c->d_total, c->d_tmpmap, c->d_kmap,
                   c->d_kfac, c->d_kinv, c->d_kir, c->d_ovf_cell, c->d_ovf_cnt, c->d_ovf_n,
@@ -924,6 +934,7 @@ static void srcs_params(cg_ctx *c, int ipop, cg_srcs_params &p)
   p.factor_vel = (float)(-c->cfg.fgrowth_0 / (1.5 * c->cfg.hubble_0 * c->cfg.omega_m));
   p.need_beaming = c->cfg.need_beaming;
   p.nside_base = c->cfg.nside_base;
+  p.base_r2n = c->d_r2n;
   p.nside_count = c->cfg.nside_count[ipop];
   p.cmap = c->cat[ipop].cmap;
   p.counts = c->d_counts;

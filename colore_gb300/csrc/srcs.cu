@@ -244,7 +244,9 @@ __global__ void __launch_bounds__(SB) k_emit(const float *__restrict__ phi, cg_s
     float r, cth, ph;
     cg_cart2sph(px, py, pz, &r, &cth, &ph);
     int64_t pr = cg_ang2pix_ring(p.nside_base, cth, ph);
-    p.ipix[id] = (int)cg_ring2nest(p.nside_base, pr);
+    /* ring2nest costs several 64-bit divisions; nside_base is small, so its
+     * table (built on the host with the same function) replaces them */
+    p.ipix[id] = p.base_r2n ? __ldg(p.base_r2n + pr) : (int)cg_ring2nest(p.nside_base, pr);
     float *q = p.src + (size_t)id * 9;
     cg_radec(cth, ph, &q[0], &q[1]);                              /* ra, dec */
     q[2] = bg(p.zt, p.g, r);                                      /* z0  */

@@ -23,6 +23,7 @@ struct cg_srcs_params {
   float factor_vel;  /* -f0/(1.5 H0 Om), srcs.c:233 */
   int need_beaming;
   int64_t nside_base, nside_count;
+  const int *base_r2n;       /* RING -> NEST ids at nside_base, or NULL (computed per source) */
   int *cmap;                 /* count map or NULL */
   unsigned short *counts;    /* N^3; CG_COUNT_ESC marks a cell in the overflow list */
   long long *ovf_cell;       /* cells holding CG_COUNT_ESC or more sources ...     */
