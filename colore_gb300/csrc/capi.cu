@@ -91,6 +91,9 @@ struct cg_ctx {
   FillParams fill;
   /* grids */
   float *d_dens = nullptr, *d_npot = nullptr, *d_disp[3] = {nullptr, nullptr, nullptr};
+  /* 2LPT work grids: the six second derivatives, then the source in [5]
+   * and the second-order displacements in [0..2] */
+  float *d_lpt2[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   double2 *d_part = nullptr;
   size_t npart = 0;
   double *d_stats = nullptr;
@@ -275,6 +278,18 @@ static cudaError_t run_lpt(int n, const cg_field_launch *L)
   return cudaErrorInvalidValue;
 }
 
+static cudaError_t run_lpt2(int n, const cg_field_launch *L)
+{
+  switch (n) {
+#define X(k) \
+  case k:    \
+    return cg_field_lpt2_##k(L);
+    CG_FIELD_SIZES(X)
+#undef X
+  }
+  return cudaErrorInvalidValue;
+}
+
 static size_t npartials(int n)
 {
   switch (n) {
@@ -311,9 +326,11 @@ static int validate(const cg_config *cfg, char *msg, size_t len)
   for (int i = 0; i < cfg->n_cstm; i++)
     if (!cfg->cstm_kz_arr[i] || !cfg->cstm_bz_arr[i] || cfg->nside_cstm[i] < 1)
       return snprintf(msg, len, "custom-map table missing or nside < 1"), CG_EINVAL;
-  if (cfg->dens_type == CG_DENS_1LPT && (cfg->lpt_interp_type < 0 || cfg->lpt_interp_type > 2))
+  if ((cfg->dens_type == CG_DENS_1LPT || cfg->dens_type == CG_DENS_2LPT) &&
+      (cfg->lpt_interp_type < 0 || cfg->lpt_interp_type > 2))
     return snprintf(msg, len, "lpt_interp_type %d: 0 (NGP), 1 (CIC) or 2 (TSC)", cfg->lpt_interp_type), CG_EINVAL;
-  if (cfg->dens_type != CG_DENS_LGNR && cfg->dens_type != CG_DENS_1LPT && cfg->dens_type != CG_DENS_CLIP)
+  if (cfg->dens_type != CG_DENS_LGNR && cfg->dens_type != CG_DENS_1LPT && cfg->dens_type != CG_DENS_2LPT &&
+      cfg->dens_type != CG_DENS_CLIP)
     return snprintf(msg, len, "dens_type %d not supported", cfg->dens_type), CG_EINVAL;
   const double *req[] = {cfg->r_arr_r2z, cfg->z_arr_r2z, cfg->growth_d_arr, cfg->growth_d2_arr, cfg->growth_v_arr,
                          cfg->growth_pd_arr, cfg->ihub_arr, cfg->a_arr_a2r, cfg->r_arr_a2r};
@@ -500,6 +517,7 @@ extern "C" int cg_memory_estimate(const cg_config *cfg, unsigned long long *byte
   unsigned long long grid = N * N * NH * 8ull;
   unsigned long long b = 2 * grid;
   if (cfg->dens_type == CG_DENS_1LPT) b += 3 * grid;
+  if (cfg->dens_type == CG_DENS_2LPT) b += 9 * grid;
   if (cfg->n_srcs > 0) b += N * N * N * 2ull;
   for (int i = 0; i < cfg->n_imap; i++)
     b += (unsigned long long)cfg->imap_nr[i] * 12ull * cfg->nside_imap[i] * cfg->nside_imap[i] * 8ull;
@@ -530,6 +548,8 @@ extern "C" void cg_destroy(cg_ctx *c)
     cudaEventDestroy(c->graph_done);
     c->graph_done = nullptr;
   }
+  for (float *q : c->d_lpt2)
+    if (q) cudaFree(q);
   void *ptrs[] = {c->d_tabs, c->d_norm, c->d_zr, c->d_r2n, c->d_pk, c->d_twN, c->d_twH, c->d_dens, c->d_npot, c->d_disp[0],
                   c->d_disp[1], c->d_disp[2], c->d_part, c->d_stats, c->d_s2f, c->d_err, c->d_ncount,
                   c->d_zsum, c->d_bsum, c->d_counts, c->d_bsums, c->d_total, c->d_tmpmap, c->d_kmap,
@@ -664,16 +684,36 @@ extern "C" int cg_compute_physical_density_field(cg_ctx *c)
     c->pending_mode = CG_DMODE_CLIP;
   } else {
     int rc;
+    const bool two = c->cfg.dens_type == CG_DENS_2LPT;
     for (int a = 0; a < 3; a++)
       if (!c->d_disp[a] && (rc = dalloc(c, &c->d_disp[a], c->grid_floats))) return rc;
+    if (two)
+      for (int a = 0; a < 6; a++)
+        if (!c->d_lpt2[a] && (rc = dalloc(c, &c->d_lpt2[a], c->grid_floats))) return rc;
     cg_field_launch L;
+    memset(&L, 0, sizeof(L));
     L.stream = c->stream;
-    for (int a = 0; a < 3; a++) L.f[a] = reinterpret_cast<float2 *>(c->d_disp[a]);
     L.fill = c->fill;
     L.norm = 1.0f;
     L.partials = nullptr;
     L.twN = c->d_twN;
     L.twH = c->d_twH;
+    if (two) { /* lpt_2, density.c:646-812 */
+      ProfScope ps(c, "lpt2_fft");
+      for (int set = 0; set < 2; set++) { /* xx xy xz, then yy yz zz */
+        L.fill.lpt_kind = 1 + set;
+        for (int a = 0; a < 3; a++) L.f[a] = reinterpret_cast<float2 *>(c->d_lpt2[3 * set + a]);
+        CUDA_TRY(c, run_lpt(c->N, &L));
+      }
+      CUDA_TRY(c, cg_lpt2_source(c->stream, c->d_lpt2[0], c->d_lpt2[1], c->d_lpt2[2], c->d_lpt2[3], c->d_lpt2[4],
+                                 c->d_lpt2[5], c->N, c->nsm));
+      L.src = reinterpret_cast<float2 *>(c->d_lpt2[5]);
+      for (int a = 0; a < 3; a++) L.f[a] = reinterpret_cast<float2 *>(c->d_lpt2[a]);
+      CUDA_TRY(c, run_lpt2(c->N, &L));
+      c->launches += 2 * 3 + 1 + 5;
+    }
+    L.fill.lpt_kind = 0;
+    for (int a = 0; a < 3; a++) L.f[a] = reinterpret_cast<float2 *>(c->d_disp[a]);
     {
       ProfScope ps(c, "lpt_fft");
       CUDA_TRY(c, run_lpt(c->N, &L));
@@ -685,6 +725,10 @@ extern "C" int cg_compute_physical_density_field(cg_ctx *c)
     lp.g = c->g;
     lp.d1 = c->d1;
     lp.interp = c->cfg.lpt_interp_type;
+    lp.d2x = two ? c->d_lpt2[0] : nullptr;
+    lp.d2y = two ? c->d_lpt2[1] : nullptr;
+    lp.d2z = two ? c->d_lpt2[2] : nullptr;
+    lp.d2 = c->d2;
     CUDA_TRY(c, cg_lpt_cic(c->stream, c->d_dens, c->d_disp[0], c->d_disp[1], c->d_disp[2], &lp, c->nsm));
     c->launches += 4;
     c->pending_mode = CG_DMODE_RHO;
@@ -1708,6 +1752,7 @@ extern "C" int cg_download_grid(cg_ctx *c, int which, void *dst)
     src = c->d_dens;
   } else if (which == 1) src = c->d_npot;
   else if (which >= 2 && which <= 4) src = c->d_disp[which - 2];
+  else if (which >= 5 && which <= 7) src = c->d_lpt2[which - 5];
   if (!src) return fail(c, CG_ESTATE, "grid %d not available", which);
   CUDA_TRY(c, cudaMemcpyAsync(dst, src, c->grid_floats * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));

@@ -138,6 +138,7 @@ struct FillParams {
   float logkmin, logkmax, idlogk, n_scal;
   uint32_t key0, key1;
   float lpt_norm; /* (sqrt(2 pi)/L)^3, used by the 1LPT displacement fill */
+  int lpt_kind;   /* three-field fill: 0 Psi_x,y,z; 1 phi_xx,xy,xz; 2 phi_yy,yz,zz */
 };
 
 /* Geometry of the Cartesian box. */

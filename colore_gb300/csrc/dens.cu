@@ -219,12 +219,19 @@ __global__ void __launch_bounds__(256) k_lpt_deposit(float *grid, const float *_
     const float r = cg_norm3(xv[0], xv[1], xv[2]);
     const float dg = bg(p.d1, p.g, r);
     const float dsp[3] = {__ldg(&dx_[id]), __ldg(&dy_[id]), __ldg(&dz_[id])};
+    /* 2LPT: x = q + D1 Psi1 + D2 Psi2 (density.c:890) */
+    const bool two = p.d2x != nullptr;
+    const float d2g = two ? bg(p.d2, p.g, r) : 0.0f;
+    const float ds2[3] = {two ? __ldg(&p.d2x[id]) : 0.0f, two ? __ldg(&p.d2y[id]) : 0.0f,
+                          two ? __ldg(&p.d2z[id]) : 0.0f};
     int ib[3], bb[3]; /* first stencil cell of each axis, in the grid and in the box */
     float w[3][K];
     bool inbox = true;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-      float q = CG_ADD(CG_FMA(dg, dsp[a], xv[a]), po[a]);
+      float q = CG_FMA(dg, dsp[a], xv[a]);
+      if (two) q = CG_FMA(d2g, ds2[a], q);
+      q = CG_ADD(q, po[a]);
       if (q < 0.0f) q = CG_ADD(q, p.box.L);
       if (q >= p.box.L) q = CG_SUB(q, p.box.L);
       const float u = CG_MUL(q, iag);
@@ -341,7 +348,34 @@ __global__ void __launch_bounds__(256) k_norm_tables(const unsigned long long *_
   }
 }
 
+__global__ void __launch_bounds__(256) k_lpt2_source(const float *__restrict__ xx, const float *__restrict__ xy,
+                                                     const float *__restrict__ xz, const float *__restrict__ yy,
+                                                     const float *__restrict__ yz, float *zz, int N)
+{
+  const long long ncell = (long long)N * N * N;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncell;
+       c += (long long)gridDim.x * blockDim.x) {
+    const long long row = c / N;
+    const int ix = (int)(c - row * N);
+    const long long id = (long long)ix + (long long)(2 * (N / 2 + 1)) * row;
+    const float a = xx[id], b = yy[id], d = zz[id], e = xy[id], f = xz[id], g = yz[id];
+    float v = CG_ADD(CG_ADD(CG_MUL(a, b), CG_MUL(a, d)), CG_MUL(b, d));
+    v = CG_SUB(CG_SUB(CG_SUB(v, CG_MUL(e, e)), CG_MUL(f, f)), CG_MUL(g, g));
+    zz[id] = v;
+  }
+}
+
 } /* namespace */
+
+cudaError_t cg_lpt2_source(cudaStream_t s, const float *xx, const float *xy, const float *xz, const float *yy,
+                           const float *yz, float *zz, int N, int nsm)
+{
+  const long long ncell = (long long)N * N * N;
+  long long blocks = (ncell + 255) / 256;
+  if (blocks > (long long)nsm * 16) blocks = (long long)nsm * 16;
+  k_lpt2_source<<<(unsigned)blocks, 256, 0, s>>>(xx, xy, xz, yy, yz, zz, N);
+  return cudaGetLastError();
+}
 
 cudaError_t cg_norm_tables(cudaStream_t s, const unsigned long long *ncount, const double *zsum, const double *bsum,
                            int nz, int nt, double zlast, const double *zr, float *out)

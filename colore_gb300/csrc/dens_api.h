@@ -29,7 +29,15 @@ struct cg_lpt_params {
   cg::Grid1 g;
   cg::Tab d1;
   int interp; /* 0 NGP, 1 CIC, 2 TSC (pos_2_dens, density.c:178-187) */
+  /* 2LPT: second-order displacements and the D2 growth (density.c:890), or NULL */
+  const float *d2x, *d2y, *d2z;
+  cg::Tab d2;
 };
+/* Second-order source of 2LPT (density.c:739-759), in place into zz:
+ * xx yy + xx zz + yy zz - xy^2 - xz^2 - yz^2 over the N^3 cells of the
+ * padded grids. */
+cudaError_t cg_lpt2_source(cudaStream_t s, const float *xx, const float *xy, const float *xz, const float *yy,
+                           const float *yz, float *zz, int N, int nsm);
 
 cudaError_t cg_moments_final(cudaStream_t s, const double2 *part, size_t n, double inv_ncell, double *stats,
                              float *s2f);

@@ -18,6 +18,7 @@ struct cg_field_launch {
   double2 *partials;    /* per-block (sum d, sum d^2) of grid 0       */
   const float2 *twN;    /* exp(+2 pi i j/N), j < N                   */
   const float2 *twH;    /* exp(+2 pi i j/(N/2)), j < N/2             */
+  float2 *src;          /* 2LPT: the source grid (padded real in, destroyed) */
 };
 
 #define CG_FIELD_SIZES(X) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(1024) X(2048)
@@ -25,6 +26,7 @@ struct cg_field_launch {
 #define CG_FIELD_DECL(n)                                                 \
   extern "C" cudaError_t cg_field_gauss_##n(const cg_field_launch *L); \
   extern "C" cudaError_t cg_field_lpt_##n(const cg_field_launch *L);   \
+  extern "C" cudaError_t cg_field_lpt2_##n(const cg_field_launch *L);  \
   extern "C" size_t cg_field_npartials_##n(void);
 CG_FIELD_SIZES(CG_FIELD_DECL)
 #undef CG_FIELD_DECL

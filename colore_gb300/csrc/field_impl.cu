@@ -22,6 +22,11 @@
  * FFTW's c2r semantics for the kx = 0 and kx = N/2 planes (the imaginary
  * parts of each row's DC and Nyquist terms are ignored after the y and z
  * transforms) are reproduced by dropping those imaginary parts in pass 3.
+ *
+ * 2LPT (density.c:646-1031) adds the forward transform of the second-order
+ * source: an r2c row pass along x, the forward y pass, and a z pass that
+ * transforms forward, forms Psi2_a = -i k_a S_k / (N^3 k^2) for the three
+ * axes and transforms each back along z; the inverse y and x passes follow.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -89,7 +94,9 @@ __device__ __forceinline__ float2 gen_mode(const FillParams &p, int kx, int ky, 
 /* Field values of one mode: F = 2 -> (delta_k, phi_k) (fourier.c:337-352);
  * F = 3 -> 1LPT displacements i k_a delta'_k / (N^3 k^2) (density.c:430-436)
  * where delta'_k = r2c(delta_G) = N^3 norm H(delta_k) and H is the Hermitian
- * projection that the c2r applied on the kx = 0 and kx = N/2 planes. */
+ * projection that the c2r applied on the kx = 0 and kx = N/2 planes; with
+ * lpt_kind 1 or 2 the second derivatives i k_i (i k_j delta'_k / (N^3 k^2))
+ * of 2LPT (density.c:704-709), xx xy xz or yy yz zz. */
 template <int F>
 __device__ __forceinline__ void gen_fields(const FillParams &p, int kx, int ky, int kz, float2 *f)
 {
@@ -126,8 +133,18 @@ __device__ __forceinline__ void gen_fields(const FillParams &p, int kx, int ky, 
     }
     float s = p.lpt_norm / k2;
     float kv[3] = {(float)kx * p.dk, kcomp(ky, N, p.dk), kcomp(kz, N, p.dk)};
+    if (p.lpt_kind == 0) {
 #pragma unroll
-    for (int a = 0; a < 3; a++) f[a] = make_float2(-kv[a] * s * d.y, kv[a] * s * d.x);
+      for (int a = 0; a < 3; a++) f[a] = make_float2(-kv[a] * s * d.y, kv[a] * s * d.x);
+    } else {
+      const float ki[3] = {p.lpt_kind == 1 ? kv[0] : kv[1], p.lpt_kind == 1 ? kv[0] : kv[1], p.lpt_kind == 1 ? kv[0] : kv[2]};
+      const float kj[3] = {p.lpt_kind == 1 ? kv[0] : kv[1], p.lpt_kind == 1 ? kv[1] : kv[2], kv[2]};
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        const float g = -ki[a] * kj[a] * s;
+        f[a] = make_float2(g * d.x, g * d.y);
+      }
+    }
   }
 }
 
@@ -167,8 +184,9 @@ __global__ void __launch_bounds__(TX *PF) k_fill_z(float2 *o0, float2 *o1, float
   }
 }
 
-/* Pass 2: in-place column transform along y.  grid = (ceil(NH/TX), N, nf). */
-template <int TX>
+/* Pass 2: in-place column transform along y (inverse, S = 1, or forward,
+ * S = -1).  grid = (ceil(NH/TX), N, nf). */
+template <int TX, int S>
 __global__ void __launch_bounds__(TX *P) k_col_y(float2 *f0, float2 *f1, float2 *f2,
                                                  const float2 *__restrict__ twN)
 {
@@ -183,7 +201,86 @@ __global__ void __launch_bounds__(TX *P) k_col_y(float2 *f0, float2 *f1, float2 
   auto st = [&](int pos, float2 v) {
     if (ok) base[(size_t)pos * NH] = v;
   };
-  cgfft::transform<N, PL::CR, PL::C0, PL::C1, PL::C2, 1>(t, twN, ld, st, sm);
+  cgfft::transform<N, PL::CR, PL::C0, PL::C1, PL::C2, S>(t, twN, ld, st, sm);
+}
+
+/* Forward pass 1 of the 2LPT source: row r2c along x, in place.  A row's N
+ * reals are read as N/2 complex z_j = x_2j + i x_2j+1, transformed forward,
+ * and split into the N/2 + 1 modes
+ *   X_k = (E_k - i e^{-2 pi i k/N} O_k) / 2,  E_k = Z_k + conj Z_{N/2-k},
+ *   O_k = Z_k - conj Z_{N/2-k}  (Z_{N/2} = Z_0).
+ * The half-length spectrum goes to its own shared buffer: the exchange
+ * buffer may still be read by other threads when the last stage stores. */
+__global__ void __launch_bounds__(PL::RB *PR) k_row_r2c(float2 *f, const float2 *__restrict__ twN,
+                                                        const float2 *__restrict__ twH)
+{
+  extern __shared__ float2 smem[];
+  float2 *zb = smem + PL::RB * ROWS;
+  const int t = threadIdx.x % PR, rl = threadIdx.x / PR;
+  const size_t row0 = (size_t)blockIdx.x * PL::RB;
+  const float2 *src = f + row0 * NH;
+  for (int i = threadIdx.x; i < PL::RB * NH; i += PL::RB * PR) {
+    int r = i / NH, k = i - r * NH;
+    if (k < LH) smem[r * ROWS + k] = src[i];
+  }
+  __syncthreads();
+  float2 *row = smem + rl * ROWS;
+  float2 *z = zb + rl * LH;
+  auto ld = [&](int j) -> float2 { return row[j]; };
+  auto sm = [&](int pos) -> float2 & { return row[pos + (pos >> 5)]; };
+  auto st = [&](int n, float2 v) { z[n] = v; };
+  cgfft::transform<LH, PL::RR, PL::R0, PL::R1, PL::R2, -1>(t, twH, ld, st, sm);
+  __syncthreads();
+  float2 *dst = f + (row0 + rl) * NH;
+  for (int k = t; k <= LH; k += PR) {
+    const float2 a = z[k == LH ? 0 : k], b = z[k == 0 ? 0 : LH - k];
+    const float2 e = make_float2(a.x + b.x, a.y - b.y), o = make_float2(a.x - b.x, a.y + b.y);
+    const float2 w = __ldg(&twN[k]); /* exp(+2 pi i k/N); the split takes its conjugate */
+    const float2 wo = make_float2(w.x * o.x + w.y * o.y, w.x * o.y - w.y * o.x);
+    dst[k] = make_float2(0.5f * (e.x + wo.y), 0.5f * (e.y - wo.x));
+  }
+}
+
+/* Forward z pass of the 2LPT source with the second-order displacement
+ * fill (density.c:764-809): per column (kx, ky) the forward transform along
+ * z into shared memory, then for each axis a the product
+ * -i k_a S_k / (N^3 k^2) (0 at k = 0) transformed back along z.
+ * grid = (ceil(NH/TX), N). */
+template <int TX>
+__global__ void __launch_bounds__(TX *PF) k_z_lpt2(const float2 *__restrict__ src, float2 *o0, float2 *o1,
+                                                   float2 *o2, float dk, float inv_n3,
+                                                   const float2 *__restrict__ twN)
+{
+  extern __shared__ float2 smem[];
+  float2 *X = smem + (size_t)N * TX;
+  const int c = threadIdx.x % TX, t = threadIdx.x / TX;
+  const int kx = blockIdx.x * TX + c, ky = blockIdx.y;
+  const bool ok = kx < NH;
+  auto sm = [&](int pos) -> float2 & { return smem[pos * TX + c]; };
+  auto ld = [&](int pos) -> float2 { return ok ? src[((size_t)pos * N + ky) * NH + kx] : make_float2(0.0f, 0.0f); };
+  auto stx = [&](int pos, float2 v) { X[pos * TX + c] = v; };
+  cgfft::transform<N, PL::FR, PL::F0, PL::F1, PL::F2, -1>(t, twN, ld, stx, sm);
+  __syncthreads();
+  float2 *outs[3] = {o0, o1, o2};
+  const float kxf = (float)kx * dk, kyf = kcomp(ky, N, dk);
+#pragma unroll 1
+  for (int a = 0; a < 3; a++) {
+    auto ld2 = [&](int pos) -> float2 {
+      const float kzf = kcomp(pos, N, dk);
+      const float k2 = kxf * kxf + kyf * kyf + kzf * kzf;
+      if (!(k2 > 0.0f)) return make_float2(0.0f, 0.0f);
+      const float ka = a == 0 ? kxf : (a == 1 ? kyf : kzf);
+      const float g = ka * inv_n3 / k2;
+      const float2 v = X[pos * TX + c];
+      return make_float2(g * v.y, -g * v.x); /* -i g v */
+    };
+    float2 *o = outs[a];
+    auto st = [&](int pos, float2 v) {
+      if (ok) o[((size_t)pos * N + ky) * NH + kx] = v;
+    };
+    cgfft::transform<N, PL::FR, PL::F0, PL::F1, PL::F2, 1>(t, twN, ld2, st, sm);
+    __syncthreads();
+  }
 }
 
 /* Pass 3: row c2r along x with normalisation and optional moment sums.
@@ -275,13 +372,13 @@ extern "C" cudaError_t CG_CAT(cg_field_gauss_, CG_N)(const cg_field_launch *L)
   size_t sm3 = (size_t)PL::RB * ROWS * sizeof(float2);
   cudaError_t e;
   if ((e = prep(k_fill_z<2, TX2>, sm1)) != cudaSuccess) return e;
-  if ((e = prep(k_col_y<TXY>, sm2)) != cudaSuccess) return e;
+  if ((e = prep(k_col_y<TXY, 1>, sm2)) != cudaSuccess) return e;
   if ((e = prep(k_row_c2r<true>, sm3)) != cudaSuccess) return e;
   if ((e = prep(k_row_c2r<false>, sm3)) != cudaSuccess) return e;
   dim3 g1((NH + TX2 - 1) / TX2, N);
   k_fill_z<2, TX2><<<g1, TX2 * PF, sm1, L->stream>>>(L->f[0], L->f[1], nullptr, L->fill, L->twN);
   dim3 g2((NH + TXY - 1) / TXY, N, 2);
-  k_col_y<TXY><<<g2, TXY * P, sm2, L->stream>>>(L->f[0], L->f[1], nullptr, L->twN);
+  k_col_y<TXY, 1><<<g2, TXY * P, sm2, L->stream>>>(L->f[0], L->f[1], nullptr, L->twN);
   dim3 g3((unsigned)((size_t)N * N / PL::RB), 1);
   k_row_c2r<true><<<g3, PL::RB * PR, sm3, L->stream>>>(L->f[0], nullptr, nullptr, L->norm, L->partials,
                                                         L->twN, L->twH);
@@ -300,12 +397,44 @@ extern "C" cudaError_t CG_CAT(cg_field_lpt_, CG_N)(const cg_field_launch *L)
   size_t sm3 = (size_t)PL::RB * ROWS * sizeof(float2);
   cudaError_t e;
   if ((e = prep(k_fill_z<3, TX3>, sm1)) != cudaSuccess) return e;
-  if ((e = prep(k_col_y<TXY>, sm2)) != cudaSuccess) return e;
+  if ((e = prep(k_col_y<TXY, 1>, sm2)) != cudaSuccess) return e;
   if ((e = prep(k_row_c2r<false>, sm3)) != cudaSuccess) return e;
   dim3 g1((NH + TX3 - 1) / TX3, N);
   k_fill_z<3, TX3><<<g1, TX3 * PF, sm1, L->stream>>>(L->f[0], L->f[1], L->f[2], L->fill, L->twN);
   dim3 g2((NH + TXY - 1) / TXY, N, 3);
-  k_col_y<TXY><<<g2, TXY * P, sm2, L->stream>>>(L->f[0], L->f[1], L->f[2], L->twN);
+  k_col_y<TXY, 1><<<g2, TXY * P, sm2, L->stream>>>(L->f[0], L->f[1], L->f[2], L->twN);
+  dim3 g3((unsigned)((size_t)N * N / PL::RB), 3);
+  k_row_c2r<false><<<g3, PL::RB * PR, sm3, L->stream>>>(L->f[0], L->f[1], L->f[2], 1.0f, nullptr, L->twN,
+                                                         L->twH);
+  return cudaGetLastError();
+}
+
+/* 2LPT second-order displacements from the source grid L->src (padded
+ * real, overwritten): r2c along x, forward y, the fused z pass into
+ * L->f[0..2], then the inverse y and x passes of those three grids. */
+extern "C" cudaError_t CG_CAT(cg_field_lpt2_, CG_N)(const cg_field_launch *L)
+{
+  using namespace cg;
+  constexpr int TX3 = PL::TX3, TXY = PL::TXY;
+  size_t smr = (size_t)PL::RB * (ROWS + LH) * sizeof(float2);
+  size_t sm2 = (size_t)N * TXY * sizeof(float2);
+  size_t smz = (size_t)2 * N * TX3 * sizeof(float2);
+  size_t sm3 = (size_t)PL::RB * ROWS * sizeof(float2);
+  cudaError_t e;
+  if ((e = prep(k_row_r2c, smr)) != cudaSuccess) return e;
+  if ((e = prep(k_col_y<TXY, -1>, sm2)) != cudaSuccess) return e;
+  if ((e = prep(k_z_lpt2<TX3>, smz)) != cudaSuccess) return e;
+  if ((e = prep(k_col_y<TXY, 1>, sm2)) != cudaSuccess) return e;
+  if ((e = prep(k_row_c2r<false>, sm3)) != cudaSuccess) return e;
+  dim3 gr((unsigned)((size_t)N * N / PL::RB), 1);
+  k_row_r2c<<<gr, PL::RB * PR, smr, L->stream>>>(L->src, L->twN, L->twH);
+  dim3 gy1((NH + TXY - 1) / TXY, N, 1);
+  k_col_y<TXY, -1><<<gy1, TXY * P, sm2, L->stream>>>(L->src, nullptr, nullptr, L->twN);
+  dim3 gz((NH + TX3 - 1) / TX3, N);
+  const float inv_n3 = 1.0f / ((float)N * (float)N * (float)N);
+  k_z_lpt2<TX3><<<gz, TX3 * PF, smz, L->stream>>>(L->src, L->f[0], L->f[1], L->f[2], L->fill.dk, inv_n3, L->twN);
+  dim3 g2((NH + TXY - 1) / TXY, N, 3);
+  k_col_y<TXY, 1><<<g2, TXY * P, sm2, L->stream>>>(L->f[0], L->f[1], L->f[2], L->twN);
   dim3 g3((unsigned)((size_t)N * N / PL::RB), 3);
   k_row_c2r<false><<<g3, PL::RB * PR, sm3, L->stream>>>(L->f[0], L->f[1], L->f[2], 1.0f, nullptr, L->twN,
                                                          L->twH);

@@ -1046,6 +1046,7 @@ extern "C" int cg64_run_mock(cg64_ctx *c, float *ms)
   if (c->cfg.dens_type == CG_DENS_1LPT && c->cfg.lpt_interp_type != 1)
     return fail(c, CG_EINVAL, "the FP64 baseline deposits 1LPT particles with CIC only");
   if (c->cfg.n_cstm > 0 || c->cfg.do_isw) return fail(c, CG_EINVAL, "the FP64 baseline has no custom or ISW maps");
+  if (c->cfg.dens_type == CG_DENS_2LPT) return fail(c, CG_EINVAL, "the FP64 baseline has no 2LPT");
   if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, CG_ECUDA, "cudaSetDevice");
   cudaEvent_t a, b;
   CU(c, cudaEventCreate(&a));

@@ -58,6 +58,7 @@ extern "C" {
 /* dens_type values, src/common.h:115-118 */
 #define CG_DENS_LGNR 0
 #define CG_DENS_1LPT 1
+#define CG_DENS_2LPT 2
 #define CG_DENS_CLIP 3
 
 /* bias models, src/common.h:414-431 */
@@ -218,7 +219,8 @@ void cg_batch_destroy(cg_batch *b);
 
 /* Host mirrors -------------------------------------------------------------- */
 /* which: 0 = density (grid_dens), 1 = potential (grid_npot), 2..4 = 1LPT
- * displacement x,y,z.  dst holds N*N*2(N/2+1) values of the context's
+ * (first-order) displacement x,y,z, 5..7 = 2LPT second-order displacement
+ * x,y,z.  dst holds N*N*2(N/2+1) values of the context's
  * precision (float or double), padded layout. */
 int cg_download_grid(cg_ctx *ctx, int which, void *dst);
 long long cg_num_sources(cg_ctx *ctx, int ipop);

@@ -15,6 +15,7 @@
  *   or_isw64         isw_get_beam_properties       isw.c:78-147
  *   or_cstm_steps    custom-map step tables        cstm.c:81-116
  *   or_cstm64        cstm_get_beam_properties      cstm.c:68-145
+ *   or_lpt2_64       2LPT displacements + deposit  density.c:646-1031
  *   or_lens64        source lensing along the LOS  srcs.c:452-625, 715-723
  *   or_skw64         source skewers                srcs.c:509-536, 725-733
  *   or_run_mock64    the driver sequence of main.c:66-125 for timing.
@@ -40,6 +41,7 @@ static double bg(const cg_config *c, const double *f, double f0, double ff, doub
 #define BG_D1(c, r) bg((c), (c)->growth_d_arr, 1, (c)->growth_d_arr[CG_NA - 1], (r))
 #define BG_V1(c, r) bg((c), (c)->growth_v_arr, (c)->growth_v_arr[0], (c)->growth_v_arr[CG_NA - 1], (r))
 #define BG_IH(c, r) bg((c), (c)->ihub_arr, (c)->ihub_arr[0], (c)->ihub_arr[CG_NA - 1], (r))
+#define BG_D2(c, r) bg((c), (c)->growth_d2_arr, (c)->growth_d2_arr[0], (c)->growth_d2_arr[CG_NA - 1], (r))
 
 static double bias_model64(double d, double b, int model) /* common.h:414-431 */
 {
@@ -154,28 +156,13 @@ int or_density64(const cg_config *c, double *dens, double sigma2)
   return 0;
 }
 
-int or_lpt64(const cg_config *c, const double *dg_in, double *dens_out, double *disp)
+/* Particle positions q + D1 Psi1 (+ D2 Psi2 for 2LPT, density.c:890) and
+ * the mass assignment of pos_2_dens (density.c:178-187): NGP (37-62), CIC
+ * (64-105) or TSC (107-176); then rho - 1 (density.c:621, 1015). */
+static void lpt_deposit64(const cg_config *c, const double *disp, const double *disp2, double *dens_out)
 {
-  const int N = c->n_grid, NH = N / 2 + 1;
-  const size_t nh = (size_t)N * N * NH, ncell = (size_t)N * N * N;
-  double complex *dk = malloc(nh * sizeof(double complex)), *ck = malloc(nh * sizeof(double complex));
-  if (!dk || !ck) return -1;
-  or_r2c_3d(N, dg_in, dk); /* density.c:392 */
-  const double dkk = 2 * M_PI / c->l_box, fftnorm = (double)N * N * N;
-  for (int ax = 0; ax < 3; ax++) { /* density.c:408-440 */
-#pragma omp parallel for schedule(static)
-    for (int kz = 0; kz < N; kz++)
-      for (int ky = 0; ky < N; ky++)
-        for (int kx = 0; kx <= N / 2; kx++) {
-          double kv[3] = {kx * dkk, kc(ky, N, dkk), kc(kz, N, dkk)};
-          double k2 = fftnorm * (kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2]);
-          size_t idx = kx + (size_t)NH * (ky + (size_t)N * kz);
-          ck[idx] = k2 <= 0 ? 0 : I * kv[ax] * dk[idx] / k2;
-        }
-    or_c2r_3d(N, ck, disp + (size_t)ax * ncell);
-  }
-  free(dk);
-  free(ck);
+  const int N = c->n_grid;
+  const size_t ncell = (size_t)N * N * N;
   const double dx = c->l_box / N;
   memset(dens_out, 0, ncell * sizeof(double));
   /* positions (density.c:473-501) and the deposit of pos_2_dens
@@ -187,12 +174,13 @@ int or_lpt64(const cg_config *c, const double *dg_in, double *dens_out, double *
       for (int ix = 0; ix < N; ix++) {
         double xv[3] = {ix * dx - c->pos_obs[0], iy * dx - c->pos_obs[1], iz * dx - c->pos_obs[2]};
         double r = sqrt(xv[0] * xv[0] + xv[1] * xv[1] + xv[2] * xv[2]);
-        double g = BG_D1(c, r);
+        double g = BG_D1(c, r), g2 = disp2 ? BG_D2(c, r) : 0;
         size_t id = ix + (size_t)N * (iy + (size_t)N * iz);
         int ib[3], K = S + 1;
         double w[3][3];
         for (int ax = 0; ax < 3; ax++) {
-          double q = xv[ax] + g * disp[(size_t)ax * ncell + id] + c->pos_obs[ax];
+          double q = xv[ax] + g * disp[(size_t)ax * ncell + id] +
+                     (disp2 ? g2 * disp2[(size_t)ax * ncell + id] : 0) + c->pos_obs[ax];
           if (q < 0) q += c->l_box;
           if (q >= c->l_box) q -= c->l_box;
           double u = q * iag;
@@ -221,7 +209,101 @@ int or_lpt64(const cg_config *c, const double *dg_in, double *dens_out, double *
               dens_out[gx + (size_t)N * (gy + (size_t)N * gz)] += w[0][cx] * w[1][cy] * w[2][cz];
             }
       }
-  for (size_t i = 0; i < ncell; i++) dens_out[i] -= 1; /* density.c:621 */
+  for (size_t i = 0; i < ncell; i++) dens_out[i] -= 1;
+}
+
+int or_lpt64(const cg_config *c, const double *dg_in, double *dens_out, double *disp)
+{
+  const int N = c->n_grid, NH = N / 2 + 1;
+  const size_t nh = (size_t)N * N * NH, ncell = (size_t)N * N * N;
+  double complex *dk = malloc(nh * sizeof(double complex)), *ck = malloc(nh * sizeof(double complex));
+  if (!dk || !ck) return -1;
+  or_r2c_3d(N, dg_in, dk); /* density.c:392 */
+  const double dkk = 2 * M_PI / c->l_box, fftnorm = (double)N * N * N;
+  for (int ax = 0; ax < 3; ax++) { /* density.c:408-440 */
+#pragma omp parallel for schedule(static)
+    for (int kz = 0; kz < N; kz++)
+      for (int ky = 0; ky < N; ky++)
+        for (int kx = 0; kx <= N / 2; kx++) {
+          double kv[3] = {kx * dkk, kc(ky, N, dkk), kc(kz, N, dkk)};
+          double k2 = fftnorm * (kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2]);
+          size_t idx = kx + (size_t)NH * (ky + (size_t)N * kz);
+          ck[idx] = k2 <= 0 ? 0 : I * kv[ax] * dk[idx] / k2;
+        }
+    or_c2r_3d(N, ck, disp + (size_t)ax * ncell);
+  }
+  free(dk);
+  free(ck);
+  lpt_deposit64(c, disp, NULL, dens_out);
+  return 0;
+}
+
+/* lpt_2 (density.c:646-1031) in double precision: r2c of the Gaussian
+ * density, the six second derivatives of the first-order potential, the
+ * source xx yy + xx zz + yy zz - xy^2 - xz^2 - yz^2, its r2c, the
+ * second-order displacements -i k S_k / (N^3 k^2), the first-order ones,
+ * positions q + D1 Psi1 + D2 Psi2 and the deposit.  disp, disp2: 3 N^3 each. */
+int or_lpt2_64(const cg_config *c, const double *dg_in, double *dens_out, double *disp, double *disp2)
+{
+  const int N = c->n_grid, NH = N / 2 + 1;
+  const size_t nh = (size_t)N * N * NH, ncell = (size_t)N * N * N;
+  double complex *dk = malloc(nh * sizeof(double complex)), *ck = malloc(nh * sizeof(double complex));
+  double *dig = malloc(6 * ncell * sizeof(double));
+  if (!dk || !ck || !dig) return -1;
+  or_r2c_3d(N, dg_in, dk); /* density.c:667 */
+  const double dkk = 2 * M_PI / c->l_box, fftnorm = (double)N * N * N;
+  const int pi_[6] = {0, 0, 0, 1, 1, 2}, pj_[6] = {0, 1, 2, 1, 2, 2};
+  for (int m = 0; m < 6; m++) { /* density.c:688-709, 712-714 */
+#pragma omp parallel for schedule(static)
+    for (int kz = 0; kz < N; kz++)
+      for (int ky = 0; ky < N; ky++)
+        for (int kx = 0; kx <= N / 2; kx++) {
+          double kv[3] = {kx * dkk, kc(ky, N, dkk), kc(kz, N, dkk)};
+          double k2 = fftnorm * (kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2]);
+          size_t idx = kx + (size_t)NH * (ky + (size_t)N * kz);
+          double complex cd = k2 <= 0 ? 0 : I * kv[pi_[m]] * dk[idx] / k2;
+          ck[idx] = I * kv[pj_[m]] * cd;
+        }
+    or_c2r_3d(N, ck, dig + (size_t)m * ncell);
+  }
+  double *src = malloc(ncell * sizeof(double));
+  if (!src) return -1;
+  for (size_t i = 0; i < ncell; i++) { /* density.c:749-755 */
+    const double *g = dig + i;
+    src[i] = g[0] * g[3 * ncell] + g[0] * g[5 * ncell] + g[3 * ncell] * g[5 * ncell] - g[ncell] * g[ncell] -
+             g[2 * ncell] * g[2 * ncell] - g[4 * ncell] * g[4 * ncell];
+  }
+  free(dig);
+  double complex *sk = malloc(nh * sizeof(double complex));
+  if (!sk) return -1;
+  or_r2c_3d(N, src, sk); /* density.c:763 */
+  free(src);
+  for (int ax = 0; ax < 3; ax++) {
+#pragma omp parallel for schedule(static)
+    for (int kz = 0; kz < N; kz++)
+      for (int ky = 0; ky < N; ky++)
+        for (int kx = 0; kx <= N / 2; kx++) {
+          double kv[3] = {kx * dkk, kc(ky, N, dkk), kc(kz, N, dkk)};
+          double k2 = fftnorm * (kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2]);
+          size_t idx = kx + (size_t)NH * (ky + (size_t)N * kz);
+          ck[idx] = k2 <= 0 ? 0 : -I * kv[ax] * sk[idx] / k2; /* density.c:802-805 */
+        }
+    or_c2r_3d(N, ck, disp2 + (size_t)ax * ncell);
+#pragma omp parallel for schedule(static)
+    for (int kz = 0; kz < N; kz++)
+      for (int ky = 0; ky < N; ky++)
+        for (int kx = 0; kx <= N / 2; kx++) {
+          double kv[3] = {kx * dkk, kc(ky, N, dkk), kc(kz, N, dkk)};
+          double k2 = fftnorm * (kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2]);
+          size_t idx = kx + (size_t)NH * (ky + (size_t)N * kz);
+          ck[idx] = k2 <= 0 ? 0 : I * kv[ax] * dk[idx] / k2; /* density.c:700-704 */
+        }
+    or_c2r_3d(N, ck, disp + (size_t)ax * ncell);
+  }
+  free(sk);
+  free(dk);
+  free(ck);
+  lpt_deposit64(c, disp, disp2, dens_out);
   return 0;
 }
 

@@ -39,6 +39,7 @@ int or_fill64(const cg_config *cfg, double complex *dk, double complex *pk);
 int or_field64(const cg_config *cfg, double *dens, double *npot, double stats[4]);
 int or_density64(const cg_config *cfg, double *dens, double sigma2);
 int or_lpt64(const cg_config *cfg, const double *dens_gauss, double *dens_out, double *disp);
+int or_lpt2_64(const cg_config *cfg, const double *dens_gauss, double *dens_out, double *disp, double *disp2);
 int or_bins64(const cg_config *cfg, const double *dens, int nz, double idz, unsigned long long *narr, double *zarr,
               double *bsum);
 int or_norm_tables64(const cg_config *cfg, double *tabs, double *e0f, int *nz_out, unsigned long long *narr,

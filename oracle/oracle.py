@@ -25,7 +25,7 @@ def lib():
         vp, d, i, f = C.c_void_p, C.c_double, C.c_int, C.c_float
         sig = {
             "or_fill64": [vp, vp, vp], "or_field64": [vp, vp, vp, vp], "or_density64": [vp, vp, d],
-            "or_lpt64": [vp, vp, vp, vp], "or_bins64": [vp, vp, i, d, vp, vp, vp],
+            "or_lpt64": [vp, vp, vp, vp], "or_lpt2_64": [vp, vp, vp, vp, vp], "or_bins64": [vp, vp, i, d, vp, vp, vp],
             "or_norm_tables64": [vp, vp, vp, vp, vp, vp, vp, vp],
             "or_lambda64": [vp, i, vp, vp, d, d, vp], "or_kappa64": [vp, vp, vp],
             "or_imap64": [vp, i, vp, vp, vp, d, d, vp, vp], "or_run_mock64": [vp, i, vp, vp],
@@ -106,6 +106,17 @@ def lpt64(cfg, dens_gauss):
     disp = np.empty((3, n, n, n))
     assert lib().or_lpt64(cfgp(cfg), P(dg), P(out), P(disp)) == 0
     return out, disp
+
+
+def lpt2_64(cfg, dens_gauss):
+    """2LPT in double: (density, first-order displacements, second-order ones)."""
+    n = cfg.n_grid
+    dg = np.ascontiguousarray(dens_gauss, np.float64)
+    out = np.empty((n, n, n))
+    d1 = np.empty((3, n, n, n))
+    d2 = np.empty((3, n, n, n))
+    assert lib().or_lpt2_64(cfgp(cfg), P(dg), P(out), P(d1), P(d2)) == 0
+    return out, d1, d2
 
 
 def norm_tables64(cfg, dens):

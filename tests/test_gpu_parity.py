@@ -57,6 +57,11 @@ def _spec(kind):
         base["srcs"] = [dict(nz=("gauss", 0.3, 0.15), density=30.0, bias=("const", 1.3), nside_count=16)]
         base.pop("imap")
         base.pop("kappa")
+    elif kind == "lpt2":
+        base["dens_type"] = 2
+        base["seed"] = 47
+        base["srcs"] = base["srcs"][:1]
+        base.pop("kappa")
     elif kind in ("lpt_ngp", "lpt_tsc"):
         base["dens_type"] = 1
         base["lpt_interp_type"] = 0 if kind == "lpt_ngp" else 2
@@ -112,8 +117,10 @@ class Run:
         self.phi = m.grid(1).copy()
         self.s2, self.mean = m.sigma2()
         m.compute_physical_density_field()
-        if self.cfg.dens_type == 1:
+        if self.cfg.dens_type in (1, 2):
             self.disp = [m.grid(w).copy() for w in (2, 3, 4)]
+        if self.cfg.dens_type == 2:
+            self.disp2 = [m.grid(w).copy() for w in (5, 6, 7)]
         m.compute_density_normalization()
         self.d = m.grid(0).copy()
         self.norm_s = [m.norm_table(0, i) for i in range(self.cfg.n_srcs)]
@@ -226,6 +233,23 @@ def test_lpt_vs_fp64_literal_path(runs):
     for a in range(3):
         assert rel_rms(unpad(r.need('disp')[a]), disp[a]) < 2e-5, a
     assert rel_rms(unpad(r.need('d')), out) < 1e-4
+
+
+def test_2lpt_vs_fp64(runs):
+    """2LPT (density.c:646-1031): first- and second-order displacements and
+    the deposited density against the FP64 restatement, which takes the
+    reference's literal route (r2c of the Gaussian field and of the source).
+    The second order goes through an FP32 r2c of a source made of products
+    of FP32 derivatives: relative rms 1e-4."""
+    import oracle as orc
+    r = runs("lpt2")
+    d64, _, _ = orc.field64(r.cfg)
+    out, d1, d2 = orc.lpt2_64(r.cfg, d64)
+    for a in range(3):
+        assert rel_rms(unpad(r.need('disp')[a]), d1[a]) < 2e-5, a
+        assert rel_rms(unpad(r.need('disp2')[a]), d2[a]) < 1e-4, (a, rel_rms(unpad(r.need('disp2')[a]), d2[a]))
+    assert rel_rms(unpad(r.need('d')), out) < 1e-4
+    assert np.std(d2[0]) > 1e-3 * np.std(d1[0])
 
 
 @pytest.mark.parametrize("kind", ["lpt_ngp", "lpt_tsc"])
