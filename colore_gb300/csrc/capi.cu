@@ -206,7 +206,8 @@ static int check_device_errors(cg_ctx *c)
   if (h) {
     CUDA_TRY(c, cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), c->stream));
     return fail(c, CG_EDEVICE, "device error flags 0x%x (1: source count overflow, 2: catalog overflow, "
-                               "4: shell search, 8: imap sub-sampling, 16: imap cell list)", h);
+                               "4: shell search, 8: imap sub-sampling, 16: imap cell list, 32: bulk copy timeout)",
+                h);
   }
   return CG_OK;
 }
@@ -648,6 +649,8 @@ extern "C" int cg_create_cartesian_fields(cg_ctx *c)
   L.partials = c->d_part;
   L.twN = c->d_twN;
   L.twH = c->d_twH;
+  L.src = nullptr;
+  L.err = c->d_err;
   {
     ProfScope ps(c, "field_fft");
     CUDA_TRY(c, run_gauss(c->N, &L));
@@ -698,6 +701,7 @@ extern "C" int cg_compute_physical_density_field(cg_ctx *c)
     L.partials = nullptr;
     L.twN = c->d_twN;
     L.twH = c->d_twH;
+    L.err = c->d_err;
     if (two) { /* lpt_2, density.c:646-812 */
       ProfScope ps(c, "lpt2_fft");
       for (int set = 0; set < 2; set++) { /* xx xy xz, then yy yz zz */

@@ -15,7 +15,9 @@
  *   2. y        : the same column transform along y, read-modify-write.
  *   3. x (c2r)  : a group of threads owns one row of N/2+1 complex values;
  *                 the Hermitian even/odd split turns the length-N real
- *                 inverse into a length-N/2 complex one.  The normalisation
+ *                 inverse into a length-N/2 complex one.  The block's rows
+ *                 (contiguous in HBM) are staged into shared memory by one
+ *                 bulk copy of the copy engine.  The normalisation
  *                 (sqrt(2 pi)/L)^3 (fourier.c:383-398) and the partial sums
  *                 of <d> and <d^2> (fourier.c:24-79) are fused here.
  *
@@ -32,6 +34,7 @@
 #include <stdint.h>
 
 #include "cg_dev.cuh"
+#include "cg_tma.cuh"
 #include "fft.cuh"
 #include "field_api.h"
 #include "fft_plans.h"
@@ -212,21 +215,18 @@ __global__ void __launch_bounds__(TX *P) k_col_y(float2 *f0, float2 *f1, float2 
  * The half-length spectrum goes to its own shared buffer: the exchange
  * buffer may still be read by other threads when the last stage stores. */
 __global__ void __launch_bounds__(PL::RB *PR) k_row_r2c(float2 *f, const float2 *__restrict__ twN,
-                                                        const float2 *__restrict__ twH)
+                                                        const float2 *__restrict__ twH, unsigned int *err)
 {
-  extern __shared__ float2 smem[];
+  extern __shared__ __align__(16) float2 smem[];
+  __shared__ uint64_t bar;
   float2 *zb = smem + PL::RB * ROWS;
   const int t = threadIdx.x % PR, rl = threadIdx.x / PR;
   const size_t row0 = (size_t)blockIdx.x * PL::RB;
-  const float2 *src = f + row0 * NH;
-  for (int i = threadIdx.x; i < PL::RB * NH; i += PL::RB * PR) {
-    int r = i / NH, k = i - r * NH;
-    if (k < LH) smem[r * ROWS + k] = src[i];
-  }
-  __syncthreads();
+  if (!cgtma::stage_rows(smem, f + row0 * NH, (unsigned)(PL::RB * NH * sizeof(float2)), &bar, err)) return;
+  const float2 *rin = smem + rl * NH;
   float2 *row = smem + rl * ROWS;
   float2 *z = zb + rl * LH;
-  auto ld = [&](int j) -> float2 { return row[j]; };
+  auto ld = [&](int j) -> float2 { return rin[j]; };
   auto sm = [&](int pos) -> float2 & { return row[pos + (pos >> 5)]; };
   auto st = [&](int n, float2 v) { z[n] = v; };
   cgfft::transform<LH, PL::RR, PL::R0, PL::R1, PL::R2, -1>(t, twH, ld, st, sm);
@@ -288,23 +288,23 @@ __global__ void __launch_bounds__(TX *PF) k_z_lpt2(const float2 *__restrict__ sr
 template <bool STATS>
 __global__ void __launch_bounds__(PL::RB *PR) k_row_c2r(float2 *f0, float2 *f1, float2 *f2, float norm,
                                                         double2 *partials, const float2 *__restrict__ twN,
-                                                        const float2 *__restrict__ twH)
+                                                        const float2 *__restrict__ twH, unsigned int *err)
 {
-  extern __shared__ float2 smem[];
+  extern __shared__ __align__(16) float2 smem[];
+  __shared__ uint64_t bar;
   const int t = threadIdx.x % PR, rl = threadIdx.x / PR;
   float2 *f = blockIdx.y == 0 ? f0 : (blockIdx.y == 1 ? f1 : f2);
   const size_t row0 = (size_t)blockIdx.x * PL::RB;
-  /* stage the block's rows (contiguous in memory) */
-  const float2 *src = f + row0 * NH;
-  for (int i = threadIdx.x; i < PL::RB * NH; i += PL::RB * PR) {
-    int r = i / NH, k = i - r * NH;
-    smem[r * ROWS + k] = src[i];
-  }
-  __syncthreads();
+  /* the block's rows, contiguous in HBM (RB NH float2, a multiple of 16
+   * bytes at a 16-byte boundary since RB is even), in one bulk copy; they
+   * land at a stride of NH and the transform then exchanges through the
+   * same buffer at the padded stride ROWS, once every input is loaded */
+  if (!cgtma::stage_rows(smem, f + row0 * NH, (unsigned)(PL::RB * NH * sizeof(float2)), &bar, err)) return;
+  const float2 *rin = smem + rl * NH;
   float2 *row = smem + rl * ROWS;
   float2 *dst = f + (row0 + rl) * NH;
   auto ld = [&](int j) -> float2 {
-    float2 a = row[j], b = row[LH - j];
+    float2 a = rin[j], b = rin[LH - j];
     if (j == 0) {
       a.y = 0.0f;
       b.y = 0.0f;
@@ -381,9 +381,9 @@ extern "C" cudaError_t CG_CAT(cg_field_gauss_, CG_N)(const cg_field_launch *L)
   k_col_y<TXY, 1><<<g2, TXY * P, sm2, L->stream>>>(L->f[0], L->f[1], nullptr, L->twN);
   dim3 g3((unsigned)((size_t)N * N / PL::RB), 1);
   k_row_c2r<true><<<g3, PL::RB * PR, sm3, L->stream>>>(L->f[0], nullptr, nullptr, L->norm, L->partials,
-                                                        L->twN, L->twH);
+                                                        L->twN, L->twH, L->err);
   k_row_c2r<false><<<g3, PL::RB * PR, sm3, L->stream>>>(L->f[1], nullptr, nullptr, L->norm, nullptr,
-                                                         L->twN, L->twH);
+                                                         L->twN, L->twH, L->err);
   return cudaGetLastError();
 }
 
@@ -405,7 +405,7 @@ extern "C" cudaError_t CG_CAT(cg_field_lpt_, CG_N)(const cg_field_launch *L)
   k_col_y<TXY, 1><<<g2, TXY * P, sm2, L->stream>>>(L->f[0], L->f[1], L->f[2], L->twN);
   dim3 g3((unsigned)((size_t)N * N / PL::RB), 3);
   k_row_c2r<false><<<g3, PL::RB * PR, sm3, L->stream>>>(L->f[0], L->f[1], L->f[2], 1.0f, nullptr, L->twN,
-                                                         L->twH);
+                                                         L->twH, L->err);
   return cudaGetLastError();
 }
 
@@ -427,7 +427,7 @@ extern "C" cudaError_t CG_CAT(cg_field_lpt2_, CG_N)(const cg_field_launch *L)
   if ((e = prep(k_col_y<TXY, 1>, sm2)) != cudaSuccess) return e;
   if ((e = prep(k_row_c2r<false>, sm3)) != cudaSuccess) return e;
   dim3 gr((unsigned)((size_t)N * N / PL::RB), 1);
-  k_row_r2c<<<gr, PL::RB * PR, smr, L->stream>>>(L->src, L->twN, L->twH);
+  k_row_r2c<<<gr, PL::RB * PR, smr, L->stream>>>(L->src, L->twN, L->twH, L->err);
   dim3 gy1((NH + TXY - 1) / TXY, N, 1);
   k_col_y<TXY, -1><<<gy1, TXY * P, sm2, L->stream>>>(L->src, nullptr, nullptr, L->twN);
   dim3 gz((NH + TX3 - 1) / TX3, N);
@@ -437,7 +437,7 @@ extern "C" cudaError_t CG_CAT(cg_field_lpt2_, CG_N)(const cg_field_launch *L)
   k_col_y<TXY, 1><<<g2, TXY * P, sm2, L->stream>>>(L->f[0], L->f[1], L->f[2], L->twN);
   dim3 g3((unsigned)((size_t)N * N / PL::RB), 3);
   k_row_c2r<false><<<g3, PL::RB * PR, sm3, L->stream>>>(L->f[0], L->f[1], L->f[2], 1.0f, nullptr, L->twN,
-                                                         L->twH);
+                                                         L->twH, L->err);
   return cudaGetLastError();
 }
 
