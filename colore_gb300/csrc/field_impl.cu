@@ -151,7 +151,13 @@ __device__ __forceinline__ void gen_fields(const FillParams &p, int kx, int ky, 
   }
 }
 
-/* Pass 1: fill + z transform of F fields.  grid = (ceil(NH/TX), N). */
+/* Pass 1: fill + z transform of F fields.  grid = (ceil(NH/TX), N).
+ * Each thread first generates, in a rolled loop, the modes its stage-0
+ * loads will read and parks every field in shared memory (one copy of the
+ * generator in the instruction stream: inlined per register element it
+ * overflowed the instruction cache); field 0's slot is also the exchange
+ * buffer of the transforms, safe because a transform reads all its inputs
+ * before its first exchange write. */
 template <int F, int TX>
 __global__ void __launch_bounds__(TX *PF) k_fill_z(float2 *o0, float2 *o1, float2 *o2, FillParams p,
                                                   const float2 *__restrict__ twN)
@@ -160,24 +166,25 @@ __global__ void __launch_bounds__(TX *PF) k_fill_z(float2 *o0, float2 *o1, float
   const int c = threadIdx.x % TX, t = threadIdx.x / TX;
   const int kx = blockIdx.x * TX + c, ky = blockIdx.y;
   const bool ok = kx < NH;
+#pragma unroll 1
+  for (int e = 0; e < PL::FR; e++) {
+    const int i = e / PL::F0, q = e - i * PL::F0;
+    const int pos = t + (N / PL::FR) * i + q * (N / PL::F0); /* cgfft::in_pos of stage 0 */
+    float2 f[F];
+    if (ok) {
+      gen_fields<F>(p, kx, ky, pos, f);
+    } else {
+#pragma unroll
+      for (int jj = 0; jj < F; jj++) f[jj] = make_float2(0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int jj = 0; jj < F; jj++) smem[(size_t)jj * N * TX + pos * TX + c] = f[jj];
+  }
   float2 *outs[3] = {o0, o1, o2};
   auto sm = [&](int pos) -> float2 & { return smem[pos * TX + c]; };
 #pragma unroll
   for (int j = 0; j < F; j++) {
-    auto ld = [&](int pos) -> float2 {
-      if (j == 0) {
-        float2 f[F];
-        if (ok) gen_fields<F>(p, kx, ky, pos, f);
-        else {
-#pragma unroll
-          for (int q = 0; q < F; q++) f[q] = make_float2(0.0f, 0.0f);
-        }
-#pragma unroll
-        for (int q = 1; q < F; q++) smem[(size_t)q * N * TX + pos * TX + c] = f[q];
-        return f[0];
-      }
-      return smem[(size_t)j * N * TX + pos * TX + c];
-    };
+    auto ld = [&](int pos) -> float2 { return smem[(size_t)j * N * TX + pos * TX + c]; };
     float2 *o = outs[j];
     auto st = [&](int pos, float2 v) {
       if (ok) o[((size_t)pos * N + ky) * NH + kx] = v;
