@@ -111,7 +111,7 @@ __device__ __forceinline__ void add_runs(K key, int tag, float temp, int lane, c
 }
 
 template <typename K>
-__global__ void __launch_bounds__(IW * 32, 1) k_imap_cells(const float *__restrict__ dens, const float *__restrict__ phi,
+__global__ void __launch_bounds__(IW * 32, 16) k_imap_cells(const float *__restrict__ dens, const float *__restrict__ phi,
                                                      cg_imap_params p)
 {
   extern __shared__ unsigned char sraw[];
