@@ -163,7 +163,7 @@ __device__ __forceinline__ void grad_phi(const float *__restrict__ phi, int ix, 
   v[2] = CG_SUB(__ldg(&phi[pidx(ix, iy, zh, N)]), __ldg(&phi[pidx(ix, iy, zl, N)]));
 }
 
-__global__ void __launch_bounds__(SB) k_emit(const float *__restrict__ phi, cg_srcs_params p)
+__global__ void __launch_bounds__(SB, 8) k_emit(const float *__restrict__ phi, cg_srcs_params p)
 {
   __shared__ int coff[CPB + 1]; /* exclusive source offset of each cell in the block */
   __shared__ int ws[SB / 32];
