@@ -85,7 +85,7 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v)
  * for the redshift and every tracer. */
 __host__ __device__ inline size_t bins_warp_bytes(int nz, int nt) { return (size_t)nz * (4 + 8 * (1 + nt)); }
 
-__global__ void __launch_bounds__(BINS_WARPS * 32, 6) k_dens_bins(float *grid, cg_bins_params p)
+__global__ void __launch_bounds__(BINS_WARPS * 32, 2) k_dens_bins(float *grid, cg_bins_params p)
 {
   extern __shared__ unsigned char sbins[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwb = blockDim.x >> 5;
