@@ -131,6 +131,10 @@ def lib():
             "cg_write_healpix_map": (C.c_int, [C.c_char_p, vp, C.c_long]),
             "cg_write_catalog": (C.c_int, [C.c_char_p, C.c_int, C.c_int, vp, C.c_longlong, C.c_int, vp]),
             "cg_download_skewers": (C.c_int, [vp, C.c_int, vp, vp]),
+            "cg_write_predictions": (C.c_int, [vp]),
+            "cg_pk_linear0": (C.c_double, [vp, C.c_double]),
+            "cg_pk2xi": (None, [C.c_int, vp, vp, vp, vp]),
+            "cg_xi2pk": (None, [C.c_int, vp, vp, vp, vp]),
             "cg_write_density_grid": (C.c_int, [C.c_char_p, C.c_char_p, vp, C.c_int, C.c_double]),
             "cg_read_run_params": (C.c_int, [C.c_char_p, C.POINTER(vp), C.c_char_p, C.c_size_t]),
             "cg_params_free": (None, [vp]),
@@ -156,7 +160,8 @@ def exported_symbols():
             "cg_params_free", "cg_params_to_config", "cg_write_healpix_map", "cg_write_catalog",
             "cg_write_density_grid", "cg_graph_capture", "cg_graph_launch", "cg_batch_create", "cg_batch_run",
             "cg_batch_streams", "cg_batch_tuning", "cg_batch_context", "cg_batch_last_error", "cg_batch_destroy",
-            "cg_skewer_background", "cg64_create", "cg64_destroy", "cg64_last_error",
+            "cg_skewer_background", "cg_write_predictions", "cg_pk_linear0", "cg_pk2xi", "cg_xi2pk",
+            "cg64_create", "cg64_destroy", "cg64_last_error",
             "cg64_run_mock", "cg64_num_sources", "cg64_download"]
 
 
@@ -174,6 +179,32 @@ def write_healpix_map(fname, m, nside):
         raise ValueError("map has %d pixels, nside %d needs %d" % (m.size, nside, 12 * nside * nside))
     if lib().cg_write_healpix_map(os.fsencode(fname), m.ctypes.data, nside):
         raise CGError("cannot write %s" % fname)
+
+
+def write_predictions(params):
+    """The theory-prediction files of write_predictions for these parameters."""
+    if lib().cg_write_predictions(params._p):
+        raise CGError("write_predictions failed (write_pred and pred_dz set?)")
+
+
+def pk2xi(k, pk):
+    """FFTLog P(k) -> xi(r) on log-spaced k (the reference's pk2xi): (r, xi)."""
+    k = np.ascontiguousarray(k, np.float64)
+    pk = np.ascontiguousarray(pk, np.float64)
+    r = np.empty_like(k)
+    xi = np.empty_like(k)
+    lib().cg_pk2xi(len(k), k.ctypes.data, pk.ctypes.data, r.ctypes.data, xi.ctypes.data)
+    return r, xi
+
+
+def xi2pk(r, xi):
+    """FFTLog xi(r) -> P(k) on log-spaced r (the reference's xi2pk): (k, pk)."""
+    r = np.ascontiguousarray(r, np.float64)
+    xi = np.ascontiguousarray(xi, np.float64)
+    k = np.empty_like(r)
+    pk = np.empty_like(r)
+    lib().cg_xi2pk(len(r), r.ctypes.data, xi.ctypes.data, k.ctypes.data, pk.ctypes.data)
+    return k, pk
 
 
 class SkewerSet(C.Structure):

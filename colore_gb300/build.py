@@ -74,7 +74,7 @@ def _jobs():
         src = os.path.join(CSRC, name + ".cu")
         out = os.path.join(BUILD, name + ".o")
         units.append((out, [nvcc()] + NVFLAGS + ["-c", src, "-o", out], [src] + hdr))
-    for name in ("host_cosmo", "host_params", "host_io"):
+    for name in ("host_cosmo", "host_params", "host_io", "host_pred"):
         src = os.path.join(HOST, name + ".c")
         out = os.path.join(BUILD, name + ".o")
         units.append((out, ["gcc"] + CFLAGS + ["-c", src, "-o", out], [src] + hdr))

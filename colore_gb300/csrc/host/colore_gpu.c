@@ -96,6 +96,14 @@ int main(int argc, char **argv)
     return 0;
   }
   printf("Seed : %llu\n", (unsigned long long)p->seed);
+  if (p->write_pred) { /* main.c:61-63 */
+    printf("*** Writing predictions\n");
+    if ((rc = cg_write_predictions(p))) die(NULL, rc, "write_predictions");
+  }
+  if (p->just_write_pred) {
+    cg_params_free(p);
+    return 0;
+  }
   cg_ctx *c;
   if ((rc = cg_create(&c, &cfg, 0))) die(NULL, rc, "cg_create");
   printf("*** Creating Gaussian density field \n");

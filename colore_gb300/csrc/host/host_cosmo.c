@@ -205,6 +205,8 @@ static double pk_lin0(const cg_params *p, double lgk) /* pk_linear0, cosmo.c:291
   return p->pkarr[p->numk - 1] * pow(10, -3 * (lgk - p->logkmax));
 }
 
+double cg_pk_linear0(const cg_params *p, double lgk) { return pk_lin0(p, lgk); }
+
 static double wind(double x, int setwf) /* cosmo.c:265-289 */
 {
   if (setwf == 1) return exp(-0.5 * x * x);

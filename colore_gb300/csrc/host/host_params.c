@@ -389,6 +389,10 @@ int cg_read_run_params(const char *fname, cg_params **out, char *err, size_t el)
   rd_int(&r, "global", "seed", &seed);
   p->seed = (unsigned int)seed;
   rd_bool(&r, "global", "write_pred", &p->write_pred);
+  if (p->write_pred) { /* io.c:273-276 */
+    rd_bool(&r, "global", "just_write_pred", &p->just_write_pred);
+    rd_double(&r, "global", "pred_dz", &p->pred_dz);
+  }
   rd_double(&r, "field_par", "r_smooth", &p->r_smooth);
   rd_bool(&r, "field_par", "smooth_potential", &p->smooth_potential);
   rd_int(&r, "field_par", "n_grid", &p->n_grid);

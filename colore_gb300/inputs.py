@@ -113,8 +113,11 @@ def write_inputs(dirname, spec, prefix="run"):
     add("global:\n{\n  prefix_out= \"%s\";\n  output_format= \"%s\";\n  output_density= %s;" %
         (os.path.join(dirname, prefix), spec.get("output_format", "ASCII"),
          "true" if spec.get("output_density") else "false"))
-    add("  pk_filename= \"%s\";\n  z_min= %r;\n  z_max= %r;\n  seed= %d;\n  write_pred= false;" %
-        (pkf, float(spec["z_min"]), float(spec["z_max"]), spec["seed"]))
+    pred = spec.get("pred")
+    pred_txt = ("write_pred= true;\n  just_write_pred= %s;\n  pred_dz= %r;" %
+                ("true" if pred.get("just") else "false", float(pred["dz"]))) if pred else "write_pred= false;"
+    add("  pk_filename= \"%s\";\n  z_min= %r;\n  z_max= %r;\n  seed= %d;\n  %s" %
+        (pkf, float(spec["z_min"]), float(spec["z_max"]), spec["seed"], pred_txt))
     add("  bias_model= %d;\n}\n" % spec.get("bias_model", 2))
     add("field_par:\n{\n  r_smooth= %r;\n  smooth_potential= true;\n  n_grid= %d;\n  dens_type= %d;" %
         (float(spec["r_smooth"]), spec["n_grid"], spec.get("dens_type", 0)))

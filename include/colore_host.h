@@ -27,7 +27,8 @@ typedef struct {
   double z_min, z_max;
   int output_density;
   unsigned long long seed;
-  int write_pred;
+  int write_pred, just_write_pred; /* write_pred, just_write_pred (io.c:272-276) */
+  double pred_dz;
   /* field_par */
   double r_smooth;          /* as read; r2_smooth = r_smooth^2 (io.c:453-458) */
   double r2_smooth;
@@ -134,6 +135,18 @@ int cg_skewer_background(const cg_params *p, int nr, float *r, float *z, float *
 /* <prefix>_dens_<tag>_0.dat from a padded [N][N][2(N/2+1)] float grid, the
  * layout of write_density_grid (src/io.c:565-595) on one node. */
 int cg_write_density_grid(const char *prefix, const char *tag, const float *grid, int n_grid, double l_box);
+
+/* Theory predictions (write_predictions, src/predictions.c:26-173): for z =
+ * 0, pred_dz, ... <= z_max, <prefix>_gbias.txt and, per source population,
+ * intensity species and custom map, <prefix>_{pk,xi}_{srcs,imap,custom}_pop<i>_z<z>.txt
+ * with the linear and lognormal spectra and correlation functions. */
+int cg_write_predictions(const cg_params *p);
+/* linear P(k) at log10 k (pk_linear0, src/cosmo.c:291-308) */
+double cg_pk_linear0(const cg_params *p, double lgk);
+/* FFTLog transforms of pk2xi / xi2pk (src/fftlog.c:147-157) on n log-spaced
+ * points: the output grid is written to r (resp. k). */
+void cg_pk2xi(int n, const double *k, const double *pk, double *r, double *xi);
+void cg_xi2pk(int n, const double *r, const double *xi, double *k, double *pk);
 
 #ifdef __cplusplus
 }
