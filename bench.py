@@ -99,12 +99,20 @@ def config_spec(name, n):
 # Algorithmic HBM bytes per cell of each launch group (FP32 grids; per pass
 # and field one read and one write of 4 bytes per cell; the fill+z pass only
 # writes).  fields: fill+z 2x4 W, y 2x(4R+4W), x 2x(4R+4W) = 40 B/cell.
-ALGO_BYTES_PER_CELL = {"field_fft": 40.0, "lpt_fft": 60.0, "dens_bins": 8.0, "srcs_count": 6.0}
+ALGO_BYTES_PER_CELL = {"field_fft": 40.0, "lpt_fft": 60.0, "dens_bins": 8.0, "srcs_count": 6.0,
+                       "field_fill": 8.0, "field_y": 16.0, "field_x": 16.0,
+                       "lpt_fill": 12.0, "lpt_y": 24.0, "lpt_x": 24.0}
+# passes whose bound is HBM traffic: the y and x transform passes.  The
+# fills generate their modes, the density/bins pass evaluates exp/log per
+# cell and tracer, the Poisson count draws per cell: those are issue bound
+# (ncu: 5-18 % of DRAM peak) and are reported under "kernels" only.
+HBM_PASSES = ("lpt_y", "lpt_x", "field_y", "field_x")
 # DRAM bytes (read + write) per cell of the same groups measured by ncu on the
 # 512^3 case of config c4 (grids larger than L2); traffic grows with the cell
 # count, so a launch at N^3 moves N^3 times these (profiles/fft_passes_c4_512.md,
 # profiles/k_dens_bins_c4_512.md).
-MEASURED_DRAM_BYTES_PER_CELL = {"field_fft": 38.5, "lpt_fft": 59.8, "dens_bins": 7.6}
+MEASURED_DRAM_BYTES_PER_CELL = {"field_fft": 38.5, "lpt_fft": 59.8, "dens_bins": 7.6, "field_fill": 7.6,
+                                "field_y": 15.65, "field_x": 15.2, "lpt_fill": 11.8, "lpt_x": 23.7}
 
 
 # ---- replicas: one realisation per rank, no exchange on the data path ----
@@ -252,8 +260,8 @@ def run_ours(args):
     # roofline of the dominant HBM-bound group
     rl = None
     avg = {k: v[0] / max(v[1], 1) for k, v in groups.items()}
-    for name in ("field_fft", "lpt_fft", "dens_bins", "srcs_count"):
-        if name in avg:
+    for name in HBM_PASSES:
+        if avg.get(name, 0) > 0:
             bytes_launch = ALGO_BYTES_PER_CELL[name] * ncell
             a = bytes_launch / (avg[name] / 1e3) / 1e9
             if rl is None or avg[name] > rl["_t"]:
@@ -263,14 +271,18 @@ def run_ours(args):
                       "traffic_source": "ncu DRAM bytes per cell at 512^3 x cells" if tr else None,
                       "peak_kind": peak_kind,
                       "algorithmic_bytes_per_launch": bytes_launch, "avg_launch_ms": round(avg[name], 3),
+                      "note": "the HBM-bound pass with the most time per step (fills, bins, Poisson count, "
+                              "deposit and painting are issue bound: see kernels and roofline_dominant)",
                       "_t": avg[name]}
     if rl:
         rl.pop("_t")
+    # the step's largest launch group and what bounds it
+    dom = max(avg.items(), key=lambda kv: kv[1]) if avg else None
     # per group: GB/s of the HBM-bound passes, samples/s where atomics or
     # gathers bound the kernel (intensity-map sub-samples, kappa ray steps)
     kern = {}
     for name, t in avg.items():
-        if name in ALGO_BYTES_PER_CELL:
+        if name in ALGO_BYTES_PER_CELL and t > 0:
             gbs = ALGO_BYTES_PER_CELL[name] * ncell / (t / 1e3) / 1e9
             kern[name] = {"ms": round(t, 3), "GB/s": round(gbs, 1), "frac_hbm": round(gbs / hbm, 4)}
         else:
@@ -301,6 +313,9 @@ def run_ours(args):
         "sources": nsrc,
         "wall_s_timed": t_wall,
         "roofline": rl,
+        "roofline_dominant": {"kernel": dom[0], "ms": round(dom[1], 3), "share": round(dom[1] / (t_step * 1e3), 3),
+                              "bound": "instruction issue (ncu: 91 % issue-active, 7 % of DRAM peak at 512^3)"
+                              if dom[0] == "imap_paint" else "see kernels"} if dom else None,
         "clocks": clk.summary(),
     }
     if world == 1 and not args.no_fp64:
@@ -316,19 +331,21 @@ def run_ours(args):
                            "path": "plain FP64 kernels + cuFFT, no fusion, same GPU"}
     if world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, quick=True)
+    if world == 1 and not args.no_batched:
+        # the batching pattern on the 48-realisation workload, after this
+        # configuration's context is released
+        m.close()
+        bt = batched_measure(args, rank, world, local, None, baselines=not args.no_fp64)
+        keep = ("metric", "value", "unit", "ms_per_step", "cells_per_s", "e2e", "gpu_launches", "fp64_seq", "clocks")
+        out["batched"] = {k: bt[k] for k in keep if k in bt}
+        out["batched"]["streams"] = bt["config"]["streams"]
+        out["batched"]["workload"] = bt["config"]["workload"]
     print(json.dumps(out))
 
 
 def run_batched(args):
-    """The batched workload (48 independent realisations at 128^3, 256^3 and
-    384^3, one source population each): one captured graph per realisation,
-    dealt over autotuned streams.  value = realisations/s of whole passes,
-    device-timed; e2e adds, every pass, the download of every catalogue
-    into pinned host memory; fp64_seq runs the plain FP64 path over the same
-    48 configurations one after the other."""
+    """The batched workload on its own JSON line (`--config c3`)."""
     import torch
-    import colore_gb300 as cg
-    from colore_gb300 import inputs
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -340,6 +357,22 @@ def run_batched(args):
     else:
         dist = None
     torch.cuda.set_device(local)
+    out = batched_measure(args, rank, world, local, dist, baselines=True)
+    if out is not None:
+        print(json.dumps(out))
+
+
+def batched_measure(args, rank, world, local, dist, baselines):
+    """The batched workload (48 independent realisations at 128^3, 256^3 and
+    384^3, one source population each): one captured graph per realisation,
+    dealt over autotuned streams.  value = realisations/s of whole passes,
+    device-timed; e2e adds, every pass, the download of every catalogue
+    into pinned host memory; fp64_seq runs the plain FP64 path over the same
+    48 configurations one after the other.  Returns the result (rank 0)."""
+    import torch
+    import colore_gb300 as cg
+    from colore_gb300 import inputs
+
     specs = inputs.batch_specs()
     nreal = len(specs)
     for s in specs:
@@ -389,7 +422,7 @@ def run_batched(args):
         t_step, t_e2e = max_over_ranks([t_step, t_e2e], dist, "cuda")
     if rank != 0:
         b.close()
-        return
+        return None
     sizes = sorted({p.config.n_grid for p in prms})
     out = {
         "metric": "realisations/s, batched uneven grids (48 x {128^3, 256^3, 384^3}), FP32 vs sequential FP64",
@@ -411,7 +444,7 @@ def run_batched(args):
         "clocks": clk.summary(),
     }
     b.close()
-    if world == 1 and not args.no_fp64:
+    if world == 1 and not args.no_fp64 and baselines:
         t64 = 0.0
         warm = set()
         for p in prms:
@@ -424,9 +457,9 @@ def run_batched(args):
         out["fp64_seq"] = {"value": nreal / (t64 / 1e3), "unit": "realisations/s", "ms_per_pass": t64,
                            "speedup_of_value": out["value"] / (nreal / (t64 / 1e3)),
                            "path": "plain FP64 kernels + cuFFT, one realisation after another, same GPU"}
-    if world == 1 and not args.no_cpu_baseline:
+    if world == 1 and not args.no_cpu_baseline and baselines:
         out["cpu_baseline"] = cpu_baseline_batched(args)
-    print(json.dumps(out))
+    return out
 
 
 def cpu_baseline_batched(args):
@@ -590,6 +623,7 @@ def main():
     ap.add_argument("--cpu-n", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--streams", type=int, default=0, help="batched workload: streams (0 autotunes)")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-workload measurement")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

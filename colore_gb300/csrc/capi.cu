@@ -141,6 +141,7 @@ struct cg_ctx {
   struct Ev {
     const char *name;
     cudaEvent_t a, b;
+    bool own_a; /* false when a is the previous entry's b */
   };
   std::vector<Ev> evlog;
   /* state */
@@ -221,6 +222,7 @@ struct ProfScope {
     if (!c->profiling) return;
     cg_ctx::Ev e;
     e.name = name;
+    e.own_a = true;
     cudaEventCreate(&e.a);
     cudaEventCreate(&e.b);
     cudaEventRecord(e.a, c->stream);
@@ -230,6 +232,28 @@ struct ProfScope {
   ~ProfScope()
   {
     if (i != (size_t)-1) cudaEventRecord(c->evlog[i].b, c->stream);
+  }
+};
+
+/* When profiling, events around the three passes of a 3-D transform: the
+ * start, then one after each pass (recorded by the launcher), logged as
+ * three entries <base>_fill, <base>_y, <base>_x that share their boundary
+ * events.  base is one of a fixed set of names with static storage. */
+struct PassEvents {
+  cg_ctx *c;
+  const char *names[3];
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  PassEvents(cg_ctx *c_, const char *n_fill, const char *n_y, const char *n_x) : c(c_), names{n_fill, n_y, n_x}
+  {
+    if (!c->profiling) return;
+    for (cudaEvent_t &e : ev) cudaEventCreate(&e);
+    cudaEventRecord(ev[0], c->stream);
+  }
+  cudaEvent_t *after() { return c->profiling ? ev + 1 : nullptr; }
+  ~PassEvents()
+  {
+    if (!c->profiling) return;
+    for (int k = 0; k < 3; k++) c->evlog.push_back(cg_ctx::Ev{names[k], ev[k], ev[k + 1], k == 0});
   }
 };
 
@@ -653,6 +677,8 @@ extern "C" int cg_create_cartesian_fields(cg_ctx *c)
   L.err = c->d_err;
   {
     ProfScope ps(c, "field_fft");
+    PassEvents pe(c, "field_fill", "field_y", "field_x");
+    L.ev = pe.after();
     CUDA_TRY(c, run_gauss(c->N, &L));
     const double ncell = (double)c->N * c->N * c->N;
     CUDA_TRY(c, cg_moments_final(c->stream, c->d_part, c->npart, 1.0 / ncell, c->d_stats, c->d_s2f));
@@ -720,7 +746,10 @@ extern "C" int cg_compute_physical_density_field(cg_ctx *c)
     for (int a = 0; a < 3; a++) L.f[a] = reinterpret_cast<float2 *>(c->d_disp[a]);
     {
       ProfScope ps(c, "lpt_fft");
+      PassEvents pe(c, "lpt_fill", "lpt_y", "lpt_x");
+      L.ev = pe.after();
       CUDA_TRY(c, run_lpt(c->N, &L));
+      L.ev = nullptr;
     }
     ProfScope ps2(c, "lpt_cic");
     CUDA_TRY(c, cudaMemsetAsync(c->d_dens, 0, c->grid_floats * sizeof(float), c->stream));
@@ -1907,7 +1936,10 @@ extern "C" int cg_kernel_times(cg_ctx *c, char *names, size_t names_len, float *
       }
     }
     k++;
-    cudaEventDestroy(e.a);
+  }
+  /* entries may share a boundary event: destroy once every time is read */
+  for (auto &e : c->evlog) {
+    if (e.own_a) cudaEventDestroy(e.a);
     cudaEventDestroy(e.b);
   }
   c->evlog.clear();

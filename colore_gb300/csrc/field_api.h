@@ -20,6 +20,7 @@ struct cg_field_launch {
   const float2 *twH;    /* exp(+2 pi i j/(N/2)), j < N/2             */
   float2 *src;          /* 2LPT: the source grid (padded real in, destroyed) */
   unsigned int *err;    /* device error word (bulk-copy timeouts) */
+  cudaEvent_t *ev;      /* NULL, or events recorded after each pass (fill+z, y, x) */
 };
 
 #define CG_FIELD_SIZES(X) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(1024) X(2048)

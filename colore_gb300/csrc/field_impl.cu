@@ -384,13 +384,16 @@ extern "C" cudaError_t CG_CAT(cg_field_gauss_, CG_N)(const cg_field_launch *L)
   if ((e = prep(k_row_c2r<false>, sm3)) != cudaSuccess) return e;
   dim3 g1((NH + TX2 - 1) / TX2, N);
   k_fill_z<2, TX2><<<g1, TX2 * PF, sm1, L->stream>>>(L->f[0], L->f[1], nullptr, L->fill, L->twN);
+  if (L->ev) cudaEventRecord(L->ev[0], L->stream);
   dim3 g2((NH + TXY - 1) / TXY, N, 2);
   k_col_y<TXY, 1><<<g2, TXY * P, sm2, L->stream>>>(L->f[0], L->f[1], nullptr, L->twN);
+  if (L->ev) cudaEventRecord(L->ev[1], L->stream);
   dim3 g3((unsigned)((size_t)N * N / PL::RB), 1);
   k_row_c2r<true><<<g3, PL::RB * PR, sm3, L->stream>>>(L->f[0], nullptr, nullptr, L->norm, L->partials,
                                                         L->twN, L->twH, L->err);
   k_row_c2r<false><<<g3, PL::RB * PR, sm3, L->stream>>>(L->f[1], nullptr, nullptr, L->norm, nullptr,
                                                          L->twN, L->twH, L->err);
+  if (L->ev) cudaEventRecord(L->ev[2], L->stream);
   return cudaGetLastError();
 }
 
@@ -408,11 +411,14 @@ extern "C" cudaError_t CG_CAT(cg_field_lpt_, CG_N)(const cg_field_launch *L)
   if ((e = prep(k_row_c2r<false>, sm3)) != cudaSuccess) return e;
   dim3 g1((NH + TX3 - 1) / TX3, N);
   k_fill_z<3, TX3><<<g1, TX3 * PF, sm1, L->stream>>>(L->f[0], L->f[1], L->f[2], L->fill, L->twN);
+  if (L->ev) cudaEventRecord(L->ev[0], L->stream);
   dim3 g2((NH + TXY - 1) / TXY, N, 3);
   k_col_y<TXY, 1><<<g2, TXY * P, sm2, L->stream>>>(L->f[0], L->f[1], L->f[2], L->twN);
+  if (L->ev) cudaEventRecord(L->ev[1], L->stream);
   dim3 g3((unsigned)((size_t)N * N / PL::RB), 3);
   k_row_c2r<false><<<g3, PL::RB * PR, sm3, L->stream>>>(L->f[0], L->f[1], L->f[2], 1.0f, nullptr, L->twN,
                                                          L->twH, L->err);
+  if (L->ev) cudaEventRecord(L->ev[2], L->stream);
   return cudaGetLastError();
 }
 
