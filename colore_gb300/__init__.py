@@ -107,6 +107,7 @@ def lib():
             "cg_srcs_set_cartesian": (C.c_int, [vp, C.POINTER(C.c_longlong)]),
             "cg_imap_set_cartesian": (C.c_int, [vp]),
             "cg_imap_samples": (C.c_int, [vp, C.c_int, C.POINTER(C.c_ulonglong)]),
+            "cg_set_imap_list_cap": (C.c_int, [vp, C.c_longlong]),
             "cg_get_beam_properties": (C.c_int, [vp]),
             "cg_run_mock": (C.c_int, [vp]),
             "cg_download_grid": (C.c_int, [vp, C.c_int, vp]),
@@ -154,7 +155,7 @@ def exported_symbols():
             "cg_upload_tables", "cg_create_cartesian_fields", "cg_get_sigma2",
             "cg_compute_physical_density_field", "cg_compute_density_normalization",
             "cg_collect_density_normalization", "cg_collect_density_normalization_static", "cg_set_norm_tables", "cg_srcs_set_cartesian",
-            "cg_imap_set_cartesian", "cg_imap_samples", "cg_get_beam_properties", "cg_run_mock", "cg_download_grid",
+            "cg_imap_set_cartesian", "cg_imap_samples", "cg_set_imap_list_cap", "cg_get_beam_properties", "cg_run_mock", "cg_download_grid",
             "cg_num_sources", "cg_download_catalog", "cg_download_count_map", "cg_download_imap",
             "cg_download_kappa", "cg_download_isw", "cg_download_custom", "cg_download_skewers", "cg_download_norm", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_read_run_params",
             "cg_params_free", "cg_params_to_config", "cg_write_healpix_map", "cg_write_catalog",
@@ -346,6 +347,11 @@ class Mock:
 
     def imap_set_cartesian(self):
         self._chk(lib().cg_imap_set_cartesian(self._c), "imap_set_cartesian")
+
+    def set_imap_list_cap(self, cap):
+        """Bound the intensity-map cell list (0: by free device memory);
+        cells past it are painted by the listing kernel."""
+        self._chk(lib().cg_set_imap_list_cap(self._c, int(cap)), "set_imap_list_cap")
 
     def imap_samples(self, ipop):
         """Sub-samples painted for intensity species ipop by the last run."""

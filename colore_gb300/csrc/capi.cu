@@ -117,6 +117,7 @@ struct cg_ctx {
   long long *d_cell_off = nullptr, *d_scan_tmp = nullptr;
   unsigned long long *d_imap_ctr = nullptr;
   long long list_cap = 0;
+  long long list_cap_max = 0; /* cg_set_imap_list_cap; 0: by free memory */
   /* kappa */
   float *d_kmap = nullptr, *d_kfac = nullptr, *d_kinv = nullptr;
   /* ISW */
@@ -1219,7 +1220,8 @@ extern "C" int cg_imap_set_cartesian(cg_ctx *c)
       size_t fr = 0, tot = 0;
       CUDA_TRY(c, cudaMemGetInfo(&fr, &tot));
       const double budget = (double)(fr + (size_t)c->list_cap * CG_IMAP_CELL_BYTES) * 0.25 / CG_IMAP_CELL_BYTES;
-      const long long want = (long long)fmin(fmin(ball, ncell), budget) + 1;
+      long long want = (long long)fmin(fmin(ball, ncell), budget) + 1;
+      if (c->list_cap_max > 0 && want > c->list_cap_max) want = c->list_cap_max;
       if (want > c->list_cap) {
         if ((rc = dalloc(c, &c->d_cells, (size_t)want)) || (rc = dalloc(c, &c->d_cell_n, (size_t)want)) ||
             (rc = dalloc(c, &c->d_cell_off, (size_t)want)) ||
@@ -1228,7 +1230,7 @@ extern "C" int cg_imap_set_cartesian(cg_ctx *c)
         c->list_cap = want;
       }
       if (!c->d_imap_ctr && (rc = dalloc(c, &c->d_imap_ctr, (size_t)5))) return rc;
-      p.list_cap = c->list_cap;
+      p.list_cap = c->list_cap_max > 0 && c->list_cap > c->list_cap_max ? c->list_cap_max : c->list_cap;
 
       p.ctr = c->d_imap_ctr;
       p.cells = c->d_cells;
@@ -1246,6 +1248,13 @@ extern "C" int cg_imap_set_cartesian(cg_ctx *c)
     M.samples = ctr[3] + ctr[4];
     c->launches += ctr[0] > 0 ? 5 : 1; /* cells, 3 scan passes, paint */
   }
+  return CG_OK;
+}
+
+extern "C" int cg_set_imap_list_cap(cg_ctx *c, long long cap)
+{
+  if (!c || cap < 0) return CG_EINVAL;
+  c->list_cap_max = cap;
   return CG_OK;
 }
 

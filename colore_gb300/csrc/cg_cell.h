@@ -181,12 +181,11 @@ CG_HD int64_t cg_ang2pix_ring(int64_t nside64, float cth, float phi)
     int ir = nside + 1 + jp - jm;
     int kshift = 1 - (ir & 1);
     int ip = (jp + jm - nside + kshift + 1) / 2;
-    int m = 4 * nside;
-    if ((nside & (nside - 1)) == 0) ip &= m - 1; /* same as the modulo below */
-    else {
-      ip = ip % m;
-      if (ip < 0) ip += m;
-    }
+    /* ip mod 4 nside: phi in [0, 2 pi) puts tt in [0, 4] and temp1 in
+     * [nside / 2, 4.5 nside], so jp + jm is in [nside - 1, 9 nside + 1], ip
+     * in [0, 4 nside + 1], and one subtraction gives the modulo */
+    const int m = 4 * nside;
+    if (ip >= m) ip -= m;
     return (int64_t)(nside * (nside - 1) * 2 + (ir - 1) * 4 * nside + ip);
   } else {
     float tp = CG_SUB(tt, (float)(int)tt);
@@ -195,9 +194,10 @@ CG_HD int64_t cg_ang2pix_ring(int64_t nside64, float cth, float phi)
     int jm = (int)CG_MUL(CG_SUB(1.0f, tp), tmp);
     int ir = jp + jm + 1;
     int ip = (int)CG_MUL(tt, (float)ir);
-    int m = 4 * ir;
-    ip = ip % m;
-    if (ip < 0) ip += m;
+    /* ip mod 4 ir: tt in [0, 4] makes ip 4 ir at most (exactly when tt * ir
+     * rounds up to it) */
+    const int m = 4 * ir;
+    if (ip >= m) ip -= m;
     if (cth > 0.0f) return (int64_t)(2 * ir * (ir - 1) + ip);
     return (int64_t)(12 * nside * nside - 2 * ir * (ir + 1) + ip);
   }

@@ -182,6 +182,12 @@ int cg_imap_set_cartesian(cg_ctx *ctx);
 /* Sub-samples (cells x nsub^3, imap.c:158-231) painted for species ipop by
  * the last cg_imap_set_cartesian. */
 int cg_imap_samples(cg_ctx *ctx, int ipop, unsigned long long *n);
+/* Upper bound on the intensity-map cell list (no counterpart in the
+ * reference, whose loop paints each cell as it goes; 0, the default: every
+ * cell inside the shells' outer radius, up to a quarter of the free device
+ * memory).  Cells past the bound are painted by the listing kernel itself;
+ * the maps are the same either way. */
+int cg_set_imap_list_cap(cg_ctx *ctx, long long cap);
 int cg_get_beam_properties(cg_ctx *ctx);
 /* Run the whole driver sequence of src/main.c:66-125 in one call. */
 int cg_run_mock(cg_ctx *ctx);

@@ -421,6 +421,32 @@ def test_imap_vs_dev32(runs, kind):
         assert gn.sum() > 0
 
 
+@pytest.mark.parametrize("cap", [1, 3000])
+def test_imap_list_overflow(runs, cap):
+    """With the cell list bounded, the cells past the bound are painted by the
+    listing kernel itself (the path a run takes when the list would not fit
+    in device memory): the same hit counts as the oracle, the same sample
+    count, brightness within float rounding."""
+    import oracle as orc
+    r = runs("full")
+    want_n = [r.m.imap_samples(ip) for ip in range(r.cfg.n_imap)]
+    r.m.set_imap_list_cap(cap)
+    try:
+        r.m.imap_set_cartesian()
+        got = [r.m.imap(ip, with_nadd=True) for ip in range(r.cfg.n_imap)]
+        got_n = [r.m.imap_samples(ip) for ip in range(r.cfg.n_imap)]
+    finally:
+        r.m.set_imap_list_cap(0)
+    assert got_n == want_n
+    for ip in range(r.cfg.n_imap):
+        tab, e = r.need('norm_i')[ip]
+        data, nadd = orc.imap32(r.cfg, ip, r.need('d'), r.phi, tab, e)
+        gm, gn = got[ip]
+        assert np.array_equal(gn, nadd)
+        ref = np.where(nadd > 0, data / np.maximum(nadd, 1), data)
+        assert np.allclose(gm, ref, rtol=5e-5, atol=1e-12)
+
+
 @pytest.mark.parametrize("kind", ["full", "heavy"])
 def test_imap_sample_count(runs, kind):
     """Sub-samples painted (cells in range x nsub^3) against the FP64 count;
