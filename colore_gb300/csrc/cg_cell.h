@@ -394,6 +394,34 @@ CG_HD int cg_shell_index(const float *r0, const float *rf, int nr, float r, int 
   return -1;
 }
 
+/* cg_shell_index(r0, rf, nr, r, 0) in O(log nr) steps.  The walk from shell
+ * 0 climbs while r >= r0[i] and r >= rf[i] and stops at the first shell j
+ * where r < r0[j] (a gap or below the shells: the walk then oscillates and
+ * gives -1) or r < rf[j] (r0[j] <= r: shell j); past the last shell it gives
+ * nr.  With r0 sorted ascending and rfm the running maximum of rf
+ * (rfm[i] = max(rf[0..i])), j is the first index with r < r0[j] or
+ * r < rfm[j], both found by bisection. */
+CG_HD int cg_shell_index0(const float *r0, const float *rfm, int nr, float r)
+{
+  int lo = 0, hi = nr; /* first i with r < r0[i] (nr if none) */
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (r < r0[mid]) hi = mid;
+    else lo = mid + 1;
+  }
+  const int j0 = lo;
+  lo = 0;
+  hi = nr; /* first i with r < rfm[i] */
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (r < rfm[mid]) hi = mid;
+    else lo = mid + 1;
+  }
+  const int jf = lo;
+  if (jf < j0) return jf;
+  return j0 == nr ? nr : -1;
+}
+
 /* Radial velocity from a centred potential difference (get_rvel,
  * srcs.c:87-118): 0.5*idx*(dphi . u) with u = x * (1/r). */
 CG_HD float cg_rvel(float vx, float vy, float vz, float x0, float y0, float z0, float rr, float idx)

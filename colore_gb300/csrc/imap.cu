@@ -119,6 +119,7 @@ __global__ void __launch_bounds__(IW * 32, 16) k_imap_cells(const float *__restr
   float4 *shp = reinterpret_cast<float4 *>(cells + IW * 32);
   float *r0 = reinterpret_cast<float *>(shp + p.nr + 2);
   float *rf = r0 + p.nr;
+  float *rfm = rf + p.nr; /* running maximum of rf, for cg_shell_index0 */
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   CellPar *wc = cells + wid * 32;
   for (int i = threadIdx.x; i < p.nr; i += blockDim.x) {
@@ -126,6 +127,9 @@ __global__ void __launch_bounds__(IW * 32, 16) k_imap_cells(const float *__restr
     rf[i] = p.rf[i];
   }
   for (int i = threadIdx.x; i < p.nr + 2; i += blockDim.x) shp[i] = p.shp[i];
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int i = 0; i < p.nr; i++) rfm[i] = i == 0 ? rf[0] : (rf[i] > rfm[i - 1] ? rf[i] : rfm[i - 1]);
   __syncthreads();
   const int N = p.box.N;
   const int nch = (N + 31) / 32;
@@ -193,7 +197,7 @@ __global__ void __launch_bounds__(IW * 32, 16) k_imap_cells(const float *__restr
           cp.drr = cg_imap_drsd(rvel, bgv(p.v1, at), bgv(p.ih, at));
           const float d = __ldg(&dens[pidx(ix, iy, iz, N)]);
           cp.temp = cg_imap_temp(tmean, d, bias, dnorm, p.bias_model);
-          cp.irad0 = cg_shell_index(r0, rf, p.nr, rc, 0);
+          cp.irad0 = cg_shell_index0(r0, rfm, p.nr, rc);
           /* nsub of the cell's shell (the first one below the shells, the
            * last one beyond or in a gap), with dx / nsub and 1 / nsub */
           const float4 sp = shp[cp.irad0 + 1];
@@ -415,7 +419,7 @@ __global__ void __launch_bounds__(IW * 32, 1) k_imap_paint(cg_imap_params p)
 template <typename K>
 cudaError_t launch(cudaStream_t s, const float *dens, const float *phi, const cg_imap_params *p, int nsm)
 {
-  size_t smem = IW * 32 * sizeof(CellPar) + (size_t)(p->nr + 2) * sizeof(float4) + (size_t)p->nr * 2 * sizeof(float);
+  size_t smem = IW * 32 * sizeof(CellPar) + (size_t)(p->nr + 2) * sizeof(float4) + (size_t)p->nr * 3 * sizeof(float);
   cudaError_t e = cudaFuncSetAttribute(k_imap_cells<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;

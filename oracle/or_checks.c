@@ -44,3 +44,12 @@ void or_pix2vec_nest(long nside, const long long *in, float *v, long n)
 {
   for (long i = 0; i < n; i++) cg_pix2vec_nest(nside, in[i], v + 3 * i);
 }
+void or_shell_index(const float *r0, const float *rf, int nr, const float *r, int *walk, int *bisect, long n)
+{
+  float rfm[4096];
+  for (int i = 0; i < nr && i < 4096; i++) rfm[i] = i == 0 ? rf[0] : (rf[i] > rfm[i - 1] ? rf[i] : rfm[i - 1]);
+  for (long i = 0; i < n; i++) {
+    walk[i] = cg_shell_index(r0, rf, nr, r[i], 0);
+    bisect[i] = cg_shell_index0(r0, rfm, nr, r[i]);
+  }
+}

@@ -47,8 +47,10 @@ def lib():
             "or_philox": [vp, vp, vp], "or_poisson": [vp, vp, C.c_long, C.c_uint32, C.c_uint32],
             "or_ang2pix": [C.c_long, vp, vp, vp, C.c_long], "or_nest2ring": [C.c_long, vp, vp, C.c_long],
             "or_ring2nest": [C.c_long, vp, vp, C.c_long], "or_pix2vec_nest": [C.c_long, vp, vp, C.c_long],
+            "or_shell_index": [vp, vp, i, vp, vp, vp, C.c_long],
         }
-        void = ("or_philox", "or_poisson", "or_ang2pix", "or_nest2ring", "or_ring2nest", "or_pix2vec_nest")
+        void = ("or_philox", "or_poisson", "or_ang2pix", "or_nest2ring", "or_ring2nest", "or_pix2vec_nest",
+                "or_shell_index")
         for k, a in sig.items():
             fn = getattr(L, k)
             fn.argtypes = a
@@ -339,6 +341,18 @@ def ang2pix(nside, cth, phi):
     p = np.empty(len(cth), np.int64)
     lib().or_ang2pix(nside, P(cth), P(phi), P(p), len(cth))
     return p
+
+
+def shell_index(r0, rf, r):
+    """Shell of each radius r: the walk from shell 0 and its bisection form
+    (both from the shared cell header)."""
+    r0 = np.ascontiguousarray(r0, np.float32)
+    rf = np.ascontiguousarray(rf, np.float32)
+    r = np.ascontiguousarray(r, np.float32)
+    w = np.empty(len(r), np.int32)
+    b = np.empty(len(r), np.int32)
+    lib().or_shell_index(P(r0), P(rf), len(r0), P(r), P(w), P(b), len(r))
+    return w, b
 
 
 def nest2ring(nside, ip):
