@@ -208,7 +208,8 @@ static int check_device_errors(cg_ctx *c)
   if (h) {
     CUDA_TRY(c, cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), c->stream));
     return fail(c, CG_EDEVICE, "device error flags 0x%x (1: source count overflow, 2: catalog overflow, "
-                               "4: shell search, 8: imap sub-sampling, 16: imap cell list, 32: bulk copy timeout)",
+                               "4: shell search, 8: imap sub-sampling, 16: imap cell list, 32: bulk copy timeout, "
+                               "64: particle deposit overflow)",
                 h);
   }
   return CG_OK;
@@ -808,6 +809,7 @@ static int run_bins(cg_ctx *c, int nz, double idz)
   p.zt = c->zt;
   p.d1 = c->d1;
   p.mode = c->pending_mode;
+  p.err = c->d_err;
   p.sigma2f = c->d_s2f;
   p.nz = nz;
   p.idz = (float)idz;
@@ -906,6 +908,7 @@ extern "C" int cg_collect_density_normalization_static(cg_ctx *c, int nz, double
   p.zt = c->zt;
   p.d1 = c->d1;
   p.mode = c->pending_mode;
+  p.err = c->d_err;
   p.sigma2f = c->d_s2f;
   p.nz = nz;
   p.idz = (float)idz;
@@ -1775,6 +1778,7 @@ static int apply_pending(cg_ctx *c)
   p.zt = c->zt;
   p.d1 = c->d1;
   p.mode = c->pending_mode;
+  p.err = c->d_err;
   p.sigma2f = c->d_s2f;
   p.nz = 0;
   p.nt = 0;

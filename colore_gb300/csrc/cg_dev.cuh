@@ -22,7 +22,16 @@ enum : unsigned int {
   ERR_SHELL_WALK = 4u,       /* imap shell search did not terminate    */
   ERR_IMAP_NSUB = 8u,        /* sub-sampling factor out of range       */
   ERR_IMAP_HEAVY = 16u,      /* nsub > 128 in a cell past the list     */
+  ERR_DEPOSIT_OVERFLOW = 64u, /* a cell of the particle deposit holds 2^11 or more */
 };
+
+/* The particle deposit accumulates mass in fixed point, 2^20 units per
+ * particle, with integer atomics: integer addition is associative, so the
+ * density does not depend on the order in which threads add (float atomics
+ * would make every run differ in the last bits).  A cell holds up to
+ * 2^11 - 2^-20 particles. */
+constexpr float DEPOSIT_ONE = 1048576.0f;          /* 2^20 */
+constexpr float DEPOSIT_UNIT = 9.5367431640625e-7f; /* 2^-20 */
 
 /* One background table with the edge values of get_bg (cosmo.c:40-86). */
 struct Tab {

@@ -120,6 +120,13 @@ __global__ void __launch_bounds__(BINS_WARPS * 32, 2) k_dens_bins(float *grid, c
       const float r = cg_norm3(x0, y0, z0);
       const BgAt at = bg_at(p.g, r);
       if (p.mode != CG_DMODE_NONE) {
+        if (p.mode == CG_DMODE_RHO) {
+          /* the particle deposit's fixed-point mass (never negative unless
+           * a cell overflowed) */
+          const int m = __float_as_int(d);
+          if (m < 0 && p.err) atomicOr(p.err, ERR_DEPOSIT_OVERFLOW);
+          d = CG_MUL((float)m, DEPOSIT_UNIT);
+        }
         d = cg_dens_transform(p.mode, d, need_d1 ? bgv(p.d1, at) : 0.0f, s2);
         *ptr = d;
       }
@@ -189,22 +196,25 @@ __global__ void __launch_bounds__(BINS_WARPS * 32, 2) k_dens_bins(float *grid, c
  * shared-memory box that extends the tile by CT_H cells on every side; the
  * box is added to the grid at the end with one atomic per non-zero cell.
  * Deposits that fall outside the box (particles displaced by more than about
- * CT_H - 1 cells) go straight to the grid. */
+ * CT_H - 1 cells) go straight to the grid.  Masses are fixed point
+ * (DEPOSIT_ONE per particle, integer atomics; the grid holds the int32 bits
+ * until the density pass turns them into rho - 1), so the result does not
+ * depend on the order of the atomic additions. */
 constexpr int CT_X = 32, CT_Y = 8, CT_Z = 8, CT_H = 2;
 constexpr int CB_X = CT_X + 2 * CT_H, CB_Y = CT_Y + 2 * CT_H, CB_Z = CT_Z + 2 * CT_H;
 
 template <int S>
-__global__ void __launch_bounds__(256) k_lpt_deposit(float *grid, const float *__restrict__ dx_,
+__global__ void __launch_bounds__(256) k_lpt_deposit(int *grid, const float *__restrict__ dx_,
                                                      const float *__restrict__ dy_, const float *__restrict__ dz_,
                                                      cg_lpt_params p)
 {
   constexpr int K = S + 1; /* cells per axis of the stencil */
-  __shared__ float box[CB_Z][CB_Y][CB_X];
+  __shared__ int box[CB_Z][CB_Y][CB_X];
   const int N = p.box.N;
   const int ntx = (N + CT_X - 1) / CT_X, nty = (N + CT_Y - 1) / CT_Y;
   const int t = blockIdx.x;
   const int tx0 = (t % ntx) * CT_X, ty0 = ((t / ntx) % nty) * CT_Y, tz0 = (t / (ntx * nty)) * CT_Z;
-  for (int i = threadIdx.x; i < CB_X * CB_Y * CB_Z; i += blockDim.x) (&box[0][0][0])[i] = 0.0f;
+  for (int i = threadIdx.x; i < CB_X * CB_Y * CB_Z; i += blockDim.x) (&box[0][0][0])[i] = 0;
   __syncthreads();
   const float iag = CG_DIV((float)N, p.box.L);
   const float po[3] = {p.box.p0, p.box.p1, p.box.p2};
@@ -270,7 +280,9 @@ __global__ void __launch_bounds__(256) k_lpt_deposit(float *grid, const float *_
       for (int cy = 0; cy < K; cy++)
 #pragma unroll
         for (int cx = 0; cx < K; cx++) {
-          const float v = CG_MUL(CG_MUL(w[0][cx], w[1][cy]), w[2][cz]);
+          /* the weight in units of 2^-20, rounded to nearest (the
+           * scaling by a power of two is exact) */
+          const int v = __float2int_rn(CG_MUL(CG_MUL(CG_MUL(w[0][cx], w[1][cy]), w[2][cz]), DEPOSIT_ONE));
           if (inbox) {
             atomicAdd(&box[bb[2] + cz][bb[1] + cy][bb[0] + cx], v);
           } else {
@@ -283,8 +295,8 @@ __global__ void __launch_bounds__(256) k_lpt_deposit(float *grid, const float *_
   }
   __syncthreads();
   for (int i = threadIdx.x; i < CB_X * CB_Y * CB_Z; i += blockDim.x) {
-    const float v = (&box[0][0][0])[i];
-    if (v == 0.0f) continue;
+    const int v = (&box[0][0][0])[i];
+    if (v == 0) continue;
     const int bx = i % CB_X, by = (i / CB_X) % CB_Y, bz = i / (CB_X * CB_Y);
     /* box cells lie within one period of the tile */
     int gx = org[0] + bx, gy = org[1] + by, gz = org[2] + bz;
@@ -453,8 +465,11 @@ cudaError_t cg_lpt_cic(cudaStream_t s, float *grid, const float *dx, const float
   (void)nsm;
   const long long N = p->box.N;
   const long long tiles = ((N + CT_X - 1) / CT_X) * ((N + CT_Y - 1) / CT_Y) * ((N + CT_Z - 1) / CT_Z);
-  if (p->interp == 0) k_lpt_deposit<0><<<(unsigned)tiles, 256, 0, s>>>(grid, dx, dy, dz, *p);
-  else if (p->interp == 2) k_lpt_deposit<2><<<(unsigned)tiles, 256, 0, s>>>(grid, dx, dy, dz, *p);
-  else k_lpt_deposit<1><<<(unsigned)tiles, 256, 0, s>>>(grid, dx, dy, dz, *p);
+  /* the grid (zeroed by the caller) holds int32 fixed-point masses until
+   * the density pass of mode CG_DMODE_RHO */
+  int *mass = reinterpret_cast<int *>(grid);
+  if (p->interp == 0) k_lpt_deposit<0><<<(unsigned)tiles, 256, 0, s>>>(mass, dx, dy, dz, *p);
+  else if (p->interp == 2) k_lpt_deposit<2><<<(unsigned)tiles, 256, 0, s>>>(mass, dx, dy, dz, *p);
+  else k_lpt_deposit<1><<<(unsigned)tiles, 256, 0, s>>>(mass, dx, dy, dz, *p);
   return cudaGetLastError();
 }

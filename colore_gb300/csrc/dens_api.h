@@ -22,6 +22,7 @@ struct cg_bins_params {
   unsigned long long *ncount; /* [nz] */
   double *zsum;               /* [nz] */
   double *bsum;               /* [nt][nz] */
+  unsigned int *err;          /* device error bits (mode CG_DMODE_RHO) */
 };
 
 struct cg_lpt_params {
