@@ -109,6 +109,32 @@ __device__ __forceinline__ void stencil19(const float *__restrict__ phi, int x0,
 {
   const int ngx = 2 * (N / 2 + 1);
   const size_t plane = (size_t)ngx * N;
+  if (x0 > 0 && x0 < N - 1 && y0 > 0 && y0 < N - 1 && z0 > 0 && z0 < N - 1) {
+    /* away from the box faces: nine row pointers, the x neighbours at
+     * constant offsets from them */
+    const float *c = phi + (size_t)z0 * plane + (size_t)y0 * ngx + x0;
+    const float *yp = c + ngx, *ym = c - ngx, *zp = c + plane, *zm = c - plane;
+    f[0] = __ldg(c);
+    f[1] = __ldg(c + 1);
+    f[2] = __ldg(c - 1);
+    f[3] = __ldg(yp);
+    f[4] = __ldg(ym);
+    f[5] = __ldg(zp);
+    f[6] = __ldg(zm);
+    f[7] = __ldg(yp + 1);
+    f[8] = __ldg(ym - 1);
+    f[9] = __ldg(ym + 1);
+    f[10] = __ldg(yp - 1);
+    f[11] = __ldg(zp + 1);
+    f[12] = __ldg(zm - 1);
+    f[13] = __ldg(zm + 1);
+    f[14] = __ldg(zp - 1);
+    f[15] = __ldg(zp + ngx);
+    f[16] = __ldg(zm - ngx);
+    f[17] = __ldg(zm + ngx);
+    f[18] = __ldg(zp - ngx);
+    return;
+  }
   const int xh = wrap(x0 + 1, N), xl = wrap(x0 - 1, N);
   const int yh = wrap(y0 + 1, N), yl = wrap(y0 - 1, N);
   const int zh = wrap(z0 + 1, N), zl = wrap(z0 - 1, N);

@@ -35,8 +35,6 @@ __global__ void __launch_bounds__(256) k_kappa(const float *__restrict__ phi, cg
   const long long ip = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (ip >= p.npix) return;
   const int N = p.box.N;
-  const int ngx = 2 * (N / 2 + 1);
-  const size_t plane = (size_t)ngx * N;
   float u[3], rot[6];
   cg_pix2vec_nest(p.nside, ip, u);
   cg_kappa_rot(u, CG_MUL(p.box.idx, p.box.idx), rot);
@@ -50,18 +48,8 @@ __global__ void __launch_bounds__(256) k_kappa(const float *__restrict__ phi, cg
       const int x0 = cg_ngp_cell(rm, u[0], po[0], p.box.idx, N);
       const int y0 = cg_ngp_cell(rm, u[1], po[1], p.box.idx, N);
       const int z0 = cg_ngp_cell(rm, u[2], po[2], p.box.idx, N);
-      const int xh = wrap(x0 + 1, N), xl = wrap(x0 - 1, N);
-      const int yh = wrap(y0 + 1, N), yl = wrap(y0 - 1, N);
-      const int zh = wrap(z0 + 1, N), zl = wrap(z0 - 1, N);
-      /* plane pointers in 64 bits, offsets within a plane in 32 */
-      const float *P0 = phi + (size_t)z0 * plane, *Ph = phi + (size_t)zh * plane, *Pl = phi + (size_t)zl * plane;
-      const int o0 = y0 * ngx, oh = yh * ngx, ol = yl * ngx;
-#define PHI(X, OY, PZ) __ldg((PZ) + (OY) + (X))
-      const float f[19] = {PHI(x0, o0, P0), PHI(xh, o0, P0), PHI(xl, o0, P0), PHI(x0, oh, P0), PHI(x0, ol, P0),
-                           PHI(x0, o0, Ph), PHI(x0, o0, Pl), PHI(xh, oh, P0), PHI(xl, ol, P0), PHI(xh, ol, P0),
-                           PHI(xl, oh, P0), PHI(xh, o0, Ph), PHI(xl, o0, Pl), PHI(xh, o0, Pl), PHI(xl, o0, Ph),
-                           PHI(x0, oh, Ph), PHI(x0, ol, Pl), PHI(x0, oh, Pl), PHI(x0, ol, Ph)};
-#undef PHI
+      float f[19];
+      stencil19(phi, x0, y0, z0, N, f);
       float t[6];
       cg_tidal(f, t);
       const float dot = cg_dot6(rot, t);
