@@ -112,7 +112,7 @@ HBM_PASSES = ("lpt_y", "lpt_x", "field_y", "field_x")
 # count, so a launch at N^3 moves N^3 times these (profiles/fft_passes_c4_512.md,
 # profiles/misc_kernels_c4_512.md).
 MEASURED_DRAM_BYTES_PER_CELL = {"field_fft": 38.5, "lpt_fft": 59.8, "dens_bins": 7.6, "field_fill": 7.6,
-                                "field_y": 15.65, "field_x": 15.2, "lpt_fill": 11.8, "lpt_x": 23.7}
+                                "field_y": 15.65, "field_x": 15.2, "lpt_fill": 11.8, "lpt_y": 23.68, "lpt_x": 23.7}
 
 
 # ---- replicas: one realisation per rank, no exchange on the data path ----
