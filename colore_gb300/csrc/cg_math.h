@@ -14,9 +14,10 @@
  * The elementary functions (exp, log, log1p, atan2, acos) are written from
  * their textbook definitions: Cody-Waite range reduction plus the Taylor
  * series of e^r for exp; the atanh series log(1+f) = 2 atanh(f/(2+f)) for
- * log; a least-squares polynomial for atan(t)/t on [0, tan(pi/8)] (the
- * coefficients were fitted for this file on Chebyshev nodes).  Accuracy is
- * within 2 ulp of the correctly rounded result over the ranges used.
+ * log; a minimax polynomial for atan(t)/t on [0, 1] (the coefficients were
+ * fitted for this file by Remez exchange) after the octant reduction of
+ * atan2.  Accuracy is within 2 ulp of the correctly rounded result over the
+ * ranges used.
  *
  * The counter-based generator is Philox4x32-10 (Salmon, Moraes, Dror and
  * Shaw, "Parallel random numbers: as easy as 1, 2, 3", SC'11).
