@@ -200,8 +200,6 @@ def run_ours(args):
     outs = {}
     for i in range(cfg.n_srcs):
         k = int(nsrc[i] * 1.25) + 1024
-        outs["pos%d" % i] = torch.empty((k, 4), dtype=torch.float32, pin_memory=True).numpy()
-        outs["ipix%d" % i] = torch.empty(k, dtype=torch.int32, pin_memory=True).numpy()
         outs["src%d" % i] = torch.empty((k, 9), dtype=torch.float32, pin_memory=True).numpy()
         if cfg.nside_count[i]:
             outs["cmap%d" % i] = torch.empty(12 * cfg.nside_count[i] ** 2, dtype=torch.int32,
@@ -228,11 +226,13 @@ def run_ours(args):
         split = {}
         for i in range(cfg.n_srcs):
             ns = m.num_sources(i)
-            c = {"pos": outs["pos%d" % i][:ns], "ipix": outs["ipix%d" % i][:ns], "src": outs["src%d" % i][:ns]}
+            # the catalogue as the reference's writers take it: the Src array
+            # (src/common.h:169-179), 9 floats per source
+            c = {"src": outs["src%d" % i][:ns]}
             ta = time.perf_counter()
-            m.catalog(i, out=c)
+            m.catalog(i, pos=False, ipix=False, out=c)
             split["catalog%d" % i] = time.perf_counter() - ta
-            d2h += ns * (16 + 4 + 36)
+            d2h += ns * 36
             if cfg.nside_count[i]:
                 m.count_map(i, out=outs["cmap%d" % i])
                 d2h += outs["cmap%d" % i].nbytes
@@ -366,7 +366,7 @@ def batched_measure(args, rank, world, local, dist, baselines):
     """The batched workload (48 independent realisations at 128^3, 256^3 and
     384^3, one source population each): one captured graph per realisation,
     dealt over autotuned streams.  value = realisations/s of whole passes,
-    device-timed; e2e adds, every pass, the download of every catalogue
+    device-timed; e2e adds, every pass, the copy of every catalogue's Src array
     into pinned host memory; fp64_seq runs the plain FP64 path over the same
     48 configurations one after the other.  Returns the result (rank 0)."""
     import torch
@@ -402,22 +402,27 @@ def batched_measure(args, rank, world, local, dist, baselines):
     launches = sum(m.launches() for m in b.mocks) - l0
     t_step = sum(ms) / len(ms) / 1e3
     nsrc = [m.num_sources(0) for m in b.mocks]
-    # end to end: a pass plus every catalogue into pinned host memory
-    cap = max(nsrc) + 1024
-    pos = torch.empty((cap, 4), dtype=torch.float32, pin_memory=True).numpy()
-    ipx = torch.empty(cap, dtype=torch.int32, pin_memory=True).numpy()
-    src = torch.empty((cap, 9), dtype=torch.float32, pin_memory=True).numpy()
+    # end to end: every pass also copies each realisation's catalogue (its
+    # Src array, the columns the reference's writers take) into pinned host
+    # memory, behind the realisation's graph on its stream
+    # (cg_batch_set_host_catalog), so the copies overlap the other graphs
+    hosts = []
+    for i, n in enumerate(nsrc):
+        src_i = torch.empty((n + n // 8 + 1024, 9), dtype=torch.float32, pin_memory=True).numpy()
+        cnt_i = torch.empty(1, dtype=torch.int64, pin_memory=True).numpy()
+        b.set_host_catalog(i, 0, src_i, cnt_i)
+        hosts.append((src_i, cnt_i))
+    b.run()  # warm the copies
     e2e_steps = max(1, min(args.steps, 2))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     d2h = 0
     for _ in range(e2e_steps):
         b.run()
-        d2h = 0
-        for m, n in zip(b.mocks, nsrc):
-            m.catalog(0, out={"pos": pos[:n], "ipix": ipx[:n], "src": src[:n]})
-            d2h += n * (16 + 4 + 36)
+        d2h = sum(int(c[0]) * 36 + 8 for _, c in hosts)
     t_e2e = (time.perf_counter() - t0) / e2e_steps
+    if any(int(c[0]) > h.shape[0] for h, c in hosts):
+        raise RuntimeError("a host catalogue buffer was too short")
     if dist:
         t_step, t_e2e = max_over_ranks([t_step, t_e2e], dist, "cuda")
     if rank != 0:

@@ -91,6 +91,7 @@ def lib():
             "cg_batch_streams": (C.c_int, [vp]),
             "cg_batch_tuning": (C.c_int, [vp, C.POINTER(C.c_float), C.c_int]),
             "cg_batch_context": (vp, [vp, C.c_int]),
+            "cg_batch_set_host_catalog": (C.c_int, [vp, C.c_int, C.c_int, vp, C.c_longlong, vp]),
             "cg_batch_last_error": (C.c_char_p, [vp]),
             "cg_batch_destroy": (None, [vp]),
             "cg_memory_estimate": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_ulonglong)]),
@@ -160,7 +161,8 @@ def exported_symbols():
             "cg_download_kappa", "cg_download_isw", "cg_download_custom", "cg_download_skewers", "cg_download_norm", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_read_run_params",
             "cg_params_free", "cg_params_to_config", "cg_write_healpix_map", "cg_write_catalog",
             "cg_write_density_grid", "cg_graph_capture", "cg_graph_launch", "cg_batch_create", "cg_batch_run",
-            "cg_batch_streams", "cg_batch_tuning", "cg_batch_context", "cg_batch_last_error", "cg_batch_destroy",
+            "cg_batch_streams", "cg_batch_tuning", "cg_batch_context", "cg_batch_set_host_catalog",
+            "cg_batch_last_error", "cg_batch_destroy",
             "cg_skewer_background", "cg_write_predictions", "cg_pk_linear0", "cg_pk2xi", "cg_xi2pk",
             "cg64_create", "cg64_destroy", "cg64_last_error",
             "cg64_run_mock", "cg64_num_sources", "cg64_download"]
@@ -471,6 +473,7 @@ class Batch:
             self.close()
             raise CGError("cg_batch_create: %s (%s)" % (ERRORS.get(rc, rc), msg.decode() if msg else ""))
         self.mocks = [Mock(self.params[i], _handle=L.cg_batch_context(self._b, i)) for i in range(n)]
+        self._hold = {}  # host catalogue buffers the runs write to
 
     def run(self):
         """Every realisation once; returns the device time of the pass in ms."""
@@ -479,6 +482,26 @@ class Batch:
         if rc:
             raise CGError("cg_batch_run: %s (%s)" % (ERRORS.get(rc, rc), lib().cg_batch_last_error(self._b).decode()))
         return ms.value
+
+    def set_host_catalog(self, i, ipop, src, n_out):
+        """Copy realisation i's Src array of population ipop into src (a
+        page-locked float32 array of shape (cap, 9)) and its source count
+        into n_out[0] (a page-locked int64 array) during every run(); None
+        stops the copies."""
+        if src is None:
+            rc = lib().cg_batch_set_host_catalog(self._b, i, ipop, None, 0, None)
+            self._hold.pop(i, None)
+        else:
+            if src.dtype != np.float32 or src.ndim != 2 or src.shape[1] != 9 or not src.flags.c_contiguous:
+                raise ValueError("src must be a C-contiguous float32 array of shape (cap, 9)")
+            if n_out.dtype != np.int64 or n_out.size < 1:
+                raise ValueError("n_out must be an int64 array")
+            rc = lib().cg_batch_set_host_catalog(self._b, i, ipop, src.ctypes.data, src.shape[0], n_out.ctypes.data)
+            if not rc:
+                self._hold[i] = (src, n_out)
+        if rc:
+            raise CGError("cg_batch_set_host_catalog: %s (%s)" % (ERRORS.get(rc, rc),
+                                                                  lib().cg_batch_last_error(self._b).decode()))
 
     @property
     def streams(self):

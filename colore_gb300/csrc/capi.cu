@@ -1637,6 +1637,13 @@ struct cg_batch {
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   std::vector<cudaEvent_t> joins;
   std::vector<float> tune_ms; /* autotuner: time per stream count tried */
+  /* cg_batch_set_host_catalog: per realisation, the population whose Src
+   * array each pass copies to pinned host memory (-1: none), the device views
+   * of the destination and of the count slot, and the destination's size */
+  std::vector<int> out_pop;
+  std::vector<float *> out_src;
+  std::vector<long long *> out_n;
+  std::vector<long long> out_cap;
   char err[1024] = {0};
 };
 
@@ -1672,9 +1679,19 @@ static int batch_pass(cg_batch *b, float *ms)
   if (cudaEventRecord(b->t0, s0) != cudaSuccess) return batch_fail(b, CG_ECUDA, "event record");
   for (int k = 1; k < b->nstreams; k++) cudaStreamWaitEvent(b->streams[k], b->t0, 0);
   for (size_t j = 0; j < b->order.size(); j++) {
-    cg_ctx *c = b->ctx[b->order[j]];
-    if (int rc = cg_graph_launch(c, b->streams[j % b->nstreams]))
-      return batch_fail(b, rc, "realisation %d: %s", b->order[j], c->err);
+    const int i = b->order[j];
+    cg_ctx *c = b->ctx[i];
+    cudaStream_t st = b->streams[j % b->nstreams];
+    if (int rc = cg_graph_launch(c, st)) return batch_fail(b, rc, "realisation %d: %s", i, c->err);
+    /* the catalogue goes to the host behind the graph on its stream, while
+     * the other streams compute */
+    const int ip = b->out_pop.empty() ? -1 : b->out_pop[i];
+    if (ip >= 0) {
+      const Cat &K = c->cat[ip];
+      if (cg_srcs_copy_out(st, K.src, c->d_total + ip, K.cap, b->out_src[i], b->out_cap[i], b->out_n[i]) !=
+          cudaSuccess)
+        return batch_fail(b, CG_ECUDA, "realisation %d: catalogue copy", i);
+    }
   }
   for (int k = 1; k < b->nstreams; k++) {
     cudaEventRecord(b->joins[k], b->streams[k]);
@@ -1733,6 +1750,42 @@ extern "C" int cg_batch_run(cg_batch *b, float *ms)
   if (!b || b->nstreams < 1) return CG_EINVAL;
   cudaSetDevice(b->device);
   return batch_pass(b, ms);
+}
+
+extern "C" int cg_batch_set_host_catalog(cg_batch *b, int i, int ipop, float *src9, long long cap, long long *n_out)
+{
+  if (!b || i < 0 || i >= b->n) return CG_EINVAL;
+  if (b->out_pop.empty()) {
+    b->out_pop.assign(b->n, -1);
+    b->out_src.assign(b->n, nullptr);
+    b->out_n.assign(b->n, nullptr);
+    b->out_cap.assign(b->n, 0);
+  }
+  if (!src9) { /* unregister */
+    b->out_pop[i] = -1;
+    return CG_OK;
+  }
+  cg_ctx *c = b->ctx[i];
+  if (ipop < 0 || ipop >= c->cfg.n_srcs || cap < 0 || !n_out) return CG_EINVAL;
+  if (!c->d_total || !c->gexec)
+    return batch_fail(b, CG_ESTATE, "realisation %d: no captured source stage", i);
+  cudaSetDevice(b->device);
+  /* both ends must be page-locked host memory that the device can address */
+  void *dv[2] = {nullptr, nullptr};
+  const void *hp[2] = {src9, n_out};
+  for (int k = 0; k < 2; k++) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, hp[k]) != cudaSuccess || a.type != cudaMemoryTypeHost || !a.devicePointer) {
+      cudaGetLastError();
+      return batch_fail(b, CG_EINVAL, "realisation %d: host catalogue buffers must be pinned (cudaHostAlloc)", i);
+    }
+    dv[k] = a.devicePointer;
+  }
+  b->out_pop[i] = ipop;
+  b->out_src[i] = static_cast<float *>(dv[0]);
+  b->out_n[i] = static_cast<long long *>(dv[1]);
+  b->out_cap[i] = cap;
+  return CG_OK;
 }
 
 extern "C" int cg_batch_streams(const cg_batch *b) { return b ? b->nstreams : -1; }

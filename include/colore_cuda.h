@@ -220,6 +220,14 @@ int cg_batch_streams(const cg_batch *b);
 /* stream-count autotuning: the pass time of each candidate, in order */
 int cg_batch_tuning(const cg_batch *b, float *ms, int cap);
 cg_ctx *cg_batch_context(cg_batch *b, int i);
+/* Have every cg_batch_run copy realisation i's catalogue of population ipop
+ * (its Src array, 9 floats per source) into src9 and its source count into
+ * *n_out, behind the realisation's graph on the same stream, so the copies
+ * overlap the other realisations' work and need no host synchronisation.
+ * src9 (cap sources) and n_out must be page-locked host memory the device
+ * can address (cudaHostAlloc); when *n_out > cap only cap sources were
+ * copied.  src9 = NULL stops the copies for realisation i. */
+int cg_batch_set_host_catalog(cg_batch *b, int i, int ipop, float *src9, long long cap, long long *n_out);
 const char *cg_batch_last_error(const cg_batch *b);
 void cg_batch_destroy(cg_batch *b);
 

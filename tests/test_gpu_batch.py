@@ -91,3 +91,46 @@ def test_batch_fixed_streams(built, tmp_path):
     b.run()
     assert all(m.num_sources(0) > 0 for m in b.mocks)
     b.close()
+
+
+def _pinned(shape, dtype):
+    torch = pytest.importorskip("torch")
+    t = torch.empty(shape, dtype={np.float32: torch.float32, np.int64: torch.int64}[dtype], pin_memory=True)
+    return t, t.numpy()
+
+
+def test_batch_host_catalogs(built, tmp_path):
+    """cg_batch_set_host_catalog: each pass copies every realisation's Src
+    array into page-locked host memory behind its graph; the copies equal
+    the catalogues downloaded afterwards, a short buffer receives its first
+    cap sources and the full count, and pageable memory is refused."""
+    import colore_gb300 as cg
+    prms = [_params(tmp_path, _spec(n, 110 + i), "h%d" % i) for i, n in enumerate([64, 96, 128, 64])]
+    b = cg.Batch(prms, nstreams=2)
+    b.run()
+    ns = [m.num_sources(0) for m in b.mocks]
+    keep = []
+    outs = []
+    for i, n in enumerate(ns):
+        cap = n + 64 if i != 3 else n // 2  # the last one too short
+        ts, src = _pinned((cap, 9), np.float32)
+        tn, cnt = _pinned((1,), np.int64)
+        src[:] = -7.0
+        cnt[0] = -1
+        keep += [ts, tn]
+        b.set_host_catalog(i, 0, src, cnt)
+        outs.append((src, cnt, cap))
+    for _ in range(2):
+        b.run()
+        for i, (src, cnt, cap) in enumerate(outs):
+            n = b.mocks[i].num_sources(0)
+            assert cnt[0] == n == ns[i]
+            ref = b.mocks[i].catalog(0, pos=False, ipix=False)["src"]
+            k = min(n, cap)
+            assert np.array_equal(src[:k], ref[:k]), i
+            if cap > n:
+                assert np.all(src[n:] == -7.0)
+    with pytest.raises(cg.CGError, match="pinned"):
+        b.set_host_catalog(0, 0, np.zeros((10, 9), np.float32), np.zeros(1, np.int64))
+    b.set_host_catalog(1, 0, None, None)
+    b.close()
