@@ -109,6 +109,9 @@ def lib():
             "cg_imap_set_cartesian": (C.c_int, [vp]),
             "cg_imap_samples": (C.c_int, [vp, C.c_int, C.POINTER(C.c_ulonglong)]),
             "cg_set_imap_list_cap": (C.c_int, [vp, C.c_longlong]),
+            "cg_set_host_catalog": (C.c_int, [vp, C.c_int, vp, C.c_longlong, vp]),
+            "cg_set_host_imap": (C.c_int, [vp, C.c_int, vp]),
+            "cg_set_host_kappa": (C.c_int, [vp, vp]),
             "cg_get_beam_properties": (C.c_int, [vp]),
             "cg_run_mock": (C.c_int, [vp]),
             "cg_download_grid": (C.c_int, [vp, C.c_int, vp]),
@@ -156,7 +159,8 @@ def exported_symbols():
             "cg_upload_tables", "cg_create_cartesian_fields", "cg_get_sigma2",
             "cg_compute_physical_density_field", "cg_compute_density_normalization",
             "cg_collect_density_normalization", "cg_collect_density_normalization_static", "cg_set_norm_tables", "cg_srcs_set_cartesian",
-            "cg_imap_set_cartesian", "cg_imap_samples", "cg_set_imap_list_cap", "cg_get_beam_properties", "cg_run_mock", "cg_download_grid",
+            "cg_imap_set_cartesian", "cg_imap_samples", "cg_set_imap_list_cap", "cg_set_host_catalog",
+            "cg_set_host_imap", "cg_set_host_kappa", "cg_get_beam_properties", "cg_run_mock", "cg_download_grid",
             "cg_num_sources", "cg_download_catalog", "cg_download_count_map", "cg_download_imap",
             "cg_download_kappa", "cg_download_isw", "cg_download_custom", "cg_download_skewers", "cg_download_norm", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_read_run_params",
             "cg_params_free", "cg_params_to_config", "cg_write_healpix_map", "cg_write_catalog",
@@ -354,6 +358,42 @@ class Mock:
         """Bound the intensity-map cell list (0: by free device memory);
         cells past it are painted by the listing kernel."""
         self._chk(lib().cg_set_imap_list_cap(self._c, int(cap)), "set_imap_list_cap")
+
+    def set_host_outputs(self, catalogs=None, imaps=None, kappa=None):
+        """Register page-locked host arrays that run() fills as each output
+        is final, overlapping the later stages (valid after sync()):
+        catalogs {ipop: (src float32 (cap, 9), n int64 (1,))}, imaps
+        {ipop: float32 (nr, npix)}, kappa float32 (n_kappa, npix).  Passing
+        None for a group leaves it as it is; an entry of None stops it."""
+        L = lib()
+        hold = self.__dict__.setdefault("_host_out", {})
+        for ip, v in (catalogs or {}).items():
+            if v is None:
+                self._chk(L.cg_set_host_catalog(self._c, ip, None, 0, None), "set_host_catalog")
+                hold.pop(("cat", ip), None)
+                continue
+            src, n = v
+            if src.dtype != np.float32 or src.ndim != 2 or src.shape[1] != 9 or not src.flags.c_contiguous:
+                raise ValueError("catalogue buffers are C-contiguous float32 arrays of shape (cap, 9)")
+            if n.dtype != np.int64 or n.size < 1:
+                raise ValueError("the count slot is an int64 array")
+            self._chk(L.cg_set_host_catalog(self._c, ip, src.ctypes.data, src.shape[0], n.ctypes.data),
+                      "set_host_catalog")
+            hold[("cat", ip)] = v
+        for ip, a in (imaps or {}).items():
+            if a is not None:
+                ns, nr = self.cfg.nside_imap[ip], self.cfg.imap_nr[ip]
+                if a.dtype != np.float32 or a.size != nr * 12 * ns * ns or not a.flags.c_contiguous:
+                    raise ValueError("map buffers are C-contiguous float32 arrays of nr x 12 nside^2")
+            self._chk(L.cg_set_host_imap(self._c, ip, a.ctypes.data if a is not None else None), "set_host_imap")
+            hold[("imap", ip)] = a
+        if kappa is not None:
+            ns = self.cfg.nside_kappa
+            if kappa.dtype != np.float32 or kappa.size != self.cfg.n_kappa * 12 * ns * ns or \
+                    not kappa.flags.c_contiguous:
+                raise ValueError("the kappa buffer is a C-contiguous float32 array of n_kappa x 12 nside^2")
+            self._chk(L.cg_set_host_kappa(self._c, kappa.ctypes.data), "set_host_kappa")
+            hold["kappa"] = kappa
 
     def imap_samples(self, ipop):
         """Sub-samples painted for intensity species ipop by the last run."""

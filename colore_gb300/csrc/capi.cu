@@ -153,6 +153,18 @@ struct cg_ctx {
   cudaGraphExec_t gexec = nullptr;
   cudaEvent_t graph_done = nullptr;
   long long graph_launches = 0; /* kernels per replay */
+  /* cg_set_host_*: page-locked host destinations (device views) that the
+   * stages fill as each output becomes final, on a copy stream that overlaps
+   * the stages still to run; one event per output kind orders the next
+   * writer of its source after the copy (0 catalogues, 1 maps, 2 kappa) */
+  float *h_src[CG_NPOP_MAX] = {};
+  long long *h_n[CG_NPOP_MAX] = {};
+  long long h_cap[CG_NPOP_MAX] = {};
+  float *h_imap[CG_NPOP_MAX] = {};
+  float *h_kappa = nullptr;
+  cudaStream_t ostream = nullptr;
+  cudaEvent_t oev[4] = {};
+  bool opend[3] = {false, false, false};
   char err[1024];
 };
 
@@ -178,6 +190,7 @@ static int fail(cg_ctx *c, int code, const char *fmt, ...)
   } while (0)
 
 static void graph_free(cg_ctx *c);
+static void out_wait_all(cg_ctx *c);
 
 /* (Re)allocate a device buffer.  A captured graph holds the old addresses,
  * so any reallocation drops the graph: replaying it would touch freed
@@ -186,6 +199,7 @@ template <class T>
 static int dalloc(cg_ctx *c, T **p, size_t n)
 {
   graph_free(c);
+  out_wait_all(c); /* a host copy may still read the old buffer */
   if (*p) {
     cudaFree(*p);
     *p = nullptr;
@@ -555,6 +569,63 @@ extern "C" int cg_memory_estimate(const cg_config *cfg, unsigned long long *byte
   return CG_OK;
 }
 
+/* write_imap's normalisation (io.c:738-741): data/nadd where nadd > 0. */
+__global__ void k_div_nadd(const float *__restrict__ d, const int *__restrict__ n, float *out, long long m)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x) {
+    int k = n[i];
+    out[i] = k > 0 ? d[i] / (float)k : d[i];
+  }
+}
+
+/* ---- host outputs (cg_set_host_*) ---- */
+static void out_wait_all(cg_ctx *c)
+{
+  if (c->ostream && (c->opend[0] || c->opend[1] || c->opend[2])) cudaStreamSynchronize(c->ostream);
+  c->opend[0] = c->opend[1] = c->opend[2] = false;
+}
+
+/* The next writer of output kind k waits (on the device) for its copy. */
+static void out_join(cg_ctx *c, int k)
+{
+  if (c->opend[k]) {
+    cudaStreamWaitEvent(c->stream, c->oev[k], 0);
+    c->opend[k] = false;
+  }
+}
+
+/* Start copies of output kind k: the copy stream waits for the work queued
+ * so far on the context's stream. */
+static int out_begin(cg_ctx *c)
+{
+  if (!c->ostream) {
+    CUDA_TRY(c, cudaStreamCreateWithFlags(&c->ostream, cudaStreamNonBlocking));
+    for (cudaEvent_t &e : c->oev) CUDA_TRY(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  CUDA_TRY(c, cudaEventRecord(c->oev[3], c->stream));
+  CUDA_TRY(c, cudaStreamWaitEvent(c->ostream, c->oev[3], 0));
+  return CG_OK;
+}
+
+static int out_end(cg_ctx *c, int k)
+{
+  CUDA_TRY(c, cudaEventRecord(c->oev[k], c->ostream));
+  c->opend[k] = true;
+  return CG_OK;
+}
+
+/* Device view of page-locked host memory, or an error. */
+static int host_view(cg_ctx *c, const void *p, void **dv)
+{
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess || a.type != cudaMemoryTypeHost || !a.devicePointer) {
+    cudaGetLastError();
+    return fail(c, CG_EINVAL, "host output buffers must be page-locked (cudaHostAlloc)");
+  }
+  *dv = a.devicePointer;
+  return CG_OK;
+}
+
 static void graph_free(cg_ctx *c)
 {
   if (!c->gexec && !c->graph) return;
@@ -570,6 +641,14 @@ extern "C" void cg_destroy(cg_ctx *c)
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->ostream) {
+    cudaStreamSynchronize(c->ostream);
+    cudaStreamDestroy(c->ostream);
+    c->ostream = nullptr;
+    for (cudaEvent_t &e : c->oev)
+      if (e) cudaEventDestroy(e);
+  }
+  c->opend[0] = c->opend[1] = c->opend[2] = false;
   graph_free(c); /* waits for a replay still running */
   if (c->graph_done) {
     cudaEventDestroy(c->graph_done);
@@ -652,6 +731,8 @@ extern "C" int cg_set_stream(cg_ctx *c, void *s)
 extern "C" int cg_sync(cg_ctx *c)
 {
   if (!c) return CG_EINVAL;
+  if (c->ostream) CUDA_TRY(c, cudaStreamSynchronize(c->ostream));
+  c->opend[0] = c->opend[1] = c->opend[2] = false;
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return check_device_errors(c);
 }
@@ -1098,6 +1179,7 @@ static int srcs_run(cg_ctx *c, long long *nsrc, bool readback)
 extern "C" int cg_srcs_set_cartesian(cg_ctx *c, long long *nsrc)
 {
   if (!c) return CG_EINVAL;
+  out_join(c, 0); /* the catalogues are rewritten */
   return srcs_run(c, nsrc, true);
 }
 
@@ -1134,6 +1216,7 @@ extern "C" int cg_imap_set_cartesian(cg_ctx *c)
   if (c->cfg.n_imap == 0) return CG_OK;
   if (!c->have_norm) return fail(c, CG_ESTATE, "compute_density_normalization first");
   cudaSetDevice(c->device);
+  out_join(c, 1); /* the maps are rewritten */
   int rc;
   for (int ip = 0; ip < c->cfg.n_imap; ip++) {
     Imap &M = c->im[ip];
@@ -1250,6 +1333,19 @@ extern "C" int cg_imap_set_cartesian(cg_ctx *c)
     CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host vectors above go out of scope */
     M.samples = ctr[3] + ctr[4];
     c->launches += ctr[0] > 0 ? 5 : 1; /* cells, 3 scan passes, paint */
+  }
+  /* final maps to registered host buffers (write_imap, io.c:738-741:
+   * data/nadd where nadd > 0), overlapping the stages still to run */
+  for (int ip = 0; ip < c->cfg.n_imap; ip++) {
+    if (!c->h_imap[ip]) continue;
+    const Imap &M = c->im[ip];
+    const long long m = (long long)M.nr * M.npix;
+    if (int rc = out_begin(c)) return rc;
+    k_div_nadd<<<(unsigned)std::min<long long>((m + 255) / 256, (long long)c->nsm * 16), 256, 0, c->ostream>>>(
+        M.data, M.nadd, c->h_imap[ip], m);
+    CUDA_TRY(c, cudaGetLastError());
+    c->launches++;
+    if (int rc = out_end(c, 1)) return rc;
   }
   return CG_OK;
 }
@@ -1527,19 +1623,32 @@ static int srcs_los_run(cg_ctx *c, int ip)
   return CG_OK;
 }
 
+/* Final catalogues to registered host buffers. */
+static int out_catalogs(cg_ctx *c)
+{
+  for (int ip = 0; ip < c->cfg.n_srcs; ip++) {
+    if (!c->h_src[ip] || !c->d_total) continue;
+    const Cat &K = c->cat[ip];
+    if (int rc = out_begin(c)) return rc;
+    CUDA_TRY(c, cg_srcs_copy_out(c->ostream, K.src, c->d_total + ip, K.cap, c->h_src[ip], c->h_cap[ip], c->h_n[ip]));
+    c->launches++;
+    if (int rc = out_end(c, 0)) return rc;
+  }
+  return CG_OK;
+}
+
 extern "C" int cg_get_beam_properties(cg_ctx *c)
 {
   if (!c) return CG_EINVAL;
   if (int rc = refresh_counts(c)) return rc;
-  if (!c->cfg.need_beaming) return CG_OK; /* beaming.c:296-299 */
+  if (!c->cfg.need_beaming) return out_catalogs(c); /* beaming.c:296-299 */
   if (!c->have_fields) return fail(c, CG_ESTATE, "fields not created");
   cudaSetDevice(c->device);
-  if (c->cfg.do_kappa)
-    if (int rc = kappa_run(c)) return rc;
-  if (c->cfg.do_isw)
-    if (int rc = isw_run(c)) return rc;
-  if (c->cfg.n_cstm > 0)
-    if (int rc = cstm_run(c)) return rc;
+  out_join(c, 0); /* RSD and lensing columns are rewritten */
+  out_join(c, 2);
+  /* The source quantities first (the reference computes them last,
+   * beaming.c:293-374; the passes are independent): the catalogues can then
+   * go to the host while the maps are computed. */
   if (c->cfg.n_srcs > 0) {
     if (!c->have_srcs) return fail(c, CG_ESTATE, "srcs_set_cartesian first");
     for (int ip = 0; ip < c->cfg.n_srcs; ip++) {
@@ -1550,7 +1659,64 @@ extern "C" int cg_get_beam_properties(cg_ctx *c)
       if (c->cat[ip].n > 0) c->launches++;
       if (int rc = srcs_los_run(c, ip)) return rc;
     }
+    if (int rc = out_catalogs(c)) return rc;
   }
+  if (c->cfg.do_kappa) {
+    if (int rc = kappa_run(c)) return rc;
+    if (c->h_kappa) {
+      if (int rc = out_begin(c)) return rc;
+      CUDA_TRY(c, cudaMemcpyAsync(c->h_kappa, c->d_kmap, (size_t)c->kpl * c->knpix * sizeof(float),
+                                  cudaMemcpyDeviceToHost, c->ostream));
+      if (int rc = out_end(c, 2)) return rc;
+    }
+  }
+  if (c->cfg.do_isw)
+    if (int rc = isw_run(c)) return rc;
+  if (c->cfg.n_cstm > 0)
+    if (int rc = cstm_run(c)) return rc;
+  return CG_OK;
+}
+
+extern "C" int cg_set_host_catalog(cg_ctx *c, int ipop, float *src9, long long cap, long long *n_out)
+{
+  if (!c || ipop < 0 || ipop >= c->cfg.n_srcs) return CG_EINVAL;
+  cudaSetDevice(c->device);
+  out_wait_all(c);
+  if (!src9) {
+    c->h_src[ipop] = nullptr;
+    return CG_OK;
+  }
+  if (cap < 0 || !n_out) return CG_EINVAL;
+  void *a = nullptr, *b = nullptr;
+  if (int rc = host_view(c, src9, &a)) return rc;
+  if (int rc = host_view(c, n_out, &b)) return rc;
+  c->h_src[ipop] = static_cast<float *>(a);
+  c->h_n[ipop] = static_cast<long long *>(b);
+  c->h_cap[ipop] = cap;
+  return CG_OK;
+}
+
+extern "C" int cg_set_host_imap(cg_ctx *c, int ipop, float *map)
+{
+  if (!c || ipop < 0 || ipop >= c->cfg.n_imap) return CG_EINVAL;
+  cudaSetDevice(c->device);
+  out_wait_all(c);
+  void *a = nullptr;
+  if (map)
+    if (int rc = host_view(c, map, &a)) return rc;
+  c->h_imap[ipop] = static_cast<float *>(a);
+  return CG_OK;
+}
+
+extern "C" int cg_set_host_kappa(cg_ctx *c, float *map)
+{
+  if (!c || (map && !c->cfg.do_kappa)) return CG_EINVAL;
+  cudaSetDevice(c->device);
+  out_wait_all(c);
+  void *a = nullptr;
+  if (map)
+    if (int rc = host_view(c, map, &a)) return rc;
+  c->h_kappa = map;
   return CG_OK;
 }
 
@@ -1899,13 +2065,6 @@ extern "C" int cg_download_count_map(cg_ctx *c, int ipop, int *counts)
   return check_device_errors(c);
 }
 
-__global__ void k_div_nadd(const float *__restrict__ d, const int *__restrict__ n, float *out, long long m)
-{
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x) {
-    int k = n[i];
-    out[i] = k > 0 ? d[i] / (float)k : d[i];
-  }
-}
 
 extern "C" int cg_download_imap(cg_ctx *c, int ipop, float *map, int *nadd)
 {

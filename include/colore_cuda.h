@@ -189,6 +189,20 @@ int cg_imap_samples(cg_ctx *ctx, int ipop, unsigned long long *n);
  * the maps are the same either way. */
 int cg_set_imap_list_cap(cg_ctx *ctx, long long cap);
 int cg_get_beam_properties(cg_ctx *ctx);
+
+/* Host outputs (no counterpart in the reference, whose writers read host
+ * arrays the run filled).  Each call registers page-locked host memory
+ * (cudaHostAlloc) that the stages fill as the output becomes final, on a
+ * copy stream that overlaps the stages still to run: the maps of species
+ * ipop (nr x 12 nside^2 floats, RING, data/nadd as cg_download_imap gives)
+ * after cg_imap_set_cartesian; the Src array of population ipop (cap
+ * sources, 9 floats each; *n_out receives the source count, more than cap
+ * when the buffer was short) and the convergence maps (as cg_download_kappa
+ * gives) during cg_get_beam_properties.  The data are valid after cg_sync.
+ * NULL stops the copies. */
+int cg_set_host_catalog(cg_ctx *ctx, int ipop, float *src9, long long cap, long long *n_out);
+int cg_set_host_imap(cg_ctx *ctx, int ipop, float *map);
+int cg_set_host_kappa(cg_ctx *ctx, float *map);
 /* Run the whole driver sequence of src/main.c:66-125 in one call. */
 int cg_run_mock(cg_ctx *ctx);
 
