@@ -409,7 +409,9 @@ def batched_measure(args, rank, world, local, dist, baselines):
     # (cg_batch_set_host_catalog), so the copies overlap the other graphs
     hosts = []
     for i, n in enumerate(nsrc):
-        src_i = torch.empty((n + n // 8 + 1024, 9), dtype=torch.float32, pin_memory=True).numpy()
+        # replays of a realisation repeat its catalogue, so the count of the
+        # first pass sizes the buffer (the copy moves up to its size)
+        src_i = torch.empty((n + 1024, 9), dtype=torch.float32, pin_memory=True).numpy()
         cnt_i = torch.empty(1, dtype=torch.int64, pin_memory=True).numpy()
         b.set_host_catalog(i, 0, src_i, cnt_i)
         hosts.append((src_i, cnt_i))

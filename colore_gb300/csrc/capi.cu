@@ -153,14 +153,17 @@ struct cg_ctx {
   cudaGraphExec_t gexec = nullptr;
   cudaEvent_t graph_done = nullptr;
   long long graph_launches = 0; /* kernels per replay */
-  /* cg_set_host_*: page-locked host destinations (device views) that the
-   * stages fill as each output becomes final, on a copy stream that overlaps
-   * the stages still to run; one event per output kind orders the next
-   * writer of its source after the copy (0 catalogues, 1 maps, 2 kappa) */
+  /* cg_set_host_*: page-locked host destinations that the stages fill as
+   * each output becomes final, with copy-engine transfers on a copy stream
+   * that overlap the stages still to run (no SM is taken from them); one
+   * event per output kind orders the next writer of its source after the
+   * copy (0 catalogues, 1 maps, 2 kappa) */
   float *h_src[CG_NPOP_MAX] = {};
   long long *h_n[CG_NPOP_MAX] = {};
   long long h_cap[CG_NPOP_MAX] = {};
   float *h_imap[CG_NPOP_MAX] = {};
+  float *d_imap_out[CG_NPOP_MAX] = {}; /* data/nadd staged for the copy */
+  long long imap_out_n[CG_NPOP_MAX] = {};
   float *h_kappa = nullptr;
   cudaStream_t ostream = nullptr;
   cudaEvent_t oev[4] = {};
@@ -655,6 +658,8 @@ extern "C" void cg_destroy(cg_ctx *c)
     c->graph_done = nullptr;
   }
   for (float *q : c->d_lpt2)
+    if (q) cudaFree(q);
+  for (float *q : c->d_imap_out)
     if (q) cudaFree(q);
   void *ptrs[] = {c->d_tabs, c->d_norm, c->d_zr, c->d_r2n, c->d_pk, c->d_twN, c->d_twH, c->d_dens, c->d_npot, c->d_disp[0],
                   c->d_disp[1], c->d_disp[2], c->d_part, c->d_stats, c->d_s2f, c->d_err, c->d_ncount,
@@ -1340,11 +1345,17 @@ extern "C" int cg_imap_set_cartesian(cg_ctx *c)
     if (!c->h_imap[ip]) continue;
     const Imap &M = c->im[ip];
     const long long m = (long long)M.nr * M.npix;
-    if (int rc = out_begin(c)) return rc;
-    k_div_nadd<<<(unsigned)std::min<long long>((m + 255) / 256, (long long)c->nsm * 16), 256, 0, c->ostream>>>(
-        M.data, M.nadd, c->h_imap[ip], m);
+    if (c->imap_out_n[ip] != m) {
+      if (int rc = dalloc(c, &c->d_imap_out[ip], (size_t)m)) return rc;
+      c->imap_out_n[ip] = m;
+    }
+    k_div_nadd<<<(unsigned)std::min<long long>((m + 255) / 256, (long long)c->nsm * 16), 256, 0, c->stream>>>(
+        M.data, M.nadd, c->d_imap_out[ip], m);
     CUDA_TRY(c, cudaGetLastError());
     c->launches++;
+    if (int rc = out_begin(c)) return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(c->h_imap[ip], c->d_imap_out[ip], m * sizeof(float), cudaMemcpyDeviceToHost,
+                                c->ostream));
     if (int rc = out_end(c, 1)) return rc;
   }
   return CG_OK;
@@ -1623,15 +1634,19 @@ static int srcs_los_run(cg_ctx *c, int ip)
   return CG_OK;
 }
 
-/* Final catalogues to registered host buffers. */
+/* Final catalogues to registered host buffers (the counts are current:
+ * cg_get_beam_properties reads them first). */
 static int out_catalogs(cg_ctx *c)
 {
   for (int ip = 0; ip < c->cfg.n_srcs; ip++) {
-    if (!c->h_src[ip] || !c->d_total) continue;
+    if (!c->h_src[ip]) continue;
     const Cat &K = c->cat[ip];
+    const long long k = std::min(K.n, c->h_cap[ip]);
+    *c->h_n[ip] = K.n;
+    if (k <= 0) continue;
     if (int rc = out_begin(c)) return rc;
-    CUDA_TRY(c, cg_srcs_copy_out(c->ostream, K.src, c->d_total + ip, K.cap, c->h_src[ip], c->h_cap[ip], c->h_n[ip]));
-    c->launches++;
+    CUDA_TRY(c, cudaMemcpyAsync(c->h_src[ip], K.src, (size_t)k * 9 * sizeof(float), cudaMemcpyDeviceToHost,
+                                c->ostream));
     if (int rc = out_end(c, 0)) return rc;
   }
   return CG_OK;
@@ -1687,11 +1702,10 @@ extern "C" int cg_set_host_catalog(cg_ctx *c, int ipop, float *src9, long long c
     return CG_OK;
   }
   if (cap < 0 || !n_out) return CG_EINVAL;
-  void *a = nullptr, *b = nullptr;
+  void *a = nullptr;
   if (int rc = host_view(c, src9, &a)) return rc;
-  if (int rc = host_view(c, n_out, &b)) return rc;
-  c->h_src[ipop] = static_cast<float *>(a);
-  c->h_n[ipop] = static_cast<long long *>(b);
+  c->h_src[ipop] = src9;
+  c->h_n[ipop] = n_out;
   c->h_cap[ipop] = cap;
   return CG_OK;
 }
@@ -1704,7 +1718,7 @@ extern "C" int cg_set_host_imap(cg_ctx *c, int ipop, float *map)
   void *a = nullptr;
   if (map)
     if (int rc = host_view(c, map, &a)) return rc;
-  c->h_imap[ipop] = static_cast<float *>(a);
+  c->h_imap[ipop] = map;
   return CG_OK;
 }
 
@@ -1804,8 +1818,8 @@ struct cg_batch {
   std::vector<cudaEvent_t> joins;
   std::vector<float> tune_ms; /* autotuner: time per stream count tried */
   /* cg_batch_set_host_catalog: per realisation, the population whose Src
-   * array each pass copies to pinned host memory (-1: none), the device views
-   * of the destination and of the count slot, and the destination's size */
+   * array each pass copies to pinned host memory (-1: none), the destination,
+   * the count slot and the destination's size */
   std::vector<int> out_pop;
   std::vector<float *> out_src;
   std::vector<long long *> out_n;
@@ -1853,9 +1867,15 @@ static int batch_pass(cg_batch *b, float *ms)
      * the other streams compute */
     const int ip = b->out_pop.empty() ? -1 : b->out_pop[i];
     if (ip >= 0) {
+      /* copy-engine transfers (no SM taken from the other graphs): the count,
+       * and the catalogue up to the smaller of the two capacities, since the
+       * count is only known on the device */
       const Cat &K = c->cat[ip];
-      if (cg_srcs_copy_out(st, K.src, c->d_total + ip, K.cap, b->out_src[i], b->out_cap[i], b->out_n[i]) !=
-          cudaSuccess)
+      const long long k = std::min(K.cap, b->out_cap[i]);
+      if (cudaMemcpyAsync(b->out_n[i], c->d_total + ip, sizeof(long long), cudaMemcpyDeviceToHost, st) !=
+              cudaSuccess ||
+          (k > 0 && cudaMemcpyAsync(b->out_src[i], K.src, (size_t)k * 9 * sizeof(float), cudaMemcpyDeviceToHost, st) !=
+                        cudaSuccess))
         return batch_fail(b, CG_ECUDA, "realisation %d: catalogue copy", i);
     }
   }
@@ -1936,20 +1956,18 @@ extern "C" int cg_batch_set_host_catalog(cg_batch *b, int i, int ipop, float *sr
   if (!c->d_total || !c->gexec)
     return batch_fail(b, CG_ESTATE, "realisation %d: no captured source stage", i);
   cudaSetDevice(b->device);
-  /* both ends must be page-locked host memory that the device can address */
-  void *dv[2] = {nullptr, nullptr};
+  /* both ends must be page-locked, or the copies would not be asynchronous */
   const void *hp[2] = {src9, n_out};
   for (int k = 0; k < 2; k++) {
     cudaPointerAttributes a;
-    if (cudaPointerGetAttributes(&a, hp[k]) != cudaSuccess || a.type != cudaMemoryTypeHost || !a.devicePointer) {
+    if (cudaPointerGetAttributes(&a, hp[k]) != cudaSuccess || a.type != cudaMemoryTypeHost) {
       cudaGetLastError();
       return batch_fail(b, CG_EINVAL, "realisation %d: host catalogue buffers must be pinned (cudaHostAlloc)", i);
     }
-    dv[k] = a.devicePointer;
   }
   b->out_pop[i] = ipop;
-  b->out_src[i] = static_cast<float *>(dv[0]);
-  b->out_n[i] = static_cast<long long *>(dv[1]);
+  b->out_src[i] = src9;
+  b->out_n[i] = n_out;
   b->out_cap[i] = cap;
   return CG_OK;
 }

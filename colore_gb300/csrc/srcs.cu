@@ -490,39 +490,3 @@ cudaError_t cg_srcs_beam_rsd(cudaStream_t s, const float *phi, const cg_srcs_par
   k_beam_rsd<<<(unsigned)blocks, 256, 0, s>>>(phi, *p, nsrc);
   return cudaGetLastError();
 }
-
-namespace {
-/* Source records are 36 B: the bulk moves as 16-byte words when both ends
- * are 16-byte aligned, the rest as floats.  The copy is bound by the host
- * link, so a few blocks per SM pair suffice and the other graphs of a batch
- * keep the SMs. */
-__global__ void __launch_bounds__(256) k_copy_out(const float *__restrict__ src, const long long *__restrict__ total,
-                                                  long long dev_cap, float *dst, long long host_cap,
-                                                  long long *n_out)
-{
-  const long long n = *total;
-  long long m = n < dev_cap ? n : dev_cap;
-  if (m > host_cap) m = host_cap;
-  if (m < 0) m = 0;
-  if (blockIdx.x == 0 && threadIdx.x == 0) *n_out = n;
-  const long long nf = m * 9;
-  const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, nt = (long long)gridDim.x * blockDim.x;
-  if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0) {
-    const long long n4 = nf / 4;
-    const float4 *s4 = reinterpret_cast<const float4 *>(src);
-    float4 *d4 = reinterpret_cast<float4 *>(dst);
-    for (long long i = t0; i < n4; i += nt) d4[i] = __ldg(&s4[i]);
-    for (long long i = 4 * n4 + t0; i < nf; i += nt) dst[i] = __ldg(&src[i]);
-  } else {
-    for (long long i = t0; i < nf; i += nt) dst[i] = __ldg(&src[i]);
-  }
-}
-} /* namespace */
-
-cudaError_t cg_srcs_copy_out(cudaStream_t s, const float *src, const long long *total, long long dev_cap, float *dst,
-                             long long host_cap, long long *n_out)
-{
-  if (!total || !dst || !n_out || dev_cap < 0 || host_cap < 0) return cudaErrorInvalidValue;
-  k_copy_out<<<64, 256, 0, s>>>(src, total, dev_cap, dst, host_cap, n_out);
-  return cudaGetLastError();
-}

@@ -70,10 +70,4 @@ cudaError_t cg_srcs_emit(cudaStream_t s, const float *phi, const cg_srcs_params 
 cudaError_t cg_srcs_beam_rsd(cudaStream_t s, const float *phi, const cg_srcs_params *p, long long nsrc, int nsm);
 cudaError_t cg_srcs_lensing(cudaStream_t s, const float *phi, const cg_los_params *p, int nsm);
 cudaError_t cg_srcs_skewers(cudaStream_t s, const float *dens, const float *phi, const cg_los_params *p, int nsm);
-/* Copy the first min(*total, dev_cap, host_cap) sources' 9 floats of src to
- * dst (device-visible pinned host memory) and *total to *n_out, with no host
- * synchronisation: the source count is read on the device. */
-cudaError_t cg_srcs_copy_out(cudaStream_t s, const float *src, const long long *total, long long dev_cap, float *dst,
-                             long long host_cap, long long *n_out);
-
 #endif

@@ -238,9 +238,11 @@ cg_ctx *cg_batch_context(cg_batch *b, int i);
  * (its Src array, 9 floats per source) into src9 and its source count into
  * *n_out, behind the realisation's graph on the same stream, so the copies
  * overlap the other realisations' work and need no host synchronisation.
- * src9 (cap sources) and n_out must be page-locked host memory the device
- * can address (cudaHostAlloc); when *n_out > cap only cap sources were
- * copied.  src9 = NULL stops the copies for realisation i. */
+ * src9 (cap sources) and n_out must be page-locked host memory
+ * (cudaHostAlloc).  The count is only known on the device, so the copy
+ * moves min(cap, the catalogue's device capacity) records; those past
+ * *n_out are unspecified, and when *n_out > cap only cap sources arrived.
+ * src9 = NULL stops the copies for realisation i. */
 int cg_batch_set_host_catalog(cg_batch *b, int i, int ipop, float *src9, long long cap, long long *n_out);
 const char *cg_batch_last_error(const cg_batch *b);
 void cg_batch_destroy(cg_batch *b);

@@ -127,9 +127,7 @@ def test_batch_host_catalogs(built, tmp_path):
             assert cnt[0] == n == ns[i]
             ref = b.mocks[i].catalog(0, pos=False, ipix=False)["src"]
             k = min(n, cap)
-            assert np.array_equal(src[:k], ref[:k]), i
-            if cap > n:
-                assert np.all(src[n:] == -7.0)
+            assert np.array_equal(src[:k], ref[:k]), i  # records past the count are unspecified
     with pytest.raises(cg.CGError, match="pinned"):
         b.set_host_catalog(0, 0, np.zeros((10, 9), np.float32), np.zeros(1, np.int64))
     b.set_host_catalog(1, 0, None, None)
