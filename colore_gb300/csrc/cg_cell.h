@@ -158,20 +158,14 @@ CG_HD void cg_cart2sph(float x, float y, float z, float *r, float *cth, float *p
   *phi = ph;
 }
 
-/* he_ang2pix (RING), healpix_extra.c:118-172.  Integer work is 32-bit:
- * every intermediate fits for nside <= 8192 (NSIDE_MAX_HPX, common.h:94). */
-CG_HD int64_t cg_ang2pix_ring(int64_t nside64, float cth, float phi)
+/* he_ang2pix (RING), healpix_extra.c:118-172, for phi already in
+ * [0, 2 pi).  Integer work is 32-bit: every intermediate fits for
+ * nside <= 8192 (NSIDE_MAX_HPX, common.h:94). */
+CG_HD int64_t cg_ang2pix_ring_02pi(int64_t nside64, float cth, float ph)
 {
   const int nside = (int)nside64;
   float ctha = cg_fabsf(cth);
-  float ph = phi;
-  if (ph >= 0.0f) {
-    if (!(ph < CG_TWOPI_F)) ph = fmodf(ph, CG_TWOPI_F);
-  } else {
-    float tmp = CG_ADD(fmodf(ph, CG_TWOPI_F), CG_TWOPI_F);
-    ph = (tmp == CG_TWOPI_F) ? 0.0f : tmp;
-  }
-  float tt = CG_MUL(ph, 0.636619772367581343f); /* in [0,4) */
+  float tt = CG_MUL(ph, 0.636619772367581343f); /* in [0,4] */
   float ns = (float)nside;
   if (ctha <= 0.666666666666666667f) {
     float temp1 = CG_MUL(ns, CG_ADD(0.5f, tt));
@@ -201,6 +195,19 @@ CG_HD int64_t cg_ang2pix_ring(int64_t nside64, float cth, float phi)
     if (cth > 0.0f) return (int64_t)(2 * ir * (ir - 1) + ip);
     return (int64_t)(12 * nside * nside - 2 * ir * (ir + 1) + ip);
   }
+}
+
+/* he_ang2pix (RING) for any phi: reduced to [0, 2 pi) first. */
+CG_HD int64_t cg_ang2pix_ring(int64_t nside64, float cth, float phi)
+{
+  float ph = phi;
+  if (ph >= 0.0f) {
+    if (!(ph < CG_TWOPI_F)) ph = fmodf(ph, CG_TWOPI_F);
+  } else {
+    float tmp = CG_ADD(fmodf(ph, CG_TWOPI_F), CG_TWOPI_F);
+    ph = (tmp == CG_TWOPI_F) ? 0.0f : tmp;
+  }
+  return cg_ang2pix_ring_02pi(nside64, cth, ph);
 }
 
 /* ---- NEST <-> RING (Gorski et al. 2005, ApJ 622, 759), integer only ---- */
@@ -504,7 +511,11 @@ CG_HD int cg_imap_sample(float x, float y, float z, float yz2, float drr, const 
     ph = cg_atan2f(y, x);
     if (ph < 0.0f) ph = CG_ADD(ph, CG_TWOPI_F);
   }
-  *pix = cg_ang2pix_ring(nside, cth, ph);
+  /* atan2 in (-pi, pi] shifted by 2 pi below 0 gives [0, 2 pi] in exact
+   * arithmetic; the rounded sum can reach 2 pi itself, which the general
+   * entry point maps to 0 */
+  if (!(ph < CG_TWOPI_F)) ph = 0.0f;
+  *pix = cg_ang2pix_ring_02pi(nside, cth, ph);
   return ir;
 }
 
