@@ -174,10 +174,11 @@ CG_HD int64_t cg_ang2pix_ring_02pi(int64_t nside64, float cth, float ph)
     int jm = (int)CG_ADD(temp1, temp2);
     int ir = nside + 1 + jp - jm;
     int kshift = 1 - (ir & 1);
-    int ip = (jp + jm - nside + kshift + 1) / 2;
+    int ip = (jp + jm - nside + kshift + 1) >> 1; /* the sum is >= kshift >= 0 (below) */
     /* ip mod 4 nside: phi in [0, 2 pi) puts tt in [0, 4] and temp1 in
-     * [nside / 2, 4.5 nside], so jp + jm is in [nside - 1, 9 nside + 1], ip
-     * in [0, 4 nside + 1], and one subtraction gives the modulo */
+     * [nside / 2, 4.5 nside], so jp + jm is in [nside - 1, 9 nside + 1]
+     * (each truncation loses less than 1), ip in [0, 4 nside + 1], and one
+     * subtraction gives the modulo */
     const int m = 4 * nside;
     if (ip >= m) ip -= m;
     return (int64_t)(nside * (nside - 1) * 2 + (ir - 1) * 4 * nside + ip);
