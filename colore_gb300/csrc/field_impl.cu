@@ -94,15 +94,12 @@ __device__ __forceinline__ float2 gen_mode(const FillParams &p, int kx, int ky, 
   return make_float2(mod * c, mod * s);
 }
 
-/* Field values of one mode: F = 2 -> (delta_k, phi_k) (fourier.c:337-352);
- * F = 3 -> 1LPT displacements i k_a delta'_k / (N^3 k^2) (density.c:430-436)
- * where delta'_k = r2c(delta_G) = N^3 norm H(delta_k) and H is the Hermitian
- * projection that the c2r applied on the kx = 0 and kx = N/2 planes; with
- * lpt_kind 1 or 2 the second derivatives i k_i (i k_j delta'_k / (N^3 k^2))
- * of 2LPT (density.c:704-709), xx xy xz or yy yz zz. */
+/* Field values of one mode of the two-field fill: (delta_k, phi_k)
+ * (fourier.c:337-352). */
 template <int F>
 __device__ __forceinline__ void gen_fields(const FillParams &p, int kx, int ky, int kz, float2 *f)
 {
+  static_assert(F == 2, "the three-field fills use lpt_base and lpt_field");
   float k2, sm;
   float2 d = gen_mode(p, kx, ky, kz, k2, sm);
   if (!(k2 > 0.0f)) {
@@ -110,45 +107,18 @@ __device__ __forceinline__ void gen_fields(const FillParams &p, int kx, int ky, 
     for (int j = 0; j < F; j++) f[j] = make_float2(0.0f, 0.0f);
     return;
   }
-  if (F == 2) {
-    float g = -p.prefac / k2;
-    float2 phi = make_float2(g * d.x, g * d.y);
-    if (p.do_smooth) {
-      d.x *= sm;
-      d.y *= sm;
-      if (p.smooth_pot) {
-        phi.x *= sm;
-        phi.y *= sm;
-      }
-    }
-    f[0] = d;
-    f[1] = phi;
-  } else {
+  float g = -p.prefac / k2;
+  float2 phi = make_float2(g * d.x, g * d.y);
+  if (p.do_smooth) {
     d.x *= sm;
     d.y *= sm;
-    if (kx == 0 || kx == N / 2) {
-      int ky2 = ky == 0 ? 0 : N - ky, kz2 = kz == 0 ? 0 : N - kz;
-      float k2b, smb;
-      float2 e = gen_mode(p, kx, ky2, kz2, k2b, smb);
-      e.x *= smb;
-      e.y *= smb;
-      d = make_float2(0.5f * (d.x + e.x), 0.5f * (d.y - e.y));
-    }
-    float s = p.lpt_norm / k2;
-    float kv[3] = {(float)kx * p.dk, kcomp(ky, N, p.dk), kcomp(kz, N, p.dk)};
-    if (p.lpt_kind == 0) {
-#pragma unroll
-      for (int a = 0; a < 3; a++) f[a] = make_float2(-kv[a] * s * d.y, kv[a] * s * d.x);
-    } else {
-      const float ki[3] = {p.lpt_kind == 1 ? kv[0] : kv[1], p.lpt_kind == 1 ? kv[0] : kv[1], p.lpt_kind == 1 ? kv[0] : kv[2]};
-      const float kj[3] = {p.lpt_kind == 1 ? kv[0] : kv[1], p.lpt_kind == 1 ? kv[1] : kv[2], kv[2]};
-#pragma unroll
-      for (int a = 0; a < 3; a++) {
-        const float g = -ki[a] * kj[a] * s;
-        f[a] = make_float2(g * d.x, g * d.y);
-      }
+    if (p.smooth_pot) {
+      phi.x *= sm;
+      phi.y *= sm;
     }
   }
+  f[0] = d;
+  f[1] = phi;
 }
 
 /* Pass 1: fill + z transform of F fields.  grid = (ceil(NH/TX), N).
@@ -185,6 +155,77 @@ __global__ void __launch_bounds__(TX *PF) k_fill_z(float2 *o0, float2 *o1, float
 #pragma unroll
   for (int j = 0; j < F; j++) {
     auto ld = [&](int pos) -> float2 { return smem[(size_t)j * N * TX + pos * TX + c]; };
+    float2 *o = outs[j];
+    auto st = [&](int pos, float2 v) {
+      if (ok) o[((size_t)pos * N + ky) * NH + kx] = v;
+    };
+    cgfft::transform<N, PL::FR, PL::F0, PL::F1, PL::F2, 1>(t, twN, ld, st, sm);
+    __syncthreads();
+  }
+}
+
+/* The three-field fills: 1LPT displacements i k_a delta'_k / (N^3 k^2)
+ * (density.c:430-436), where delta'_k = r2c(delta_G) = N^3 norm H(delta_k)
+ * and H is the Hermitian projection that the c2r applied on the kx = 0 and
+ * kx = N/2 planes; with lpt_kind 1 or 2 the second derivatives
+ * i k_i (i k_j delta'_k / (N^3 k^2)) of 2LPT (density.c:704-709), xx xy xz
+ * or yy yz zz.  One value per mode is kept, b = delta'_k / (N^3 k^2) with
+ * the smoothing (0 at k = 0), and each field is formed from it as the
+ * transform loads it. */
+__device__ __forceinline__ float2 lpt_base(const FillParams &p, int kx, int ky, int kz)
+{
+  float k2, sm;
+  float2 d = gen_mode(p, kx, ky, kz, k2, sm);
+  if (!(k2 > 0.0f)) return make_float2(0.0f, 0.0f);
+  d.x *= sm;
+  d.y *= sm;
+  if (kx == 0 || kx == N / 2) {
+    int ky2 = ky == 0 ? 0 : N - ky, kz2 = kz == 0 ? 0 : N - kz;
+    float k2b, smb;
+    float2 e = gen_mode(p, kx, ky2, kz2, k2b, smb);
+    e.x *= smb;
+    e.y *= smb;
+    d = make_float2(0.5f * (d.x + e.x), 0.5f * (d.y - e.y));
+  }
+  const float s = p.lpt_norm / k2;
+  return make_float2(s * d.x, s * d.y);
+}
+
+__device__ __forceinline__ float2 lpt_field(const FillParams &p, int j, int kx, int ky, int kz, float2 b)
+{
+  const float kv[3] = {(float)kx * p.dk, kcomp(ky, N, p.dk), kcomp(kz, N, p.dk)};
+  if (p.lpt_kind == 0) return make_float2(-kv[j] * b.y, kv[j] * b.x);
+  const float ki[3] = {p.lpt_kind == 1 ? kv[0] : kv[1], p.lpt_kind == 1 ? kv[0] : kv[1], p.lpt_kind == 1 ? kv[0] : kv[2]};
+  const float kj[3] = {p.lpt_kind == 1 ? kv[0] : kv[1], p.lpt_kind == 1 ? kv[1] : kv[2], kv[2]};
+  const float g = -ki[j] * kj[j];
+  return make_float2(g * b.x, g * b.y);
+}
+
+/* Pass 1 of the three-field fills: as k_fill_z, but each thread parks one
+ * value per mode (lpt_base) in the second shared-memory slot and the first
+ * stage of each transform forms the field from it (lpt_field); the first
+ * slot is the exchange buffer.  Two slots instead of three per block, so
+ * three blocks fit on an SM. */
+template <int TX>
+__global__ void __launch_bounds__(TX *PF, 3) k_fill_z3(float2 *o0, float2 *o1, float2 *o2, FillParams p,
+                                                       const float2 *__restrict__ twN)
+{
+  extern __shared__ float2 smem[];
+  const int c = threadIdx.x % TX, t = threadIdx.x / TX;
+  const int kx = blockIdx.x * TX + c, ky = blockIdx.y;
+  const bool ok = kx < NH;
+  float2 *base = smem + (size_t)N * TX;
+#pragma unroll 1
+  for (int e = 0; e < PL::FR; e++) {
+    const int i = e / PL::F0, q = e - i * PL::F0;
+    const int pos = t + (N / PL::FR) * i + q * (N / PL::F0); /* cgfft::in_pos of stage 0 */
+    base[pos * TX + c] = ok ? lpt_base(p, kx, ky, pos) : make_float2(0.0f, 0.0f);
+  }
+  float2 *outs[3] = {o0, o1, o2};
+  auto sm = [&](int pos) -> float2 & { return smem[pos * TX + c]; };
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    auto ld = [&](int pos) -> float2 { return lpt_field(p, j, kx, ky, pos, base[pos * TX + c]); };
     float2 *o = outs[j];
     auto st = [&](int pos, float2 v) {
       if (ok) o[((size_t)pos * N + ky) * NH + kx] = v;
@@ -402,15 +443,15 @@ extern "C" cudaError_t CG_CAT(cg_field_lpt_, CG_N)(const cg_field_launch *L)
 {
   using namespace cg;
   constexpr int TX3 = PL::TX3, TXY = PL::TXY;
-  size_t sm1 = (size_t)3 * N * TX3 * sizeof(float2);
+  size_t sm1 = (size_t)2 * N * TX3 * sizeof(float2); /* one value per mode + the exchange buffer */
   size_t sm2 = (size_t)N * TXY * sizeof(float2);
   size_t sm3 = (size_t)PL::RB * ROWS * sizeof(float2);
   cudaError_t e;
-  if ((e = prep(k_fill_z<3, TX3>, sm1)) != cudaSuccess) return e;
+  if ((e = prep(k_fill_z3<TX3>, sm1)) != cudaSuccess) return e;
   if ((e = prep(k_col_y<TXY, 1>, sm2)) != cudaSuccess) return e;
   if ((e = prep(k_row_c2r<false>, sm3)) != cudaSuccess) return e;
   dim3 g1((NH + TX3 - 1) / TX3, N);
-  k_fill_z<3, TX3><<<g1, TX3 * PF, sm1, L->stream>>>(L->f[0], L->f[1], L->f[2], L->fill, L->twN);
+  k_fill_z3<TX3><<<g1, TX3 * PF, sm1, L->stream>>>(L->f[0], L->f[1], L->f[2], L->fill, L->twN);
   if (L->ev) cudaEventRecord(L->ev[0], L->stream);
   dim3 g2((NH + TXY - 1) / TXY, N, 3);
   k_col_y<TXY, 1><<<g2, TXY * P, sm2, L->stream>>>(L->f[0], L->f[1], L->f[2], L->twN);
