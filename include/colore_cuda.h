@@ -199,7 +199,9 @@ int cg_get_beam_properties(cg_ctx *ctx);
  * sources, 9 floats each; *n_out receives the source count, more than cap
  * when the buffer was short) and the convergence maps (as cg_download_kappa
  * gives) during cg_get_beam_properties.  The data are valid after cg_sync.
- * NULL stops the copies. */
+ * A registered map costs a device staging buffer of its size (data/nadd is
+ * formed there for the copy), beyond cg_memory_estimate.  NULL stops the
+ * copies. */
 int cg_set_host_catalog(cg_ctx *ctx, int ipop, float *src9, long long cap, long long *n_out);
 int cg_set_host_imap(cg_ctx *ctx, int ipop, float *map);
 int cg_set_host_kappa(cg_ctx *ctx, float *map);
