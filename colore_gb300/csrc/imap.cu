@@ -274,9 +274,17 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_sum(const unsigned int *__restr
 {
   const long long i0 = ((long long)blockIdx.x * SCAN_T + threadIdx.x) * SCAN_I;
   long long t = 0;
+  if (i0 + SCAN_I <= H) { /* 16 records, 64 B aligned */
 #pragma unroll
-  for (int i = 0; i < SCAN_I; i++)
-    if (i0 + i < H) t += n[i0 + i];
+    for (int i = 0; i < SCAN_I; i += 4) {
+      const uint4 q = __ldg(reinterpret_cast<const uint4 *>(n + i0 + i));
+      t += (long long)q.x + q.y + q.z + q.w;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < SCAN_I; i++)
+      if (i0 + i < H) t += n[i0 + i];
+  }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
   __shared__ long long ws[SCAN_T / 32];
@@ -319,13 +327,24 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_out(const unsigned int *__restr
                                                       const long long *__restrict__ bexcl, long long *off)
 {
   const long long i0 = ((long long)blockIdx.x * SCAN_T + threadIdx.x) * SCAN_I;
+  const bool full = i0 + SCAN_I <= H; /* a thread's 16 records, 64 B aligned */
   unsigned int v[SCAN_I];
   long long t = 0;
+  if (full) {
 #pragma unroll
-  for (int i = 0; i < SCAN_I; i++) {
-    v[i] = i0 + i < H ? n[i0 + i] : 0u;
-    t += v[i];
+    for (int i = 0; i < SCAN_I; i += 4) {
+      const uint4 q = __ldg(reinterpret_cast<const uint4 *>(n + i0 + i));
+      v[i] = q.x;
+      v[i + 1] = q.y;
+      v[i + 2] = q.z;
+      v[i + 3] = q.w;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < SCAN_I; i++) v[i] = i0 + i < H ? n[i0 + i] : 0u;
   }
+#pragma unroll
+  for (int i = 0; i < SCAN_I; i++) t += v[i];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   long long inc = t;
 #pragma unroll
@@ -339,10 +358,20 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_out(const unsigned int *__restr
   long long run = bexcl[blockIdx.x];
   for (int w = 0; w < wid; w++) run += ws[w];
   run += inc - t;
+  if (full) {
 #pragma unroll
-  for (int i = 0; i < SCAN_I; i++) {
-    if (i0 + i < H) off[i0 + i] = run;
-    run += v[i];
+    for (int i = 0; i < SCAN_I; i += 2) {
+      const long long a = run;
+      run += v[i];
+      reinterpret_cast<longlong2 *>(off + i0)[i / 2] = make_longlong2(a, run);
+      run += v[i + 1];
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < SCAN_I; i++) {
+      if (i0 + i < H) off[i0 + i] = run;
+      run += v[i];
+    }
   }
 }
 
