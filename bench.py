@@ -220,7 +220,32 @@ def run_ours(args):
         outs["kappa"] = torch.empty((cfg.n_kappa, 12 * cfg.nside_kappa ** 2), dtype=torch.float32,
                                     pin_memory=True).numpy()
     m.set_host_outputs(catalogs=cats, imaps=imaps, kappa=outs.get("kappa"))
-    e2e_steps = max(1, min(args.steps, 3))
+
+    def e2e_step():
+        m.upload_tables()
+        m.run()
+        m.sync()
+        t1 = time.perf_counter()
+        nb = 0
+        for i in range(cfg.n_srcs):
+            ns = int(outs["n%d" % i][0])
+            if ns > outs["src%d" % i].shape[0]:
+                raise RuntimeError("host catalogue buffer too short")
+            nb += ns * 36 + 8
+            if cfg.nside_count[i]:
+                m.count_map(i, out=outs["cmap%d" % i])
+                nb += outs["cmap%d" % i].nbytes
+        for i in range(cfg.n_imap):
+            nb += outs["imap%d" % i].nbytes
+        if cfg.do_kappa:
+            nb += outs["kappa"].nbytes
+        return nb, time.perf_counter() - t1
+
+    # untimed steps first: the first steps after registering the host
+    # outputs set up the copy stream and the maps' staging buffers
+    for _ in range(max(1, min(args.warmup, 3))):
+        e2e_step()
+    e2e_steps = max(10, args.steps)
     d2h = 0
     h2d = 0
     barrier()
@@ -228,24 +253,8 @@ def run_ours(args):
     t0 = time.perf_counter()
     t_dl = 0.0
     for _ in range(e2e_steps):
-        m.upload_tables()
-        m.run()
-        m.sync()
-        t1 = time.perf_counter()
-        d2h = 0
-        for i in range(cfg.n_srcs):
-            ns = int(outs["n%d" % i][0])
-            if ns > outs["src%d" % i].shape[0]:
-                raise RuntimeError("host catalogue buffer too short")
-            d2h += ns * 36 + 8
-            if cfg.nside_count[i]:
-                m.count_map(i, out=outs["cmap%d" % i])
-                d2h += outs["cmap%d" % i].nbytes
-        for i in range(cfg.n_imap):
-            d2h += outs["imap%d" % i].nbytes
-        if cfg.do_kappa:
-            d2h += outs["kappa"].nbytes
-        t_dl += time.perf_counter() - t1
+        d2h, dt = e2e_step()
+        t_dl += dt
     torch.cuda.synchronize()
     t_e2e = (time.perf_counter() - t0) / e2e_steps
     t_dl /= e2e_steps
@@ -319,6 +328,21 @@ def run_ours(args):
                               if dom[0] == "imap_paint" else "see kernels"} if dom else None,
         "clocks": clk.summary(),
     }
+    if not args.no_fp64:
+        # the metric's gate: the Gaussian field and potential of this
+        # realisation against the FP64 path's, mode for mode, on the device
+        # (relative rms and the P(k) error per shell of width k_f)
+        from colore_gb300 import validate
+        m.create_cartesian_fields()
+        f64 = cg.Mock64(prm, device=local)
+        f64.create_cartesian_fields()
+        fe = validate.field_errors(m, f64)
+        f64.close()
+        torch.cuda.empty_cache()
+        out["pk_max_rel_err"] = max(fe[0]["pk_max_rel_err"], fe[1]["pk_max_rel_err"])
+        out["field_errors_vs_fp64"] = {
+            lab: {"rel_rms": fe[w]["rel_rms"], "pk_max_rel_err": fe[w]["pk_max_rel_err"],
+                  "shells": len(fe[w]["pk_rel_err"])} for w, lab in ((0, "delta_G"), (1, "phi"))}
     if world == 1 and not args.no_fp64:
         # the plain FP64 path of the same sequence on the same GPU (first run
         # allocates; the second is timed with CUDA events)
@@ -415,8 +439,9 @@ def batched_measure(args, rank, world, local, dist, baselines):
         cnt_i = torch.empty(1, dtype=torch.int64, pin_memory=True).numpy()
         b.set_host_catalog(i, 0, src_i, cnt_i)
         hosts.append((src_i, cnt_i))
-    b.run()  # warm the copies
-    e2e_steps = max(1, min(args.steps, 2))
+    for _ in range(2):  # warm the copies
+        b.run()
+    e2e_steps = max(10, args.steps)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     d2h = 0
@@ -474,7 +499,6 @@ def cpu_baseline_batched(args):
     """The FP64 oracle on one realisation of each grid size of the batch
     (field, density, bins, Poisson totals; OpenMP on every host core),
     scaled to the 48 realisations (16 of each size)."""
-    import colore_gb300 as cg
     from colore_gb300 import inputs
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
@@ -485,7 +509,7 @@ def cpu_baseline_batched(args):
         n = s["n_grid"]
         if n in per:
             continue
-        c = cg.Params(inputs.write_inputs(os.path.join(d, str(n)), s))
+        c = orc.Params(inputs.write_inputs(os.path.join(d, str(n)), s))
         cfg = c.config
         t = time.perf_counter()
         dens, npot, st = orc.field64(cfg)
@@ -523,17 +547,16 @@ def cpu_baseline(args):
       kappa: every pix_stride-th pixel gives the ray steps/s, times the full
         grid's ray steps."""
     import numpy as np
-    import colore_gb300 as cg
     from colore_gb300 import inputs
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
     full = config_spec(args.config, args.n)
     ns_ = args.cpu_n
     d = tempfile.mkdtemp(prefix="colore_cpu_")
-    prm_f = cg.Params(inputs.write_inputs(os.path.join(d, "full"), full))
+    prm_f = orc.Params(inputs.write_inputs(os.path.join(d, "full"), full))
     cf = prm_f.config
     nf = cf.n_grid
-    prm = cg.Params(inputs.write_inputs(os.path.join(d, "sample"), config_spec(args.config, ns_)))
+    prm = orc.Params(inputs.write_inputs(os.path.join(d, "sample"), config_spec(args.config, ns_)))
     c = prm.config
     T = {}
     t = time.perf_counter()
@@ -599,15 +622,16 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import colore_gb300 as cg
     from colore_gb300 import inputs
-    prm = cg.Params(inputs.write_inputs(tempfile.mkdtemp(prefix="colore_ref_"), config_spec(args.config, args.n)))
+    # the CPU arm loads the oracle library alone (its own build of the host
+    # param reader and tables), never the GPU library
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    prm = orc.Params(inputs.write_inputs(tempfile.mkdtemp(prefix="colore_ref_"), config_spec(args.config, args.n)))
     # warm-up steps: the oracle library loaded and its OpenMP pool running, on
     # the same configuration at 64^3 (each timed step is a bounded sample of
     # the full workload)
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as orc
-    small = cg.Params(inputs.write_inputs(tempfile.mkdtemp(prefix="colore_refw_"), config_spec(args.config, 64)))
+    small = orc.Params(inputs.write_inputs(tempfile.mkdtemp(prefix="colore_refw_"), config_spec(args.config, 64)))
     for _ in range(args.warmup):
         orc.field64(small.config)
     vals = []

@@ -131,6 +131,7 @@ def lib():
             "cg64_destroy": (None, [vp]),
             "cg64_last_error": (C.c_char_p, [vp]),
             "cg64_run_mock": (C.c_int, [vp, C.POINTER(C.c_float)]),
+            "cg64_create_cartesian_fields": (C.c_int, [vp]),
             "cg64_num_sources": (C.c_longlong, [vp, C.c_int]),
             "cg64_download": (C.c_int, [vp, C.c_int, C.c_int, vp]),
             "cg_write_healpix_map": (C.c_int, [C.c_char_p, vp, C.c_long]),
@@ -169,7 +170,7 @@ def exported_symbols():
             "cg_batch_last_error", "cg_batch_destroy",
             "cg_skewer_background", "cg_write_predictions", "cg_pk_linear0", "cg_pk2xi", "cg_xi2pk",
             "cg64_create", "cg64_destroy", "cg64_last_error",
-            "cg64_run_mock", "cg64_num_sources", "cg64_download"]
+            "cg64_run_mock", "cg64_create_cartesian_fields", "cg64_num_sources", "cg64_download"]
 
 
 class CGError(RuntimeError):
@@ -424,8 +425,11 @@ class Mock:
 
     # host mirrors
     def grid(self, which=0, out=None):
+        """Padded grid `which` (cg_download_grid) into a new host array, or
+        into `out`: a host array or a CUDA torch tensor of the padded shape."""
         a = out if out is not None else np.empty(grid_shape(self.n), np.float32)
-        self._chk(lib().cg_download_grid(self._c, which, a.ctypes.data), "download_grid")
+        ptr = a.data_ptr() if hasattr(a, "data_ptr") else a.ctypes.data
+        self._chk(lib().cg_download_grid(self._c, which, ptr), "download_grid")
         return a
 
     def num_sources(self, ipop):
@@ -601,13 +605,20 @@ class Mock64:
         self._chk(lib().cg64_run_mock(self._c, C.byref(ms)), "cg64_run_mock")
         return ms.value
 
+    def create_cartesian_fields(self):
+        """Only the Gaussian field and potential (then density(0) is delta_G)."""
+        self._chk(lib().cg64_create_cartesian_fields(self._c), "cg64_create_cartesian_fields")
+
     def num_sources(self, ipop):
         return lib().cg64_num_sources(self._c, ipop)
 
-    def density(self, which=0):
+    def density(self, which=0, out=None):
+        """Unpadded N^3 doubles of the density (0) or potential (1), into a new
+        host array or into `out` (a host array or a CUDA torch tensor)."""
         n = self.cfg.n_grid
-        a = np.empty((n, n, n), np.float64)
-        self._chk(lib().cg64_download(self._c, which, 0, a.ctypes.data), "cg64_download")
+        a = out if out is not None else np.empty((n, n, n), np.float64)
+        ptr = a.data_ptr() if hasattr(a, "data_ptr") else a.ctypes.data
+        self._chk(lib().cg64_download(self._c, which, 0, ptr), "cg64_download")
         return a
 
     def imap(self, ipop):

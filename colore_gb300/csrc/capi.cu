@@ -941,13 +941,15 @@ extern "C" int cg_collect_density_normalization(cg_ctx *c, int nz, double idz, d
 /* Device address of the static bins scratch, looked up once per device with
  * that device current (cudaGetSymbolAddress may load the module, so the
  * first call on a device must not be inside a stream capture) and kept for
- * the life of the process. */
+ * the life of the process.  The address belongs to the device's primary
+ * context: a host that calls cudaDeviceReset and keeps using the library
+ * leaves a stale entry here. */
 static std::mutex g_bins_scratch_mu;
-static void *g_bins_scratch_ptr[64];
+static void *g_bins_scratch_ptr[CG_MAX_DEVICES];
 
 static int bins_static_scratch(cg_ctx *c, void **out)
 {
-  if (c->device < 0 || c->device >= 64) return fail(c, CG_EINVAL, "device %d out of range", c->device);
+  if (c->device < 0 || c->device >= CG_MAX_DEVICES) return fail(c, CG_EINVAL, "device %d out of range", c->device);
   std::lock_guard<std::mutex> lock(g_bins_scratch_mu);
   if (!g_bins_scratch_ptr[c->device]) {
     void *ptr = nullptr;
@@ -1004,7 +1006,10 @@ extern "C" int cg_collect_density_normalization_static(cg_ctx *c, int nz, double
   p.ncount = ncount;
   p.zsum = zsum;
   p.bsum = bsum;
-  CUDA_TRY(c, cg_dens_bins(c->stream, c->d_dens, &p, c->nsm));
+  {
+    ProfScope ps(c, "dens_bins");
+    CUDA_TRY(c, cg_dens_bins(c->stream, c->d_dens, &p, c->nsm));
+  }
   c->launches++;
   c->pending_mode = CG_DMODE_NONE;
   if (narr)
@@ -2037,7 +2042,7 @@ extern "C" int cg_download_grid(cg_ctx *c, int which, void *dst)
   else if (which >= 2 && which <= 4) src = c->d_disp[which - 2];
   else if (which >= 5 && which <= 7) src = c->d_lpt2[which - 5];
   if (!src) return fail(c, CG_ESTATE, "grid %d not available", which);
-  CUDA_TRY(c, cudaMemcpyAsync(dst, src, c->grid_floats * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(dst, src, c->grid_floats * sizeof(float), cudaMemcpyDefault, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return check_device_errors(c);
 }

@@ -721,7 +721,9 @@ int dalloc(cg64_ctx *c, void **p, size_t bytes)
   return CG_OK;
 }
 
-int run(cg64_ctx *c)
+/* Gaussian field and potential (create_cartesian_fields, fourier.c:361-423):
+ * the fill, the two c2r transforms and the normalisation with the moments. */
+int run_fields(cg64_ctx *c)
 {
   const cg_config &cf = c->cfg;
   const int N = c->N, NH = c->NH, nsm = c->nsm;
@@ -753,6 +755,18 @@ int run(cg64_ctx *c)
   const double norm = pow(sqrt(2 * M_PI) / cf.l_box, 3);
   k64_scale<<<grid_for((long long)ncell, nsm), 256, 0, s>>>(p, c->d_dens, c->d_npot, norm, c->d_stats);
   CU(c, cudaGetLastError());
+  return CG_OK;
+}
+
+int run(cg64_ctx *c)
+{
+  const cg_config &cf = c->cfg;
+  const int N = c->N, NH = c->NH, nsm = c->nsm;
+  const size_t ncell = (size_t)N * N * N, nh = (size_t)N * N * NH, gbytes = nh * sizeof(double2);
+  cudaStream_t s = c->stream;
+  P64 p = params(c);
+  int rc;
+  if ((rc = run_fields(c))) return rc;
   /* physical density */
   if (cf.dens_type == CG_DENS_1LPT) {
     for (int a = 0; a < 3; a++)
@@ -1069,6 +1083,16 @@ extern "C" int cg64_run_mock(cg64_ctx *c, float *ms)
   return CG_OK;
 }
 
+extern "C" int cg64_create_cartesian_fields(cg64_ctx *c)
+{
+  if (!c) return CG_EINVAL;
+  if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, CG_ECUDA, "cudaSetDevice");
+  int rc = run_fields(c);
+  if (rc) return rc;
+  CU(c, cudaStreamSynchronize(c->stream));
+  return CG_OK;
+}
+
 extern "C" long long cg64_num_sources(const cg64_ctx *c, int ipop)
 {
   return (c && ipop >= 0 && ipop < c->cfg.n_srcs) ? c->nsrc[ipop] : -1;
@@ -1088,7 +1112,7 @@ extern "C" int cg64_download(cg64_ctx *c, int what, int ipop, void *dst)
     const double *g = what == 0 ? c->d_dens : c->d_npot;
     if (!g) return fail(c, CG_ESTATE, "not run");
     CU(c, cudaMemcpy2D(dst, N * sizeof(double), g, 2 * NH * sizeof(double), N * sizeof(double), (size_t)N * N,
-                       cudaMemcpyDeviceToHost));
+                       cudaMemcpyDefault));
     return CG_OK;
   }
   if (what == 2 || what == 3) {

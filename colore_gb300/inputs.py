@@ -53,8 +53,8 @@ def _bias(z, b):
     raise ValueError(b)
 
 
-# Run configurations (benchmark configs; nside choices where unstated are
-# written beside them).
+# Run configurations c1-c5 of the benchmark suite, as their text states them
+# (nside choices where the text leaves them open are written beside them).
 CONFIGS = {
     "c1": dict(n_grid=128, z_min=0.1, z_max=0.5, r_smooth=2.0, seed=1001, dens_type=0, bias_model=1,
                srcs=[dict(nz=("gauss", 0.3, 0.05), density=100.0, bias=("const", 1.5), nside_count=64)]),

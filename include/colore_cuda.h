@@ -166,9 +166,14 @@ int cg_collect_density_normalization(cg_ctx *ctx, int nz, double idz, double *za
  *  - nz is limited to 2..1024 bins (CG_EINVAL beyond, with a message);
  *  - the first call on each device looks up that array's address with the
  *    device current; make that first call before any stream capture;
+ *  - that address is kept for the life of the process: it belongs to the
+ *    device's primary context and goes stale if the host calls
+ *    cudaDeviceReset and then keeps using the library;
  *  - calls that overlap on the GPU (two contexts on one device, or the
  *    same context on two streams) share the array and race.
- * The sums are zeroed on the context's stream at every call. */
+ * The sums are zeroed on the context's stream at every call.  With
+ * profiling switched on (cg_set_profiling, off by default) the call logs a
+ * CUDA event pair around its kernel, as every stage does. */
 int cg_collect_density_normalization_static(cg_ctx *ctx, int nz, double idz, double *zarr,
                                             unsigned long long *narr, double *norm_srcs,
                                             double *norm_imap);
@@ -253,7 +258,8 @@ void cg_batch_destroy(cg_batch *b);
 /* which: 0 = density (grid_dens), 1 = potential (grid_npot), 2..4 = 1LPT
  * (first-order) displacement x,y,z, 5..7 = 2LPT second-order displacement
  * x,y,z.  dst holds N*N*2(N/2+1) values of the context's
- * precision (float or double), padded layout. */
+ * precision (float or double), padded layout; it may be host or device
+ * memory. */
 int cg_download_grid(cg_ctx *ctx, int which, void *dst);
 long long cg_num_sources(cg_ctx *ctx, int ipop);
 /* pos4: 4 floats per source (x,y,z,dz_rsd) as CatalogCartesian.pos;
@@ -310,10 +316,14 @@ const char *cg64_last_error(const cg64_ctx *ctx);
 /* Whole sequence; *ms (may be NULL) gets its device time from CUDA events. */
 int cg64_run_mock(cg64_ctx *ctx, float *ms);
 long long cg64_num_sources(const cg64_ctx *ctx, int ipop);
+/* Gaussian field and potential only (create_cartesian_fields,
+ * fourier.c:361-423); cg64_download 0 and 1 then give delta_G and phi. */
+int cg64_create_cartesian_fields(cg64_ctx *ctx);
 /* what: 0 density, 1 potential (N^3 doubles, [z][y][x]); 2 intensity-map
  * temperature sums and 3 hit counts (int) of species ipop (nr * npix, RING);
  * 4 convergence (n_kappa * npix doubles, RING); 5 normalisation table of
- * tracer ipop (CG_NA doubles; source populations first, then species). */
+ * tracer ipop (CG_NA doubles; source populations first, then species).
+ * dst of 0 and 1 may be host or device memory. */
 int cg64_download(cg64_ctx *ctx, int what, int ipop, void *dst);
 
 #ifdef __cplusplus

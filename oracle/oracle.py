@@ -68,6 +68,35 @@ def P(a):
     return a.ctypes.data if a is not None else None
 
 
+class Params:
+    """Run parameters and FP64 tables read by the oracle library's own build
+    of the host C side (no GPU library loaded): the same param-file reader
+    and table builder, for the CPU reference arm."""
+
+    def __init__(self, fname):
+        from colore_gb300 import Config  # the ctypes mirror of cg_config only
+        L = lib()
+        for name, res, args in (("cg_read_run_params", C.c_int, [C.c_char_p, C.POINTER(C.c_void_p), C.c_char_p,
+                                                                  C.c_size_t]),
+                                ("cg_params_free", None, [C.c_void_p]),
+                                ("cg_params_to_config", C.c_int, [C.c_void_p, C.POINTER(Config)])):
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        self._p = C.c_void_p()
+        err = C.create_string_buffer(1024)
+        if L.cg_read_run_params(os.fsencode(fname), C.byref(self._p), err, 1024):
+            raise RuntimeError("read_run_params(%s): %s" % (fname, err.value.decode()))
+        self.config = Config()
+        L.cg_params_to_config(self._p, C.byref(self.config))
+        self.config._owner = self
+
+    def __del__(self):
+        if getattr(self, "_p", None) and _lib is not None:
+            _lib.cg_params_free(self._p)
+            self._p = None
+
+
 def cfgp(cfg):
     return C.cast(C.pointer(cfg), C.c_void_p)
 

@@ -37,6 +37,12 @@ def _collect(fn, m, nz, idz):
     return n, z, bs[:nts * nz], bi[:nti * nz]
 
 
+def _free_bytes():
+    import torch
+    torch.cuda.synchronize(0)
+    return torch.cuda.mem_get_info(0)[0]
+
+
 @pytest.fixture
 def mock(built, tmp_path):
     import colore_gb300 as cg
@@ -57,12 +63,17 @@ def test_static_bins_match_allocating_entry(mock):
     # the first call also applies the pending lognormal transform in place
     ref = _collect(L.cg_collect_density_normalization, mock, nz, idz)
     assert ref[0].sum() > 0
-    for _ in range(2):
+    free = []
+    for _ in range(3):
         got = _collect(L.cg_collect_density_normalization_static, mock, nz, idz)
         assert np.array_equal(got[0], ref[0])
         for a, b in zip(got[1:], ref[1:]):
             assert np.all(np.isfinite(a))
             np.testing.assert_allclose(a, b, rtol=1e-12, atol=0)
+        free.append(_free_bytes())
+    # after the first call (which looks up the scratch array once per
+    # device) the entry takes no device memory: free memory stays put
+    assert free[1] == free[0] and free[2] == free[0], free
 
 
 def test_static_bins_rejects_more_bins_than_its_scratch(mock):
