@@ -123,6 +123,9 @@ def lib():
             "cg_download_isw": (C.c_int, [vp, vp]),
             "cg_download_custom": (C.c_int, [vp, C.c_int, vp]),
             "cg_download_norm": (C.c_int, [vp, C.c_int, C.c_int, vp, vp]),
+            "cg_download_norm64": (C.c_int, [vp, C.c_int, C.c_int, vp, vp]),
+            "cg_set_decisions_in_double": (C.c_int, [vp, C.c_int]),
+            "cg_exact_stats": (C.c_int, [vp, vp, C.c_int]),
             "cg_kernel_launches": (C.c_longlong, [vp]),
             "cg_set_profiling": (C.c_int, [vp, C.c_int]),
             "cg_kernel_times": (C.c_int, [vp, C.c_char_p, C.c_size_t, C.POINTER(C.c_float), C.c_int,
@@ -163,7 +166,8 @@ def exported_symbols():
             "cg_imap_set_cartesian", "cg_imap_samples", "cg_set_imap_list_cap", "cg_set_host_catalog",
             "cg_set_host_imap", "cg_set_host_kappa", "cg_get_beam_properties", "cg_run_mock", "cg_download_grid",
             "cg_num_sources", "cg_download_catalog", "cg_download_count_map", "cg_download_imap",
-            "cg_download_kappa", "cg_download_isw", "cg_download_custom", "cg_download_skewers", "cg_download_norm", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_read_run_params",
+            "cg_download_kappa", "cg_download_isw", "cg_download_custom", "cg_download_skewers", "cg_download_norm", "cg_download_norm64", "cg_set_decisions_in_double",
+            "cg_exact_stats", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_read_run_params",
             "cg_params_free", "cg_params_to_config", "cg_write_healpix_map", "cg_write_catalog",
             "cg_write_density_grid", "cg_graph_capture", "cg_graph_launch", "cg_batch_create", "cg_batch_run",
             "cg_batch_streams", "cg_batch_tuning", "cg_batch_context", "cg_batch_set_host_catalog",
@@ -499,6 +503,23 @@ class Mock:
         e = np.empty(2, np.float32)
         self._chk(lib().cg_download_norm(self._c, kind, ipop, t.ctypes.data, e.ctypes.data), "download_norm")
         return t, e
+
+    def norm_table64(self, kind, ipop):
+        """The same table in double, as the double decisions read it."""
+        t = np.empty(NA, np.float64)
+        e = np.empty(2, np.float64)
+        self._chk(lib().cg_download_norm64(self._c, kind, ipop, t.ctypes.data, e.ctypes.data), "download_norm64")
+        return t, e
+
+    def set_decisions_in_double(self, on=True):
+        """Take every integer decision (counts, pixels, hits) in double."""
+        self._chk(lib().cg_set_decisions_in_double(self._c, 1 if on else 0), "set_decisions_in_double")
+
+    def exact_stats(self, reset=False):
+        """Decisions taken in double since the last reset: dict of counts."""
+        a = np.zeros(4, np.uint64)
+        self._chk(lib().cg_exact_stats(self._c, a.ctypes.data, 1 if reset else 0), "exact_stats")
+        return dict(count_cells=int(a[0]), src_pixels=int(a[1]), imap_cells=int(a[2]), imap_samples=int(a[3]))
 
 
 class Batch:

@@ -78,6 +78,16 @@ struct cg_ctx {
   Tab tz[CG_NPOP_MAX], bzi[CG_NPOP_MAX], normi[CG_NPOP_MAX];
   Tab kzc[CG_NPOP_MAX], bzc[CG_NPOP_MAX], normc[CG_NPOP_MAX]; /* custom maps */
   float *d_norm = nullptr; /* (n_srcs + n_imap + n_cstm) tables of NA values and their 2 edge values */
+  /* the same tables in double, for the decisions that the float margins
+   * leave to the reference's double arithmetic (cg_exact.h): background r,
+   * z, V1, 1/H, then n(r), b(r) per source population and T(r), b(r) per
+   * intensity species; the normalisation tables with their edges; the cell
+   * corners i*dx - p per axis rounded once to float; and the counts of
+   * decisions taken in double (cg_exact_stats) */
+  double *d_tabs64 = nullptr, *d_norm64 = nullptr;
+  float *d_corner = nullptr;
+  unsigned long long *d_xstats = nullptr;
+  int force_double = 0;
   /* normalisation bins (density.c:1233-1245): z(r_i) of the table radii,
    * z(L/2), the bin count and width; bin buffers keep their capacity */
   double *d_zr = nullptr;
@@ -486,6 +496,43 @@ extern "C" int cg_upload_tables(cg_ctx *c, const cg_config *cfg)
     for (int p = 0; p < cfg->n_cstm; p++)
       c->normc[p] = Tab{c->d_norm + (size_t)(cfg->n_srcs + cfg->n_imap + p) * nas, 1.0f, 1.0f};
   }
+  /* double tables and float corners for the exact decisions */
+  {
+    const int nd = 4 + 2 * cfg->n_srcs + 2 * cfg->n_imap;
+    std::vector<double> hd((size_t)nd * na);
+    const double *bgd[4] = {cfg->r_arr_r2z, cfg->z_arr_r2z, cfg->growth_v_arr, cfg->ihub_arr};
+    for (int t = 0; t < 4; t++) memcpy(hd.data() + (size_t)t * na, bgd[t], na * sizeof(double));
+    for (int p = 0; p < cfg->n_srcs; p++) {
+      memcpy(hd.data() + (size_t)(4 + 2 * p) * na, cfg->srcs_nz_arr[p], na * sizeof(double));
+      memcpy(hd.data() + (size_t)(5 + 2 * p) * na, cfg->srcs_bz_arr[p], na * sizeof(double));
+    }
+    for (int p = 0; p < cfg->n_imap; p++) {
+      memcpy(hd.data() + (size_t)(4 + 2 * cfg->n_srcs + 2 * p) * na, cfg->imap_tz_arr[p], na * sizeof(double));
+      memcpy(hd.data() + (size_t)(5 + 2 * cfg->n_srcs + 2 * p) * na, cfg->imap_bz_arr[p], na * sizeof(double));
+    }
+    if (int rc = dalloc(c, &c->d_tabs64, hd.size())) return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_tabs64, hd.data(), hd.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                c->stream));
+    const int N = cfg->n_grid;
+    const double dx = cfg->l_box / N;
+    std::vector<float> cr((size_t)3 * N);
+    for (int k3 = 0; k3 < 3; k3++)
+      for (int i = 0; i < N; i++) cr[(size_t)k3 * N + i] = (float)cgx_coord(i, dx, cfg->pos_obs[k3]);
+    if (int rc = dalloc(c, &c->d_corner, cr.size())) return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_corner, cr.data(), cr.size() * sizeof(float), cudaMemcpyHostToDevice,
+                                c->stream));
+    if (nnorm > 0) {
+      std::vector<double> ones((size_t)nnorm * nas, 1.0);
+      if (int rc = dalloc(c, &c->d_norm64, ones.size())) return rc;
+      CUDA_TRY(c, cudaMemcpyAsync(c->d_norm64, ones.data(), ones.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                  c->stream));
+    }
+    if (!c->d_xstats) {
+      if (int rc = dalloc(c, &c->d_xstats, (size_t)4)) return rc;
+      CUDA_TRY(c, cudaMemsetAsync(c->d_xstats, 0, 4 * sizeof(unsigned long long), c->stream));
+    }
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host staging vectors */
+  }
   /* RING -> NEST table of the base pixels (srcs.c:268-270) */
   if (cfg->n_srcs > 0 && cfg->nside_base <= 1024) {
     const long long nb = 12LL * cfg->nside_base * cfg->nside_base;
@@ -661,7 +708,7 @@ extern "C" void cg_destroy(cg_ctx *c)
     if (q) cudaFree(q);
   for (float *q : c->d_imap_out)
     if (q) cudaFree(q);
-  void *ptrs[] = {c->d_tabs, c->d_norm, c->d_zr, c->d_r2n, c->d_pk, c->d_twN, c->d_twH, c->d_dens, c->d_npot, c->d_disp[0],
+  void *ptrs[] = {c->d_tabs, c->d_norm, c->d_tabs64, c->d_norm64, c->d_corner, c->d_xstats, c->d_zr, c->d_r2n, c->d_pk, c->d_twN, c->d_twH, c->d_dens, c->d_npot, c->d_disp[0],
                   c->d_disp[1], c->d_disp[2], c->d_part, c->d_stats, c->d_s2f, c->d_err, c->d_ncount,
                   c->d_zsum, c->d_bsum, c->d_counts, c->d_bsums, c->d_total, c->d_tmpmap, c->d_kmap,
                   c->d_kfac, c->d_kinv, c->d_kir, c->d_ovf_cell, c->d_ovf_cnt, c->d_ovf_n,
@@ -1040,7 +1087,17 @@ extern "C" int cg_set_norm_tables(cg_ctx *c, const double *srcs_norm, const doub
     h[(size_t)p * nas + na + 1] = (float)e[1];
   }
   CUDA_TRY(c, cudaMemcpyAsync(c->d_norm, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-  CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* h is a local buffer */
+  std::vector<double> hd((size_t)(nts + nti) * nas);
+  for (int p = 0; p < nts + nti; p++) {
+    const double *src = p < nts ? srcs_norm + (size_t)p * na : imap_norm + (size_t)(p - nts) * na;
+    const double *e = p < nts ? srcs_norm_0f + 2 * p : imap_norm_0f + 2 * (p - nts);
+    memcpy(hd.data() + (size_t)p * nas, src, na * sizeof(double));
+    hd[(size_t)p * nas + na] = e[0];
+    hd[(size_t)p * nas + na + 1] = e[1];
+  }
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_norm64, hd.data(), hd.size() * sizeof(double), cudaMemcpyHostToDevice,
+                              c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* h and hd are local buffers */
   for (int p = 0; p < nts + nti; p++) {
     const Tab t = Tab{c->d_norm + (size_t)p * nas, h[(size_t)p * nas + na], h[(size_t)p * nas + na + 1]};
     if (p < nts) c->norm[p] = t;
@@ -1067,7 +1124,7 @@ extern "C" int cg_compute_density_normalization(cg_ctx *c)
   if (nt > 0) {
     ProfScope ps(c, "norm_tables");
     CUDA_TRY(c, cg_norm_tables(c->stream, c->d_ncount, c->d_zsum, c->d_bsum, nz, nt, c->norm_zlast, c->d_zr,
-                               c->d_norm));
+                               c->d_norm, c->d_norm64));
     c->launches++;
   }
   const int nas = CG_NA + 2, nsp = c->cfg.n_imap;
@@ -1119,6 +1176,40 @@ static void srcs_params(cg_ctx *c, int ipop, cg_srcs_params &p)
   p.ipix = c->cat[ipop].ipix;
   p.src = c->cat[ipop].src;
   p.err = c->d_err;
+  /* the exact decisions (cg_exact.h) */
+  const int na = CG_NA, N = c->N, nas = CG_NA + 2;
+  cg_pois_args &a = p.pa;
+  a.r = c->g.r;
+  a.nz = c->nz[ipop].f;
+  a.bz = c->bz[ipop].f;
+  a.norm = c->norm[ipop].f;
+  a.xc = c->d_corner;
+  a.yc = c->d_corner + N;
+  a.zc = c->d_corner + 2 * N;
+  a.idr = c->g.idr;
+  a.r_last = c->g.r_last;
+  a.bz0 = (float)c->cfg.srcs_bz_arr[ipop][0];
+  a.cell_vol = p.cell_vol;
+  a.rlim = p.rlim;
+  a.na = na;
+  a.bias_model = c->cfg.bias_model;
+  cgx_srcs_tabs &x = a.x;
+  x.r = c->d_tabs64;
+  x.nz = c->d_tabs64 + (size_t)(4 + 2 * ipop) * na;
+  x.bz = c->d_tabs64 + (size_t)(5 + 2 * ipop) * na;
+  x.norm = c->d_norm64 + (size_t)ipop * nas;
+  x.idr = c->cfg.glob_idr;
+  x.r_last = c->cfg.r_arr_r2z[na - 1];
+  x.bz0 = c->cfg.srcs_bz_arr[ipop][0];
+  x.dx = dx;
+  x.cell_vol = dx * dx * dx;
+  x.rlim = c->cfg.l_box / 2 + 20.;
+  for (int k = 0; k < 3; k++) x.p[k] = c->cfg.pos_obs[k];
+  x.bias_model = c->cfg.bias_model;
+  p.dx64 = dx;
+  for (int k = 0; k < 3; k++) p.p64[k] = c->cfg.pos_obs[k];
+  p.force_double = c->force_double;
+  p.xstats = c->d_xstats;
 }
 
 /* srcs_set_cartesian for every population: count -> scan -> emit.  With
@@ -2156,6 +2247,40 @@ extern "C" int cg_download_norm(cg_ctx *c, int kind, int ipop, float *tab, float
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   edges[0] = e[0];
   edges[1] = e[1];
+  return CG_OK;
+}
+
+extern "C" int cg_download_norm64(cg_ctx *c, int kind, int ipop, double *tab, double *edges)
+{
+  if (!c || !tab || !edges || !c->d_norm64) return CG_EINVAL;
+  int t = -1;
+  if (kind == 0 && ipop >= 0 && ipop < c->cfg.n_srcs) t = ipop;
+  if (kind == 1 && ipop >= 0 && ipop < c->cfg.n_imap) t = c->cfg.n_srcs + ipop;
+  if (kind == 2 && ipop >= 0 && ipop < c->cfg.n_cstm) t = c->cfg.n_srcs + c->cfg.n_imap + ipop;
+  if (t < 0) return fail(c, CG_EINVAL, "no normalisation table %d/%d", kind, ipop);
+  const double *src = c->d_norm64 + (size_t)t * (CG_NA + 2);
+  CUDA_TRY(c, cudaMemcpyAsync(tab, src, CG_NA * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(edges, src + CG_NA, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return CG_OK;
+}
+
+extern "C" int cg_set_decisions_in_double(cg_ctx *c, int all)
+{
+  if (!c) return CG_EINVAL;
+  graph_free(c); /* a captured graph holds the old setting */
+  c->force_double = all ? 1 : 0;
+  return CG_OK;
+}
+
+extern "C" int cg_exact_stats(cg_ctx *c, unsigned long long *out, int reset)
+{
+  if (!c || !c->d_xstats) return CG_EINVAL;
+  if (out) {
+    CUDA_TRY(c, cudaMemcpyAsync(out, c->d_xstats, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  }
+  if (reset) CUDA_TRY(c, cudaMemsetAsync(c->d_xstats, 0, 4 * sizeof(unsigned long long), c->stream));
   return CG_OK;
 }
 

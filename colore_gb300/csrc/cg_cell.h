@@ -471,11 +471,15 @@ CG_HD float cg_src_offset(float x0, float dx, uint32_t bits)
   return CG_ADD(x0, CG_MUL(dx, CG_SUB(cg_u01f(bits), 0.5f)));
 }
 
-/* ra, dec in degrees from (cos theta, phi), srcs.c:408-409 */
-CG_HD void cg_radec(float cth, float ph, float *ra, float *dec)
+/* ra, dec in degrees of the direction (x, y, z) with azimuth ph in
+ * [0, 2 pi], srcs.c:408-409: ra = RTOD phi and dec = 90 - RTOD theta, with
+ * theta = atan2(sqrt(x^2 + y^2), z) (acos of z/r loses half its digits near
+ * the poles in single precision). */
+CG_HD void cg_radec(float x, float y, float z, float ph, float *ra, float *dec)
 {
   *ra = CG_MUL(57.2957795f, ph);
-  *dec = CG_SUB(90.0f, CG_MUL(57.2957795f, cg_acosf(cth)));
+  const float rho = CG_SQRT(CG_FMA(x, x, CG_MUL(y, y)));
+  *dec = CG_SUB(90.0f, CG_MUL(57.2957795f, cg_atan2f(rho, z)));
 }
 
 /* sub-cell centre c0 + (i + 1/2) dxs, imap.c:212-218 */

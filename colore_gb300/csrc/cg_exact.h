@@ -1,0 +1,623 @@
+/*
+ * cg_exact.h -- integer outputs equal to the reference's double-precision
+ * arithmetic.
+ *
+ * Poisson counts, HEALPix pixel ids, intensity-map shells and hit counts are
+ * decisions: a comparison or a truncation of a value that the reference
+ * computes in double precision (srcs.c:156-183, healpix_extra.c:141-172,
+ * imap.c:179-231).  The kernels compute those values in single precision
+ * together with a bound on their distance to the reference's double value,
+ * and keep the single-precision decision only when the value is farther from
+ * the decision boundary than the bound; otherwise they decide again with the
+ * double-precision restatement below.  The result is the reference
+ * arithmetic's decision in every case, at the cost of single precision for
+ * all but a small fraction of the decisions.
+ *
+ * Part 1 restates the reference's double arithmetic (expression order
+ * included: products and sums associate as in the C source, never
+ * contracted into fused multiply-adds).  On the device the elementary
+ * functions are CUDA's double exp, log, pow, atan2 and fmod; on the host
+ * libm's.  Those two may differ in the last bit, which moves a decision only
+ * when a value falls within ~1e-16 relative of its boundary.
+ *
+ * Part 2 holds the single-precision evaluations and their error bounds.
+ * Bounds are stated for the device's documented accuracies (rsqrt.approx
+ * and rcp.approx: relative error below 2^-22; expf: 2 ulp), which also cover
+ * the host's correctly rounded operations.
+ */
+#ifndef CG_EXACT_H
+#define CG_EXACT_H
+
+#include "cg_cell.h"
+#include "colore_cuda.h"
+
+#if defined(__CUDA_ARCH__)
+#define X_ADD(a, b) __dadd_rn((a), (b))
+#define X_SUB(a, b) __dsub_rn((a), (b))
+#define X_MUL(a, b) __dmul_rn((a), (b))
+#define X_DIV(a, b) __ddiv_rn((a), (b))
+#define X_SQRT(a) __dsqrt_rn((a))
+#else
+#define X_ADD(a, b) ((double)(a) + (double)(b))
+#define X_SUB(a, b) ((double)(a) - (double)(b))
+#define X_MUL(a, b) ((double)(a) * (double)(b))
+#define X_DIV(a, b) ((double)(a) / (double)(b))
+#define X_SQRT(a) sqrt((double)(a))
+#endif
+
+#define CGX_TWOPI 6.283185307179586476925286766559005768394  /* healpix_extra.c:137 */
+#define CGX_INV_HALFPI 0.6366197723675813430755350534900574   /* healpix_extra.c:139 */
+#define CGX_2PI_M (2 * 3.14159265358979323846)                /* 2*M_PI, srcs.c:82 */
+
+/* ======================================================================= */
+/* Part 1: the reference's double-precision arithmetic                     */
+/* ======================================================================= */
+
+/* f_of_r_linear, cosmo.c:30-38. */
+CG_HD double cgx_bg(const double *f, const double *r_arr, double idr, double r_last, double f0, double ff, double r)
+{
+  if (r <= 0) return f0;
+  if (r >= r_last) return ff;
+  const int ir = (int)X_MUL(r, idr);
+  return X_ADD(f[ir], X_MUL(X_MUL(X_SUB(f[ir + 1], f[ir]), X_SUB(r, r_arr[ir])), idr));
+}
+
+/* bias_model, common.h:414-431. */
+CG_HD double cgx_bias(double d, double b, int model)
+{
+  if (d <= -1) return 0;
+  if (model == CG_BIAS_EXPLIN) {
+    if (d < 0) return exp(X_DIV(X_MUL(b, d), X_ADD(1.0, d)));
+    return X_ADD(1.0, X_MUL(b, d));
+  }
+  if (model == CG_BIAS_LIN) {
+    const double v = X_ADD(1.0, X_MUL(b, d));
+    return v > 0 ? v : 0;
+  }
+  return pow(X_ADD(1.0, d), b);
+}
+
+/* Cell corner i*dx - p (srcs.c:159-167, imap.c:184-192). */
+CG_HD double cgx_coord(int i, double dx, double p) { return X_SUB(X_MUL((double)i, dx), p); }
+
+/* sqrt(x*x+y*y+z*z) (srcs.c:168, imap.c:195, cart2sph srcs.c:70). */
+CG_HD double cgx_norm3(double x, double y, double z)
+{
+  return X_SQRT(X_ADD(X_ADD(X_MUL(x, x), X_MUL(y, y)), X_MUL(z, z)));
+}
+
+/* Tables of one source population in double: the background radii, n(r),
+ * b(r) and the normalisation (CG_NA values, then its two edge values). */
+typedef struct {
+  const double *r, *nz, *bz, *norm;
+  double idr, r_last, bz0;
+  double dx, cell_vol, rlim, p[3];
+  int bias_model;
+} cgx_srcs_tabs;
+
+/* lambda = ndens*cell_vol*bias_model(d,b)*dnorm of a cell (srcs.c:163-178);
+ * 0 where the reference draws no deviate (r >= L/2+20 or ndens <= 0). */
+CG_HD double cgx_lambda(const cgx_srcs_tabs *t, int ix, int iy, int iz, float d)
+{
+  const double x0 = cgx_coord(ix, t->dx, t->p[0]), y0 = cgx_coord(iy, t->dx, t->p[1]);
+  const double z0 = cgx_coord(iz, t->dx, t->p[2]);
+  const double r = cgx_norm3(x0, y0, z0);
+  if (!(r < t->rlim)) return 0;
+  const double nd = cgx_bg(t->nz, t->r, t->idr, t->r_last, 0, 0, r);
+  if (!(nd > 0)) return 0;
+  const double b = cgx_bg(t->bz, t->r, t->idr, t->r_last, t->bz0, 1, r);
+  const double dn = cgx_bg(t->norm, t->r, t->idr, t->r_last, t->norm[CG_NA], t->norm[CG_NA + 1], r);
+  return X_MUL(X_MUL(X_MUL(nd, t->cell_vol), cgx_bias((double)d, b, t->bias_model)), dn);
+}
+
+/* The Poisson stream (replacing gsl_ran_poisson, common.c:185-189, whose
+ * MT19937 stream follows the OpenMP thread count): cells 4m..4m+3 take the
+ * four words of one Philox4x32-10 block with counter (m, 0, 0, 0); a cell's
+ * uniform is its word's top 24 bits times 2^-24, exact in float and double.
+ * The PTRS branch draws its pairs from counter (cell, iteration, 1, 0). */
+CG_HD uint32_t cg_pois_word(long long cid, uint32_t k0, uint32_t k1)
+{
+  const unsigned long long m = (unsigned long long)cid >> 2;
+  const cg_u32x4 w = cg_philox4x32_10((uint32_t)m, (uint32_t)(m >> 32), 0u, 0u, k0, k1);
+  return w.v[cid & 3];
+}
+
+/* Poisson deviate with mean lam in double: inversion by sequential search
+ * for lam < 10 with the cell's uniform u; PTRS transformed rejection
+ * (W. Hormann, "The transformed rejection method for generating Poisson
+ * random variables", Insurance: Mathematics and Economics 12 (1993) 39-45)
+ * for lam >= 10, with log k! from lgamma.  Iterations are bounded. */
+CG_HD_COLD int cgx_poisson_ptrs(double lam, long long cid, uint32_t k0, uint32_t k1)
+{
+  const double slam = X_SQRT(lam);
+  const double loglam = log(lam);
+  const double b = X_ADD(X_MUL(2.53, slam), 0.931);
+  const double a = X_ADD(X_MUL(0.02483, b), -0.059);
+  const double invalpha = X_ADD(1.1239, X_DIV(1.1328, X_SUB(b, 3.4)));
+  const double vr = X_SUB(0.9277, X_DIV(3.6224, X_SUB(b, 2.0)));
+  for (uint32_t it = 0; it < 64u; it++) {
+    const cg_u32x4 w = cg_philox4x32_10((uint32_t)cid, (uint32_t)((unsigned long long)cid >> 32), it, 1u, k0, k1);
+    const double U = X_SUB((double)cg_u01f(w.v[0]), 0.5);
+    const double V = (double)cg_u01f(w.v[1]);
+    const double us = X_SUB(0.5, fabs(U));
+    const double kd = floor(X_ADD(X_ADD(X_MUL(X_ADD(X_DIV(X_MUL(2.0, a), us), b), U), lam), 0.43));
+    if (us >= 0.07 && V <= vr) return (int)kd;
+    if (kd < 0 || (us < 0.013 && V > us)) continue;
+    const double lhs = X_ADD(log(V), X_SUB(log(invalpha), log(X_ADD(X_DIV(a, X_MUL(us, us)), b))));
+    const double rhs = X_SUB(X_SUB(X_MUL(kd, loglam), lam), lgamma(X_ADD(kd, 1.0)));
+    if (lhs <= rhs) return (int)kd;
+  }
+  return (int)floor(lam);
+}
+
+CG_HD int cgx_poisson(double lam, double u, long long cid, uint32_t k0, uint32_t k1)
+{
+  if (!(lam > 0)) return 0;
+  if (lam < 10) {
+    double p = exp(-lam), F = p;
+    int k = 0;
+    while (u >= F && k < 200) {
+      k++;
+      p = X_MUL(p, X_DIV(lam, (double)k));
+      F = X_ADD(F, p);
+    }
+    return k;
+  }
+  return cgx_poisson_ptrs(lam, cid, k0, k1);
+}
+
+/* cart2sph, srcs.c:68-85 and imap.c:24-41: the direction normalised by r
+ * before atan2, phi shifted into [0, 2 pi]. */
+CG_HD void cgx_cart2sph(double x, double y, double z, double *r, double *cth, double *phi)
+{
+  *r = cgx_norm3(x, y, z);
+  if (*r == 0) {
+    *cth = 1;
+    *phi = 0;
+    return;
+  }
+  const double xn = X_DIV(x, *r), yn = X_DIV(y, *r);
+  *cth = X_DIV(z, *r);
+  *phi = atan2(yn, xn);
+  if (*phi < 0) *phi = X_ADD(*phi, CGX_2PI_M);
+}
+
+/* he_ang2pix (RING), healpix_extra.c:118-172. */
+CG_HD double cgx_fmodulo(double v1, double v2)
+{
+  if (v1 >= 0) return (v1 < v2) ? v1 : fmod(v1, v2);
+  const double tmp = X_ADD(fmod(v1, v2), v2);
+  return (tmp == v2) ? 0. : tmp;
+}
+
+CG_HD long long cgx_ang2pix(long long nside, double cth, double phi)
+{
+  const double ctha = fabs(cth);
+  const double tt = X_MUL(cgx_fmodulo(phi, CGX_TWOPI), CGX_INV_HALFPI);
+  const double ns = (double)nside;
+  if (ctha <= 2.0 / 3.0) {
+    const double temp1 = X_MUL(ns, X_ADD(0.5, tt));
+    const double temp2 = X_MUL(X_MUL(ns, cth), 0.75);
+    const int jp = (int)X_SUB(temp1, temp2), jm = (int)X_ADD(temp1, temp2);
+    const int ir = (int)nside + 1 + jp - jm;
+    const int kshift = 1 - (ir & 1);
+    int ip = (jp + jm - (int)nside + kshift + 1) / 2;
+    ip %= 4 * (int)nside;
+    if (ip < 0) ip += 4 * (int)nside;
+    return nside * (nside - 1) * 2 + (long long)(ir - 1) * 4 * nside + ip;
+  }
+  const double tp = X_SUB(tt, (double)(int)tt);
+  const double tmp = X_MUL(ns, X_SQRT(X_MUL(3.0, X_SUB(1.0, ctha))));
+  const int jp = (int)X_MUL(tp, tmp), jm = (int)X_MUL(X_SUB(1.0, tp), tmp);
+  const int ir = jp + jm + 1;
+  int ip = (int)X_MUL(tt, (double)ir);
+  ip %= 4 * ir;
+  if (ip < 0) ip += 4 * ir;
+  if (cth > 0) return 2LL * ir * (ir - 1) + ip;
+  return 12 * nside * nside - 2LL * ir * (ir + 1) + ip;
+}
+
+/* vec2pix_ring (chealpix, srcs.c:268) for the base pixels: z = v_z/|v| and
+ * phi = atan2(v_y, v_x) into the same RING pixelisation. */
+CG_HD long long cgx_vec2pix_ring(long long nside, double x, double y, double z)
+{
+  const double vlen = cgx_norm3(x, y, z);
+  return cgx_ang2pix(nside, X_DIV(z, vlen), atan2(y, x));
+}
+
+/* Source position component x0 + dx (u - 1/2) in double, stored as float
+ * (srcs.c:261-263). */
+CG_HD float cgx_src_offset(double x0, double dx, uint32_t bits)
+{
+  return (float)X_ADD(x0, X_MUL(dx, X_SUB((double)cg_u01f(bits), 0.5)));
+}
+
+/* Shell of radius r among contiguous sorted shells (edges b[0..nr], shell i
+ * between b[i] and b[i+1]): the walk of get_r_index_imap (imap.c:76-103)
+ * gives this from any start; -1 below the shells, nr at or beyond them. */
+CG_HD int cgx_shell(const float *b, int nr, double r)
+{
+  if (r < (double)b[0]) return -1;
+  if (r >= (double)b[nr]) return nr;
+  int lo = 0, hi = nr - 1; /* last i with b[i] <= r */
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if ((double)b[mid] <= r) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+/* ======================================================================= */
+/* Part 2: single precision with error bounds                              */
+/* ======================================================================= */
+
+#define CG_E24 5.9604644775390625e-08f /* 2^-24 */
+#define CG_E22 2.384185791015625e-07f  /* 2^-22 */
+
+/* Fast reciprocal square root and reciprocal: the device's approximate
+ * instructions (relative error below 2^-22), correctly rounded on the host. */
+CG_HD float cg_rsqrt_fast(float x)
+{
+#if defined(__CUDA_ARCH__)
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+#else
+  return 1.0f / sqrtf(x);
+#endif
+}
+
+CG_HD float cg_rcp_fast(float x)
+{
+#if defined(__CUDA_ARCH__)
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+#else
+  return 1.0f / x;
+#endif
+}
+
+CG_HD float cg_fmaxf(float a, float b) { return a > b ? a : b; }
+CG_HD float cg_fminf(float a, float b) { return a < b ? a : b; }
+
+/* Distance of x >= 0 to the nearest integer, and floor(x). */
+CG_HD float cg_int_dist(float x, int *fl)
+{
+  const float f = cg_floorf(x);
+  *fl = (int)f;
+  const float d = CG_SUB(x, f); /* exact: x and f share the exponent range */
+  return d < 0.5f ? d : CG_SUB(1.0f, d);
+}
+
+/* Table lookup f_of_r_linear in single precision with a bound on its
+ * distance to the double lookup of the double table at the double radius.
+ * tf: float table (the double table rounded); ir, t from the float radius;
+ * dt bounds |t - t_double| in units of one table step.  Near a node the
+ * double radius may fall in the neighbouring segment: the slope bound then
+ * takes the larger of the adjacent segments. */
+typedef struct {
+  float v, e;
+} cg_ve;
+
+CG_HD cg_ve cg_tab_ve(const float *tf, int na, int ir, float t, float dt)
+{
+  const float fi = tf[ir], fj = tf[ir + 1];
+  const float df = CG_SUB(fj, fi);
+  cg_ve o;
+  o.v = CG_FMA(df, t, fi);
+  float sl = cg_fabsf(df);
+  if (t < dt && ir > 0) sl = cg_fmaxf(sl, cg_fabsf(CG_SUB(fi, tf[ir - 1])));
+  if (t > 1.0f - dt && ir + 2 < na) sl = cg_fmaxf(sl, cg_fabsf(CG_SUB(tf[ir + 2], fj)));
+  const float mag = cg_fmaxf(cg_fabsf(fi), cg_fabsf(fj));
+  /* table roundings (2 x 2^-24 of the nodes), the slope times the radius
+   * error, the subtraction and the fused multiply-add (2 x 2^-24), with a
+   * factor 2 to spare */
+  o.e = CG_MUL(2.0f, CG_FMA(sl, CG_ADD(dt, CG_E24), CG_MUL(4.0f * CG_E24, CG_ADD(mag, cg_fabsf(o.v)))));
+  return o;
+}
+
+/* bias_model in single precision, value and absolute error bound given an
+ * absolute error eb on b (d is exact: the same float on both sides). */
+CG_HD cg_ve cg_bias_ve(float d, float b, float eb, int model)
+{
+  cg_ve o;
+  o.v = 0.0f;
+  o.e = 0.0f;
+  if (d <= -1.0f) return o;
+  if (model == CG_BIAS_EXPLIN && d < 0.0f) {
+    const float q = CG_DIV(d, CG_ADD(1.0f, d)); /* d/(1+d), relative error 2^-23 */
+    const float e = CG_MUL(b, q);
+    o.v = expf(e);
+    /* exponent error |q| eb + |e| 2^-22; expf 2 ulp; then e^x scaling */
+    const float ee = CG_FMA(cg_fabsf(q), eb, CG_MUL(cg_fabsf(e), CG_E22));
+    o.e = CG_MUL(o.v, CG_ADD(CG_MUL(2.0f, ee), 8.0f * CG_E24));
+    return o;
+  }
+  if (model == CG_BIAS_EXPLIN || model == CG_BIAS_LIN) {
+    float v = CG_FMA(b, d, 1.0f);
+    const float ev = CG_FMA(cg_fabsf(d), eb, CG_MUL(2.0f * CG_E24, cg_fabsf(v) + 1.0f));
+    if (model == CG_BIAS_LIN && v <= 0.0f) v = 0.0f;
+    o.v = v;
+    o.e = CG_MUL(2.0f, ev);
+    return o;
+  }
+  /* (1+d)^b = exp(b log1p(d)) */
+  const float l = cg_log1pf(d); /* within 4 ulp */
+  const float e = CG_MUL(b, l);
+  o.v = expf(e);
+  const float ee = CG_FMA(cg_fabsf(l), eb, CG_MUL(cg_fabsf(e), 6.0f * CG_E24));
+  o.e = CG_MUL(o.v, CG_ADD(CG_MUL(2.0f, ee), 8.0f * CG_E24));
+  return o;
+}
+
+/* Poisson inversion in single precision for lam < 10 with a proof that the
+ * double inversion at a mean within elam of lam gives the same count:
+ * returns the count, or -1 when u lies too close to a cumulative value.
+ * dF_j/dlam = -p_j(lam), and p_j <= 1/sqrt(2 pi j) for j >= 1 (Stirling),
+ * p_0 <= 1; the float recursion is within (3j+5) 2^-24 of F_j(lam). */
+CG_HD int cg_poisson_inv_checked(float lam, float elam, float u)
+{
+  float p = expf(-lam), F = p;
+  float Fp = 0.0f;
+  int k = 0;
+  while (u >= F && k < 64) {
+    k++;
+    p = CG_MUL(p, CG_DIV(lam, (float)k));
+    Fp = F;
+    F = CG_ADD(F, p);
+  }
+  if (k >= 64) return -1;
+  /* margins of the two cumulative values that bracket u */
+  const float pk = k == 0 ? 1.0f : CG_MUL(0.4f, cg_rsqrt_fast((float)k));
+  const float mk = CG_MUL(1.25f, CG_FMA(elam, pk, (float)(3 * k + 6) * CG_E24));
+  if (!(CG_SUB(F, u) > mk)) return -1;
+  if (k > 0) {
+    const float pj = k == 1 ? 1.0f : CG_MUL(0.4f, cg_rsqrt_fast((float)(k - 1)));
+    const float mj = CG_MUL(1.25f, CG_FMA(elam, pj, (float)(3 * k + 3) * CG_E24));
+    if (!(CG_SUB(u, Fp) > mj)) return -1;
+  }
+  return k;
+}
+
+/* ---- RING pixel with a margin ----------------------------------------- */
+
+/* Direction of (x, y, z) in the form the pixel decisions need: cos(theta),
+ * the quadrant q and fraction f of tt = phi / (pi/2) = q + f, rho^2 =
+ * x^2 + y^2 and 1/r, with error bounds ecth and ef given a relative error
+ * ein of the coordinates (0 when the float position is the reference's).
+ * f is formed from the octant-reduced atan of min/max, so that it carries
+ * absolute, not relative-to-2pi, rounding. */
+typedef struct {
+  float cth, f, rho2, rinv, ecth, ef;
+  int q;
+} cg_dir;
+
+CG_HD cg_dir cg_dir_of(float x, float y, float z, float ein)
+{
+  cg_dir o;
+  o.rho2 = CG_FMA(x, x, CG_MUL(y, y));
+  const float r2 = CG_FMA(z, z, o.rho2);
+  o.rinv = cg_rsqrt_fast(r2);
+  o.cth = CG_MUL(z, o.rinv);
+  const float ax = cg_fabsf(x), ay = cg_fabsf(y);
+  const float mx = cg_fmaxf(ax, ay), mn = cg_fminf(ax, ay);
+  const float t = mx > 0.0f ? CG_MUL(mn, cg_rcp_fast(mx)) : 0.0f;
+  const float th = cg_atan01(t); /* atan(t) in [0, pi/4] */
+  float g = CG_MUL(th, 0.636619772367581343f);
+  if (ay > ax) g = CG_SUB(1.0f, g); /* atan(ay/ax) / (pi/2) */
+  /* quadrant: phi in [0, pi/2) for x > 0, y >= 0; atan2(0, 0) = 0 */
+  int q;
+  float f;
+  if (x > 0.0f && y >= 0.0f) {
+    q = 0;
+    f = g;
+  } else if (x <= 0.0f && y > 0.0f) {
+    q = 1;
+    f = CG_SUB(1.0f, g);
+  } else if (x < 0.0f && y <= 0.0f) {
+    q = 2;
+    f = g;
+  } else if (x >= 0.0f && y < 0.0f) {
+    q = 3;
+    f = CG_SUB(1.0f, g);
+  } else {
+    q = 0;
+    f = 0.0f;
+  }
+  if (f >= 1.0f) {
+    f = CG_SUB(f, 1.0f);
+    q = (q + 1) & 3;
+  }
+  o.q = q;
+  o.f = f;
+  /* cos(theta): r^2 (2 roundings), rsqrt (2^-22), product (2^-24); the
+   * inputs' error ein (relative to r) moves cos(theta) by at most 2 ein */
+  o.ecth = CG_FMA(cg_fabsf(o.cth), 8.0f * CG_E24, CG_MUL(2.0f, ein));
+  /* f: atan01 within 1.3 ulp of atan on [0,1] (below 1e-7 absolute); the
+   * ratio's relative error 2^-22 moves atan by at most that times
+   * t/(1+t^2) <= 1/2; the roundings of g and f: 2.4e-7 in all, doubled.  The
+   * inputs' share, which depends on 1/sin(theta), is added by
+   * cg_pix_checked. */
+  o.ef = 4.5e-7f;
+  return o;
+}
+
+/* RING pixel of a direction at nside (a power of two), or -1 when a decision
+ * lies within its error bound of the boundary.  ein bounds the distance of
+ * the float coordinates to the reference's double ones relative to r (0 when
+ * they are the same floats); cg_dir_of was given the same ein. */
+CG_HD long long cg_pix_checked(const cg_dir *d, int nside, float ein)
+{
+  const float ns = (float)nside;
+  const float ctha = cg_fabsf(d->cth);
+  const float c23 = 0.666666686534881592f; /* float(2/3) = 2/3 + 1.99e-8 */
+  /* region: ctha <= 2/3 in double; the float constant is 2e-8 above 2/3 */
+  if (cg_fabsf(CG_SUB(ctha, c23)) <= CG_ADD(d->ecth, 4.0e-8f)) return -1;
+  if (ctha < c23) {
+    /* phi error from the inputs: sqrt(2) ein / sin(theta) with
+     * sin(theta) >= sqrt(5)/3 here, times 2/pi */
+    const float ef = CG_FMA(1.21f, ein, d->ef);
+    /* temp1 -+ temp2 = ns (q + 0.5 + f -+ 0.75 cth): the integer ns q is
+     * split off and ns v is exact (ns a power of two) */
+    const float va = CG_FMA(-0.75f, d->cth, CG_ADD(0.5f, d->f));
+    const float vb = CG_FMA(0.75f, d->cth, CG_ADD(0.5f, d->f));
+    const float ev = CG_MUL(ns, CG_FMA(0.75f, d->ecth, CG_ADD(ef, 3.0f * CG_E24 * 2.25f)));
+    int ja, jb;
+    const float da = cg_int_dist(CG_MUL(ns, va), &ja);
+    const float db = cg_int_dist(CG_MUL(ns, vb), &jb);
+    if (!(da > CG_ADD(ev, 1e-9f)) || !(db > CG_ADD(ev, 1e-9f))) return -1;
+    const int jp = nside * d->q + ja, jm = nside * d->q + jb;
+    const int ir = nside + 1 + jp - jm;
+    const int kshift = 1 - (ir & 1);
+    int ip = (jp + jm - nside + kshift + 1) >> 1;
+    const int m = 4 * nside;
+    ip %= m;
+    return (long long)nside * (nside - 1) * 2 + (long long)(ir - 1) * 4 * nside + ip;
+  }
+  /* polar caps: tmp = ns sqrt(3 (1 - |cth|)) with 1 - |cth| = rho^2 /
+   * (r (r + |z|)), free of the cancellation near the poles */
+  if (!(d->rho2 > 0.0f)) return -1; /* on the polar axis */
+  const float rho = CG_MUL(d->rho2, cg_rsqrt_fast(d->rho2));
+  const float sth = CG_MUL(rho, d->rinv); /* sin(theta), relative error 2^-21 */
+  if (!(sth > 1e-20f)) return -1;
+  /* 1 - |cth| = sin^2(theta) / (1 + |cth|) */
+  const float s = CG_MUL(sth, CG_MUL(1.7320508075688772f, cg_rsqrt_fast(CG_ADD(1.0f, ctha))));
+  const float tmp = CG_MUL(ns, s);
+  /* relative error of s: rho (2^-22 + 2^-24), rinv 2^-22, |cth| through
+   * 1/sqrt(1+|cth|) by ecth/2, rsqrt 2^-22, three products; the inputs move
+   * sin(theta) by at most 2 ein, relatively 2 ein / sin(theta) */
+  const float isth = cg_rcp_fast(sth);
+  const float es = CG_MUL(tmp, CG_FMA(0.5f, d->ecth, CG_FMA(2.0f * ein, isth, 20.0f * CG_E24)));
+  /* phi: the inputs move it by at most sqrt(2) ein / sin(theta) */
+  const float ef = CG_FMA(0.91f * ein, isth, d->ef);
+  const float tp = d->f;
+  const float p1 = CG_MUL(tp, tmp), p2 = CG_MUL(CG_SUB(1.0f, tp), tmp);
+  const float e1 = CG_FMA(tmp, ef, CG_FMA(tp, es, CG_MUL(2.0f * CG_E24, CG_ADD(p1, 1.0f))));
+  const float e2 = CG_FMA(tmp, CG_ADD(ef, CG_E24), CG_FMA(CG_SUB(1.0f, tp), es, CG_MUL(2.0f * CG_E24, CG_ADD(p2, 1.0f))));
+  int jp, jm;
+  const float d1 = cg_int_dist(p1, &jp), d2 = cg_int_dist(p2, &jm);
+  if (!(d1 > CG_ADD(e1, 1e-9f)) || !(d2 > CG_ADD(e2, 1e-9f))) return -1;
+  const int ir = jp + jm + 1;
+  int ipf;
+  const float p3 = CG_MUL(d->f, (float)ir);
+  const float d3 = cg_int_dist(p3, &ipf);
+  if (!(d3 > CG_ADD(CG_FMA((float)ir, ef, CG_MUL(2.0f * CG_E24, CG_ADD(p3, 1.0f))), 1e-9f))) return -1;
+  int ip = d->q * ir + ipf;
+  const int m = 4 * ir;
+  if (ip >= m) ip -= m;
+  if (d->cth > 0.0f) return 2LL * ir * (ir - 1) + ip;
+  return 12LL * nside * nside - 2LL * ir * (ir + 1) + ip;
+}
+
+/* ---- Poisson counts (srcs.c:156-183) ------------------------------------ */
+
+/* Everything a cell's count needs: the float tables with the float corners
+ * (each the double corner i*dx - p rounded once), and the double tables. */
+typedef struct {
+  const float *r, *nz, *bz, *norm; /* norm: CG_NA values, then the two edges */
+  const float *xc, *yc, *zc;       /* cell corners per axis */
+  float idr, r_last, bz0, cell_vol, rlim;
+  int na, bias_model;
+  cgx_srcs_tabs x;
+} cg_pois_args;
+
+/* lambda of cell (ix, iy, iz) in single precision with a bound *elam on its
+ * distance to cgx_lambda: returns 0 when the double lambda is 0, 1 when
+ * (*lam, *elam) hold and lambda < 10 (inversion), 2 when only the double
+ * computation can decide. */
+CG_HD int cg_lambda_checked(const cg_pois_args *a, int ix, int iy, int iz, float d, float *lam, float *elam)
+{
+  *lam = 0.0f;
+  *elam = 0.0f;
+  const float x = a->xc[ix], y = a->yc[iy], z = a->zc[iz];
+  const float r2 = CG_FMA(z, z, CG_FMA(y, y, CG_MUL(x, x)));
+  const float r = r2 > 0.0f ? CG_MUL(r2, cg_rsqrt_fast(r2)) : 0.0f;
+  /* corners rounded once (2^-24 each), r^2 (3 roundings), rsqrt, product */
+  const float er = CG_MUL(r, 8.0f * CG_E24);
+  if (cg_fabsf(CG_SUB(r, a->rlim)) <= CG_FMA(a->rlim, CG_E24, er)) return 2;
+  if (!(r < a->rlim)) return 0;
+  cg_ve nd, b, dn;
+  if (r > 0.0f) {
+    if (!(r < a->r_last) || cg_fabsf(CG_SUB(r, a->r_last)) <= er) return 2;
+    const int ir = (int)CG_MUL(r, a->idr);
+    const float t = CG_MUL(CG_SUB(r, a->r[ir]), a->idr);
+    /* t against the double t: the radius, the float node radius, the
+     * subtraction and the product */
+    const float dt = CG_FMA(CG_FMA(r, CG_E24, er), a->idr, 4.0f * CG_E24);
+    nd = cg_tab_ve(a->nz, a->na, ir, t, dt);
+    b = cg_tab_ve(a->bz, a->na, ir, t, dt);
+    dn = cg_tab_ve(a->norm, a->na, ir, t, dt);
+  } else { /* the observer's cell: the edge values below r = 0 */
+    nd.v = 0.0f;
+    nd.e = 0.0f;
+    b.v = a->bz0;
+    b.e = CG_MUL(cg_fabsf(a->bz0), 2.0f * CG_E24);
+    dn.v = a->norm[a->na];
+    dn.e = CG_MUL(cg_fabsf(dn.v), 2.0f * CG_E24);
+  }
+  if (!(nd.v > nd.e)) return nd.e == 0.0f ? 0 : 2; /* ndens > 0 (srcs.c:171) */
+  const cg_ve bm = cg_bias_ve(d, b.v, b.e, a->bias_model);
+  const float nc = CG_MUL(nd.v, a->cell_vol);
+  const float l = CG_MUL(CG_MUL(nc, bm.v), dn.v);
+  const float bmh = CG_ADD(bm.v, bm.e), dnh = CG_ADD(dn.v, dn.e);
+  /* |d lambda| <= cv (e_nd bm dn + nd e_bm dn + nd bm e_dn) to first order
+   * (the hatted factors keep the second order), plus the cell volume's and
+   * the three products' roundings */
+  float e = CG_MUL(CG_MUL(nd.e, bmh), dnh);
+  e = CG_FMA(CG_MUL(nd.v, bm.e), dnh, e);
+  e = CG_FMA(CG_MUL(nd.v, bm.v), dn.e, e);
+  e = CG_FMA(CG_MUL(1.01f, a->cell_vol), e, CG_MUL(l, 8.0f * CG_E24));
+  *lam = l;
+  *elam = e;
+  if (!(l > 0.0f)) return e == 0.0f ? 0 : 2;
+  if (!(CG_ADD(l, e) < 10.0f)) return 2; /* PTRS, or too close to the switch */
+  return 1;
+}
+
+/* The count of one cell given its Poisson word w: single precision when its
+ * margins hold, the double restatement otherwise (*fb set to 1). */
+CG_HD int cg_count_cell(const cg_pois_args *a, int ix, int iy, int iz, float d, long long cid, uint32_t w,
+                        uint32_t k0, uint32_t k1, int *fb)
+{
+  float lam, elam;
+  int st = cg_lambda_checked(a, ix, iy, iz, d, &lam, &elam);
+  *fb = 0;
+  if (st == 0) return 0;
+  if (st == 1) {
+    const int n = cg_poisson_inv_checked(lam, elam, cg_u01f(w));
+    if (n >= 0) return n;
+  }
+  *fb = 1;
+  return cgx_poisson(cgx_lambda(&a->x, ix, iy, iz, d), (double)cg_u01f(w), cid, k0, k1);
+}
+
+/* ---- source pixels (srcs.c:268-270 and the count map) ---------------------
+ * The base pixel is vec2pix_ring of the source's float position, the count
+ * map's pixel he_ang2pix of that position's (cos theta, phi) from cart2sph:
+ * both the reference's double arithmetic, decided in single precision where
+ * the margins allow (*fb counts the double decisions). */
+CG_HD void cg_src_pixels(float px, float py, float pz, int nside_base, int nside_count, long long *pix_base,
+                         long long *pix_count, int *fb)
+{
+  const cg_dir dr = cg_dir_of(px, py, pz, 0.0f);
+  long long pb = cg_pix_checked(&dr, nside_base, 0.0f);
+  if (pb < 0) {
+    pb = cgx_vec2pix_ring(nside_base, (double)px, (double)py, (double)pz);
+    (*fb)++;
+  }
+  *pix_base = pb;
+  if (nside_count > 0) {
+    long long pc = cg_pix_checked(&dr, nside_count, 0.0f);
+    if (pc < 0) {
+      double r, cth, ph;
+      cgx_cart2sph((double)px, (double)py, (double)pz, &r, &cth, &ph);
+      pc = cgx_ang2pix(nside_count, cth, ph);
+      (*fb)++;
+    }
+    *pix_count = pc;
+  }
+}
+
+#endif /* CG_EXACT_H */

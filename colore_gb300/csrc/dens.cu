@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(256) k_lpt_deposit(int *grid, const float *__r
 __global__ void __launch_bounds__(256) k_norm_tables(const unsigned long long *__restrict__ ncount,
                                                      const double *__restrict__ zsum,
                                                      const double *__restrict__ bsum, int nz, double zlast,
-                                                     const double *__restrict__ zr, float *out)
+                                                     const double *__restrict__ zr, float *out, double *out64)
 {
   extern __shared__ double nsh[];
   double *zz = nsh, *y = nsh + nz;
@@ -336,6 +336,7 @@ __global__ void __launch_bounds__(256) k_norm_tables(const unsigned long long *_
   }
   __syncthreads();
   float *o = out + (size_t)t * (CG_NA + 2);
+  double *o64 = out64 ? out64 + (size_t)t * (CG_NA + 2) : nullptr;
   for (int i = threadIdx.x; i < CG_NA; i += blockDim.x) {
     const double z = zr[i];
     double nm;
@@ -353,10 +354,15 @@ __global__ void __launch_bounds__(256) k_norm_tables(const unsigned long long *_
       nm = __dadd_rn(y[lo], __ddiv_rn(__dmul_rn(__dsub_rn(z, zz[lo]), __dsub_rn(y[hi], y[lo])), __dsub_rn(zz[hi], zz[lo])));
     }
     o[i] = (float)nm;
+    if (o64) o64[i] = nm;
   }
   if (threadIdx.x == 0) {
     o[CG_NA] = (float)y[0];
     o[CG_NA + 1] = (float)y[nz - 1];
+    if (o64) {
+      o64[CG_NA] = y[0];
+      o64[CG_NA + 1] = y[nz - 1];
+    }
   }
 }
 
@@ -390,7 +396,7 @@ cudaError_t cg_lpt2_source(cudaStream_t s, const float *xx, const float *xy, con
 }
 
 cudaError_t cg_norm_tables(cudaStream_t s, const unsigned long long *ncount, const double *zsum, const double *bsum,
-                           int nz, int nt, double zlast, const double *zr, float *out)
+                           int nz, int nt, double zlast, const double *zr, float *out, double *out64)
 {
   if (nz < 2 || nz > CG_NORM_NZ_MAX || nt < 1) return cudaErrorInvalidValue;
   const size_t smem = 2 * sizeof(double) * (size_t)nz;
@@ -406,7 +412,7 @@ cudaError_t cg_norm_tables(cudaStream_t s, const unsigned long long *ncount, con
       set[dev] = true;
     }
   }
-  k_norm_tables<<<nt, 256, smem, s>>>(ncount, zsum, bsum, nz, zlast, zr, out);
+  k_norm_tables<<<nt, 256, smem, s>>>(ncount, zsum, bsum, nz, zlast, zr, out, out64);
   return cudaGetLastError();
 }
 

@@ -47,12 +47,13 @@ int cg_dens_bins_max_tracers(void);
 /* Normalisation tables from the bin sums, on the device (the host part of
  * compute_density_normalization, density.c:1272-1355, in the same double
  * operations): per tracer t, out[t (CG_NA + 2) + i] = norm(z(r_i)) for the
- * CG_NA table radii, then the two edge values.  zr: z(r_i) (CG_NA doubles);
- * zlast: z(L/2).  nz <= CG_NORM_NZ_MAX. */
+ * CG_NA table radii, then the two edge values, and the same in double into
+ * out64 (or NULL).  zr: z(r_i) (CG_NA doubles); zlast: z(L/2).
+ * nz <= CG_NORM_NZ_MAX. */
 #define CG_NORM_NZ_MAX 3072
 #define CG_MAX_DEVICES 64
 cudaError_t cg_norm_tables(cudaStream_t s, const unsigned long long *ncount, const double *zsum, const double *bsum,
-                           int nz, int nt, double zlast, const double *zr, float *out);
+                           int nz, int nt, double zlast, const double *zr, float *out, double *out64);
 
 /* Largest number of redshift bins of the allocation-free bins entry, whose
  * scratch (per bin: cell count, redshift sum and one bias sum per tracer,

@@ -47,17 +47,6 @@ __device__ __forceinline__ void cell_of(long long c, const Box &b, int &ix, int 
   iz = (int)z;
 }
 
-__device__ __forceinline__ float pois_lambda(const cg_srcs_params &p, float d, float r)
-{
-  if (!(r < p.rlim)) return 0.0f;
-  const BgAt at = bg_at(p.g, r);
-  float nd = bgv(p.nz, at);
-  if (!(nd > 0.0f)) return 0.0f;
-  float b = bgv(p.bz, at);
-  float dn = bgvn(p.norm, at);
-  return cg_src_lambda(nd, p.cell_vol, d, b, dn, p.bias_model);
-}
-
 /* True count of a cell whose stored count is the escape value. */
 __device__ __forceinline__ int ovf_lookup(const cg_srcs_params &p, long long cid)
 {
@@ -68,36 +57,65 @@ __device__ __forceinline__ int ovf_lookup(const cg_srcs_params &p, long long cid
   return CG_COUNT_ESC;
 }
 
-/* Counts of CPT consecutive cells of one row per thread.  The cell loop is
- * not unrolled and the PTRS branch of the sampler is out of line, so the
- * loop stays small in the instruction cache (unrolled, the loop ran
- * instruction-fetch bound where the mean count per cell is a few); the
- * counts are packed in two 64-bit registers.  Each warp adds its total to
- * the block's entry (zeroed before the launch), so warps that finish early
- * do not wait for the block's slowest. */
+/* The count of a cell that the float margins leave open: the reference's
+ * double arithmetic (out of line: rare, and long). */
+__device__ __noinline__ int count_double(const cg_srcs_params &p, int ix, int iy, int iz, float d, long long cid,
+                                         uint32_t w)
+{
+  const double lam = cgx_lambda(&p.pa.x, ix, iy, iz, d);
+  if (lam > 1073741824.0) {
+    atomicOr(p.err, ERR_COUNT_OVERFLOW);
+    return 0;
+  }
+  return cgx_poisson(lam, (double)cg_u01f(w), cid, p.kp0, p.kp1);
+}
+
+/* Counts of CPT consecutive cells of one row per thread.  Each cell's lambda
+ * is formed in single precision with a bound on its distance to the
+ * reference's double lambda, and the Poisson inversion keeps its float
+ * count when the uniform lies farther from the bracketing cumulative values
+ * than that bound carries them (cg_exact.h); the other cells -- and every
+ * cell with lambda >= 10, for PTRS -- take the double arithmetic.  Cells
+ * 4m..4m+3 share one Philox block, drawn only when one of them has a
+ * positive lambda.  The cell loop is not unrolled (unrolled, the kernel ran
+ * instruction-fetch bound); the counts are packed in two 64-bit registers.
+ * Each warp adds its total to the block's entry (zeroed before the launch),
+ * so warps that finish early do not wait for the block's slowest. */
 __global__ void __launch_bounds__(SB, 4) k_pois_count(const float *__restrict__ grid, cg_srcs_params p)
 {
   const int N = p.box.N;
   const long long ncell = (long long)N * N * N;
   const long long c0 = (long long)blockIdx.x * CPB + (long long)threadIdx.x * CPT;
   long long tot = 0;
+  unsigned int nfb = 0;
   if (c0 < ncell) {
     int ix, iy, iz;
     cell_of(c0, p.box, ix, iy, iz);
     const float *row = grid + pidx(ix, iy, iz, N);
-    const float y0 = cg_cell_coord(iy, p.box.dx, p.box.p1), z0 = cg_cell_coord(iz, p.box.dx, p.box.p2);
     unsigned long long lo = 0, hi = 0;
+    long long wm = -1; /* the Philox block held in w */
+    cg_u32x4 w;
+    w.v[0] = w.v[1] = w.v[2] = w.v[3] = 0u;
 #pragma unroll 1
     for (int h = 0; h < CPT; h++) {
-      const float x0 = cg_cell_coord(ix + h, p.box.dx, p.box.p0);
-      const float r = cg_norm3(x0, y0, z0);
-      const float lam = pois_lambda(p, __ldg(row + h), r);
-      int n = 0;
       const long long cid = c0 + h;
-      if (lam > 1073741824.0f) {
-        atomicOr(p.err, ERR_COUNT_OVERFLOW);
-      } else if (lam > 0.0f) {
-        n = cg_poisson(lam, p.kp0, p.kp1, (uint32_t)cid, (uint32_t)(cid >> 32));
+      const float d = __ldg(row + h);
+      float lam, elam;
+      int st = cg_lambda_checked(&p.pa, ix + h, iy, iz, d, &lam, &elam);
+      if (p.force_double && st == 1) st = 2;
+      int n = 0;
+      if (st != 0) {
+        if ((cid >> 2) != wm) {
+          wm = cid >> 2;
+          w = cg_philox4x32_10((uint32_t)wm, (uint32_t)((unsigned long long)wm >> 32), 0u, 0u, p.kp0, p.kp1);
+        }
+        const int q = (int)(cid & 3);
+        const uint32_t wq = q == 0 ? w.v[0] : (q == 1 ? w.v[1] : (q == 2 ? w.v[2] : w.v[3]));
+        n = st == 1 ? cg_poisson_inv_checked(lam, elam, cg_u01f(wq)) : -1;
+        if (n < 0) {
+          n = count_double(p, ix + h, iy, iz, d, cid, wq);
+          nfb++;
+        }
       }
       unsigned long long v = (unsigned long long)n;
       if (n >= CG_COUNT_ESC) {
@@ -118,9 +136,14 @@ __global__ void __launch_bounds__(SB, 4) k_pois_count(const float *__restrict__ 
         make_uint4((unsigned)lo, (unsigned)(lo >> 32), (unsigned)hi, (unsigned)(hi >> 32));
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
-  if ((threadIdx.x & 31) == 0 && tot)
-    atomicAdd(reinterpret_cast<unsigned long long *>(&p.block_sums[blockIdx.x]), (unsigned long long)tot);
+  for (int o = 16; o > 0; o >>= 1) {
+    tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    nfb += __shfl_xor_sync(0xffffffffu, nfb, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (tot) atomicAdd(reinterpret_cast<unsigned long long *>(&p.block_sums[blockIdx.x]), (unsigned long long)tot);
+    if (nfb) atomicAdd(p.xstats, (unsigned long long)nfb);
+  }
 }
 
 /* Exclusive scan of n block totals in place; total into *total. */
@@ -161,6 +184,26 @@ __device__ __forceinline__ void grad_phi(const float *__restrict__ phi, int ix, 
   v[0] = CG_SUB(__ldg(&phi[pidx(xh, iy, iz, N)]), __ldg(&phi[pidx(xl, iy, iz, N)]));
   v[1] = CG_SUB(__ldg(&phi[pidx(ix, yh, iz, N)]), __ldg(&phi[pidx(ix, yl, iz, N)]));
   v[2] = CG_SUB(__ldg(&phi[pidx(ix, iy, zh, N)]), __ldg(&phi[pidx(ix, iy, zl, N)]));
+}
+
+/* Base and count-map pixels of a source by the reference's double
+ * arithmetic (vec2pix_ring, srcs.c:268; he_ang2pix of cart2sph); returns the
+ * number of pixels decided here.  Out of line: rare. */
+__device__ __noinline__ unsigned int pixels_double(const cg_srcs_params &p, float px, float py, float pz, long long *pr,
+                                                   long long *pc)
+{
+  unsigned int k = 0;
+  if (*pr < 0) {
+    *pr = cgx_vec2pix_ring(p.nside_base, (double)px, (double)py, (double)pz);
+    k++;
+  }
+  if (p.cmap && *pc < 0) {
+    double r, cth, ph;
+    cgx_cart2sph((double)px, (double)py, (double)pz, &r, &cth, &ph);
+    *pc = cgx_ang2pix(p.nside_count, cth, ph);
+    k++;
+  }
+  return k;
 }
 
 __global__ void __launch_bounds__(SB, 8) k_emit(const float *__restrict__ phi, cg_srcs_params p)
@@ -211,6 +254,7 @@ __global__ void __launch_bounds__(SB, 8) k_emit(const float *__restrict__ phi, c
   const int T = coff[CPB];
   const long long base = p.block_sums[blockIdx.x];
   const float dx = p.box.dx;
+  unsigned int nfb = 0; /* pixels decided in double */
   for (int k = threadIdx.x; k < T; k += SB) {
     /* the cell holding source k: the last cell whose offset is <= k (cells
      * without sources share their successor's offset) */
@@ -237,18 +281,29 @@ __global__ void __launch_bounds__(SB, 8) k_emit(const float *__restrict__ phi, c
     const float rvel = CG_MUL(p.factor_vel, cg_rvel(v[0], v[1], v[2], x0, y0, z0, rr, p.box.idx));
     const float dz_rsd = CG_MUL(rvel, bg(p.v1, p.g, rr));
     cg_u32x4 u = cg_philox4x32_10((uint32_t)cid, (uint32_t)(cid >> 32), (uint32_t)j, 0u, p.kq0, p.kq1);
-    const float px = cg_src_offset(x0, dx, u.v[0]);
-    const float py = cg_src_offset(y0, dx, u.v[1]);
-    const float pz = cg_src_offset(z0, dx, u.v[2]);
+    /* the position in double, stored as float (srcs.c:261-263) */
+    const float px = cgx_src_offset(cgx_coord(ix, p.dx64, p.p64[0]), p.dx64, u.v[0]);
+    const float py = cgx_src_offset(cgx_coord(iy, p.dx64, p.p64[1]), p.dx64, u.v[1]);
+    const float pz = cgx_src_offset(cgx_coord(iz, p.dx64, p.p64[2]), p.dx64, u.v[2]);
     p.pos[id] = make_float4(px, py, pz, dz_rsd);
     float r, cth, ph;
     cg_cart2sph(px, py, pz, &r, &cth, &ph);
-    int64_t pr = cg_ang2pix_ring(p.nside_base, cth, ph);
+    /* the base pixel and the count-map pixel: the reference's double
+     * decisions, in single precision where the margins allow */
+    long long pr = -1, pc = -1;
+    if (!p.force_double) {
+      const cg_dir dr = cg_dir_of(px, py, pz, 0.0f);
+      pr = cg_pix_checked(&dr, (int)p.nside_base, 0.0f);
+      if (p.cmap) pc = cg_pix_checked(&dr, (int)p.nside_count, 0.0f);
+    }
+    if (pr < 0 || (p.cmap && pc < 0)) {
+      nfb += pixels_double(p, px, py, pz, &pr, &pc);
+    }
     /* ring2nest costs several 64-bit divisions; nside_base is small, so its
      * table (built on the host with the same function) replaces them */
     p.ipix[id] = p.base_r2n ? __ldg(p.base_r2n + pr) : (int)cg_ring2nest(p.nside_base, pr);
     float *q = p.src + (size_t)id * 9;
-    cg_radec(cth, ph, &q[0], &q[1]);                              /* ra, dec */
+    cg_radec(px, py, pz, ph, &q[0], &q[1]);                       /* ra, dec */
     q[2] = bg(p.zt, p.g, r);                                      /* z0  */
     q[3] = p.need_beaming ? 0.0f : dz_rsd;                        /* dz_rsd */
     q[4] = p.need_beaming ? 0.0f : -1.0f;                         /* e1  */
@@ -256,8 +311,11 @@ __global__ void __launch_bounds__(SB, 8) k_emit(const float *__restrict__ phi, c
     q[6] = 0.0f;
     q[7] = 0.0f;
     q[8] = 0.0f;
-    if (p.cmap) atomicAdd(&p.cmap[cg_ang2pix_ring(p.nside_count, cth, ph)], 1);
+    if (p.cmap) atomicAdd(&p.cmap[pc], 1);
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) nfb += __shfl_xor_sync(0xffffffffu, nfb, o);
+  if ((threadIdx.x & 31) == 0 && nfb) atomicAdd(p.xstats + 1, (unsigned long long)nfb);
 }
 
 /* Trilinear potential gradient at a point with corner cells i0/i1 and

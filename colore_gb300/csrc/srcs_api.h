@@ -8,6 +8,7 @@
 #include <stdint.h>
 
 #include "cg_dev.cuh"
+#include "cg_exact.h"
 
 struct cg_srcs_params {
   cg::Box box;
@@ -35,6 +36,14 @@ struct cg_srcs_params {
   int *ipix;
   float *src;                /* 9 floats per source (Src) */
   unsigned int *err;
+  /* the count and pixel decisions of the reference's double arithmetic
+   * (cg_exact.h): float and double tables, corners; the double corners of
+   * the emitted positions; every decision in double when force_double;
+   * xstats[0] cells and xstats[1] pixels decided in double */
+  cg_pois_args pa;
+  double dx64, p64[3];
+  int force_double;
+  unsigned long long *xstats;
 };
 
 /* Per-cell counts are stored as uint16; the few cells at or above the escape

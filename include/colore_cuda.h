@@ -293,12 +293,26 @@ int cg_download_skewers(cg_ctx *ctx, int ipop, float *dens, float *vel);
  * src/cosmo.c:78-81).  tab: CG_NA floats; edges: the values
  * below and above the table (norm_*_0 / norm_*_f). */
 int cg_download_norm(cg_ctx *ctx, int kind, int ipop, float *tab, float *edges);
+/* The same table in double, as the double decisions read it
+ * (compute_density_normalization keeps both, density.c:1323-1355). */
+int cg_download_norm64(cg_ctx *ctx, int kind, int ipop, double *tab, double *edges);
 
 /* Per-kernel timing: when on, every launch group is bracketed by CUDA
  * events on the context's stream; cg_kernel_times synchronises, returns the
  * groups in launch order (names ';'-separated, milliseconds) and clears the
  * log. */
 int cg_set_profiling(cg_ctx *ctx, int on);
+
+/* Integer outputs by the reference's double arithmetic (no counterpart in
+ * the reference, which computes in double throughout): Poisson counts,
+ * base and count-map pixels and intensity-map hits are decided in single
+ * precision where a bound on the distance to the double value proves the
+ * decision, and in double otherwise.  With all != 0 every such decision is
+ * taken in double (slow; for checking).  cg_exact_stats reads the numbers of
+ * decisions taken in double since the last reset: [0] cells' counts,
+ * [1] source pixels, [2] intensity-map cells, [3] intensity-map samples. */
+int cg_set_decisions_in_double(cg_ctx *ctx, int all);
+int cg_exact_stats(cg_ctx *ctx, unsigned long long *out4, int reset);
 int cg_kernel_times(cg_ctx *ctx, char *names, size_t names_len, float *ms, int cap, int *n);
 
 /* Launch accounting: number of kernels this context has launched. */

@@ -5,7 +5,7 @@
  */
 #include <stdint.h>
 
-#include "../colore_gb300/csrc/cg_cell.h"
+#include "../colore_gb300/csrc/cg_exact.h"
 
 void or_vec_expf(const float *x, float *y, long n) { for (long i = 0; i < n; i++) y[i] = cg_expf(x[i]); }
 void or_vec_logf(const float *x, float *y, long n) { for (long i = 0; i < n; i++) y[i] = cg_logf(x[i]); }
@@ -51,5 +51,27 @@ void or_shell_index(const float *r0, const float *rf, int nr, const float *r, in
   for (long i = 0; i < n; i++) {
     walk[i] = cg_shell_index(r0, rf, nr, r[i], 0);
     bisect[i] = cg_shell_index0(r0, rfm, nr, r[i]);
+  }
+}
+
+/* RING pixels of float directions by the margin-checked single-precision
+ * path (cg_pix_checked; -1 where it defers to double), with coordinate
+ * error ein relative to r. */
+void or_pix_checked(long nside, const float *xyz, long n, float ein, long long *pix)
+{
+  for (long i = 0; i < n; i++) {
+    const cg_dir d = cg_dir_of(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], ein);
+    pix[i] = cg_pix_checked(&d, (int)nside, ein);
+  }
+}
+
+/* The same decision by the double restatement shared with the kernels
+ * (cgx_cart2sph + cgx_ang2pix). */
+void or_pix_cgx(long nside, const double *xyz, long n, long long *pix)
+{
+  for (long i = 0; i < n; i++) {
+    double r, cth, ph;
+    cgx_cart2sph(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], &r, &cth, &ph);
+    pix[i] = cgx_ang2pix(nside, cth, ph);
   }
 }

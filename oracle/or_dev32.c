@@ -24,7 +24,7 @@
 #include <stdlib.h>
 #include <string.h>
 
-#include "../colore_gb300/csrc/cg_cell.h"
+#include "../colore_gb300/csrc/cg_exact.h"
 #include "oracle.h"
 
 typedef struct {
@@ -161,70 +161,113 @@ static void src_keys(const cg_config *c, int ipop, uint32_t *kp0, uint32_t *kp1,
   *kq1 = (uint32_t)(c->seed >> 32) ^ (CG_STREAM_POS + (uint32_t)ipop);
 }
 
-static int cell_count(const cg_config *cfg, const S32 *s, int ipop, const float *dens, T32 nrm, int ix, int iy,
-                      int iz, float rlim, float cvol, uint32_t kp0, uint32_t kp1)
+/* The arguments of cg_count_cell for population ipop, as the GPU builds
+ * them: float tables and corners, double tables for the decisions that the
+ * float margins leave open.  norm32 / norm64: CG_NA values and two edges. */
+typedef struct {
+  cg_pois_args a;
+  float *corner;
+} PoisArgs;
+
+static void pois_args(PoisArgs *P, const cg_config *cfg, const S32 *s, int ipop, const float *norm32,
+                      const double *norm64)
 {
-  const int N = s->N;
-  float x0 = cg_cell_coord(ix, s->dx, s->p[0]), y0 = cg_cell_coord(iy, s->dx, s->p[1]),
-        z0 = cg_cell_coord(iz, s->dx, s->p[2]);
-  float r = cg_norm3(x0, y0, z0);
-  if (!(r < rlim)) return 0;
-  float nd = bg32(s, s->nz[ipop], r);
-  if (!(nd > 0.0f)) return 0;
-  float lam = cg_src_lambda(nd, cvol, dens[pidx(ix, iy, iz, N)], bg32(s, s->bz[ipop], r), bg32(s, nrm, r),
-                            cfg->bias_model);
-  if (!(lam > 0.0f)) return 0;
-  long long cid = (long long)ix + (long long)N * ((long long)iy + (long long)N * iz);
-  return cg_poisson(lam, kp0, kp1, (uint32_t)cid, (uint32_t)(cid >> 32));
+  cg_pois_args *a = &P->a;
+  const int N = cfg->n_grid;
+  memset(a, 0, sizeof(*a));
+  a->r = s->r;
+  a->nz = s->nz[ipop].f;
+  a->bz = s->bz[ipop].f;
+  a->norm = norm32;
+  a->idr = s->idr;
+  a->r_last = s->r_last;
+  a->bz0 = s->bz[ipop].f0;
+  a->na = CG_NA;
+  a->bias_model = cfg->bias_model;
+  const double dx = cfg->l_box / N;
+  a->cell_vol = (float)(dx * dx * dx);
+  a->rlim = (float)(cfg->l_box / 2 + 20.);
+  P->corner = malloc(3 * (size_t)N * sizeof(float));
+  for (int k = 0; k < 3; k++)
+    for (int i = 0; i < N; i++) P->corner[k * N + i] = (float)cgx_coord(i, dx, cfg->pos_obs[k]);
+  a->xc = P->corner;
+  a->yc = P->corner + N;
+  a->zc = P->corner + 2 * N;
+  cgx_srcs_tabs *x = &a->x;
+  x->r = cfg->r_arr_r2z;
+  x->nz = cfg->srcs_nz_arr[ipop];
+  x->bz = cfg->srcs_bz_arr[ipop];
+  x->norm = norm64;
+  x->idr = cfg->glob_idr;
+  x->r_last = cfg->r_arr_r2z[CG_NA - 1];
+  x->bz0 = cfg->srcs_bz_arr[ipop][0];
+  x->dx = dx;
+  x->cell_vol = dx * dx * dx;
+  x->rlim = cfg->l_box / 2 + 20.;
+  for (int k = 0; k < 3; k++) x->p[k] = cfg->pos_obs[k];
+  x->bias_model = cfg->bias_model;
 }
 
-int or_counts32(const cg_config *cfg, int ipop, const float *dens, const float *normtab, float n0, float nf,
-                int *counts, long long *total)
+/* Counts of population ipop as the GPU computes them (cg_count_cell: float
+ * margins, double decisions where they do not hold); *fallbacks counts the
+ * cells decided in double. */
+int or_counts32(const cg_config *cfg, int ipop, const float *dens, const float *norm32, const double *norm64,
+                int *counts, long long *total, long long *fallbacks)
 {
   S32 s;
   s32_init(&s, cfg);
+  PoisArgs P;
+  pois_args(&P, cfg, &s, ipop, norm32, norm64);
   const int N = s.N;
-  T32 nrm = {normtab, n0, nf};
   uint32_t kp0, kp1, kq0, kq1;
   src_keys(cfg, ipop, &kp0, &kp1, &kq0, &kq1);
-  const float rlim = (float)(cfg->l_box / 2 + 20.);
-  const double dxd = cfg->l_box / N;
-  const float cvol = (float)(dxd * dxd * dxd);
-  long long tot = 0;
-#pragma omp parallel for schedule(static) reduction(+ : tot)
+  long long tot = 0, nfb = 0;
+#pragma omp parallel for schedule(static) reduction(+ : tot, nfb)
   for (int iz = 0; iz < N; iz++)
     for (int iy = 0; iy < N; iy++)
       for (int ix = 0; ix < N; ix++) {
-        int n = cell_count(cfg, &s, ipop, dens, nrm, ix, iy, iz, rlim, cvol, kp0, kp1);
-        if (counts) counts[(size_t)ix + (size_t)N * ((size_t)iy + (size_t)N * iz)] = n;
+        const long long cid = (long long)ix + (long long)N * ((long long)iy + (long long)N * iz);
+        int fb = 0;
+        const int n = cg_count_cell(&P.a, ix, iy, iz, dens[pidx(ix, iy, iz, N)], cid, cg_pois_word(cid, kp0, kp1),
+                                    kp0, kp1, &fb);
+        if (counts) counts[cid] = n;
         tot += n;
+        nfb += fb;
       }
   *total = tot;
+  if (fallbacks) *fallbacks = nfb;
+  free(P.corner);
   s32_free(&s);
   return 0;
 }
 
-int or_emit32(const cg_config *cfg, int ipop, const float *dens, const float *npot, const float *normtab, float n0,
-              float nf, long long cap, float *pos4, int *ipix, float *src9, int *cmap, long long *nsrc)
+/* The catalogue as the GPU writes it: positions in double rounded to float
+ * (the reference's), the base and count-map pixels by cg_src_pixels, the
+ * velocity, RA, Dec and redshift in single precision. */
+int or_emit32(const cg_config *cfg, int ipop, const float *dens, const float *npot, const float *norm32,
+              const double *norm64, long long cap, float *pos4, int *ipix, float *src9, int *cmap, long long *nsrc,
+              long long *fallbacks)
 {
   S32 s;
   s32_init(&s, cfg);
+  PoisArgs P;
+  pois_args(&P, cfg, &s, ipop, norm32, norm64);
   const int N = s.N;
-  T32 nrm = {normtab, n0, nf};
   uint32_t kp0, kp1, kq0, kq1;
   src_keys(cfg, ipop, &kp0, &kp1, &kq0, &kq1);
-  const float rlim = (float)(cfg->l_box / 2 + 20.);
   const double dxd = cfg->l_box / N;
-  const float cvol = (float)(dxd * dxd * dxd);
   const float fvel = (float)(-cfg->fgrowth_0 / (1.5 * cfg->hubble_0 * cfg->omega_m));
-  const int64_t nsb = cfg->nside_base, nsc = cfg->nside_count[ipop];
-  long long id = 0;
+  const int nsb = cfg->nside_base, nsc = cfg->nside_count[ipop];
+  long long id = 0, nfb = 0;
   for (int iz = 0; iz < N; iz++) {
     float z0 = cg_cell_coord(iz, s.dx, s.p[2]);
     for (int iy = 0; iy < N; iy++) {
       float y0 = cg_cell_coord(iy, s.dx, s.p[1]);
       for (int ix = 0; ix < N; ix++) {
-        int n = cell_count(cfg, &s, ipop, dens, nrm, ix, iy, iz, rlim, cvol, kp0, kp1);
+        const long long cid = (long long)ix + (long long)N * ((long long)iy + (long long)N * iz);
+        int fb = 0;
+        const int n = cg_count_cell(&P.a, ix, iy, iz, dens[pidx(ix, iy, iz, N)], cid, cg_pois_word(cid, kp0, kp1),
+                                    kp0, kp1, &fb);
         if (n == 0) continue;
         float x0 = cg_cell_coord(ix, s.dx, s.p[0]);
         float rr = cg_norm3(x0, y0, z0);
@@ -235,40 +278,48 @@ int or_emit32(const cg_config *cfg, int ipop, const float *dens, const float *np
         float v2 = CG_SUB(npot[pidx(ix, iy, zh, N)], npot[pidx(ix, iy, zl, N)]);
         float rvel = CG_MUL(fvel, cg_rvel(v0, v1, v2, x0, y0, z0, rr, s.idx));
         float dz = CG_MUL(rvel, bg32(&s, s.v1, rr));
-        long long cid = (long long)ix + (long long)N * ((long long)iy + (long long)N * iz);
+        const double x0d = cgx_coord(ix, dxd, cfg->pos_obs[0]), y0d = cgx_coord(iy, dxd, cfg->pos_obs[1]);
+        const double z0d = cgx_coord(iz, dxd, cfg->pos_obs[2]);
         for (int j = 0; j < n; j++, id++) {
           if (id >= cap) {
+            free(P.corner);
             s32_free(&s);
             return -1;
           }
           cg_u32x4 u = cg_philox4x32_10((uint32_t)cid, (uint32_t)(cid >> 32), (uint32_t)j, 0u, kq0, kq1);
-          float px = cg_src_offset(x0, s.dx, u.v[0]);
-          float py = cg_src_offset(y0, s.dx, u.v[1]);
-          float pz = cg_src_offset(z0, s.dx, u.v[2]);
+          float px = cgx_src_offset(x0d, dxd, u.v[0]);
+          float py = cgx_src_offset(y0d, dxd, u.v[1]);
+          float pz = cgx_src_offset(z0d, dxd, u.v[2]);
           if (pos4) {
             pos4[4 * id + 0] = px;
             pos4[4 * id + 1] = py;
             pos4[4 * id + 2] = pz;
             pos4[4 * id + 3] = dz;
           }
+          long long pb = 0, pc = 0;
+          int pfb = 0;
+          cg_src_pixels(px, py, pz, nsb, cmap ? nsc : 0, &pb, &pc, &pfb);
+          nfb += pfb;
+          if (ipix) ipix[id] = (int)cg_ring2nest(nsb, pb);
           float r, cth, ph;
           cg_cart2sph(px, py, pz, &r, &cth, &ph);
-          if (ipix) ipix[id] = (int)cg_ring2nest(nsb, cg_ang2pix_ring(nsb, cth, ph));
           if (src9) {
             float *q = src9 + 9 * id;
-            cg_radec(cth, ph, &q[0], &q[1]);
+            cg_radec(px, py, pz, ph, &q[0], &q[1]);
             q[2] = bg32(&s, s.zt, r);
             q[3] = cfg->need_beaming ? 0.0f : dz;
             q[4] = cfg->need_beaming ? 0.0f : -1.0f;
             q[5] = cfg->need_beaming ? 0.0f : -1.0f;
             q[6] = q[7] = q[8] = 0.0f;
           }
-          if (cmap && nsc > 0) cmap[cg_ang2pix_ring(nsc, cth, ph)]++;
+          if (cmap && nsc > 0) cmap[pc]++;
         }
       }
     }
   }
   *nsrc = id;
+  if (fallbacks) *fallbacks = nfb;
+  free(P.corner);
   s32_free(&s);
   return 0;
 }

@@ -450,6 +450,17 @@ static void cart2sph64(double x, double y, double z, double *r, double *cth, dou
   if (*phi < 0) *phi += 2 * M_PI;
 }
 
+/* RING pixel of he_ang2pix after cart2sph (imap.c:210-231, srcs.c:404-409)
+ * for each double direction (independent restatement). */
+void or_pix64(long nside, const double *xyz, long n, long long *pix)
+{
+  for (long i = 0; i < n; i++) {
+    double r, cth, ph;
+    cart2sph64(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], &r, &cth, &ph);
+    pix[i] = ang2pix64(nside, cth, ph);
+  }
+}
+
 static double rvel64(const cg_config *c, const double *p, int ix, int iy, int iz, double x0, double y0, double z0,
                      double rr)
 {
@@ -760,20 +771,150 @@ int or_isw64(const cg_config *c, const double *p, double *map)
   return 0;
 }
 
-/* Poisson deviate by inversion in double from the same Philox cell stream. */
+/* The Poisson stream of the build (gsl_ran_poisson's MT19937 stream cannot
+ * be reproduced): the uniform of cell cid is word cid % 4 of the Philox block
+ * with counter (cid / 4, 0, 0, 0), its top 24 bits times 2^-24; the PTRS
+ * pairs of cell cid come from counter (cid, iteration, 1, 0). */
+static double pois_u(long long cid, uint32_t k0, uint32_t k1)
+{
+  unsigned long long m = (unsigned long long)cid >> 2;
+  cg_u32x4 w = cg_philox4x32_10((uint32_t)m, (uint32_t)(m >> 32), 0u, 0u, k0, k1);
+  return (double)(w.v[cid & 3] >> 8) * 5.9604644775390625e-08;
+}
+
+/* PTRS transformed rejection (Hormann 1993) for lam >= 10, in double. */
+static int ptrs64(double lam, long long cid, uint32_t k0, uint32_t k1)
+{
+  double slam = sqrt(lam), loglam = log(lam);
+  double b = 2.53 * slam + 0.931;
+  double a = 0.02483 * b + -0.059;
+  double invalpha = 1.1239 + 1.1328 / (b - 3.4);
+  double vr = 0.9277 - 3.6224 / (b - 2.0);
+  for (uint32_t it = 0; it < 64u; it++) {
+    cg_u32x4 w = cg_philox4x32_10((uint32_t)cid, (uint32_t)((unsigned long long)cid >> 32), it, 1u, k0, k1);
+    double U = (double)(w.v[0] >> 8) * 5.9604644775390625e-08 - 0.5;
+    double V = (double)(w.v[1] >> 8) * 5.9604644775390625e-08;
+    double us = 0.5 - fabs(U);
+    double kd = floor(((2.0 * a / us + b) * U + lam) + 0.43);
+    if (us >= 0.07 && V <= vr) return (int)kd;
+    if (kd < 0 || (us < 0.013 && V > us)) continue;
+    double lhs = log(V) + (log(invalpha) - log(a / (us * us) + b));
+    double rhs = (kd * loglam - lam) - lgamma(kd + 1.0);
+    if (lhs <= rhs) return (int)kd;
+  }
+  return (int)floor(lam);
+}
+
+/* Poisson deviate in double: inversion by sequential search for lam < 10,
+ * PTRS above. */
 static int poisson64(double lam, uint32_t k0, uint32_t k1, long long cid)
 {
   if (!(lam > 0)) return 0;
-  cg_u32x4 w = cg_philox4x32_10((uint32_t)cid, (uint32_t)(cid >> 32), 0u, 0u, k0, k1);
-  double u = cg_u01d(w.v[0], w.v[1]), p = exp(-lam), F = p;
+  if (lam >= 10) return ptrs64(lam, cid, k0, k1);
+  double u = pois_u(cid, k0, k1), p = exp(-lam), F = p;
   int k = 0;
-  while (u >= F && k < 100000) {
+  while (u >= F && k < 200) {
     k++;
     p *= lam / k;
     F += p;
-    if (p == 0 && F < u) break;
   }
   return k;
+}
+
+/* Counts of every cell of population ipop (srcs_set_cartesian_single pass 1,
+ * srcs.c:156-183) in double from the float density dens (unpadded, as
+ * doubles) and the normalisation table normtab (CG_NA values, then the two
+ * edge values). */
+int or_counts64(const cg_config *c, int ipop, const double *dens, const double *normtab, int *counts,
+                long long *total)
+{
+  const size_t ncell = (size_t)c->n_grid * c->n_grid * c->n_grid;
+  double *lam = malloc(ncell * sizeof(double));
+  if (!lam) return -1;
+  or_lambda64(c, ipop, dens, normtab, normtab[CG_NA], normtab[CG_NA + 1], lam);
+  const uint32_t k0 = (uint32_t)c->seed, k1 = (uint32_t)(c->seed >> 32) ^ (CG_STREAM_POIS + (uint32_t)ipop);
+  long long t = 0;
+#pragma omp parallel for schedule(static) reduction(+ : t)
+  for (size_t i = 0; i < ncell; i++) {
+    int n = poisson64(lam[i], k0, k1, (long long)i);
+    if (counts) counts[i] = n;
+    t += n;
+  }
+  free(lam);
+  *total = t;
+  return 0;
+}
+
+/* The catalogue of population ipop in double (srcs_set_cartesian_single
+ * pass 2, srcs.c:238-276; srcs_get_local_properties_single, srcs.c:386-416):
+ * sources in cell order; pos4 = x, y, z, dz_rsd as the reference's float
+ * CatalogCartesian.pos; ipix the NEST base pixel of vec2pix_ring of the float
+ * position; src9 the Src record (ra, dec, z0, dz_rsd, e1, e2, then 0s); cmap
+ * the count map at nside_count (he_ang2pix of cart2sph of the float
+ * position).  counts: the cell counts (or_counts64).  Returns -1 when more
+ * than cap sources. */
+#define RTOD64 57.2957795 /* RTOD, common.h:124 */
+int or_emit64(const cg_config *c, int ipop, const double *npot, const int *counts, long long cap, float *pos4,
+              int *ipix, float *src9, int *cmap, long long *nsrc)
+{
+  const int N = c->n_grid;
+  const double dx = c->l_box / N, idx = c->n_grid / c->l_box;
+  const double fvel = -c->fgrowth_0 / (1.5 * c->hubble_0 * c->omega_m);
+  const uint32_t kq0 = (uint32_t)c->seed, kq1 = (uint32_t)(c->seed >> 32) ^ (CG_STREAM_POS + (uint32_t)ipop);
+  const long nsb = c->nside_base, nsc = c->nside_count[ipop];
+  long long id = 0;
+  for (int iz = 0; iz < N; iz++) {
+    double z0 = (iz + 0.0) * dx - c->pos_obs[2];
+    for (int iy = 0; iy < N; iy++) {
+      double y0 = (iy + 0.0) * dx - c->pos_obs[1];
+      for (int ix = 0; ix < N; ix++) {
+        size_t cid = ix + (size_t)N * (iy + (size_t)N * iz);
+        int n = counts[cid];
+        if (n <= 0) continue;
+        double x0 = (ix + 0.0) * dx - c->pos_obs[0];
+        double rr = sqrt(x0 * x0 + y0 * y0 + z0 * z0);
+        /* get_rvel (srcs.c:87-118): float differences of the float grid */
+        int xh = (ix + 1) % N, xl = (ix + N - 1) % N, yh = (iy + 1) % N, yl = (iy + N - 1) % N;
+        int zh = (iz + 1) % N, zl = (iz + N - 1) % N;
+#define P(X, Y, Z) npot[(X) + (size_t)N * ((Y) + (size_t)N * (Z))]
+        double v0 = (float)(P(xh, iy, iz) - P(xl, iy, iz)), v1 = (float)(P(ix, yh, iz) - P(ix, yl, iz));
+        double v2 = (float)(P(ix, iy, zh) - P(ix, iy, zl));
+#undef P
+        double u0 = x0 / rr, u1 = y0 / rr, u2 = z0 / rr;
+        double rvel = fvel * (0.5 * idx * (v0 * u0 + v1 * u1 + v2 * u2));
+        double dz_rsd = rvel * BG_V1(c, rr);
+        for (int j = 0; j < n; j++, id++) {
+          if (id >= cap) return -1;
+          cg_u32x4 u = cg_philox4x32_10((uint32_t)cid, (uint32_t)((unsigned long long)cid >> 32), (uint32_t)j, 0u,
+                                        kq0, kq1);
+          float p[4];
+          p[0] = (float)(x0 + dx * ((double)(u.v[0] >> 8) * 5.9604644775390625e-08 - 0.5));
+          p[1] = (float)(y0 + dx * ((double)(u.v[1] >> 8) * 5.9604644775390625e-08 - 0.5));
+          p[2] = (float)(z0 + dx * ((double)(u.v[2] >> 8) * 5.9604644775390625e-08 - 0.5));
+          p[3] = (float)dz_rsd;
+          if (pos4) memcpy(pos4 + 4 * id, p, sizeof(p));
+          double v[3] = {p[0], p[1], p[2]};
+          double vlen = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+          if (ipix) ipix[id] = (int)cg_ring2nest(nsb, ang2pix64(nsb, v[2] / vlen, atan2(v[1], v[0])));
+          double r, cth, ph;
+          cart2sph64(v[0], v[1], v[2], &r, &cth, &ph);
+          if (src9) {
+            float *q = src9 + 9 * id;
+            q[0] = (float)(RTOD64 * ph);
+            q[1] = (float)(90 - RTOD64 * acos(cth));
+            q[2] = (float)BG_Z(c, r);
+            q[3] = c->need_beaming ? 0.0f : p[3];
+            q[4] = c->need_beaming ? 0.0f : -1.0f;
+            q[5] = c->need_beaming ? 0.0f : -1.0f;
+            q[6] = q[7] = q[8] = 0.0f;
+          }
+          if (cmap && nsc > 0) cmap[ang2pix64(nsc, cth, ph)]++;
+        }
+      }
+    }
+  }
+  *nsrc = id;
+  return 0;
 }
 
 long long or_poisson_total64(const cg_config *c, int ipop, const double *lam)

@@ -61,16 +61,29 @@ int or_imap64_part(const cg_config *cfg, int ipop, const double *dens, const dou
 long long or_imap_samples(const cg_config *cfg, int ipop);
 int or_kappa64_part(const cg_config *cfg, const double *npot, int pix_stride, double *map);
 long long or_poisson_total64(const cg_config *cfg, int ipop, const double *lam);
+/* Counts and catalogue in double (srcs.c:156-283, 386-416) from the float
+ * density as doubles (unpadded) and the double normalisation table (CG_NA
+ * values, then the two edges); or_emit64 takes the counts and the potential
+ * (unpadded doubles of the float grid). */
+int or_counts64(const cg_config *cfg, int ipop, const double *dens, const double *normtab, int *counts,
+                long long *total);
+int or_emit64(const cg_config *cfg, int ipop, const double *npot, const int *counts, long long cap, float *pos4,
+              int *ipix, float *src9, int *cmap, long long *nsrc);
 int or_run_mock64(const cg_config *cfg, int nthreads_hint, long long *nsrc_total, double *checksum);
 
 /* ---- dev32 (or_dev32.c) ---- */
 int or_density32(const cg_config *cfg, float *dens, float sigma2f, int mode);
 int or_bins32(const cg_config *cfg, const float *dens, int nz, double idz, unsigned long long *narr, double *zarr,
               double *bsum);
-int or_counts32(const cg_config *cfg, int ipop, const float *dens, const float *normtab, float n0, float nf,
-                int *counts, long long *total);
-int or_emit32(const cg_config *cfg, int ipop, const float *dens, const float *npot, const float *normtab, float n0,
-              float nf, long long cap, float *pos4, int *ipix, float *src9, int *cmap, long long *nsrc);
+/* Source counts and catalogue as the GPU computes them: float margins with
+ * double decisions where they do not hold (cg_exact.h).  norm32 / norm64:
+ * the normalisation table (CG_NA values, then the two edges) in float and
+ * double; *fallbacks: cells (counts) or pixels (emit) decided in double. */
+int or_counts32(const cg_config *cfg, int ipop, const float *dens, const float *norm32, const double *norm64,
+                int *counts, long long *total, long long *fallbacks);
+int or_emit32(const cg_config *cfg, int ipop, const float *dens, const float *npot, const float *norm32,
+              const double *norm64, long long cap, float *pos4, int *ipix, float *src9, int *cmap, long long *nsrc,
+              long long *fallbacks);
 int or_beam_rsd32(const cg_config *cfg, const float *npot, long long n, const float *pos4, float *src9);
 int or_imap32(const cg_config *cfg, int ipop, const float *dens, const float *npot, const float *normtab, float n0,
               float nf, float *data, int *nadd);

@@ -32,8 +32,10 @@ def lib():
             "or_imap64_part": [vp, i, vp, vp, vp, d, d, i, vp, vp, vp], "or_imap_samples": [vp, i],
             "or_kappa64_part": [vp, vp, i, vp], "or_poisson_total64": [vp, i, vp],
             "or_density32": [vp, vp, f, i], "or_bins32": [vp, vp, i, d, vp, vp, vp],
-            "or_counts32": [vp, i, vp, vp, f, f, vp, vp],
-            "or_emit32": [vp, i, vp, vp, vp, f, f, C.c_longlong, vp, vp, vp, vp, vp],
+            "or_counts32": [vp, i, vp, vp, vp, vp, vp, vp],
+            "or_emit32": [vp, i, vp, vp, vp, vp, C.c_longlong, vp, vp, vp, vp, vp, vp],
+            "or_counts64": [vp, i, vp, vp, vp, vp],
+            "or_emit64": [vp, i, vp, vp, C.c_longlong, vp, vp, vp, vp, vp],
             "or_beam_rsd32": [vp, vp, C.c_longlong, vp, vp], "or_imap32": [vp, i, vp, vp, vp, f, f, vp, vp],
             "or_kappa32": [vp, vp, vp], "or_isw32": [vp, vp, vp], "or_isw64": [vp, vp, vp],
             "or_cstm_steps": [vp, i, vp, vp, vp, vp], "or_cstm64": [vp, i, vp, vp, d, d, vp],
@@ -48,9 +50,11 @@ def lib():
             "or_ang2pix": [C.c_long, vp, vp, vp, C.c_long], "or_nest2ring": [C.c_long, vp, vp, C.c_long],
             "or_ring2nest": [C.c_long, vp, vp, C.c_long], "or_pix2vec_nest": [C.c_long, vp, vp, C.c_long],
             "or_shell_index": [vp, vp, i, vp, vp, vp, C.c_long],
+            "or_pix_checked": [C.c_long, vp, C.c_long, f, vp], "or_pix_cgx": [C.c_long, vp, C.c_long, vp],
+            "or_pix64": [C.c_long, vp, C.c_long, vp],
         }
         void = ("or_philox", "or_poisson", "or_ang2pix", "or_nest2ring", "or_ring2nest", "or_pix2vec_nest",
-                "or_shell_index")
+                "or_shell_index", "or_pix_checked", "or_pix_cgx", "or_pix64")
         for k, a in sig.items():
             fn = getattr(L, k)
             fn.argtypes = a
@@ -222,25 +226,72 @@ def bins32(cfg, dens, nz, idz):
     return narr, zarr, bsum[:nt]
 
 
-def counts32(cfg, ipop, dens, tab, e):
+def _norm_pair(tab32, e32, tab64, e64):
+    """The float and double normalisation tables with their edges appended
+    (CG_NA + 2 values each), as the kernels hold them."""
+    t32 = np.concatenate([np.asarray(tab32, np.float32), np.asarray(e32, np.float32)])
+    t64 = np.concatenate([np.asarray(tab64, np.float64), np.asarray(e64, np.float64)])
+    return t32, t64
+
+
+def counts32(cfg, ipop, dens, tab32, e32, tab64, e64):
+    """Counts as the GPU computes them (float margins, double where they do
+    not hold): (counts [N][N][N], total, cells decided in double)."""
     n = cfg.n_grid
     cnt = np.empty((n, n, n), np.int32)
     tot = C.c_longlong()
-    lib().or_counts32(cfgp(cfg), ipop, P(dens), P(tab), float(e[0]), float(e[1]), P(cnt), C.byref(tot))
-    return cnt, tot.value
+    fb = C.c_longlong()
+    t32, t64 = _norm_pair(tab32, e32, tab64, e64)
+    lib().or_counts32(cfgp(cfg), ipop, P(np.ascontiguousarray(dens, np.float32)), P(t32), P(t64), P(cnt),
+                      C.byref(tot), C.byref(fb))
+    return cnt, tot.value, fb.value
 
 
-def emit32(cfg, ipop, dens, npot, tab, e, cap):
+def emit32(cfg, ipop, dens, npot, tab32, e32, tab64, e64, cap):
+    """The catalogue as the GPU writes it; 'fallbacks': pixels decided in
+    double."""
     pos = np.empty((cap, 4), np.float32)
     ipix = np.empty(cap, np.int32)
     src = np.empty((cap, 9), np.float32)
     ns = cfg.nside_count[ipop]
     cmap = np.zeros(12 * ns * ns, np.int32) if ns > 0 else None
     n = C.c_longlong()
-    rc = lib().or_emit32(cfgp(cfg), ipop, P(dens), P(npot), P(tab), float(e[0]), float(e[1]), cap, P(pos), P(ipix),
-                         P(src), P(cmap), C.byref(n))
+    fb = C.c_longlong()
+    t32, t64 = _norm_pair(tab32, e32, tab64, e64)
+    rc = lib().or_emit32(cfgp(cfg), ipop, P(np.ascontiguousarray(dens, np.float32)),
+                         P(np.ascontiguousarray(npot, np.float32)), P(t32), P(t64), cap, P(pos), P(ipix), P(src),
+                         P(cmap), C.byref(n), C.byref(fb))
     assert rc == 0
     k = n.value
+    return dict(pos=pos[:k], ipix=ipix[:k], src=src[:k], cmap=cmap, fallbacks=fb.value)
+
+
+def counts64(cfg, ipop, dens, tab64, e64):
+    """Counts in double (srcs.c:156-183) from the float density (any float
+    grid, padded or not, is read as its N^3 cells): (counts, total)."""
+    n = cfg.n_grid
+    d = np.ascontiguousarray(np.asarray(dens)[:, :, :n], np.float64)
+    cnt = np.empty((n, n, n), np.int32)
+    tot = C.c_longlong()
+    t64 = np.concatenate([np.asarray(tab64, np.float64), np.asarray(e64, np.float64)])
+    assert lib().or_counts64(cfgp(cfg), ipop, P(d), P(t64), P(cnt), C.byref(tot)) == 0
+    return cnt, tot.value
+
+
+def emit64(cfg, ipop, npot, counts, cap):
+    """The catalogue in double (srcs.c:238-276, 386-416) from the counts and
+    the float potential: pos, ipix, src, cmap."""
+    n = cfg.n_grid
+    ph = np.ascontiguousarray(np.asarray(npot)[:, :, :n], np.float64)
+    pos = np.empty((cap, 4), np.float32)
+    ipix = np.empty(cap, np.int32)
+    src = np.empty((cap, 9), np.float32)
+    ns = cfg.nside_count[ipop]
+    cmap = np.zeros(12 * ns * ns, np.int32) if ns > 0 else None
+    k = C.c_longlong()
+    assert lib().or_emit64(cfgp(cfg), ipop, P(ph), P(np.ascontiguousarray(counts, np.int32)), cap, P(pos), P(ipix),
+                           P(src), P(cmap), C.byref(k)) == 0
+    k = k.value
     return dict(pos=pos[:k], ipix=ipix[:k], src=src[:k], cmap=cmap)
 
 
@@ -429,3 +480,20 @@ def kappa64_part(cfg, npot, pix_stride):
 
 def poisson_total64(cfg, ipop, lam):
     return lib().or_poisson_total64(cfgp(cfg), ipop, P(np.ascontiguousarray(lam, np.float64)))
+
+
+def pix_checked(nside, xyz32, ein=0.0):
+    """Margin-checked float RING pixels of float directions (-1: deferred)."""
+    a = np.ascontiguousarray(xyz32, np.float32)
+    out = np.empty(len(a), np.int64)
+    lib().or_pix_checked(nside, P(a), len(a), float(ein), P(out))
+    return out
+
+
+def pix64(nside, xyz, shared=False):
+    """RING pixels of double directions by the oracle's restatement (or the
+    kernels' double restatement with shared=True)."""
+    a = np.ascontiguousarray(xyz, np.float64)
+    out = np.empty(len(a), np.int64)
+    (lib().or_pix_cgx if shared else lib().or_pix64)(nside, P(a), len(a), P(out))
+    return out

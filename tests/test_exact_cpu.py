@@ -1,0 +1,124 @@
+"""Integer outputs equal to the reference's double arithmetic, on the CPU.
+
+The kernels decide Poisson counts and HEALPix pixels in single precision
+where a bound on the distance to the double value proves the decision, and
+in double otherwise (colore_gb300/csrc/cg_exact.h).  These tests run the
+same functions on the CPU (the oracle's dev32 mirror) against the oracle's
+independent double restatement of the reference (or_ref64.c):
+
+  pixels   directions at random and next to every kind of RING pixel edge
+           (equatorial edge lines, polar-cap lines, the phi = k pi/2 lines,
+           |cos theta| = 2/3), exact float inputs and inputs carrying a
+           relative error; every decision kept in single precision must be
+           the double one;
+  counts   every cell's Poisson count of 64^3 mocks (three bias models, a
+           population dense enough near the observer to take PTRS) equals
+           the double restatement's;
+  sources  positions, base pixels and count maps equal; RA, Dec, z within
+           single-precision tolerance.
+"""
+import numpy as np
+import pytest
+
+rng = np.random.default_rng(7)
+
+
+def _dirs(z, tt):
+    phi = tt * np.pi / 2
+    s = np.sqrt(np.maximum(0, 1 - z * z))
+    return np.stack([s * np.cos(phi), s * np.sin(phi), z], 1)
+
+
+def _edge_points(ns, n):
+    """Directions within 1e-9..1e-4 of RING pixel edges at nside ns."""
+    zs, ts = [], []
+    z = rng.uniform(-2 / 3, 2 / 3, n)
+    k = rng.integers(0, 4 * ns + 2, n)
+    sgn = rng.choice([-1, 1], n)
+    zs.append(z)
+    ts.append((k / ns - 0.5 - sgn * 0.75 * z) % 4)
+    z = rng.uniform(2 / 3, 1, n) * rng.choice([-1, 1], n)
+    tmp = ns * np.sqrt(3 * (1 - np.abs(z)))
+    k = np.floor(rng.uniform(0, 1, n) * tmp)
+    tp = np.where(rng.uniform(size=n) < 0.5, k / np.maximum(tmp, 1e-9), 1 - k / np.maximum(tmp, 1e-9))
+    zs.append(z)
+    ts.append((rng.integers(0, 4, n) + np.clip(tp, 0, 1)) % 4)
+    ir = rng.integers(1, ns + 1, n)
+    kk = rng.integers(0, 4 * ir)
+    zs.append((1 - (ir / ns) ** 2 / 3 * rng.uniform(0.9, 1.0, n)) * rng.choice([-1, 1], n))
+    ts.append((kk / ir) % 4)
+    zs.append(rng.uniform(-1, 1, n))
+    ts.append(rng.integers(0, 4, n).astype(float))
+    zs.append(rng.choice([-2 / 3, 2 / 3], n))
+    ts.append(rng.uniform(0, 4, n))
+    z = np.concatenate(zs)
+    tt = np.concatenate(ts)
+    sc = 10 ** rng.uniform(-9, -4, len(z))
+    z = np.clip(z + rng.normal(size=len(z)) * sc, -1, 1)
+    tt = (tt + rng.normal(size=len(z)) * sc) % 4
+    return _dirs(z, tt)
+
+
+@pytest.mark.parametrize("ns", [1, 2, 16, 256, 512, 1024])
+def test_pixel_margins_never_disagree_with_double(ns):
+    import oracle as orc
+    for kind in ("random", "edges"):
+        v = rng.normal(size=(100000, 3)) if kind == "random" else _edge_points(ns, 20000)
+        v *= rng.uniform(10, 4000, (len(v), 1))
+        v32 = v.astype(np.float32)
+        fast = orc.pix_checked(ns, v32, 0.0)
+        ref = orc.pix64(ns, v32.astype(np.float64))
+        ok = fast >= 0
+        assert np.array_equal(fast[ok], ref[ok]), (ns, kind)
+        # the kernels' own double restatement agrees with the oracle's
+        assert np.array_equal(orc.pix64(ns, v32.astype(np.float64), shared=True), ref)
+        if kind == "random":
+            assert 1 - ok.mean() < 5e-6 * ns + 1e-4, (ns, 1 - ok.mean())
+        # float coordinates within a relative 2^-24 of the double point
+        pert = (v * (1 + rng.uniform(-1, 1, v.shape) * 2.0 ** -24)).astype(np.float32)
+        fast = orc.pix_checked(ns, pert, 2.0 ** -23)
+        ref = orc.pix64(ns, v)
+        ok = fast >= 0
+        assert np.array_equal(fast[ok], ref[ok]), (ns, kind, "perturbed")
+
+
+def _spec(bias_model):
+    return dict(n_grid=64, z_min=0.05, z_max=0.6, r_smooth=2.0, seed=11 + bias_model, dens_type=0,
+                bias_model=bias_model,
+                srcs=[dict(nz=("gauss", 0.3, 0.1), density=40.0, bias=("1+z",), nside_count=64),
+                      dict(nz=("flat", 0.0, 0.5), density=30.0, bias=("const", 2.0), nside_count=512)])
+
+
+@pytest.mark.parametrize("bias_model", [1, 2, 3])
+def test_counts_and_sources_equal_double(tmp_path, bias_model):
+    import oracle as orc
+    from colore_gb300 import inputs
+    prm = orc.Params(inputs.write_inputs(str(tmp_path), _spec(bias_model)))
+    cfg = prm.config
+    n = cfg.n_grid
+    d64, p64, st = orc.field64(cfg)
+    dens = orc.density64(cfg, d64, st[3])
+    d32 = dens.astype(np.float32)
+    phi32 = p64.astype(np.float32)
+    tabs, e0f, _ = orc.norm_tables64(cfg, d32.astype(np.float64))
+    pad = lambda a: np.ascontiguousarray(np.pad(a, ((0, 0), (0, 0), (0, 2 * (n // 2 + 1) - n))))
+    for ip in range(cfg.n_srcs):
+        t64, e64 = tabs[ip], np.asarray(e0f[ip], np.float64)
+        t32, e32 = t64.astype(np.float32), e64.astype(np.float32)
+        c32, tot32, fb = orc.counts32(cfg, ip, pad(d32), t32, e32, t64, e64)
+        c64, tot64 = orc.counts64(cfg, ip, d32, t64, e64)
+        assert tot64 > 1000
+        assert np.array_equal(c32, c64), (ip, int((c32 != c64).sum()))
+        if ip == 1:
+            assert c64.max() >= 10  # the dense cells near the observer take PTRS
+        o32 = orc.emit32(cfg, ip, pad(d32), pad(phi32), t32, e32, t64, e64, cap=tot64 + 16)
+        o64 = orc.emit64(cfg, ip, phi32, c64, cap=tot64 + 16)
+        assert np.array_equal(o32["pos"][:, :3].view(np.uint32), o64["pos"][:, :3].view(np.uint32))
+        assert np.array_equal(o32["ipix"], o64["ipix"])
+        assert np.array_equal(o32["cmap"], o64["cmap"])
+        np.testing.assert_allclose(o32["pos"][:, 3], o64["pos"][:, 3], rtol=1e-4, atol=1e-3)
+        s32, s64 = o32["src"], o64["src"]
+        dra = np.abs(s32[:, 0] - s64[:, 0])
+        assert np.all(np.minimum(dra, 360 - dra) < 2e-4)
+        assert np.max(np.abs(s32[:, 1] - s64[:, 1])) < 2e-4
+        np.testing.assert_allclose(s32[:, 2], s64[:, 2], rtol=2e-6, atol=1e-7)

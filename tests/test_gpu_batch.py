@@ -45,7 +45,8 @@ def test_graph_replay_matches_plain_run(built, tmp_path):
     # the replayed pipeline against the oracle: emit from the replay's own
     # density and normalisation table
     tab, e = m.norm_table(0, 0)
-    o = orc.emit32(prm.config, 0, m.grid(0), m.grid(1), tab, e, cap=n0 + 100)
+    t64, e64 = m.norm_table64(0, 0)
+    o = orc.emit32(prm.config, 0, m.grid(0), m.grid(1), tab, e, t64, e64, cap=n0 + 100)
     assert np.array_equal(o["pos"].view(np.uint32), ref[0].view(np.uint32))
     m.close()
 

@@ -124,9 +124,13 @@ class Run:
         m.compute_density_normalization()
         self.d = m.grid(0).copy()
         self.norm_s = [m.norm_table(0, i) for i in range(self.cfg.n_srcs)]
+        self.norm_s64 = [m.norm_table64(0, i) for i in range(self.cfg.n_srcs)]
+        self.norm_i64 = [m.norm_table64(1, i) for i in range(self.cfg.n_imap)]
         self.norm_i = [m.norm_table(1, i) for i in range(self.cfg.n_imap)]
         self.norm_c = [m.norm_table(2, i) for i in range(self.cfg.n_cstm)]
+        m.exact_stats(reset=True)
         self.nsrc = m.srcs_set_cartesian()
+        self.xstats_srcs = m.exact_stats(reset=True)
         self.cats = [m.catalog(i) for i in range(self.cfg.n_srcs)]
         self.cmaps = [m.count_map(i) if self.cfg.nside_count[i] > 0 else None for i in range(self.cfg.n_srcs)]
         m.imap_set_cartesian()
@@ -323,14 +327,67 @@ def test_norm_tables_vs_fp64(runs, kind):
 
 
 @pytest.mark.parametrize("kind", ["full", "nobeam", "lpt", "n96", "ptrs", "clip"])
+def test_sources_equal_double_arithmetic(runs, kind):
+    """Counts of every cell, positions, base-pixel ids and count maps equal
+    the oracle's double restatement of the reference (srcs.c:156-283,
+    386-416) on the same density, potential and normalisation table, bit for
+    bit; RA, Dec, z and the RSD shift agree to single-precision accuracy."""
+    import oracle as orc
+    r = runs(kind)
+    for ip in range(r.cfg.n_srcs):
+        t64, e64 = r.need('norm_s64')[ip]
+        c64, tot64 = orc.counts64(r.cfg, ip, r.need('d'), t64, e64)
+        assert tot64 == r.need('nsrc')[ip], (tot64, r.need('nsrc')[ip])
+        o = orc.emit64(r.cfg, ip, r.phi, c64, cap=tot64 + 16)
+        g = r.need('cats')[ip]
+        assert np.array_equal(o["pos"][:, :3].view(np.uint32), g["pos"][:, :3].view(np.uint32))
+        assert np.array_equal(o["ipix"], g["ipix"])
+        if r.need('cmaps')[ip] is not None:
+            assert np.array_equal(o["cmap"], r.need('cmaps')[ip])
+        np.testing.assert_allclose(g["pos"][:, 3], o["pos"][:, 3], rtol=1e-4, atol=1e-3)
+        if not r.cfg.need_beaming:
+            dra = np.abs(g["src"][:, 0] - o["src"][:, 0])
+            assert np.all(np.minimum(dra, 360 - dra) < 2e-4)
+            assert np.max(np.abs(g["src"][:, 1] - o["src"][:, 1])) < 2e-4
+            np.testing.assert_allclose(g["src"][:, 2], o["src"][:, 2], rtol=2e-6, atol=1e-7)
+    print(kind, "decisions in double:", r.need('xstats_srcs'))
+
+
+def test_sources_all_decisions_in_double(runs, tmp_path):
+    """With every count and pixel decided by the device's double arithmetic
+    the catalogue is the same: the double restatement on the device agrees
+    with the float margins everywhere."""
+    import colore_gb300 as cg
+    from colore_gb300 import inputs
+    r = runs("full")
+    m = cg.Mock(cg.Params(inputs.write_inputs(str(tmp_path), _spec("full"))))
+    m.set_decisions_in_double(True)
+    m.create_cartesian_fields()
+    m.compute_physical_density_field()
+    m.compute_density_normalization()
+    m.exact_stats(reset=True)
+    nsrc = m.srcs_set_cartesian()
+    st = m.exact_stats()
+    assert list(nsrc) == list(r.need('nsrc'))
+    assert st["count_cells"] > 1000 and st["src_pixels"] >= 2 * sum(nsrc)
+    for ip in range(r.cfg.n_srcs):
+        g = m.catalog(ip)
+        for k in ("pos", "ipix"):
+            assert np.array_equal(g[k], r.need('cats')[ip][k]), k
+    m.close()
+
+
+@pytest.mark.parametrize("kind", ["full", "nobeam", "lpt", "n96", "ptrs", "clip"])
 def test_sources_bitexact(runs, kind):
     """Counts, catalogue order, positions, base-pixel ids, ra/dec/z, RSD and
-    the count map equal the dev32 restatement bit for bit."""
+    the count map equal the dev32 restatement (the CPU mirror of the kernels'
+    arithmetic) bit for bit."""
     import oracle as orc
     r = runs(kind)
     for ip in range(r.cfg.n_srcs):
         tab, e = r.need('norm_s')[ip]
-        ref = orc.emit32(r.cfg, ip, r.need('d'), r.phi, tab, e, cap=int(r.need('nsrc')[ip] * 1.2) + 100)
+        t64, e64 = r.need('norm_s64')[ip]
+        ref = orc.emit32(r.cfg, ip, r.need('d'), r.phi, tab, e, t64, e64, cap=int(r.need('nsrc')[ip] * 1.2) + 100)
         g = r.need('cats')[ip]
         assert len(ref["pos"]) == r.need('nsrc')[ip]
         assert np.array_equal(ref["pos"].view(np.uint32), g["pos"].view(np.uint32))
