@@ -9,7 +9,7 @@ any size:
   1LPT density          every particle deposits unit mass: mean of 1 + delta
                         is 1 to FP32 accumulation accuracy (2e-6)
   sources               the count map adds up to the catalogue; every source
-                        inside the box, RA in [0, 360), Dec in [-90, 90],
+                        inside the box, RA in [0, 360], Dec in [-90, 90],
                         HEALPix ids in range
   intensity map         samples painted = the oracle's count from the
                         geometry (1e-3, FP32 vs FP64 radii at the edges);
@@ -82,7 +82,9 @@ def test_c4_full_size_properties(c4):
     pos, src, ipix = cat["pos"], cat["src"], cat["ipix"]
     r = np.sqrt((pos[:, :3].astype(np.float64) ** 2).sum(1))
     assert r.max() <= cfg.l_box * np.sqrt(3) / 2 + 1
-    assert np.all((src[:, 0] >= 0) & (src[:, 0] < 360))
+    # RA = RTOD phi with phi in [0, 2 pi]: rounded to float, a source within
+    # ~3e-7 rad below 2 pi reads 360 (as the reference's float RA does)
+    assert np.all((src[:, 0] >= 0) & (src[:, 0] <= 360))
     assert np.all((src[:, 1] >= -90) & (src[:, 1] <= 90))
     # redshifts of the cells the sources sit in: up to the box edge, a little past z_max = 1.5
     assert np.all((src[:, 2] >= 0) & (src[:, 2] < 2.0))
