@@ -51,12 +51,15 @@ struct Cat {
 struct Imap {
   int nr = 0, nside = 0;
   long long npix = 0;
-  float *r0 = nullptr, *rf = nullptr;
-  float4 *shp = nullptr; /* per shell index + 1: nsub, dx/nsub, 1/nsub */
-  float rmin = 0, rmax = 0;
+  /* shells (cg_imap_shells): edges, shell of each interval, nsub and
+   * dx/nsub per bucket; bucket slots and counts */
+  float *b = nullptr, *dxs = nullptr;
+  int *shell_of = nullptr, *nsub = nullptr;
+  long long *base = nullptr, *cap = nullptr;
+  unsigned long long *cnt = nullptr, *chunk_off = nullptr;
   float *data = nullptr;
   int *nadd = nullptr;
-  unsigned long long samples = 0; /* sub-samples painted by the last run */
+  unsigned long long samples = 0; /* sub-samples drawn by the last run */
 };
 
 } /* namespace */
@@ -122,11 +125,10 @@ struct cg_ctx {
   Imap im[CG_NPOP_MAX];
   float *d_tmpmap = nullptr;
   size_t tmpmap_n = 0;
-  cg_imap_cell *d_cells = nullptr;
-  unsigned int *d_cell_n = nullptr;
-  long long *d_cell_off = nullptr, *d_scan_tmp = nullptr;
+  cg_imap_rec *d_recs = nullptr;         /* listed cells of one species */
+  unsigned long long *d_imap_queue = nullptr; /* samples for the double pass */
   unsigned long long *d_imap_ctr = nullptr;
-  long long list_cap = 0;
+  long long list_cap = 0, queue_cap = 0;
   long long list_cap_max = 0; /* cg_set_imap_list_cap; 0: by free memory */
   /* kappa */
   float *d_kmap = nullptr, *d_kfac = nullptr, *d_kinv = nullptr;
@@ -235,7 +237,7 @@ static int check_device_errors(cg_ctx *c)
   if (h) {
     CUDA_TRY(c, cudaMemsetAsync(c->d_err, 0, sizeof(unsigned int), c->stream));
     return fail(c, CG_EDEVICE, "device error flags 0x%x (1: source count overflow, 2: catalog overflow, "
-                               "4: shell search, 8: imap sub-sampling, 16: imap cell list, 32: bulk copy timeout, "
+                               "4: shell search, 8: imap sub-sampling, 16: imap double-decision queue full, 32: bulk copy timeout, "
                                "64: particle deposit overflow)",
                 h);
   }
@@ -515,9 +517,15 @@ extern "C" int cg_upload_tables(cg_ctx *c, const cg_config *cfg)
                                 c->stream));
     const int N = cfg->n_grid;
     const double dx = cfg->l_box / N;
-    std::vector<float> cr((size_t)3 * N);
+    /* per axis the corner rounded to float, then (three more rows) the rest
+     * corner - rounded corner, a double-float pair */
+    std::vector<float> cr((size_t)6 * N);
     for (int k3 = 0; k3 < 3; k3++)
-      for (int i = 0; i < N; i++) cr[(size_t)k3 * N + i] = (float)cgx_coord(i, dx, cfg->pos_obs[k3]);
+      for (int i = 0; i < N; i++) {
+        const double cd = cgx_coord(i, dx, cfg->pos_obs[k3]);
+        cr[(size_t)k3 * N + i] = (float)cd;
+        cr[(size_t)(3 + k3) * N + i] = (float)(cd - (double)(float)cd);
+      }
     if (int rc = dalloc(c, &c->d_corner, cr.size())) return rc;
     CUDA_TRY(c, cudaMemcpyAsync(c->d_corner, cr.data(), cr.size() * sizeof(float), cudaMemcpyHostToDevice,
                                 c->stream));
@@ -712,13 +720,14 @@ extern "C" void cg_destroy(cg_ctx *c)
                   c->d_disp[1], c->d_disp[2], c->d_part, c->d_stats, c->d_s2f, c->d_err, c->d_ncount,
                   c->d_zsum, c->d_bsum, c->d_counts, c->d_bsums, c->d_total, c->d_tmpmap, c->d_kmap,
                   c->d_kfac, c->d_kinv, c->d_kir, c->d_ovf_cell, c->d_ovf_cnt, c->d_ovf_n,
-                  c->d_cells, c->d_cell_n, c->d_cell_off, c->d_scan_tmp, c->d_imap_ctr,
+                  c->d_recs, c->d_imap_queue, c->d_imap_ctr,
                   c->d_imap_isw, c->d_ifac, c->d_iir, c->d_cfac, c->d_losfac};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < CG_NPOP_MAX; i++) {
-    void *q[] = {c->cat[i].pos, c->cat[i].ipix, c->cat[i].src, c->cat[i].cmap, c->im[i].r0, c->im[i].rf,
-                 c->im[i].shp, c->im[i].data, c->im[i].nadd, c->d_cmap[i], c->cat[i].skw_d, c->cat[i].skw_v};
+    void *q[] = {c->cat[i].pos, c->cat[i].ipix, c->cat[i].src, c->cat[i].cmap, c->im[i].b, c->im[i].dxs,
+                 c->im[i].shell_of, c->im[i].nsub, c->im[i].base, c->im[i].cap, c->im[i].cnt, c->im[i].chunk_off,
+                 c->im[i].data, c->im[i].nadd, c->d_cmap[i], c->cat[i].skw_d, c->cat[i].skw_v};
     for (void *p : q)
       if (p) cudaFree(p);
   }
@@ -1324,34 +1333,23 @@ extern "C" int cg_imap_set_cartesian(cg_ctx *c)
     const int nr = c->cfg.imap_nr[ip];
     const int nside = c->cfg.nside_imap[ip];
     const long long npix = 12LL * nside * nside;
-    /* imap_preproc (imap.c:105-133): sort shells by r0, full-sky maps */
-    std::vector<int> order(nr);
-    for (int i = 0; i < nr; i++) order[i] = i;
-    std::vector<float> r0(nr), rf(nr);
-    for (int i = 0; i < nr; i++) {
-      r0[i] = (float)c->cfg.imap_r0[ip][i];
-      rf[i] = (float)c->cfg.imap_rf[ip][i];
-    }
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return r0[a] < r0[b]; });
-    std::vector<float> sr0(nr), srf(nr);
-    for (int i = 0; i < nr; i++) {
-      sr0[i] = r0[order[i]];
-      srf[i] = rf[order[i]];
-    }
-    /* sub-sampling factors, imap.c:153-174 */
+    /* imap_preproc (imap.c:105-133) and the sub-sampling factors
+     * (imap.c:153-174): shells sorted by r0, their edges as intervals */
     const double dx = c->cfg.l_box / c->N;
-    const double ps = sqrt(4 * M_PI / (double)npix);
-    std::vector<int> nsub(nr);
-    for (int i = 0; i < nr; i++) {
-      double a = sr0[i], b = srf[i];
-      double vol = (b * b * b - a * a * a) * ps * ps / 3;
-      double sct = a * ps, scr = b - a, scv = pow(vol, 0.333333);
-      double sc0 = fmin(scv, fmin(sct, scr));
-      nsub[i] = (int)(dx / sc0 + 0.5) + 1;
-    }
+    const int nbk = nr + 2;
+    if (nbk > CG_IMAP_BUCKETS_MAX) return fail(c, CG_EINVAL, "intensity species %d: %d shells", ip, nr);
+    std::vector<float> r0f(nr), rff(nr), bb(2 * nr), dxs(nr + 2);
+    std::vector<int> shell_of(2 * nr + 1), nsub(nr + 2);
+    const int nb = cg_imap_shells(c->cfg.imap_r0[ip], c->cfg.imap_rf[ip], nr, dx, npix, r0f.data(), rff.data(),
+                                  bb.data(), shell_of.data(), nsub.data(), dxs.data());
+    for (int i = 0; i < nr + 2; i++)
+      if (nsub[i] < 1 || nsub[i] > 1024)
+        return fail(c, CG_EINVAL, "intensity species %d: nsub %d outside 1..1024", ip, nsub[i]);
     if (M.nr != nr) {
-      if ((rc = dalloc(c, &M.r0, (size_t)nr)) || (rc = dalloc(c, &M.rf, (size_t)nr)) ||
-          (rc = dalloc(c, &M.shp, (size_t)nr + 2)))
+      if ((rc = dalloc(c, &M.b, (size_t)2 * nr)) || (rc = dalloc(c, &M.shell_of, (size_t)2 * nr + 1)) ||
+          (rc = dalloc(c, &M.nsub, (size_t)nr + 2)) || (rc = dalloc(c, &M.dxs, (size_t)nr + 2)) ||
+          (rc = dalloc(c, &M.base, (size_t)nbk)) || (rc = dalloc(c, &M.cap, (size_t)nbk)) ||
+          (rc = dalloc(c, &M.cnt, (size_t)nbk)) || (rc = dalloc(c, &M.chunk_off, (size_t)nbk + 1)))
         return rc;
     }
     if (M.nr != nr || M.npix != npix) {
@@ -1360,71 +1358,120 @@ extern "C" int cg_imap_set_cartesian(cg_ctx *c)
     M.nr = nr;
     M.nside = nside;
     M.npix = npix;
-    CUDA_TRY(c, cudaMemcpyAsync(M.r0, sr0.data(), nr * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-    CUDA_TRY(c, cudaMemcpyAsync(M.rf, srf.data(), nr * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-    /* get_r_index_imap gives -1 below the shells (nsub_lo) and nr beyond
-     * them (nsub_hi); a gap between shells also gives -1 (imap.c:196-208) */
-    std::vector<float4> shp(nr + 2);
-    for (int i = -1; i <= nr; i++) {
-      const int ns = i < 0 ? nsub[0] : (i >= nr ? nsub[nr - 1] : nsub[i]);
-      if (ns < 1 || ns > 1024) return fail(c, CG_EINVAL, "intensity species %d: nsub %d outside 1..1024", ip, ns);
-      float nsbits;
-      memcpy(&nsbits, &ns, sizeof(nsbits));
-      shp[i + 1] = make_float4(nsbits, c->box.dx / (float)ns, 1.0f / (float)ns, 0.0f);
+    const double rmin = (double)r0f[0] - 20., rmax = (double)rff[nr - 1] + 20.;
+    /* slots per bucket: the corners of the cells of bucket j + 1 lie in the
+     * radii of the intervals of shell j; each corner's dx-cube lies within
+     * sqrt(3)/2 dx of it, so (expanded shell volume) / dx^3 bounds them */
+    std::vector<double> want(nbk, 0.0);
+    const double h = 0.8660254037844386 * dx, ncell = (double)c->N * c->N * c->N;
+    for (int k = -1; k < nb; k++) {
+      double lo = k < 0 ? rmin : (double)bb[k], hi = k + 1 < nb ? (double)bb[k + 1] : rmax;
+      lo = lo < rmin ? rmin : lo;
+      hi = hi > rmax ? rmax : hi;
+      if (hi <= lo) continue;
+      const double a = lo - h > 0 ? lo - h : 0, z = hi + h;
+      want[shell_of[k + 1] + 1] += 4.0 / 3.0 * M_PI * (z * z * z - a * a * a) / (dx * dx * dx);
     }
-    CUDA_TRY(c, cudaMemcpyAsync(M.shp, shp.data(), (nr + 2) * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+    double tot = 0;
+    for (int i = 0; i < nbk; i++) {
+      want[i] = std::min(want[i], ncell) + 64;
+      tot += want[i];
+    }
+    /* room: every cell, within a quarter of the free memory and the
+     * caller's bound (cells beyond are painted by the listing kernel) */
+    size_t fr = 0, tt = 0;
+    CUDA_TRY(c, cudaMemGetInfo(&fr, &tt));
+    double room = (double)(fr + (size_t)c->list_cap * CG_IMAP_REC_BYTES) * 0.25 / CG_IMAP_REC_BYTES;
+    if (c->list_cap_max > 0 && room > (double)c->list_cap_max) room = (double)c->list_cap_max;
+    const double scale = tot > room ? room / tot : 1.0;
+    std::vector<long long> base(nbk), capv(nbk);
+    long long acc = 0;
+    for (int i = 0; i < nbk; i++) {
+      base[i] = acc;
+      capv[i] = (long long)(want[i] * scale);
+      acc += capv[i];
+    }
+    if (acc > c->list_cap) {
+      if ((rc = dalloc(c, &c->d_recs, (size_t)acc))) return rc;
+      c->list_cap = acc;
+    }
+    if (!c->d_imap_ctr && (rc = dalloc(c, &c->d_imap_ctr, (size_t)5))) return rc;
+    if (!c->d_imap_queue) {
+      const long long qc = 1LL << 27;
+      if ((rc = dalloc(c, &c->d_imap_queue, (size_t)qc))) return rc;
+      c->queue_cap = qc;
+    }
+    CUDA_TRY(c, cudaMemcpyAsync(M.b, bb.data(), nb * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(M.shell_of, shell_of.data(), (nb + 1) * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(M.nsub, nsub.data(), (nr + 2) * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(M.dxs, dxs.data(), (nr + 2) * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(M.base, base.data(), nbk * sizeof(long long), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(M.cap, capv.data(), nbk * sizeof(long long), cudaMemcpyHostToDevice, c->stream));
     CUDA_TRY(c, cudaMemsetAsync(M.data, 0, (size_t)nr * npix * sizeof(float), c->stream));
     CUDA_TRY(c, cudaMemsetAsync(M.nadd, 0, (size_t)nr * npix * sizeof(int), c->stream));
     cg_imap_params p;
     memset(&p, 0, sizeof(p));
     p.box = c->box;
-    p.g = c->g;
-    p.tz = c->tz[ip];
-    p.bz = c->bzi[ip];
-    p.norm = c->normi[ip];
-    p.v1 = c->v1;
-    p.ih = c->ih;
-    p.bias_model = c->cfg.bias_model;
-    p.factor_vel = (float)(-c->cfg.fgrowth_0 / (1.5 * c->cfg.hubble_0 * c->cfg.omega_m));
+    cg_imap_args &a = p.a;
+    const int na = CG_NA, N = c->N, nt0 = 4 + 2 * c->cfg.n_srcs;
+    a.r = c->g.r;
+    a.tz = c->tz[ip].f;
+    a.bz = c->bzi[ip].f;
+    a.norm = c->normi[ip].f;
+    a.v1 = c->v1.f;
+    a.ih = c->ih.f;
+    a.xc = c->d_corner;
+    a.yc = c->d_corner + N;
+    a.zc = c->d_corner + 2 * N;
+    a.xl = c->d_corner + 3 * N;
+    a.yl = c->d_corner + 4 * N;
+    a.zl = c->d_corner + 5 * N;
+    a.idr = c->g.idr;
+    a.r_last = c->g.r_last;
+    a.rmin = (float)rmin;
+    a.rmax = (float)rmax;
+    const double fv = -c->cfg.fgrowth_0 / (1.5 * c->cfg.hubble_0 * c->cfg.omega_m);
+    a.fvh = (float)(fv * (0.5 * (c->cfg.n_grid / c->cfg.l_box)));
+    a.dx = (float)dx;
+    a.na = na;
+    a.bias_model = c->cfg.bias_model;
+    a.nside = nside;
+    a.sh.b = M.b;
+    a.sh.shell_of = M.shell_of;
+    a.sh.nb = nb;
+    a.sh.nr = nr;
+    a.nsub = M.nsub;
+    a.dxs = M.dxs;
+    a.r64 = c->d_tabs64;
+    a.v164 = c->d_tabs64 + (size_t)2 * na;
+    a.ih64 = c->d_tabs64 + (size_t)3 * na;
+    a.tz64 = c->d_tabs64 + (size_t)(nt0 + 2 * ip) * na;
+    a.bz64 = c->d_tabs64 + (size_t)(nt0 + 2 * ip + 1) * na;
+    a.norm64 = c->d_norm64 + (size_t)(c->cfg.n_srcs + ip) * (na + 2);
+    a.idr64 = c->cfg.glob_idr;
+    a.r_last64 = c->cfg.r_arr_r2z[na - 1];
+    a.dx64 = dx;
+    for (int k = 0; k < 3; k++) a.p64[k] = c->cfg.pos_obs[k];
+    a.idx64 = c->cfg.n_grid / c->cfg.l_box;
+    a.fv64 = fv;
+    a.rmin64 = rmin;
+    a.rmax64 = rmax;
     p.nr = nr;
-    p.r0 = M.r0;
-    p.rf = M.rf;
-    p.shp = M.shp;
-    p.rmin_here = (float)((double)sr0[0] - 20.);
-    p.rmax_here = (float)((double)srf[nr - 1] + 20.);
-    p.nside = nside;
+    p.nbk = nbk;
     p.npix = npix;
     p.data = M.data;
     p.nadd = M.nadd;
     p.err = c->d_err;
-    /* The cell list holds every cell within the shells' outer radius (or the
-     * whole box), up to a quarter of the free device memory; cells past its
-     * capacity are painted by the first kernel. */
-    {
-      const double rb = (double)p.rmax_here / dx + 2.0;
-      const double ball = 4.0 / 3.0 * M_PI * rb * rb * rb;
-      const double ncell = (double)c->N * c->N * c->N;
-      size_t fr = 0, tot = 0;
-      CUDA_TRY(c, cudaMemGetInfo(&fr, &tot));
-      const double budget = (double)(fr + (size_t)c->list_cap * CG_IMAP_CELL_BYTES) * 0.25 / CG_IMAP_CELL_BYTES;
-      long long want = (long long)fmin(fmin(ball, ncell), budget) + 1;
-      if (c->list_cap_max > 0 && want > c->list_cap_max) want = c->list_cap_max;
-      if (want > c->list_cap) {
-        if ((rc = dalloc(c, &c->d_cells, (size_t)want)) || (rc = dalloc(c, &c->d_cell_n, (size_t)want)) ||
-            (rc = dalloc(c, &c->d_cell_off, (size_t)want)) ||
-            (rc = dalloc(c, &c->d_scan_tmp, (size_t)cg_imap_scan_blocks(want))))
-          return rc;
-        c->list_cap = want;
-      }
-      if (!c->d_imap_ctr && (rc = dalloc(c, &c->d_imap_ctr, (size_t)5))) return rc;
-      p.list_cap = c->list_cap_max > 0 && c->list_cap > c->list_cap_max ? c->list_cap_max : c->list_cap;
-
-      p.ctr = c->d_imap_ctr;
-      p.cells = c->d_cells;
-      p.cell_n = c->d_cell_n;
-      p.cell_off = c->d_cell_off;
-      p.scan_tmp = c->d_scan_tmp;
-    }
+    p.xstats = c->d_xstats;
+    p.force_double = c->force_double;
+    p.recs = c->d_recs;
+    p.base = M.base;
+    p.cap = M.cap;
+    p.cnt = M.cnt;
+    p.chunk_off = M.chunk_off;
+    p.ctr = c->d_imap_ctr;
+    p.queue = c->d_imap_queue;
+    p.queue_cap = c->queue_cap;
     {
       ProfScope ps(c, "imap_paint");
       CUDA_TRY(c, cg_imap_paint(c->stream, c->d_dens, c->d_npot, &p, c->nsm));
@@ -1432,8 +1479,8 @@ extern "C" int cg_imap_set_cartesian(cg_ctx *c)
     unsigned long long ctr[5] = {0, 0, 0, 0, 0};
     CUDA_TRY(c, cudaMemcpyAsync(ctr, c->d_imap_ctr, sizeof(ctr), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host vectors above go out of scope */
-    M.samples = ctr[3] + ctr[4];
-    c->launches += ctr[0] > 0 ? 5 : 1; /* cells, 3 scan passes, paint */
+    M.samples = ctr[2];
+    c->launches += 4; /* list, chunks, paint, double */
   }
   /* final maps to registered host buffers (write_imap, io.c:738-741:
    * data/nadd where nadd > 0), overlapping the stages still to run */

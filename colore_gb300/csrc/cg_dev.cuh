@@ -21,7 +21,7 @@ enum : unsigned int {
   ERR_CATALOG_OVERFLOW = 2u, /* emit wrote past the allocated catalog  */
   ERR_SHELL_WALK = 4u,       /* imap shell search did not terminate    */
   ERR_IMAP_NSUB = 8u,        /* sub-sampling factor out of range       */
-  ERR_IMAP_HEAVY = 16u,      /* nsub > 128 in a cell past the list     */
+  ERR_IMAP_QUEUE = 16u,      /* intensity-map double-decision queue full */
   ERR_DEPOSIT_OVERFLOW = 64u, /* a cell of the particle deposit holds 2^11 or more */
 };
 

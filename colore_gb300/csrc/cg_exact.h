@@ -390,7 +390,7 @@ CG_HD int cg_poisson_inv_checked(float lam, float elam, float u)
  * f is formed from the octant-reduced atan of min/max, so that it carries
  * absolute, not relative-to-2pi, rounding. */
 typedef struct {
-  float cth, f, rho2, rinv, ecth, ef;
+  float cth, f, rho2, r2, rinv, ecth, ef;
   int q;
 } cg_dir;
 
@@ -399,6 +399,7 @@ CG_HD cg_dir cg_dir_of(float x, float y, float z, float ein)
   cg_dir o;
   o.rho2 = CG_FMA(x, x, CG_MUL(y, y));
   const float r2 = CG_FMA(z, z, o.rho2);
+  o.r2 = r2;
   o.rinv = cg_rsqrt_fast(r2);
   o.cth = CG_MUL(z, o.rinv);
   const float ax = cg_fabsf(x), ay = cg_fabsf(y);
@@ -618,6 +619,286 @@ CG_HD void cg_src_pixels(float px, float py, float pz, int nside_base, int nside
     }
     *pix_count = pc;
   }
+}
+
+/* ---- intensity maps (imap.c:135-245) ------------------------------------ */
+
+/* Shells as intervals between their sorted distinct edges b[0..nb-1] (the
+ * float r0 and rf of imap_preproc, imap.c:105-133): interval k is
+ * [b[k], b[k+1]) (k = -1 below b[0], nb-1 at or above b[nb-1]) and
+ * shell_of[k+1] its shell (-1 below the shells, nr beyond).  For contiguous
+ * shells (each rf the next r0) this is get_r_index_imap's answer from any
+ * start (imap.c:76-103); otherwise it is the walk's answer from shell 0. */
+typedef struct {
+  const float *b;
+  const int *shell_of; /* nb + 1 */
+  int nb, nr;
+} cg_shells;
+
+CG_HD int cg_interval(const cg_shells *sh, float r)
+{
+  int lo = -1, hi = sh->nb - 1; /* last k with b[k] <= r, -1 if none */
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (sh->b[mid] <= r) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+CG_HD int cgx_interval(const cg_shells *sh, double r)
+{
+  int lo = -1, hi = sh->nb - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if ((double)sh->b[mid] <= r) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+/* Distance of r to the edges of its interval k. */
+CG_HD float cg_interval_margin(const cg_shells *sh, int k, float r)
+{
+  const float below = k >= 0 ? CG_SUB(r, sh->b[k]) : 3.0e38f;
+  const float above = k + 1 < sh->nb ? CG_SUB(sh->b[k + 1], r) : 3.0e38f;
+  return cg_fminf(below, above);
+}
+
+/* Everything a species' cells and samples need, in float and in double. */
+typedef struct {
+  const float *r, *tz, *bz, *norm, *v1, *ih; /* norm: CG_NA values then the two edges */
+  const float *xc, *yc, *zc;                 /* corners i*dx - p rounded once */
+  const float *xl, *yl, *zl;                 /* the rest: corner - rounded corner */
+  float idr, r_last, bz0, v10, v1f, ih0, ihf;
+  float rmin, rmax;                          /* r0[0] - 20, rf[nr-1] + 20 (imap.c:151-152) */
+  float fvh;                                 /* factor_vel * 0.5 * idx */
+  float dx;
+  int na, bias_model, nside;
+  cg_shells sh;
+  const int *nsub;                           /* nsub of shell s + 1, s = -1 .. nr (imap.c:153-174) */
+  const float *dxs;                          /* dx / nsub, the same index, rounded once */
+  /* double */
+  const double *r64, *tz64, *bz64, *norm64, *v164, *ih64;
+  double idr64, r_last64, dx64, p64[3], idx64, fv64, rmin64, rmax64;
+} cg_imap_args;
+
+/* One listed cell. */
+typedef struct {
+  float temp, drr, edrr;
+  int j;      /* shell of the cell's corner radius: its nsub */
+  int single; /* every sample's shifted radius certainly in shell j + delta */
+  int delta;
+} cg_imap_cell;
+
+/* Float lookup with its bound at radius r (0 < r < r_last) whose own bound
+ * is er. */
+CG_HD cg_ve cg_tab_at(const float *tf, int na, float idr, const float *rt, float r, float er)
+{
+  const int ir = (int)CG_MUL(r, idr);
+  const float t = CG_MUL(CG_SUB(r, rt[ir]), idr);
+  const float dt = CG_FMA(CG_FMA(r, CG_E24, er), idr, 4.0f * CG_E24);
+  return cg_tab_ve(tf, na, ir, t, dt);
+}
+
+/* A cell in single precision (imap.c:184-208): returns 0 when the double
+ * arithmetic certainly leaves it out (outside [rmin, rmax] or T(r) <= 0), 1
+ * with *o filled when it certainly lists it, 2 when only double can decide.
+ * d: the cell's density; v: the potential's centred differences
+ * (float - float, as the reference forms them). */
+CG_HD int cg_imap_cell_checked(const cg_imap_args *a, int ix, int iy, int iz, float d, const float v[3],
+                               cg_imap_cell *o)
+{
+  const float x0 = a->xc[ix], y0 = a->yc[iy], z0 = a->zc[iz];
+  const float r2 = CG_FMA(z0, z0, CG_FMA(y0, y0, CG_MUL(x0, x0)));
+  if (!(r2 > 0.0f)) return 0; /* the observer's corner: T = 0 below r = 0 */
+  const float rinv = cg_rsqrt_fast(r2);
+  const float rc = CG_MUL(r2, rinv);
+  const float erc = CG_MUL(rc, 8.0f * CG_E24);
+  if (cg_fabsf(CG_SUB(rc, a->rmax)) <= CG_FMA(cg_fabsf(a->rmax), CG_E24, erc)) return 2;
+  if (cg_fabsf(CG_SUB(rc, a->rmin)) <= CG_FMA(cg_fabsf(a->rmin), CG_E24, erc)) return 2;
+  if (!(rc <= a->rmax && rc >= a->rmin)) return 0;
+  if (!(rc < a->r_last) || cg_fabsf(CG_SUB(rc, a->r_last)) <= erc) return 2;
+  const cg_ve tm = cg_tab_at(a->tz, a->na, a->idr, a->r, rc, erc);
+  if (!(tm.v > tm.e)) return (tm.v == 0.0f && tm.e == 0.0f) ? 0 : 2;
+  const int k = cg_interval(&a->sh, rc);
+  if (!(cg_interval_margin(&a->sh, k, rc) > erc)) return 2;
+  const int j = a->sh.shell_of[k + 1];
+  o->j = j;
+  /* brightness (imap.c:199, 201) and radial shift (imap.c:196-198) */
+  const cg_ve b = cg_tab_at(a->bz, a->na, a->idr, a->r, rc, erc);
+  const cg_ve dn = cg_tab_at(a->norm, a->na, a->idr, a->r, rc, erc);
+  o->temp = CG_MUL(CG_MUL(tm.v, cg_bias_model(d, b.v, a->bias_model)), dn.v);
+  const float u0 = CG_MUL(x0, rinv), u1 = CG_MUL(y0, rinv), u2 = CG_MUL(z0, rinv);
+  const float t0 = CG_MUL(v[0], u0), t1 = CG_MUL(v[1], u1), t2 = CG_MUL(v[2], u2);
+  const float dot = CG_ADD(CG_ADD(t0, t1), t2);
+  const cg_ve v1 = cg_tab_at(a->v1, a->na, a->idr, a->r, rc, erc);
+  const cg_ve ih = cg_tab_at(a->ih, a->na, a->idr, a->r, rc, erc);
+  const float g = CG_MUL(CG_MUL(a->fvh, v1.v), ih.v);
+  o->drr = CG_MUL(dot, g);
+  /* the dot product against the double one (unit vector 2^-22 per
+   * component, products and sums), the tables and the constants */
+  const float sabs = CG_ADD(CG_ADD(cg_fabsf(t0), cg_fabsf(t1)), cg_fabsf(t2));
+  const float erel_t = CG_ADD(CG_DIV(v1.e, cg_fmaxf(cg_fabsf(v1.v), 1e-30f)),
+                              CG_DIV(ih.e, cg_fmaxf(cg_fabsf(ih.v), 1e-30f)));
+  o->edrr = CG_MUL(2.0f, CG_FMA(CG_MUL(cg_fabsf(g), sabs), 12.0f * CG_E24,
+                                CG_MUL(cg_fabsf(o->drr), CG_ADD(erel_t, 8.0f * CG_E24))));
+  /* every sample in one shell?  Sample centres span [c + dxs/2, c + dx -
+   * dxs/2] per axis: the nearest and farthest points of that box */
+  const float hs = CG_MUL(0.5f, a->dxs[j + 1]);
+  const float lo[3] = {CG_ADD(x0, hs), CG_ADD(y0, hs), CG_ADD(z0, hs)};
+  const float hi[3] = {CG_SUB(CG_ADD(x0, a->dx), hs), CG_SUB(CG_ADD(y0, a->dx), hs), CG_SUB(CG_ADD(z0, a->dx), hs)};
+  float n2 = 0.0f, f2 = 0.0f;
+  for (int q = 0; q < 3; q++) {
+    const float nq = lo[q] > 0.0f ? lo[q] : (hi[q] < 0.0f ? hi[q] : 0.0f);
+    const float fq = cg_fmaxf(cg_fabsf(lo[q]), cg_fabsf(hi[q]));
+    n2 = CG_FMA(nq, nq, n2);
+    f2 = CG_FMA(fq, fq, f2);
+  }
+  const float rlo = n2 > 0.0f ? CG_MUL(n2, cg_rsqrt_fast(n2)) : 0.0f;
+  const float rhi = CG_MUL(f2, cg_rsqrt_fast(f2));
+  /* the samples' radii against the double ones: positions within
+   * 2^-24 (|x| + 2 dx) per axis, the radius arithmetic 8 2^-24 */
+  const float er = CG_FMA(rhi, 16.0f * CG_E24, CG_MUL(a->dx, 8.0f * CG_E24));
+  const float e = CG_ADD(CG_ADD(er, o->edrr), CG_MUL(1e-6f, a->dx));
+  const float slo = CG_SUB(CG_ADD(rlo, o->drr), e), shi = CG_ADD(CG_ADD(rhi, o->drr), e);
+  const int kl = cg_interval(&a->sh, slo), kh = cg_interval(&a->sh, shi);
+  o->single = 0;
+  o->delta = 0;
+  if (kl == kh) {
+    const int sh = a->sh.shell_of[kl + 1];
+    if (sh - j >= -1 && sh - j <= 1) {
+      o->single = 1;
+      o->delta = sh - j;
+    }
+  }
+  return 1;
+}
+
+/* The cell in double (imap.c:184-208): 0 when not painted, 1 with the shell
+ * of its corner radius (*j) and the radial shift (*drr). */
+CG_HD int cgx_imap_cell(const cg_imap_args *a, int ix, int iy, int iz, const float v[3], int *j, double *drr)
+{
+  const double x0 = cgx_coord(ix, a->dx64, a->p64[0]), y0 = cgx_coord(iy, a->dx64, a->p64[1]);
+  const double z0 = cgx_coord(iz, a->dx64, a->p64[2]);
+  const double r0 = cgx_norm3(x0, y0, z0);
+  const double tmean = cgx_bg(a->tz64, a->r64, a->idr64, a->r_last64, 0, 0, r0);
+  if (!(r0 <= a->rmax64 && r0 >= a->rmin64)) return 0;
+  if (!(tmean > 0)) return 0;
+  *j = a->sh.shell_of[cgx_interval(&a->sh, r0) + 1];
+  const double u0 = X_DIV(x0, r0), u1 = X_DIV(y0, r0), u2 = X_DIV(z0, r0);
+  const double dot = X_ADD(X_ADD(X_MUL((double)v[0], u0), X_MUL((double)v[1], u1)), X_MUL((double)v[2], u2));
+  const double rvel = X_MUL(a->fv64, X_MUL(X_MUL(0.5, a->idx64), dot));
+  const double v1 = cgx_bg(a->v164, a->r64, a->idr64, a->r_last64, a->v164[0], a->v164[CG_NA - 1], r0);
+  const double ih = cgx_bg(a->ih64, a->r64, a->idr64, a->r_last64, a->ih64[0], a->ih64[CG_NA - 1], r0);
+  *drr = X_MUL(X_MUL(rvel, v1), ih);
+  return 1;
+}
+
+/* A sample in single precision (imap.c:210-231): sub-cell (sx, sy, sz) of
+ * the listed cell c at (ix, iy, iz) with nsub ns.  Returns 1 with the shell
+ * (*s, maybe -1 or nr: not painted) and the RING pixel when the double
+ * arithmetic certainly agrees, 0 when only double can decide. */
+CG_HD int cg_imap_sample_checked(const cg_imap_args *a, int ix, int iy, int iz, const cg_imap_cell *c, int ns,
+                                 int sx, int sy, int sz, int *s, long long *pix)
+{
+  const float dxs = a->dxs[c->j + 1];
+  const float x = CG_ADD(a->xc[ix], CG_FMA(CG_ADD((float)sx, 0.5f), dxs, a->xl[ix]));
+  const float y = CG_ADD(a->yc[iy], CG_FMA(CG_ADD((float)sy, 0.5f), dxs, a->yl[iy]));
+  const float z = CG_ADD(a->zc[iz], CG_FMA(CG_ADD((float)sz, 0.5f), dxs, a->zl[iz]));
+  (void)ns;
+  const cg_dir dr = cg_dir_of(x, y, z, 0.0f);
+  /* coordinates within 2^-24 (|x| + 2 dx) of the double ones */
+  const float ein = CG_MUL(1.8f * CG_E24, CG_FMA(2.0f * a->dx, dr.rinv, 1.0f));
+  int sh;
+  if (c->single) {
+    sh = c->j + c->delta;
+  } else {
+    const float r = CG_MUL(dr.r2, dr.rinv);
+    const float rs = CG_ADD(r, c->drr);
+    const float e = CG_ADD(CG_FMA(r, CG_ADD(8.0f * CG_E24, ein), c->edrr), CG_MUL(2.0f * CG_E24, cg_fabsf(rs)));
+    const int k = cg_interval(&a->sh, rs);
+    if (!(cg_interval_margin(&a->sh, k, rs) > e)) return 0;
+    sh = a->sh.shell_of[k + 1];
+  }
+  *s = sh;
+  if (sh < 0 || sh >= a->sh.nr) return 1;
+  cg_dir d2 = dr;
+  d2.ecth = CG_FMA(2.0f, ein, d2.ecth);
+  const long long p = cg_pix_checked(&d2, a->nside, ein);
+  if (p < 0) return 0;
+  *pix = p;
+  return 1;
+}
+
+/* The sample in double (imap.c:210-231). */
+CG_HD void cgx_imap_sample(const cg_imap_args *a, int ix, int iy, int iz, int ns, double drr, int sx, int sy, int sz,
+                           int *s, long long *pix)
+{
+  const double dxs = X_DIV(a->dx64, (double)ns);
+  const double x = X_ADD(cgx_coord(ix, a->dx64, a->p64[0]), X_MUL(X_ADD((double)sx, 0.5), dxs));
+  const double y = X_ADD(cgx_coord(iy, a->dx64, a->p64[1]), X_MUL(X_ADD((double)sy, 0.5), dxs));
+  const double z = X_ADD(cgx_coord(iz, a->dx64, a->p64[2]), X_MUL(X_ADD((double)sz, 0.5), dxs));
+  double r, cth, phi;
+  cgx_cart2sph(x, y, z, &r, &cth, &phi);
+  *s = a->sh.shell_of[cgx_interval(&a->sh, X_ADD(r, drr)) + 1];
+  if (*s >= 0 && *s < a->sh.nr) *pix = cgx_ang2pix(a->nside, cth, phi);
+}
+
+/* Host set-up of a species' shells (imap_preproc, imap.c:105-133, and the
+ * sub-sampling factors, imap.c:153-174): the float edges sorted by r0
+ * (stable), the distinct edge values b (nb of them), the shell of each
+ * interval, nsub and dx/nsub of shells -1 .. nr.  Arrays: r0f, rff, nr
+ * floats; b, 2 nr floats; shell_of, 2 nr + 1 ints; nsub and dxs, nr + 2.
+ * Returns nb. */
+static inline int cg_imap_shells(const double *r0d, const double *rfd, int nr, double dx, long long npix,
+                                 float *r0f, float *rff, float *b, int *shell_of, int *nsub, float *dxs)
+{
+  for (int i = 0; i < nr; i++) {
+    r0f[i] = (float)r0d[i];
+    rff[i] = (float)rfd[i];
+  }
+  for (int i = 1; i < nr; i++) /* stable insertion sort by r0 */
+    for (int k = i; k > 0 && r0f[k] < r0f[k - 1]; k--) {
+      float t = r0f[k];
+      r0f[k] = r0f[k - 1];
+      r0f[k - 1] = t;
+      t = rff[k];
+      rff[k] = rff[k - 1];
+      rff[k - 1] = t;
+    }
+  int nb = 0;
+  for (int i = 0; i < nr; i++) {
+    b[nb++] = r0f[i];
+    b[nb++] = rff[i];
+  }
+  for (int i = 1; i < nb; i++)
+    for (int k = i; k > 0 && b[k] < b[k - 1]; k--) {
+      const float t = b[k];
+      b[k] = b[k - 1];
+      b[k - 1] = t;
+    }
+  int m = 0;
+  for (int i = 0; i < nb; i++)
+    if (m == 0 || b[i] != b[m - 1]) b[m++] = b[i];
+  nb = m;
+  /* the walk from shell 0 at each interval's lower edge */
+  float rfm[4096];
+  for (int i = 0; i < nr && i < 4096; i++) rfm[i] = i == 0 ? rff[0] : (rff[i] > rfm[i - 1] ? rff[i] : rfm[i - 1]);
+  for (int k = -1; k < nb; k++) {
+    const float r = k < 0 ? b[0] - 1.0f : b[k];
+    shell_of[k + 1] = cg_shell_index0(r0f, rfm, nr, r);
+  }
+  const double ps = sqrt(4 * 3.14159265358979323846 / (double)npix);
+  for (int i = -1; i <= nr; i++) {
+    const int q = i < 0 ? 0 : (i >= nr ? nr - 1 : i);
+    const double a0 = r0f[q], a1 = rff[q];
+    const double vol = (a1 * a1 * a1 - a0 * a0 * a0) * ps * ps / 3;
+    const double sc0 = fmin(pow(vol, 0.333333), fmin(a0 * ps, a1 - a0));
+    nsub[i + 1] = (int)(dx / sc0 + 0.5) + 1;
+    dxs[i + 1] = (float)(dx / nsub[i + 1]);
+  }
+  return nb;
 }
 
 #endif /* CG_EXACT_H */

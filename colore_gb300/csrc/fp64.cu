@@ -461,7 +461,8 @@ __device__ double rvel64(const P64 &p, const double *npot, int ix, int iy, int i
   const double v0 = npot[pid(p, xh, iy, iz)] - npot[pid(p, xl, iy, iz)];
   const double v1 = npot[pid(p, ix, yh, iz)] - npot[pid(p, ix, yl, iz)];
   const double v2 = npot[pid(p, ix, iy, zh)] - npot[pid(p, ix, iy, zl)];
-  return 0.5 * p.idx * (v0 * x0 / rr + v1 * y0 / rr + v2 * z0 / rr);
+  const double u0 = x0 / rr, u1 = y0 / rr, u2 = z0 / rr; /* get_rvel, imap.c:65-73 */
+  return 0.5 * p.idx * (v0 * u0 + v1 * u1 + v2 * u2);
 }
 
 /* srcs_set_cartesian_single pass 2 (srcs.c:186-283) with the local

@@ -5,37 +5,38 @@
  * Every cell in the radial range of the shells carries a brightness
  * temp = T(r) bias_model(d, b(r)) norm(r) and a redshift-space shift dr_rsd;
  * it is split into nsub^3 sub-cells whose centres are placed in a shell (by
- * r + dr_rsd) and a RING pixel, where temp is added and a hit counted.
+ * r + dr_rsd) and a RING pixel, where temp is added and a hit counted.  The
+ * shells and pixels are decided as the reference's double arithmetic
+ * decides them: in single precision where a bound on the distance to the
+ * double value proves the decision, in double otherwise (cg_exact.h), so the
+ * hit counts are those of the double arithmetic.
  *
- * The work per cell is nsub^3 and nsub grows as 1/r towards the observer
- * (the sub-cell follows the pixel size r * sqrt(4 pi / npix)): from 8 samples
- * per cell at high redshift to thousands near the observer.  So the cells
- * are first listed and their samples then painted as one even stream:
+ * nsub is fixed by the shell of the cell's corner radius and grows towards
+ * the observer (from 2 at high redshift to ~20 for the nearest shells), so
+ * cells are listed per shell -- one bucket per shell, holding cells of one
+ * nsub -- and painted bucket after bucket:
  *
- *   k_imap_cells  Warps take groups of whole rows from a counter; a lane
- *                 computes one cell's brightness, radial shift, shell and
- *                 nsub and appends the cell to the list (one atomic per warp).
- *                 Cells past the list's capacity are painted here, 32
- *                 consecutive samples of the warp's cells at a time.
- *   k_scan_*      exclusive scan of the listed cells' sample counts: the
- *                 first sample of every listed cell.
- *   k_imap_paint  The listed samples are cut into 8 chunks per warp, taken
- *                 from a counter; a warp finds the first cell of its chunk by
- *                 binary search on the offsets and paints 32 consecutive
- *                 samples at a time, each lane walking forward to its cell.
- *
- * Consecutive samples (x fastest) of a cell often land on the same (shell,
- * pixel); each run of equal keys across the lanes is found with one shuffle
- * and a ballot and added to the maps once, with one float and one integer
- * atomic (data += temp * run, nadd += run).  GB300's L2 sustains these
- * without staging: a shared-memory hash table that merged the runs of a
- * warp before the global atomics was measured slower at every nsub.  Keys
- * (shell * npix + pixel) are 32-bit when nr * npix < 2^32 - 1.
+ *   k_imap_list    Warps take groups of rows from a counter; a lane decides
+ *                  one cell (listed or not, its shell, brightness, radial
+ *                  shift, and whether all its samples certainly stay in one
+ *                  shell, which spares them the radial test) and appends it
+ *                  to its bucket with one atomic per bucket and warp.  A cell
+ *                  that finds its bucket full is painted by its warp on the
+ *                  spot.
+ *   k_imap_chunks  One thread cuts each bucket into chunks of about CHS
+ *                  samples: whole cells, or slices of one cell.
+ *   k_imap_paint   Warps take chunks in bucket order, so the maps' working
+ *                  set at any time is a few shells (25 MB per shell at nside
+ *                  512) and the atomics stay in L2.  32 consecutive samples
+ *                  per step; runs of equal (cell, shell, pixel) across the
+ *                  lanes are added with one float and one integer atomic.
+ *                  Samples whose margins fail are queued.
+ *   k_imap_double  One thread per queued sample: the cell's radial shift and
+ *                  the sample's shell and pixel in double, then its atomics.
  */
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
-
-#include <algorithm>
 
 #include "cg_dev.cuh"
 #include "imap_api.h"
@@ -43,16 +44,59 @@
 namespace {
 using namespace cg;
 
-constexpr int IW = 4;          /* warps per block                        */
-constexpr int ROWS = 4;        /* rows per fetch in k_imap               */
-constexpr int CHUNKS = 8;      /* sample chunks per warp in k_imap_paint */
-constexpr int SCAN_T = 256;    /* threads per block of the offset scan    */
-constexpr int SCAN_I = 16;     /* records per thread of the offset scan   */
+constexpr int IW = 4;     /* warps per block                     */
+constexpr int ROWS = 2;   /* rows per fetch in k_imap_list        */
+constexpr int CHS = 2048; /* samples per painting chunk           */
+constexpr unsigned FULL = 0xffffffffu;
+constexpr unsigned F_SINGLE = 1u, F_DOUBLE = 8u;
 
-struct CellPar {
-  float x0, temp, drr, dxs, inv_ns;
-  int nsub, irad0, pad;
+/* Per-block copies of the species' shell tables. */
+struct Sh {
+  float *b, *dxs, *invns;
+  int *shell_of, *nsub;
+  unsigned long long *chunk_off;
 };
+
+__host__ __device__ __forceinline__ size_t shell_smem(int nr, int nbk, bool chunks)
+{
+  size_t n = (size_t)(2 * nr) * 4 + (size_t)(2 * nr + 1) * 4 + 3 * (size_t)(nr + 2) * 4;
+  n = (n + 7) & ~(size_t)7;
+  if (chunks) n += (size_t)(nbk + 1) * 8;
+  return n;
+}
+
+__device__ __forceinline__ Sh load_shells(const cg_imap_params &p, unsigned char *raw, bool chunks)
+{
+  const int nr = p.nr, nb = p.a.sh.nb;
+  Sh s;
+  s.b = reinterpret_cast<float *>(raw);
+  s.shell_of = reinterpret_cast<int *>(s.b + 2 * nr);
+  s.nsub = s.shell_of + 2 * nr + 1;
+  s.dxs = reinterpret_cast<float *>(s.nsub + nr + 2);
+  s.invns = s.dxs + nr + 2;
+  size_t off = shell_smem(nr, p.nbk, false);
+  s.chunk_off = reinterpret_cast<unsigned long long *>(raw + off);
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) s.b[i] = p.a.sh.b[i];
+  for (int i = threadIdx.x; i <= nb; i += blockDim.x) s.shell_of[i] = p.a.sh.shell_of[i];
+  for (int i = threadIdx.x; i < nr + 2; i += blockDim.x) {
+    s.nsub[i] = p.a.nsub[i];
+    s.dxs[i] = p.a.dxs[i];
+    s.invns[i] = 1.0f / (float)p.a.nsub[i];
+  }
+  if (chunks)
+    for (int i = threadIdx.x; i <= p.nbk; i += blockDim.x) s.chunk_off[i] = p.chunk_off[i];
+  return s;
+}
+
+__device__ __forceinline__ cg_imap_args args_with(const cg_imap_params &p, const Sh &s)
+{
+  cg_imap_args A = p.a;
+  A.sh.b = s.b;
+  A.sh.shell_of = s.shell_of;
+  A.nsub = s.nsub;
+  A.dxs = s.dxs;
+  return A;
+}
 
 template <typename K>
 __device__ __forceinline__ K empty_key()
@@ -60,44 +104,22 @@ __device__ __forceinline__ K empty_key()
   return (K)~(K)0;
 }
 
-/* Key of sample q (0 <= q < ns^3, x fastest, then y, then z) of cell c, whose
- * corner is (c.x0, y0, z0), or the empty key outside the shells. */
 template <typename K>
-__device__ __forceinline__ K sample_key(const cg_imap_params &p, const float *r0, const float *rf, const CellPar &c,
-                                        float y0, float z0, int q)
+__device__ __forceinline__ K key_of(const cg_imap_params &p, int s, long long pix)
 {
-  const int ns = c.nsub;
-  int line, izz;
-  if (ns <= 128) {
-    /* (q + 1/2)/ns is at least 1/(2 ns) from an integer and the float
-     * product is within ns^2 2^-23 of it: exact while ns^3 < 2^22 */
-    line = (int)(((float)q + 0.5f) * c.inv_ns);
-    izz = (int)(((float)line + 0.5f) * c.inv_ns);
-  } else {
-    line = q / ns;
-    izz = line / ns;
-  }
-  const int ixx = q - line * ns, iyy = line - izz * ns;
-  const float zc = cg_sub_centre(z0, izz, c.dxs);
-  const float yc = cg_sub_centre(y0, iyy, c.dxs);
-  const float yz2 = cg_yz2(yc, zc);
-  const float xc = cg_sub_centre(c.x0, ixx, c.dxs);
-  int64_t pix = 0;
-  const int ir = cg_imap_sample(xc, yc, zc, yz2, c.drr, r0, rf, p.nr, c.irad0, p.nside, &pix);
-  if (ir < 0 || ir >= p.nr) return empty_key<K>();
-  if (sizeof(K) == 4) return (K)((unsigned)ir * (unsigned)p.npix + (unsigned)pix);
-  return (K)((long long)ir * p.npix + pix);
+  if (s < 0 || s >= p.nr) return empty_key<K>();
+  if (sizeof(K) == 4) return (K)((unsigned)s * (unsigned)p.npix + (unsigned)pix);
+  return (K)((long long)s * p.npix + pix);
 }
 
 /* The lanes hold consecutive samples: each run of equal (tag, key) is added
  * to the maps once, by its first lane, with its length (data += temp * run,
  * nadd += run).  tag separates cells, whose brightness differs. */
 template <typename K>
-__device__ __forceinline__ void add_runs(K key, int tag, float temp, int lane, const cg_imap_params &p)
+__device__ __forceinline__ void add_runs(K key, long long tag, float temp, int lane, const cg_imap_params &p)
 {
-  const unsigned FULL = 0xffffffffu;
   const K pk = __shfl_up_sync(FULL, key, 1);
-  const int pt = __shfl_up_sync(FULL, tag, 1);
+  const long long pt = __shfl_up_sync(FULL, tag, 1);
   const bool valid = key != empty_key<K>();
   const bool head = valid && (lane == 0 || pk != key || pt != tag);
   const unsigned bnd = __ballot_sync(FULL, head || !valid);
@@ -110,390 +132,390 @@ __device__ __forceinline__ void add_runs(K key, int tag, float temp, int lane, c
   }
 }
 
-template <typename K>
-__global__ void __launch_bounds__(IW * 32, 16) k_imap_cells(const float *__restrict__ dens, const float *__restrict__ phi,
-                                                     cg_imap_params p)
+/* Sub-cell (sx, sy, sz) of sample q < ns^3, x fastest. */
+__device__ __forceinline__ void sub_of(int q, int ns, float inv_ns, int *sx, int *sy, int *sz)
 {
-  extern __shared__ unsigned char sraw[];
-  CellPar *cells = reinterpret_cast<CellPar *>(sraw);
-  float4 *shp = reinterpret_cast<float4 *>(cells + IW * 32);
-  float *r0 = reinterpret_cast<float *>(shp + p.nr + 2);
-  float *rf = r0 + p.nr;
-  float *rfm = rf + p.nr; /* running maximum of rf, for cg_shell_index0 */
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  CellPar *wc = cells + wid * 32;
-  for (int i = threadIdx.x; i < p.nr; i += blockDim.x) {
-    r0[i] = p.r0[i];
-    rf[i] = p.rf[i];
+  int line, z;
+  if (ns <= 128) {
+    /* (q + 1/2)/ns is at least 1/(2 ns) from an integer and the float
+     * product is within ns^2 2^-23 of it: exact while ns^3 < 2^22 */
+    line = (int)(((float)q + 0.5f) * inv_ns);
+    z = (int)(((float)line + 0.5f) * inv_ns);
+  } else {
+    line = q / ns;
+    z = line / ns;
   }
-  for (int i = threadIdx.x; i < p.nr + 2; i += blockDim.x) shp[i] = p.shp[i];
+  *sx = q - line * ns;
+  *sy = line - z * ns;
+  *sz = z;
+}
+
+/* Centred potential differences at a cell (get_rvel, imap.c:43-74): float
+ * minus float, as the reference forms them from its float grid. */
+__device__ __forceinline__ void grad_phi(const float *__restrict__ phi, int ix, int iy, int iz, int N, float v[3])
+{
+  v[0] = CG_SUB(__ldg(&phi[pidx(wrap(ix + 1, N), iy, iz, N)]), __ldg(&phi[pidx(wrap(ix - 1, N), iy, iz, N)]));
+  v[1] = CG_SUB(__ldg(&phi[pidx(ix, wrap(iy + 1, N), iz, N)]), __ldg(&phi[pidx(ix, wrap(iy - 1, N), iz, N)]));
+  v[2] = CG_SUB(__ldg(&phi[pidx(ix, iy, wrap(iz + 1, N), N)]), __ldg(&phi[pidx(ix, iy, wrap(iz - 1, N), N)]));
+}
+
+/* Brightness of a cell whose decisions were taken in double (imap.c:199,
+ * 201), in single precision like every other cell's. */
+__device__ __forceinline__ float temp32(const cg_imap_args &A, int ix, int iy, int iz, float d)
+{
+  const float x0 = A.xc[ix], y0 = A.yc[iy], z0 = A.zc[iz];
+  const float r2 = CG_FMA(z0, z0, CG_FMA(y0, y0, CG_MUL(x0, x0)));
+  const float rc = CG_MUL(r2, cg_rsqrt_fast(r2));
+  const float tm = cg_tab_at(A.tz, A.na, A.idr, A.r, rc, 0.0f).v;
+  const float b = cg_tab_at(A.bz, A.na, A.idr, A.r, rc, 0.0f).v;
+  const float dn = cg_tab_at(A.norm, A.na, A.idr, A.r, rc, 0.0f).v;
+  return CG_MUL(CG_MUL(tm, cg_bias_model(d, b, A.bias_model)), dn);
+}
+
+__device__ __forceinline__ cg_imap_rec pack(int ix, int iy, int iz, const cg_imap_cell &c, unsigned flags)
+{
+  cg_imap_rec r;
+  r.ixy = (unsigned)ix | ((unsigned)iy << 16);
+  const unsigned short eh = __half_as_ushort(__float2half_ru(c.edrr));
+  r.izf = (unsigned)iz | (flags << 12) | ((unsigned)eh << 16);
+  r.temp = c.temp;
+  r.drr = c.drr;
+  return r;
+}
+
+__device__ __forceinline__ cg_imap_cell unpack(const cg_imap_rec &r, int j, int *ix, int *iy, int *iz, int *dbl)
+{
+  cg_imap_cell c;
+  *ix = (int)(r.ixy & 0xffffu);
+  *iy = (int)(r.ixy >> 16);
+  *iz = (int)(r.izf & 0xfffu);
+  const unsigned f = (r.izf >> 12) & 0xfu;
+  c.single = (f & F_SINGLE) ? 1 : 0;
+  c.delta = (int)((f >> 1) & 3u) - 1;
+  *dbl = (f & F_DOUBLE) ? 1 : 0;
+  c.edrr = __half2float(__ushort_as_half((unsigned short)(r.izf >> 16)));
+  c.temp = r.temp;
+  c.drr = r.drr;
+  c.j = j;
+  return c;
+}
+
+/* A sample of a cell the listing kernel paints itself: its double decision,
+ * when needed, on the spot. */
+template <typename K>
+__device__ __noinline__ K sample_key_inline(const cg_imap_params &p, const cg_imap_args &A, const float *phi, int ix,
+                                            int iy, int iz, const cg_imap_cell &c, int dbl, int ns, int q,
+                                            float inv_ns)
+{
+  int sx, sy, sz, s = -1;
+  long long pix = 0;
+  sub_of(q, ns, inv_ns, &sx, &sy, &sz);
+  if (dbl || p.force_double || !cg_imap_sample_checked(&A, ix, iy, iz, &c, ns, sx, sy, sz, &s, &pix)) {
+    float v[3];
+    grad_phi(phi, ix, iy, iz, p.box.N, v);
+    int j;
+    double drr = 0;
+    cgx_imap_cell(&A, ix, iy, iz, v, &j, &drr);
+    cgx_imap_sample(&A, ix, iy, iz, ns, drr, sx, sy, sz, &s, &pix);
+    atomicAdd(p.xstats + 3, 1ull);
+  }
+  return key_of<K>(p, s, pix);
+}
+
+template <typename K>
+__global__ void __launch_bounds__(IW * 32) k_imap_list(const float *__restrict__ dens, const float *__restrict__ phi,
+                                                       cg_imap_params p)
+{
+  extern __shared__ __align__(16) unsigned char sraw[];
+  const Sh sh = load_shells(p, sraw, false);
   __syncthreads();
-  if (threadIdx.x == 0)
-    for (int i = 0; i < p.nr; i++) rfm[i] = i == 0 ? rf[0] : (rf[i] > rfm[i - 1] ? rf[i] : rfm[i - 1]);
-  __syncthreads();
+  const cg_imap_args A = args_with(p, sh);
+  const int lane = threadIdx.x & 31;
   const int N = p.box.N;
-  const int nch = (N + 31) / 32;
-  const int nrow = N * N;
-  const float dx = p.box.dx;
-  const unsigned FULL = 0xffffffffu;
-  unsigned long long painted = 0; /* samples of the cells painted by this lane */
+  const int nrow = N * N, nch = (N + 31) / 32;
+  const float rlo = A.rmin - 1.0f, rhi = A.rmax + 1.0f;
+  unsigned long long drawn = 0, ndbl = 0;
   for (;;) {
     int rbeg = 0;
-    if (lane == 0) rbeg = (int)atomicAdd(&p.ctr[2], (unsigned long long)ROWS);
+    if (lane == 0) rbeg = (int)atomicAdd(&p.ctr[1], (unsigned long long)ROWS);
     rbeg = __shfl_sync(FULL, rbeg, 0);
-    if (rbeg >= nrow) {
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) painted += __shfl_xor_sync(FULL, painted, o);
-      if (lane == 0 && painted) atomicAdd(&p.ctr[3], painted);
-      break;
-    }
+    if (rbeg >= nrow) break;
     const int rend = rbeg + ROWS < nrow ? rbeg + ROWS : nrow;
-    /* whether a cell is listed depends on its radius alone: count the row
-     * group's listed cells first and reserve their slots with one atomic */
-    int nlist = 0;
-    for (int row = rbeg; row < rend; row++) {
-      const int iz = row / N, iy = row - iz * N;
-      const float y0 = cg_cell_coord(iy, dx, p.box.p1), z0 = cg_cell_coord(iz, dx, p.box.p2);
-      for (int ix = lane; ix < N; ix += 32) {
-        const float rc = cg_norm3(cg_cell_coord(ix, dx, p.box.p0), y0, z0);
-        nlist += (rc <= p.rmax_here && rc >= p.rmin_here && bgv(p.tz, bg_at(p.g, rc)) > 0.0f) ? 1 : 0;
-      }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) nlist += __shfl_xor_sync(FULL, nlist, o);
-    unsigned long long next = 0; /* the warp's next slot */
-    if (lane == 0 && nlist > 0) {
-      /* once the list is full the counter overshoots its capacity by at most
-       * one row group per warp in flight */
-      const unsigned long long cur = *(volatile unsigned long long *)&p.ctr[0];
-      next = cur < (unsigned long long)p.list_cap ? atomicAdd(&p.ctr[0], (unsigned long long)nlist)
-                                                  : (unsigned long long)p.list_cap;
-    }
-    next = __shfl_sync(FULL, next, 0);
     for (int row = rbeg; row < rend; row++)
-    for (int ch = 0; ch < nch; ch++) {
-      const int iz = row / N, iy = row - iz * N;
-      const int ix = ch * 32 + lane;
-      const float y0 = cg_cell_coord(iy, dx, p.box.p1), z0 = cg_cell_coord(iz, dx, p.box.p2);
-      CellPar cp = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0, 0, 0};
-      int n = 0;
-      bool lst = false; /* the condition counted in the first pass */
-      if (ix < N) {
-        cp.x0 = cg_cell_coord(ix, dx, p.box.p0);
-        const float rc = cg_norm3(cp.x0, y0, z0);
-        const BgAt at = bg_at(p.g, rc);
-        const float tmean = bgv(p.tz, at);
-        lst = rc <= p.rmax_here && rc >= p.rmin_here && tmean > 0.0f;
-        if (lst) {
-          const float bias = bgv(p.bz, at);
-          const float dnorm = bgvn(p.norm, at);
-          const int xh = wrap(ix + 1, N), xl = wrap(ix - 1, N);
-          const int yh = wrap(iy + 1, N), yl = wrap(iy - 1, N);
-          const int zh = wrap(iz + 1, N), zl = wrap(iz - 1, N);
-          float v0 = CG_SUB(__ldg(&phi[pidx(xh, iy, iz, N)]), __ldg(&phi[pidx(xl, iy, iz, N)]));
-          float v1 = CG_SUB(__ldg(&phi[pidx(ix, yh, iz, N)]), __ldg(&phi[pidx(ix, yl, iz, N)]));
-          float v2 = CG_SUB(__ldg(&phi[pidx(ix, iy, zh, N)]), __ldg(&phi[pidx(ix, iy, zl, N)]));
-          float rvel = CG_MUL(p.factor_vel, cg_rvel(v0, v1, v2, cp.x0, y0, z0, rc, p.box.idx));
-          cp.drr = cg_imap_drsd(rvel, bgv(p.v1, at), bgv(p.ih, at));
-          const float d = __ldg(&dens[pidx(ix, iy, iz, N)]);
-          cp.temp = cg_imap_temp(tmean, d, bias, dnorm, p.bias_model);
-          cp.irad0 = cg_shell_index0(r0, rfm, p.nr, rc);
-          /* nsub of the cell's shell (the first one below the shells, the
-           * last one beyond or in a gap), with dx / nsub and 1 / nsub */
-          const float4 sp = shp[cp.irad0 + 1];
-          const int ns = __float_as_int(sp.x);
-          if (ns < 1 || ns > 1024) {
-            atomicOr(p.err, ERR_IMAP_NSUB);
-          } else {
-            cp.nsub = ns;
-            cp.dxs = sp.y;
-            cp.inv_ns = sp.z;
-            n = ns * ns * ns;
+      for (int ch = 0; ch < nch; ch++) {
+        const int iz = row / N, iy = row - iz * N;
+        const int ix = ch * 32 + lane;
+        cg_imap_cell c;
+        bool want = false; /* listed and painted */
+        int dbl = 0;
+        float d = 0.0f;
+        if (ix < N) {
+          const float x0 = A.xc[ix], y0 = A.yc[iy], z0 = A.zc[iz];
+          const float r2 = CG_FMA(z0, z0, CG_FMA(y0, y0, CG_MUL(x0, x0)));
+          if (r2 >= rlo * rlo * (rlo > 0.0f ? 1.0f : 0.0f) && r2 <= rhi * rhi) {
+            d = __ldg(&dens[pidx(ix, iy, iz, N)]);
+            float v[3];
+            grad_phi(phi, ix, iy, iz, N, v);
+            int st = cg_imap_cell_checked(&A, ix, iy, iz, d, v, &c);
+            if (p.force_double && st == 1) st = 2;
+            if (st == 2) {
+              ndbl++;
+              int j;
+              double drr;
+              if (cgx_imap_cell(&A, ix, iy, iz, v, &j, &drr)) {
+                c.j = j;
+                c.temp = temp32(A, ix, iy, iz, d);
+                c.drr = (float)drr;
+                c.edrr = 0.0f;
+                c.single = 0;
+                c.delta = 0;
+                dbl = 1;
+                st = 1;
+              } else {
+                st = 0;
+              }
+            }
+            if (st == 1) {
+              const int ns = A.nsub[c.j + 1];
+              drawn += (unsigned long long)ns * ns * ns;
+              const int sfin = c.j + c.delta;
+              want = !(c.single && (sfin < 0 || sfin >= p.nr));
+            }
           }
         }
-      }
-      /* every cell goes to the list, in the slots reserved above; past its
-       * capacity it is painted here */
-      const unsigned lm = __ballot_sync(FULL, lst);
-      if (lm) {
-        const long long slot = (long long)next + __popc(lm & ((1u << lane) - 1u));
-        next += (unsigned long long)__popc(lm);
-        if (lst && slot < p.list_cap) {
-          float4 *q = reinterpret_cast<float4 *>(p.cells + slot);
-          q[0] = make_float4(cp.x0, y0, z0, cp.temp);
-          q[1] = make_float4(cp.drr, cp.dxs, cp.inv_ns, __int_as_float(cp.nsub | ((cp.irad0 + 1) << 11)));
-          p.cell_n[slot] = (unsigned int)n;
-          n = 0;
+        /* append to the buckets: one atomic per bucket present in the warp */
+        bool over = false;
+        long long slot = 0;
+        unsigned m = __ballot_sync(FULL, want);
+        const int bk = want ? c.j + 1 : -1;
+        while (m) {
+          const int leader = __ffs(m) - 1;
+          const int bb = __shfl_sync(FULL, bk, leader);
+          const unsigned same = __ballot_sync(FULL, want && bk == bb);
+          unsigned long long old = 0;
+          if (lane == leader) old = atomicAdd(&p.cnt[bb], (unsigned long long)__popc(same));
+          old = __shfl_sync(FULL, old, leader);
+          if (same & (1u << lane)) {
+            const long long k = (long long)old + __popc(same & ((1u << lane) - 1u));
+            if (k < p.cap[bb]) slot = p.base[bb] + k;
+            else over = true;
+          }
+          m &= ~same;
+        }
+        if (want && !over)
+          p.recs[slot] = pack(ix, iy, iz, c, (c.single ? F_SINGLE : 0u) | ((unsigned)(c.delta + 1) << 1) |
+                                                  (dbl ? F_DOUBLE : 0u));
+        /* cells past their bucket's room: painted here by the warp */
+        unsigned om = __ballot_sync(FULL, want && over);
+        while (om) {
+          const int l = __ffs(om) - 1;
+          om &= om - 1;
+          const int cx = __shfl_sync(FULL, ix, l);
+          cg_imap_cell cc;
+          cc.j = __shfl_sync(FULL, c.j, l);
+          cc.temp = __shfl_sync(FULL, c.temp, l);
+          cc.drr = __shfl_sync(FULL, c.drr, l);
+          cc.edrr = __shfl_sync(FULL, c.edrr, l);
+          cc.single = __shfl_sync(FULL, c.single, l);
+          cc.delta = __shfl_sync(FULL, c.delta, l);
+          const int cd = __shfl_sync(FULL, dbl, l);
+          const int ns = A.nsub[cc.j + 1];
+          const int n3 = ns * ns * ns;
+          const float inv = sh.invns[cc.j + 1];
+          const long long tag = ((long long)row << 16) | cx;
+          for (int q0 = 0; q0 < n3; q0 += 32) {
+            const int q = q0 + lane;
+            K key = empty_key<K>();
+            if (q < n3) key = sample_key_inline<K>(p, A, phi, cx, iy, iz, cc, cd, ns, q, inv);
+            add_runs(key, tag, cc.temp, lane, p);
+          }
+          if (lane == 0) atomicAdd(&p.ctr[3], (unsigned long long)n3);
         }
       }
-      /* cells painted here keep the warp's sample count below 2^26 */
-      if (n > 0 && cp.nsub > 128) {
-        atomicOr(p.err, ERR_IMAP_HEAVY);
-        n = 0;
-      }
-      if (!__any_sync(FULL, n > 0)) continue;
-      wc[lane] = cp;
-      painted += (unsigned long long)n;
-      /* inclusive scan of the sample counts (nsub^3 per cell) over the warp */
-      int incl = n;
+  }
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        int t = __shfl_up_sync(FULL, incl, o);
-        if (lane >= o) incl += t;
-      }
-      const int excl = incl - n;
-      const int total = __shfl_sync(FULL, incl, 31);
-      __syncwarp();
-      for (int base = 0; base < total; base += 32) {
-        const int s = base + lane;
-        /* owning lane j = number of lanes whose inclusive prefix is <= s */
-        int j = 0;
-#pragma unroll
-        for (int st = 16; st > 0; st >>= 1) {
-          int v = __shfl_sync(FULL, incl, j + st - 1);
-          if (v <= s) j += st;
-        }
-        if (j > 31) j = 31;
-        const int ex = __shfl_sync(FULL, excl, j);
-        K key = empty_key<K>();
-        float temp = 0.0f;
-        if (s < total) {
-          const CellPar c = wc[j];
-          key = sample_key<K>(p, r0, rf, c, y0, z0, s - ex);
-          temp = c.temp;
-        }
-        add_runs(key, j, temp, lane, p);
-      }
-      __syncwarp();
-    }
+  for (int o = 16; o > 0; o >>= 1) {
+    drawn += __shfl_xor_sync(FULL, drawn, o);
+    ndbl += __shfl_xor_sync(FULL, ndbl, o);
+  }
+  if (lane == 0) {
+    if (drawn) atomicAdd(&p.ctr[2], drawn);
+    if (ndbl) atomicAdd(p.xstats + 2, ndbl);
   }
 }
 
-/* Sum of the sample counts of each block of SCAN_T * SCAN_I records. */
-__global__ void __launch_bounds__(SCAN_T) k_scan_sum(const unsigned int *__restrict__ n, long long H, long long *bsum)
+/* Chunks of every bucket: cells of nsub^3 <= CHS samples go CHS / nsub^3
+ * to a chunk; a larger cell is cut into ceil(nsub^3 / CHS) slices. */
+__global__ void k_imap_chunks(cg_imap_params p)
 {
-  const long long i0 = ((long long)blockIdx.x * SCAN_T + threadIdx.x) * SCAN_I;
-  long long t = 0;
-  if (i0 + SCAN_I <= H) { /* 16 records, 64 B aligned */
-#pragma unroll
-    for (int i = 0; i < SCAN_I; i += 4) {
-      const uint4 q = __ldg(reinterpret_cast<const uint4 *>(n + i0 + i));
-      t += (long long)q.x + q.y + q.z + q.w;
-    }
-  } else {
-#pragma unroll
-    for (int i = 0; i < SCAN_I; i++)
-      if (i0 + i < H) t += n[i0 + i];
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-  __shared__ long long ws[SCAN_T / 32];
-  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = t;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    long long b = 0;
-    for (int w = 0; w < SCAN_T / 32; w++) b += ws[w];
-    bsum[blockIdx.x] = b;
-  }
-}
-
-/* Exclusive scan of the nb block sums in place (one block); total -> *total. */
-__global__ void __launch_bounds__(1024) k_scan_top(long long *v, long long nb, unsigned long long *total)
-{
-  __shared__ long long sm[1024];
-  const long long per = (nb + 1023) / 1024;
-  const long long b = (long long)threadIdx.x * per, e = b + per < nb ? b + per : nb;
-  long long acc = 0;
-  for (long long i = b; i < e; i++) acc += v[i];
-  sm[threadIdx.x] = acc;
-  __syncthreads();
-  for (int o = 1; o < 1024; o <<= 1) {
-    const long long t = (int)threadIdx.x >= o ? sm[threadIdx.x - o] : 0;
-    __syncthreads();
-    sm[threadIdx.x] += t;
-    __syncthreads();
-  }
-  long long run = sm[threadIdx.x] - acc;
-  for (long long i = b; i < e; i++) {
-    const long long x = v[i];
-    v[i] = run;
-    run += x;
-  }
-  if (threadIdx.x == 1023) *total = (unsigned long long)sm[1023];
-}
-
-/* First sample of every record: block offset + in-block exclusive scan. */
-__global__ void __launch_bounds__(SCAN_T) k_scan_out(const unsigned int *__restrict__ n, long long H,
-                                                      const long long *__restrict__ bexcl, long long *off)
-{
-  const long long i0 = ((long long)blockIdx.x * SCAN_T + threadIdx.x) * SCAN_I;
-  const bool full = i0 + SCAN_I <= H; /* a thread's 16 records, 64 B aligned */
-  unsigned int v[SCAN_I];
-  long long t = 0;
-  if (full) {
-#pragma unroll
-    for (int i = 0; i < SCAN_I; i += 4) {
-      const uint4 q = __ldg(reinterpret_cast<const uint4 *>(n + i0 + i));
-      v[i] = q.x;
-      v[i + 1] = q.y;
-      v[i + 2] = q.z;
-      v[i + 3] = q.w;
-    }
-  } else {
-#pragma unroll
-    for (int i = 0; i < SCAN_I; i++) v[i] = i0 + i < H ? n[i0 + i] : 0u;
-  }
-#pragma unroll
-  for (int i = 0; i < SCAN_I; i++) t += v[i];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  long long inc = t;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const long long u = __shfl_up_sync(0xffffffffu, inc, o);
-    if (lane >= o) inc += u;
-  }
-  __shared__ long long ws[SCAN_T / 32];
-  if (lane == 31) ws[wid] = inc;
-  __syncthreads();
-  long long run = bexcl[blockIdx.x];
-  for (int w = 0; w < wid; w++) run += ws[w];
-  run += inc - t;
-  if (full) {
-#pragma unroll
-    for (int i = 0; i < SCAN_I; i += 2) {
-      const long long a = run;
-      run += v[i];
-      reinterpret_cast<longlong2 *>(off + i0)[i / 2] = make_longlong2(a, run);
-      run += v[i + 1];
-    }
-  } else {
-#pragma unroll
-    for (int i = 0; i < SCAN_I; i++) {
-      if (i0 + i < H) off[i0 + i] = run;
-      run += v[i];
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  unsigned long long acc = 0;
+  for (int b = 0; b < p.nbk; b++) {
+    p.chunk_off[b] = acc;
+    const unsigned long long n = p.cnt[b] < (unsigned long long)p.cap[b] ? p.cnt[b] : (unsigned long long)p.cap[b];
+    const long long ns = p.a.nsub[b], s3 = ns * ns * ns;
+    if (n == 0) continue;
+    if (s3 <= CHS) {
+      const unsigned long long R = (unsigned long long)(CHS / s3);
+      acc += (n + R - 1) / R;
+    } else {
+      acc += n * (unsigned long long)((s3 + CHS - 1) / CHS);
     }
   }
+  p.chunk_off[p.nbk] = acc;
 }
 
 template <typename K>
-__global__ void __launch_bounds__(IW * 32, 1) k_imap_paint(cg_imap_params p)
+__global__ void __launch_bounds__(IW * 32) k_imap_paint(cg_imap_params p)
 {
-  extern __shared__ unsigned char sraw[];
-  float *r0 = reinterpret_cast<float *>(sraw);
-  float *rf = r0 + p.nr;
-  const int lane = threadIdx.x & 31;
-  for (int i = threadIdx.x; i < p.nr; i += blockDim.x) {
-    r0[i] = p.r0[i];
-    rf[i] = p.rf[i];
-  }
+  extern __shared__ __align__(16) unsigned char sraw[];
+  const Sh sh = load_shells(p, sraw, true);
   __syncthreads();
-  long long H = (long long)*(volatile unsigned long long *)&p.ctr[0];
-  if (H > p.list_cap) H = p.list_cap;
-  const unsigned long long S = *(volatile unsigned long long *)&p.ctr[4];
-  if (H <= 0 || S == 0) return;
-  const cg_imap_cell *cl = p.cells;
-  const long long *off = p.cell_off;
-  const unsigned long long NC = (unsigned long long)gridDim.x * IW * CHUNKS;
-  const unsigned FULL = 0xffffffffu;
+  const cg_imap_args A = args_with(p, sh);
+  const int lane = threadIdx.x & 31;
+  const unsigned long long total = sh.chunk_off[p.nbk];
   for (;;) {
-    unsigned long long k = 0;
-    if (lane == 0) k = atomicAdd(&p.ctr[1], 1ull);
-    k = __shfl_sync(FULL, k, 0);
-    if (k >= NC) break;
-    const long long s0 = (long long)(S * k / NC), s1 = (long long)(S * (k + 1) / NC);
-    if (s0 >= s1) continue;
-    /* last record starting at or before s0 */
-    long long lo = 0, hi = H - 1;
+    unsigned long long ck = 0;
+    if (lane == 0) ck = atomicAdd(&p.ctr[0], 1ull);
+    ck = __shfl_sync(FULL, ck, 0);
+    if (ck >= total) break;
+    /* the bucket: last b with chunk_off[b] <= ck */
+    int lo = 0, hi = p.nbk - 1;
     while (lo < hi) {
-      const long long mid = (lo + hi + 1) >> 1;
-      if (__ldg(&off[mid]) <= s0) lo = mid;
+      const int mid = (lo + hi + 1) >> 1;
+      if (sh.chunk_off[mid] <= ck) lo = mid;
       else hi = mid - 1;
     }
-    long long hw = lo, ow = __ldg(&off[lo]); /* the warp's current record and its first sample */
-    for (long long sb = s0; sb < s1; sb += 32) {
-      const long long s = sb + lane;
-      long long h = hw, oh = ow;
+    const int b = lo;
+    const unsigned long long lc = ck - sh.chunk_off[b];
+    const unsigned long long nrec =
+        p.cnt[b] < (unsigned long long)p.cap[b] ? p.cnt[b] : (unsigned long long)p.cap[b];
+    const int ns = sh.nsub[b];
+    const int s3 = ns * ns * ns;
+    const float inv = sh.invns[b];
+    long long r0;  /* first record of the chunk (within the bucket) */
+    int q0, nq;    /* first sample of r0 and the chunk's sample count */
+    int per;       /* samples per record walked in this chunk (s3, or the slice) */
+    if (s3 <= CHS) {
+      const int R = CHS / s3;
+      r0 = (long long)lc * R;
+      const long long r1 = r0 + R < (long long)nrec ? r0 + R : (long long)nrec;
+      q0 = 0;
+      nq = (int)(r1 - r0) * s3;
+      per = s3;
+    } else {
+      const int Kq = (s3 + CHS - 1) / CHS;
+      r0 = (long long)(lc / (unsigned long long)Kq);
+      q0 = (int)(lc % (unsigned long long)Kq) * CHS;
+      nq = s3 - q0 < CHS ? s3 - q0 : CHS;
+      per = 0;
+    }
+    const float inv_s3 = per ? 1.0f / (float)per : 0.0f;
+    for (int t0 = 0; t0 < nq; t0 += 32) {
+      const int t = t0 + lane;
       K key = empty_key<K>();
       float temp = 0.0f;
-      if (s < s1) {
-        while (h + 1 < H) {
-          const long long nx = __ldg(&off[h + 1]);
-          if (nx > s) break;
-          h++;
-          oh = nx;
+      long long rec = p.base[b] + r0;
+      if (t < nq) {
+        int q = q0 + t;
+        if (per) {
+          /* t < CHS: (t + 1/2)/per is exact in float */
+          const int rl = (int)(((float)t + 0.5f) * inv_s3);
+          rec += rl;
+          q = t - rl * per;
         }
-        const float4 qa = __ldg(reinterpret_cast<const float4 *>(cl + h));
-        const float4 qb = __ldg(reinterpret_cast<const float4 *>(cl + h) + 1);
-        const int pk = __float_as_int(qb.w);
-        CellPar c;
-        c.x0 = qa.x;
-        c.temp = qa.w;
-        c.drr = qb.x;
-        c.dxs = qb.y;
-        c.inv_ns = qb.z;
-        c.nsub = pk & 2047;
-        c.irad0 = (pk >> 11) - 1;
-        c.pad = 0;
-        key = sample_key<K>(p, r0, rf, c, qa.y, qa.z, (int)(s - oh));
+        const cg_imap_rec rr = p.recs[rec];
+        int ix, iy, iz, dbl;
+        const cg_imap_cell c = unpack(rr, b - 1, &ix, &iy, &iz, &dbl);
         temp = c.temp;
+        int sx, sy, sz, s = -1;
+        long long pix = 0;
+        sub_of(q, ns, inv, &sx, &sy, &sz);
+        if (dbl || p.force_double || !cg_imap_sample_checked(&A, ix, iy, iz, &c, ns, sx, sy, sz, &s, &pix)) {
+          const unsigned long long k = atomicAdd(&p.ctr[4], 1ull);
+          if ((long long)k < p.queue_cap) p.queue[k] = ((unsigned long long)rec << 30) | (unsigned long long)q;
+          else atomicOr(p.err, ERR_IMAP_QUEUE);
+        } else {
+          key = key_of<K>(p, s, pix);
+        }
       }
-      add_runs(key, (int)h, temp, lane, p);
-      hw = __shfl_sync(FULL, h, 31);
-      ow = __shfl_sync(FULL, oh, 31);
+      add_runs(key, rec, temp, lane, p);
     }
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) p.ctr[4] = S; /* listed samples, for the caller */
+}
+
+/* The queued samples in double: the cell's radial shift (imap.c:196-198)
+ * and the sample's shell and pixel (imap.c:210-231). */
+__global__ void __launch_bounds__(256) k_imap_double(const float *__restrict__ phi, cg_imap_params p)
+{
+  extern __shared__ __align__(16) unsigned char sraw[];
+  const Sh sh = load_shells(p, sraw, false);
+  __syncthreads();
+  const cg_imap_args A = args_with(p, sh);
+  const unsigned long long nq0 = p.ctr[4];
+  const long long nq = (long long)nq0 < p.queue_cap ? (long long)nq0 : p.queue_cap;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && nq > 0) atomicAdd(p.xstats + 3, (unsigned long long)nq);
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nq; k += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long e = p.queue[k];
+    const long long rec = (long long)(e >> 30);
+    const int q = (int)(e & ((1ull << 30) - 1));
+    /* the record's bucket: last b with base[b] <= rec */
+    int lo = 0, hi = p.nbk - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (p.base[mid] <= rec) lo = mid;
+      else hi = mid - 1;
+    }
+    int ix, iy, iz, dbl;
+    const cg_imap_cell c = unpack(p.recs[rec], lo - 1, &ix, &iy, &iz, &dbl);
+    const int ns = sh.nsub[lo];
+    float v[3];
+    grad_phi(phi, ix, iy, iz, p.box.N, v);
+    int j, s = -1, sx, sy, sz;
+    double drr = 0;
+    cgx_imap_cell(&A, ix, iy, iz, v, &j, &drr);
+    sub_of(q, ns, sh.invns[lo], &sx, &sy, &sz);
+    long long pix = 0;
+    cgx_imap_sample(&A, ix, iy, iz, ns, drr, sx, sy, sz, &s, &pix);
+    if (s >= 0 && s < p.nr) {
+      const long long key = (long long)s * p.npix + pix;
+      atomicAdd(&p.data[key], c.temp);
+      atomicAdd(&p.nadd[key], 1);
+    }
+  }
 }
 
 template <typename K>
 cudaError_t launch(cudaStream_t s, const float *dens, const float *phi, const cg_imap_params *p, int nsm)
 {
-  size_t smem = IW * 32 * sizeof(CellPar) + (size_t)(p->nr + 2) * sizeof(float4) + (size_t)p->nr * 3 * sizeof(float);
-  cudaError_t e = cudaFuncSetAttribute(k_imap_cells<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaMemsetAsync(p->ctr, 0, 5 * sizeof(unsigned long long), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(p->cnt, 0, (size_t)p->nbk * sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
+  const size_t sm_list = shell_smem(p->nr, p->nbk, false), sm_paint = shell_smem(p->nr, p->nbk, true);
+  if ((e = cudaFuncSetAttribute(k_imap_list<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_list)) ||
+      (e = cudaFuncSetAttribute(k_imap_paint<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_paint)) ||
+      (e = cudaFuncSetAttribute(k_imap_double, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_list)))
+    return e;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_imap_cells<K>, IW * 32, smem);
-  if (e != cudaSuccess) return e;
-  if (per_sm < 1) per_sm = 1;
-  e = cudaMemsetAsync(p->ctr, 0, 5 * sizeof(unsigned long long), s);
-  if (e != cudaSuccess) return e;
-  long long nrow = (long long)p->box.N * p->box.N;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_imap_list<K>, IW * 32, sm_list))) return e;
+  const long long nrow = (long long)p->box.N * p->box.N;
   long long blocks = (nrow + IW * ROWS - 1) / (IW * ROWS);
-  if (blocks > (long long)nsm * per_sm) blocks = (long long)nsm * per_sm;
-  k_imap_cells<K><<<(unsigned)blocks, IW * 32, smem, s>>>(dens, phi, *p);
-  e = cudaGetLastError();
-  if (e != cudaSuccess || p->list_cap <= 0) return e;
-  /* records listed (the count may overshoot the capacity) */
-  unsigned long long h = 0;
-  e = cudaMemcpyAsync(&h, p->ctr, sizeof(h), cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return e;
-  const long long H = (long long)std::min<unsigned long long>(h, (unsigned long long)p->list_cap);
-  if (H == 0) return cudaSuccess;
-  const long long nb = (H + SCAN_T * SCAN_I - 1) / (SCAN_T * SCAN_I);
-  k_scan_sum<<<(unsigned)nb, SCAN_T, 0, s>>>(p->cell_n, H, p->scan_tmp);
-  k_scan_top<<<1, 1024, 0, s>>>(p->scan_tmp, nb, p->ctr + 4);
-  k_scan_out<<<(unsigned)nb, SCAN_T, 0, s>>>(p->cell_n, H, p->scan_tmp, p->cell_off);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  /* every warp of the painting pass resident at once */
-  const size_t psmem = (size_t)p->nr * 2 * sizeof(float);
-  e = cudaFuncSetAttribute(k_imap_paint<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem);
-  if (e != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_imap_paint<K>, IW * 32, psmem);
-  if (e != cudaSuccess) return e;
-  if (per_sm < 1) per_sm = 1;
-  k_imap_paint<K><<<(unsigned)(nsm * per_sm), IW * 32, psmem, s>>>(*p);
+  if (blocks > (long long)nsm * (per_sm > 0 ? per_sm : 1)) blocks = (long long)nsm * (per_sm > 0 ? per_sm : 1);
+  k_imap_list<K><<<(unsigned)blocks, IW * 32, sm_list, s>>>(dens, phi, *p);
+  k_imap_chunks<<<1, 32, 0, s>>>(*p);
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_imap_paint<K>, IW * 32, sm_paint))) return e;
+  k_imap_paint<K><<<(unsigned)(nsm * (per_sm > 0 ? per_sm : 1)), IW * 32, sm_paint, s>>>(*p);
+  k_imap_double<<<(unsigned)(nsm * 4), 256, sm_list, s>>>(phi, *p);
   return cudaGetLastError();
 }
 
 } /* namespace */
 
-long long cg_imap_scan_blocks(long long cap) { return (cap + SCAN_T * SCAN_I - 1) / (SCAN_T * SCAN_I); }
+size_t cg_imap_shell_smem(int nr, int nbk) { return shell_smem(nr, nbk, true); }
 
 cudaError_t cg_imap_paint(cudaStream_t s, const float *dens, const float *phi, const cg_imap_params *p, int nsm)
 {
-  if (!p->ctr) return cudaErrorInvalidValue;
+  if (!p->ctr || !p->recs || !p->queue) return cudaErrorInvalidValue;
   /* 32-bit keys when every (shell, pixel) index and the empty key fit */
   if ((unsigned long long)p->nr * (unsigned long long)p->npix < 0xffffffffull)
     return launch<unsigned int>(s, dens, phi, p, nsm);

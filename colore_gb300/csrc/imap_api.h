@@ -8,47 +8,47 @@
 #include <stdint.h>
 
 #include "cg_dev.cuh"
+#include "cg_exact.h"
+
+/* One listed cell (16 bytes): ix | iy << 16; iz | flags << 12 | half(edrr)
+ * << 16 with the flags single (1), delta + 1 (2 bits, shifted by 1) and
+ * double (8: every sample decided in double); brightness; radial shift. */
+struct __align__(16) cg_imap_rec {
+  unsigned int ixy, izf;
+  float temp, drr;
+};
+
+#define CG_IMAP_REC_BYTES 16
+#define CG_IMAP_BUCKETS_MAX 4100 /* shells -1 .. nr: nr <= 4096 */
 
 struct cg_imap_params {
   cg::Box box;
-  cg::Grid1 g;
-  cg::Tab tz, bz, norm, v1, ih;
-  int bias_model;
-  float factor_vel;
-  int nr;             /* shells, sorted by r0 (imap_preproc, imap.c:105-133) */
-  const float *r0, *rf;
-  /* per shell index + 1 (index -1 below the shells, nr beyond them):
-   * nsub (imap.c:158-174, as int bits), dx / nsub, 1 / nsub */
-  const float4 *shp;
-  float rmin_here, rmax_here;
-  int64_t nside, npix;
-  float *data;        /* nr * npix, RING */
-  int *nadd;          /* nr * npix       */
+  cg_imap_args a;    /* tables, corners, shells (device pointers) */
+  int nr, nbk;       /* shells; buckets nbk = nr + 2, bucket j + 1 for shell j */
+  long long npix;
+  float *data;       /* nr * npix, RING */
+  int *nadd;         /* nr * npix       */
   unsigned int *err;
-  /* The first kernel lists every cell it computes (while the list has room)
-   * and the second paints the listed cells' samples, split evenly over all
-   * warps.  ctr[0] counts records, ctr[1] sample chunks taken, ctr[2] rows
-   * taken, ctr[3] and ctr[4] the samples painted by each kernel (all zeroed
-   * per launch). */
-  long long list_cap;
+  unsigned long long *xstats; /* [2] cells, [3] samples decided in double */
+  int force_double;
+  /* cells are listed per bucket (the shell of their corner, which fixes
+   * nsub), in the slots [base[b], base[b] + cap[b]); cnt[b] counts them
+   * (may exceed cap: those cells are painted by the listing kernel) */
+  cg_imap_rec *recs;
+  const long long *base, *cap;
+  unsigned long long *cnt;
+  /* chunks of the painting pass: chunk_off[b] the first chunk of bucket b
+   * (nbk + 1 entries, set on the device) */
+  unsigned long long *chunk_off;
+  /* ctr: [0] chunks taken, [1] rows taken, [2] samples drawn, [3] samples
+   * painted by the listing kernel, [4] double-queue entries */
   unsigned long long *ctr;
-  struct cg_imap_cell *cells;     /* list_cap records                       */
-  unsigned int *cell_n;           /* samples of each record (nsub^3)        */
-  long long *cell_off;            /* first sample of each record (scanned)  */
-  long long *scan_tmp;            /* cg_imap_scan_blocks(list_cap) entries  */
+  unsigned long long *queue; /* record << 30 | sample, for the double pass */
+  long long queue_cap;
 };
 
-/* One listed cell: corner, brightness, radial shift, sub-cell size, 1/nsub,
- * and nsub | (shell index + 1) << 11. */
-struct __align__(16) cg_imap_cell {
-  float x0, y0, z0, temp, drr, dxs, inv_ns;
-  int packed;
-};
-
-/* Bytes per listed cell (record, sample count, offset). */
-#define CG_IMAP_CELL_BYTES (sizeof(struct cg_imap_cell) + sizeof(unsigned int) + sizeof(long long))
-
-long long cg_imap_scan_blocks(long long cap);
 cudaError_t cg_imap_paint(cudaStream_t s, const float *dens, const float *phi, const cg_imap_params *p, int nsm);
+/* Shared memory of the painting kernel for nr shells and nbk buckets. */
+size_t cg_imap_shell_smem(int nr, int nbk);
 
 #endif

@@ -394,80 +394,166 @@ static int cmp_float_idx(const void *a, const void *b)
   return (x[0] < y[0]) ? -1 : (x[0] > y[0] ? 1 : (x[1] < y[1] ? -1 : 1));
 }
 
-int or_imap32(const cg_config *cfg, int ipop, const float *dens, const float *npot, const float *normtab, float n0,
-              float nf, float *data, int *nadd)
+/* The arguments of the intensity-map decisions for species ipop, as the GPU
+ * builds them (cg_imap_args); the buffers are owned by *B. */
+typedef struct {
+  cg_imap_args a;
+  float *corner, *r0f, *rff, *b, *dxs;
+  int *shell_of, *nsub;
+} ImapArgs;
+
+static void imap_args(ImapArgs *B, const cg_config *cfg, const S32 *s, int ipop, const float *norm32,
+                      const double *norm64)
+{
+  cg_imap_args *a = &B->a;
+  memset(a, 0, sizeof(*a));
+  const int N = cfg->n_grid, nr = cfg->imap_nr[ipop], na = CG_NA;
+  const double dx = cfg->l_box / N;
+  B->corner = malloc(6 * (size_t)N * sizeof(float));
+  for (int k = 0; k < 3; k++)
+    for (int i = 0; i < N; i++) {
+      const double c = cgx_coord(i, dx, cfg->pos_obs[k]);
+      B->corner[k * N + i] = (float)c;
+      B->corner[(3 + k) * N + i] = (float)(c - (double)(float)c);
+    }
+  a->xc = B->corner;
+  a->yc = B->corner + N;
+  a->zc = B->corner + 2 * N;
+  a->xl = B->corner + 3 * N;
+  a->yl = B->corner + 4 * N;
+  a->zl = B->corner + 5 * N;
+  B->r0f = malloc(nr * sizeof(float));
+  B->rff = malloc(nr * sizeof(float));
+  B->b = malloc(2 * nr * sizeof(float));
+  B->shell_of = malloc((2 * nr + 1) * sizeof(int));
+  B->nsub = malloc((nr + 2) * sizeof(int));
+  B->dxs = malloc((nr + 2) * sizeof(float));
+  const long long npix = 12LL * cfg->nside_imap[ipop] * cfg->nside_imap[ipop];
+  const int nb = cg_imap_shells(cfg->imap_r0[ipop], cfg->imap_rf[ipop], nr, dx, npix, B->r0f, B->rff, B->b,
+                                B->shell_of, B->nsub, B->dxs);
+  a->sh.b = B->b;
+  a->sh.shell_of = B->shell_of;
+  a->sh.nb = nb;
+  a->sh.nr = nr;
+  a->nsub = B->nsub;
+  a->dxs = B->dxs;
+  a->r = s->r;
+  a->tz = s->tz[ipop].f;
+  a->bz = s->bzi[ipop].f;
+  a->norm = norm32;
+  a->v1 = s->v1.f;
+  a->ih = s->ih.f;
+  a->idr = s->idr;
+  a->r_last = s->r_last;
+  a->na = na;
+  a->bias_model = cfg->bias_model;
+  a->nside = cfg->nside_imap[ipop];
+  a->dx = (float)dx;
+  const double fv = -cfg->fgrowth_0 / (1.5 * cfg->hubble_0 * cfg->omega_m);
+  a->fvh = (float)(fv * (0.5 * (cfg->n_grid / cfg->l_box)));
+  a->rmin64 = (double)B->r0f[0] - 20.;
+  a->rmax64 = (double)B->rff[nr - 1] + 20.;
+  a->rmin = (float)a->rmin64;
+  a->rmax = (float)a->rmax64;
+  a->r64 = cfg->r_arr_r2z;
+  a->tz64 = cfg->imap_tz_arr[ipop];
+  a->bz64 = cfg->imap_bz_arr[ipop];
+  a->norm64 = norm64;
+  a->v164 = cfg->growth_v_arr;
+  a->ih64 = cfg->ihub_arr;
+  a->idr64 = cfg->glob_idr;
+  a->r_last64 = cfg->r_arr_r2z[na - 1];
+  a->dx64 = dx;
+  for (int k = 0; k < 3; k++) a->p64[k] = cfg->pos_obs[k];
+  a->idx64 = cfg->n_grid / cfg->l_box;
+  a->fv64 = fv;
+}
+
+static void imap_args_free(ImapArgs *B)
+{
+  free(B->corner);
+  free(B->r0f);
+  free(B->rff);
+  free(B->b);
+  free(B->shell_of);
+  free(B->nsub);
+  free(B->dxs);
+}
+
+/* The intensity map of species ipop as the GPU paints it: cells and samples
+ * decided in single precision where the margins hold and in double
+ * otherwise (cg_exact.h); brightness summed in cell order in float.  stats:
+ * [0] cells and [1] samples decided in double, [2] samples drawn (may be
+ * NULL).  norm32 / norm64: the normalisation table with its two edges. */
+int or_imap32(const cg_config *cfg, int ipop, const float *dens, const float *npot, const float *norm32,
+              const double *norm64, float *data, int *nadd, long long *stats)
 {
   S32 s;
   s32_init(&s, cfg);
-  const int N = s.N, nr = cfg->imap_nr[ipop], nside = cfg->nside_imap[ipop];
-  const long long npix = 12LL * nside * nside;
-  /* imap_preproc: shells sorted by r0 (stable in the original order) */
-  float *pr = malloc(2 * nr * sizeof(float)), *r0 = malloc(nr * sizeof(float)), *rf = malloc(nr * sizeof(float));
-  for (int i = 0; i < nr; i++) {
-    pr[2 * i] = (float)cfg->imap_r0[ipop][i];
-    pr[2 * i + 1] = (float)i;
-  }
-  qsort(pr, nr, 2 * sizeof(float), cmp_float_idx);
-  for (int i = 0; i < nr; i++) {
-    int o = (int)pr[2 * i + 1];
-    r0[i] = (float)cfg->imap_r0[ipop][o];
-    rf[i] = (float)cfg->imap_rf[ipop][o];
-  }
-  free(pr);
-  const double dx = cfg->l_box / N, ps = sqrt(4 * M_PI / (double)npix);
-  int *nsub = malloc(nr * sizeof(int));
-  for (int i = 0; i < nr; i++) { /* imap.c:158-172 */
-    double a = r0[i], b = rf[i];
-    double vol = (b * b * b - a * a * a) * ps * ps / 3;
-    double sc0 = fmin(pow(vol, 0.333333), fmin(a * ps, b - a));
-    nsub[i] = (int)(dx / sc0 + 0.5) + 1;
-  }
-  const float rmin = (float)((double)r0[0] - 20.), rmax = (float)((double)rf[nr - 1] + 20.);
+  ImapArgs B;
+  imap_args(&B, cfg, &s, ipop, norm32, norm64);
+  const cg_imap_args *a = &B.a;
+  const int N = s.N, nr = cfg->imap_nr[ipop];
+  const long long npix = 12LL * cfg->nside_imap[ipop] * cfg->nside_imap[ipop];
   const float fvel = (float)(-cfg->fgrowth_0 / (1.5 * cfg->hubble_0 * cfg->omega_m));
-  T32 nrm = {normtab, n0, nf};
   memset(data, 0, (size_t)nr * npix * sizeof(float));
   memset(nadd, 0, (size_t)nr * npix * sizeof(int));
-  for (int iz = 0; iz < N; iz++) {
-    float z0 = cg_cell_coord(iz, s.dx, s.p[2]);
-    for (int iy = 0; iy < N; iy++) {
-      float y0 = cg_cell_coord(iy, s.dx, s.p[1]);
+  long long st[3] = {0, 0, 0};
+  for (int iz = 0; iz < N; iz++)
+    for (int iy = 0; iy < N; iy++)
       for (int ix = 0; ix < N; ix++) {
-        float x0 = cg_cell_coord(ix, s.dx, s.p[0]);
-        float rc = cg_norm3(x0, y0, z0);
-        float tmean = bg32(&s, s.tz[ipop], rc);
-        if (!(rc <= rmax && rc >= rmin && tmean > 0.0f)) continue;
-        float bias = bg32(&s, s.bzi[ipop], rc), dnorm = bg32(&s, nrm, rc);
         float v[3];
         grad32(npot, ix, iy, iz, N, v);
-        float rvel = CG_MUL(fvel, cg_rvel(v[0], v[1], v[2], x0, y0, z0, rc, s.idx));
-        float drr = cg_imap_drsd(rvel, bg32(&s, s.v1, rc), bg32(&s, s.ih, rc));
-        float temp = cg_imap_temp(tmean, dens[pidx(ix, iy, iz, N)], bias, dnorm, cfg->bias_model);
-        int ir0 = cg_shell_index(r0, rf, nr, rc, 0);
-        int ns = ir0 < 0 ? nsub[0] : (ir0 >= nr ? nsub[nr - 1] : nsub[ir0]);
-        float dxs = CG_DIV(s.dx, (float)ns);
-        for (int izz = 0; izz < ns; izz++) {
-          float zc = cg_sub_centre(z0, izz, dxs);
-          for (int iyy = 0; iyy < ns; iyy++) {
-            float yc = cg_sub_centre(y0, iyy, dxs);
-            float yz2 = cg_yz2(yc, zc);
-            for (int ixx = 0; ixx < ns; ixx++) {
-              float xc = cg_sub_centre(x0, ixx, dxs);
-              int64_t pix = 0;
-              int ir = cg_imap_sample(xc, yc, zc, yz2, drr, r0, rf, nr, ir0, nside, &pix);
-              if (ir >= 0 && ir < nr) {
-                long long k = (long long)ir * npix + pix;
-                data[k] += temp;
-                nadd[k]++;
+        const float d = dens[pidx(ix, iy, iz, N)];
+        cg_imap_cell c;
+        int k = cg_imap_cell_checked(a, ix, iy, iz, d, v, &c);
+        double drr64 = 0;
+        int dbl = 0;
+        if (k == 2) {
+          st[0]++;
+          int j;
+          if (!cgx_imap_cell(a, ix, iy, iz, v, &j, &drr64)) continue;
+          /* listed: the float fields, with the double shell of the corner */
+          float x0 = cg_cell_coord(ix, s.dx, s.p[0]), y0 = cg_cell_coord(iy, s.dx, s.p[1]),
+                z0 = cg_cell_coord(iz, s.dx, s.p[2]);
+          float rc = cg_norm3(x0, y0, z0);
+          c.j = j;
+          c.single = 0;
+          c.delta = 0;
+          c.temp = cg_imap_temp(bg32(&s, s.tz[ipop], rc), d, bg32(&s, s.bzi[ipop], rc),
+                                cg_bg_eval(norm32, s.r, norm32[CG_NA], norm32[CG_NA + 1], rc, s.r_last, s.idr),
+                                cfg->bias_model);
+          dbl = 1;
+        } else if (k == 0) {
+          continue;
+        }
+        (void)fvel;
+        const int ns = a->nsub[c.j + 1];
+        st[2] += (long long)ns * ns * ns;
+        for (int sz = 0; sz < ns; sz++)
+          for (int sy = 0; sy < ns; sy++)
+            for (int sx = 0; sx < ns; sx++) {
+              int sh = -1;
+              long long pix = 0;
+              if (dbl || !cg_imap_sample_checked(a, ix, iy, iz, &c, ns, sx, sy, sz, &sh, &pix)) {
+                if (!dbl) {
+                  int j2;
+                  cgx_imap_cell(a, ix, iy, iz, v, &j2, &drr64);
+                  dbl = 2;
+                }
+                cgx_imap_sample(a, ix, iy, iz, ns, drr64, sx, sy, sz, &sh, &pix);
+                st[1]++;
+                if (dbl == 2) dbl = 0; /* keep the float path for the cell's other samples */
+              }
+              if (sh >= 0 && sh < nr) {
+                const long long q = (long long)sh * npix + pix;
+                data[q] += c.temp;
+                nadd[q]++;
               }
             }
-          }
-        }
       }
-    }
-  }
-  free(r0);
-  free(rf);
-  free(nsub);
+  if (stats) memcpy(stats, st, sizeof(st));
+  imap_args_free(&B);
   s32_free(&s);
   return 0;
 }

@@ -461,20 +461,30 @@ void or_pix64(long nside, const double *xyz, long n, long long *pix)
   }
 }
 
+/* get_rvel (imap.c:43-74, srcs.c:87-118): the unit vector x0/rr is formed
+ * before the products; with sprec (the reference built with _SPREC, float
+ * grids) the potential's centred differences are float - float. */
 static double rvel64(const cg_config *c, const double *p, int ix, int iy, int iz, double x0, double y0, double z0,
-                     double rr)
+                     double rr, int sprec)
 {
   const int N = c->n_grid;
+  const double idx = c->n_grid / c->l_box;
 #define P(X, Y, Z) p[(X) + (size_t)N * ((Y) + (size_t)N * (Z))]
   int xh = (ix + 1) % N, xl = (ix + N - 1) % N, yh = (iy + 1) % N, yl = (iy + N - 1) % N, zh = (iz + 1) % N,
       zl = (iz + N - 1) % N;
   double v0 = P(xh, iy, iz) - P(xl, iy, iz), v1 = P(ix, yh, iz) - P(ix, yl, iz), v2 = P(ix, iy, zh) - P(ix, iy, zl);
+  if (sprec) { /* float grid: the difference is a float */
+    v0 = (float)v0;
+    v1 = (float)v1;
+    v2 = (float)v2;
+  }
 #undef P
-  return 0.5 * (N / c->l_box) * (v0 * x0 / rr + v1 * y0 / rr + v2 * z0 / rr);
+  double u0 = x0 / rr, u1 = y0 / rr, u2 = z0 / rr;
+  return 0.5 * idx * (v0 * u0 + v1 * u1 + v2 * u2);
 }
 
 int or_imap64_part(const cg_config *c, int ipop, const double *dens, const double *npot, const double *nrm,
-                   double n0, double nf, int iz_stride, double *data, int *nadd, long long *nsamp)
+                   double n0, double nf, int iz_stride, double *data, int *nadd, long long *nsamp, int sprec)
 {
   long long ns_tot = 0;
   const int N = c->n_grid, nr = c->imap_nr[ipop], nside = c->nside_imap[ipop];
@@ -488,9 +498,9 @@ int or_imap64_part(const cg_config *c, int ipop, const double *dens, const doubl
       ord[j] = ord[j - 1];
       ord[j - 1] = t;
     }
-  for (int i = 0; i < nr; i++) {
-    r0[i] = c->imap_r0[ipop][ord[i]];
-    rf[i] = c->imap_rf[ipop][ord[i]];
+  for (int i = 0; i < nr; i++) { /* the shells are flouble: float with _SPREC */
+    r0[i] = sprec ? (float)c->imap_r0[ipop][ord[i]] : c->imap_r0[ipop][ord[i]];
+    rf[i] = sprec ? (float)c->imap_rf[ipop][ord[i]] : c->imap_rf[ipop][ord[i]];
   }
   const double dx = c->l_box / N, ps = sqrt(4 * M_PI / npix);
   for (int i = 0; i < nr; i++) {
@@ -513,7 +523,7 @@ int or_imap64_part(const cg_config *c, int ipop, const double *dens, const doubl
         double tm = bg(c, tz, 0, 0, rc);
         if (!(rc <= rmax && rc >= rmin && tm > 0)) continue;
         double b = bg(c, bz, bz[0], 1, rc), dn = bg(c, nrm, n0, nf, rc);
-        double rv = fvel * rvel64(c, npot, ix, iy, iz, x0, y0, z0, rc);
+        double rv = fvel * rvel64(c, npot, ix, iy, iz, x0, y0, z0, rc, sprec);
         double drr = rv * BG_V1(c, rc) * BG_IH(c, rc);
         size_t id = ix + (size_t)N * (iy + (size_t)N * iz);
         double temp = tm * bias_model64(dens[id], b, c->bias_model) * dn;
@@ -558,9 +568,9 @@ int or_imap64_part(const cg_config *c, int ipop, const double *dens, const doubl
 }
 
 int or_imap64(const cg_config *c, int ipop, const double *dens, const double *npot, const double *nrm, double n0,
-              double nf, double *data, int *nadd)
+              double nf, double *data, int *nadd, int sprec)
 {
-  return or_imap64_part(c, ipop, dens, npot, nrm, n0, nf, 1, data, nadd, NULL);
+  return or_imap64_part(c, ipop, dens, npot, nrm, n0, nf, 1, data, nadd, NULL, sprec);
 }
 
 /* Number of sub-samples imap_set_cartesian_single draws for species ipop at
@@ -576,14 +586,14 @@ long long or_imap_samples(const cg_config *c, int ipop)
   int *ord = malloc(nr * sizeof(int));
   for (int i = 0; i < nr; i++) ord[i] = i;
   for (int i = 1; i < nr; i++)
-    for (int j = i; j > 0 && c->imap_r0[ipop][ord[j]] < c->imap_r0[ipop][ord[j - 1]]; j--) {
+    for (int j = i; j > 0 && (float)c->imap_r0[ipop][ord[j]] < (float)c->imap_r0[ipop][ord[j - 1]]; j--) {
       int t = ord[j];
       ord[j] = ord[j - 1];
       ord[j - 1] = t;
     }
-  for (int i = 0; i < nr; i++) {
-    r0[i] = c->imap_r0[ipop][ord[i]];
-    rf[i] = c->imap_rf[ipop][ord[i]];
+  for (int i = 0; i < nr; i++) { /* the shells are flouble (float) in the reference */
+    r0[i] = (float)c->imap_r0[ipop][ord[i]];
+    rf[i] = (float)c->imap_rf[ipop][ord[i]];
   }
   const double dx = c->l_box / N, ps = sqrt(4 * M_PI / npix);
   for (int i = 0; i < nr; i++) {
@@ -968,7 +978,7 @@ int or_run_mock64(const cg_config *c, int nthreads_hint, long long *nsrc_total, 
     double *data = malloc((size_t)c->imap_nr[p] * npix * sizeof(double));
     int *nadd = malloc((size_t)c->imap_nr[p] * npix * sizeof(int));
     or_imap64(c, p, dens, npot, tabs + (size_t)(c->n_srcs + p) * CG_NA, e0f[2 * (c->n_srcs + p)],
-              e0f[2 * (c->n_srcs + p) + 1], data, nadd);
+              e0f[2 * (c->n_srcs + p) + 1], data, nadd, 1);
     for (long i = 0; i < (long)c->imap_nr[p] * npix; i++) cs += nadd[i];
     free(data);
     free(nadd);

@@ -54,10 +54,13 @@ int or_cstm64(const cg_config *cfg, int ipop, const double *dens, const double *
 int or_lens64(const cg_config *cfg, const double *npot, long long n, const float *pos4, double *out);
 int or_skw64(const cg_config *cfg, const double *dens, const double *npot, int gauss, double sigma2, long long n,
              const float *pos4, double *dout, double *vout);
+/* sprec: the reference built with _SPREC (float grids and shells, float
+ * potential differences), the build the FP32 path matches; 0: the double
+ * build, which the FP64 baseline path matches. */
 int or_imap64(const cg_config *cfg, int ipop, const double *dens, const double *npot, const double *normtab,
-              double n0, double nf, double *data, int *nadd);
+              double n0, double nf, double *data, int *nadd, int sprec);
 int or_imap64_part(const cg_config *cfg, int ipop, const double *dens, const double *npot, const double *normtab,
-                   double n0, double nf, int iz_stride, double *data, int *nadd, long long *nsamp);
+                   double n0, double nf, int iz_stride, double *data, int *nadd, long long *nsamp, int sprec);
 long long or_imap_samples(const cg_config *cfg, int ipop);
 int or_kappa64_part(const cg_config *cfg, const double *npot, int pix_stride, double *map);
 long long or_poisson_total64(const cg_config *cfg, int ipop, const double *lam);
@@ -85,8 +88,10 @@ int or_emit32(const cg_config *cfg, int ipop, const float *dens, const float *np
               const double *norm64, long long cap, float *pos4, int *ipix, float *src9, int *cmap, long long *nsrc,
               long long *fallbacks);
 int or_beam_rsd32(const cg_config *cfg, const float *npot, long long n, const float *pos4, float *src9);
-int or_imap32(const cg_config *cfg, int ipop, const float *dens, const float *npot, const float *normtab, float n0,
-              float nf, float *data, int *nadd);
+/* The intensity map as the GPU paints it (float margins, double where they
+ * do not hold); stats: cells and samples decided in double, samples drawn. */
+int or_imap32(const cg_config *cfg, int ipop, const float *dens, const float *npot, const float *norm32,
+              const double *norm64, float *data, int *nadd, long long *stats);
 int or_kappa32(const cg_config *cfg, const float *npot, float *map);
 int or_isw32(const cg_config *cfg, const float *npot, float *map);
 int or_cstm32(const cg_config *cfg, int ipop, const float *dens, const float *normtab, float n0, float nf,

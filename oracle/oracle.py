@@ -28,15 +28,15 @@ def lib():
             "or_lpt64": [vp, vp, vp, vp], "or_lpt2_64": [vp, vp, vp, vp, vp], "or_bins64": [vp, vp, i, d, vp, vp, vp],
             "or_norm_tables64": [vp, vp, vp, vp, vp, vp, vp, vp],
             "or_lambda64": [vp, i, vp, vp, d, d, vp], "or_kappa64": [vp, vp, vp],
-            "or_imap64": [vp, i, vp, vp, vp, d, d, vp, vp], "or_run_mock64": [vp, i, vp, vp],
-            "or_imap64_part": [vp, i, vp, vp, vp, d, d, i, vp, vp, vp], "or_imap_samples": [vp, i],
+            "or_imap64": [vp, i, vp, vp, vp, d, d, vp, vp, i], "or_run_mock64": [vp, i, vp, vp],
+            "or_imap64_part": [vp, i, vp, vp, vp, d, d, i, vp, vp, vp, i], "or_imap_samples": [vp, i],
             "or_kappa64_part": [vp, vp, i, vp], "or_poisson_total64": [vp, i, vp],
             "or_density32": [vp, vp, f, i], "or_bins32": [vp, vp, i, d, vp, vp, vp],
             "or_counts32": [vp, i, vp, vp, vp, vp, vp, vp],
             "or_emit32": [vp, i, vp, vp, vp, vp, C.c_longlong, vp, vp, vp, vp, vp, vp],
             "or_counts64": [vp, i, vp, vp, vp, vp],
             "or_emit64": [vp, i, vp, vp, C.c_longlong, vp, vp, vp, vp, vp],
-            "or_beam_rsd32": [vp, vp, C.c_longlong, vp, vp], "or_imap32": [vp, i, vp, vp, vp, f, f, vp, vp],
+            "or_beam_rsd32": [vp, vp, C.c_longlong, vp, vp], "or_imap32": [vp, i, vp, vp, vp, vp, vp, vp, vp],
             "or_kappa32": [vp, vp, vp], "or_isw32": [vp, vp, vp], "or_isw64": [vp, vp, vp],
             "or_cstm_steps": [vp, i, vp, vp, vp, vp], "or_cstm64": [vp, i, vp, vp, d, d, vp],
             "or_cstm32": [vp, i, vp, vp, f, f, vp],
@@ -193,15 +193,18 @@ def kappa64(cfg, npot):
     return m
 
 
-def imap64(cfg, ipop, dens, npot, tab, e):
+def imap64(cfg, ipop, dens, npot, tab, e, sprec=True):
+    """Intensity map in double (imap.c:135-245): (summed brightness, hits).
+    sprec: the reference built with _SPREC (float shells and potential
+    differences), which the FP32 path matches; False: the double build, which
+    the FP64 baseline path matches."""
     ns, nr = cfg.nside_imap[ipop], cfg.imap_nr[ipop]
     data = np.empty((nr, 12 * ns * ns))
     nadd = np.empty((nr, 12 * ns * ns), np.int32)
     lib().or_imap64(cfgp(cfg), ipop, P(np.ascontiguousarray(dens, np.float64)),
                     P(np.ascontiguousarray(npot, np.float64)), P(np.ascontiguousarray(tab, np.float64)),
-                    float(e[0]), float(e[1]), P(data), P(nadd))
+                    float(e[0]), float(e[1]), P(data), P(nadd), 1 if sprec else 0)
     return data, nadd
-
 
 def run_mock64(cfg):
     n = C.c_longlong()
@@ -301,13 +304,18 @@ def beam_rsd32(cfg, npot, pos, src):
     return s
 
 
-def imap32(cfg, ipop, dens, npot, tab, e):
+def imap32(cfg, ipop, dens, npot, tab32, e32, tab64, e64):
+    """The intensity map as the GPU paints it: (summed brightness, hit
+    counts, stats) with stats = (cells and samples decided in double,
+    samples drawn)."""
     ns, nr = cfg.nside_imap[ipop], cfg.imap_nr[ipop]
     data = np.empty((nr, 12 * ns * ns), np.float32)
     nadd = np.empty((nr, 12 * ns * ns), np.int32)
-    lib().or_imap32(cfgp(cfg), ipop, P(dens), P(npot), P(tab), float(e[0]), float(e[1]), P(data), P(nadd))
-    return data, nadd
-
+    st = np.zeros(3, np.int64)
+    t32, t64 = _norm_pair(tab32, e32, tab64, e64)
+    lib().or_imap32(cfgp(cfg), ipop, P(np.ascontiguousarray(dens, np.float32)),
+                    P(np.ascontiguousarray(npot, np.float32)), P(t32), P(t64), P(data), P(nadd), P(st))
+    return data, nadd, st
 
 def isw64(cfg, npot):
     ns = cfg.nside_isw
@@ -463,7 +471,7 @@ def imap64_part(cfg, ipop, dens, npot, tab, e, iz_stride):
     nsamp = C.c_longlong()
     lib().or_imap64_part(cfgp(cfg), ipop, P(np.ascontiguousarray(dens, np.float64)),
                          P(np.ascontiguousarray(npot, np.float64)), P(np.ascontiguousarray(tab, np.float64)),
-                         float(e[0]), float(e[1]), iz_stride, P(data), P(nadd), C.byref(nsamp))
+                         float(e[0]), float(e[1]), iz_stride, P(data), P(nadd), C.byref(nsamp), 1)
     return nsamp.value
 
 

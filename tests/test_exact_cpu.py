@@ -122,3 +122,40 @@ def test_counts_and_sources_equal_double(tmp_path, bias_model):
         assert np.all(np.minimum(dra, 360 - dra) < 2e-4)
         assert np.max(np.abs(s32[:, 1] - s64[:, 1])) < 2e-4
         np.testing.assert_allclose(s32[:, 2], s64[:, 2], rtol=2e-6, atol=1e-7)
+
+
+def _imap_spec(case):
+    base = dict(n_grid=64, z_min=0.05, z_max=0.6, r_smooth=2.0, seed=41, dens_type=0, bias_model=2,
+                imap=[dict(tz=0.1, bias=("const", 1.0), z_range=(0.05, 0.5), nbands=12, nside=64)])
+    if case == "fine":
+        base["imap"] = [dict(tz=0.1, bias=("1+z",), z_range=(0.2, 0.55), nbands=24, nside=256)]
+        base["seed"] = 43
+        base["bias_model"] = 1
+    return base
+
+
+@pytest.mark.parametrize("case", ["coarse", "fine"])
+def test_imap_hits_equal_double(tmp_path, case):
+    """Every sub-sample's shell and RING pixel (imap.c:179-231), decided as
+    the GPU decides them, equals the oracle's double restatement: hit counts
+    exactly; brightness (float sums) to 2e-6 relative."""
+    import oracle as orc
+    from colore_gb300 import inputs
+    prm = orc.Params(inputs.write_inputs(str(tmp_path), _imap_spec(case)))
+    cfg = prm.config
+    n = cfg.n_grid
+    d64, p64, st = orc.field64(cfg)
+    dens = orc.density64(cfg, d64, st[3])
+    d32 = dens.astype(np.float32)
+    phi32 = p64.astype(np.float32)
+    tabs, e0f, _ = orc.norm_tables64(cfg, d32.astype(np.float64))
+    pad = lambda a: np.ascontiguousarray(np.pad(a, ((0, 0), (0, 0), (0, 2 * (n // 2 + 1) - n))))
+    t64, e64 = tabs[0], np.asarray(e0f[0], np.float64)
+    data32, nadd32, stats = orc.imap32(cfg, 0, pad(d32), pad(phi32), t64.astype(np.float32),
+                                       e64.astype(np.float32), t64, e64)
+    data64, nadd64 = orc.imap64(cfg, 0, d32.astype(np.float64), phi32.astype(np.float64), t64, e64)
+    assert nadd64.sum() > 10 ** 6
+    assert np.array_equal(nadd32, nadd64), int((nadd32 != nadd64).sum())
+    np.testing.assert_allclose(data32, data64, rtol=2e-6, atol=1e-12)
+    # the double path is the exception
+    assert stats[1] < 5e-3 * stats[2], stats

@@ -64,7 +64,7 @@ def test_fp64_path_vs_oracle(runs, kind):
     for t in range(cfg.n_srcs + cfg.n_imap):
         np.testing.assert_allclose(m.norm_table(t), tabs[t], rtol=1e-9)
     for ip in range(cfg.n_imap):
-        data, nadd = orc.imap64(cfg, ip, dens, p64, tabs[nts + ip], e0f[nts + ip])
+        data, nadd = orc.imap64(cfg, ip, dens, p64, tabs[nts + ip], e0f[nts + ip], sprec=False)
         gd, gn = m.imap(ip)
         assert gn.sum() > 0
         assert np.abs(gn.astype(np.int64) - nadd).sum() <= 1e-6 * nadd.sum() + 4

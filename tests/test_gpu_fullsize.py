@@ -11,9 +11,8 @@ any size:
   sources               the count map adds up to the catalogue; every source
                         inside the box, RA in [0, 360], Dec in [-90, 90],
                         HEALPix ids in range
-  intensity map         samples painted = the oracle's count from the
-                        geometry (1e-3, FP32 vs FP64 radii at the edges);
-                        hits <= samples
+  intensity map         samples drawn = the double arithmetic's count from
+                        the geometry, exactly; hits <= samples
   rerun                 a second run of the same context gives the same
                         catalogue, count map, hit counts and convergence
                         maps bit for bit (brightness sums use float atomics
@@ -93,7 +92,7 @@ def test_c4_full_size_properties(c4):
     m.imap_set_cartesian()
     got = m.imap_samples(0)
     want = orc.lib().or_imap_samples(orc.cfgp(cfg), 0)
-    assert want > 10 ** 9 and abs(got - want) <= 1e-3 * want, (got, want)
+    assert want > 10 ** 9 and got == want, (got, want)
     imap, nadd = m.imap(0, with_nadd=True)
     assert 0 < int(nadd.sum(dtype=np.int64)) <= got
     m.get_beam_properties()
