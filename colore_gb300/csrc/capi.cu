@@ -1440,6 +1440,7 @@ extern "C" int cg_imap_set_cartesian(cg_ctx *c)
     a.sh.shell_of = M.shell_of;
     a.sh.nb = nb;
     a.sh.nr = nr;
+    a.sh.contig = cg_imap_contig(r0f.data(), rff.data(), nr, nb);
     a.nsub = M.nsub;
     a.dxs = M.dxs;
     a.r64 = c->d_tabs64;

@@ -285,7 +285,7 @@ CG_HD float cg_fminf(float a, float b) { return a < b ? a : b; }
 /* Distance of x >= 0 to the nearest integer, and floor(x). */
 CG_HD float cg_int_dist(float x, int *fl)
 {
-  const float f = cg_floorf(x);
+  const float f = floorf(x);
   *fl = (int)f;
   const float d = CG_SUB(x, f); /* exact: x and f share the exponent range */
   return d < 0.5f ? d : CG_SUB(1.0f, d);
@@ -404,33 +404,22 @@ CG_HD cg_dir cg_dir_of(float x, float y, float z, float ein)
   o.cth = CG_MUL(z, o.rinv);
   const float ax = cg_fabsf(x), ay = cg_fabsf(y);
   const float mx = cg_fmaxf(ax, ay), mn = cg_fminf(ax, ay);
-  const float t = mx > 0.0f ? CG_MUL(mn, cg_rcp_fast(mx)) : 0.0f;
-  const float th = cg_atan01(t); /* atan(t) in [0, pi/4] */
-  float g = CG_MUL(th, 0.636619772367581343f);
-  if (ay > ax) g = CG_SUB(1.0f, g); /* atan(ay/ax) / (pi/2) */
-  /* quadrant: phi in [0, pi/2) for x > 0, y >= 0; atan2(0, 0) = 0 */
-  int q;
-  float f;
-  if (x > 0.0f && y >= 0.0f) {
-    q = 0;
-    f = g;
-  } else if (x <= 0.0f && y > 0.0f) {
-    q = 1;
-    f = CG_SUB(1.0f, g);
-  } else if (x < 0.0f && y <= 0.0f) {
-    q = 2;
-    f = g;
-  } else if (x >= 0.0f && y < 0.0f) {
-    q = 3;
-    f = CG_SUB(1.0f, g);
-  } else {
-    q = 0;
+  const float t = CG_MUL(mn, cg_rcp_fast(cg_fmaxf(mx, 1e-30f))); /* atan2(0, 0) = 0 */
+  const float g = CG_MUL(cg_atan01(t), 0.636619772367581343f); /* atan(min/max) / (pi/2) */
+  /* tt = phi / (pi/2) in [0, 4) is base + g' or base - g' with
+   * g' = atan(ay/ax) / (pi/2) (g, or 1 - g when ay > ax) and, by quadrant,
+   * (base, sign) = (0, +) x >= 0 y >= 0, (2, -) x < 0 y >= 0, (2, +) x < 0 y < 0,
+   * (4, -) x >= 0 y < 0; q and f = tt - q follow without forming tt, so f
+   * keeps absolute rounding */
+  const int neg = (x < 0.0f) != (y < 0.0f);
+  const int swap = ay > ax;
+  int q = ((x < 0.0f) ? 2 : ((y < 0.0f) ? 4 : 0)) - neg;
+  float f = (swap != neg) ? CG_SUB(1.0f, g) : g;
+  if (f >= 1.0f) { /* g' = 0 on the negative side: tt is the next integer */
     f = 0.0f;
+    q = q + 1;
   }
-  if (f >= 1.0f) {
-    f = CG_SUB(f, 1.0f);
-    q = (q + 1) & 3;
-  }
+  q &= 3;
   o.q = q;
   o.f = f;
   /* cos(theta): r^2 (2 roundings), rsqrt (2^-22), product (2^-24); the
@@ -455,35 +444,38 @@ CG_HD long long cg_pix_checked(const cg_dir *d, int nside, float ein)
   const float ctha = cg_fabsf(d->cth);
   const float c23 = 0.666666686534881592f; /* float(2/3) = 2/3 + 1.99e-8 */
   /* region: ctha <= 2/3 in double; the float constant is 2e-8 above 2/3 */
-  if (cg_fabsf(CG_SUB(ctha, c23)) <= CG_ADD(d->ecth, 4.0e-8f)) return -1;
+  const bool region_ok = cg_fabsf(CG_SUB(ctha, c23)) > CG_ADD(d->ecth, 4.0e-8f);
   if (ctha < c23) {
     /* phi error from the inputs: sqrt(2) ein / sin(theta) with
      * sin(theta) >= sqrt(5)/3 here, times 2/pi */
     const float ef = CG_FMA(1.21f, ein, d->ef);
     /* temp1 -+ temp2 = ns (q + 0.5 + f -+ 0.75 cth): the integer ns q is
      * split off and ns v is exact (ns a power of two) */
-    const float va = CG_FMA(-0.75f, d->cth, CG_ADD(0.5f, d->f));
-    const float vb = CG_FMA(0.75f, d->cth, CG_ADD(0.5f, d->f));
-    const float ev = CG_MUL(ns, CG_FMA(0.75f, d->ecth, CG_ADD(ef, 3.0f * CG_E24 * 2.25f)));
-    int ja, jb;
-    const float da = cg_int_dist(CG_MUL(ns, va), &ja);
-    const float db = cg_int_dist(CG_MUL(ns, vb), &jb);
-    if (!(da > CG_ADD(ev, 1e-9f)) || !(db > CG_ADD(ev, 1e-9f))) return -1;
-    const int jp = nside * d->q + ja, jm = nside * d->q + jb;
+    const float hf = CG_ADD(0.5f, d->f);
+    const float A = CG_MUL(ns, CG_FMA(-0.75f, d->cth, hf));
+    const float B = CG_MUL(ns, CG_FMA(0.75f, d->cth, hf));
+    const float ev = CG_FMA(ns, CG_FMA(0.75f, d->ecth, CG_ADD(ef, 3.0f * CG_E24 * 2.25f)), 1e-9f);
+    const float fa = floorf(A), fb = floorf(B);
+    const float da = CG_SUB(A, fa), db = CG_SUB(B, fb);
+    const float dm = cg_fminf(cg_fminf(da, CG_SUB(1.0f, da)), cg_fminf(db, CG_SUB(1.0f, db)));
+    if (!(region_ok && dm > ev)) return -1;
+    const int jp = nside * d->q + (int)fa, jm = nside * d->q + (int)fb;
     const int ir = nside + 1 + jp - jm;
     const int kshift = 1 - (ir & 1);
     int ip = (jp + jm - nside + kshift + 1) >> 1;
+    /* ip mod 4 nside: with q in 0..3 and 0 <= A/ns, B/ns < 2.25, jp + jm is
+     * in [nside - 1, 2 (3 + 2.25) nside) (each floor loses less than 1), so
+     * ip is in [0, 5 nside) and one subtraction is the modulo */
     const int m = 4 * nside;
-    ip %= m;
-    return (long long)nside * (nside - 1) * 2 + (long long)(ir - 1) * 4 * nside + ip;
+    if (ip >= m) ip -= m;
+    return (long long)(nside * (nside - 1) * 2 + (ir - 1) * 4 * nside + ip);
   }
-  /* polar caps: tmp = ns sqrt(3 (1 - |cth|)) with 1 - |cth| = rho^2 /
-   * (r (r + |z|)), free of the cancellation near the poles */
-  if (!(d->rho2 > 0.0f)) return -1; /* on the polar axis */
+  /* polar caps: tmp = ns sqrt(3 (1 - |cth|)) with 1 - |cth| = sin^2(theta) /
+   * (1 + |cth|), free of the cancellation near the poles */
+  if (!region_ok || !(d->rho2 > 0.0f)) return -1; /* or on the polar axis */
   const float rho = CG_MUL(d->rho2, cg_rsqrt_fast(d->rho2));
   const float sth = CG_MUL(rho, d->rinv); /* sin(theta), relative error 2^-21 */
   if (!(sth > 1e-20f)) return -1;
-  /* 1 - |cth| = sin^2(theta) / (1 + |cth|) */
   const float s = CG_MUL(sth, CG_MUL(1.7320508075688772f, cg_rsqrt_fast(CG_ADD(1.0f, ctha))));
   const float tmp = CG_MUL(ns, s);
   /* relative error of s: rho (2^-22 + 2^-24), rinv 2^-22, |cth| through
@@ -495,21 +487,23 @@ CG_HD long long cg_pix_checked(const cg_dir *d, int nside, float ein)
   const float ef = CG_FMA(0.91f * ein, isth, d->ef);
   const float tp = d->f;
   const float p1 = CG_MUL(tp, tmp), p2 = CG_MUL(CG_SUB(1.0f, tp), tmp);
-  const float e1 = CG_FMA(tmp, ef, CG_FMA(tp, es, CG_MUL(2.0f * CG_E24, CG_ADD(p1, 1.0f))));
-  const float e2 = CG_FMA(tmp, CG_ADD(ef, CG_E24), CG_FMA(CG_SUB(1.0f, tp), es, CG_MUL(2.0f * CG_E24, CG_ADD(p2, 1.0f))));
-  int jp, jm;
-  const float d1 = cg_int_dist(p1, &jp), d2 = cg_int_dist(p2, &jm);
-  if (!(d1 > CG_ADD(e1, 1e-9f)) || !(d2 > CG_ADD(e2, 1e-9f))) return -1;
+  const float e1 = CG_FMA(tmp, ef, CG_FMA(tp, es, CG_FMA(2.0f * CG_E24, p1, 2.0f * CG_E24 + 1e-9f)));
+  const float e2 = CG_FMA(tmp, CG_ADD(ef, CG_E24), CG_FMA(CG_SUB(1.0f, tp), es, CG_FMA(2.0f * CG_E24, p2, 2.0f * CG_E24 + 1e-9f)));
+  const float f1 = floorf(p1), f2 = floorf(p2);
+  const float d1 = CG_SUB(p1, f1), d2 = CG_SUB(p2, f2);
+  const int jp = (int)f1, jm = (int)f2;
   const int ir = jp + jm + 1;
-  int ipf;
   const float p3 = CG_MUL(d->f, (float)ir);
-  const float d3 = cg_int_dist(p3, &ipf);
-  if (!(d3 > CG_ADD(CG_FMA((float)ir, ef, CG_MUL(2.0f * CG_E24, CG_ADD(p3, 1.0f))), 1e-9f))) return -1;
-  int ip = d->q * ir + ipf;
+  const float f3 = floorf(p3), d3 = CG_SUB(p3, f3);
+  const float e3 = CG_FMA((float)ir, ef, CG_FMA(2.0f * CG_E24, p3, 2.0f * CG_E24 + 1e-9f));
+  if (!(cg_fminf(d1, CG_SUB(1.0f, d1)) > e1 && cg_fminf(d2, CG_SUB(1.0f, d2)) > e2 &&
+        cg_fminf(d3, CG_SUB(1.0f, d3)) > e3))
+    return -1;
+  int ip = d->q * ir + (int)f3;
   const int m = 4 * ir;
   if (ip >= m) ip -= m;
-  if (d->cth > 0.0f) return 2LL * ir * (ir - 1) + ip;
-  return 12LL * nside * nside - 2LL * ir * (ir + 1) + ip;
+  if (d->cth > 0.0f) return (long long)(2 * ir * (ir - 1) + ip);
+  return (long long)(12 * nside * nside - 2 * ir * (ir + 1) + ip);
 }
 
 /* ---- Poisson counts (srcs.c:156-183) ------------------------------------ */
@@ -633,6 +627,7 @@ typedef struct {
   const float *b;
   const int *shell_of; /* nb + 1 */
   int nb, nr;
+  int contig; /* shell k is interval k (each rf the next r0) */
 } cg_shells;
 
 CG_HD int cg_interval(const cg_shells *sh, float r)
@@ -655,6 +650,19 @@ CG_HD int cgx_interval(const cg_shells *sh, double r)
     else hi = mid - 1;
   }
   return lo;
+}
+
+/* Interval of r found from interval k0 by walking (a few steps when r is
+ * near the edges of k0). */
+CG_HD int cg_interval_from(const cg_shells *sh, int k0, float r)
+{
+  int k = k0 < -1 ? -1 : (k0 >= sh->nb ? sh->nb - 1 : k0);
+  for (int it = 0; it < 8; it++) {
+    if (k >= 0 && r < sh->b[k]) k--;
+    else if (k + 1 < sh->nb && r >= sh->b[k + 1]) k++;
+    else return k;
+  }
+  return cg_interval(sh, r);
 }
 
 /* Distance of r to the edges of its interval k. */
@@ -817,7 +825,7 @@ CG_HD int cg_imap_sample_checked(const cg_imap_args *a, int ix, int iy, int iz, 
     const float r = CG_MUL(dr.r2, dr.rinv);
     const float rs = CG_ADD(r, c->drr);
     const float e = CG_ADD(CG_FMA(r, CG_ADD(8.0f * CG_E24, ein), c->edrr), CG_MUL(2.0f * CG_E24, cg_fabsf(rs)));
-    const int k = cg_interval(&a->sh, rs);
+    const int k = a->sh.contig ? cg_interval_from(&a->sh, c->j, rs) : cg_interval(&a->sh, rs);
     if (!(cg_interval_margin(&a->sh, k, rs) > e)) return 0;
     sh = a->sh.shell_of[k + 1];
   }
@@ -882,6 +890,7 @@ static inline int cg_imap_shells(const double *r0d, const double *rfd, int nr, d
   for (int i = 0; i < nb; i++)
     if (m == 0 || b[i] != b[m - 1]) b[m++] = b[i];
   nb = m;
+
   /* the walk from shell 0 at each interval's lower edge */
   float rfm[4096];
   for (int i = 0; i < nr && i < 4096; i++) rfm[i] = i == 0 ? rff[0] : (rff[i] > rfm[i - 1] ? rff[i] : rfm[i - 1]);
@@ -899,6 +908,16 @@ static inline int cg_imap_shells(const double *r0d, const double *rfd, int nr, d
     dxs[i + 1] = (float)(dx / nsub[i + 1]);
   }
   return nb;
+}
+
+/* Whether the sorted shells are contiguous (each rf the next r0): then
+ * interval k is shell k. */
+static inline int cg_imap_contig(const float *r0f, const float *rff, int nr, int nb)
+{
+  if (nb != nr + 1) return 0;
+  for (int i = 0; i + 1 < nr; i++)
+    if (rff[i] != r0f[i + 1]) return 0;
+  return 1;
 }
 
 #endif /* CG_EXACT_H */

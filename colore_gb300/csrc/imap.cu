@@ -116,10 +116,10 @@ __device__ __forceinline__ K key_of(const cg_imap_params &p, int s, long long pi
  * to the maps once, by its first lane, with its length (data += temp * run,
  * nadd += run).  tag separates cells, whose brightness differs. */
 template <typename K>
-__device__ __forceinline__ void add_runs(K key, long long tag, float temp, int lane, const cg_imap_params &p)
+__device__ __forceinline__ void add_runs(K key, int tag, float temp, int lane, const cg_imap_params &p)
 {
   const K pk = __shfl_up_sync(FULL, key, 1);
-  const long long pt = __shfl_up_sync(FULL, tag, 1);
+  const int pt = __shfl_up_sync(FULL, tag, 1);
   const bool valid = key != empty_key<K>();
   const bool head = valid && (lane == 0 || pk != key || pt != tag);
   const unsigned bnd = __ballot_sync(FULL, head || !valid);
@@ -322,7 +322,7 @@ __global__ void __launch_bounds__(IW * 32) k_imap_list(const float *__restrict__
           const int ns = A.nsub[cc.j + 1];
           const int n3 = ns * ns * ns;
           const float inv = sh.invns[cc.j + 1];
-          const long long tag = ((long long)row << 16) | cx;
+          const int tag = cx;
           for (int q0 = 0; q0 < n3; q0 += 32) {
             const int q = q0 + lane;
             K key = empty_key<K>();
@@ -411,35 +411,46 @@ __global__ void __launch_bounds__(IW * 32) k_imap_paint(cg_imap_params p)
       per = 0;
     }
     const float inv_s3 = per ? 1.0f / (float)per : 0.0f;
+    const long long rbase = p.base[b] + r0;
     for (int t0 = 0; t0 < nq; t0 += 32) {
       const int t = t0 + lane;
       K key = empty_key<K>();
       float temp = 0.0f;
-      long long rec = p.base[b] + r0;
+      int rl = 0, q = q0 + t;
+      bool dq = false; /* queued for the double pass */
       if (t < nq) {
-        int q = q0 + t;
         if (per) {
           /* t < CHS: (t + 1/2)/per is exact in float */
-          const int rl = (int)(((float)t + 0.5f) * inv_s3);
-          rec += rl;
+          rl = (int)(((float)t + 0.5f) * inv_s3);
           q = t - rl * per;
         }
-        const cg_imap_rec rr = p.recs[rec];
+        const cg_imap_rec rr = p.recs[rbase + rl];
         int ix, iy, iz, dbl;
         const cg_imap_cell c = unpack(rr, b - 1, &ix, &iy, &iz, &dbl);
         temp = c.temp;
         int sx, sy, sz, s = -1;
         long long pix = 0;
         sub_of(q, ns, inv, &sx, &sy, &sz);
-        if (dbl || p.force_double || !cg_imap_sample_checked(&A, ix, iy, iz, &c, ns, sx, sy, sz, &s, &pix)) {
-          const unsigned long long k = atomicAdd(&p.ctr[4], 1ull);
-          if ((long long)k < p.queue_cap) p.queue[k] = ((unsigned long long)rec << 30) | (unsigned long long)q;
-          else atomicOr(p.err, ERR_IMAP_QUEUE);
-        } else {
+        if (dbl || p.force_double || !cg_imap_sample_checked(&A, ix, iy, iz, &c, ns, sx, sy, sz, &s, &pix))
+          dq = true;
+        else
           key = key_of<K>(p, s, pix);
+      }
+      /* the queued samples of the step: one atomic for the warp */
+      const unsigned qm = __ballot_sync(FULL, dq);
+      if (qm) {
+        unsigned long long k0 = 0;
+        if (lane == 0) k0 = atomicAdd(&p.ctr[4], (unsigned long long)__popc(qm));
+        k0 = __shfl_sync(FULL, k0, 0);
+        if (dq) {
+          const unsigned long long k = k0 + __popc(qm & ((1u << lane) - 1u));
+          if ((long long)k < p.queue_cap)
+            p.queue[k] = ((unsigned long long)(rbase + rl) << 30) | (unsigned long long)q;
+          else
+            atomicOr(p.err, ERR_IMAP_QUEUE);
         }
       }
-      add_runs(key, rec, temp, lane, p);
+      add_runs(key, rl, temp, lane, p);
     }
   }
 }

@@ -435,6 +435,7 @@ static void imap_args(ImapArgs *B, const cg_config *cfg, const S32 *s, int ipop,
   a->sh.shell_of = B->shell_of;
   a->sh.nb = nb;
   a->sh.nr = nr;
+  a->sh.contig = cg_imap_contig(B->r0f, B->rff, nr, nb);
   a->nsub = B->nsub;
   a->dxs = B->dxs;
   a->r = s->r;
