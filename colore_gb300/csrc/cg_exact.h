@@ -444,7 +444,7 @@ CG_HD long long cg_pix_checked(const cg_dir *d, int nside, float ein)
   const float ctha = cg_fabsf(d->cth);
   const float c23 = 0.666666686534881592f; /* float(2/3) = 2/3 + 1.99e-8 */
   /* region: ctha <= 2/3 in double; the float constant is 2e-8 above 2/3 */
-  const bool region_ok = cg_fabsf(CG_SUB(ctha, c23)) > CG_ADD(d->ecth, 4.0e-8f);
+  const int region_ok = cg_fabsf(CG_SUB(ctha, c23)) > CG_ADD(d->ecth, 4.0e-8f);
   if (ctha < c23) {
     /* phi error from the inputs: sqrt(2) ein / sin(theta) with
      * sin(theta) >= sqrt(5)/3 here, times 2/pi */
