@@ -691,11 +691,18 @@ typedef struct {
   double idr64, r_last64, dx64, p64[3], idx64, fv64, rmin64, rmax64;
 } cg_imap_args;
 
-/* One listed cell. */
+/* One listed cell.  mode says how its samples find their shell:
+ * CG_SH_SINGLE every sample's shifted radius is certainly in shell j + delta;
+ * CG_SH_EDGE the shifted radii certainly lie in intervals kl = j + delta and
+ * kl + 1, so one comparison with the edge b[kl + 1] decides; CG_SH_WALK the
+ * interval is searched per sample. */
+#define CG_SH_WALK 0
+#define CG_SH_SINGLE 1
+#define CG_SH_EDGE 2
 typedef struct {
   float temp, drr, edrr;
-  int j;      /* shell of the cell's corner radius: its nsub */
-  int single; /* every sample's shifted radius certainly in shell j + delta */
+  int j;     /* shell of the cell's corner radius: its nsub */
+  int mode;
   int delta;
 } cg_imap_cell;
 
@@ -771,14 +778,17 @@ CG_HD int cg_imap_cell_checked(const cg_imap_args *a, int ix, int iy, int iz, fl
   const float e = CG_ADD(CG_ADD(er, o->edrr), CG_MUL(1e-6f, a->dx));
   const float slo = CG_SUB(CG_ADD(rlo, o->drr), e), shi = CG_ADD(CG_ADD(rhi, o->drr), e);
   const int kl = cg_interval(&a->sh, slo), kh = cg_interval(&a->sh, shi);
-  o->single = 0;
+  o->mode = CG_SH_WALK;
   o->delta = 0;
   if (kl == kh) {
     const int sh = a->sh.shell_of[kl + 1];
     if (sh - j >= -1 && sh - j <= 1) {
-      o->single = 1;
+      o->mode = CG_SH_SINGLE;
       o->delta = sh - j;
     }
+  } else if (kh == kl + 1 && kl - j >= -1 && kl - j <= 1) {
+    o->mode = CG_SH_EDGE;
+    o->delta = kl - j;
   }
   return 1;
 }
@@ -803,40 +813,67 @@ CG_HD int cgx_imap_cell(const cg_imap_args *a, int ix, int iy, int iz, const flo
   return 1;
 }
 
-/* A sample in single precision (imap.c:210-231): sub-cell (sx, sy, sz) of
- * the listed cell c at (ix, iy, iz) with nsub ns.  Returns 1 with the shell
- * (*s, maybe -1 or nr: not painted) and the RING pixel when the double
- * arithmetic certainly agrees, 0 when only double can decide. */
+/* Coordinate of sub-cell centre s of cell i along one axis: the corner as
+ * a double-float pair (c, l) plus (s + 1/2) dxs, within 2^-24 (|x| + 2 dx) of
+ * the double centre (imap.c:212-218). */
+CG_HD float cg_imap_coord(const float *c, const float *l, int i, int s, float dxs)
+{
+  return CG_ADD(c[i], CG_FMA(CG_ADD((float)s, 0.5f), dxs, l[i]));
+}
+
+/* The shell of a sample at float radius r (relative position error ein) of
+ * cell c: 1 with *s when the double arithmetic certainly agrees, 0 when
+ * only double can decide. */
+CG_HD int cg_imap_shell_checked(const cg_imap_args *a, const cg_imap_cell *c, float r, float ein, int *s)
+{
+  if (c->mode == CG_SH_SINGLE) {
+    *s = c->j + c->delta;
+    return 1;
+  }
+  const float rs = CG_ADD(r, c->drr);
+  const float e = CG_ADD(CG_FMA(r, CG_ADD(8.0f * CG_E24, ein), c->edrr), CG_MUL(2.0f * CG_E24, cg_fabsf(rs)));
+  if (c->mode == CG_SH_EDGE) {
+    const int kl = c->j + c->delta;
+    const float B = a->sh.b[kl + 1];
+    if (!(cg_fabsf(CG_SUB(rs, B)) > e)) return 0;
+    *s = a->sh.shell_of[(rs >= B ? kl + 1 : kl) + 1];
+    return 1;
+  }
+  const int k = a->sh.contig ? cg_interval_from(&a->sh, c->j, rs) : cg_interval(&a->sh, rs);
+  if (!(cg_interval_margin(&a->sh, k, rs) > e)) return 0;
+  *s = a->sh.shell_of[k + 1];
+  return 1;
+}
+
+/* Shell and RING pixel of the sample at float position (x, y, z) of cell c
+ * (imap.c:210-231): 1 with *s (maybe -1 or nr: not painted) and *pix when the
+ * double arithmetic certainly agrees, 0 when only double can decide. */
+CG_HD int cg_imap_decide(const cg_imap_args *a, const cg_imap_cell *c, float x, float y, float z, int *s,
+                         long long *pix)
+{
+  cg_dir dr = cg_dir_of(x, y, z, 0.0f);
+  /* coordinates within 2^-24 (|x| + 2 dx) of the double ones */
+  const float ein = CG_MUL(1.8f * CG_E24, CG_FMA(2.0f * a->dx, dr.rinv, 1.0f));
+  if (!cg_imap_shell_checked(a, c, CG_MUL(dr.r2, dr.rinv), ein, s)) return 0;
+  if (*s < 0 || *s >= a->sh.nr) return 1;
+  dr.ecth = CG_FMA(2.0f, ein, dr.ecth);
+  const long long p = cg_pix_checked(&dr, a->nside, ein);
+  if (p < 0) return 0;
+  *pix = p;
+  return 1;
+}
+
+/* A sample in single precision: sub-cell (sx, sy, sz) of the listed cell c
+ * at (ix, iy, iz). */
 CG_HD int cg_imap_sample_checked(const cg_imap_args *a, int ix, int iy, int iz, const cg_imap_cell *c, int ns,
                                  int sx, int sy, int sz, int *s, long long *pix)
 {
   const float dxs = a->dxs[c->j + 1];
-  const float x = CG_ADD(a->xc[ix], CG_FMA(CG_ADD((float)sx, 0.5f), dxs, a->xl[ix]));
-  const float y = CG_ADD(a->yc[iy], CG_FMA(CG_ADD((float)sy, 0.5f), dxs, a->yl[iy]));
-  const float z = CG_ADD(a->zc[iz], CG_FMA(CG_ADD((float)sz, 0.5f), dxs, a->zl[iz]));
   (void)ns;
-  const cg_dir dr = cg_dir_of(x, y, z, 0.0f);
-  /* coordinates within 2^-24 (|x| + 2 dx) of the double ones */
-  const float ein = CG_MUL(1.8f * CG_E24, CG_FMA(2.0f * a->dx, dr.rinv, 1.0f));
-  int sh;
-  if (c->single) {
-    sh = c->j + c->delta;
-  } else {
-    const float r = CG_MUL(dr.r2, dr.rinv);
-    const float rs = CG_ADD(r, c->drr);
-    const float e = CG_ADD(CG_FMA(r, CG_ADD(8.0f * CG_E24, ein), c->edrr), CG_MUL(2.0f * CG_E24, cg_fabsf(rs)));
-    const int k = a->sh.contig ? cg_interval_from(&a->sh, c->j, rs) : cg_interval(&a->sh, rs);
-    if (!(cg_interval_margin(&a->sh, k, rs) > e)) return 0;
-    sh = a->sh.shell_of[k + 1];
-  }
-  *s = sh;
-  if (sh < 0 || sh >= a->sh.nr) return 1;
-  cg_dir d2 = dr;
-  d2.ecth = CG_FMA(2.0f, ein, d2.ecth);
-  const long long p = cg_pix_checked(&d2, a->nside, ein);
-  if (p < 0) return 0;
-  *pix = p;
-  return 1;
+  const float x = cg_imap_coord(a->xc, a->xl, ix, sx, dxs);
+  const float y = cg_imap_coord(a->yc, a->yl, iy, sy, dxs);
+  const float z = cg_imap_coord(a->zc, a->zl, iz, sz, dxs);
+  return cg_imap_decide(a, c, x, y, z, s, pix);
 }
 
 /* The sample in double (imap.c:210-231). */

@@ -48,7 +48,7 @@ constexpr int IW = 4;     /* warps per block                     */
 constexpr int ROWS = 2;   /* rows per fetch in k_imap_list        */
 constexpr int CHS = 2048; /* samples per painting chunk           */
 constexpr unsigned FULL = 0xffffffffu;
-constexpr unsigned F_SINGLE = 1u, F_DOUBLE = 8u;
+constexpr unsigned F_DOUBLE = 16u; /* flags: mode (2 bits), delta + 1 (2 bits), double */
 
 /* Per-block copies of the species' shell tables. */
 struct Sh {
@@ -177,7 +177,7 @@ __device__ __forceinline__ cg_imap_rec pack(int ix, int iy, int iz, const cg_ima
   cg_imap_rec r;
   r.ixy = (unsigned)ix | ((unsigned)iy << 16);
   const unsigned short eh = __half_as_ushort(__float2half_ru(c.edrr));
-  r.izf = (unsigned)iz | (flags << 12) | ((unsigned)eh << 16);
+  r.izf = (unsigned)iz | (flags << 11) | ((unsigned)eh << 16);
   r.temp = c.temp;
   r.drr = c.drr;
   return r;
@@ -188,10 +188,10 @@ __device__ __forceinline__ cg_imap_cell unpack(const cg_imap_rec &r, int j, int 
   cg_imap_cell c;
   *ix = (int)(r.ixy & 0xffffu);
   *iy = (int)(r.ixy >> 16);
-  *iz = (int)(r.izf & 0xfffu);
-  const unsigned f = (r.izf >> 12) & 0xfu;
-  c.single = (f & F_SINGLE) ? 1 : 0;
-  c.delta = (int)((f >> 1) & 3u) - 1;
+  *iz = (int)(r.izf & 0x7ffu);
+  const unsigned f = (r.izf >> 11) & 0x1fu;
+  c.mode = (int)(f & 3u);
+  c.delta = (int)((f >> 2) & 3u) - 1;
   *dbl = (f & F_DOUBLE) ? 1 : 0;
   c.edrr = __half2float(__ushort_as_half((unsigned short)(r.izf >> 16)));
   c.temp = r.temp;
@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(IW * 32) k_imap_list(const float *__restrict__
                 c.temp = temp32(A, ix, iy, iz, d);
                 c.drr = (float)drr;
                 c.edrr = 0.0f;
-                c.single = 0;
+                c.mode = CG_SH_WALK;
                 c.delta = 0;
                 dbl = 1;
                 st = 1;
@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(IW * 32) k_imap_list(const float *__restrict__
               const int ns = A.nsub[c.j + 1];
               drawn += (unsigned long long)ns * ns * ns;
               const int sfin = c.j + c.delta;
-              want = !(c.single && (sfin < 0 || sfin >= p.nr));
+              want = !(c.mode == CG_SH_SINGLE && (sfin < 0 || sfin >= p.nr));
             }
           }
         }
@@ -303,8 +303,7 @@ __global__ void __launch_bounds__(IW * 32) k_imap_list(const float *__restrict__
           m &= ~same;
         }
         if (want && !over)
-          p.recs[slot] = pack(ix, iy, iz, c, (c.single ? F_SINGLE : 0u) | ((unsigned)(c.delta + 1) << 1) |
-                                                  (dbl ? F_DOUBLE : 0u));
+          p.recs[slot] = pack(ix, iy, iz, c, (unsigned)c.mode | ((unsigned)(c.delta + 1) << 2) | (dbl ? F_DOUBLE : 0u));
         /* cells past their bucket's room: painted here by the warp */
         unsigned om = __ballot_sync(FULL, want && over);
         while (om) {
@@ -316,7 +315,7 @@ __global__ void __launch_bounds__(IW * 32) k_imap_list(const float *__restrict__
           cc.temp = __shfl_sync(FULL, c.temp, l);
           cc.drr = __shfl_sync(FULL, c.drr, l);
           cc.edrr = __shfl_sync(FULL, c.edrr, l);
-          cc.single = __shfl_sync(FULL, c.single, l);
+          cc.mode = __shfl_sync(FULL, c.mode, l);
           cc.delta = __shfl_sync(FULL, c.delta, l);
           const int cd = __shfl_sync(FULL, dbl, l);
           const int ns = A.nsub[cc.j + 1];
@@ -344,8 +343,24 @@ __global__ void __launch_bounds__(IW * 32) k_imap_list(const float *__restrict__
   }
 }
 
-/* Chunks of every bucket: cells of nsub^3 <= CHS samples go CHS / nsub^3
- * to a chunk; a larger cell is cut into ceil(nsub^3 / CHS) slices. */
+/* Work units of a bucket of nsub ns: whole cells for ns <= 4 (8 to 64
+ * samples), one z-slab of a cell for ns <= 32 (ns^2 samples), one x-line
+ * beyond; each lane of a warp walks one unit. */
+__host__ __device__ __forceinline__ long long units_per_cell(int ns)
+{
+  return ns <= 4 ? 1 : (ns <= 32 ? ns : (long long)ns * ns);
+}
+
+/* Unit groups of 32 per chunk so that a chunk is about CHS samples per lane
+ * count: G = max(1, CHS / (32 x samples per unit)). */
+__host__ __device__ __forceinline__ int groups_per_chunk(int ns)
+{
+  const long long su = (long long)ns * ns * ns / units_per_cell(ns);
+  const long long g = CHS / (32 * su);
+  return g > 1 ? (int)g : 1;
+}
+
+/* Chunks of every bucket: 32 G units each. */
 __global__ void k_imap_chunks(cg_imap_params p)
 {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -353,18 +368,31 @@ __global__ void k_imap_chunks(cg_imap_params p)
   for (int b = 0; b < p.nbk; b++) {
     p.chunk_off[b] = acc;
     const unsigned long long n = p.cnt[b] < (unsigned long long)p.cap[b] ? p.cnt[b] : (unsigned long long)p.cap[b];
-    const long long ns = p.a.nsub[b], s3 = ns * ns * ns;
-    if (n == 0) continue;
-    if (s3 <= CHS) {
-      const unsigned long long R = (unsigned long long)(CHS / s3);
-      acc += (n + R - 1) / R;
-    } else {
-      acc += n * (unsigned long long)((s3 + CHS - 1) / CHS);
-    }
+    const int ns = p.a.nsub[b];
+    const unsigned long long nu = n * (unsigned long long)units_per_cell(ns);
+    const unsigned long long per = 32ull * (unsigned long long)groups_per_chunk(ns);
+    acc += (nu + per - 1) / per;
   }
   p.chunk_off[p.nbk] = acc;
 }
 
+/* Add a run of cnt samples of brightness temp to key k. */
+template <typename K>
+__device__ __forceinline__ void flush(const cg_imap_params &p, K k, unsigned cnt, float temp)
+{
+  if (cnt) {
+    atomicAdd(&p.data[(long long)k], CG_MUL(temp, (float)cnt));
+    atomicAdd(&p.nadd[(long long)k], (int)cnt);
+  }
+}
+
+/* Warps take chunks in bucket order; each lane walks one unit (a cell, a
+ * slab or a line) sample by sample with its row coordinates and the cell's
+ * fields held in registers, keeping two (key, count) slots: a sample whose key
+ * is in a slot adds to it, another key evicts the older slot to the maps.
+ * Every lane of a warp runs the same sample loop (one nsub per bucket), so
+ * the samples that only double can decide are queued with one atomic per
+ * warp and step. */
 template <typename K>
 __global__ void __launch_bounds__(IW * 32) k_imap_paint(cg_imap_params p)
 {
@@ -387,70 +415,107 @@ __global__ void __launch_bounds__(IW * 32) k_imap_paint(cg_imap_params p)
       else hi = mid - 1;
     }
     const int b = lo;
-    const unsigned long long lc = ck - sh.chunk_off[b];
     const unsigned long long nrec =
         p.cnt[b] < (unsigned long long)p.cap[b] ? p.cnt[b] : (unsigned long long)p.cap[b];
     const int ns = sh.nsub[b];
-    const int s3 = ns * ns * ns;
-    const float inv = sh.invns[b];
-    long long r0;  /* first record of the chunk (within the bucket) */
-    int q0, nq;    /* first sample of r0 and the chunk's sample count */
-    int per;       /* samples per record walked in this chunk (s3, or the slice) */
-    if (s3 <= CHS) {
-      const int R = CHS / s3;
-      r0 = (long long)lc * R;
-      const long long r1 = r0 + R < (long long)nrec ? r0 + R : (long long)nrec;
-      q0 = 0;
-      nq = (int)(r1 - r0) * s3;
-      per = s3;
-    } else {
-      const int Kq = (s3 + CHS - 1) / CHS;
-      r0 = (long long)(lc / (unsigned long long)Kq);
-      q0 = (int)(lc % (unsigned long long)Kq) * CHS;
-      nq = s3 - q0 < CHS ? s3 - q0 : CHS;
-      per = 0;
-    }
-    const float inv_s3 = per ? 1.0f / (float)per : 0.0f;
-    const long long rbase = p.base[b] + r0;
-    for (int t0 = 0; t0 < nq; t0 += 32) {
-      const int t = t0 + lane;
-      K key = empty_key<K>();
-      float temp = 0.0f;
-      int rl = 0, q = q0 + t;
-      bool dq = false; /* queued for the double pass */
-      if (t < nq) {
-        if (per) {
-          /* t < CHS: (t + 1/2)/per is exact in float */
-          rl = (int)(((float)t + 0.5f) * inv_s3);
-          q = t - rl * per;
+    const long long U = units_per_cell(ns);
+    const unsigned long long nu = nrec * (unsigned long long)U;
+    const int G = groups_per_chunk(ns);
+    const float dxs = sh.dxs[b];
+    const unsigned long long u0 = (ck - sh.chunk_off[b]) * 32ull * (unsigned long long)G;
+    for (int g = 0; g < G; g++) {
+      const unsigned long long u = u0 + (unsigned long long)g * 32ull + (unsigned long long)lane;
+      const bool valid = u < nu;
+      /* the unit: record and its range of (sz, sy) */
+      long long rl = 0;
+      int z0 = 0, z1 = ns, y0 = 0, y1 = ns;
+      if (valid) {
+        if (U == 1) {
+          rl = (long long)u;
+        } else {
+          rl = (long long)(u / (unsigned long long)U);
+          const int w = (int)(u - (unsigned long long)rl * (unsigned long long)U);
+          if (ns <= 32) {
+            z0 = w;
+            z1 = w + 1;
+          } else {
+            z0 = w / ns;
+            z1 = z0 + 1;
+            y0 = w - z0 * ns;
+            y1 = y0 + 1;
+          }
         }
-        const cg_imap_rec rr = p.recs[rbase + rl];
-        int ix, iy, iz, dbl;
-        const cg_imap_cell c = unpack(rr, b - 1, &ix, &iy, &iz, &dbl);
-        temp = c.temp;
-        int sx, sy, sz, s = -1;
-        long long pix = 0;
-        sub_of(q, ns, inv, &sx, &sy, &sz);
-        if (dbl || p.force_double || !cg_imap_sample_checked(&A, ix, iy, iz, &c, ns, sx, sy, sz, &s, &pix))
-          dq = true;
-        else
-          key = key_of<K>(p, s, pix);
+      } else {
+        z1 = z0 + (ns <= 4 ? ns : 1);
+        y1 = y0 + (ns <= 32 ? ns : 1);
       }
-      /* the queued samples of the step: one atomic for the warp */
-      const unsigned qm = __ballot_sync(FULL, dq);
-      if (qm) {
-        unsigned long long k0 = 0;
-        if (lane == 0) k0 = atomicAdd(&p.ctr[4], (unsigned long long)__popc(qm));
-        k0 = __shfl_sync(FULL, k0, 0);
-        if (dq) {
-          const unsigned long long k = k0 + __popc(qm & ((1u << lane) - 1u));
-          if ((long long)k < p.queue_cap)
-            p.queue[k] = ((unsigned long long)(rbase + rl) << 30) | (unsigned long long)q;
-          else
-            atomicOr(p.err, ERR_IMAP_QUEUE);
+      const long long rec = p.base[b] + rl;
+      cg_imap_cell c;
+      int ix = 0, iy = 0, iz = 0, dbl = 0;
+      float xc = 0.0f, xl = 0.0f, yc = 0.0f, yl = 0.0f, zc = 0.0f, zl = 0.0f;
+      if (valid) {
+        c = unpack(p.recs[rec], b - 1, &ix, &iy, &iz, &dbl);
+        dbl |= p.force_double;
+        xc = A.xc[ix];
+        xl = A.xl[ix];
+        yc = A.yc[iy];
+        yl = A.yl[iy];
+        zc = A.zc[iz];
+        zl = A.zl[iz];
+      } else {
+        c.temp = 0.0f;
+        c.drr = 0.0f;
+        c.edrr = 0.0f;
+        c.j = b - 1;
+        c.mode = CG_SH_SINGLE;
+        c.delta = 0;
+      }
+      K k0 = empty_key<K>(), k1 = empty_key<K>();
+      unsigned n0 = 0, n1 = 0;
+      for (int sz = z0; sz < z1; sz++) {
+        const float z = CG_ADD(zc, CG_FMA(CG_ADD((float)sz, 0.5f), dxs, zl));
+        for (int sy = y0; sy < y1; sy++) {
+          const float y = CG_ADD(yc, CG_FMA(CG_ADD((float)sy, 0.5f), dxs, yl));
+          for (int sx = 0; sx < ns; sx++) {
+            const float x = CG_ADD(xc, CG_FMA(CG_ADD((float)sx, 0.5f), dxs, xl));
+            int s = -1;
+            long long pix = 0;
+            bool dq = false;
+            if (valid) dq = dbl || !cg_imap_decide(&A, &c, x, y, z, &s, &pix);
+            /* the samples only double can decide: one queue atomic per warp */
+            const unsigned qm = __ballot_sync(FULL, dq);
+            if (qm) {
+              unsigned long long q0 = 0;
+              if (lane == __ffs(qm) - 1) q0 = atomicAdd(&p.ctr[4], (unsigned long long)__popc(qm));
+              q0 = __shfl_sync(FULL, q0, __ffs(qm) - 1);
+              if (dq) {
+                const unsigned long long kq = q0 + __popc(qm & ((1u << lane) - 1u));
+                const int q = sx + ns * (sy + ns * sz);
+                if ((long long)kq < p.queue_cap)
+                  p.queue[kq] = ((unsigned long long)rec << 30) | (unsigned long long)q;
+                else
+                  atomicOr(p.err, ERR_IMAP_QUEUE);
+              }
+            }
+            if (!valid || dq) continue;
+            const K key = key_of<K>(p, s, pix);
+            if (key == empty_key<K>()) continue;
+            if (key == k0) {
+              n0++;
+            } else if (key == k1) {
+              n1++;
+            } else {
+              flush<K>(p, k1, n1, c.temp);
+              k1 = k0;
+              n1 = n0;
+              k0 = key;
+              n0 = 1;
+            }
+          }
         }
       }
-      add_runs(key, rl, temp, lane, p);
+      flush<K>(p, k0, n0, c.temp);
+      flush<K>(p, k1, n1, c.temp);
     }
   }
 }

@@ -10,9 +10,10 @@
 #include "cg_dev.cuh"
 #include "cg_exact.h"
 
-/* One listed cell (16 bytes): ix | iy << 16; iz | flags << 12 | half(edrr)
- * << 16 with the flags single (1), delta + 1 (2 bits, shifted by 1) and
- * double (8: every sample decided in double); brightness; radial shift. */
+/* One listed cell (16 bytes): ix | iy << 16; iz | flags << 11 | half(edrr)
+ * << 16 with the flags the shell mode (2 bits, CG_SH_*), delta + 1 (2 bits)
+ * and double (16: every sample decided in double); brightness; radial
+ * shift.  Grids up to 2048 cells a side. */
 struct __align__(16) cg_imap_rec {
   unsigned int ixy, izf;
   float temp, drr;

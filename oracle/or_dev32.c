@@ -519,7 +519,7 @@ int or_imap32(const cg_config *cfg, int ipop, const float *dens, const float *np
                 z0 = cg_cell_coord(iz, s.dx, s.p[2]);
           float rc = cg_norm3(x0, y0, z0);
           c.j = j;
-          c.single = 0;
+          c.mode = CG_SH_WALK;
           c.delta = 0;
           c.temp = cg_imap_temp(bg32(&s, s.tz[ipop], rc), d, bg32(&s, s.bzi[ipop], rc),
                                 cg_bg_eval(norm32, s.r, norm32[CG_NA], norm32[CG_NA + 1], rc, s.r_last, s.idr),
