@@ -734,21 +734,31 @@ CG_HD int cg_imap_cell_checked(const cg_imap_args *a, int ix, int iy, int iz, fl
   if (cg_fabsf(CG_SUB(rc, a->rmin)) <= CG_FMA(cg_fabsf(a->rmin), CG_E24, erc)) return 2;
   if (!(rc <= a->rmax && rc >= a->rmin)) return 0;
   if (!(rc < a->r_last) || cg_fabsf(CG_SUB(rc, a->r_last)) <= erc) return 2;
-  const cg_ve tm = cg_tab_at(a->tz, a->na, a->idr, a->r, rc, erc);
+  /* one table position for the five lookups at rc */
+  const int ir = (int)CG_MUL(rc, a->idr);
+  const float tt = CG_MUL(CG_SUB(rc, a->r[ir]), a->idr);
+  const float dt = CG_FMA(CG_FMA(rc, CG_E24, erc), a->idr, 4.0f * CG_E24);
+  const cg_ve tm = cg_tab_ve(a->tz, a->na, ir, tt, dt);
   if (!(tm.v > tm.e)) return (tm.v == 0.0f && tm.e == 0.0f) ? 0 : 2;
-  const int k = cg_interval(&a->sh, rc);
-  if (!(cg_interval_margin(&a->sh, k, rc) > erc)) return 2;
+  /* the shell of the corner radius fixes nsub; near an edge it is decided
+   * on the double radius (the listing is certain, only j was open) */
+  int k = cg_interval(&a->sh, rc);
+  if (!(cg_interval_margin(&a->sh, k, rc) > erc)) {
+    const double r64 = cgx_norm3(cgx_coord(ix, a->dx64, a->p64[0]), cgx_coord(iy, a->dx64, a->p64[1]),
+                                 cgx_coord(iz, a->dx64, a->p64[2]));
+    k = cgx_interval(&a->sh, r64);
+  }
   const int j = a->sh.shell_of[k + 1];
   o->j = j;
   /* brightness (imap.c:199, 201) and radial shift (imap.c:196-198) */
-  const cg_ve b = cg_tab_at(a->bz, a->na, a->idr, a->r, rc, erc);
-  const cg_ve dn = cg_tab_at(a->norm, a->na, a->idr, a->r, rc, erc);
+  const cg_ve b = cg_tab_ve(a->bz, a->na, ir, tt, dt);
+  const cg_ve dn = cg_tab_ve(a->norm, a->na, ir, tt, dt);
   o->temp = CG_MUL(CG_MUL(tm.v, cg_bias_model(d, b.v, a->bias_model)), dn.v);
   const float u0 = CG_MUL(x0, rinv), u1 = CG_MUL(y0, rinv), u2 = CG_MUL(z0, rinv);
   const float t0 = CG_MUL(v[0], u0), t1 = CG_MUL(v[1], u1), t2 = CG_MUL(v[2], u2);
   const float dot = CG_ADD(CG_ADD(t0, t1), t2);
-  const cg_ve v1 = cg_tab_at(a->v1, a->na, a->idr, a->r, rc, erc);
-  const cg_ve ih = cg_tab_at(a->ih, a->na, a->idr, a->r, rc, erc);
+  const cg_ve v1 = cg_tab_ve(a->v1, a->na, ir, tt, dt);
+  const cg_ve ih = cg_tab_ve(a->ih, a->na, ir, tt, dt);
   const float g = CG_MUL(CG_MUL(a->fvh, v1.v), ih.v);
   o->drr = CG_MUL(dot, g);
   /* the dot product against the double one (unit vector 2^-22 per
@@ -777,7 +787,8 @@ CG_HD int cg_imap_cell_checked(const cg_imap_args *a, int ix, int iy, int iz, fl
   const float er = CG_FMA(rhi, 16.0f * CG_E24, CG_MUL(a->dx, 8.0f * CG_E24));
   const float e = CG_ADD(CG_ADD(er, o->edrr), CG_MUL(1e-6f, a->dx));
   const float slo = CG_SUB(CG_ADD(rlo, o->drr), e), shi = CG_ADD(CG_ADD(rhi, o->drr), e);
-  const int kl = cg_interval(&a->sh, slo), kh = cg_interval(&a->sh, shi);
+  const int kl = a->sh.contig ? cg_interval_from(&a->sh, k, slo) : cg_interval(&a->sh, slo);
+  const int kh = a->sh.contig ? cg_interval_from(&a->sh, k, shi) : cg_interval(&a->sh, shi);
   o->mode = CG_SH_WALK;
   o->delta = 0;
   if (kl == kh) {

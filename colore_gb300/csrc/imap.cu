@@ -223,7 +223,7 @@ __device__ __noinline__ K sample_key_inline(const cg_imap_params &p, const cg_im
 }
 
 template <typename K>
-__global__ void __launch_bounds__(IW * 32) k_imap_list(const float *__restrict__ dens, const float *__restrict__ phi,
+__global__ void __launch_bounds__(IW * 32, 8) k_imap_list(const float *__restrict__ dens, const float *__restrict__ phi,
                                                        cg_imap_params p)
 {
   extern __shared__ __align__(16) unsigned char sraw[];
@@ -394,7 +394,7 @@ __device__ __forceinline__ void flush(const cg_imap_params &p, K k, unsigned cnt
  * the samples that only double can decide are queued with one atomic per
  * warp and step. */
 template <typename K>
-__global__ void __launch_bounds__(IW * 32) k_imap_paint(cg_imap_params p)
+__global__ void __launch_bounds__(IW * 32, 8) k_imap_paint(cg_imap_params p)
 {
   extern __shared__ __align__(16) unsigned char sraw[];
   const Sh sh = load_shells(p, sraw, true);
