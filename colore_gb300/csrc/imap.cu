@@ -223,7 +223,7 @@ __device__ __noinline__ K sample_key_inline(const cg_imap_params &p, const cg_im
 }
 
 template <typename K>
-__global__ void __launch_bounds__(IW * 32, 8) k_imap_list(const float *__restrict__ dens, const float *__restrict__ phi,
+__global__ void __launch_bounds__(IW * 32) k_imap_list(const float *__restrict__ dens, const float *__restrict__ phi,
                                                        cg_imap_params p)
 {
   extern __shared__ __align__(16) unsigned char sraw[];
@@ -376,6 +376,14 @@ __global__ void k_imap_chunks(cg_imap_params p)
   p.chunk_off[p.nbk] = acc;
 }
 
+/* One sample for the double pass, queued on its own. */
+__device__ __noinline__ void queue_one(const cg_imap_params &p, long long rec, int q)
+{
+  const unsigned long long k = atomicAdd(&p.ctr[4], 1ull);
+  if ((long long)k < p.queue_cap) p.queue[k] = ((unsigned long long)rec << 30) | (unsigned long long)q;
+  else atomicOr(p.err, ERR_IMAP_QUEUE);
+}
+
 /* Add a run of cnt samples of brightness temp to key k. */
 template <typename K>
 __device__ __forceinline__ void flush(const cg_imap_params &p, K k, unsigned cnt, float temp)
@@ -394,7 +402,7 @@ __device__ __forceinline__ void flush(const cg_imap_params &p, K k, unsigned cnt
  * the samples that only double can decide are queued with one atomic per
  * warp and step. */
 template <typename K>
-__global__ void __launch_bounds__(IW * 32, 8) k_imap_paint(cg_imap_params p)
+__global__ void __launch_bounds__(IW * 32, 6) k_imap_paint(cg_imap_params p)
 {
   extern __shared__ __align__(16) unsigned char sraw[];
   const Sh sh = load_shells(p, sraw, true);
@@ -472,50 +480,69 @@ __global__ void __launch_bounds__(IW * 32, 8) k_imap_paint(cg_imap_params p)
       }
       K k0 = empty_key<K>(), k1 = empty_key<K>();
       unsigned n0 = 0, n1 = 0;
-      for (int sz = z0; sz < z1; sz++) {
-        const float z = CG_ADD(zc, CG_FMA(CG_ADD((float)sz, 0.5f), dxs, zl));
-        for (int sy = y0; sy < y1; sy++) {
-          const float y = CG_ADD(yc, CG_FMA(CG_ADD((float)sy, 0.5f), dxs, yl));
-          for (int sx = 0; sx < ns; sx++) {
-            const float x = CG_ADD(xc, CG_FMA(CG_ADD((float)sx, 0.5f), dxs, xl));
-            int s = -1;
-            long long pix = 0;
-            bool dq = false;
-            if (valid) dq = dbl || !cg_imap_decide(&A, &c, x, y, z, &s, &pix);
-            /* the samples only double can decide: one queue atomic per warp */
-            const unsigned qm = __ballot_sync(FULL, dq);
-            if (qm) {
-              unsigned long long q0 = 0;
-              if (lane == __ffs(qm) - 1) q0 = atomicAdd(&p.ctr[4], (unsigned long long)__popc(qm));
-              q0 = __shfl_sync(FULL, q0, __ffs(qm) - 1);
-              if (dq) {
-                const unsigned long long kq = q0 + __popc(qm & ((1u << lane) - 1u));
+      /* samples only double can decide: up to four per lane held here and
+       * queued after the unit, the rest queued at once */
+      int nf = 0, f0 = 0, f1 = 0, f2 = 0, f3 = 0;
+      if (valid) {
+        for (int sz = z0; sz < z1; sz++) {
+          const float z = CG_ADD(zc, CG_FMA(CG_ADD((float)sz, 0.5f), dxs, zl));
+          for (int sy = y0; sy < y1; sy++) {
+            const float y = CG_ADD(yc, CG_FMA(CG_ADD((float)sy, 0.5f), dxs, yl));
+#pragma unroll 2
+            for (int sx = 0; sx < ns; sx++) {
+              const float x = CG_ADD(xc, CG_FMA(CG_ADD((float)sx, 0.5f), dxs, xl));
+              int s = -1;
+              long long pix = 0;
+              if (dbl || !cg_imap_decide(&A, &c, x, y, z, &s, &pix)) {
                 const int q = sx + ns * (sy + ns * sz);
-                if ((long long)kq < p.queue_cap)
-                  p.queue[kq] = ((unsigned long long)rec << 30) | (unsigned long long)q;
-                else
-                  atomicOr(p.err, ERR_IMAP_QUEUE);
+                if (nf == 0) f0 = q;
+                else if (nf == 1) f1 = q;
+                else if (nf == 2) f2 = q;
+                else if (nf == 3) f3 = q;
+                else queue_one(p, rec, q);
+                nf++;
+                continue;
               }
-            }
-            if (!valid || dq) continue;
-            const K key = key_of<K>(p, s, pix);
-            if (key == empty_key<K>()) continue;
-            if (key == k0) {
-              n0++;
-            } else if (key == k1) {
-              n1++;
-            } else {
-              flush<K>(p, k1, n1, c.temp);
-              k1 = k0;
-              n1 = n0;
-              k0 = key;
-              n0 = 1;
+              const K key = key_of<K>(p, s, pix);
+              if (key == empty_key<K>()) continue;
+              if (key == k0) {
+                n0++;
+              } else if (key == k1) {
+                n1++;
+              } else {
+                flush<K>(p, k1, n1, c.temp);
+                k1 = k0;
+                n1 = n0;
+                k0 = key;
+                n0 = 1;
+              }
             }
           }
         }
       }
       flush<K>(p, k0, n0, c.temp);
       flush<K>(p, k1, n1, c.temp);
+      /* the held samples: one queue atomic per warp */
+      const int held = nf < 4 ? nf : 4;
+      int incl = held;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += t;
+      }
+      const int tot = __shfl_sync(FULL, incl, 31);
+      if (tot) {
+        unsigned long long q0 = 0;
+        if (lane == 31) q0 = atomicAdd(&p.ctr[4], (unsigned long long)tot);
+        q0 = __shfl_sync(FULL, q0, 31) + (unsigned long long)(incl - held);
+        for (int h = 0; h < held; h++) {
+          const int q = h == 0 ? f0 : (h == 1 ? f1 : (h == 2 ? f2 : f3));
+          if ((long long)(q0 + h) < p.queue_cap)
+            p.queue[q0 + h] = ((unsigned long long)rec << 30) | (unsigned long long)q;
+          else
+            atomicOr(p.err, ERR_IMAP_QUEUE);
+        }
+      }
     }
   }
 }
