@@ -126,6 +126,7 @@ def lib():
             "cg_download_norm64": (C.c_int, [vp, C.c_int, C.c_int, vp, vp]),
             "cg_set_decisions_in_double": (C.c_int, [vp, C.c_int]),
             "cg_exact_stats": (C.c_int, [vp, vp, C.c_int]),
+            "cg_ring_pixels_checked": (C.c_int, [C.c_int, C.c_int, vp, C.c_longlong, C.c_float, vp]),
             "cg_kernel_launches": (C.c_longlong, [vp]),
             "cg_set_profiling": (C.c_int, [vp, C.c_int]),
             "cg_kernel_times": (C.c_int, [vp, C.c_char_p, C.c_size_t, C.POINTER(C.c_float), C.c_int,
@@ -167,7 +168,7 @@ def exported_symbols():
             "cg_set_host_imap", "cg_set_host_kappa", "cg_get_beam_properties", "cg_run_mock", "cg_download_grid",
             "cg_num_sources", "cg_download_catalog", "cg_download_count_map", "cg_download_imap",
             "cg_download_kappa", "cg_download_isw", "cg_download_custom", "cg_download_skewers", "cg_download_norm", "cg_download_norm64", "cg_set_decisions_in_double",
-            "cg_exact_stats", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_read_run_params",
+            "cg_exact_stats", "cg_ring_pixels_checked", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_read_run_params",
             "cg_params_free", "cg_params_to_config", "cg_write_healpix_map", "cg_write_catalog",
             "cg_write_density_grid", "cg_graph_capture", "cg_graph_launch", "cg_batch_create", "cg_batch_run",
             "cg_batch_streams", "cg_batch_tuning", "cg_batch_context", "cg_batch_set_host_catalog",
@@ -179,6 +180,18 @@ def exported_symbols():
 
 class CGError(RuntimeError):
     pass
+
+
+def ring_pixels_checked(nside, xyz, ein=0.0, device=0):
+    """RING pixels of float directions (n x 3) decided on the GPU by the
+    margin-checked single precision of the intensity maps; -1 where only the
+    double arithmetic can decide."""
+    a = np.ascontiguousarray(xyz, np.float32)
+    out = np.empty(len(a), np.int64)
+    rc = lib().cg_ring_pixels_checked(device, nside, a.ctypes.data, len(a), float(ein), out.ctypes.data)
+    if rc:
+        raise CGError("cg_ring_pixels_checked: %s" % ERRORS.get(rc, rc))
+    return out
 
 
 OUT_ASCII, OUT_FITS = 0, 1

@@ -2313,6 +2313,31 @@ extern "C" int cg_download_norm64(cg_ctx *c, int kind, int ipop, double *tab, do
   return CG_OK;
 }
 
+extern "C" int cg_ring_pixels_checked(int device, int nside, const float *xyz, long long n, float ein,
+                                      long long *pix)
+{
+  if (!xyz || !pix || n < 0 || nside < 1 || nside > 8192 || (nside & (nside - 1))) return CG_EINVAL;
+  if (n == 0) return CG_OK;
+  if (cudaSetDevice(device) != cudaSuccess) return CG_ECUDA;
+  int nsm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+  float *dx = nullptr;
+  long long *dp = nullptr;
+  int rc = CG_OK;
+  if (cudaMalloc((void **)&dx, (size_t)n * 3 * sizeof(float)) != cudaSuccess ||
+      cudaMalloc((void **)&dp, (size_t)n * sizeof(long long)) != cudaSuccess) {
+    rc = CG_ENOMEM;
+  } else if (cudaMemcpy(dx, xyz, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+             cg_pix_checked_dev(0, nside, dx, n, ein, dp, nsm) != cudaSuccess ||
+             cudaMemcpy(pix, dp, (size_t)n * sizeof(long long), cudaMemcpyDeviceToHost) != cudaSuccess) {
+    rc = CG_ECUDA;
+  }
+  if (dx) cudaFree(dx);
+  if (dp) cudaFree(dp);
+  cudaGetLastError();
+  return rc;
+}
+
 extern "C" int cg_set_decisions_in_double(cg_ctx *c, int all)
 {
   if (!c) return CG_EINVAL;

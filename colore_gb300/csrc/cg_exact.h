@@ -425,12 +425,12 @@ CG_HD cg_dir cg_dir_of(float x, float y, float z, float ein)
   /* cos(theta): r^2 (2 roundings), rsqrt (2^-22), product (2^-24); the
    * inputs' error ein (relative to r) moves cos(theta) by at most 2 ein */
   o.ecth = CG_FMA(cg_fabsf(o.cth), 8.0f * CG_E24, CG_MUL(2.0f, ein));
-  /* f: atan01 within 1.3 ulp of atan on [0,1] (below 1e-7 absolute); the
-   * ratio's relative error 2^-22 moves atan by at most that times
-   * t/(1+t^2) <= 1/2; the roundings of g and f: 2.4e-7 in all, doubled.  The
-   * inputs' share, which depends on 1/sin(theta), is added by
-   * cg_pix_checked. */
-  o.ef = 4.5e-7f;
+  /* f: atan01 within 1.3 ulp of atan on [0,1] (7.8e-8 absolute below
+   * pi/4), times 2/pi; the ratio's relative error 2^-22 moves atan by at most
+   * that times t/(1+t^2) <= 1/2 (6e-8); the roundings of g and of 1 - g
+   * (3e-8 each): 1.5e-7 in all, taken as 2.5e-7.  The inputs' share, which
+   * depends on 1/sin(theta), is added by cg_pix_checked. */
+  o.ef = 2.5e-7f;
   return o;
 }
 
@@ -454,7 +454,9 @@ CG_HD long long cg_pix_checked(const cg_dir *d, int nside, float ein)
     const float hf = CG_ADD(0.5f, d->f);
     const float A = CG_MUL(ns, CG_FMA(-0.75f, d->cth, hf));
     const float B = CG_MUL(ns, CG_FMA(0.75f, d->cth, hf));
-    const float ev = CG_FMA(ns, CG_FMA(0.75f, d->ecth, CG_ADD(ef, 3.0f * CG_E24 * 2.25f)), 1e-9f);
+    /* roundings of 0.5 + f (<= 1.5) and of the fused multiply-add (<= 2.25):
+     * 1.8e-7, taken as 2.5e-7 */
+    const float ev = CG_FMA(ns, CG_FMA(0.75f, d->ecth, CG_ADD(ef, 2.5e-7f)), 1e-9f);
     const float fa = floorf(A), fb = floorf(B);
     const float da = CG_SUB(A, fa), db = CG_SUB(B, fb);
     const float dm = cg_fminf(cg_fminf(da, CG_SUB(1.0f, da)), cg_fminf(db, CG_SUB(1.0f, db)));

@@ -488,7 +488,7 @@ __global__ void __launch_bounds__(IW * 32, 6) k_imap_paint(cg_imap_params p)
           const float z = CG_ADD(zc, CG_FMA(CG_ADD((float)sz, 0.5f), dxs, zl));
           for (int sy = y0; sy < y1; sy++) {
             const float y = CG_ADD(yc, CG_FMA(CG_ADD((float)sy, 0.5f), dxs, yl));
-#pragma unroll 2
+#pragma unroll 4
             for (int sx = 0; sx < ns; sx++) {
               const float x = CG_ADD(xc, CG_FMA(CG_ADD((float)sx, 0.5f), dxs, xl));
               int s = -1;
@@ -612,7 +612,28 @@ cudaError_t launch(cudaStream_t s, const float *dens, const float *phi, const cg
   return cudaGetLastError();
 }
 
+/* RING pixels of float directions by the margin-checked single-precision
+ * decision, on the device. */
+__global__ void k_pix_checked(int nside, const float *__restrict__ xyz, long long n, float ein, long long *pix)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    cg_dir d = cg_dir_of(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], 0.0f);
+    d.ecth = CG_FMA(2.0f, ein, d.ecth);
+    pix[i] = cg_pix_checked(&d, nside, ein);
+  }
+}
+
 } /* namespace */
+
+cudaError_t cg_pix_checked_dev(cudaStream_t s, int nside, const float *xyz, long long n, float ein, long long *pix,
+                               int nsm)
+{
+  long long blocks = (n + 255) / 256;
+  if (blocks > (long long)nsm * 8) blocks = (long long)nsm * 8;
+  if (blocks < 1) blocks = 1;
+  k_pix_checked<<<(unsigned)blocks, 256, 0, s>>>(nside, xyz, n, ein, pix);
+  return cudaGetLastError();
+}
 
 size_t cg_imap_shell_smem(int nr, int nbk) { return shell_smem(nr, nbk, true); }
 

@@ -49,6 +49,11 @@ struct cg_imap_params {
 };
 
 cudaError_t cg_imap_paint(cudaStream_t s, const float *dens, const float *phi, const cg_imap_params *p, int nsm);
+/* RING pixels of n float directions (device arrays) at nside by the
+ * margin-checked decision the painting uses, with coordinate error ein
+ * relative to r; -1 where only double can decide. */
+cudaError_t cg_pix_checked_dev(cudaStream_t s, int nside, const float *xyz, long long n, float ein, long long *pix,
+                               int nsm);
 /* Shared memory of the painting kernel for nr shells and nbk buckets. */
 size_t cg_imap_shell_smem(int nr, int nbk);
 

@@ -312,6 +312,13 @@ int cg_set_profiling(cg_ctx *ctx, int on);
  * decisions taken in double since the last reset: [0] cells' counts,
  * [1] source pixels, [2] intensity-map cells, [3] intensity-map samples. */
 int cg_set_decisions_in_double(cg_ctx *ctx, int all);
+/* The RING pixel decision of the intensity maps on its own, on device
+ * `device`: pix[i] = he_ang2pix(nside, cos theta, phi) of direction
+ * xyz[3i..3i+2] (host arrays) as the reference's double arithmetic decides
+ * it, or -1 where the single-precision margin does not prove the decision
+ * (the kernels then decide in double); ein bounds the coordinates' error
+ * relative to |xyz|.  nside a power of two up to 8192. */
+int cg_ring_pixels_checked(int device, int nside, const float *xyz, long long n, float ein, long long *pix);
 int cg_exact_stats(cg_ctx *ctx, unsigned long long *out4, int reset);
 int cg_kernel_times(cg_ctx *ctx, char *names, size_t names_len, float *ms, int cap, int *n);
 

@@ -25,11 +25,11 @@ HOST_SRCS = ["host_cosmo.c", "host_params.c", "host_io.c", "host_pred.c"]
 def build(verbose=False):
     os.makedirs(OUTDIR, exist_ok=True)
     srcs = [os.path.join(HERE, s) for s in SRCS] + [os.path.join(HOST, s) for s in HOST_SRCS]
+    csrc = os.path.join(ROOT, "colore_gb300", "csrc")
     deps = srcs + [os.path.join(HERE, "oracle.h"),
-                   os.path.join(ROOT, "colore_gb300", "csrc", "cg_math.h"),
-                   os.path.join(ROOT, "colore_gb300", "csrc", "cg_cell.h"),
                    os.path.join(ROOT, "include", "colore_cuda.h"),
                    os.path.join(ROOT, "include", "colore_host.h")]
+    deps += [os.path.join(csrc, f) for f in os.listdir(csrc) if f.endswith(".h")]
     deps += [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".h")]
     if os.path.exists(LIB) and all(os.path.getmtime(d) <= os.path.getmtime(LIB) for d in deps):
         return LIB
