@@ -345,7 +345,10 @@ int cg_host_cosmo_set(cg_params *p, char *err, size_t el)
   p->r_min = cg_cosmo_chi(&c, 1 / (1 + p->z_min));
   p->r_max = cg_cosmo_chi(&c, 1 / (1 + p->z_max));
   p->prefac_lensing = 1.5 * p->hubble_0 * p->hubble_0 * p->omega_m;
-  p->l_box = 2 * p->r_max * (1 + 2. / p->n_grid);
+  /* cosmo.c:544-547; l_box is a flouble, a float in the single-precision
+   * build (common.h:277) that this path reproduces, so the box side is the
+   * float nearest the double expression and the observer sits at its half */
+  p->l_box = (double)(float)(2 * p->r_max * (1 + 2. / p->n_grid));
   p->pos_obs[0] = p->pos_obs[1] = p->pos_obs[2] = 0.5 * p->l_box;
   int rc;
   cg_spline snz[CG_NPOP_MAX], sbz[CG_NPOP_MAX], stz[CG_NPOP_MAX], sbi[CG_NPOP_MAX], skc[CG_NPOP_MAX],
