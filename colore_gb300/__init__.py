@@ -670,6 +670,13 @@ class Mock64:
         self._chk(lib().cg64_download(self._c, 4, 0, m.ctypes.data), "cg64_download")
         return m
 
+    def count_map(self, ipop):
+        """Sources of population ipop per RING pixel at nside_count[ipop]."""
+        ns = self.cfg.nside_count[ipop]
+        m = np.empty(12 * ns * ns, np.int32)
+        self._chk(lib().cg64_download(self._c, 6, ipop, m.ctypes.data), "cg64_download")
+        return m
+
     def norm_table(self, tracer):
         t = np.empty(NA, np.float64)
         self._chk(lib().cg64_download(self._c, 5, tracer, t.ctypes.data), "cg64_download")

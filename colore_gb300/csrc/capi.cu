@@ -115,6 +115,7 @@ struct cg_ctx {
   /* normalisation bins */
   unsigned long long *d_ncount = nullptr;
   double *d_zsum = nullptr, *d_bsum = nullptr;
+  unsigned long long *d_bacc = nullptr; /* fixed-point accumulators of the bin sums */
   int pending_mode = CG_DMODE_NONE;
   /* sources */
   unsigned short *d_counts = nullptr;
@@ -718,7 +719,7 @@ extern "C" void cg_destroy(cg_ctx *c)
     if (q) cudaFree(q);
   void *ptrs[] = {c->d_tabs, c->d_norm, c->d_tabs64, c->d_norm64, c->d_corner, c->d_xstats, c->d_zr, c->d_r2n, c->d_pk, c->d_twN, c->d_twH, c->d_dens, c->d_npot, c->d_disp[0],
                   c->d_disp[1], c->d_disp[2], c->d_part, c->d_stats, c->d_s2f, c->d_err, c->d_ncount,
-                  c->d_zsum, c->d_bsum, c->d_counts, c->d_bsums, c->d_total, c->d_tmpmap, c->d_kmap,
+                  c->d_zsum, c->d_bsum, c->d_bacc, c->d_counts, c->d_bsums, c->d_total, c->d_tmpmap, c->d_kmap,
                   c->d_kfac, c->d_kinv, c->d_kir, c->d_ovf_cell, c->d_ovf_cnt, c->d_ovf_n,
                   c->d_recs, c->d_imap_queue, c->d_imap_ctr,
                   c->d_imap_isw, c->d_ifac, c->d_iir, c->d_cfac, c->d_losfac};
@@ -936,14 +937,14 @@ static int run_bins(cg_ctx *c, int nz, double idz)
   if (nz > c->bins_nz_cap || std::max(nt, 1) > c->bins_nt_cap) { /* grow only */
     c->bins_nz_cap = c->bins_nt_cap = 0;
     if ((rc = dalloc(c, &c->d_ncount, (size_t)nz)) || (rc = dalloc(c, &c->d_zsum, (size_t)nz)) ||
-        (rc = dalloc(c, &c->d_bsum, (size_t)std::max(nt, 1) * nz)))
+        (rc = dalloc(c, &c->d_bsum, (size_t)std::max(nt, 1) * nz)) ||
+        (rc = dalloc(c, &c->d_bacc, (size_t)2 * (1 + std::max(nt, 1)) * nz)))
       return rc;
     c->bins_nz_cap = nz;
     c->bins_nt_cap = std::max(nt, 1);
   }
   CUDA_TRY(c, cudaMemsetAsync(c->d_ncount, 0, sizeof(unsigned long long) * nz, c->stream));
-  CUDA_TRY(c, cudaMemsetAsync(c->d_zsum, 0, sizeof(double) * nz, c->stream));
-  CUDA_TRY(c, cudaMemsetAsync(c->d_bsum, 0, sizeof(double) * std::max(nt, 1) * nz, c->stream));
+  CUDA_TRY(c, cudaMemsetAsync(c->d_bacc, 0, sizeof(unsigned long long) * 2 * (1 + nt) * nz, c->stream));
   cg_bins_params p;
   memset(&p, 0, sizeof(p));
   p.box = c->box;
@@ -959,13 +960,14 @@ static int run_bins(cg_ctx *c, int nz, double idz)
   p.nt = nt;
   for (int t = 0; t < nt; t++) p.bz[t] = tracer_bias(c, t);
   p.ncount = c->d_ncount;
+  p.acc = c->d_bacc;
   p.zsum = c->d_zsum;
   p.bsum = c->d_bsum;
   {
     ProfScope ps(c, "dens_bins");
     CUDA_TRY(c, cg_dens_bins(c->stream, c->d_dens, &p, c->nsm));
   }
-  c->launches++;
+  c->launches += 2;
   c->pending_mode = CG_DMODE_NONE;
   return CG_OK;
 }
@@ -1041,10 +1043,10 @@ extern "C" int cg_collect_density_normalization_static(cg_ctx *c, int nz, double
   unsigned long long *ncount = static_cast<unsigned long long *>(scratch);
   double *zsum = static_cast<double *>(scratch) + CG_BINS_STATIC_NZ;
   double *bsum = static_cast<double *>(scratch) + 2 * CG_BINS_STATIC_NZ;
+  unsigned long long *acc = static_cast<unsigned long long *>(scratch) + (size_t)(2 + cg_dens_bins_max_tracers()) * CG_BINS_STATIC_NZ;
   /* the sums start at zero on every call */
   CUDA_TRY(c, cudaMemsetAsync(ncount, 0, sizeof(unsigned long long) * nz, c->stream));
-  CUDA_TRY(c, cudaMemsetAsync(zsum, 0, sizeof(double) * nz, c->stream));
-  if (nt > 0) CUDA_TRY(c, cudaMemsetAsync(bsum, 0, sizeof(double) * nt * nz, c->stream));
+  CUDA_TRY(c, cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * 2 * (1 + nt) * nz, c->stream));
   cg_bins_params p;
   memset(&p, 0, sizeof(p));
   p.box = c->box;
@@ -1060,13 +1062,14 @@ extern "C" int cg_collect_density_normalization_static(cg_ctx *c, int nz, double
   p.nt = nt;
   for (int t = 0; t < nt; t++) p.bz[t] = tracer_bias(c, t);
   p.ncount = ncount;
+  p.acc = acc;
   p.zsum = zsum;
   p.bsum = bsum;
   {
     ProfScope ps(c, "dens_bins");
     CUDA_TRY(c, cg_dens_bins(c->stream, c->d_dens, &p, c->nsm));
   }
-  c->launches++;
+  c->launches += 2;
   c->pending_mode = CG_DMODE_NONE;
   if (narr)
     CUDA_TRY(c, cudaMemcpyAsync(narr, ncount, nz * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));

@@ -15,7 +15,11 @@
  *                    memory: integer counts and compensated (Kahan) FP32
  *                    sums, since FP64 arithmetic is scarce on this GPU.  Each
  *                    block combines its warps' bins in FP64 in a fixed order
- *                    and sends them to global memory with one atomic each.
+ *                    and adds them to global 128-bit fixed-point
+ *                    accumulators with integer atomics, whose sum does not
+ *                    depend on the order the blocks arrive in.
+ *  k_bins_finish   : the accumulators back to FP64 sums, the same bits on
+ *                    every run.
  *  k_lpt_deposit   : 1LPT particle positions (density.c:473-501) and their
  *                    NGP, CIC or TSC deposit (density.c:37-187), staged per
  *                    tile of particles in shared memory.
@@ -79,6 +83,34 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v)
   const float t = __fadd_rn(s, y);
   c = __fsub_rn(__fsub_rn(t, s), y);
   s = t;
+}
+
+/* 128-bit two's-complement fixed point with FIX_FRAC fraction bits, as a
+ * (low, high) pair of u64: integer additions commute, so the total of the
+ * blocks' FP64 partials is the same whatever order they arrive in.  A
+ * partial x (|x| < 2^(127 - FIX_FRAC)) is rounded to the nearest multiple
+ * of 2^-FIX_FRAC: |x| 2^(FIX_FRAC - 64) splits exactly into its integer part
+ * (the high word) and its fraction, which scaled by 2^64 is the low word. */
+constexpr int FIX_FRAC = 60;
+constexpr double FIX_HI = 16.0;                                        /* 2^(64 - FIX_FRAC) */
+constexpr double FIX_LO = 1.0 / 1152921504606846976.0;                 /* 2^-FIX_FRAC */
+constexpr double FIX_TO_HI = 1.0 / 16.0;                               /* 2^(FIX_FRAC - 64) */
+constexpr double TWO64 = 18446744073709551616.0;
+
+__device__ __forceinline__ void fix_add(unsigned long long *a, double x)
+{
+  const bool neg = x < 0.0;
+  const double y = __dmul_rn(fabs(x), FIX_TO_HI);
+  const double h = floor(y);
+  const double f = __dsub_rn(y, h); /* exact: y >= 0 */
+  unsigned long long hi = __double2ull_rn(h), lo = __double2ull_rn(__dmul_rn(f, TWO64));
+  if (neg) {
+    lo = ~lo + 1ull;
+    hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+  }
+  const unsigned long long old = atomicAdd(a, lo);
+  const unsigned long long carry = (old + lo < old) ? 1ull : 0ull;
+  if (hi + carry) atomicAdd(a + 1, hi + carry);
 }
 
 /* Shared-memory bytes of one warp's bins: u32 count, then (sum, correction)
@@ -181,11 +213,30 @@ __global__ void __launch_bounds__(BINS_WARPS * 32, 2) k_dens_bins(float *grid, c
         const float *aw = reinterpret_cast<const float *>(cw + nz);
         sum += (double)aw[(size_t)b * W + k - 1] - (double)aw[(size_t)nz * W + (size_t)b * W + k - 1];
       }
-      if (sum != 0.0) {
-        if (k == 1) atomicAdd(&p.zsum[b], sum);
-        else atomicAdd(&p.bsum[(size_t)(k - 2) * nz + b], sum);
-      }
+      if (sum != 0.0) fix_add(p.acc + 2 * ((size_t)(k - 1) * nz + b), sum);
     }
+  }
+}
+
+/* Accumulator value v -> FP64: redshift sums v = b, bias sums of tracer t at
+ * v = (1 + t) nz + b.  One rounding from the exact 128-bit sum (the high
+ * part holds at most 2^53 in magnitude for any realistic grid). */
+__global__ void __launch_bounds__(256) k_bins_finish(const unsigned long long *__restrict__ acc, int nz, int nt,
+                                                    double *__restrict__ zsum, double *__restrict__ bsum)
+{
+  const int nv = nz * (1 + nt);
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
+    unsigned long long lo = acc[2 * (size_t)v], hi = acc[2 * (size_t)v + 1];
+    const bool neg = (long long)hi < 0;
+    if (neg) { /* two's complement of the 128-bit pair */
+      lo = ~lo + 1ull;
+      hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+    }
+    /* value = hi 2^(64 - FIX_FRAC) + lo 2^-FIX_FRAC */
+    double d = __dadd_rn(__dmul_rn(__ull2double_rn(hi), FIX_HI), __dmul_rn(__ull2double_rn(lo), FIX_LO));
+    if (neg) d = -d;
+    if (v < nz) zsum[v] = d;
+    else bsum[v - nz] = d;
   }
 }
 
@@ -448,16 +499,23 @@ cudaError_t cg_dens_bins(cudaStream_t s, float *grid, const cg_bins_params *p, i
   long long cap = (long long)nsm * 8;
   if (blocks > cap) blocks = cap;
   k_dens_bins<<<(unsigned)blocks, nwb * 32, smem, s>>>(grid, *p);
+  if (p->nz > 0) {
+    const int nv = p->nz * (1 + p->nt);
+    k_bins_finish<<<(nv + 255) / 256, 256, 0, s>>>(p->acc, p->nz, p->nt, p->zsum, p->bsum);
+  }
   return cudaGetLastError();
 }
 
 int cg_dens_bins_max_tracers(void) { return MAXT; }
 
 /* Scratch of the allocation-free bins entry: u64 counts [CG_BINS_STATIC_NZ],
- * redshift sums [CG_BINS_STATIC_NZ], bias sums [MAXT][nz] (doubles).  A
- * module-scope array costs no allocation call at run time: it exists in
- * every context that loads this module. */
-static __device__ __align__(256) unsigned char g_bins_scratch[(size_t)CG_BINS_STATIC_NZ * (2 + MAXT) * 8];
+ * redshift sums [CG_BINS_STATIC_NZ], bias sums [MAXT][nz] (doubles), then
+ * the 128-bit accumulators [1 + MAXT][nz][2] (u64).  A module-scope array
+ * costs no allocation call at run time: it exists in every context that
+ * loads this module. */
+static_assert(CG_BINS_STATIC_BYTES == (size_t)CG_BINS_STATIC_NZ * ((2 + MAXT) + 2 * (1 + MAXT)) * 8,
+              "static bins scratch layout");
+static __device__ __align__(256) unsigned char g_bins_scratch[CG_BINS_STATIC_BYTES];
 
 cudaError_t cg_dens_bins_static_scratch(void **ptr, size_t *bytes)
 {

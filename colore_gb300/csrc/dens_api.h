@@ -19,9 +19,10 @@ struct cg_bins_params {
   float idz;
   int nt, bias_model;
   cg::Tab bz[8];          /* bias tables of the tracers of this launch */
-  unsigned long long *ncount; /* [nz] */
-  double *zsum;               /* [nz] */
-  double *bsum;               /* [nt][nz] */
+  unsigned long long *ncount; /* [nz], zeroed by the caller */
+  unsigned long long *acc;    /* [1 + nt][nz][2] fixed-point sums, zeroed by the caller */
+  double *zsum;               /* [nz], written from acc */
+  double *bsum;               /* [nt][nz], written from acc */
   unsigned int *err;          /* device error bits (mode CG_DMODE_RHO) */
 };
 
@@ -57,9 +58,11 @@ cudaError_t cg_norm_tables(cudaStream_t s, const unsigned long long *ncount, con
 
 /* Largest number of redshift bins of the allocation-free bins entry, whose
  * scratch (per bin: cell count, redshift sum and one bias sum per tracer,
- * for up to cg_dens_bins_max_tracers() tracers) is a fixed device array of
- * CG_BINS_STATIC_NZ * 10 * 8 bytes = 80 KiB. */
+ * for up to cg_dens_bins_max_tracers() = 8 tracers, and a 16-byte
+ * accumulator for each sum) is a fixed device array of
+ * CG_BINS_STATIC_NZ * 28 * 8 bytes = 224 KiB. */
 #define CG_BINS_STATIC_NZ 1024
+#define CG_BINS_STATIC_BYTES ((size_t)CG_BINS_STATIC_NZ * 28 * 8)
 /* Device address and size of that array in the current device's context. */
 cudaError_t cg_dens_bins_static_scratch(void **ptr, size_t *bytes);
 cudaError_t cg_lpt_cic(cudaStream_t s, float *grid, const float *dx, const float *dy, const float *dz,

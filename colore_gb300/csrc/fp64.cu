@@ -1103,7 +1103,8 @@ extern "C" long long cg64_num_sources(const cg64_ctx *c, int ipop)
  * map data (nr * npix doubles, RING, summed temperatures) and 3 its hit
  * counts (ints) of species ipop; 4 convergence (n_kappa * npix doubles,
  * RING); 5 normalisation tables (CG_NA doubles of tracer ipop, sources
- * first). */
+ * first); 6 source count map of population ipop (12 nside_count^2 ints,
+ * RING). */
 extern "C" int cg64_download(cg64_ctx *c, int what, int ipop, void *dst)
 {
   if (!c || !dst) return CG_EINVAL;
@@ -1127,6 +1128,12 @@ extern "C" int cg64_download(cg64_ctx *c, int what, int ipop, void *dst)
     if (!c->d_kmap) return fail(c, CG_ESTATE, "no convergence maps");
     const size_t m = (size_t)c->cfg.n_kappa * 12 * c->cfg.nside_kappa * c->cfg.nside_kappa;
     CU(c, cudaMemcpy(dst, c->d_kmap, m * sizeof(double), cudaMemcpyDeviceToHost));
+    return CG_OK;
+  }
+  if (what == 6) {
+    if (ipop < 0 || ipop >= c->cfg.n_srcs || !c->d_cmap[ipop]) return fail(c, CG_ESTATE, "no count map %d", ipop);
+    const size_t m = 12ull * c->cfg.nside_count[ipop] * c->cfg.nside_count[ipop];
+    CU(c, cudaMemcpy(dst, c->d_cmap[ipop], m * sizeof(int), cudaMemcpyDeviceToHost));
     return CG_OK;
   }
   if (what == 5) {

@@ -161,7 +161,7 @@ int cg_collect_density_normalization(cg_ctx *ctx, int nz, double idz, double *za
 /* Allocation-free variant of cg_collect_density_normalization (no
  * counterpart in the reference): same arguments and results, for callers
  * that may not allocate while the pipeline runs (a fixed memory budget, a
- * pool that must not grow).  Its per-bin scratch is a fixed 80 KiB
+ * pool that must not grow).  Its per-bin scratch is a fixed 224 KiB
  * module-scope device array rather than cudaMalloc'd buffers, so
  *  - nz is limited to 2..1024 bins (CG_EINVAL beyond, with a message);
  *  - the first call on each device looks up that array's address with the
@@ -343,7 +343,8 @@ int cg64_create_cartesian_fields(cg64_ctx *ctx);
 /* what: 0 density, 1 potential (N^3 doubles, [z][y][x]); 2 intensity-map
  * temperature sums and 3 hit counts (int) of species ipop (nr * npix, RING);
  * 4 convergence (n_kappa * npix doubles, RING); 5 normalisation table of
- * tracer ipop (CG_NA doubles; source populations first, then species).
+ * tracer ipop (CG_NA doubles; source populations first, then species);
+ * 6 source count map of population ipop (12 nside_count^2 ints, RING).
  * dst of 0 and 1 may be host or device memory. */
 int cg64_download(cg64_ctx *ctx, int what, int ipop, void *dst);
 

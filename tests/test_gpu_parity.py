@@ -608,6 +608,14 @@ def test_rerun_is_deterministic(runs, tmp_path):
         assert np.array_equal(m.catalog(ip, src=False)["pos"], r.need('cats')[ip]["pos"])
     assert np.array_equal(m.kappa(), r.kappa)
     assert m.launches() > 0
+    # the normalisation sums do not depend on the order the blocks finish
+    m2 = cg.Mock(r.params)
+    m2.run()
+    for kind, npop in ((0, r.cfg.n_srcs), (1, r.cfg.n_imap)):
+        for ip in range(npop):
+            for a, b in zip(m.norm_table64(kind, ip), m2.norm_table64(kind, ip)):
+                assert np.array_equal(a.view(np.uint64), b.view(np.uint64)), (kind, ip)
+    m2.close()
 
 
 def test_stage_order_is_enforced(runs):
