@@ -306,7 +306,8 @@ def run_ours(args):
     if rank != 0:
         return
     out = {
-        "metric": METRIC, "value": job_cells_per_s(ncell, world, t_step), "unit": "cells/s", "n_gpus": world,
+        "metric": METRIC if args.config == "c4" and not args.n else "end-to-end cells/s, %s %d^3" % (args.config, n),
+        "value": job_cells_per_s(ncell, world, t_step), "unit": "cells/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (EH98 no-wiggle P(k), analytic N(z)/b(z)/T(z); random seeds per rank)",
@@ -323,6 +324,7 @@ def run_ours(args):
         "sources": nsrc,
         "wall_s_timed": t_wall,
         "roofline": rl,
+        "fft_plan": m.field_plan(),
         "roofline_dominant": {"kernel": dom[0], "ms": round(dom[1], 3), "share": round(dom[1] / (t_step * 1e3), 3),
                               "bound": "instruction issue (ncu: 91 % issue-active, 7 % of DRAM peak at 512^3)"
                               if dom[0] == "imap_paint" else "see kernels"} if dom else None,

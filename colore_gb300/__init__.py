@@ -129,6 +129,8 @@ def lib():
             "cg_ring_pixels_checked": (C.c_int, [C.c_int, C.c_int, vp, C.c_longlong, C.c_float, vp]),
             "cg_kernel_launches": (C.c_longlong, [vp]),
             "cg_set_profiling": (C.c_int, [vp, C.c_int]),
+            "cg_set_field_variant": (C.c_int, [vp, C.c_int, C.c_int]),
+            "cg_field_plan": (C.c_int, [vp, C.c_char_p, C.c_size_t]),
             "cg_kernel_times": (C.c_int, [vp, C.c_char_p, C.c_size_t, C.POINTER(C.c_float), C.c_int,
                                           C.POINTER(C.c_int)]),
             "cg64_create": (C.c_int, [C.POINTER(vp), C.POINTER(Config), C.c_int]),
@@ -168,7 +170,7 @@ def exported_symbols():
             "cg_set_host_imap", "cg_set_host_kappa", "cg_get_beam_properties", "cg_run_mock", "cg_download_grid",
             "cg_num_sources", "cg_download_catalog", "cg_download_count_map", "cg_download_imap",
             "cg_download_kappa", "cg_download_isw", "cg_download_custom", "cg_download_skewers", "cg_download_norm", "cg_download_norm64", "cg_set_decisions_in_double",
-            "cg_exact_stats", "cg_ring_pixels_checked", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_read_run_params",
+            "cg_exact_stats", "cg_ring_pixels_checked", "cg_kernel_launches", "cg_set_profiling", "cg_kernel_times", "cg_set_field_variant", "cg_field_plan", "cg_read_run_params",
             "cg_params_free", "cg_params_to_config", "cg_write_healpix_map", "cg_write_catalog",
             "cg_write_density_grid", "cg_graph_capture", "cg_graph_launch", "cg_batch_create", "cg_batch_run",
             "cg_batch_streams", "cg_batch_tuning", "cg_batch_context", "cg_batch_set_host_catalog",
@@ -523,6 +525,22 @@ class Mock:
         e = np.empty(2, np.float64)
         self._chk(lib().cg_download_norm64(self._c, kind, ipop, t.ctypes.data, e.ctypes.data), "download_norm64")
         return t, e
+
+    # passes of the transform whose tile width the autotuner picks
+    PASSES = {"fill2": 0, "fill3": 1, "y": 2, "x": 3}
+
+    def set_field_variant(self, pass_name, v):
+        """Force tile variant v (0 the plan's, 1 half, 2 twice; -1 the tuner's
+        choice) for one pass of the transforms."""
+        self._chk(lib().cg_set_field_variant(self._c, self.PASSES[pass_name], v), "set_field_variant")
+
+    def field_plan(self):
+        """The transform passes' tile widths in use at this grid size and the
+        autotuner's timings per candidate (ms), as a dict."""
+        import json
+        buf = C.create_string_buffer(4096)
+        self._chk(lib().cg_field_plan(self._c, buf, len(buf)), "field_plan")
+        return json.loads(buf.value.decode())
 
     def set_decisions_in_double(self, on=True):
         """Take every integer decision (counts, pixels, hits) in double."""

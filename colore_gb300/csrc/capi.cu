@@ -152,6 +152,7 @@ struct cg_ctx {
   long long knpix = 0;
   /* optional per-kernel event log */
   int profiling = 0;
+  int fforce[4] = {-1, -1, -1, -1}; /* forced tile variant per pass (CG_PASS_*), -1: the tuner's */
   struct Ev {
     const char *name;
     cudaEvent_t a, b;
@@ -345,6 +346,141 @@ static cudaError_t run_lpt2(int n, const cg_field_launch *L)
 #undef X
   }
   return cudaErrorInvalidValue;
+}
+
+static int field_tile(int n, int pass, int v)
+{
+  switch (n) {
+#define X(k) \
+  case k:    \
+    return cg_field_tile_##k(pass, v);
+    CG_FIELD_SIZES(X)
+#undef X
+  }
+  return 0;
+}
+
+static cudaError_t field_pass(int n, const cg_field_launch *L, int pass, int v, int nf)
+{
+  switch (n) {
+#define X(k) \
+  case k:    \
+    return cg_field_pass_##k(L, pass, v, nf);
+    CG_FIELD_SIZES(X)
+#undef X
+  }
+  return cudaErrorInvalidValue;
+}
+
+/* ---- tile autotuner of the transform passes ------------------------------
+ * The first time a grid size runs on a device, each pass (the two fills,
+ * the y and the x pass) is timed with every valid tile variant on the
+ * context's own grids (before the real passes overwrite them): one launch to
+ * warm up, then the mean of three with CUDA events.  The fastest variant is
+ * kept for the life of the process, for every context of that size on that
+ * device.  Variants differ only in block shape, so the choice never changes
+ * a result.  COLORE_GB300_TUNE=0 keeps the plans' tiles. */
+struct FieldTune {
+  bool done[4] = {false, false, false, false};
+  int var[4] = {0, 0, 0, 0};
+  float ms[4][3] = {{-1, -1, -1}, {-1, -1, -1}, {-1, -1, -1}, {-1, -1, -1}};
+};
+static std::mutex g_tune_mu;
+static std::vector<std::pair<long long, FieldTune>> g_tune; /* key: device * 65536 + N */
+
+static FieldTune *tune_entry(int device, int n)
+{
+  const long long key = (long long)device * 65536 + n;
+  for (auto &e : g_tune)
+    if (e.first == key) return &e.second;
+  g_tune.emplace_back(key, FieldTune());
+  return &g_tune.back().second;
+}
+
+static bool tuning_enabled()
+{
+  const char *e = getenv("COLORE_GB300_TUNE");
+  return !(e && e[0] == '0');
+}
+
+/* Tune the passes listed (nf grids each) unless done; fills L->var. */
+static int tune_field_passes(cg_ctx *c, cg_field_launch *L, const int *passes, const int *nfs, int np)
+{
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  FieldTune *t = tune_entry(c->device, c->N);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CUDA_TRY(c, cudaStreamIsCapturing(c->stream, &cs));
+  const bool can = tuning_enabled() && cs == cudaStreamCaptureStatusNone;
+  for (int i = 0; i < np && can; i++) {
+    const int pass = passes[i];
+    if (t->done[pass]) continue;
+    cudaEvent_t e0, e1;
+    CUDA_TRY(c, cudaEventCreate(&e0));
+    CUDA_TRY(c, cudaEventCreate(&e1));
+    float best = 3.0e38f;
+    int bv = 0;
+    for (int v = 0; v < 3; v++) {
+      t->ms[pass][v] = -1.0f;
+      if (!field_tile(c->N, pass, v)) continue;
+      cudaError_t e = field_pass(c->N, L, pass, v, nfs[i]);
+      if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
+      for (int r = 0; r < 3 && e == cudaSuccess; r++) e = field_pass(c->N, L, pass, v, nfs[i]);
+      if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float ms = 0.0f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (e != cudaSuccess) { /* a variant the device refuses (resources) is skipped */
+        cudaGetLastError();
+        continue;
+      }
+      t->ms[pass][v] = ms / 3.0f;
+      if (t->ms[pass][v] < best) {
+        best = t->ms[pass][v];
+        bv = v;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    t->var[pass] = bv;
+    t->done[pass] = true;
+  }
+  for (int p = 0; p < 4; p++) L->var[p] = c->fforce[p] >= 0 ? c->fforce[p] : t->var[p];
+  return CG_OK;
+}
+
+extern "C" int cg_set_field_variant(cg_ctx *c, int pass, int v)
+{
+  if (!c) return CG_EINVAL;
+  if (pass < 0 || pass > 3 || v < -1 || v > 2) return fail(c, CG_EINVAL, "pass %d, variant %d out of range", pass, v);
+  if (v >= 0 && !field_tile(c->N, pass, v))
+    return fail(c, CG_EINVAL, "variant %d of pass %d is not valid at %d^3", v, pass, c->N);
+  c->fforce[pass] = v;
+  return CG_OK;
+}
+
+extern "C" int cg_field_plan(cg_ctx *c, char *buf, size_t len)
+{
+  if (!c || !buf || !len) return CG_EINVAL;
+  static const char *names[4] = {"fill2", "fill3", "y", "x"};
+  static const char *tiles[4] = {"TX", "TX", "TXY", "RB"};
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  const FieldTune *t = tune_entry(c->device, c->N);
+  size_t o = (size_t)snprintf(buf, len, "{\"n_grid\": %d, \"tuned\": %s", c->N, tuning_enabled() ? "true" : "false");
+  for (int p = 0; p < 4 && o < len; p++) {
+    const int v = c->fforce[p] >= 0 ? c->fforce[p] : t->var[p];
+    o += (size_t)snprintf(buf + o, len - o, ", \"%s\": {\"%s\": %d, \"timed\": %s, \"ms\": {", names[p], tiles[p],
+                          field_tile(c->N, p, v), t->done[p] ? "true" : "false");
+    bool first = true;
+    for (int w = 0; w < 3 && o < len; w++) {
+      const int tw = field_tile(c->N, p, w);
+      if (!tw || t->ms[p][w] < 0) continue;
+      o += (size_t)snprintf(buf + o, len - o, "%s\"%d\": %.4f", first ? "" : ", ", tw, t->ms[p][w]);
+      first = false;
+    }
+    if (o < len) o += (size_t)snprintf(buf + o, len - o, "}}");
+  }
+  if (o < len) snprintf(buf + o, len - o, "}");
+  return o < len ? CG_OK : fail(c, CG_EINVAL, "buffer of %zu bytes too short", len);
 }
 
 static size_t npartials(int n)
@@ -820,6 +956,11 @@ extern "C" int cg_create_cartesian_fields(cg_ctx *c)
   L.twH = c->d_twH;
   L.src = nullptr;
   L.err = c->d_err;
+  L.ev = nullptr;
+  {
+    const int passes[3] = {CG_PASS_FILL2, CG_PASS_Y, CG_PASS_X}, nfs[3] = {2, 2, 1};
+    if (int rc = tune_field_passes(c, &L, passes, nfs, 3)) return rc;
+  }
   {
     ProfScope ps(c, "field_fft");
     PassEvents pe(c, "field_fill", "field_y", "field_x");
@@ -873,6 +1014,11 @@ extern "C" int cg_compute_physical_density_field(cg_ctx *c)
     L.twN = c->d_twN;
     L.twH = c->d_twH;
     L.err = c->d_err;
+    {
+      for (int a = 0; a < 3; a++) L.f[a] = reinterpret_cast<float2 *>(c->d_disp[a]);
+      const int passes[3] = {CG_PASS_FILL3, CG_PASS_Y, CG_PASS_X}, nfs[3] = {3, 3, 3};
+      if (int rc = tune_field_passes(c, &L, passes, nfs, 3)) return rc;
+    }
     if (two) { /* lpt_2, density.c:646-812 */
       ProfScope ps(c, "lpt2_fft");
       for (int set = 0; set < 2; set++) { /* xx xy xz, then yy yz zz */

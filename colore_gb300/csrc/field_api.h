@@ -21,7 +21,14 @@ struct cg_field_launch {
   float2 *src;          /* 2LPT: the source grid (padded real in, destroyed) */
   unsigned int *err;    /* device error word (bulk-copy timeouts) */
   cudaEvent_t *ev;      /* NULL, or events recorded after each pass (fill+z, y, x) */
+  int var[4];           /* tile variant of each pass (CG_PASS_*): 0 the plan's, 1 half, 2 twice */
 };
+
+/* Passes whose tile width the autotuner picks. */
+#define CG_PASS_FILL2 0 /* fill + z of the Gaussian field and potential */
+#define CG_PASS_FILL3 1 /* fill + z of the 1LPT displacements          */
+#define CG_PASS_Y 2     /* column transforms along y                   */
+#define CG_PASS_X 3     /* row c2r along x (without the moment sums)   */
 
 #define CG_FIELD_SIZES(X) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(1024) X(2048)
 
@@ -29,7 +36,9 @@ struct cg_field_launch {
   extern "C" cudaError_t cg_field_gauss_##n(const cg_field_launch *L); \
   extern "C" cudaError_t cg_field_lpt_##n(const cg_field_launch *L);   \
   extern "C" cudaError_t cg_field_lpt2_##n(const cg_field_launch *L);  \
-  extern "C" size_t cg_field_npartials_##n(void);
+  extern "C" size_t cg_field_npartials_##n(void);                      \
+  extern "C" int cg_field_tile_##n(int pass, int v);                    \
+  extern "C" cudaError_t cg_field_pass_##n(const cg_field_launch *L, int pass, int v, int nf);
 CG_FIELD_SIZES(CG_FIELD_DECL)
 #undef CG_FIELD_DECL
 

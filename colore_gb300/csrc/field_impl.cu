@@ -331,10 +331,11 @@ __global__ void __launch_bounds__(TX *PF) k_z_lpt2(const float2 *__restrict__ sr
   }
 }
 
-/* Pass 3: row c2r along x with normalisation and optional moment sums.
- * grid = (N*N/RB, nf).  partials[blockIdx.x] = (sum d, sum d^2). */
-template <bool STATS>
-__global__ void __launch_bounds__(PL::RB *PR) k_row_c2r(float2 *f0, float2 *f1, float2 *f2, float norm,
+/* Pass 3: row c2r along x with normalisation and optional moment sums,
+ * RB rows per block.  grid = (N*N/RB, nf).  partials[blockIdx.x] =
+ * (sum d, sum d^2). */
+template <bool STATS, int RB>
+__global__ void __launch_bounds__(RB *PR) k_row_c2r(float2 *f0, float2 *f1, float2 *f2, float norm,
                                                         double2 *partials, const float2 *__restrict__ twN,
                                                         const float2 *__restrict__ twH, unsigned int *err)
 {
@@ -342,12 +343,12 @@ __global__ void __launch_bounds__(PL::RB *PR) k_row_c2r(float2 *f0, float2 *f1, 
   __shared__ uint64_t bar;
   const int t = threadIdx.x % PR, rl = threadIdx.x / PR;
   float2 *f = blockIdx.y == 0 ? f0 : (blockIdx.y == 1 ? f1 : f2);
-  const size_t row0 = (size_t)blockIdx.x * PL::RB;
+  const size_t row0 = (size_t)blockIdx.x * RB;
   /* the block's rows, contiguous in HBM (RB NH float2, a multiple of 16
    * bytes at a 16-byte boundary since RB is even), in one bulk copy; they
    * land at a stride of NH and the transform then exchanges through the
    * same buffer at the padded stride ROWS, once every input is loaded */
-  if (!cgtma::stage_rows(smem, f + row0 * NH, (unsigned)(PL::RB * NH * sizeof(float2)), &bar, err)) return;
+  if (!cgtma::stage_rows(smem, f + row0 * NH, (unsigned)(RB * NH * sizeof(float2)), &bar, err)) return;
   const float2 *rin = smem + rl * NH;
   float2 *row = smem + rl * ROWS;
   float2 *dst = f + (row0 + rl) * NH;
@@ -390,7 +391,7 @@ __global__ void __launch_bounds__(PL::RB *PR) k_row_c2r(float2 *f0, float2 *f1, 
     __syncthreads();
     if (threadIdx.x == 0) {
       double a = 0.0, b = 0.0;
-      for (int w = 0; w < (PL::RB * PR + 31) / 32; w++) {
+      for (int w = 0; w < (RB * PR + 31) / 32; w++) {
         a += red[0][w];
         b += red[1][w];
       }
@@ -405,6 +406,122 @@ cudaError_t prep(K kern, size_t smem)
   return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
+/* ---- tile candidates of the autotuner ----------------------------------
+ * Each pass has up to three tile widths: variant 0 is the plan's (fft_plans.h),
+ * 1 half of it, 2 twice it.  A variant is valid when its shared memory fits
+ * in 200 KiB and its block in 1024 threads (x pass: an even row count, for
+ * the 16-byte bulk copy).  Only the block shape changes: every column and
+ * row goes through the same transform, so all variants give the same bits.
+ * The x pass that also sums the moments keeps the plan's RB, since the
+ * per-block partial sums depend on it. */
+constexpr size_t SMEM_MAX = 200u * 1024u;
+constexpr int tile_of(int def, int v) { return v == 1 ? def / 2 : (v == 2 ? def * 2 : def); }
+constexpr bool fill_ok(int T) { return T >= 1 && (size_t)2 * N * T * sizeof(float2) <= SMEM_MAX && T * PF <= 1024; }
+constexpr bool y_ok(int T) { return T >= 1 && (size_t)N * T * sizeof(float2) <= SMEM_MAX && T * P <= 1024; }
+constexpr bool x_ok(int R)
+{
+  return R >= 2 && R % 2 == 0 && ((size_t)N * N) % R == 0 && (size_t)R * ROWS * sizeof(float2) <= SMEM_MAX &&
+         R * PR <= 1024;
+}
+static_assert(fill_ok(PL::TX2) && fill_ok(PL::TX3) && y_ok(PL::TXY) && x_ok(PL::RB), "plan out of limits");
+
+template <int T>
+cudaError_t fill2(const cg_field_launch *L)
+{
+  if constexpr (!fill_ok(T)) {
+    return cudaErrorInvalidValue;
+  } else {
+    const size_t sm = (size_t)2 * N * T * sizeof(float2);
+    cudaError_t e = prep(k_fill_z<2, T>, sm);
+    if (e != cudaSuccess) return e;
+    dim3 g((NH + T - 1) / T, N);
+    k_fill_z<2, T><<<g, T * PF, sm, L->stream>>>(L->f[0], L->f[1], nullptr, L->fill, L->twN);
+    return cudaGetLastError();
+  }
+}
+
+template <int T>
+cudaError_t fill3(const cg_field_launch *L)
+{
+  if constexpr (!fill_ok(T)) {
+    return cudaErrorInvalidValue;
+  } else {
+    const size_t sm = (size_t)2 * N * T * sizeof(float2); /* one value per mode + the exchange buffer */
+    cudaError_t e = prep(k_fill_z3<T>, sm);
+    if (e != cudaSuccess) return e;
+    dim3 g((NH + T - 1) / T, N);
+    k_fill_z3<T><<<g, T * PF, sm, L->stream>>>(L->f[0], L->f[1], L->f[2], L->fill, L->twN);
+    return cudaGetLastError();
+  }
+}
+
+template <int T, int S>
+cudaError_t ypass(const cg_field_launch *L, float2 *a, float2 *b, float2 *c, int nf)
+{
+  if constexpr (!y_ok(T)) {
+    return cudaErrorInvalidValue;
+  } else {
+    const size_t sm = (size_t)N * T * sizeof(float2);
+    cudaError_t e = prep(k_col_y<T, S>, sm);
+    if (e != cudaSuccess) return e;
+    dim3 g((NH + T - 1) / T, N, nf);
+    k_col_y<T, S><<<g, T * P, sm, L->stream>>>(a, b, c, L->twN);
+    return cudaGetLastError();
+  }
+}
+
+template <bool STATS, int R>
+cudaError_t xpass(const cg_field_launch *L, float2 *a, float2 *b, float2 *c, int nf, float norm, double2 *part)
+{
+  if constexpr (!x_ok(R)) {
+    return cudaErrorInvalidValue;
+  } else {
+    const size_t sm = (size_t)R * ROWS * sizeof(float2);
+    cudaError_t e = prep(k_row_c2r<STATS, R>, sm);
+    if (e != cudaSuccess) return e;
+    dim3 g((unsigned)((size_t)N * N / R), nf);
+    k_row_c2r<STATS, R><<<g, R * PR, sm, L->stream>>>(a, b, c, norm, part, L->twN, L->twH, L->err);
+    return cudaGetLastError();
+  }
+}
+
+cudaError_t fill2_v(const cg_field_launch *L, int v)
+{
+  switch (v) {
+    case 1: return fill2<tile_of(PL::TX2, 1)>(L);
+    case 2: return fill2<tile_of(PL::TX2, 2)>(L);
+    default: return fill2<PL::TX2>(L);
+  }
+}
+
+cudaError_t fill3_v(const cg_field_launch *L, int v)
+{
+  switch (v) {
+    case 1: return fill3<tile_of(PL::TX3, 1)>(L);
+    case 2: return fill3<tile_of(PL::TX3, 2)>(L);
+    default: return fill3<PL::TX3>(L);
+  }
+}
+
+template <int S>
+cudaError_t ypass_v(const cg_field_launch *L, int v, float2 *a, float2 *b, float2 *c, int nf)
+{
+  switch (v) {
+    case 1: return ypass<tile_of(PL::TXY, 1), S>(L, a, b, c, nf);
+    case 2: return ypass<tile_of(PL::TXY, 2), S>(L, a, b, c, nf);
+    default: return ypass<PL::TXY, S>(L, a, b, c, nf);
+  }
+}
+
+cudaError_t xpass_v(const cg_field_launch *L, int v, float2 *a, float2 *b, float2 *c, int nf)
+{
+  switch (v) {
+    case 1: return xpass<false, tile_of(PL::RB, 1)>(L, a, b, c, nf, L->norm, nullptr);
+    case 2: return xpass<false, tile_of(PL::RB, 2)>(L, a, b, c, nf, L->norm, nullptr);
+    default: return xpass<false, PL::RB>(L, a, b, c, nf, L->norm, nullptr);
+  }
+}
+
 } /* namespace */
 
 #define CG_CAT2(a, b) a##b
@@ -414,26 +531,13 @@ cudaError_t prep(K kern, size_t smem)
 extern "C" cudaError_t CG_CAT(cg_field_gauss_, CG_N)(const cg_field_launch *L)
 {
   using namespace cg;
-  constexpr int TX2 = PL::TX2, TXY = PL::TXY;
-  size_t sm1 = (size_t)2 * N * TX2 * sizeof(float2);
-  size_t sm2 = (size_t)N * TXY * sizeof(float2);
-  size_t sm3 = (size_t)PL::RB * ROWS * sizeof(float2);
   cudaError_t e;
-  if ((e = prep(k_fill_z<2, TX2>, sm1)) != cudaSuccess) return e;
-  if ((e = prep(k_col_y<TXY, 1>, sm2)) != cudaSuccess) return e;
-  if ((e = prep(k_row_c2r<true>, sm3)) != cudaSuccess) return e;
-  if ((e = prep(k_row_c2r<false>, sm3)) != cudaSuccess) return e;
-  dim3 g1((NH + TX2 - 1) / TX2, N);
-  k_fill_z<2, TX2><<<g1, TX2 * PF, sm1, L->stream>>>(L->f[0], L->f[1], nullptr, L->fill, L->twN);
+  if ((e = fill2_v(L, L->var[CG_PASS_FILL2])) != cudaSuccess) return e;
   if (L->ev) cudaEventRecord(L->ev[0], L->stream);
-  dim3 g2((NH + TXY - 1) / TXY, N, 2);
-  k_col_y<TXY, 1><<<g2, TXY * P, sm2, L->stream>>>(L->f[0], L->f[1], nullptr, L->twN);
+  if ((e = ypass_v<1>(L, L->var[CG_PASS_Y], L->f[0], L->f[1], nullptr, 2)) != cudaSuccess) return e;
   if (L->ev) cudaEventRecord(L->ev[1], L->stream);
-  dim3 g3((unsigned)((size_t)N * N / PL::RB), 1);
-  k_row_c2r<true><<<g3, PL::RB * PR, sm3, L->stream>>>(L->f[0], nullptr, nullptr, L->norm, L->partials,
-                                                        L->twN, L->twH, L->err);
-  k_row_c2r<false><<<g3, PL::RB * PR, sm3, L->stream>>>(L->f[1], nullptr, nullptr, L->norm, nullptr,
-                                                         L->twN, L->twH, L->err);
+  if ((e = xpass<true, PL::RB>(L, L->f[0], nullptr, nullptr, 1, L->norm, L->partials)) != cudaSuccess) return e;
+  if ((e = xpass_v(L, L->var[CG_PASS_X], L->f[1], nullptr, nullptr, 1)) != cudaSuccess) return e;
   if (L->ev) cudaEventRecord(L->ev[2], L->stream);
   return cudaGetLastError();
 }
@@ -442,23 +546,12 @@ extern "C" cudaError_t CG_CAT(cg_field_gauss_, CG_N)(const cg_field_launch *L)
 extern "C" cudaError_t CG_CAT(cg_field_lpt_, CG_N)(const cg_field_launch *L)
 {
   using namespace cg;
-  constexpr int TX3 = PL::TX3, TXY = PL::TXY;
-  size_t sm1 = (size_t)2 * N * TX3 * sizeof(float2); /* one value per mode + the exchange buffer */
-  size_t sm2 = (size_t)N * TXY * sizeof(float2);
-  size_t sm3 = (size_t)PL::RB * ROWS * sizeof(float2);
   cudaError_t e;
-  if ((e = prep(k_fill_z3<TX3>, sm1)) != cudaSuccess) return e;
-  if ((e = prep(k_col_y<TXY, 1>, sm2)) != cudaSuccess) return e;
-  if ((e = prep(k_row_c2r<false>, sm3)) != cudaSuccess) return e;
-  dim3 g1((NH + TX3 - 1) / TX3, N);
-  k_fill_z3<TX3><<<g1, TX3 * PF, sm1, L->stream>>>(L->f[0], L->f[1], L->f[2], L->fill, L->twN);
+  if ((e = fill3_v(L, L->var[CG_PASS_FILL3])) != cudaSuccess) return e;
   if (L->ev) cudaEventRecord(L->ev[0], L->stream);
-  dim3 g2((NH + TXY - 1) / TXY, N, 3);
-  k_col_y<TXY, 1><<<g2, TXY * P, sm2, L->stream>>>(L->f[0], L->f[1], L->f[2], L->twN);
+  if ((e = ypass_v<1>(L, L->var[CG_PASS_Y], L->f[0], L->f[1], L->f[2], 3)) != cudaSuccess) return e;
   if (L->ev) cudaEventRecord(L->ev[1], L->stream);
-  dim3 g3((unsigned)((size_t)N * N / PL::RB), 3);
-  k_row_c2r<false><<<g3, PL::RB * PR, sm3, L->stream>>>(L->f[0], L->f[1], L->f[2], 1.0f, nullptr, L->twN,
-                                                         L->twH, L->err);
+  if ((e = xpass_v(L, L->var[CG_PASS_X], L->f[0], L->f[1], L->f[2], 3)) != cudaSuccess) return e;
   if (L->ev) cudaEventRecord(L->ev[2], L->stream);
   return cudaGetLastError();
 }
@@ -469,31 +562,52 @@ extern "C" cudaError_t CG_CAT(cg_field_lpt_, CG_N)(const cg_field_launch *L)
 extern "C" cudaError_t CG_CAT(cg_field_lpt2_, CG_N)(const cg_field_launch *L)
 {
   using namespace cg;
-  constexpr int TX3 = PL::TX3, TXY = PL::TXY;
+  constexpr int TX3 = PL::TX3;
   size_t smr = (size_t)PL::RB * (ROWS + LH) * sizeof(float2);
-  size_t sm2 = (size_t)N * TXY * sizeof(float2);
   size_t smz = (size_t)2 * N * TX3 * sizeof(float2);
-  size_t sm3 = (size_t)PL::RB * ROWS * sizeof(float2);
   cudaError_t e;
   if ((e = prep(k_row_r2c, smr)) != cudaSuccess) return e;
-  if ((e = prep(k_col_y<TXY, -1>, sm2)) != cudaSuccess) return e;
   if ((e = prep(k_z_lpt2<TX3>, smz)) != cudaSuccess) return e;
-  if ((e = prep(k_col_y<TXY, 1>, sm2)) != cudaSuccess) return e;
-  if ((e = prep(k_row_c2r<false>, sm3)) != cudaSuccess) return e;
   dim3 gr((unsigned)((size_t)N * N / PL::RB), 1);
   k_row_r2c<<<gr, PL::RB * PR, smr, L->stream>>>(L->src, L->twN, L->twH, L->err);
-  dim3 gy1((NH + TXY - 1) / TXY, N, 1);
-  k_col_y<TXY, -1><<<gy1, TXY * P, sm2, L->stream>>>(L->src, nullptr, nullptr, L->twN);
+  if ((e = ypass_v<-1>(L, L->var[CG_PASS_Y], L->src, nullptr, nullptr, 1)) != cudaSuccess) return e;
   dim3 gz((NH + TX3 - 1) / TX3, N);
   const float inv_n3 = 1.0f / ((float)N * (float)N * (float)N);
   k_z_lpt2<TX3><<<gz, TX3 * PF, smz, L->stream>>>(L->src, L->f[0], L->f[1], L->f[2], L->fill.dk, inv_n3, L->twN);
-  dim3 g2((NH + TXY - 1) / TXY, N, 3);
-  k_col_y<TXY, 1><<<g2, TXY * P, sm2, L->stream>>>(L->f[0], L->f[1], L->f[2], L->twN);
-  dim3 g3((unsigned)((size_t)N * N / PL::RB), 3);
-  k_row_c2r<false><<<g3, PL::RB * PR, sm3, L->stream>>>(L->f[0], L->f[1], L->f[2], 1.0f, nullptr, L->twN,
-                                                         L->twH, L->err);
+  if ((e = ypass_v<1>(L, L->var[CG_PASS_Y], L->f[0], L->f[1], L->f[2], 3)) != cudaSuccess) return e;
+  cg_field_launch L1 = *L;
+  L1.norm = 1.0f;
+  if ((e = xpass_v(&L1, L->var[CG_PASS_X], L->f[0], L->f[1], L->f[2], 3)) != cudaSuccess) return e;
   return cudaGetLastError();
 }
 
 /* Number of blocks of the moment-sum pass (size of the partials array). */
 extern "C" size_t CG_CAT(cg_field_npartials_, CG_N)(void) { return (size_t)N * N / PL::RB; }
+
+/* Tile width of variant v of a pass (CG_PASS_*), or 0 when the variant is
+ * not valid at this size. */
+extern "C" int CG_CAT(cg_field_tile_, CG_N)(int pass, int v)
+{
+  if (v < 0 || v > 2) return 0;
+  switch (pass) {
+    case CG_PASS_FILL2: return fill_ok(tile_of(PL::TX2, v)) ? tile_of(PL::TX2, v) : 0;
+    case CG_PASS_FILL3: return fill_ok(tile_of(PL::TX3, v)) ? tile_of(PL::TX3, v) : 0;
+    case CG_PASS_Y: return y_ok(tile_of(PL::TXY, v)) ? tile_of(PL::TXY, v) : 0;
+    case CG_PASS_X: return x_ok(tile_of(PL::RB, v)) ? tile_of(PL::RB, v) : 0;
+  }
+  return 0;
+}
+
+/* One pass alone with variant v, for timing: the fills write f[0..1] (two
+ * fields) or f[0..2] (three); the y and x passes transform f[0..nf-1] in
+ * place (inverse, no moment sums). */
+extern "C" cudaError_t CG_CAT(cg_field_pass_, CG_N)(const cg_field_launch *L, int pass, int v, int nf)
+{
+  switch (pass) {
+    case CG_PASS_FILL2: return fill2_v(L, v);
+    case CG_PASS_FILL3: return fill3_v(L, v);
+    case CG_PASS_Y: return ypass_v<1>(L, v, L->f[0], nf > 1 ? L->f[1] : nullptr, nf > 2 ? L->f[2] : nullptr, nf);
+    case CG_PASS_X: return xpass_v(L, v, L->f[0], nf > 1 ? L->f[1] : nullptr, nf > 2 ? L->f[2] : nullptr, nf);
+  }
+  return cudaErrorInvalidValue;
+}

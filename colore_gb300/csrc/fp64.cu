@@ -25,8 +25,9 @@
  *   k64_kappa     convergence                     kappa.c:78-175
  *
  * Random numbers come from the Philox streams of the FP32 path; the Poisson
- * deviate is drawn in double (inversion below 10, PTRS above).  Sources are
- * written in an unspecified order (one atomic cursor).
+ * deviate is drawn in double from the same uniforms (inversion below 10,
+ * PTRS above), so a cell whose mean agrees draws the same count.  Sources
+ * are written in an unspecified order (one atomic cursor).
  */
 #include <cuda_runtime.h>
 #include <cufft.h>
@@ -42,6 +43,7 @@
 #include "../../include/colore_cuda.h"
 #include "cg_math.h"
 #include "cg_cell.h"
+#include "cg_exact.h"
 
 struct cg64_ctx {
   cg_config cfg;
@@ -348,34 +350,13 @@ __global__ void k64_bins(P64 p, const double *dens, int nz, double idz, int bias
   }
 }
 
-/* Poisson deviate in double: inversion below 10, PTRS (Hormann 1993) above. */
+/* Poisson deviate in double from the FP32 path's streams (cg_exact.h): the
+ * cell's uniform from its word of the shared Philox block, inversion below
+ * 10, PTRS (Hormann 1993) above. */
 __device__ long long poisson64(double lam, uint32_t k0, uint32_t k1, long long cid)
 {
   if (!(lam > 0)) return 0;
-  if (lam < 10) {
-    const cg_u32x4 w = cg_philox4x32_10((uint32_t)cid, (uint32_t)(cid >> 32), 0u, 0u, k0, k1);
-    const double u = cg_u01d(w.v[0], w.v[1]);
-    double q = exp(-lam), F = q;
-    long long k = 0;
-    while (u >= F && k < 200) {
-      k++;
-      q *= lam / k;
-      F += q;
-    }
-    return k;
-  }
-  const double slam = sqrt(lam), b = 0.931 + 2.53 * slam, a = -0.059 + 0.02483 * b;
-  const double inva = 1.1239 + 1.1328 / (b - 3.4), vr = 0.9277 - 3.6224 / (b - 2);
-  for (uint32_t it = 0; it < 64u; it++) {
-    const cg_u32x4 w = cg_philox4x32_10((uint32_t)cid, (uint32_t)(cid >> 32), it, 0u, k0, k1);
-    const double U = cg_u01d(w.v[0], w.v[1]) - 0.5, V = cg_u01d(w.v[2], w.v[3]);
-    const double us = 0.5 - fabs(U);
-    const double kf = floor((2 * a / us + b) * U + lam + 0.43);
-    if (us >= 0.07 && V <= vr) return (long long)kf;
-    if (kf < 0 || (us < 0.013 && V > us)) continue;
-    if (log(V * inva / (a / (us * us) + b)) <= -lam + kf * log(lam) - lgamma(kf + 1)) return (long long)kf;
-  }
-  return (long long)floor(lam);
+  return cgx_poisson(lam, (double)cg_u01f(cg_pois_word(cid, k0, k1)), cid, k0, k1);
 }
 
 struct Src64 {

@@ -322,6 +322,20 @@ int cg_ring_pixels_checked(int device, int nside, const float *xyz, long long n,
 int cg_exact_stats(cg_ctx *ctx, unsigned long long *out4, int reset);
 int cg_kernel_times(cg_ctx *ctx, char *names, size_t names_len, float *ms, int cap, int *n);
 
+/* Tile autotuner of the transform passes (no counterpart in the reference;
+ * the reference plans with FFTW_ESTIMATE, src/fourier.c:84-91).  The first
+ * time a grid size runs on a device, each pass -- pass 0 the fill + z of the
+ * Gaussian field and potential, 1 the fill + z of the 1LPT displacements,
+ * 2 the y columns, 3 the x rows -- is timed with each valid tile width (the
+ * plan's, half, twice) on the context's grids and the fastest is kept for
+ * the process.  Tile widths change only the block shape: results are the
+ * same bits.  Environment COLORE_GB300_TUNE=0 keeps the plans' widths.
+ * cg_set_field_variant forces variant v (0 plan, 1 half, 2 twice; -1 back to
+ * the tuner) of one pass for this context; cg_field_plan writes the widths
+ * in use and the timings as a JSON object. */
+int cg_set_field_variant(cg_ctx *ctx, int pass, int v);
+int cg_field_plan(cg_ctx *ctx, char *buf, size_t len);
+
 /* Launch accounting: number of kernels this context has launched. */
 long long cg_kernel_launches(const cg_ctx *ctx);
 

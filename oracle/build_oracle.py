@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 OUTDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUTDIR, "liboracle.so")
-SRCS = ["or_fft.c", "or_ref64.c", "or_dev32.c", "or_checks.c"]
+SRCS = ["or_fft.c", "or_ref64.c", "or_dev32.c", "or_checks.c", "or_sht.c"]
 HOST = os.path.join(ROOT, "colore_gb300", "csrc", "host")
 HOST_SRCS = ["host_cosmo.c", "host_params.c", "host_io.c", "host_pred.c"]
 

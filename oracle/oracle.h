@@ -100,4 +100,9 @@ int or_lens32(const cg_config *cfg, const float *npot, long long n, const float 
 int or_skw32(const cg_config *cfg, const float *dens, const float *npot, int gauss, float sigma2f, long long n,
              const float *pos4, float *dout, float *vout);
 
+/* or_sht.c: Legendre part of the FP64 map -> a_lm analysis (per m and
+ * northern ring, symmetric / antisymmetric ring Fourier sums of K maps). */
+int or_sht_legendre(int lmax, int nring, int K, const double *z, const double *S, const double *A, double omega,
+                    double *alm);
+
 #endif

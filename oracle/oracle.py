@@ -52,6 +52,7 @@ def lib():
             "or_shell_index": [vp, vp, i, vp, vp, vp, C.c_long],
             "or_pix_checked": [C.c_long, vp, C.c_long, f, vp], "or_pix_cgx": [C.c_long, vp, C.c_long, vp],
             "or_pix64": [C.c_long, vp, C.c_long, vp],
+            "or_sht_legendre": [i, i, i, vp, vp, vp, d, vp],
         }
         void = ("or_philox", "or_poisson", "or_ang2pix", "or_nest2ring", "or_ring2nest", "or_pix2vec_nest",
                 "or_shell_index", "or_pix_checked", "or_pix_cgx", "or_pix64")

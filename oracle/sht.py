@@ -17,10 +17,13 @@ F_m = exp(-i m phi_0) sum_j map_j exp(-2 pi i m j / n_ring) (periodic in m,
 so m >= n_ring folds back), and per m the normalised associated Legendre
 functions lambda_lm(z) (Condon-Shortley phase) come from the standard
 three-term recursion in l, started from lambda_mm evaluated in logarithms so
-that the polar rings underflow to zero instead of overflowing.  The ring
-geometry is that of he_ang2pix (healpix_extra.c:141-172): the tests check
-that every pixel centre produced here maps back to its own index, and the
-transform itself against scipy's spherical harmonics on small maps.
+that the polar rings underflow to zero instead of overflowing.  map2alm runs
+the Legendre sums in C (or_sht.c, OpenMP over m, north and south rings
+paired through lambda_lm(-z) = (-1)^(l+m) lambda_lm(z)); map2alm_py is the
+same transform in numpy, kept as an independent check.  The ring geometry is
+that of he_ang2pix (healpix_extra.c:141-172): the tests check that every
+pixel centre produced here maps back to its own index, and both transforms
+against scipy's spherical harmonics on small maps.
 """
 import numpy as np
 
@@ -76,6 +79,40 @@ def _ring_fourier(maps, nside, lmax):
 def map2alm(maps, nside, lmax=None):
     """a_lm of one map or a stack of maps (RING order), as alm[k][l, m]
     (m <= l, zero above the diagonal), with pixel-area quadrature."""
+    import ctypes as C
+    import oracle as orc
+    maps = np.atleast_2d(np.asarray(maps, np.float64))
+    ns = int(nside)
+    lmax = 3 * ns - 1 if lmax is None else int(lmax)
+    z, phi0, nr, first = ring_geometry(ns)
+    K = maps.shape[0]
+    m = np.arange(lmax + 1)
+    nn = 2 * ns  # northern rings, the equator included
+    S = np.zeros((lmax + 1, nn, K), np.complex128)
+    A = np.zeros((lmax + 1, nn, K), np.complex128)
+    for r in range(len(z)):
+        n, f = nr[r], first[r]
+        c = np.fft.fft(maps[:, f:f + n], axis=1)
+        Fr = (c[:, m % n] * np.exp(-1j * m * phi0[r])[None, :]).T
+        if r < nn:
+            S[:, r, :] += Fr
+            A[:, r, :] += Fr
+        else:
+            q = 4 * ns - 2 - r  # the northern mirror
+            S[:, q, :] += Fr
+            A[:, q, :] -= Fr
+    alm = np.zeros((K, lmax + 1, lmax + 1), np.complex128)
+    zn = np.ascontiguousarray(z[:nn])
+    rc = orc.lib().or_sht_legendre(lmax, nn, K, zn.ctypes.data, S.ctypes.data, A.ctypes.data,
+                                   C.c_double(4.0 * np.pi / (12.0 * ns * ns)), alm.ctypes.data)
+    if rc:
+        raise MemoryError("or_sht_legendre")
+    return alm
+
+
+def map2alm_py(maps, nside, lmax=None):
+    """map2alm in numpy (per m, the recursion over every ring and a matrix
+    product with the ring Fourier sums)."""
     maps = np.atleast_2d(np.asarray(maps, np.float64))
     lmax = 3 * nside - 1 if lmax is None else int(lmax)
     F, z = _ring_fourier(maps, nside, lmax)
