@@ -59,7 +59,13 @@ struct Imap {
   unsigned long long *cnt = nullptr, *chunk_off = nullptr;
   float *data = nullptr;
   int *nadd = nullptr;
-  unsigned long long samples = 0; /* sub-samples drawn by the last run */
+  unsigned long long *ctr = nullptr; /* the kernels' counters (5) */
+  unsigned long long samples = 0;    /* sub-samples drawn by the last run */
+  bool samples_stale = false;        /* a run since samples was read */
+  /* the species' tables were built for table generation gen (0: never) */
+  unsigned long long gen = 0;
+  int nb = 0, contig = 0;
+  double rmin = 0, rmax = 0;
 };
 
 } /* namespace */
@@ -128,7 +134,11 @@ struct cg_ctx {
   size_t tmpmap_n = 0;
   cg_imap_rec *d_recs = nullptr;         /* listed cells of one species */
   unsigned long long *d_imap_queue = nullptr; /* samples for the double pass */
-  unsigned long long *d_imap_ctr = nullptr;
+  /* bumped by cg_upload_tables: stage tables built from the host tables
+   * (convergence, ISW, custom-map, line-of-sight, intensity shells) are
+   * rebuilt when their generation is older */
+  unsigned long long tab_gen = 1, kgen = 0, igen = 0, cgen = 0, losgen = 0;
+  int cir[2 * CG_NPOP_MAX] = {0}; /* custom maps' radial step ranges */
   long long list_cap = 0, queue_cap = 0;
   long long list_cap_max = 0; /* cg_set_imap_list_cap; 0: by free memory */
   /* kappa */
@@ -549,6 +559,7 @@ extern "C" int cg_upload_tables(cg_ctx *c, const cg_config *cfg)
   if (int rc = validate(cfg, c->err, sizeof(c->err))) return rc;
   if (cfg->n_grid != c->N) return fail(c, CG_EINVAL, "n_grid differs from the context's");
   c->cfg = *cfg;
+  c->tab_gen++;
   const int na = CG_NA;
   auto cp = [&](std::vector<double> &v, const double *src) { v.assign(src, src + na); };
   cp(c->h_r, cfg->r_arr_r2z);
@@ -857,14 +868,14 @@ extern "C" void cg_destroy(cg_ctx *c)
                   c->d_disp[1], c->d_disp[2], c->d_part, c->d_stats, c->d_s2f, c->d_err, c->d_ncount,
                   c->d_zsum, c->d_bsum, c->d_bacc, c->d_counts, c->d_bsums, c->d_total, c->d_tmpmap, c->d_kmap,
                   c->d_kfac, c->d_kinv, c->d_kir, c->d_ovf_cell, c->d_ovf_cnt, c->d_ovf_n,
-                  c->d_recs, c->d_imap_queue, c->d_imap_ctr,
+                  c->d_recs, c->d_imap_queue,
                   c->d_imap_isw, c->d_ifac, c->d_iir, c->d_cfac, c->d_losfac};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < CG_NPOP_MAX; i++) {
     void *q[] = {c->cat[i].pos, c->cat[i].ipix, c->cat[i].src, c->cat[i].cmap, c->im[i].b, c->im[i].dxs,
                  c->im[i].shell_of, c->im[i].nsub, c->im[i].base, c->im[i].cap, c->im[i].cnt, c->im[i].chunk_off,
-                 c->im[i].data, c->im[i].nadd, c->d_cmap[i], c->cat[i].skw_d, c->cat[i].skw_v};
+                 c->im[i].data, c->im[i].nadd, c->im[i].ctr, c->d_cmap[i], c->cat[i].skw_d, c->cat[i].skw_v};
     for (void *p : q)
       if (p) cudaFree(p);
   }
@@ -1469,169 +1480,203 @@ extern "C" long long cg_num_sources(cg_ctx *c, int ipop)
   return c->cat[ipop].n;
 }
 
-extern "C" int cg_imap_set_cartesian(cg_ctx *c)
+/* Stage tables are built outside a stream capture only. */
+static int not_capturing(cg_ctx *c, const char *what)
 {
-  if (!c) return CG_EINVAL;
-  if (c->cfg.n_imap == 0) return CG_OK;
-  if (!c->have_norm) return fail(c, CG_ESTATE, "compute_density_normalization first");
-  cudaSetDevice(c->device);
-  out_join(c, 1); /* the maps are rewritten */
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CUDA_TRY(c, cudaStreamIsCapturing(c->stream, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return fail(c, CG_ESTATE, "%s: tables not built before the capture", what);
+  return CG_OK;
+}
+
+/* Tables of intensity species ip (imap_preproc, imap.c:105-133, and the
+ * sub-sampling factors, imap.c:153-174): shells sorted by r0 and their edges
+ * as intervals, the buckets' slots, the cell list and the queue.  Built
+ * once per table generation (or list bound), with host round trips; never
+ * inside a stream capture. */
+static int imap_prepare(cg_ctx *c, int ip)
+{
+  Imap &M = c->im[ip];
+  if (M.gen == c->tab_gen) return CG_OK;
   int rc;
-  for (int ip = 0; ip < c->cfg.n_imap; ip++) {
-    Imap &M = c->im[ip];
-    const int nr = c->cfg.imap_nr[ip];
-    const int nside = c->cfg.nside_imap[ip];
-    const long long npix = 12LL * nside * nside;
-    /* imap_preproc (imap.c:105-133) and the sub-sampling factors
-     * (imap.c:153-174): shells sorted by r0, their edges as intervals */
-    const double dx = c->cfg.l_box / c->N;
-    const int nbk = nr + 2;
-    if (nbk > CG_IMAP_BUCKETS_MAX) return fail(c, CG_EINVAL, "intensity species %d: %d shells", ip, nr);
-    std::vector<float> r0f(nr), rff(nr), bb(2 * nr), dxs(nr + 2);
-    std::vector<int> shell_of(2 * nr + 1), nsub(nr + 2);
-    const int nb = cg_imap_shells(c->cfg.imap_r0[ip], c->cfg.imap_rf[ip], nr, dx, npix, r0f.data(), rff.data(),
-                                  bb.data(), shell_of.data(), nsub.data(), dxs.data());
-    for (int i = 0; i < nr + 2; i++)
-      if (nsub[i] < 1 || nsub[i] > 1024)
-        return fail(c, CG_EINVAL, "intensity species %d: nsub %d outside 1..1024", ip, nsub[i]);
-    if (M.nr != nr) {
-      if ((rc = dalloc(c, &M.b, (size_t)2 * nr)) || (rc = dalloc(c, &M.shell_of, (size_t)2 * nr + 1)) ||
-          (rc = dalloc(c, &M.nsub, (size_t)nr + 2)) || (rc = dalloc(c, &M.dxs, (size_t)nr + 2)) ||
-          (rc = dalloc(c, &M.base, (size_t)nbk)) || (rc = dalloc(c, &M.cap, (size_t)nbk)) ||
-          (rc = dalloc(c, &M.cnt, (size_t)nbk)) || (rc = dalloc(c, &M.chunk_off, (size_t)nbk + 1)))
-        return rc;
-    }
-    if (M.nr != nr || M.npix != npix) {
-      if ((rc = dalloc(c, &M.data, (size_t)nr * npix)) || (rc = dalloc(c, &M.nadd, (size_t)nr * npix))) return rc;
-    }
-    M.nr = nr;
-    M.nside = nside;
-    M.npix = npix;
-    const double rmin = (double)r0f[0] - 20., rmax = (double)rff[nr - 1] + 20.;
-    /* slots per bucket: the corners of the cells of bucket j + 1 lie in the
-     * radii of the intervals of shell j; each corner's dx-cube lies within
-     * sqrt(3)/2 dx of it, so (expanded shell volume) / dx^3 bounds them */
-    std::vector<double> want(nbk, 0.0);
-    const double h = 0.8660254037844386 * dx, ncell = (double)c->N * c->N * c->N;
-    for (int k = -1; k < nb; k++) {
-      double lo = k < 0 ? rmin : (double)bb[k], hi = k + 1 < nb ? (double)bb[k + 1] : rmax;
-      lo = lo < rmin ? rmin : lo;
-      hi = hi > rmax ? rmax : hi;
-      if (hi <= lo) continue;
-      const double a = lo - h > 0 ? lo - h : 0, z = hi + h;
-      want[shell_of[k + 1] + 1] += 4.0 / 3.0 * M_PI * (z * z * z - a * a * a) / (dx * dx * dx);
-    }
-    double tot = 0;
-    for (int i = 0; i < nbk; i++) {
-      want[i] = std::min(want[i], ncell) + 64;
-      tot += want[i];
-    }
-    /* room: every cell, within a quarter of the free memory and the
-     * caller's bound (cells beyond are painted by the listing kernel) */
-    size_t fr = 0, tt = 0;
-    CUDA_TRY(c, cudaMemGetInfo(&fr, &tt));
-    double room = (double)(fr + (size_t)c->list_cap * CG_IMAP_REC_BYTES) * 0.25 / CG_IMAP_REC_BYTES;
-    if (c->list_cap_max > 0 && room > (double)c->list_cap_max) room = (double)c->list_cap_max;
-    const double scale = tot > room ? room / tot : 1.0;
-    std::vector<long long> base(nbk), capv(nbk);
-    long long acc = 0;
-    for (int i = 0; i < nbk; i++) {
-      base[i] = acc;
-      capv[i] = (long long)(want[i] * scale);
-      acc += capv[i];
-    }
-    if (acc > c->list_cap) {
-      if ((rc = dalloc(c, &c->d_recs, (size_t)acc))) return rc;
-      c->list_cap = acc;
-    }
-    if (!c->d_imap_ctr && (rc = dalloc(c, &c->d_imap_ctr, (size_t)5))) return rc;
-    if (!c->d_imap_queue) {
-      const long long qc = 1LL << 27;
-      if ((rc = dalloc(c, &c->d_imap_queue, (size_t)qc))) return rc;
-      c->queue_cap = qc;
-    }
-    CUDA_TRY(c, cudaMemcpyAsync(M.b, bb.data(), nb * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-    CUDA_TRY(c, cudaMemcpyAsync(M.shell_of, shell_of.data(), (nb + 1) * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    CUDA_TRY(c, cudaMemcpyAsync(M.nsub, nsub.data(), (nr + 2) * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    CUDA_TRY(c, cudaMemcpyAsync(M.dxs, dxs.data(), (nr + 2) * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-    CUDA_TRY(c, cudaMemcpyAsync(M.base, base.data(), nbk * sizeof(long long), cudaMemcpyHostToDevice, c->stream));
-    CUDA_TRY(c, cudaMemcpyAsync(M.cap, capv.data(), nbk * sizeof(long long), cudaMemcpyHostToDevice, c->stream));
-    CUDA_TRY(c, cudaMemsetAsync(M.data, 0, (size_t)nr * npix * sizeof(float), c->stream));
-    CUDA_TRY(c, cudaMemsetAsync(M.nadd, 0, (size_t)nr * npix * sizeof(int), c->stream));
-    cg_imap_params p;
-    memset(&p, 0, sizeof(p));
-    p.box = c->box;
-    cg_imap_args &a = p.a;
-    const int na = CG_NA, N = c->N, nt0 = 4 + 2 * c->cfg.n_srcs;
-    a.r = c->g.r;
-    a.tz = c->tz[ip].f;
-    a.bz = c->bzi[ip].f;
-    a.norm = c->normi[ip].f;
-    a.v1 = c->v1.f;
-    a.ih = c->ih.f;
-    a.xc = c->d_corner;
-    a.yc = c->d_corner + N;
-    a.zc = c->d_corner + 2 * N;
-    a.xl = c->d_corner + 3 * N;
-    a.yl = c->d_corner + 4 * N;
-    a.zl = c->d_corner + 5 * N;
-    a.idr = c->g.idr;
-    a.r_last = c->g.r_last;
-    a.rmin = (float)rmin;
-    a.rmax = (float)rmax;
-    const double fv = -c->cfg.fgrowth_0 / (1.5 * c->cfg.hubble_0 * c->cfg.omega_m);
-    a.fvh = (float)(fv * (0.5 * (c->cfg.n_grid / c->cfg.l_box)));
-    a.dx = (float)dx;
-    a.na = na;
-    a.bias_model = c->cfg.bias_model;
-    a.nside = nside;
-    a.sh.b = M.b;
-    a.sh.shell_of = M.shell_of;
-    a.sh.nb = nb;
-    a.sh.nr = nr;
-    a.sh.contig = cg_imap_contig(r0f.data(), rff.data(), nr, nb);
-    a.nsub = M.nsub;
-    a.dxs = M.dxs;
-    a.r64 = c->d_tabs64;
-    a.v164 = c->d_tabs64 + (size_t)2 * na;
-    a.ih64 = c->d_tabs64 + (size_t)3 * na;
-    a.tz64 = c->d_tabs64 + (size_t)(nt0 + 2 * ip) * na;
-    a.bz64 = c->d_tabs64 + (size_t)(nt0 + 2 * ip + 1) * na;
-    a.norm64 = c->d_norm64 + (size_t)(c->cfg.n_srcs + ip) * (na + 2);
-    a.idr64 = c->cfg.glob_idr;
-    a.r_last64 = c->cfg.r_arr_r2z[na - 1];
-    a.dx64 = dx;
-    for (int k = 0; k < 3; k++) a.p64[k] = c->cfg.pos_obs[k];
-    a.idx64 = c->cfg.n_grid / c->cfg.l_box;
-    a.fv64 = fv;
-    a.rmin64 = rmin;
-    a.rmax64 = rmax;
-    p.nr = nr;
-    p.nbk = nbk;
-    p.npix = npix;
-    p.data = M.data;
-    p.nadd = M.nadd;
-    p.err = c->d_err;
-    p.xstats = c->d_xstats;
-    p.force_double = c->force_double;
-    p.recs = c->d_recs;
-    p.base = M.base;
-    p.cap = M.cap;
-    p.cnt = M.cnt;
-    p.chunk_off = M.chunk_off;
-    p.ctr = c->d_imap_ctr;
-    p.queue = c->d_imap_queue;
-    p.queue_cap = c->queue_cap;
-    {
-      ProfScope ps(c, "imap_paint");
-      CUDA_TRY(c, cg_imap_paint(c->stream, c->d_dens, c->d_npot, &p, c->nsm));
-    }
-    unsigned long long ctr[5] = {0, 0, 0, 0, 0};
-    CUDA_TRY(c, cudaMemcpyAsync(ctr, c->d_imap_ctr, sizeof(ctr), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host vectors above go out of scope */
-    M.samples = ctr[2];
-    c->launches += 4; /* list, chunks, paint, double */
+  if ((rc = not_capturing(c, "intensity maps"))) return rc;
+  const int nr = c->cfg.imap_nr[ip];
+  const int nside = c->cfg.nside_imap[ip];
+  const long long npix = 12LL * nside * nside;
+  const double dx = c->cfg.l_box / c->N;
+  const int nbk = nr + 2;
+  if (nbk > CG_IMAP_BUCKETS_MAX) return fail(c, CG_EINVAL, "intensity species %d: %d shells", ip, nr);
+  std::vector<float> r0f(nr), rff(nr), bb(2 * nr), dxs(nr + 2);
+  std::vector<int> shell_of(2 * nr + 1), nsub(nr + 2);
+  const int nb = cg_imap_shells(c->cfg.imap_r0[ip], c->cfg.imap_rf[ip], nr, dx, npix, r0f.data(), rff.data(),
+                                bb.data(), shell_of.data(), nsub.data(), dxs.data());
+  for (int i = 0; i < nr + 2; i++)
+    if (nsub[i] < 1 || nsub[i] > 1024)
+      return fail(c, CG_EINVAL, "intensity species %d: nsub %d outside 1..1024", ip, nsub[i]);
+  if (M.nr != nr) {
+    if ((rc = dalloc(c, &M.b, (size_t)2 * nr)) || (rc = dalloc(c, &M.shell_of, (size_t)2 * nr + 1)) ||
+        (rc = dalloc(c, &M.nsub, (size_t)nr + 2)) || (rc = dalloc(c, &M.dxs, (size_t)nr + 2)) ||
+        (rc = dalloc(c, &M.base, (size_t)nbk)) || (rc = dalloc(c, &M.cap, (size_t)nbk)) ||
+        (rc = dalloc(c, &M.cnt, (size_t)nbk)) || (rc = dalloc(c, &M.chunk_off, (size_t)nbk + 1)))
+      return rc;
   }
+  if (M.nr != nr || M.npix != npix) {
+    if ((rc = dalloc(c, &M.data, (size_t)nr * npix)) || (rc = dalloc(c, &M.nadd, (size_t)nr * npix))) return rc;
+  }
+  M.nr = nr;
+  M.nside = nside;
+  M.npix = npix;
+  const double rmin = (double)r0f[0] - 20., rmax = (double)rff[nr - 1] + 20.;
+  /* slots per bucket: the corners of the cells of bucket j + 1 lie in the
+   * radii of the intervals of shell j; each corner's dx-cube lies within
+   * sqrt(3)/2 dx of it, so (expanded shell volume) / dx^3 bounds them */
+  std::vector<double> want(nbk, 0.0);
+  const double h = 0.8660254037844386 * dx, ncell = (double)c->N * c->N * c->N;
+  for (int k = -1; k < nb; k++) {
+    double lo = k < 0 ? rmin : (double)bb[k], hi = k + 1 < nb ? (double)bb[k + 1] : rmax;
+    lo = lo < rmin ? rmin : lo;
+    hi = hi > rmax ? rmax : hi;
+    if (hi <= lo) continue;
+    const double a = lo - h > 0 ? lo - h : 0, z = hi + h;
+    want[shell_of[k + 1] + 1] += 4.0 / 3.0 * M_PI * (z * z * z - a * a * a) / (dx * dx * dx);
+  }
+  double tot = 0;
+  for (int i = 0; i < nbk; i++) {
+    want[i] = std::min(want[i], ncell) + 64;
+    tot += want[i];
+  }
+  /* room: every cell, within a quarter of the free memory and the
+   * caller's bound (cells beyond are painted by the listing kernel) */
+  size_t fr = 0, tt = 0;
+  CUDA_TRY(c, cudaMemGetInfo(&fr, &tt));
+  double room = (double)(fr + (size_t)c->list_cap * CG_IMAP_REC_BYTES) * 0.25 / CG_IMAP_REC_BYTES;
+  if (c->list_cap_max > 0 && room > (double)c->list_cap_max) room = (double)c->list_cap_max;
+  const double scale = tot > room ? room / tot : 1.0;
+  std::vector<long long> base(nbk), capv(nbk);
+  long long acc = 0;
+  for (int i = 0; i < nbk; i++) {
+    base[i] = acc;
+    capv[i] = (long long)(want[i] * scale);
+    acc += capv[i];
+  }
+  if (acc > c->list_cap) {
+    if ((rc = dalloc(c, &c->d_recs, (size_t)acc))) return rc;
+    c->list_cap = acc;
+  }
+  if (!M.ctr && (rc = dalloc(c, &M.ctr, (size_t)5))) return rc;
+  if (!c->d_imap_queue) {
+    const long long qc = 1LL << 27;
+    if ((rc = dalloc(c, &c->d_imap_queue, (size_t)qc))) return rc;
+    c->queue_cap = qc;
+  }
+  CUDA_TRY(c, cudaMemcpyAsync(M.b, bb.data(), nb * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(M.shell_of, shell_of.data(), (nb + 1) * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(M.nsub, nsub.data(), (nr + 2) * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(M.dxs, dxs.data(), (nr + 2) * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(M.base, base.data(), nbk * sizeof(long long), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(M.cap, capv.data(), nbk * sizeof(long long), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host staging vectors */
+  M.nb = nb;
+  M.contig = cg_imap_contig(r0f.data(), rff.data(), nr, nb);
+  M.rmin = rmin;
+  M.rmax = rmax;
+  M.gen = c->tab_gen;
+  return CG_OK;
+}
+
+/* The painting of species ip on the context's stream: no host round trip,
+ * so that it can be captured in a graph; the samples drawn are read on
+ * demand (cg_imap_samples). */
+static int imap_launch(cg_ctx *c, int ip)
+{
+  Imap &M = c->im[ip];
+  const int nr = M.nr, nside = M.nside, nbk = nr + 2;
+  const long long npix = M.npix;
+  const double dx = c->cfg.l_box / c->N;
+  CUDA_TRY(c, cudaMemsetAsync(M.data, 0, (size_t)nr * npix * sizeof(float), c->stream));
+  CUDA_TRY(c, cudaMemsetAsync(M.nadd, 0, (size_t)nr * npix * sizeof(int), c->stream));
+  cg_imap_params p;
+  memset(&p, 0, sizeof(p));
+  p.box = c->box;
+  cg_imap_args &a = p.a;
+  const int na = CG_NA, N = c->N, nt0 = 4 + 2 * c->cfg.n_srcs;
+  a.r = c->g.r;
+  a.tz = c->tz[ip].f;
+  a.bz = c->bzi[ip].f;
+  a.norm = c->normi[ip].f;
+  a.v1 = c->v1.f;
+  a.ih = c->ih.f;
+  a.xc = c->d_corner;
+  a.yc = c->d_corner + N;
+  a.zc = c->d_corner + 2 * N;
+  a.xl = c->d_corner + 3 * N;
+  a.yl = c->d_corner + 4 * N;
+  a.zl = c->d_corner + 5 * N;
+  a.idr = c->g.idr;
+  a.r_last = c->g.r_last;
+  a.rmin = (float)M.rmin;
+  a.rmax = (float)M.rmax;
+  const double fv = -c->cfg.fgrowth_0 / (1.5 * c->cfg.hubble_0 * c->cfg.omega_m);
+  a.fvh = (float)(fv * (0.5 * (c->cfg.n_grid / c->cfg.l_box)));
+  a.dx = (float)dx;
+  a.na = na;
+  a.bias_model = c->cfg.bias_model;
+  a.nside = nside;
+  a.sh.b = M.b;
+  a.sh.shell_of = M.shell_of;
+  a.sh.nb = M.nb;
+  a.sh.nr = nr;
+  a.sh.contig = M.contig;
+  a.nsub = M.nsub;
+  a.dxs = M.dxs;
+  a.r64 = c->d_tabs64;
+  a.v164 = c->d_tabs64 + (size_t)2 * na;
+  a.ih64 = c->d_tabs64 + (size_t)3 * na;
+  a.tz64 = c->d_tabs64 + (size_t)(nt0 + 2 * ip) * na;
+  a.bz64 = c->d_tabs64 + (size_t)(nt0 + 2 * ip + 1) * na;
+  a.norm64 = c->d_norm64 + (size_t)(c->cfg.n_srcs + ip) * (na + 2);
+  a.idr64 = c->cfg.glob_idr;
+  a.r_last64 = c->cfg.r_arr_r2z[na - 1];
+  a.dx64 = dx;
+  for (int k = 0; k < 3; k++) a.p64[k] = c->cfg.pos_obs[k];
+  a.idx64 = c->cfg.n_grid / c->cfg.l_box;
+  a.fv64 = fv;
+  a.rmin64 = M.rmin;
+  a.rmax64 = M.rmax;
+  p.nr = nr;
+  p.nbk = nbk;
+  p.npix = npix;
+  p.data = M.data;
+  p.nadd = M.nadd;
+  p.err = c->d_err;
+  p.xstats = c->d_xstats;
+  p.force_double = c->force_double;
+  p.recs = c->d_recs;
+  p.base = M.base;
+  p.cap = M.cap;
+  p.cnt = M.cnt;
+  p.chunk_off = M.chunk_off;
+  p.ctr = M.ctr;
+  p.queue = c->d_imap_queue;
+  p.queue_cap = c->queue_cap;
+  {
+    ProfScope ps(c, "imap_paint");
+    CUDA_TRY(c, cg_imap_paint(c->stream, c->d_dens, c->d_npot, &p, c->nsm));
+  }
+  M.samples_stale = true;
+  c->launches += 4; /* list, chunks, paint, double */
+  return CG_OK;
+}
+
+/* Every species; with host_out, the final maps go to registered host
+ * buffers (not in a captured sequence). */
+static int imap_run(cg_ctx *c, bool host_out)
+{
+  for (int ip = 0; ip < c->cfg.n_imap; ip++) {
+    if (int rc = imap_prepare(c, ip)) return rc;
+    if (int rc = imap_launch(c, ip)) return rc;
+  }
+  if (!host_out) return CG_OK;
   /* final maps to registered host buffers (write_imap, io.c:738-741:
    * data/nadd where nadd > 0), overlapping the stages still to run */
   for (int ip = 0; ip < c->cfg.n_imap; ip++) {
@@ -1654,17 +1699,38 @@ extern "C" int cg_imap_set_cartesian(cg_ctx *c)
   return CG_OK;
 }
 
+extern "C" int cg_imap_set_cartesian(cg_ctx *c)
+{
+  if (!c) return CG_EINVAL;
+  if (c->cfg.n_imap == 0) return CG_OK;
+  if (!c->have_norm) return fail(c, CG_ESTATE, "compute_density_normalization first");
+  cudaSetDevice(c->device);
+  out_join(c, 1); /* the maps are rewritten */
+  return imap_run(c, true);
+}
+
+
 extern "C" int cg_set_imap_list_cap(cg_ctx *c, long long cap)
 {
   if (!c || cap < 0) return CG_EINVAL;
   c->list_cap_max = cap;
+  for (int ip = 0; ip < CG_NPOP_MAX; ip++) c->im[ip].gen = 0; /* bucket room is recomputed */
   return CG_OK;
 }
 
 extern "C" int cg_imap_samples(cg_ctx *c, int ipop, unsigned long long *n)
 {
   if (!c || !n || ipop < 0 || ipop >= c->cfg.n_imap) return CG_EINVAL;
-  *n = c->im[ipop].samples;
+  Imap &M = c->im[ipop];
+  if (M.samples_stale && M.ctr) {
+    if (c->graph_done) CUDA_TRY(c, cudaEventSynchronize(c->graph_done));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    unsigned long long ctr[5];
+    CUDA_TRY(c, cudaMemcpy(ctr, M.ctr, sizeof(ctr), cudaMemcpyDeviceToHost));
+    M.samples = ctr[2];
+    M.samples_stale = false;
+  }
+  *n = M.samples;
   return CG_OK;
 }
 
@@ -1675,40 +1741,45 @@ static int kappa_run(cg_ctx *c)
   const long long npix = 12LL * nside * nside;
   const int nr = c->N / 2; /* get_radial_params with NSAMP_RAD = 1 */
   const double dr = c->cfg.r_max / nr, idr = 1. / dr;
-  /* kappa_beams_preproc: sort planes by distance (stored as flouble) */
-  std::vector<float> rp(np);
-  for (int i = 0; i < np; i++) rp[i] = (float)c->cfg.kappa_r[i];
-  std::stable_sort(rp.begin(), rp.end());
-  std::vector<int> ir(2 * np);
-  std::vector<float> inv(np), fac(2 * (size_t)nr);
-  for (int i = 0; i < np; i++) {
-    int irh = (int)((double)rp[i] * idr + 0.5);
-    inv[i] = (float)(1. / (irh * dr));
-    ir[np + i] = std::min(irh, nr - 1);
-  }
-  ir[0] = 0;
-  for (int i = 1; i < np; i++) ir[i] = ir[np + i - 1] + 1;
-  for (int i = 0; i < nr; i++) {
-    double rm = (i + 0.5) * dr;
-    double pg = host_bg(c, c->h_d1, 1, c->h_d1[CG_NA - 1], rm) * (1 + host_bg(c, c->h_z, 0, c->h_z[CG_NA - 1], rm));
-    fac[i] = (float)(rm * pg * dr);
-    fac[nr + i] = (float)(rm * rm * pg * dr);
-  }
   int rc;
-  if (c->kpl != np || c->knpix != npix) {
-    if ((rc = dalloc(c, &c->d_kmap, (size_t)np * npix))) return rc;
+  if (c->kgen != c->tab_gen || c->kpl != np || c->knpix != npix || c->knr != nr) {
+    if ((rc = not_capturing(c, "convergence"))) return rc;
+    /* kappa_beams_preproc: sort planes by distance (stored as flouble) */
+    std::vector<float> rp(np);
+    for (int i = 0; i < np; i++) rp[i] = (float)c->cfg.kappa_r[i];
+    std::stable_sort(rp.begin(), rp.end());
+    std::vector<int> ir(2 * np);
+    std::vector<float> inv(np), fac(2 * (size_t)nr);
+    for (int i = 0; i < np; i++) {
+      int irh = (int)((double)rp[i] * idr + 0.5);
+      inv[i] = (float)(1. / (irh * dr));
+      ir[np + i] = std::min(irh, nr - 1);
+    }
+    ir[0] = 0;
+    for (int i = 1; i < np; i++) ir[i] = ir[np + i - 1] + 1;
+    for (int i = 0; i < nr; i++) {
+      double rm = (i + 0.5) * dr;
+      double pg = host_bg(c, c->h_d1, 1, c->h_d1[CG_NA - 1], rm) * (1 + host_bg(c, c->h_z, 0, c->h_z[CG_NA - 1], rm));
+      fac[i] = (float)(rm * pg * dr);
+      fac[nr + i] = (float)(rm * rm * pg * dr);
+    }
+    if (c->kpl != np || c->knpix != npix) {
+      if ((rc = dalloc(c, &c->d_kmap, (size_t)np * npix))) return rc;
+    }
+    if (c->knr != nr || c->kpl != np) {
+      if ((rc = dalloc(c, &c->d_kfac, 2 * (size_t)nr)) || (rc = dalloc(c, &c->d_kinv, (size_t)np)) ||
+          (rc = dalloc(c, &c->d_kir, 2 * (size_t)np)))
+        return rc;
+    }
+    c->kpl = np;
+    c->knpix = npix;
+    c->knr = nr;
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_kfac, fac.data(), fac.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_kinv, inv.data(), inv.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_kir, ir.data(), ir.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host staging vectors */
+    c->kgen = c->tab_gen;
   }
-  if (c->knr != nr || c->kpl != np) {
-    if ((rc = dalloc(c, &c->d_kfac, 2 * (size_t)nr)) || (rc = dalloc(c, &c->d_kinv, (size_t)np)) ||
-        (rc = dalloc(c, &c->d_kir, 2 * (size_t)np)))
-      return rc;
-  }
-  c->kpl = np;
-  c->knpix = npix;
-  c->knr = nr;
-  CUDA_TRY(c, cudaMemcpyAsync(c->d_kfac, fac.data(), fac.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-  CUDA_TRY(c, cudaMemcpyAsync(c->d_kinv, inv.data(), inv.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-  CUDA_TRY(c, cudaMemcpyAsync(c->d_kir, ir.data(), ir.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
   cg_kappa_params p;
   p.box = c->box;
   p.nside = nside;
@@ -1727,7 +1798,6 @@ static int kappa_run(cg_ctx *c)
     CUDA_TRY(c, cg_kappa_integrate(c->stream, c->d_npot, &p));
   }
   c->launches++;
-  CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host staging vectors */
   return CG_OK;
 }
 
@@ -1739,28 +1809,33 @@ static int isw_run(cg_ctx *c)
   const long long npix = 12LL * nside * nside;
   const int nr = c->N / 2; /* get_radial_params with NSAMP_RAD = 1 */
   const double dr = c->cfg.r_max / nr, idr = 1. / dr;
-  std::vector<float> rp(np); /* plane distances, stored as flouble and sorted */
-  for (int i = 0; i < np; i++) rp[i] = (float)c->cfg.isw_r[i];
-  std::stable_sort(rp.begin(), rp.end());
-  std::vector<int> ir(2 * np);
-  for (int i = 0; i < np; i++) ir[np + i] = std::min((int)((double)rp[i] * idr + 0.5), nr - 1);
-  ir[0] = 0;
-  for (int i = 1; i < np; i++) ir[i] = ir[np + i - 1] + 1;
-  std::vector<float> fac(nr);
-  for (int i = 0; i < nr; i++) {
-    const double rm = (i + 0.5) * dr;
-    fac[i] = (float)(2 * host_bg(c, c->h_pd, c->h_pd[0], c->h_pd[CG_NA - 1], rm) * dr);
-  }
   int rc;
-  if (c->ipl != np || c->inpix != npix)
-    if ((rc = dalloc(c, &c->d_imap_isw, (size_t)np * npix))) return rc;
-  if (c->inr != nr || c->ipl != np)
-    if ((rc = dalloc(c, &c->d_ifac, (size_t)nr)) || (rc = dalloc(c, &c->d_iir, 2 * (size_t)np))) return rc;
-  c->ipl = np;
-  c->inpix = npix;
-  c->inr = nr;
-  CUDA_TRY(c, cudaMemcpyAsync(c->d_ifac, fac.data(), fac.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-  CUDA_TRY(c, cudaMemcpyAsync(c->d_iir, ir.data(), ir.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  if (c->igen != c->tab_gen || c->ipl != np || c->inpix != npix || c->inr != nr) {
+    if ((rc = not_capturing(c, "ISW"))) return rc;
+    std::vector<float> rp(np); /* plane distances, stored as flouble and sorted */
+    for (int i = 0; i < np; i++) rp[i] = (float)c->cfg.isw_r[i];
+    std::stable_sort(rp.begin(), rp.end());
+    std::vector<int> ir(2 * np);
+    for (int i = 0; i < np; i++) ir[np + i] = std::min((int)((double)rp[i] * idr + 0.5), nr - 1);
+    ir[0] = 0;
+    for (int i = 1; i < np; i++) ir[i] = ir[np + i - 1] + 1;
+    std::vector<float> fac(nr);
+    for (int i = 0; i < nr; i++) {
+      const double rm = (i + 0.5) * dr;
+      fac[i] = (float)(2 * host_bg(c, c->h_pd, c->h_pd[0], c->h_pd[CG_NA - 1], rm) * dr);
+    }
+    if (c->ipl != np || c->inpix != npix)
+      if ((rc = dalloc(c, &c->d_imap_isw, (size_t)np * npix))) return rc;
+    if (c->inr != nr || c->ipl != np)
+      if ((rc = dalloc(c, &c->d_ifac, (size_t)nr)) || (rc = dalloc(c, &c->d_iir, 2 * (size_t)np))) return rc;
+    c->ipl = np;
+    c->inpix = npix;
+    c->inr = nr;
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_ifac, fac.data(), fac.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_iir, ir.data(), ir.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host staging vectors */
+    c->igen = c->tab_gen;
+  }
   cg_kappa_params p;
   memset(&p, 0, sizeof(p));
   p.box = c->box;
@@ -1778,7 +1853,6 @@ static int isw_run(cg_ctx *c)
     CUDA_TRY(c, cg_isw_integrate(c->stream, c->d_npot, &p));
   }
   c->launches++;
-  CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host staging vectors */
   return CG_OK;
 }
 
@@ -1793,43 +1867,49 @@ static int cstm_run(cg_ctx *c)
   const int nr = c->N / 2, nc = c->cfg.n_cstm; /* get_radial_params with NSAMP_RAD = 1 */
   const double dr = c->cfg.r_max / nr;
   int rc;
-  if (c->cnr != nr)
-    if ((rc = dalloc(c, &c->d_cfac, 2 * (size_t)nr * CG_NPOP_MAX))) return rc;
-  c->cnr = nr;
-  std::vector<float> tab(2 * (size_t)nr * nc);
-  std::vector<int> irange(2 * nc);
-  for (int p = 0; p < nc; p++) {
-    float *kz = tab.data() + 2 * (size_t)nr * p, *bz = kz + nr;
-    double kmax = -1e100;
-    std::vector<double> kzd(nr);
-    for (int i = 0; i < nr; i++) {
-      const double rm = (i + 0.5) * dr;
-      kzd[i] = host_bg(c, c->h_kzc[p], 0, 0, rm) / host_bg(c, c->h_ih, c->h_ih[0], c->h_ih[CG_NA - 1], rm);
-      kz[i] = (float)kzd[i];
-      bz[i] = (float)host_bg(c, c->h_bzc[p], c->h_bzc[p][0], 1, rm);
-      kmax = std::max(kmax, fabs(kzd[i]));
-    }
-    int lo = 0, hi = nr - 1;
-    for (int i = 0; i < nr; i++)
-      if (fabs(kzd[i]) > 1e-4 * kmax) {
-        lo = i;
-        break;
+  if (c->cgen != c->tab_gen || c->cnr != nr) {
+    if ((rc = not_capturing(c, "custom maps"))) return rc;
+    if (c->cnr != nr)
+      if ((rc = dalloc(c, &c->d_cfac, 2 * (size_t)nr * CG_NPOP_MAX))) return rc;
+    c->cnr = nr;
+    std::vector<float> tab(2 * (size_t)nr * nc);
+    int *irange = c->cir;
+    for (int p = 0; p < nc; p++) {
+      float *kz = tab.data() + 2 * (size_t)nr * p, *bz = kz + nr;
+      double kmax = -1e100;
+      std::vector<double> kzd(nr);
+      for (int i = 0; i < nr; i++) {
+        const double rm = (i + 0.5) * dr;
+        kzd[i] = host_bg(c, c->h_kzc[p], 0, 0, rm) / host_bg(c, c->h_ih, c->h_ih[0], c->h_ih[CG_NA - 1], rm);
+        kz[i] = (float)kzd[i];
+        bz[i] = (float)host_bg(c, c->h_bzc[p], c->h_bzc[p][0], 1, rm);
+        kmax = std::max(kmax, fabs(kzd[i]));
       }
-    for (int i = nr - 1; i >= 0; i--)
-      if (fabs(kzd[i]) > 1e-4 * kmax) {
-        hi = i;
-        break;
+      int lo = 0, hi = nr - 1;
+      for (int i = 0; i < nr; i++)
+        if (fabs(kzd[i]) > 1e-4 * kmax) {
+          lo = i;
+          break;
+        }
+      for (int i = nr - 1; i >= 0; i--)
+        if (fabs(kzd[i]) > 1e-4 * kmax) {
+          hi = i;
+          break;
+        }
+      if (hi < lo) return fail(c, CG_EINVAL, "Custom kernel %d has no support", p);
+      irange[2 * p] = lo;
+      irange[2 * p + 1] = hi;
+      const long long npix = 12LL * c->cfg.nside_cstm[p] * c->cfg.nside_cstm[p];
+      if (c->cnpix[p] != npix) {
+        if ((rc = dalloc(c, &c->d_cmap[p], (size_t)npix))) return rc;
+        c->cnpix[p] = npix;
       }
-    if (hi < lo) return fail(c, CG_EINVAL, "Custom kernel %d has no support", p);
-    irange[2 * p] = lo;
-    irange[2 * p + 1] = hi;
-    const long long npix = 12LL * c->cfg.nside_cstm[p] * c->cfg.nside_cstm[p];
-    if (c->cnpix[p] != npix) {
-      if ((rc = dalloc(c, &c->d_cmap[p], (size_t)npix))) return rc;
-      c->cnpix[p] = npix;
     }
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_cfac, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host staging vector */
+    c->cgen = c->tab_gen;
   }
-  CUDA_TRY(c, cudaMemcpyAsync(c->d_cfac, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  const int *irange = c->cir;
   for (int p = 0; p < nc; p++) {
     cg_cstm_params q;
     memset(&q, 0, sizeof(q));
@@ -1849,7 +1929,6 @@ static int cstm_run(cg_ctx *c)
     CUDA_TRY(c, cg_cstm_integrate(c->stream, c->d_dens, &q));
     c->launches++;
   }
-  CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host staging vector */
   return CG_OK;
 }
 
@@ -1861,8 +1940,10 @@ static int los_tables(cg_ctx *c)
 {
   const int nr = c->N / 2;
   const double dr = c->cfg.r_max / nr;
-  if (c->losnr == nr) return CG_OK;
-  if (int rc = dalloc(c, &c->d_losfac, 3 * (size_t)nr)) return rc;
+  if (c->losnr == nr && c->losgen == c->tab_gen) return CG_OK;
+  if (int rc = not_capturing(c, "line-of-sight quantities")) return rc;
+  if (c->losnr != nr)
+    if (int rc = dalloc(c, &c->d_losfac, 3 * (size_t)nr)) return rc;
   const double fv = -c->cfg.fgrowth_0 / (1.5 * c->cfg.hubble_0 * c->cfg.omega_m);
   std::vector<float> t(3 * (size_t)nr);
   for (int i = 0; i < nr; i++) {
@@ -1875,10 +1956,13 @@ static int los_tables(cg_ctx *c)
   CUDA_TRY(c, cudaMemcpyAsync(c->d_losfac, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host staging vector */
   c->losnr = nr;
+  c->losgen = c->tab_gen;
   return CG_OK;
 }
 
-static int srcs_los_run(cg_ctx *c, int ip)
+/* async: inside a captured sequence, the source total read on the device
+ * (the catalogue's capacity bounds the launch). */
+static int srcs_los_run(cg_ctx *c, int ip, bool async)
 {
   Cat &K = c->cat[ip];
   const bool lens = c->cfg.lensing_srcs[ip] != 0, skw = c->cfg.skw_srcs[ip] != 0;
@@ -1893,7 +1977,8 @@ static int srcs_los_run(cg_ctx *c, int ip)
   q.d1 = c->d1;
   q.pos = K.pos;
   q.src = K.src;
-  q.nsrc = K.n;
+  q.nsrc = async ? K.cap : K.n;
+  q.nsrc_dev = async ? c->d_total + ip : nullptr;
   q.nr = nr;
   q.dr = (float)(c->cfg.r_max / nr);
   q.idr = (float)(nr / c->cfg.r_max);
@@ -1901,14 +1986,16 @@ static int srcs_los_run(cg_ctx *c, int ip)
   q.vfac = c->d_losfac + 2 * (size_t)nr;
   q.skw_gauss = c->cfg.skw_gauss[ip];
   q.sigma2 = c->d_s2f;
-  if (lens && K.n > 0) {
+  if (lens && q.nsrc > 0) {
     ProfScope ps(c, "srcs_lensing");
     CUDA_TRY(c, cg_srcs_lensing(c->stream, c->d_npot, &q, c->nsm));
     c->launches++;
   }
   if (skw) {
-    if (K.n > K.skw_cap) {
-      const long long cap = K.n + K.n / 8 + 64;
+    /* room for the catalogue's capacity, so that a captured sequence fits */
+    if (async && K.skw_cap < K.cap) return fail(c, CG_ESTATE, "skewers of population %d not sized before the capture", ip);
+    if (K.n > K.skw_cap || K.cap > K.skw_cap) {
+      const long long cap = std::max(K.n + K.n / 8 + 64, K.cap);
       if ((rc = dalloc(c, &K.skw_d, (size_t)cap * nr)) || (rc = dalloc(c, &K.skw_v, (size_t)cap * nr))) {
         K.skw_cap = 0;
         return rc;
@@ -1917,12 +2004,12 @@ static int srcs_los_run(cg_ctx *c, int ip)
     }
     q.skw_d = K.skw_d;
     q.skw_v = K.skw_v;
-    if (K.n > 0) {
+    if (q.nsrc > 0) {
       ProfScope ps(c, "srcs_skewers");
       CUDA_TRY(c, cg_srcs_skewers(c->stream, c->d_dens, c->d_npot, &q, c->nsm));
       c->launches++;
     }
-    K.skw_n = K.n;
+    K.skw_n = async ? -2 : K.n; /* -2: for the device total */
   }
   return CG_OK;
 }
@@ -1945,15 +2032,22 @@ static int out_catalogs(cg_ctx *c)
   return CG_OK;
 }
 
-extern "C" int cg_get_beam_properties(cg_ctx *c)
+/* The beam stage (beaming.c:293-374).  async: inside a captured sequence --
+ * source totals stay on the device, no host outputs. */
+static int beam_run(cg_ctx *c, bool async)
 {
-  if (!c) return CG_EINVAL;
-  if (int rc = refresh_counts(c)) return rc;
-  if (!c->cfg.need_beaming) return out_catalogs(c); /* beaming.c:296-299 */
+  if (!async) {
+    if (int rc = refresh_counts(c)) return rc;
+    if (!c->cfg.need_beaming) return out_catalogs(c); /* beaming.c:296-299 */
+  } else if (!c->cfg.need_beaming) {
+    return CG_OK;
+  }
   if (!c->have_fields) return fail(c, CG_ESTATE, "fields not created");
   cudaSetDevice(c->device);
-  out_join(c, 0); /* RSD and lensing columns are rewritten */
-  out_join(c, 2);
+  if (!async) {
+    out_join(c, 0); /* RSD and lensing columns are rewritten */
+    out_join(c, 2);
+  }
   /* The source quantities first (the reference computes them last,
    * beaming.c:293-374; the passes are independent): the catalogues can then
    * go to the host while the maps are computed. */
@@ -1962,16 +2056,18 @@ extern "C" int cg_get_beam_properties(cg_ctx *c)
     for (int ip = 0; ip < c->cfg.n_srcs; ip++) {
       cg_srcs_params p;
       srcs_params(c, ip, p);
+      const long long n = async ? c->cat[ip].cap : c->cat[ip].n;
       ProfScope ps(c, "srcs_beam_rsd");
-      CUDA_TRY(c, cg_srcs_beam_rsd(c->stream, c->d_npot, &p, c->cat[ip].n, c->nsm));
-      if (c->cat[ip].n > 0) c->launches++;
-      if (int rc = srcs_los_run(c, ip)) return rc;
+      CUDA_TRY(c, cg_srcs_beam_rsd(c->stream, c->d_npot, &p, n, async ? c->d_total + ip : nullptr, c->nsm));
+      if (n > 0) c->launches++;
+      if (int rc = srcs_los_run(c, ip, async)) return rc;
     }
-    if (int rc = out_catalogs(c)) return rc;
+    if (!async)
+      if (int rc = out_catalogs(c)) return rc;
   }
   if (c->cfg.do_kappa) {
     if (int rc = kappa_run(c)) return rc;
-    if (c->h_kappa) {
+    if (!async && c->h_kappa) {
       if (int rc = out_begin(c)) return rc;
       CUDA_TRY(c, cudaMemcpyAsync(c->h_kappa, c->d_kmap, (size_t)c->kpl * c->knpix * sizeof(float),
                                   cudaMemcpyDeviceToHost, c->ostream));
@@ -1983,6 +2079,12 @@ extern "C" int cg_get_beam_properties(cg_ctx *c)
   if (c->cfg.n_cstm > 0)
     if (int rc = cstm_run(c)) return rc;
   return CG_OK;
+}
+
+extern "C" int cg_get_beam_properties(cg_ctx *c)
+{
+  if (!c) return CG_EINVAL;
+  return beam_run(c, false);
 }
 
 extern "C" int cg_set_host_catalog(cg_ctx *c, int ipop, float *src9, long long cap, long long *n_out)
@@ -2042,23 +2144,25 @@ extern "C" int cg_run_mock(cg_ctx *c)
 /* ------------------------------------------------------------------------ */
 /* graph-captured sequence and batches of realisations                      */
 /* ------------------------------------------------------------------------ */
-/* The stages without host round trips: fields, density, normalisation
- * tables and sources, totals left on the device. */
+/* The whole sequence without host round trips: fields, density,
+ * normalisation tables, sources (totals left on the device), intensity maps
+ * and the beam stage (per-source quantities bounded by the catalogue's
+ * capacity and reading the totals on the device; convergence, ISW and custom
+ * maps).  Stage tables are built by the plain run that precedes a capture. */
 static int run_mock_async(cg_ctx *c)
 {
   int rc;
   if ((rc = cg_create_cartesian_fields(c))) return rc;
   if ((rc = cg_compute_physical_density_field(c))) return rc;
   if ((rc = cg_compute_density_normalization(c))) return rc;
-  return srcs_run(c, nullptr, false);
+  if ((rc = srcs_run(c, nullptr, false))) return rc;
+  if (c->cfg.n_imap > 0 && (rc = imap_run(c, false))) return rc;
+  return beam_run(c, true);
 }
 
 extern "C" int cg_graph_capture(cg_ctx *c)
 {
   if (!c) return CG_EINVAL;
-  if (c->cfg.n_imap > 0 || c->cfg.need_beaming)
-    return fail(c, CG_EINVAL, "graph capture covers fields, density, normalisation and sources; "
-                              "intensity maps and line-of-sight quantities keep their host steps");
   if (c->profiling) return fail(c, CG_EINVAL, "switch profiling off before capturing");
   cudaSetDevice(c->device);
   graph_free(c);
@@ -2355,7 +2459,7 @@ extern "C" int cg_download_skewers(cg_ctx *c, int ipop, float *dens, float *vel)
   if (int rc = refresh_counts(c)) return rc;
   const Cat &K = c->cat[ipop];
   if (!c->cfg.skw_srcs[ipop]) return fail(c, CG_ESTATE, "population %d stores no skewers", ipop);
-  if (K.skw_n != K.n) return fail(c, CG_ESTATE, "skewers of population %d not computed", ipop);
+  if (K.skw_n != K.n && K.skw_n != -2) return fail(c, CG_ESTATE, "skewers of population %d not computed", ipop);
   const size_t m = (size_t)K.n * c->losnr;
   if (m) {
     if (dens) CUDA_TRY(c, cudaMemcpyAsync(dens, K.skw_d, m * sizeof(float), cudaMemcpyDeviceToHost, c->stream));

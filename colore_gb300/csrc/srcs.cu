@@ -355,9 +355,20 @@ __device__ __forceinline__ float los_vel(const float v[3], const float u[3], flo
  * (interpolate_from_grid CIC branch, beaming.c:183-265) projected on the
  * line of sight (srcs.c:500-504), then scaled by V1(r(z0)) * factor_vel
  * (srcs.c:657-662). */
-__global__ void __launch_bounds__(256) k_beam_rsd(const float *__restrict__ phi, cg_srcs_params p, long long nsrc)
+__device__ __forceinline__ long long src_count(long long n, const long long *n_dev)
+{
+  if (n_dev) {
+    const long long d = *n_dev;
+    if (d < n) n = d;
+  }
+  return n;
+}
+
+__global__ void __launch_bounds__(256) k_beam_rsd(const float *__restrict__ phi, cg_srcs_params p, long long nsrc,
+                                                  const long long *nsrc_dev)
 {
   const int N = p.box.N;
+  nsrc = src_count(nsrc, nsrc_dev);
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nsrc;
        i += (long long)gridDim.x * blockDim.x) {
     float4 q = p.pos[i];
@@ -416,7 +427,8 @@ __global__ void __launch_bounds__(256) k_src_lensing(const float *__restrict__ p
   const int N = p.box.N;
   const float po[3] = {p.box.p0, p.box.p1, p.box.p2};
   const float idx = p.box.idx;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.nsrc;
+  const long long nsrc = src_count(p.nsrc, p.nsrc_dev);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nsrc;
        i += (long long)gridDim.x * blockDim.x) {
     float r, u[3];
     const int kmax = los_setup(p.pos[i], p, &r, u);
@@ -463,7 +475,8 @@ __global__ void __launch_bounds__(256) k_src_skewers(const float *__restrict__ d
   const float po[3] = {p.box.p0, p.box.p1, p.box.p2};
   const float idx = p.box.idx;
   const float s2 = p.skw_gauss ? *p.sigma2 : 0.0f;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.nsrc;
+  const long long nsrc = src_count(p.nsrc, p.nsrc_dev);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nsrc;
        i += (long long)gridDim.x * blockDim.x) {
     float r, u[3];
     const int kmax = los_setup(p.pos[i], p, &r, u);
@@ -540,11 +553,12 @@ cudaError_t cg_srcs_skewers(cudaStream_t s, const float *dens, const float *phi,
   return cudaGetLastError();
 }
 
-cudaError_t cg_srcs_beam_rsd(cudaStream_t s, const float *phi, const cg_srcs_params *p, long long nsrc, int nsm)
+cudaError_t cg_srcs_beam_rsd(cudaStream_t s, const float *phi, const cg_srcs_params *p, long long nsrc,
+                             const long long *nsrc_dev, int nsm)
 {
   if (nsrc <= 0) return cudaSuccess;
   long long blocks = (nsrc + 255) / 256;
   if (blocks > (long long)nsm * 16) blocks = (long long)nsm * 16;
-  k_beam_rsd<<<(unsigned)blocks, 256, 0, s>>>(phi, *p, nsrc);
+  k_beam_rsd<<<(unsigned)blocks, 256, 0, s>>>(phi, *p, nsrc, nsrc_dev);
   return cudaGetLastError();
 }

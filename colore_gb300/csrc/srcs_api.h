@@ -63,7 +63,8 @@ struct cg_los_params {
   cg::Tab d1;            /* growth factor, for Gaussian skewers */
   const float4 *pos;     /* catalogue positions */
   float *src;            /* 9 floats per source; lensing writes e1 e2 kappa dra ddec */
-  long long nsrc;
+  long long nsrc;        /* sources, or their upper bound when nsrc_dev is set */
+  const long long *nsrc_dev; /* NULL, or the device total (min with nsrc) */
   int nr;
   float dr, idr;
   const float *lfac;     /* 2 nr: 2 pg dr, then rm pg dr, pg = D(rm) (1 + z(rm)) */
@@ -76,7 +77,10 @@ struct cg_los_params {
 long long cg_srcs_nblocks(int N);
 cudaError_t cg_srcs_count(cudaStream_t s, const float *grid, const cg_srcs_params *p, long long *total);
 cudaError_t cg_srcs_emit(cudaStream_t s, const float *phi, const cg_srcs_params *p);
-cudaError_t cg_srcs_beam_rsd(cudaStream_t s, const float *phi, const cg_srcs_params *p, long long nsrc, int nsm);
+/* nsrc sources, or with nsrc_dev non-NULL min(*nsrc_dev, nsrc) read on the
+ * device (a graph-captured sequence, whose totals stay on the device). */
+cudaError_t cg_srcs_beam_rsd(cudaStream_t s, const float *phi, const cg_srcs_params *p, long long nsrc,
+                             const long long *nsrc_dev, int nsm);
 cudaError_t cg_srcs_lensing(cudaStream_t s, const float *phi, const cg_los_params *p, int nsm);
 cudaError_t cg_srcs_skewers(cudaStream_t s, const float *dens, const float *phi, const cg_los_params *p, int nsm);
 #endif

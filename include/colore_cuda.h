@@ -215,14 +215,15 @@ int cg_run_mock(cg_ctx *ctx);
 
 /* Graph-captured sequence (no counterpart in the reference; the batching
  * pattern of the GPU path).  cg_graph_capture runs the sequence once to size
- * every buffer, then captures fields, density, normalisation and sources
- * into a CUDA graph; configurations with intensity maps or line-of-sight
- * quantities are refused (those stages keep host steps).  cg_graph_launch
- * replays it on a stream (NULL: the context's); the source totals stay on
- * the device until a download or cg_num_sources reads them, and a total
- * that outgrew the catalogue is reported there (CG_EDEVICE).  Replays
- * repeat the captured realisation: change the seed with cg_upload_tables
- * and capture again. */
+ * every buffer and build the stage tables, then captures the whole sequence
+ * -- fields, density, normalisation, sources, intensity maps and the beam
+ * stage -- into a CUDA graph.  cg_graph_launch replays it on a stream (NULL:
+ * the context's); the source totals and the intensity maps' sample counts
+ * stay on the device until a download, cg_num_sources or cg_imap_samples
+ * reads them, and a total that outgrew the catalogue is reported there
+ * (CG_EDEVICE).  Replays deliver nothing to registered host buffers
+ * (cg_set_host_*): download after cg_sync.  Replays repeat the captured
+ * realisation: change the seed with cg_upload_tables and capture again. */
 int cg_graph_capture(cg_ctx *ctx);
 int cg_graph_launch(cg_ctx *ctx, void *cuda_stream);
 

@@ -1,8 +1,11 @@
 """Graph-captured sequence and batches of realisations (cg_graph_*,
 cg_batch_*): a replay gives the plain run's catalogue bit for bit, and so
 does every realisation of a batch whose graphs run side by side on several
-streams; configurations with intensity maps or line-of-sight quantities are
-refused."""
+streams.  The whole sequence is captured, intensity maps and line-of-sight
+quantities included: a replay gives the plain run's catalogue (with RSD,
+lensing and skewer columns), count maps, convergence and ISW maps bit for
+bit, the intensity maps' hit counts exactly and their brightness sums to
+float atomics' rounding (2e-6)."""
 import numpy as np
 import pytest
 
@@ -51,14 +54,63 @@ def test_graph_replay_matches_plain_run(built, tmp_path):
     m.close()
 
 
-def test_graph_refuses_maps_and_beams(built, tmp_path):
+def _c4_style(n, seed):
+    spec = _spec(n, seed, zmax=0.45)
+    spec["dens_type"] = 1
+    spec["srcs"][0]["lensing"] = True
+    spec["srcs"][0]["skewers"] = True
+    spec["imap"] = [dict(tz=0.1, bias=("const", 1.0), z_range=(0.1, 0.4), nbands=6, nside=32)]
+    spec["kappa"] = dict(z_out=[0.2, 0.4], nside=16)
+    spec["isw"] = dict(z_out=[0.3], nside=16)
+    return spec
+
+
+def _all_outputs(m):
+    out = list(_catalog(m))
+    out += list(m.skewers(0))
+    out += [m.kappa(), m.isw()]
+    data, nadd = m.imap(0, with_nadd=True)
+    return out, data, nadd
+
+
+def test_graph_replay_with_maps_and_beams(built, tmp_path):
     import colore_gb300 as cg
-    spec = _spec(64, 72)
-    spec["kappa"] = dict(z_out=[0.3], nside=8)
-    m = cg.Mock(_params(tmp_path, spec, "k"))
-    with pytest.raises(cg.CGError, match="graph capture covers"):
-        m.graph_capture()
+    m = cg.Mock(_params(tmp_path, _c4_style(64, 72), "k"))
+    m.run()
+    ref, rdata, rnadd = _all_outputs(m)
+    n0 = m.num_sources(0)
+    assert n0 > 0 and rnadd.sum() > 0
+    m.graph_capture()
+    for _ in range(2):
+        m.graph_launch()
+        assert m.num_sources(0) == n0
+        got, data, nadd = _all_outputs(m)
+        for k, (a, b) in enumerate(zip(ref, got)):
+            assert np.array_equal(a, b), k
+        assert np.array_equal(nadd, rnadd)
+        np.testing.assert_allclose(data, rdata, rtol=2e-6, atol=0)
+        assert m.imap_samples(0) > 0
     m.close()
+
+
+def test_batch_of_c4_style_realisations(built, tmp_path):
+    """Intensity maps, convergence and 1LPT in a batch: each realisation's
+    outputs equal those of the same configuration run alone."""
+    import colore_gb300 as cg
+    prms = [_params(tmp_path, _c4_style(n, 120 + i), "c%d" % i) for i, n in enumerate([64, 96, 64])]
+    b = cg.Batch(prms, nstreams=2)
+    b.run()
+    for i, p in enumerate(prms):
+        m = cg.Mock(p)
+        m.run()
+        ref, rdata, rnadd = _all_outputs(m)
+        got, data, nadd = _all_outputs(b.mocks[i])
+        for k, (x, y) in enumerate(zip(ref, got)):
+            assert np.array_equal(x, y), (i, k)
+        assert np.array_equal(nadd, rnadd), i
+        np.testing.assert_allclose(data, rdata, rtol=2e-6, atol=0)
+        m.close()
+    b.close()
 
 
 def test_batch_matches_separate_runs(built, tmp_path):
