@@ -1377,6 +1377,9 @@ static void srcs_params(cg_ctx *c, int ipop, cg_srcs_params &p)
   x.bias_model = c->cfg.bias_model;
   p.dx64 = dx;
   for (int k = 0; k < 3; k++) p.p64[k] = c->cfg.pos_obs[k];
+  for (int k = 0; k < 3; k++) p.cl[k] = c->d_corner + (size_t)(3 + k) * N;
+  p.dxh = (float)dx;
+  p.dxl = (float)(dx - (double)p.dxh);
   p.force_double = c->force_double;
   p.xstats = c->d_xstats;
 }

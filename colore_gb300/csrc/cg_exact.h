@@ -232,6 +232,35 @@ CG_HD float cgx_src_offset(double x0, double dx, uint32_t bits)
   return (float)X_ADD(x0, X_MUL(dx, X_SUB((double)cg_u01f(bits), 0.5)));
 }
 
+/* The same float coordinate from single-precision arithmetic: 1 with *out
+ * when it is certainly the double expression rounded to float, 0 otherwise.
+ * The corner x0 and dx come as float pairs (c + l, dh + dl; each pair
+ * within 2^-48 of the double value); u - 1/2 is exact in float.  The sum
+ * x0 + dx (u - 1/2) is carried as s + lo (dh t split exactly by an FMA,
+ * c + dh t by TwoSum), within 2^-44 (|c| + |s| + dh) of the reference's
+ * double value including its two roundings; f = fl(s + lo) is then the
+ * double value's float rounding unless s + lo lies that close to the
+ * midpoint between f and its neighbour on the side of s + lo. */
+CG_HD int cg_src_offset_checked(float c, float l, float dh, float dl, uint32_t bits, float *out)
+{
+  const float t = CG_SUB(cg_u01f(bits), 0.5f); /* exact: 24-bit uniform */
+  const float ph = CG_MUL(dh, t);
+  const float pe = CG_FMA(dh, t, -ph); /* dh t = ph + pe exactly */
+  const float q = CG_MUL(dl, t);
+  const float s = CG_ADD(c, ph); /* TwoSum: c + ph = s + e */
+  const float bv = CG_SUB(s, c);
+  const float e = CG_ADD(CG_SUB(c, CG_SUB(s, bv)), CG_SUB(ph, bv));
+  const float lo = CG_ADD(CG_ADD(e, l), CG_ADD(pe, q));
+  const float f = CG_ADD(s, lo);
+  const float r = CG_ADD(CG_SUB(s, f), lo); /* s - f exact: f is within an ulp of s */
+  const float nb = nextafterf(f, r >= 0.0f ? 3.0e38f : -3.0e38f);
+  const float h = CG_MUL(0.5f, cg_fabsf(CG_SUB(nb, f)));
+  const float E = CG_FMA(cg_fabsf(r), 1.2e-7f, CG_MUL(5.7e-14f, CG_ADD(CG_ADD(cg_fabsf(c), cg_fabsf(s)), dh)));
+  if (!(CG_SUB(h, cg_fabsf(r)) > E)) return 0;
+  *out = f;
+  return 1;
+}
+
 /* Shell of radius r among contiguous sorted shells (edges b[0..nr], shell i
  * between b[i] and b[i+1]): the walk of get_r_index_imap (imap.c:76-103)
  * gives this from any start; -1 below the shells, nr at or beyond them. */
@@ -381,6 +410,97 @@ CG_HD int cg_poisson_inv_checked(float lam, float elam, float u)
   return k;
 }
 
+/* PTRS (cgx_poisson_ptrs) in single precision for lam - elam >= 10: the
+ * same uniforms, and each decision -- the floor that gives the candidate k
+ * and the quick acceptance V <= v_r -- taken in float where a bound on its
+ * distance to the double value proves it (the uniforms' own comparisons,
+ * us >= 0.07, us < 0.013, V > us, are exact: us and V are multiples of
+ * 2^-24), then the logarithmic acceptance test with its own bound.  Returns
+ * the count, or -1 when a margin fails (the cell then goes to double). */
+CG_HD int cg_poisson_ptrs_checked(float lam, float elam, long long cid, uint32_t k0, uint32_t k1)
+{
+  /* us >= 0.07 and us < 0.013 for multiples of 2^-24: ceil(0.07 2^24) = 1174406,
+   * ceil(0.013 2^24) = 218104 */
+  const float T07 = 1174406.0f * CG_E24, T013 = 218104.0f * CG_E24;
+  const float slam = CG_SQRT(lam);
+  const float es = CG_FMA(slam, CG_E24, CG_DIV(elam, CG_MUL(2.0f, CG_SQRT(CG_SUB(lam, elam)))));
+  const float b = CG_FMA(2.53f, slam, 0.931f);
+  const float eb = CG_FMA(2.53f, es, CG_FMA(2.5e-7f, CG_ADD(slam, 1.0f), CG_MUL(CG_E24, b)));
+  const float a = CG_FMA(0.02483f, b, -0.059f);
+  const float ea = CG_FMA(0.025f, eb, CG_FMA(1e-8f, CG_ADD(b, 1.0f), CG_MUL(CG_E24, cg_fabsf(a))));
+  const float g = CG_SUB(b, 2.0f);
+  const float h = CG_DIV(3.6224f, g);
+  const float vr = CG_SUB(0.9277f, h);
+  const float evr = CG_ADD(CG_DIV(CG_MUL(3.63f, CG_FMA(CG_E24, g, eb)), CG_MUL(g, g)),
+                           CG_FMA(2.0f * CG_E24, h, CG_FMA(CG_E24, cg_fabsf(vr), 1e-7f)));
+  for (uint32_t it = 0; it < 64u; it++) {
+    const cg_u32x4 w = cg_philox4x32_10((uint32_t)cid, (uint32_t)((unsigned long long)cid >> 32), it, 1u, k0, k1);
+    const float U = CG_SUB(cg_u01f(w.v[0]), 0.5f); /* exact */
+    const float V = cg_u01f(w.v[1]);
+    const float us = CG_SUB(0.5f, cg_fabsf(U)); /* exact */
+    const float t1 = CG_DIV(CG_MUL(2.0f, a), us);
+    const float t2 = CG_ADD(t1, b);
+    const float t3 = CG_MUL(t2, U);
+    const float x1 = CG_ADD(t3, lam);
+    const float X = CG_ADD(x1, 0.43f);
+    float eX = CG_MUL(cg_fabsf(U), CG_ADD(CG_ADD(CG_DIV(CG_MUL(2.0f, ea), us), eb),
+                                          CG_MUL(CG_E24, CG_ADD(cg_fabsf(t1), cg_fabsf(t2)))));
+    eX = CG_ADD(eX, CG_ADD(elam, CG_MUL(CG_E24, CG_ADD(CG_ADD(cg_fabsf(t3), cg_fabsf(x1)), cg_fabsf(X)))));
+    eX = CG_FMA(1.5f, eX, 2e-8f); /* and 0.43's representation */
+    const float fx = cg_floorf(X);
+    const float dX = CG_SUB(X, fx);
+    if (!(cg_fminf(dX, CG_SUB(1.0f, dX)) > eX)) return -1;
+    const int kd = (int)fx;
+    if (us >= T07) {
+      if (V < CG_SUB(vr, evr)) return kd;
+      if (!(V > CG_ADD(vr, evr))) return -1;
+    }
+    if (kd < 0 || (us < T013 && V > us)) continue;
+    /* the logarithmic test, log(V invalpha / (a / us^2 + b)) <= k log(lam) -
+     * lam - log k!, with the logarithms of cg_logf (within 12 2^-24 of the
+     * result, 2e-8 absolute) and log k! exact below 10, else Stirling's
+     * series to 1/(360 n^3) (truncation below 1e-8 for n >= 11) */
+    if (!(V > 0.0f)) return kd; /* log 0: accepted in double too */
+    const float lV = cg_logf(V);
+    const float ia = CG_ADD(1.1239f, CG_DIV(1.1328f, CG_SUB(b, 3.4f)));
+    const float eia = CG_FMA(1.1328f, CG_DIV(eb, CG_MUL(CG_SUB(b, 3.4f), CG_SUB(b, 3.4f))), CG_MUL(4.0f * CG_E24, ia));
+    const float us2 = CG_MUL(us, us);
+    const float qd = CG_ADD(CG_DIV(a, us2), b);
+    const float eqd = CG_ADD(CG_ADD(CG_DIV(ea, us2), eb), CG_MUL(4.0f * CG_E24, CG_ADD(CG_DIV(cg_fabsf(a), us2), qd)));
+    const float lia = cg_logf(ia), lq = cg_logf(qd);
+    const float lhs = CG_ADD(lV, CG_SUB(lia, lq));
+    float el = CG_FMA(12.0f * CG_E24, CG_ADD(CG_ADD(cg_fabsf(lV), cg_fabsf(lia)), cg_fabsf(lq)), 6e-8f);
+    el = CG_ADD(el, CG_ADD(CG_DIV(eia, ia), CG_DIV(eqd, qd)));
+    el = CG_FMA(2.0f * CG_E24, CG_ADD(cg_fabsf(lhs), CG_ADD(cg_fabsf(lia), cg_fabsf(lq))), el);
+    const float ll = cg_logf(lam);
+    const float ell = CG_ADD(CG_FMA(12.0f * CG_E24, cg_fabsf(ll), 2e-8f), CG_DIV(elam, lam));
+    const float kf = (float)kd;
+    float lg, elg;
+    if (kd < 10) {
+      lg = cg_logfact_small(kd);
+      elg = CG_MUL(CG_E24, lg);
+    } else {
+      const float nn = CG_ADD(kf, 1.0f);
+      const float ln = cg_logf(nn);
+      const float t = CG_MUL(CG_SUB(nn, 0.5f), ln);
+      const float inn = CG_DIV(1.0f, nn);
+      const float corr = CG_MUL(inn, CG_SUB(0.0833333358f, CG_MUL(CG_MUL(inn, inn), 0.00277777785f)));
+      lg = CG_ADD(CG_ADD(CG_SUB(t, nn), 0.918938533f), corr);
+      elg = CG_FMA(CG_SUB(nn, 0.5f), CG_FMA(12.0f * CG_E24, ln, 2e-8f),
+                   CG_FMA(2.0f * CG_E24, CG_ADD(CG_ADD(cg_fabsf(t), nn), cg_fabsf(lg)), 6e-8f));
+    }
+    const float kl = CG_MUL(kf, ll);
+    const float rhs = CG_SUB(CG_SUB(kl, lam), lg);
+    float er = CG_FMA(kf, ell, CG_ADD(elam, elg));
+    er = CG_FMA(2.0f * CG_E24, CG_ADD(CG_ADD(cg_fabsf(kl), cg_fabsf(CG_SUB(kl, lam))), cg_fabsf(rhs)), er);
+    const float m = CG_MUL(1.5f, CG_ADD(el, er));
+    const float dlr = CG_SUB(lhs, rhs);
+    if (dlr < -m) return kd;
+    if (!(dlr > m)) return -1;
+  }
+  return -1;
+}
+
 /* ---- RING pixel with a margin ----------------------------------------- */
 
 /* Direction of (x, y, z) in the form the pixel decisions need: cos(theta),
@@ -522,8 +642,8 @@ typedef struct {
 
 /* lambda of cell (ix, iy, iz) in single precision with a bound *elam on its
  * distance to cgx_lambda: returns 0 when the double lambda is 0, 1 when
- * (*lam, *elam) hold and lambda < 10 (inversion), 2 when only the double
- * computation can decide. */
+ * (*lam, *elam) hold and lambda < 10 (inversion), 3 when they hold and
+ * lambda >= 10 (PTRS), 2 when only the double computation can decide. */
 CG_HD int cg_lambda_checked(const cg_pois_args *a, int ix, int iy, int iz, float d, float *lam, float *elam)
 {
   *lam = 0.0f;
@@ -569,7 +689,7 @@ CG_HD int cg_lambda_checked(const cg_pois_args *a, int ix, int iy, int iz, float
   *lam = l;
   *elam = e;
   if (!(l > 0.0f)) return e == 0.0f ? 0 : 2;
-  if (!(CG_ADD(l, e) < 10.0f)) return 2; /* PTRS, or too close to the switch */
+  if (!(CG_ADD(l, e) < 10.0f)) return CG_SUB(l, e) >= 10.0f ? 3 : 2; /* PTRS, or too close to the switch */
   return 1;
 }
 
@@ -584,6 +704,9 @@ CG_HD int cg_count_cell(const cg_pois_args *a, int ix, int iy, int iz, float d, 
   if (st == 0) return 0;
   if (st == 1) {
     const int n = cg_poisson_inv_checked(lam, elam, cg_u01f(w));
+    if (n >= 0) return n;
+  } else if (st == 3) {
+    const int n = cg_poisson_ptrs_checked(lam, elam, cid, k0, k1);
     if (n >= 0) return n;
   }
   *fb = 1;

@@ -117,11 +117,13 @@ __device__ __forceinline__ void fix_add(unsigned long long *a, double x)
  * for the redshift and every tracer. */
 __host__ __device__ inline size_t bins_warp_bytes(int nz, int nt) { return (size_t)nz * (4 + 8 * (1 + nt)); }
 
+template <int NT>
 __global__ void __launch_bounds__(BINS_WARPS * 32, 2) k_dens_bins(float *grid, cg_bins_params p)
 {
   extern __shared__ unsigned char sbins[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwb = blockDim.x >> 5;
-  const int nz = p.nz, nt = p.nt, W = 1 + nt;
+  constexpr int nt = NT, MT = NT > 0 ? NT : 1;
+  const int nz = p.nz, W = 1 + nt;
   unsigned int *cnt = reinterpret_cast<unsigned int *>(sbins + (size_t)wid * bins_warp_bytes(nz, nt));
   float *acc = reinterpret_cast<float *>(cnt + nz); /* [nz][W] sums, then [nz][W] corrections */
   float *cor = acc + (size_t)nz * W;
@@ -141,9 +143,9 @@ __global__ void __launch_bounds__(BINS_WARPS * 32, 2) k_dens_bins(float *grid, c
     const int iz = row / N, iy = row - iz * N;
     const int ix = sr * 32 + lane;
     int bin = -1;
-    float zz = 0.0f, bs[MAXT];
+    float zz = 0.0f, bs[MT];
 #pragma unroll
-    for (int t = 0; t < MAXT; t++) bs[t] = 0.0f;
+    for (int t = 0; t < MT; t++) bs[t] = 0.0f;
     if (ix < N) {
       float *ptr = grid + pidx(ix, iy, iz, N);
       float d = *ptr;
@@ -169,8 +171,7 @@ __global__ void __launch_bounds__(BINS_WARPS * 32, 2) k_dens_bins(float *grid, c
           bin = b;
           zz = z;
 #pragma unroll
-          for (int t = 0; t < MAXT; t++)
-            if (t < nt) bs[t] = cg_bias_model(d, bgv(p.bz[t], at), p.bias_model);
+          for (int t = 0; t < nt; t++) bs[t] = cg_bias_model(d, bgv(p.bz[t], at), p.bias_model);
         }
       }
     }
@@ -182,16 +183,15 @@ __global__ void __launch_bounds__(BINS_WARPS * 32, 2) k_dens_bins(float *grid, c
       const bool mine = (bin == lb);
       const unsigned grp = __ballot_sync(0xffffffffu, mine);
       const float zsum = wsum(zz, mine);
-      float bsum[MAXT];
+      float bsum[MT];
 #pragma unroll
-      for (int t = 0; t < MAXT; t++) bsum[t] = (t < nt) ? wsum(bs[t], mine) : 0.0f;
+      for (int t = 0; t < nt; t++) bsum[t] = wsum(bs[t], mine);
       if (lane == 0) {
         float *a = acc + (size_t)lb * W, *c = cor + (size_t)lb * W;
         cnt[lb] += (unsigned)__popc(grp);
         kahan_add(a[0], c[0], zsum);
 #pragma unroll
-        for (int t = 0; t < MAXT; t++)
-          if (t < nt) kahan_add(a[1 + t], c[1 + t], bsum[t]);
+        for (int t = 0; t < nt; t++) kahan_add(a[1 + t], c[1 + t], bsum[t]);
       }
       todo &= ~grp;
     }
@@ -489,7 +489,11 @@ cudaError_t cg_dens_bins(cudaStream_t s, float *grid, const cg_bins_params *p, i
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= CG_MAX_DEVICES) return cudaErrorInvalidDevice;
     if (!set[dev]) {
-      cudaError_t e = cudaFuncSetAttribute(k_dens_bins, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      cudaError_t e = cudaSuccess;
+#define X(k) \
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dens_bins<k>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      X(0) X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8)
+#undef X
       if (e != cudaSuccess) return e;
       set[dev] = true;
     }
@@ -498,7 +502,14 @@ cudaError_t cg_dens_bins(cudaStream_t s, float *grid, const cg_bins_params *p, i
   long long blocks = (nrow + nwb - 1) / nwb;
   long long cap = (long long)nsm * 8;
   if (blocks > cap) blocks = cap;
-  k_dens_bins<<<(unsigned)blocks, nwb * 32, smem, s>>>(grid, *p);
+  switch (p->nt) { /* one instantiation per tracer count: loops of exact length */
+#define X(k)                                                           \
+  case k:                                                              \
+    k_dens_bins<k><<<(unsigned)blocks, nwb * 32, smem, s>>>(grid, *p); \
+    break;
+    X(0) X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8)
+#undef X
+  }
   if (p->nz > 0) {
     const int nv = p->nz * (1 + p->nt);
     k_bins_finish<<<(nv + 255) / 256, 256, 0, s>>>(p->acc, p->nz, p->nt, p->zsum, p->bsum);

@@ -70,6 +70,13 @@ __device__ __noinline__ int count_double(const cg_srcs_params &p, int ix, int iy
   return cgx_poisson(lam, (double)cg_u01f(w), cid, p.kp0, p.kp1);
 }
 
+/* PTRS in single precision (lambda >= 10: the cells next to the observer,
+ * or dense coarse grids), out of line like the double path. */
+__device__ __noinline__ int ptrs_float(float lam, float elam, long long cid, uint32_t k0, uint32_t k1)
+{
+  return cg_poisson_ptrs_checked(lam, elam, cid, k0, k1);
+}
+
 /* Counts of CPT consecutive cells of one row per thread.  Each cell's lambda
  * is formed in single precision with a bound on its distance to the
  * reference's double lambda, and the Poisson inversion keeps its float
@@ -102,7 +109,7 @@ __global__ void __launch_bounds__(SB, 4) k_pois_count(const float *__restrict__ 
       const float d = __ldg(row + h);
       float lam, elam;
       int st = cg_lambda_checked(&p.pa, ix + h, iy, iz, d, &lam, &elam);
-      if (p.force_double && st == 1) st = 2;
+      if (p.force_double && (st == 1 || st == 3)) st = 2;
       int n = 0;
       if (st != 0) {
         if ((cid >> 2) != wm) {
@@ -111,7 +118,8 @@ __global__ void __launch_bounds__(SB, 4) k_pois_count(const float *__restrict__ 
         }
         const int q = (int)(cid & 3);
         const uint32_t wq = q == 0 ? w.v[0] : (q == 1 ? w.v[1] : (q == 2 ? w.v[2] : w.v[3]));
-        n = st == 1 ? cg_poisson_inv_checked(lam, elam, cg_u01f(wq)) : -1;
+        n = st == 1 ? cg_poisson_inv_checked(lam, elam, cg_u01f(wq))
+                    : (st == 3 ? ptrs_float(lam, elam, cid, p.kp0, p.kp1) : -1);
         if (n < 0) {
           n = count_double(p, ix + h, iy, iz, d, cid, wq);
           nfb++;
@@ -281,10 +289,15 @@ __global__ void __launch_bounds__(SB, 8) k_emit(const float *__restrict__ phi, c
     const float rvel = CG_MUL(p.factor_vel, cg_rvel(v[0], v[1], v[2], x0, y0, z0, rr, p.box.idx));
     const float dz_rsd = CG_MUL(rvel, bg(p.v1, p.g, rr));
     cg_u32x4 u = cg_philox4x32_10((uint32_t)cid, (uint32_t)(cid >> 32), (uint32_t)j, 0u, p.kq0, p.kq1);
-    /* the position in double, stored as float (srcs.c:261-263) */
-    const float px = cgx_src_offset(cgx_coord(ix, p.dx64, p.p64[0]), p.dx64, u.v[0]);
-    const float py = cgx_src_offset(cgx_coord(iy, p.dx64, p.p64[1]), p.dx64, u.v[1]);
-    const float pz = cgx_src_offset(cgx_coord(iz, p.dx64, p.p64[2]), p.dx64, u.v[2]);
+    /* the position of the double arithmetic, stored as float (srcs.c:261-263):
+     * in single precision where its rounding is certain, else in double */
+    float px, py, pz;
+    if (p.force_double || !cg_src_offset_checked(p.pa.xc[ix], p.cl[0][ix], p.dxh, p.dxl, u.v[0], &px))
+      px = cgx_src_offset(cgx_coord(ix, p.dx64, p.p64[0]), p.dx64, u.v[0]);
+    if (p.force_double || !cg_src_offset_checked(p.pa.yc[iy], p.cl[1][iy], p.dxh, p.dxl, u.v[1], &py))
+      py = cgx_src_offset(cgx_coord(iy, p.dx64, p.p64[1]), p.dx64, u.v[1]);
+    if (p.force_double || !cg_src_offset_checked(p.pa.zc[iz], p.cl[2][iz], p.dxh, p.dxl, u.v[2], &pz))
+      pz = cgx_src_offset(cgx_coord(iz, p.dx64, p.p64[2]), p.dx64, u.v[2]);
     p.pos[id] = make_float4(px, py, pz, dz_rsd);
     float r, cth, ph;
     cg_cart2sph(px, py, pz, &r, &cth, &ph);

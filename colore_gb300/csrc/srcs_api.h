@@ -42,6 +42,8 @@ struct cg_srcs_params {
    * xstats[0] cells and xstats[1] pixels decided in double */
   cg_pois_args pa;
   double dx64, p64[3];
+  const float *cl[3];  /* low parts of the float corners (pa.xc..: c + l = the double corner) */
+  float dxh, dxl;      /* dx as a float pair */
   int force_double;
   unsigned long long *xstats;
 };

@@ -75,3 +75,30 @@ void or_pix_cgx(long nside, const double *xyz, long n, long long *pix)
     pix[i] = cgx_ang2pix(nside, cth, ph);
   }
 }
+
+/* cg_src_offset_checked on n (corner, uniform) pairs with one dx: out[i] the
+ * float coordinate (0 when not certain), ok[i] 1 when certain; ref[i] the
+ * double expression rounded to float (cgx_src_offset). */
+void or_src_offset_checked(long n, const double *x0, double dx, const uint32_t *bits, float *out, int *ok, float *ref)
+{
+  const float dh = (float)dx, dl = (float)(dx - (double)(float)dx);
+  for (long i = 0; i < n; i++) {
+    const float c = (float)x0[i], l = (float)(x0[i] - (double)(float)x0[i]);
+    float f = 0.0f;
+    ok[i] = cg_src_offset_checked(c, l, dh, dl, bits[i], &f);
+    out[i] = f;
+    ref[i] = cgx_src_offset(x0[i], dx, bits[i]);
+  }
+}
+
+/* cg_poisson_ptrs_checked against cgx_poisson_ptrs on n means: got[i] the
+ * single-precision count (-1: left to double), ref[i] the double one, for
+ * float means lam[i] known within elam[i] of the double mean lam64[i]. */
+void or_ptrs_checked(long n, const float *lam, const float *elam, const double *lam64, const long long *cid, uint32_t k0,
+                     uint32_t k1, int *got, int *ref)
+{
+  for (long i = 0; i < n; i++) {
+    got[i] = cg_poisson_ptrs_checked(lam[i], elam[i], cid[i], k0, k1);
+    ref[i] = cgx_poisson_ptrs(lam64[i], cid[i], k0, k1);
+  }
+}

@@ -278,6 +278,7 @@ int or_emit32(const cg_config *cfg, int ipop, const float *dens, const float *np
         float v2 = CG_SUB(npot[pidx(ix, iy, zh, N)], npot[pidx(ix, iy, zl, N)]);
         float rvel = CG_MUL(fvel, cg_rvel(v0, v1, v2, x0, y0, z0, rr, s.idx));
         float dz = CG_MUL(rvel, bg32(&s, s.v1, rr));
+        const float dxh = (float)dxd, dxl = (float)(dxd - (double)(float)dxd);
         const double x0d = cgx_coord(ix, dxd, cfg->pos_obs[0]), y0d = cgx_coord(iy, dxd, cfg->pos_obs[1]);
         const double z0d = cgx_coord(iz, dxd, cfg->pos_obs[2]);
         for (int j = 0; j < n; j++, id++) {
@@ -287,9 +288,14 @@ int or_emit32(const cg_config *cfg, int ipop, const float *dens, const float *np
             return -1;
           }
           cg_u32x4 u = cg_philox4x32_10((uint32_t)cid, (uint32_t)(cid >> 32), (uint32_t)j, 0u, kq0, kq1);
-          float px = cgx_src_offset(x0d, dxd, u.v[0]);
-          float py = cgx_src_offset(y0d, dxd, u.v[1]);
-          float pz = cgx_src_offset(z0d, dxd, u.v[2]);
+          /* the kernel's route: single precision where certain, else double */
+          float px, py, pz;
+          if (!cg_src_offset_checked((float)x0d, (float)(x0d - (double)(float)x0d), dxh, dxl, u.v[0], &px))
+            px = cgx_src_offset(x0d, dxd, u.v[0]);
+          if (!cg_src_offset_checked((float)y0d, (float)(y0d - (double)(float)y0d), dxh, dxl, u.v[1], &py))
+            py = cgx_src_offset(y0d, dxd, u.v[1]);
+          if (!cg_src_offset_checked((float)z0d, (float)(z0d - (double)(float)z0d), dxh, dxl, u.v[2], &pz))
+            pz = cgx_src_offset(z0d, dxd, u.v[2]);
           if (pos4) {
             pos4[4 * id + 0] = px;
             pos4[4 * id + 1] = py;

@@ -105,4 +105,9 @@ int or_skw32(const cg_config *cfg, const float *dens, const float *npot, int gau
 int or_sht_legendre(int lmax, int nring, int K, const double *z, const double *S, const double *A, double omega,
                     double *alm);
 
+void or_src_offset_checked(long n, const double *x0, double dx, const uint32_t *bits, float *out, int *ok, float *ref);
+
+void or_ptrs_checked(long n, const float *lam, const float *elam, const double *lam64, const long long *cid, uint32_t k0,
+                     uint32_t k1, int *got, int *ref);
+
 #endif

@@ -53,9 +53,12 @@ def lib():
             "or_pix_checked": [C.c_long, vp, C.c_long, f, vp], "or_pix_cgx": [C.c_long, vp, C.c_long, vp],
             "or_pix64": [C.c_long, vp, C.c_long, vp],
             "or_sht_legendre": [i, i, i, vp, vp, vp, d, vp],
+            "or_src_offset_checked": [C.c_long, vp, d, vp, vp, vp, vp],
+            "or_ptrs_checked": [C.c_long, vp, vp, vp, vp, C.c_uint32, C.c_uint32, vp, vp],
         }
         void = ("or_philox", "or_poisson", "or_ang2pix", "or_nest2ring", "or_ring2nest", "or_pix2vec_nest",
-                "or_shell_index", "or_pix_checked", "or_pix_cgx", "or_pix64")
+                "or_shell_index", "or_pix_checked", "or_pix_cgx", "or_pix64", "or_src_offset_checked",
+                "or_ptrs_checked")
         for k, a in sig.items():
             fn = getattr(L, k)
             fn.argtypes = a
@@ -506,3 +509,30 @@ def pix64(nside, xyz, shared=False):
     out = np.empty(len(a), np.int64)
     (lib().or_pix_cgx if shared else lib().or_pix64)(nside, P(a), len(a), P(out))
     return out
+
+
+def src_offset_checked(x0, dx, bits):
+    """The emission's single-precision source coordinate (cg_src_offset_checked)
+    for corners x0 (double) and uniform words bits: (out, ok, ref) with ref
+    the double expression rounded to float."""
+    x0 = np.ascontiguousarray(x0, np.float64)
+    bits = np.ascontiguousarray(bits, np.uint32)
+    n = len(x0)
+    out = np.empty(n, np.float32)
+    ok = np.empty(n, np.int32)
+    ref = np.empty(n, np.float32)
+    lib().or_src_offset_checked(n, P(x0), C.c_double(dx), P(bits), P(out), P(ok), P(ref))
+    return out, ok.astype(bool), ref
+
+
+def ptrs_checked(lam, elam, lam64, cid, k0, k1):
+    """Single-precision PTRS (-1 where left to double) and the double PTRS."""
+    lam = np.ascontiguousarray(lam, np.float32)
+    elam = np.ascontiguousarray(elam, np.float32)
+    lam64 = np.ascontiguousarray(lam64, np.float64)
+    cid = np.ascontiguousarray(cid, np.int64)
+    n = len(lam)
+    got = np.empty(n, np.int32)
+    ref = np.empty(n, np.int32)
+    lib().or_ptrs_checked(n, P(lam), P(elam), P(lam64), P(cid), k0, k1, P(got), P(ref))
+    return got, ref

@@ -159,3 +159,51 @@ def test_imap_hits_equal_double(tmp_path, case):
     np.testing.assert_allclose(data32, data64, rtol=2e-6, atol=1e-12)
     # the double path is the exception
     assert stats[1] < 5e-3 * stats[2], stats
+
+
+# (128, 3.0): dx = 3 2^-7 and the observer at 1.5, so every sum is exact in
+# double and often falls exactly half-way between two floats -- a tie the
+# single-precision check leaves to double
+@pytest.mark.parametrize("n_grid,l_box,fall", [(64, 874.993, 1e-4), (1024, 7727.3, 1e-4), (2048, 14401.7, 1e-4),
+                                               (128, 3.0, 5e-2)])
+def test_source_offset_in_single_precision(n_grid, l_box, fall):
+    """The emission's source coordinate (float)(x0 + dx (u - 1/2)) of the
+    double arithmetic (srcs.c:261-263), formed in single precision: whenever
+    it claims certainty it equals the double expression rounded to float,
+    including corners next to the observer (x0 near 0) and uniforms at the
+    cell edges; it falls back for a few in a million (the margin is 2^-44
+    of the corner against half a float ulp)."""
+    import oracle as orc
+    r = np.random.default_rng(n_grid)
+    dx = l_box / n_grid
+    pos_obs = 0.5 * l_box
+    n = 400000
+    i = r.integers(0, n_grid, n)
+    x0 = i * dx - pos_obs
+    bits = r.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+    bits[:1000] = np.arange(1000) << 8                  # u near 0
+    bits[1000:2000] = (2 ** 24 - 1 - np.arange(1000)) << 8  # u near 1
+    x0[2000:3000] = (n_grid // 2) * dx - pos_obs        # the observer's cell
+    out, ok, ref = orc.src_offset_checked(x0, dx, bits)
+    assert np.array_equal(out[ok].view(np.uint32), ref[ok].view(np.uint32))
+    assert 1 - ok.mean() < fall, 1 - ok.mean()
+
+
+def test_ptrs_in_single_precision():
+    """PTRS (Hormann 1993) for lambda >= 10 in single precision: wherever it
+    decides, the count equals the double PTRS of the reference's mean, for
+    float means anywhere within their bound of it; below lambda = 100 (where
+    nearly all such cells are) 99.9 % of draws decide in single precision,
+    88 % above 1000 (the logarithmic test's terms grow with lambda)."""
+    import oracle as orc
+    r = np.random.default_rng(3)
+    n = 300000
+    lam64 = np.exp(r.uniform(np.log(10.5), np.log(5e4), n))
+    elam = (lam64 * 8 * 2.0 ** -24).astype(np.float32)
+    lam = (lam64 * (1 + r.uniform(-1, 1, n) * 6 * 2.0 ** -24)).astype(np.float32)
+    cid = r.integers(0, 2 ** 40, n)
+    got, ref = orc.ptrs_checked(lam, elam, lam64, cid, 12345, 678)
+    ok = got >= 0
+    assert np.array_equal(got[ok], ref[ok])
+    low = lam64 < 100
+    assert ok[low].mean() > 0.99 and ok.mean() > 0.9, (ok[low].mean(), ok.mean())
