@@ -170,6 +170,7 @@ def run_ours(args):
     for _ in range(args.warmup):
         m.run()
     m.sync()
+    m.exact_stats(reset=True)
     # device-timed region (inputs resident; grids of 4.3 GB per field >> 129 MB L2)
     m.set_profiling(True)
     l0 = m.launches()
@@ -196,6 +197,8 @@ def run_ours(args):
         g[1] += 1
     m.set_profiling(False)
     nsrc = [m.num_sources(i) for i in range(cfg.n_srcs)]
+    # what the timed steps left to double arithmetic (cg_exact_stats)
+    exact = m.exact_stats(reset=True)
     # end-to-end through the C ABI with host buffers: the outputs the
     # reference's writers take (the catalogue's Src array, src/common.h:169-179;
     # the intensity maps as data/nadd; the convergence maps) are registered as
@@ -325,6 +328,10 @@ def run_ours(args):
         "wall_s_timed": t_wall,
         "roofline": rl,
         "fft_plan": m.field_plan(),
+        "exact_decisions": {"per_step": {k: v / max(args.steps, 1) for k, v in exact.items()},
+                            "note": "decisions taken in double per step (cells' counts, source pixels, "
+                                    "intensity-map cells and sub-samples); every other decision in single "
+                                    "precision with a proven margin"},
         "roofline_dominant": {"kernel": dom[0], "ms": round(dom[1], 3), "share": round(dom[1] / (t_step * 1e3), 3),
                               "bound": "instruction issue (ncu: 91 % issue-active, 7 % of DRAM peak at 512^3)"
                               if dom[0] == "imap_paint" else "see kernels"} if dom else None,

@@ -78,6 +78,7 @@ struct cg_ctx {
   size_t grid_floats = 0;
   /* host double tables */
   std::vector<double> h_r, h_z, h_d1, h_v1, h_ih, h_a, h_ra, h_pd;
+  std::vector<unsigned char> cfg_sig; /* the last uploaded configuration and tables */
   /* device tables */
   float *d_tabs = nullptr;
   Grid1 g;
@@ -553,13 +554,52 @@ static int validate(const cg_config *cfg, char *msg, size_t len)
   return CG_OK;
 }
 
+/* The configuration's bytes and the contents of every table it points to. */
+static std::vector<unsigned char> config_signature(const cg_config *cfg)
+{
+  std::vector<unsigned char> v;
+  auto put = [&](const void *p, size_t n) {
+    if (!p || !n) return;
+    const unsigned char *b = static_cast<const unsigned char *>(p);
+    v.insert(v.end(), b, b + n);
+  };
+  put(cfg, sizeof(*cfg));
+  const size_t na = CG_NA * sizeof(double);
+  const double *tabs[] = {cfg->r_arr_r2z, cfg->z_arr_r2z, cfg->growth_d_arr, cfg->growth_d2_arr, cfg->growth_v_arr,
+                          cfg->growth_pd_arr, cfg->ihub_arr, cfg->a_arr_a2r, cfg->r_arr_a2r};
+  for (const double *t : tabs) put(t, na);
+  put(cfg->pkarr, (size_t)(cfg->numk > 0 ? cfg->numk : 0) * sizeof(double));
+  for (int i = 0; i < cfg->n_srcs && i < CG_NPOP_MAX; i++) {
+    put(cfg->srcs_nz_arr[i], na);
+    put(cfg->srcs_bz_arr[i], na);
+  }
+  for (int i = 0; i < cfg->n_imap && i < CG_NPOP_MAX; i++) {
+    put(cfg->imap_tz_arr[i], na);
+    put(cfg->imap_bz_arr[i], na);
+    put(cfg->imap_r0[i], (size_t)(cfg->imap_nr[i] > 0 ? cfg->imap_nr[i] : 0) * sizeof(double));
+    put(cfg->imap_rf[i], (size_t)(cfg->imap_nr[i] > 0 ? cfg->imap_nr[i] : 0) * sizeof(double));
+  }
+  for (int i = 0; i < cfg->n_cstm && i < CG_NPOP_MAX; i++) {
+    put(cfg->cstm_kz_arr[i], na);
+    put(cfg->cstm_bz_arr[i], na);
+  }
+  return v;
+}
+
 extern "C" int cg_upload_tables(cg_ctx *c, const cg_config *cfg)
 {
   if (!c) return CG_EINVAL;
   if (int rc = validate(cfg, c->err, sizeof(c->err))) return rc;
   if (cfg->n_grid != c->N) return fail(c, CG_EINVAL, "n_grid differs from the context's");
   c->cfg = *cfg;
-  c->tab_gen++;
+  {
+    /* the stage tables derived from these are rebuilt only when something changed */
+    std::vector<unsigned char> sig = config_signature(cfg);
+    if (sig != c->cfg_sig) {
+      c->cfg_sig.swap(sig);
+      c->tab_gen++;
+    }
+  }
   const int na = CG_NA;
   auto cp = [&](std::vector<double> &v, const double *src) { v.assign(src, src + na); };
   cp(c->h_r, cfg->r_arr_r2z);

@@ -522,16 +522,16 @@ __global__ void __launch_bounds__(IW * 32, 6) k_imap_paint(cg_imap_params p)
       }
       flush<K>(p, k0, n0, c.temp);
       flush<K>(p, k1, n1, c.temp);
-      /* the held samples: one queue atomic per warp */
+      /* the held samples: one queue atomic per warp (most units hold none) */
       const int held = nf < 4 ? nf : 4;
-      int incl = held;
+      if (__any_sync(FULL, held > 0)) {
+        int incl = held;
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(FULL, incl, o);
-        if (lane >= o) incl += t;
-      }
-      const int tot = __shfl_sync(FULL, incl, 31);
-      if (tot) {
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(FULL, incl, o);
+          if (lane >= o) incl += t;
+        }
+        const int tot = __shfl_sync(FULL, incl, 31);
         unsigned long long q0 = 0;
         if (lane == 31) q0 = atomicAdd(&p.ctr[4], (unsigned long long)tot);
         q0 = __shfl_sync(FULL, q0, 31) + (unsigned long long)(incl - held);
@@ -558,31 +558,57 @@ __global__ void __launch_bounds__(256) k_imap_double(const float *__restrict__ p
   const unsigned long long nq0 = p.ctr[4];
   const long long nq = (long long)nq0 < p.queue_cap ? (long long)nq0 : p.queue_cap;
   if (blockIdx.x == 0 && threadIdx.x == 0 && nq > 0) atomicAdd(p.xstats + 3, (unsigned long long)nq);
-  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nq; k += (long long)gridDim.x * blockDim.x) {
-    const unsigned long long e = p.queue[k];
+  /* warp-uniform steps over the queue: consecutive entries mostly share a
+   * record (a lane queues up to four samples of its unit together), so the
+   * first lane of each run of one record takes the cell's double quantities
+   * and hands them to the rest of the run */
+  const int lane = threadIdx.x & 31;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long kb = (long long)blockIdx.x * blockDim.x + threadIdx.x - lane; kb < nq; kb += stride) {
+    const long long k = kb + lane;
+    const bool valid = k < nq;
+    const unsigned long long e = valid ? p.queue[k] : ~0ull;
     const long long rec = (long long)(e >> 30);
     const int q = (int)(e & ((1ull << 30) - 1));
-    /* the record's bucket: last b with base[b] <= rec */
-    int lo = 0, hi = p.nbk - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (p.base[mid] <= rec) lo = mid;
-      else hi = mid - 1;
-    }
-    int ix, iy, iz, dbl;
-    const cg_imap_cell c = unpack(p.recs[rec], lo - 1, &ix, &iy, &iz, &dbl);
-    const int ns = sh.nsub[lo];
-    float v[3];
-    grad_phi(phi, ix, iy, iz, p.box.N, v);
-    int j, s = -1, sx, sy, sz;
+    const long long prev = __shfl_up_sync(FULL, rec, 1);
+    const bool lead = valid && (lane == 0 || prev != rec);
+    const unsigned lm = __ballot_sync(FULL, lead);
+    const unsigned le = lm & (lane == 31 ? FULL : ((2u << lane) - 1u));
+    const int src = valid ? 31 - __clz(le) : lane;
+    int lo = 0, ix = 0, iy = 0, iz = 0;
+    float temp = 0.0f;
     double drr = 0;
-    cgx_imap_cell(&A, ix, iy, iz, v, &j, &drr);
+    if (lead) {
+      /* the record's bucket: last b with base[b] <= rec */
+      int hi = p.nbk - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (p.base[mid] <= rec) lo = mid;
+        else hi = mid - 1;
+      }
+      int dbl;
+      const cg_imap_cell c = unpack(p.recs[rec], lo - 1, &ix, &iy, &iz, &dbl);
+      temp = c.temp;
+      float v[3];
+      grad_phi(phi, ix, iy, iz, p.box.N, v);
+      int j;
+      cgx_imap_cell(&A, ix, iy, iz, v, &j, &drr);
+    }
+    lo = __shfl_sync(FULL, lo, src);
+    ix = __shfl_sync(FULL, ix, src);
+    iy = __shfl_sync(FULL, iy, src);
+    iz = __shfl_sync(FULL, iz, src);
+    temp = __shfl_sync(FULL, temp, src);
+    drr = __shfl_sync(FULL, drr, src);
+    if (!valid) continue;
+    const int ns = sh.nsub[lo];
+    int s = -1, sx, sy, sz;
     sub_of(q, ns, sh.invns[lo], &sx, &sy, &sz);
     long long pix = 0;
     cgx_imap_sample(&A, ix, iy, iz, ns, drr, sx, sy, sz, &s, &pix);
     if (s >= 0 && s < p.nr) {
       const long long key = (long long)s * p.npix + pix;
-      atomicAdd(&p.data[key], c.temp);
+      atomicAdd(&p.data[key], temp);
       atomicAdd(&p.nadd[key], 1);
     }
   }
