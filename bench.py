@@ -29,8 +29,8 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-BASELINE = json.load(open(os.path.join(ROOT, "BASELINE.json")))
-METRIC = BASELINE["metric"]
+# the headline metric of the 1024^3 workload
+METRIC = "end-to-end cells/s at 1024\u00b3, FP32/split vs FP64 on same GPU at P(k) err\u22641e-4"
 
 
 def peaks():
@@ -108,9 +108,9 @@ ALGO_BYTES_PER_CELL = {"field_fft": 40.0, "lpt_fft": 60.0, "dens_bins": 8.0, "sr
 # (ncu: 5-18 % of DRAM peak) and are reported under "kernels" only.
 HBM_PASSES = ("lpt_y", "lpt_x", "field_y", "field_x")
 # DRAM bytes (read + write) per cell of the same groups measured by ncu on the
-# 512^3 case of config c4 (grids larger than L2); traffic grows with the cell
-# count, so a launch at N^3 moves N^3 times these (profiles/fft_passes_c4_512.md,
-# profiles/misc_kernels_c4_512.md).
+# 512^3 case of config c4 (grids larger than L2; dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch over the cell count); traffic grows with
+# the cell count, so a launch at N^3 moves N^3 times these.
 MEASURED_DRAM_BYTES_PER_CELL = {"field_fft": 38.5, "lpt_fft": 59.8, "dens_bins": 7.6, "field_fill": 7.6,
                                 "field_y": 15.65, "field_x": 15.2, "lpt_fill": 11.8, "lpt_y": 23.68, "lpt_x": 23.7}
 

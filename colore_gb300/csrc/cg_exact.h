@@ -390,6 +390,9 @@ CG_HD cg_ve cg_bias_ve(float d, float b, float eb, int model)
  * ulp; with the additions, F_j is within (7j + 3) 2^-24 of F_j(lam). */
 CG_HD int cg_poisson_inv_checked(float lam, float elam, float u)
 {
+  /* most cells: u < 1 - lam_d <= exp(-lam_d) = F_0, so the count is 0
+   * (lam_d <= lam + elam; 2^-23 covers the two float roundings) */
+  if (u < CG_SUB(CG_SUB(1.0f, lam), CG_ADD(elam, 2.0f * CG_E24))) return 0;
   float p = expf(-lam), F = p;
   float Fp = 0.0f;
   int k = 0;
