@@ -559,6 +559,10 @@ CG_HD cg_dir cg_dir_of(float x, float y, float z, float ein)
   return o;
 }
 
+/* An integer-valued float x with |x| < 2^22 as int: x + 1.5 2^23 holds x in
+ * its low mantissa bits (exact), read without a conversion instruction. */
+CG_HD int cg_fint(float x) { return (int)(cg_f2u(CG_ADD(x, 12582912.0f)) - 0x4B400000u); }
+
 /* RING pixel of a direction at nside (a power of two), or -1 when a decision
  * lies within its error bound of the boundary.  ein bounds the distance of
  * the float coordinates to the reference's double ones relative to r (0 when
@@ -586,7 +590,7 @@ CG_HD long long cg_pix_checked(const cg_dir *d, int nside, float ein)
     const float da = CG_SUB(A, fa), db = CG_SUB(B, fb);
     const float dm = cg_fminf(cg_fminf(da, CG_SUB(1.0f, da)), cg_fminf(db, CG_SUB(1.0f, db)));
     if (!(region_ok && dm > ev)) return -1;
-    const int jp = nside * d->q + (int)fa, jm = nside * d->q + (int)fb;
+    const int jp = nside * d->q + cg_fint(fa), jm = nside * d->q + cg_fint(fb);
     const int ir = nside + 1 + jp - jm;
     const int kshift = 1 - (ir & 1);
     int ip = (jp + jm - nside + kshift + 1) >> 1;
@@ -618,7 +622,7 @@ CG_HD long long cg_pix_checked(const cg_dir *d, int nside, float ein)
   const float e2 = CG_FMA(tmp, CG_ADD(ef, CG_E24), CG_FMA(CG_SUB(1.0f, tp), es, CG_FMA(2.0f * CG_E24, p2, 2.0f * CG_E24 + 1e-9f)));
   const float f1 = floorf(p1), f2 = floorf(p2);
   const float d1 = CG_SUB(p1, f1), d2 = CG_SUB(p2, f2);
-  const int jp = (int)f1, jm = (int)f2;
+  const int jp = cg_fint(f1), jm = cg_fint(f2);
   const int ir = jp + jm + 1;
   const float p3 = CG_MUL(d->f, (float)ir);
   const float f3 = floorf(p3), d3 = CG_SUB(p3, f3);
@@ -626,7 +630,7 @@ CG_HD long long cg_pix_checked(const cg_dir *d, int nside, float ein)
   if (!(cg_fminf(d1, CG_SUB(1.0f, d1)) > e1 && cg_fminf(d2, CG_SUB(1.0f, d2)) > e2 &&
         cg_fminf(d3, CG_SUB(1.0f, d3)) > e3))
     return -1;
-  int ip = d->q * ir + (int)f3;
+  int ip = d->q * ir + cg_fint(f3);
   const int m = 4 * ir;
   if (ip >= m) ip -= m;
   if (d->cth > 0.0f) return (long long)(2 * ir * (ir - 1) + ip);

@@ -402,7 +402,7 @@ __device__ __forceinline__ void flush(const cg_imap_params &p, K k, unsigned cnt
  * the samples that only double can decide are queued with one atomic per
  * warp and step. */
 template <typename K>
-__global__ void __launch_bounds__(IW * 32, 6) k_imap_paint(cg_imap_params p)
+__global__ void __launch_bounds__(IW * 32, 8) k_imap_paint(cg_imap_params p)
 {
   extern __shared__ __align__(16) unsigned char sraw[];
   const Sh sh = load_shells(p, sraw, true);
@@ -488,9 +488,10 @@ __global__ void __launch_bounds__(IW * 32, 6) k_imap_paint(cg_imap_params p)
           const float z = CG_ADD(zc, CG_FMA(CG_ADD((float)sz, 0.5f), dxs, zl));
           for (int sy = y0; sy < y1; sy++) {
             const float y = CG_ADD(yc, CG_FMA(CG_ADD((float)sy, 0.5f), dxs, yl));
+            float fsx = 0.5f; /* sx + 1/2, exact, without a conversion per sample */
 #pragma unroll 4
-            for (int sx = 0; sx < ns; sx++) {
-              const float x = CG_ADD(xc, CG_FMA(CG_ADD((float)sx, 0.5f), dxs, xl));
+            for (int sx = 0; sx < ns; sx++, fsx = CG_ADD(fsx, 1.0f)) {
+              const float x = CG_ADD(xc, CG_FMA(fsx, dxs, xl));
               int s = -1;
               long long pix = 0;
               if (dbl || !cg_imap_decide(&A, &c, x, y, z, &s, &pix)) {
