@@ -115,6 +115,45 @@ MEASURED_DRAM_BYTES_PER_CELL = {"field_fft": 38.5, "lpt_fft": 59.8, "dens_bins":
                                 "field_y": 15.65, "field_x": 15.2, "lpt_fill": 11.8, "lpt_y": 23.68, "lpt_x": 23.7}
 
 
+# Thread-instructions per unit of work of the intensity-map stage's kernels,
+# from one-kernel ncu captures at 512^3 (smsp__inst_executed.sum x
+# smsp__thread_inst_executed_per_inst_executed.ratio over the units): the
+# listing kernel per cell in the shells' radial range, the painting kernel per
+# sub-sample.  The stage is bound by instruction issue, not HBM, so its
+# roofline is the issue rate: 4 schedulers x 32 lanes per SM and cycle.
+IMAP_INSTR_PER_CELL = 848.0
+IMAP_INSTR_PER_SAMPLE = 193.5
+
+
+def issue_roofline(dom, t_step, cfg, m, clocks):
+    """The step's largest launch group and what bounds it."""
+    name, ms = dom
+    out = {"kernel": name, "ms": round(ms, 3), "share": round(ms / (t_step * 1e3), 3)}
+    if name != "imap_paint":
+        out["bound"] = "see kernels"
+        return out
+    import math
+    import torch
+    n = cfg.n_grid
+    # cells in the shells' radial range: the ball of radius r_max in a box of
+    # side l_box (the shells reach r_max), pi/6 of the cells when it fits
+    frac = min(1.0, 4.0 / 3.0 * math.pi * (cfg.r_max / cfg.l_box) ** 3)
+    cells = frac * float(n) ** 3
+    samples = float(sum(m.imap_samples(i) for i in range(cfg.n_imap)))
+    instr = IMAP_INSTR_PER_CELL * cells + IMAP_INSTR_PER_SAMPLE * samples
+    mhz = clocks.get("sm_mhz") or 2070.0
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    peak = sms * 4 * 32 * mhz * 1e6
+    achieved = instr / (ms / 1e3)
+    out.update({"bound": "instruction issue", "achieved": achieved, "peak": peak, "unit": "thread-instructions/s",
+                "frac": round(achieved / peak, 4),
+                "basis": "ncu thread-instructions per unit at 512^3 (listing %.0f per cell in range, painting %.1f "
+                         "per sub-sample) x this step's cells and sub-samples / the stage's CUDA-event time; peak "
+                         "= SMs x 4 schedulers x 32 lanes x median SM clock; DRAM at 1-4 %% of peak"
+                         % (IMAP_INSTR_PER_CELL, IMAP_INSTR_PER_SAMPLE)})
+    return out
+
+
 # ---- replicas: one realisation per rank, no exchange on the data path ----
 def rank_seed(seed, rank):
     """Each rank runs its own realisation."""
@@ -332,9 +371,7 @@ def run_ours(args):
                             "note": "decisions taken in double per step (cells' counts, source pixels, "
                                     "intensity-map cells and sub-samples); every other decision in single "
                                     "precision with a proven margin"},
-        "roofline_dominant": {"kernel": dom[0], "ms": round(dom[1], 3), "share": round(dom[1] / (t_step * 1e3), 3),
-                              "bound": "instruction issue (ncu: 91 % issue-active, 7 % of DRAM peak at 512^3)"
-                              if dom[0] == "imap_paint" else "see kernels"} if dom else None,
+        "roofline_dominant": issue_roofline(dom, t_step, cfg, m, clk.summary()) if dom else None,
         "clocks": clk.summary(),
     }
     if not args.no_fp64:

@@ -9,7 +9,7 @@
  * error messages.  Numbers convert between int and float on lookup, as with
  * CONFIG_OPTION_AUTOCONVERT (io.c:261).
  *
- * Two optional keys extend the format for this build: global.bias_model
+ * Two optional keys extend the reference's format: global.bias_model
  * (1: (1+d)^b, 2: the Makefile's default _BIAS_MODEL_2, 3: _BIAS_MODEL_3;
  * default 2) and srcsN.nside_count (resolution of a source count map,
  * default 0 = none).
