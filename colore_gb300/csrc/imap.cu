@@ -65,17 +65,24 @@ __host__ __device__ __forceinline__ size_t shell_smem(int nr, int nbk, bool chun
   return n;
 }
 
-__device__ __forceinline__ Sh load_shells(const cg_imap_params &p, unsigned char *raw, bool chunks)
+/* Where the tables sit in the block's shared memory. */
+__device__ __forceinline__ Sh shells_at(const cg_imap_params &p, unsigned char *raw)
 {
-  const int nr = p.nr, nb = p.a.sh.nb;
+  const int nr = p.nr;
   Sh s;
   s.b = reinterpret_cast<float *>(raw);
   s.shell_of = reinterpret_cast<int *>(s.b + 2 * nr);
   s.nsub = s.shell_of + 2 * nr + 1;
   s.dxs = reinterpret_cast<float *>(s.nsub + nr + 2);
   s.invns = s.dxs + nr + 2;
-  size_t off = shell_smem(nr, p.nbk, false);
-  s.chunk_off = reinterpret_cast<unsigned long long *>(raw + off);
+  s.chunk_off = reinterpret_cast<unsigned long long *>(raw + shell_smem(nr, p.nbk, false));
+  return s;
+}
+
+__device__ __forceinline__ Sh load_shells(const cg_imap_params &p, unsigned char *raw, bool chunks)
+{
+  const int nb = p.a.sh.nb, nr = p.nr;
+  const Sh s = shells_at(p, raw);
   for (int i = threadIdx.x; i < nb; i += blockDim.x) s.b[i] = p.a.sh.b[i];
   for (int i = threadIdx.x; i <= nb; i += blockDim.x) s.shell_of[i] = p.a.sh.shell_of[i];
   for (int i = threadIdx.x; i < nr + 2; i += blockDim.x) {
@@ -355,9 +362,9 @@ __host__ __device__ __forceinline__ long long units_per_cell(int ns)
  * count: G = max(1, CHS / (32 x samples per unit)). */
 __host__ __device__ __forceinline__ int groups_per_chunk(int ns)
 {
-  const long long su = (long long)ns * ns * ns / units_per_cell(ns);
-  const long long g = CHS / (32 * su);
-  return g > 1 ? (int)g : 1;
+  const int su = ns <= 4 ? ns * ns * ns : (ns <= 32 ? ns * ns : ns); /* samples per unit */
+  const int g = CHS / (32 * su);
+  return g > 1 ? g : 1;
 }
 
 /* Chunks of every bucket: 32 G units each. */
@@ -394,13 +401,169 @@ __device__ __forceinline__ void flush(const cg_imap_params &p, K k, unsigned cnt
   }
 }
 
-/* Warps take chunks in bucket order; each lane walks one unit (a cell, a
+/* One sample at float position (x, y, z), sub-cell index q, of the lane's
+ * cell: added to the lane's two (key, count) slots -- a key in a slot adds to
+ * it, another key evicts the older slot to the maps -- or, when only double
+ * can decide it, held (up to four per unit) or queued. */
+template <typename K>
+__device__ __forceinline__ void paint_sample(const cg_imap_params &p, const cg_imap_args &A, const cg_imap_cell &c,
+                                             int dbl, long long rec, float x, float y, float z, int q, K &k0,
+                                             unsigned &n0, K &k1, unsigned &n1, int &nf, int &f0, int &f1, int &f2,
+                                             int &f3)
+{
+  int s = -1;
+  long long pix = 0;
+  if (dbl || !cg_imap_decide(&A, &c, x, y, z, &s, &pix)) {
+    if (nf == 0) f0 = q;
+    else if (nf == 1) f1 = q;
+    else if (nf == 2) f2 = q;
+    else if (nf == 3) f3 = q;
+    else queue_one(p, rec, q);
+    nf++;
+    return;
+  }
+  const K key = key_of<K>(p, s, pix);
+  if (key == empty_key<K>()) return;
+  if (key == k0) {
+    n0++;
+  } else if (key == k1) {
+    n1++;
+  } else {
+    flush<K>(p, k1, n1, c.temp);
+    k1 = k0;
+    n1 = n0;
+    k0 = key;
+    n0 = 1;
+  }
+}
+
+/* The G unit groups of one chunk of bucket b (nsub ns, NS when it is known
+ * at compile time: whole cells of NS^3 samples, their x offsets computed once
+ * per cell and the x loop unrolled).  Each lane walks one unit (a cell, a
  * slab or a line) sample by sample with its row coordinates and the cell's
- * fields held in registers, keeping two (key, count) slots: a sample whose key
- * is in a slot adds to it, another key evicts the older slot to the maps.
- * Every lane of a warp runs the same sample loop (one nsub per bucket), so
- * the samples that only double can decide are queued with one atomic per
- * warp and step. */
+ * fields held in registers.  Every lane of a warp runs the same sample loop,
+ * so the samples that only double can decide are queued with one atomic per
+ * warp and unit. */
+template <typename K, int NS>
+__device__ __forceinline__ void paint_chunk(const cg_imap_params &p, const cg_imap_args &A, int b, int ns,
+                                            unsigned long long u0, int G, unsigned long long nu, float dxs, int lane)
+{
+  const int U = (int)units_per_cell(ns);
+  /* the chunk's first unit as (record, unit within it); later units are
+   * within 32 G of it, so their offsets divide in 32 bits */
+  const long long r0 = (long long)(u0 / (unsigned long long)U);
+  const unsigned w0 = (unsigned)(u0 - (unsigned long long)r0 * (unsigned long long)U);
+  for (int g = 0; g < G; g++) {
+    const unsigned long long u = u0 + (unsigned long long)g * 32ull + (unsigned long long)lane;
+    const bool valid = u < nu;
+    /* the unit: record and its range of (sz, sy) */
+    long long rl = 0;
+    int z0 = 0, z1 = ns, y0 = 0, y1 = ns;
+    if (valid) {
+      if (U == 1) {
+        rl = (long long)u;
+      } else {
+        const unsigned t = w0 + (unsigned)(g * 32 + lane);
+        const unsigned dr = t / (unsigned)U;
+        const int w = (int)(t - dr * (unsigned)U);
+        rl = r0 + (long long)dr;
+        if (ns <= 32) {
+          z0 = w;
+          z1 = w + 1;
+        } else {
+          z0 = w / ns;
+          z1 = z0 + 1;
+          y0 = w - z0 * ns;
+          y1 = y0 + 1;
+        }
+      }
+    }
+    const long long rec = p.base[b] + rl;
+    cg_imap_cell c;
+    int ix = 0, iy = 0, iz = 0, dbl = 0;
+    float xc = 0.0f, xl = 0.0f, yc = 0.0f, yl = 0.0f, zc = 0.0f, zl = 0.0f;
+    if (valid) {
+      c = unpack(p.recs[rec], b - 1, &ix, &iy, &iz, &dbl);
+      dbl |= p.force_double;
+      xc = A.xc[ix];
+      xl = A.xl[ix];
+      yc = A.yc[iy];
+      yl = A.yl[iy];
+      zc = A.zc[iz];
+      zl = A.zl[iz];
+    } else {
+      c.temp = 0.0f;
+      c.drr = 0.0f;
+      c.edrr = 0.0f;
+      c.j = b - 1;
+      c.mode = CG_SH_SINGLE;
+      c.delta = 0;
+    }
+    K k0 = empty_key<K>(), k1 = empty_key<K>();
+    unsigned n0 = 0, n1 = 0;
+    /* samples only double can decide: up to four per lane held here and
+     * queued after the unit, the rest queued at once */
+    int nf = 0, f0 = 0, f1 = 0, f2 = 0, f3 = 0;
+    if (valid) {
+      if (NS > 0) {
+        float xs[NS > 0 ? NS : 1];
+#pragma unroll
+        for (int sx = 0; sx < NS; sx++) xs[sx] = CG_ADD(xc, CG_FMA((float)sx + 0.5f, dxs, xl));
+#pragma unroll 1
+        for (int sz = 0; sz < NS; sz++) {
+          const float z = CG_ADD(zc, CG_FMA(CG_ADD((float)sz, 0.5f), dxs, zl));
+#pragma unroll 1
+          for (int sy = 0; sy < NS; sy++) {
+            const float y = CG_ADD(yc, CG_FMA(CG_ADD((float)sy, 0.5f), dxs, yl));
+#pragma unroll
+            for (int sx = 0; sx < NS; sx++)
+              paint_sample<K>(p, A, c, dbl, rec, xs[sx], y, z, sx + NS * (sy + NS * sz), k0, n0, k1, n1, nf, f0,
+                              f1, f2, f3);
+          }
+        }
+      } else {
+        for (int sz = z0; sz < z1; sz++) {
+          const float z = CG_ADD(zc, CG_FMA(CG_ADD((float)sz, 0.5f), dxs, zl));
+          for (int sy = y0; sy < y1; sy++) {
+            const float y = CG_ADD(yc, CG_FMA(CG_ADD((float)sy, 0.5f), dxs, yl));
+            float fsx = 0.5f; /* sx + 1/2, exact, without a conversion per sample */
+#pragma unroll 4
+            for (int sx = 0; sx < ns; sx++, fsx = CG_ADD(fsx, 1.0f))
+              paint_sample<K>(p, A, c, dbl, rec, CG_ADD(xc, CG_FMA(fsx, dxs, xl)), y, z, sx + ns * (sy + ns * sz),
+                              k0, n0, k1, n1, nf, f0, f1, f2, f3);
+          }
+        }
+      }
+    }
+    flush<K>(p, k0, n0, c.temp);
+    flush<K>(p, k1, n1, c.temp);
+    /* the held samples: one queue atomic per warp (most units hold none) */
+    const int held = nf < 4 ? nf : 4;
+    if (__any_sync(FULL, held > 0)) {
+      int incl = held;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += t;
+      }
+      const int tot = __shfl_sync(FULL, incl, 31);
+      unsigned long long q0 = 0;
+      if (lane == 31) q0 = atomicAdd(&p.ctr[4], (unsigned long long)tot);
+      q0 = __shfl_sync(FULL, q0, 31) + (unsigned long long)(incl - held);
+      for (int h = 0; h < held; h++) {
+        const int q = h == 0 ? f0 : (h == 1 ? f1 : (h == 2 ? f2 : f3));
+        if ((long long)(q0 + h) < p.queue_cap)
+          p.queue[q0 + h] = ((unsigned long long)rec << 30) | (unsigned long long)q;
+        else
+          atomicOr(p.err, ERR_IMAP_QUEUE);
+      }
+    }
+  }
+}
+
+/* Warps take chunks in bucket order (paint_chunk paints one); buckets of
+ * nsub 2 to 4 -- cells of 8 to 64 samples, half the samples of a 1024^3 run
+ * -- have their own unrolled copy. */
 template <typename K>
 __global__ void __launch_bounds__(IW * 32, 8) k_imap_paint(cg_imap_params p)
 {
@@ -426,125 +589,14 @@ __global__ void __launch_bounds__(IW * 32, 8) k_imap_paint(cg_imap_params p)
     const unsigned long long nrec =
         p.cnt[b] < (unsigned long long)p.cap[b] ? p.cnt[b] : (unsigned long long)p.cap[b];
     const int ns = sh.nsub[b];
-    const long long U = units_per_cell(ns);
-    const unsigned long long nu = nrec * (unsigned long long)U;
+    const unsigned long long nu = nrec * (unsigned long long)units_per_cell(ns);
     const int G = groups_per_chunk(ns);
     const float dxs = sh.dxs[b];
     const unsigned long long u0 = (ck - sh.chunk_off[b]) * 32ull * (unsigned long long)G;
-    for (int g = 0; g < G; g++) {
-      const unsigned long long u = u0 + (unsigned long long)g * 32ull + (unsigned long long)lane;
-      const bool valid = u < nu;
-      /* the unit: record and its range of (sz, sy) */
-      long long rl = 0;
-      int z0 = 0, z1 = ns, y0 = 0, y1 = ns;
-      if (valid) {
-        if (U == 1) {
-          rl = (long long)u;
-        } else {
-          rl = (long long)(u / (unsigned long long)U);
-          const int w = (int)(u - (unsigned long long)rl * (unsigned long long)U);
-          if (ns <= 32) {
-            z0 = w;
-            z1 = w + 1;
-          } else {
-            z0 = w / ns;
-            z1 = z0 + 1;
-            y0 = w - z0 * ns;
-            y1 = y0 + 1;
-          }
-        }
-      } else {
-        z1 = z0 + (ns <= 4 ? ns : 1);
-        y1 = y0 + (ns <= 32 ? ns : 1);
-      }
-      const long long rec = p.base[b] + rl;
-      cg_imap_cell c;
-      int ix = 0, iy = 0, iz = 0, dbl = 0;
-      float xc = 0.0f, xl = 0.0f, yc = 0.0f, yl = 0.0f, zc = 0.0f, zl = 0.0f;
-      if (valid) {
-        c = unpack(p.recs[rec], b - 1, &ix, &iy, &iz, &dbl);
-        dbl |= p.force_double;
-        xc = A.xc[ix];
-        xl = A.xl[ix];
-        yc = A.yc[iy];
-        yl = A.yl[iy];
-        zc = A.zc[iz];
-        zl = A.zl[iz];
-      } else {
-        c.temp = 0.0f;
-        c.drr = 0.0f;
-        c.edrr = 0.0f;
-        c.j = b - 1;
-        c.mode = CG_SH_SINGLE;
-        c.delta = 0;
-      }
-      K k0 = empty_key<K>(), k1 = empty_key<K>();
-      unsigned n0 = 0, n1 = 0;
-      /* samples only double can decide: up to four per lane held here and
-       * queued after the unit, the rest queued at once */
-      int nf = 0, f0 = 0, f1 = 0, f2 = 0, f3 = 0;
-      if (valid) {
-        for (int sz = z0; sz < z1; sz++) {
-          const float z = CG_ADD(zc, CG_FMA(CG_ADD((float)sz, 0.5f), dxs, zl));
-          for (int sy = y0; sy < y1; sy++) {
-            const float y = CG_ADD(yc, CG_FMA(CG_ADD((float)sy, 0.5f), dxs, yl));
-            float fsx = 0.5f; /* sx + 1/2, exact, without a conversion per sample */
-#pragma unroll 4
-            for (int sx = 0; sx < ns; sx++, fsx = CG_ADD(fsx, 1.0f)) {
-              const float x = CG_ADD(xc, CG_FMA(fsx, dxs, xl));
-              int s = -1;
-              long long pix = 0;
-              if (dbl || !cg_imap_decide(&A, &c, x, y, z, &s, &pix)) {
-                const int q = sx + ns * (sy + ns * sz);
-                if (nf == 0) f0 = q;
-                else if (nf == 1) f1 = q;
-                else if (nf == 2) f2 = q;
-                else if (nf == 3) f3 = q;
-                else queue_one(p, rec, q);
-                nf++;
-                continue;
-              }
-              const K key = key_of<K>(p, s, pix);
-              if (key == empty_key<K>()) continue;
-              if (key == k0) {
-                n0++;
-              } else if (key == k1) {
-                n1++;
-              } else {
-                flush<K>(p, k1, n1, c.temp);
-                k1 = k0;
-                n1 = n0;
-                k0 = key;
-                n0 = 1;
-              }
-            }
-          }
-        }
-      }
-      flush<K>(p, k0, n0, c.temp);
-      flush<K>(p, k1, n1, c.temp);
-      /* the held samples: one queue atomic per warp (most units hold none) */
-      const int held = nf < 4 ? nf : 4;
-      if (__any_sync(FULL, held > 0)) {
-        int incl = held;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const int t = __shfl_up_sync(FULL, incl, o);
-          if (lane >= o) incl += t;
-        }
-        const int tot = __shfl_sync(FULL, incl, 31);
-        unsigned long long q0 = 0;
-        if (lane == 31) q0 = atomicAdd(&p.ctr[4], (unsigned long long)tot);
-        q0 = __shfl_sync(FULL, q0, 31) + (unsigned long long)(incl - held);
-        for (int h = 0; h < held; h++) {
-          const int q = h == 0 ? f0 : (h == 1 ? f1 : (h == 2 ? f2 : f3));
-          if ((long long)(q0 + h) < p.queue_cap)
-            p.queue[q0 + h] = ((unsigned long long)rec << 30) | (unsigned long long)q;
-          else
-            atomicOr(p.err, ERR_IMAP_QUEUE);
-        }
-      }
-    }
+    if (ns == 2) paint_chunk<K, 2>(p, A, b, ns, u0, G, nu, dxs, lane);
+    else if (ns == 3) paint_chunk<K, 3>(p, A, b, ns, u0, G, nu, dxs, lane);
+    else if (ns == 4) paint_chunk<K, 4>(p, A, b, ns, u0, G, nu, dxs, lane);
+    else paint_chunk<K, 0>(p, A, b, ns, u0, G, nu, dxs, lane);
   }
 }
 
