@@ -53,7 +53,7 @@ struct Imap {
   long long npix = 0;
   /* shells (cg_imap_shells): edges, shell of each interval, nsub and
    * dx/nsub per bucket; bucket slots and counts */
-  float *b = nullptr, *dxs = nullptr;
+  float *b = nullptr, *dxs = nullptr, *dxsl = nullptr;
   int *shell_of = nullptr, *nsub = nullptr;
   long long *base = nullptr, *cap = nullptr;
   unsigned long long *cnt = nullptr, *chunk_off = nullptr;
@@ -96,6 +96,7 @@ struct cg_ctx {
    * decisions taken in double (cg_exact_stats) */
   double *d_tabs64 = nullptr, *d_norm64 = nullptr;
   float *d_corner = nullptr;
+  float *d_att = nullptr; /* cg_att_table, for the float-float decisions */
   unsigned long long *d_xstats = nullptr;
   int force_double = 0;
   /* normalisation bins (density.c:1233-1245): z(r_i) of the table radii,
@@ -904,7 +905,7 @@ extern "C" void cg_destroy(cg_ctx *c)
     if (q) cudaFree(q);
   for (float *q : c->d_imap_out)
     if (q) cudaFree(q);
-  void *ptrs[] = {c->d_tabs, c->d_norm, c->d_tabs64, c->d_norm64, c->d_corner, c->d_xstats, c->d_zr, c->d_r2n, c->d_pk, c->d_twN, c->d_twH, c->d_dens, c->d_npot, c->d_disp[0],
+  void *ptrs[] = {c->d_tabs, c->d_norm, c->d_tabs64, c->d_norm64, c->d_corner, c->d_att, c->d_xstats, c->d_zr, c->d_r2n, c->d_pk, c->d_twN, c->d_twH, c->d_dens, c->d_npot, c->d_disp[0],
                   c->d_disp[1], c->d_disp[2], c->d_part, c->d_stats, c->d_s2f, c->d_err, c->d_ncount,
                   c->d_zsum, c->d_bsum, c->d_bacc, c->d_counts, c->d_bsums, c->d_total, c->d_tmpmap, c->d_kmap,
                   c->d_kfac, c->d_kinv, c->d_kir, c->d_ovf_cell, c->d_ovf_cnt, c->d_ovf_n,
@@ -914,7 +915,7 @@ extern "C" void cg_destroy(cg_ctx *c)
     if (p) cudaFree(p);
   for (int i = 0; i < CG_NPOP_MAX; i++) {
     void *q[] = {c->cat[i].pos, c->cat[i].ipix, c->cat[i].src, c->cat[i].cmap, c->im[i].b, c->im[i].dxs,
-                 c->im[i].shell_of, c->im[i].nsub, c->im[i].base, c->im[i].cap, c->im[i].cnt, c->im[i].chunk_off,
+                 c->im[i].dxsl, c->im[i].shell_of, c->im[i].nsub, c->im[i].base, c->im[i].cap, c->im[i].cnt, c->im[i].chunk_off,
                  c->im[i].data, c->im[i].nadd, c->im[i].ctr, c->d_cmap[i], c->cat[i].skw_d, c->cat[i].skw_v};
     for (void *p : q)
       if (p) cudaFree(p);
@@ -1559,6 +1560,7 @@ static int imap_prepare(cg_ctx *c, int ip)
   if (M.nr != nr) {
     if ((rc = dalloc(c, &M.b, (size_t)2 * nr)) || (rc = dalloc(c, &M.shell_of, (size_t)2 * nr + 1)) ||
         (rc = dalloc(c, &M.nsub, (size_t)nr + 2)) || (rc = dalloc(c, &M.dxs, (size_t)nr + 2)) ||
+        (rc = dalloc(c, &M.dxsl, (size_t)nr + 2)) ||
         (rc = dalloc(c, &M.base, (size_t)nbk)) || (rc = dalloc(c, &M.cap, (size_t)nbk)) ||
         (rc = dalloc(c, &M.cnt, (size_t)nbk)) || (rc = dalloc(c, &M.chunk_off, (size_t)nbk + 1)))
       return rc;
@@ -1616,6 +1618,15 @@ static int imap_prepare(cg_ctx *c, int ip)
   CUDA_TRY(c, cudaMemcpyAsync(M.shell_of, shell_of.data(), (nb + 1) * sizeof(int), cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(c, cudaMemcpyAsync(M.nsub, nsub.data(), (nr + 2) * sizeof(int), cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(c, cudaMemcpyAsync(M.dxs, dxs.data(), (nr + 2) * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  std::vector<float> dxsl(nr + 2);
+  for (int i = 0; i < nr + 2; i++) dxsl[i] = (float)(dx / nsub[i] - (double)dxs[i]);
+  CUDA_TRY(c, cudaMemcpyAsync(M.dxsl, dxsl.data(), (nr + 2) * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  std::vector<float> att(2 * (CG_ATT_N + 1));
+  if (!c->d_att) {
+    if ((rc = dalloc(c, &c->d_att, att.size()))) return rc;
+    cg_att_table(att.data());
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_att, att.data(), att.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  }
   CUDA_TRY(c, cudaMemcpyAsync(M.base, base.data(), nbk * sizeof(long long), cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(c, cudaMemcpyAsync(M.cap, capv.data(), nbk * sizeof(long long), cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host staging vectors */
@@ -1672,6 +1683,8 @@ static int imap_launch(cg_ctx *c, int ip)
   a.sh.contig = M.contig;
   a.nsub = M.nsub;
   a.dxs = M.dxs;
+  a.dxsl = M.dxsl;
+  a.att = c->d_att;
   a.r64 = c->d_tabs64;
   a.v164 = c->d_tabs64 + (size_t)2 * na;
   a.ih64 = c->d_tabs64 + (size_t)3 * na;

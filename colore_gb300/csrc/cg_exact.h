@@ -29,6 +29,7 @@
 #define CG_EXACT_H
 
 #include "cg_cell.h"
+#include "cg_ff.h"
 #include "colore_cuda.h"
 
 #if defined(__CUDA_ARCH__)
@@ -820,6 +821,8 @@ typedef struct {
   cg_shells sh;
   const int *nsub;                           /* nsub of shell s + 1, s = -1 .. nr (imap.c:153-174) */
   const float *dxs;                          /* dx / nsub, the same index, rounded once */
+  const float *dxsl;                         /* the rest: dx / nsub - dxs */
+  const float *att;                          /* cg_att_table: atan in quarter turns */
   /* double */
   const double *r64, *tz64, *bz64, *norm64, *v164, *ih64;
   double idr64, r_last64, dx64, p64[3], idx64, fv64, rmin64, rmax64;
@@ -1033,6 +1036,185 @@ CG_HD void cgx_imap_sample(const cg_imap_args *a, int ix, int iy, int iz, int ns
   cgx_cart2sph(x, y, z, &r, &cth, &phi);
   *s = a->sh.shell_of[cgx_interval(&a->sh, X_ADD(r, drr)) + 1];
   if (*s >= 0 && *s < a->sh.nr) *pix = cgx_ang2pix(a->nside, cth, phi);
+}
+
+/* ---- The float-float tier ---------------------------------------------- */
+
+/* Samples whose single-precision margins fail are decided again in
+ * float-float arithmetic (cg_ff.h, about 48 bits) before any double
+ * arithmetic: the same decision structure as cg_pix_checked with bounds of a
+ * few hundred u^2 instead of a few u, so that all but ~1e-9 of them are
+ * settled on the FP32 pipes.  The bounds below are sums of the double-word
+ * operations' relative error bounds (cg_ff.h) along each expression, plus
+ * the reference's own double roundings (2^-53 = u^2 / 32 per operation), each
+ * term rounded up; the margins take them 1.25 times. */
+
+#define CG_ATT_N 256 /* atan table nodes t = i / CG_ATT_N, i = 0 .. CG_ATT_N */
+
+/* atan(i / CG_ATT_N) in quarter turns (times 2/pi) as float pairs, t[2 i] +
+ * t[2 i + 1] within 0.6 u^2 of the value (libm's double atan, one ulp);
+ * host code. */
+#if defined(__CUDACC__)
+static inline __host__ void cg_att_table(float *t)
+#else
+static inline void cg_att_table(float *t)
+#endif
+{
+  for (int i = 0; i <= CG_ATT_N; i++) {
+    const double v = atan((double)i / CG_ATT_N) * 0.63661977236758134308;
+    t[2 * i] = (float)v;
+    t[2 * i + 1] = (float)(v - (double)t[2 * i]);
+  }
+}
+
+/* phi / (pi/2) of (x, y) as the quadrant q and f = tt - q in [0, 1), with the
+ * octant reduction of cg_dir_of: |f - f_exact| <= 17 u^2 (atan of the
+ * nearest table node plus atan((t - t_i) / (1 + t t_i)) by its series to
+ * the fifth power, whose truncation is below 1e-20 for |t - t_i| <= 1/512). */
+CG_HD void cg_ff_quarter(cg_ff x, cg_ff y, const float *att, int *q, cg_ff *f)
+{
+  const cg_ff ax = cg_ff_abs(x), ay = cg_ff_abs(y);
+  const int swap = cg_ff_cmp(ay, ax) > 0;
+  const cg_ff mx = swap ? ay : ax, mn = swap ? ax : ay;
+  cg_ff g = cg_ff_make(0.0f, 0.0f);
+  if (mx.h > 0.0f) {
+    const cg_ff t = cg_ff_div(mn, mx);
+    int i = (int)CG_ADD(CG_MUL(t.h, (float)CG_ATT_N), 0.5f);
+    i = i < 0 ? 0 : (i > CG_ATT_N ? CG_ATT_N : i);
+    const float ti = CG_MUL((float)i, 1.0f / CG_ATT_N); /* exact */
+    const cg_ff num = cg_ff_add(t, cg_ff_make(-ti, 0.0f));
+    const cg_ff den = cg_ff_add(cg_ff_make(1.0f, 0.0f), cg_ff_mulf(t, ti));
+    const cg_ff d = cg_ff_div(num, den);
+    const float d2 = CG_MUL(d.h, d.h);
+    const float corr = CG_MUL(CG_MUL(d.h, d2), CG_FMA(d2, 0.2f, -0.333333343f)); /* -d^3/3 + d^5/5 */
+    const cg_ff at = cg_ff_add(d, cg_ff_make(corr, 0.0f));
+    g = cg_ff_add(cg_ff_make(att[2 * i], att[2 * i + 1]), cg_ff_mul(at, cg_ff_make(0.636619746685028076f, 2.56825530e-08f)));
+  }
+  const int xneg = x.h < 0.0f, yneg = y.h < 0.0f;
+  const int neg = xneg != yneg;
+  int qq = (xneg ? 2 : (yneg ? 4 : 0)) - neg;
+  cg_ff ff = (swap != neg) ? cg_ff_add(cg_ff_make(1.0f, 0.0f), cg_ff_neg(g)) : g;
+  if (cg_ff_cmp(ff, cg_ff_make(1.0f, 0.0f)) >= 0) { /* g' = 0 on the negative side */
+    ff = cg_ff_add(ff, cg_ff_make(-1.0f, 0.0f));
+    qq++;
+  }
+  *q = qq & 3;
+  *f = ff;
+}
+
+CG_HD cg_ff cg_ff_scale(cg_ff x, float p2) { return cg_ff_make(CG_MUL(x.h, p2), CG_MUL(x.l, p2)); } /* p2 a power of 2 */
+
+/* RING pixel at nside (a power of two) of the float-float position
+ * (X, Y, Z), which lies within eP (Euclidean) of the reference's double
+ * position, or -1 when a decision lies within its bound of the boundary:
+ * cg_pix_checked's decisions with float-float values. */
+CG_HD long long cg_pix_ff(cg_ff X, cg_ff Y, cg_ff Z, float eP, int nside, const float *att)
+{
+  const float U = CG_U2;
+  const cg_ff rho2 = cg_ff_add(cg_ff_mul(X, X), cg_ff_mul(Y, Y));
+  const cg_ff r2 = cg_ff_add(rho2, cg_ff_mul(Z, Z));
+  if (!(r2.h > 0.0f)) return -1;
+  const cg_ff R = cg_ff_sqrt(r2);
+  const cg_ff cth = cg_ff_div(Z, R);
+  /* the position's error relative to r moves cos(theta) by at most ein and
+   * phi by at most ein / sin(theta) */
+  const float ein = CG_MUL(1.01f, CG_DIV(eP, R.h));
+  const float sth = CG_DIV(CG_SQRT(rho2.h), R.h);
+  /* cos(theta): rho^2 9u^2, r^2 13, R 10.5, quotient 16 + 10.5; the
+   * reference's cart2sph 0.125 */
+  const float ecth = CG_FMA(1.01f, ein, 28.0f * U);
+  int q;
+  cg_ff f;
+  cg_ff_quarter(X, Y, att, &q, &f);
+  /* f: 17u^2, the reference's atan2, shift and product 0.52 */
+  const float ef = CG_ADD(18.0f * U, CG_DIV(CG_MUL(0.65f, ein), sth));
+  const float ns = (float)nside;
+  const cg_ff ctha = cg_ff_abs(cth);
+  const cg_ff c23 = cg_ff_make(0.666666686534881592f, -1.98682155e-08f); /* the double 2/3 within u^2 */
+  const cg_ff dreg = cg_ff_sub(ctha, c23);
+  const int region_ok = cg_fabsf(dreg.h) > CG_FMA(1.25f, ecth, 3.0f * U);
+  if (dreg.h < 0.0f) {
+    /* 0.5 + f (6u^2), 0.75 cth (1), the sums (9), the reference's temp1 and
+     * temp2 (0.34) */
+    const cg_ff hf = cg_ff_add(cg_ff_make(0.5f, 0.0f), f);
+    const cg_ff c75 = cg_ff_mulf(cth, 0.75f);
+    const cg_ff A = cg_ff_scale(cg_ff_sub(hf, c75), ns), B = cg_ff_scale(cg_ff_add(hf, c75), ns);
+    const float ev = CG_MUL(1.25f, CG_MUL(ns, CG_ADD(CG_FMA(0.75f, ecth, ef), 17.0f * U)));
+    float fa, fb;
+    const float da = cg_ff_floor_dist(A, &fa), db = cg_ff_floor_dist(B, &fb);
+    if (!(region_ok && da > ev && db > ev)) return -1;
+    const int jp = nside * q + cg_fint(fa), jm = nside * q + cg_fint(fb);
+    const int ir = nside + 1 + jp - jm;
+    const int kshift = 1 - (ir & 1);
+    int ip = (jp + jm - nside + kshift + 1) >> 1;
+    const int m = 4 * nside;
+    if (ip >= m) ip -= m;
+    return (long long)(nside * (nside - 1) * 2 + (ir - 1) * 4 * nside + ip);
+  }
+  if (!region_ok || !(sth > 1e-20f)) return -1;
+  /* 1 - |cth| = rho^2 / (R (R + |Z|)): 56u^2 relative; the reference's
+   * 1 - |cth| is within 0.125 u^2 of the exact value; the position moves it
+   * by at most sin(theta) ein */
+  const cg_ff u1 = cg_ff_div(rho2, cg_ff_mul(R, cg_ff_add(R, cg_ff_abs(Z))));
+  if (!(u1.h > 0.0f)) return -1;
+  const float eu1 = CG_FMA(60.0f * U, u1.h, CG_FMA(1.01f, CG_MUL(sth, ein), 0.125f * U));
+  const cg_ff tmp = cg_ff_scale(cg_ff_sqrt(cg_ff_mulf(u1, 3.0f)), ns);
+  /* 3 (1 - |cth|) and its root: 6u^2, the reference's 0.06, and half the
+   * relative error of 1 - |cth| */
+  const float etmp = CG_MUL(tmp.h, CG_ADD(7.0f * U, CG_DIV(eu1, CG_MUL(2.0f, u1.h))));
+  const cg_ff omf = cg_ff_add(cg_ff_make(1.0f, 0.0f), cg_ff_neg(f));
+  const cg_ff p1 = cg_ff_mul(f, tmp), p2 = cg_ff_mul(omf, tmp);
+  const float e1 = CG_MUL(1.25f, CG_FMA(tmp.h, ef, CG_FMA(f.h, etmp, CG_MUL(6.0f * U, p1.h))));
+  const float e2 = CG_MUL(1.25f, CG_FMA(tmp.h, CG_ADD(ef, 4.0f * U), CG_FMA(omf.h, etmp, CG_MUL(6.0f * U, p2.h))));
+  float f1, f2;
+  const float d1 = cg_ff_floor_dist(p1, &f1), d2 = cg_ff_floor_dist(p2, &f2);
+  if (!(d1 > e1 && d2 > e2)) return -1;
+  const int jp = cg_fint(f1), jm = cg_fint(f2);
+  const int ir = jp + jm + 1;
+  /* f ir (2u^2) and the reference's tt ir (0.125 u^2 ir) */
+  const cg_ff p3 = cg_ff_mulf(f, (float)ir);
+  const float e3 = CG_MUL(1.25f, CG_FMA((float)ir, CG_ADD(ef, 0.2f * U), CG_MUL(3.0f * U, p3.h)));
+  float f3;
+  const float d3 = cg_ff_floor_dist(p3, &f3);
+  if (!(d3 > e3)) return -1;
+  int ip = q * ir + cg_fint(f3);
+  const int m = 4 * ir;
+  if (ip >= m) ip -= m;
+  if (cth.h > 0.0f) return (long long)(2 * ir * (ir - 1) + ip);
+  return (long long)(12 * nside * nside - 2 * ir * (ir + 1) + ip);
+}
+
+/* A sample of cell c whose single-precision decision was left open, again:
+ * the shell as cg_imap_decide takes it, then the RING pixel in float-float
+ * from the double-float corner and sub-cell step.  1 with *s (maybe -1 or
+ * nr: not painted) and *pix when the double arithmetic certainly agrees, 0
+ * when only double can decide. */
+CG_HD int cg_imap_decide_ff(const cg_imap_args *a, const cg_imap_cell *c, int ix, int iy, int iz, int sx, int sy,
+                            int sz, int *s, long long *pix)
+{
+  const int k = c->j + 1;
+  const float dxs = a->dxs[k];
+  const float x = cg_imap_coord(a->xc, a->xl, ix, sx, dxs);
+  const float y = cg_imap_coord(a->yc, a->yl, iy, sy, dxs);
+  const float z = cg_imap_coord(a->zc, a->zl, iz, sz, dxs);
+  const float r2 = CG_FMA(z, z, CG_FMA(x, x, CG_MUL(y, y)));
+  const float rinv = cg_rsqrt_fast(r2);
+  const float ein = CG_MUL(1.8f * CG_E24, CG_FMA(2.0f * a->dx, rinv, 1.0f));
+  if (!cg_imap_shell_checked(a, c, CG_MUL(r2, rinv), ein, s)) return 0;
+  if (*s < 0 || *s >= a->sh.nr) return 1;
+  /* corner pairs within u^2 of the double corners, the step within u^2 of
+   * dx / nsub; times (s + 1/2) 2u^2, the sum 4u^2 of the result, the
+   * reference's two roundings: per axis u^2 (5.1 |x| + 5.1 dx), taken
+   * Euclidean as 6 u^2 (r + 2 dx) and doubled */
+  const cg_ff dd = cg_ff_make(dxs, a->dxsl[k]);
+  const cg_ff X = cg_ff_add(cg_ff_make(a->xc[ix], a->xl[ix]), cg_ff_mulf(dd, CG_ADD((float)sx, 0.5f)));
+  const cg_ff Y = cg_ff_add(cg_ff_make(a->yc[iy], a->yl[iy]), cg_ff_mulf(dd, CG_ADD((float)sy, 0.5f)));
+  const cg_ff Z = cg_ff_add(cg_ff_make(a->zc[iz], a->zl[iz]), cg_ff_mulf(dd, CG_ADD((float)sz, 0.5f)));
+  const float eP = CG_MUL(12.0f * CG_U2, CG_FMA(r2, rinv, 2.0f * a->dx));
+  const long long p = cg_pix_ff(X, Y, Z, eP, a->nside, a->att);
+  if (p < 0) return 0;
+  *pix = p;
+  return 1;
 }
 
 /* Host set-up of a species' shells (imap_preproc, imap.c:105-133, and the

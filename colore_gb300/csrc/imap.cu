@@ -46,7 +46,7 @@ using namespace cg;
 
 constexpr int IW = 4;     /* warps per block                     */
 constexpr int ROWS = 2;   /* rows per fetch in k_imap_list        */
-constexpr int CHS = 2048; /* samples per painting chunk           */
+constexpr int CHS = 4096; /* samples per painting chunk           */
 constexpr unsigned FULL = 0xffffffffu;
 constexpr unsigned F_DOUBLE = 16u; /* flags: mode (2 bits), delta + 1 (2 bits), double */
 
@@ -600,8 +600,10 @@ __global__ void __launch_bounds__(IW * 32, 8) k_imap_paint(cg_imap_params p)
   }
 }
 
-/* The queued samples in double: the cell's radial shift (imap.c:196-198)
- * and the sample's shell and pixel (imap.c:210-231). */
+/* The queued samples: first again in float-float (cg_imap_decide_ff), which
+ * settles all but ~1e-9 of those the float margins left open; the rest, and
+ * every sample of a cell listed in double, in double: the cell's radial
+ * shift (imap.c:196-198) and the sample's shell and pixel (imap.c:210-231). */
 __global__ void __launch_bounds__(256) k_imap_double(const float *__restrict__ phi, cg_imap_params p)
 {
   extern __shared__ __align__(16) unsigned char sraw[];
@@ -610,50 +612,65 @@ __global__ void __launch_bounds__(256) k_imap_double(const float *__restrict__ p
   const cg_imap_args A = args_with(p, sh);
   const unsigned long long nq0 = p.ctr[4];
   const long long nq = (long long)nq0 < p.queue_cap ? (long long)nq0 : p.queue_cap;
-  if (blockIdx.x == 0 && threadIdx.x == 0 && nq > 0) atomicAdd(p.xstats + 3, (unsigned long long)nq);
   /* warp-uniform steps over the queue: consecutive entries mostly share a
    * record (a lane queues up to four samples of its unit together), so the
-   * first lane of each run of one record takes the cell's double quantities
-   * and hands them to the rest of the run */
+   * first lane of each run of one record that needs double takes the cell's
+   * double quantities and hands them to the rest of the run */
   const int lane = threadIdx.x & 31;
   const long long stride = (long long)gridDim.x * blockDim.x;
+  unsigned long long ndbl = 0;
   for (long long kb = (long long)blockIdx.x * blockDim.x + threadIdx.x - lane; kb < nq; kb += stride) {
     const long long k = kb + lane;
     const bool valid = k < nq;
     const unsigned long long e = valid ? p.queue[k] : ~0ull;
     const long long rec = (long long)(e >> 30);
     const int q = (int)(e & ((1ull << 30) - 1));
-    const long long prev = __shfl_up_sync(FULL, rec, 1);
-    const bool lead = valid && (lane == 0 || prev != rec);
-    const unsigned lm = __ballot_sync(FULL, lead);
-    const unsigned le = lm & (lane == 31 ? FULL : ((2u << lane) - 1u));
-    const int src = valid ? 31 - __clz(le) : lane;
-    int lo = 0, ix = 0, iy = 0, iz = 0;
-    float temp = 0.0f;
-    double drr = 0;
-    if (lead) {
-      /* the record's bucket: last b with base[b] <= rec */
+    /* the record's bucket: last b with base[b] <= rec */
+    int lo = 0, ix = 0, iy = 0, iz = 0, dbl = 1;
+    cg_imap_cell c;
+    c.temp = 0.0f;
+    if (valid) {
       int hi = p.nbk - 1;
       while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
         if (p.base[mid] <= rec) lo = mid;
         else hi = mid - 1;
       }
-      int dbl;
-      const cg_imap_cell c = unpack(p.recs[rec], lo - 1, &ix, &iy, &iz, &dbl);
-      temp = c.temp;
+      c = unpack(p.recs[rec], lo - 1, &ix, &iy, &iz, &dbl);
+    }
+    bool need = valid;
+    if (valid && !dbl && !p.force_double) {
+      const int ns = sh.nsub[lo];
+      int s = -1, sx, sy, sz;
+      long long pix = 0;
+      sub_of(q, ns, sh.invns[lo], &sx, &sy, &sz);
+      if (cg_imap_decide_ff(&A, &c, ix, iy, iz, sx, sy, sz, &s, &pix)) {
+        need = false;
+        if (s >= 0 && s < p.nr) {
+          const long long key = (long long)s * p.npix + pix;
+          atomicAdd(&p.data[key], c.temp);
+          atomicAdd(&p.nadd[key], 1);
+        }
+      }
+    }
+    const unsigned nm = __ballot_sync(FULL, need);
+    if (!nm) continue;
+    ndbl += lane == 0 ? (unsigned long long)__popc(nm) : 0ull;
+    const long long prev = __shfl_up_sync(FULL, rec, 1);
+    const bool pneed = __shfl_up_sync(FULL, (int)need, 1) != 0;
+    const bool lead = need && (lane == 0 || !pneed || prev != rec);
+    const unsigned lm = __ballot_sync(FULL, lead);
+    const unsigned le = lm & (lane == 31 ? FULL : ((2u << lane) - 1u));
+    const int src = need ? 31 - __clz(le) : lane;
+    double drr = 0;
+    if (lead) {
       float v[3];
       grad_phi(phi, ix, iy, iz, p.box.N, v);
       int j;
       cgx_imap_cell(&A, ix, iy, iz, v, &j, &drr);
     }
-    lo = __shfl_sync(FULL, lo, src);
-    ix = __shfl_sync(FULL, ix, src);
-    iy = __shfl_sync(FULL, iy, src);
-    iz = __shfl_sync(FULL, iz, src);
-    temp = __shfl_sync(FULL, temp, src);
     drr = __shfl_sync(FULL, drr, src);
-    if (!valid) continue;
+    if (!need) continue;
     const int ns = sh.nsub[lo];
     int s = -1, sx, sy, sz;
     sub_of(q, ns, sh.invns[lo], &sx, &sy, &sz);
@@ -661,10 +678,11 @@ __global__ void __launch_bounds__(256) k_imap_double(const float *__restrict__ p
     cgx_imap_sample(&A, ix, iy, iz, ns, drr, sx, sy, sz, &s, &pix);
     if (s >= 0 && s < p.nr) {
       const long long key = (long long)s * p.npix + pix;
-      atomicAdd(&p.data[key], temp);
+      atomicAdd(&p.data[key], c.temp);
       atomicAdd(&p.nadd[key], 1);
     }
   }
+  if (ndbl) atomicAdd(p.xstats + 3, ndbl);
 }
 
 template <typename K>

@@ -65,6 +65,20 @@ void or_pix_checked(long nside, const float *xyz, long n, float ein, long long *
   }
 }
 
+/* RING pixels of float-float positions (6 floats each: x, its rest, y, ...)
+ * by the float-float tier (cg_pix_ff; -1 where it defers to double), each
+ * within eP[i] of the double position. */
+void or_pix_ff(long nside, const float *p, const float *eP, long n, long long *pix)
+{
+  float att[2 * (CG_ATT_N + 1)];
+  cg_att_table(att);
+  for (long i = 0; i < n; i++) {
+    const float *q = p + 6 * i;
+    pix[i] = cg_pix_ff(cg_ff_make(q[0], q[1]), cg_ff_make(q[2], q[3]), cg_ff_make(q[4], q[5]), eP[i], (int)nside,
+                       att);
+  }
+}
+
 /* The same decision by the double restatement shared with the kernels
  * (cgx_cart2sph + cgx_ang2pix). */
 void or_pix_cgx(long nside, const double *xyz, long n, long long *pix)

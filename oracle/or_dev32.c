@@ -404,8 +404,9 @@ static int cmp_float_idx(const void *a, const void *b)
  * builds them (cg_imap_args); the buffers are owned by *B. */
 typedef struct {
   cg_imap_args a;
-  float *corner, *r0f, *rff, *b, *dxs;
+  float *corner, *r0f, *rff, *b, *dxs, *dxsl;
   int *shell_of, *nsub;
+  float att[2 * (CG_ATT_N + 1)];
 } ImapArgs;
 
 static void imap_args(ImapArgs *B, const cg_config *cfg, const S32 *s, int ipop, const float *norm32,
@@ -444,6 +445,11 @@ static void imap_args(ImapArgs *B, const cg_config *cfg, const S32 *s, int ipop,
   a->sh.contig = cg_imap_contig(B->r0f, B->rff, nr, nb);
   a->nsub = B->nsub;
   a->dxs = B->dxs;
+  B->dxsl = malloc((nr + 2) * sizeof(float));
+  for (int i = 0; i < nr + 2; i++) B->dxsl[i] = (float)(dx / B->nsub[i] - (double)B->dxs[i]);
+  a->dxsl = B->dxsl;
+  cg_att_table(B->att);
+  a->att = B->att;
   a->r = s->r;
   a->tz = s->tz[ipop].f;
   a->bz = s->bzi[ipop].f;
@@ -485,11 +491,13 @@ static void imap_args_free(ImapArgs *B)
   free(B->shell_of);
   free(B->nsub);
   free(B->dxs);
+  free(B->dxsl);
 }
 
 /* The intensity map of species ipop as the GPU paints it: cells and samples
- * decided in single precision where the margins hold and in double
- * otherwise (cg_exact.h); brightness summed in cell order in float.  stats:
+ * decided in single precision where the margins hold, then in float-float,
+ * and in double otherwise (cg_exact.h); brightness summed in cell order in
+ * float.  stats:
  * [0] cells and [1] samples decided in double, [2] samples drawn (may be
  * NULL).  norm32 / norm64: the normalisation table with its two edges. */
 int or_imap32(const cg_config *cfg, int ipop, const float *dens, const float *npot, const float *norm32,
@@ -542,7 +550,8 @@ int or_imap32(const cg_config *cfg, int ipop, const float *dens, const float *np
             for (int sx = 0; sx < ns; sx++) {
               int sh = -1;
               long long pix = 0;
-              if (dbl || !cg_imap_sample_checked(a, ix, iy, iz, &c, ns, sx, sy, sz, &sh, &pix)) {
+              if (dbl || (!cg_imap_sample_checked(a, ix, iy, iz, &c, ns, sx, sy, sz, &sh, &pix) &&
+                          !cg_imap_decide_ff(a, &c, ix, iy, iz, sx, sy, sz, &sh, &pix))) {
                 if (!dbl) {
                   int j2;
                   cgx_imap_cell(a, ix, iy, iz, v, &j2, &drr64);

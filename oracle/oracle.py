@@ -51,13 +51,13 @@ def lib():
             "or_ring2nest": [C.c_long, vp, vp, C.c_long], "or_pix2vec_nest": [C.c_long, vp, vp, C.c_long],
             "or_shell_index": [vp, vp, i, vp, vp, vp, C.c_long],
             "or_pix_checked": [C.c_long, vp, C.c_long, f, vp], "or_pix_cgx": [C.c_long, vp, C.c_long, vp],
-            "or_pix64": [C.c_long, vp, C.c_long, vp],
+            "or_pix64": [C.c_long, vp, C.c_long, vp], "or_pix_ff": [C.c_long, vp, vp, C.c_long, vp],
             "or_sht_legendre": [i, i, i, vp, vp, vp, d, vp],
             "or_src_offset_checked": [C.c_long, vp, d, vp, vp, vp, vp],
             "or_ptrs_checked": [C.c_long, vp, vp, vp, vp, C.c_uint32, C.c_uint32, vp, vp],
         }
         void = ("or_philox", "or_poisson", "or_ang2pix", "or_nest2ring", "or_ring2nest", "or_pix2vec_nest",
-                "or_shell_index", "or_pix_checked", "or_pix_cgx", "or_pix64", "or_src_offset_checked",
+                "or_shell_index", "or_pix_checked", "or_pix_cgx", "or_pix64", "or_pix_ff", "or_src_offset_checked",
                 "or_ptrs_checked")
         for k, a in sig.items():
             fn = getattr(L, k)
@@ -499,6 +499,20 @@ def pix_checked(nside, xyz32, ein=0.0):
     a = np.ascontiguousarray(xyz32, np.float32)
     out = np.empty(len(a), np.int64)
     lib().or_pix_checked(nside, P(a), len(a), float(ein), P(out))
+    return out
+
+
+def pix_ff(nside, xyz, rel=2.0 ** -47):
+    """RING pixels of double positions by the float-float tier
+    (cg_pix_ff, -1: deferred to double): each coordinate split into a float
+    pair, declared within rel |p| of the double position."""
+    a = np.ascontiguousarray(xyz, np.float64)
+    h = a.astype(np.float32)
+    lo = (a - h.astype(np.float64)).astype(np.float32)
+    q = np.ascontiguousarray(np.stack([h, lo], 2).reshape(len(a), 6), np.float32)
+    eP = (rel * np.sqrt((a * a).sum(1))).astype(np.float32)
+    out = np.empty(len(a), np.int64)
+    lib().or_pix_ff(nside, P(q), P(eP), len(a), P(out))
     return out
 
 

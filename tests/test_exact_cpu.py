@@ -82,6 +82,49 @@ def test_pixel_margins_never_disagree_with_double(ns):
         assert np.array_equal(fast[ok], ref[ok]), (ns, kind, "perturbed")
 
 
+def _edge_points_tight(ns, n, seed):
+    """Directions within 1e-15..1e-8 (in quarter turns) of equatorial RING
+    edge lines: far inside the single-precision margins."""
+    r = np.random.default_rng(seed)
+    z = r.uniform(-2 / 3, 2 / 3, n)
+    k = r.integers(0, 4 * ns + 2, n)
+    tt = (k / ns - 0.5 - r.choice([-1, 1], n) * 0.75 * z) % 4
+    tt = (tt + r.normal(size=n) * 10 ** r.uniform(-15, -8, n)) % 4
+    return _dirs(z, tt) * r.uniform(10, 4000, (n, 1))
+
+
+@pytest.mark.parametrize("ns", [1, 16, 512, 1024, 4096])
+def test_float_float_pixels_never_disagree_with_double(ns):
+    """The float-float tier (cg_pix_ff) that the samples left open by the
+    single-precision margins take before double: every pixel it keeps is the
+    double one, at random, next to every kind of edge, and within 1e-15 of
+    equatorial edges; it leaves only the poles and what lies within ~1e-12
+    of an edge."""
+    import oracle as orc
+    for kind in ("random", "edges", "tight"):
+        if kind == "random":
+            v = rng.normal(size=(100000, 3)) * rng.uniform(10, 4000, (100000, 1))
+        elif kind == "edges":
+            v = _edge_points(ns, 20000) * rng.uniform(10, 4000, (100000, 1))
+        else:
+            v = _edge_points_tight(ns, 100000, ns)
+        ref = orc.pix64(ns, v, shared=True)
+        ff = orc.pix_ff(ns, v)
+        ok = ff >= 0
+        assert np.array_equal(ff[ok], ref[ok]), (ns, kind, int((ff[ok] != ref[ok]).sum()))
+        r = np.sqrt((v * v).sum(1))
+        pole = np.hypot(v[:, 0], v[:, 1]) < 1e-6 * r
+        if kind == "random":
+            assert ok[~pole].all(), (ns, kind, int((~ok[~pole]).sum()))
+        elif kind == "edges":
+            # offsets 1e-9..1e-4 times a normal draw: a few land within 1e-12
+            assert (~ok[~pole]).mean() < 1e-3, (ns, kind, int((~ok[~pole]).sum()))
+        else:
+            # offsets log-uniform over 1e-15..1e-8: all beyond ~1e-12 decided
+            assert ok.mean() > 0.55, ok.mean()
+            assert (orc.pix_checked(ns, v.astype(np.float32)) < 0).mean() > 0.99
+
+
 def _spec(bias_model):
     return dict(n_grid=64, z_min=0.05, z_max=0.6, r_smooth=2.0, seed=11 + bias_model, dens_type=0,
                 bias_model=bias_model,
@@ -157,8 +200,11 @@ def test_imap_hits_equal_double(tmp_path, case):
     assert nadd64.sum() > 10 ** 6
     assert np.array_equal(nadd32, nadd64), int((nadd32 != nadd64).sum())
     np.testing.assert_allclose(data32, data64, rtol=2e-6, atol=1e-12)
-    # the double path is the exception
-    assert stats[1] < 5e-3 * stats[2], stats
+    # the double path is the exception: the float margins leave ~2e-3 of
+    # the samples open, the float-float tier settles their pixels, and what
+    # remains are shells within the float radial shift's bound of an edge
+    print("imap %s: %d of %d samples in double, %d cells" % (case, stats[1], stats[2], stats[0]))
+    assert stats[1] < 1e-4 * stats[2], stats
 
 
 # (128, 3.0): dx = 3 2^-7 and the observer at 1.5, so every sum is exact in
