@@ -290,24 +290,20 @@ __global__ void __launch_bounds__(IW * 32) k_imap_list(const float *__restrict__
             }
           }
         }
-        /* append to the buckets: one atomic per bucket present in the warp */
+        /* append to the buckets: one atomic per bucket present in the warp,
+         * issued together by each bucket's first lane (one round trip) */
         bool over = false;
         long long slot = 0;
-        unsigned m = __ballot_sync(FULL, want);
         const int bk = want ? c.j + 1 : -1;
-        while (m) {
-          const int leader = __ffs(m) - 1;
-          const int bb = __shfl_sync(FULL, bk, leader);
-          const unsigned same = __ballot_sync(FULL, want && bk == bb);
-          unsigned long long old = 0;
-          if (lane == leader) old = atomicAdd(&p.cnt[bb], (unsigned long long)__popc(same));
-          old = __shfl_sync(FULL, old, leader);
-          if (same & (1u << lane)) {
-            const long long k = (long long)old + __popc(same & ((1u << lane) - 1u));
-            if (k < p.cap[bb]) slot = p.base[bb] + k;
-            else over = true;
-          }
-          m &= ~same;
+        const unsigned same = __match_any_sync(FULL, bk);
+        const int leader = __ffs(same) - 1;
+        unsigned long long old = 0;
+        if (want && lane == leader) old = atomicAdd(&p.cnt[bk], (unsigned long long)__popc(same));
+        old = __shfl_sync(FULL, old, leader);
+        if (want) {
+          const long long k = (long long)old + __popc(same & ((1u << lane) - 1u));
+          if (k < p.cap[bk]) slot = p.base[bk] + k;
+          else over = true;
         }
         if (want && !over)
           p.recs[slot] = pack(ix, iy, iz, c, (unsigned)c.mode | ((unsigned)(c.delta + 1) << 2) | (dbl ? F_DOUBLE : 0u));
