@@ -47,6 +47,7 @@ using namespace cg;
 constexpr int IW = 4;     /* warps per block                     */
 constexpr int ROWS = 2;   /* rows per fetch in k_imap_list        */
 constexpr int CHS = 4096; /* samples per painting chunk           */
+constexpr int QB = 256;   /* queue entries staged per painting warp */
 constexpr unsigned FULL = 0xffffffffu;
 constexpr unsigned F_DOUBLE = 16u; /* flags: mode (2 bits), delta + 1 (2 bits), double */
 
@@ -78,6 +79,10 @@ __device__ __forceinline__ Sh shells_at(const cg_imap_params &p, unsigned char *
   s.chunk_off = reinterpret_cast<unsigned long long *>(raw + shell_smem(nr, p.nbk, false));
   return s;
 }
+
+/* The painting warps' queue stages follow the tables. */
+__host__ __device__ __forceinline__ size_t paint_stage_off(int nr, int nbk) { return (shell_smem(nr, nbk, true) + 15) & ~(size_t)15; }
+__host__ __device__ __forceinline__ size_t paint_smem(int nr, int nbk) { return paint_stage_off(nr, nbk) + (size_t)IW * QB * 8; }
 
 __device__ __forceinline__ Sh load_shells(const cg_imap_params &p, unsigned char *raw, bool chunks)
 {
@@ -387,6 +392,28 @@ __device__ __noinline__ void queue_one(const cg_imap_params &p, long long rec, i
   else atomicOr(p.err, ERR_IMAP_QUEUE);
 }
 
+/* This warp's queue stage in the painting kernel's shared memory. */
+__device__ __forceinline__ unsigned long long *stage_of(const cg_imap_params &p)
+{
+  extern __shared__ __align__(16) unsigned char sraw[];
+  return reinterpret_cast<unsigned long long *>(sraw + paint_stage_off(p.nr, p.nbk)) + (size_t)(threadIdx.x >> 5) * QB;
+}
+
+/* The warp's staged queue entries (qn of them, in shared memory) to the
+ * double queue: one atomic per QB - 128 or more entries. */
+__device__ __forceinline__ void queue_flush(const cg_imap_params &p, const unsigned long long *qb, int qn, int lane)
+{
+  __syncwarp();
+  unsigned long long q0 = 0;
+  if (lane == 0) q0 = atomicAdd(&p.ctr[4], (unsigned long long)qn);
+  q0 = __shfl_sync(FULL, q0, 0);
+  for (int i = lane; i < qn; i += 32) {
+    if ((long long)(q0 + i) < p.queue_cap) p.queue[q0 + i] = qb[i];
+    else atomicOr(p.err, ERR_IMAP_QUEUE);
+  }
+  __syncwarp();
+}
+
 /* Add a run of cnt samples of brightness temp to key k. */
 template <typename K>
 __device__ __forceinline__ void flush(const cg_imap_params &p, K k, unsigned cnt, float temp)
@@ -438,11 +465,12 @@ __device__ __forceinline__ void paint_sample(const cg_imap_params &p, const cg_i
  * per cell and the x loop unrolled).  Each lane walks one unit (a cell, a
  * slab or a line) sample by sample with its row coordinates and the cell's
  * fields held in registers.  Every lane of a warp runs the same sample loop,
- * so the samples that only double can decide are queued with one atomic per
- * warp and unit. */
+ * so the samples that only double can decide are staged per warp in shared
+ * memory (qb, qn entries) and queued in batches. */
 template <typename K, int NS>
 __device__ __forceinline__ void paint_chunk(const cg_imap_params &p, const cg_imap_args &A, int b, int ns,
-                                            unsigned long long u0, int G, unsigned long long nu, float dxs, int lane)
+                                            unsigned long long u0, int G, unsigned long long nu, float dxs, int lane,
+                                            int &qn)
 {
   const int U = (int)units_per_cell(ns);
   /* the chunk's first unit as (record, unit within it); later units are
@@ -533,7 +561,8 @@ __device__ __forceinline__ void paint_chunk(const cg_imap_params &p, const cg_im
     }
     flush<K>(p, k0, n0, c.temp);
     flush<K>(p, k1, n1, c.temp);
-    /* the held samples: one queue atomic per warp (most units hold none) */
+    /* the held samples (most units hold none) to the warp's stage; at most
+     * 128 per group, so a stage past QB - 128 entries is queued first */
     const int held = nf < 4 ? nf : 4;
     if (__any_sync(FULL, held > 0)) {
       int incl = held;
@@ -543,16 +572,15 @@ __device__ __forceinline__ void paint_chunk(const cg_imap_params &p, const cg_im
         if (lane >= o) incl += t;
       }
       const int tot = __shfl_sync(FULL, incl, 31);
-      unsigned long long q0 = 0;
-      if (lane == 31) q0 = atomicAdd(&p.ctr[4], (unsigned long long)tot);
-      q0 = __shfl_sync(FULL, q0, 31) + (unsigned long long)(incl - held);
-      for (int h = 0; h < held; h++) {
-        const int q = h == 0 ? f0 : (h == 1 ? f1 : (h == 2 ? f2 : f3));
-        if ((long long)(q0 + h) < p.queue_cap)
-          p.queue[q0 + h] = ((unsigned long long)rec << 30) | (unsigned long long)q;
-        else
-          atomicOr(p.err, ERR_IMAP_QUEUE);
+      unsigned long long *qb = stage_of(p);
+      if (qn + tot > QB) {
+        queue_flush(p, qb, qn, lane);
+        qn = 0;
       }
+      const int o = qn + incl - held;
+      for (int h = 0; h < held; h++)
+        qb[o + h] = ((unsigned long long)rec << 30) | (unsigned long long)(h == 0 ? f0 : (h == 1 ? f1 : (h == 2 ? f2 : f3)));
+      qn += tot;
     }
   }
 }
@@ -569,6 +597,7 @@ __global__ void __launch_bounds__(IW * 32, 8) k_imap_paint(cg_imap_params p)
   const cg_imap_args A = args_with(p, sh);
   const int lane = threadIdx.x & 31;
   const unsigned long long total = sh.chunk_off[p.nbk];
+  int qn = 0;
   for (;;) {
     unsigned long long ck = 0;
     if (lane == 0) ck = atomicAdd(&p.ctr[0], 1ull);
@@ -589,11 +618,12 @@ __global__ void __launch_bounds__(IW * 32, 8) k_imap_paint(cg_imap_params p)
     const int G = groups_per_chunk(ns);
     const float dxs = sh.dxs[b];
     const unsigned long long u0 = (ck - sh.chunk_off[b]) * 32ull * (unsigned long long)G;
-    if (ns == 2) paint_chunk<K, 2>(p, A, b, ns, u0, G, nu, dxs, lane);
-    else if (ns == 3) paint_chunk<K, 3>(p, A, b, ns, u0, G, nu, dxs, lane);
-    else if (ns == 4) paint_chunk<K, 4>(p, A, b, ns, u0, G, nu, dxs, lane);
-    else paint_chunk<K, 0>(p, A, b, ns, u0, G, nu, dxs, lane);
+    if (ns == 2) paint_chunk<K, 2>(p, A, b, ns, u0, G, nu, dxs, lane, qn);
+    else if (ns == 3) paint_chunk<K, 3>(p, A, b, ns, u0, G, nu, dxs, lane, qn);
+    else if (ns == 4) paint_chunk<K, 4>(p, A, b, ns, u0, G, nu, dxs, lane, qn);
+    else paint_chunk<K, 0>(p, A, b, ns, u0, G, nu, dxs, lane, qn);
   }
+  if (qn) queue_flush(p, stage_of(p), qn, lane);
 }
 
 /* The queued samples: first again in float-float (cg_imap_decide_ff), which
@@ -687,7 +717,7 @@ cudaError_t launch(cudaStream_t s, const float *dens, const float *phi, const cg
   cudaError_t e = cudaMemsetAsync(p->ctr, 0, 5 * sizeof(unsigned long long), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(p->cnt, 0, (size_t)p->nbk * sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
-  const size_t sm_list = shell_smem(p->nr, p->nbk, false), sm_paint = shell_smem(p->nr, p->nbk, true);
+  const size_t sm_list = shell_smem(p->nr, p->nbk, false), sm_paint = paint_smem(p->nr, p->nbk);
   if ((e = cudaFuncSetAttribute(k_imap_list<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_list)) ||
       (e = cudaFuncSetAttribute(k_imap_paint<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_paint)) ||
       (e = cudaFuncSetAttribute(k_imap_double, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_list)))
@@ -728,7 +758,7 @@ cudaError_t cg_pix_checked_dev(cudaStream_t s, int nside, const float *xyz, long
   return cudaGetLastError();
 }
 
-size_t cg_imap_shell_smem(int nr, int nbk) { return shell_smem(nr, nbk, true); }
+size_t cg_imap_shell_smem(int nr, int nbk) { return paint_smem(nr, nbk); }
 
 cudaError_t cg_imap_paint(cudaStream_t s, const float *dens, const float *phi, const cg_imap_params *p, int nsm)
 {
