@@ -83,6 +83,8 @@ __device__ __forceinline__ Sh shells_at(const cg_imap_params &p, unsigned char *
 /* The painting warps' queue stages follow the tables. */
 __host__ __device__ __forceinline__ size_t paint_stage_off(int nr, int nbk) { return (shell_smem(nr, nbk, true) + 15) & ~(size_t)15; }
 __host__ __device__ __forceinline__ size_t paint_smem(int nr, int nbk) { return paint_stage_off(nr, nbk) + (size_t)IW * QB * 8; }
+/* The double pass's per-warp gathers (64 entries) follow its tables. */
+__host__ __device__ __forceinline__ size_t double_stage_off(int nr, int nbk) { return (shell_smem(nr, nbk, false) + 15) & ~(size_t)15; }
 
 __device__ __forceinline__ Sh load_shells(const cg_imap_params &p, unsigned char *raw, bool chunks)
 {
@@ -626,88 +628,127 @@ __global__ void __launch_bounds__(IW * 32, 8) k_imap_paint(cg_imap_params p)
   if (qn) queue_flush(p, stage_of(p), qn, lane);
 }
 
+/* The samples of one warp batch (n <= 32 entries of the queue's form) in
+ * double: the cell's radial shift (imap.c:196-198), taken by the first lane
+ * of each run of one record and handed to the rest of the run, then the
+ * sample's shell and pixel (imap.c:210-231). */
+__device__ __forceinline__ void double_batch(const float *__restrict__ phi, const cg_imap_params &p,
+                                             const cg_imap_args &A, const Sh &sh, unsigned long long e, bool valid,
+                                             int lane)
+{
+  const long long rec = (long long)(e >> 30);
+  const int q = (int)(e & ((1ull << 30) - 1));
+  const long long prev = __shfl_up_sync(FULL, rec, 1);
+  const bool lead = valid && (lane == 0 || prev != rec);
+  const unsigned lm = __ballot_sync(FULL, lead);
+  const unsigned le = lm & (lane == 31 ? FULL : ((2u << lane) - 1u));
+  const int src = valid ? 31 - __clz(le) : lane;
+  int lo = 0, ix = 0, iy = 0, iz = 0;
+  float temp = 0.0f;
+  double drr = 0;
+  if (lead) {
+    /* the record's bucket: last b with base[b] <= rec */
+    int hi = p.nbk - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (p.base[mid] <= rec) lo = mid;
+      else hi = mid - 1;
+    }
+    int dbl;
+    const cg_imap_cell c = unpack(p.recs[rec], lo - 1, &ix, &iy, &iz, &dbl);
+    temp = c.temp;
+    float v[3];
+    grad_phi(phi, ix, iy, iz, p.box.N, v);
+    int j;
+    cgx_imap_cell(&A, ix, iy, iz, v, &j, &drr);
+  }
+  lo = __shfl_sync(FULL, lo, src);
+  ix = __shfl_sync(FULL, ix, src);
+  iy = __shfl_sync(FULL, iy, src);
+  iz = __shfl_sync(FULL, iz, src);
+  temp = __shfl_sync(FULL, temp, src);
+  drr = __shfl_sync(FULL, drr, src);
+  if (!valid) return;
+  const int ns = sh.nsub[lo];
+  int s = -1, sx, sy, sz;
+  sub_of(q, ns, sh.invns[lo], &sx, &sy, &sz);
+  long long pix = 0;
+  cgx_imap_sample(&A, ix, iy, iz, ns, drr, sx, sy, sz, &s, &pix);
+  if (s >= 0 && s < p.nr) {
+    const long long key = (long long)s * p.npix + pix;
+    atomicAdd(&p.data[key], temp);
+    atomicAdd(&p.nadd[key], 1);
+  }
+}
+
+constexpr int DB_WARPS = 8; /* warps per block of k_imap_double */
+
 /* The queued samples: first again in float-float (cg_imap_decide_ff), which
- * settles all but ~1e-9 of those the float margins left open; the rest, and
- * every sample of a cell listed in double, in double: the cell's radial
- * shift (imap.c:196-198) and the sample's shell and pixel (imap.c:210-231). */
-__global__ void __launch_bounds__(256) k_imap_double(const float *__restrict__ phi, cg_imap_params p)
+ * settles all but ~1e-9 of the pixels the float margins left open; the rest
+ * -- shells within the float radial shift's bound of an edge, and every
+ * sample of a cell listed in double -- are gathered per warp in shared
+ * memory and decided in double 32 at a time, so that the FP64 work runs in
+ * full warps. */
+__global__ void __launch_bounds__(DB_WARPS * 32) k_imap_double(const float *__restrict__ phi, cg_imap_params p)
 {
   extern __shared__ __align__(16) unsigned char sraw[];
   const Sh sh = load_shells(p, sraw, false);
   __syncthreads();
   const cg_imap_args A = args_with(p, sh);
+  unsigned long long *db = reinterpret_cast<unsigned long long *>(sraw + double_stage_off(p.nr, p.nbk)) +
+                           (size_t)(threadIdx.x >> 5) * 64;
   const unsigned long long nq0 = p.ctr[4];
   const long long nq = (long long)nq0 < p.queue_cap ? (long long)nq0 : p.queue_cap;
-  /* warp-uniform steps over the queue: consecutive entries mostly share a
-   * record (a lane queues up to four samples of its unit together), so the
-   * first lane of each run of one record that needs double takes the cell's
-   * double quantities and hands them to the rest of the run */
   const int lane = threadIdx.x & 31;
   const long long stride = (long long)gridDim.x * blockDim.x;
+  int dn = 0; /* entries gathered for double (warp-uniform) */
   unsigned long long ndbl = 0;
   for (long long kb = (long long)blockIdx.x * blockDim.x + threadIdx.x - lane; kb < nq; kb += stride) {
     const long long k = kb + lane;
     const bool valid = k < nq;
     const unsigned long long e = valid ? p.queue[k] : ~0ull;
-    const long long rec = (long long)(e >> 30);
-    const int q = (int)(e & ((1ull << 30) - 1));
-    /* the record's bucket: last b with base[b] <= rec */
-    int lo = 0, ix = 0, iy = 0, iz = 0, dbl = 1;
-    cg_imap_cell c;
-    c.temp = 0.0f;
-    if (valid) {
-      int hi = p.nbk - 1;
+    bool need = valid;
+    if (valid && !p.force_double) {
+      const long long rec = (long long)(e >> 30);
+      const int q = (int)(e & ((1ull << 30) - 1));
+      int lo = 0, hi = p.nbk - 1;
       while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
         if (p.base[mid] <= rec) lo = mid;
         else hi = mid - 1;
       }
-      c = unpack(p.recs[rec], lo - 1, &ix, &iy, &iz, &dbl);
-    }
-    bool need = valid;
-    if (valid && !dbl && !p.force_double) {
-      const int ns = sh.nsub[lo];
-      int s = -1, sx, sy, sz;
-      long long pix = 0;
-      sub_of(q, ns, sh.invns[lo], &sx, &sy, &sz);
-      if (cg_imap_decide_ff(&A, &c, ix, iy, iz, sx, sy, sz, &s, &pix)) {
-        need = false;
-        if (s >= 0 && s < p.nr) {
-          const long long key = (long long)s * p.npix + pix;
-          atomicAdd(&p.data[key], c.temp);
-          atomicAdd(&p.nadd[key], 1);
+      int ix, iy, iz, dbl;
+      const cg_imap_cell c = unpack(p.recs[rec], lo - 1, &ix, &iy, &iz, &dbl);
+      if (!dbl) {
+        const int ns = sh.nsub[lo];
+        int s = -1, sx, sy, sz;
+        long long pix = 0;
+        sub_of(q, ns, sh.invns[lo], &sx, &sy, &sz);
+        if (cg_imap_decide_ff(&A, &c, ix, iy, iz, sx, sy, sz, &s, &pix)) {
+          need = false;
+          if (s >= 0 && s < p.nr) {
+            const long long key = (long long)s * p.npix + pix;
+            atomicAdd(&p.data[key], c.temp);
+            atomicAdd(&p.nadd[key], 1);
+          }
         }
       }
     }
     const unsigned nm = __ballot_sync(FULL, need);
     if (!nm) continue;
+    if (need) db[dn + __popc(nm & ((1u << lane) - 1u))] = e;
+    dn += __popc(nm);
     ndbl += lane == 0 ? (unsigned long long)__popc(nm) : 0ull;
-    const long long prev = __shfl_up_sync(FULL, rec, 1);
-    const bool pneed = __shfl_up_sync(FULL, (int)need, 1) != 0;
-    const bool lead = need && (lane == 0 || !pneed || prev != rec);
-    const unsigned lm = __ballot_sync(FULL, lead);
-    const unsigned le = lm & (lane == 31 ? FULL : ((2u << lane) - 1u));
-    const int src = need ? 31 - __clz(le) : lane;
-    double drr = 0;
-    if (lead) {
-      float v[3];
-      grad_phi(phi, ix, iy, iz, p.box.N, v);
-      int j;
-      cgx_imap_cell(&A, ix, iy, iz, v, &j, &drr);
-    }
-    drr = __shfl_sync(FULL, drr, src);
-    if (!need) continue;
-    const int ns = sh.nsub[lo];
-    int s = -1, sx, sy, sz;
-    sub_of(q, ns, sh.invns[lo], &sx, &sy, &sz);
-    long long pix = 0;
-    cgx_imap_sample(&A, ix, iy, iz, ns, drr, sx, sy, sz, &s, &pix);
-    if (s >= 0 && s < p.nr) {
-      const long long key = (long long)s * p.npix + pix;
-      atomicAdd(&p.data[key], c.temp);
-      atomicAdd(&p.nadd[key], 1);
+    __syncwarp();
+    if (dn >= 32) {
+      double_batch(phi, p, A, sh, db[lane], true, lane);
+      __syncwarp();
+      if (lane < dn - 32) db[lane] = db[lane + 32];
+      dn -= 32;
+      __syncwarp();
     }
   }
+  if (dn > 0) double_batch(phi, p, A, sh, lane < dn ? db[lane] : ~0ull, lane < dn, lane);
   if (ndbl) atomicAdd(p.xstats + 3, ndbl);
 }
 
@@ -718,9 +759,10 @@ cudaError_t launch(cudaStream_t s, const float *dens, const float *phi, const cg
   if (e == cudaSuccess) e = cudaMemsetAsync(p->cnt, 0, (size_t)p->nbk * sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
   const size_t sm_list = shell_smem(p->nr, p->nbk, false), sm_paint = paint_smem(p->nr, p->nbk);
+  const size_t sm_double = double_stage_off(p->nr, p->nbk) + (size_t)DB_WARPS * 64 * 8;
   if ((e = cudaFuncSetAttribute(k_imap_list<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_list)) ||
       (e = cudaFuncSetAttribute(k_imap_paint<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_paint)) ||
-      (e = cudaFuncSetAttribute(k_imap_double, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_list)))
+      (e = cudaFuncSetAttribute(k_imap_double, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_double)))
     return e;
   int per_sm = 0;
   if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_imap_list<K>, IW * 32, sm_list))) return e;
@@ -731,7 +773,7 @@ cudaError_t launch(cudaStream_t s, const float *dens, const float *phi, const cg
   k_imap_chunks<<<1, 32, 0, s>>>(*p);
   if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_imap_paint<K>, IW * 32, sm_paint))) return e;
   k_imap_paint<K><<<(unsigned)(nsm * (per_sm > 0 ? per_sm : 1)), IW * 32, sm_paint, s>>>(*p);
-  k_imap_double<<<(unsigned)(nsm * 4), 256, sm_list, s>>>(phi, *p);
+  k_imap_double<<<(unsigned)(nsm * 4), DB_WARPS * 32, sm_double, s>>>(phi, *p);
   return cudaGetLastError();
 }
 
