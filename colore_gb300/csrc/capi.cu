@@ -718,6 +718,11 @@ extern "C" int cg_upload_tables(cg_ctx *c, const cg_config *cfg)
     if (int rc = dalloc(c, &c->d_corner, cr.size())) return rc;
     CUDA_TRY(c, cudaMemcpyAsync(c->d_corner, cr.data(), cr.size() * sizeof(float), cudaMemcpyHostToDevice,
                                 c->stream));
+    std::vector<float> att(2 * (CG_ATT_N + 1));
+    cg_att_table(att.data());
+    if (!c->d_att)
+      if (int rc = dalloc(c, &c->d_att, att.size())) return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_att, att.data(), att.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
     if (nnorm > 0) {
       std::vector<double> ones((size_t)nnorm * nas, 1.0);
       if (int rc = dalloc(c, &c->d_norm64, ones.size())) return rc;
@@ -1621,12 +1626,7 @@ static int imap_prepare(cg_ctx *c, int ip)
   std::vector<float> dxsl(nr + 2);
   for (int i = 0; i < nr + 2; i++) dxsl[i] = (float)(dx / nsub[i] - (double)dxs[i]);
   CUDA_TRY(c, cudaMemcpyAsync(M.dxsl, dxsl.data(), (nr + 2) * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-  std::vector<float> att(2 * (CG_ATT_N + 1));
-  if (!c->d_att) {
-    if ((rc = dalloc(c, &c->d_att, att.size()))) return rc;
-    cg_att_table(att.data());
-    CUDA_TRY(c, cudaMemcpyAsync(c->d_att, att.data(), att.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-  }
+
   CUDA_TRY(c, cudaMemcpyAsync(M.base, base.data(), nbk * sizeof(long long), cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(c, cudaMemcpyAsync(M.cap, capv.data(), nbk * sizeof(long long), cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream)); /* host staging vectors */

@@ -311,6 +311,11 @@ CG_HD float cg_rcp_fast(float x)
 
 CG_HD float cg_fmaxf(float a, float b) { return a > b ? a : b; }
 CG_HD float cg_fminf(float a, float b) { return a < b ? a : b; }
+/* min / max of values that are never NaN (magnitudes of finite coordinates,
+ * distances to integers): fminf / fmaxf, one instruction on the device,
+ * where the selects above (which keep a NaN bound NaN) take two. */
+CG_HD float cg_min_nn(float a, float b) { return fminf(a, b); }
+CG_HD float cg_max_nn(float a, float b) { return fmaxf(a, b); }
 
 /* Distance of x >= 0 to the nearest integer, and floor(x). */
 CG_HD float cg_int_dist(float x, int *fl)
@@ -529,8 +534,8 @@ CG_HD cg_dir cg_dir_of(float x, float y, float z, float ein)
   o.rinv = cg_rsqrt_fast(r2);
   o.cth = CG_MUL(z, o.rinv);
   const float ax = cg_fabsf(x), ay = cg_fabsf(y);
-  const float mx = cg_fmaxf(ax, ay), mn = cg_fminf(ax, ay);
-  const float t = CG_MUL(mn, cg_rcp_fast(cg_fmaxf(mx, 1e-30f))); /* atan2(0, 0) = 0 */
+  const float mx = cg_max_nn(ax, ay), mn = cg_min_nn(ax, ay);
+  const float t = CG_MUL(mn, cg_rcp_fast(cg_max_nn(mx, 1e-30f))); /* atan2(0, 0) = 0 */
   const float g = CG_MUL(cg_atan01(t), 0.636619772367581343f); /* atan(min/max) / (pi/2) */
   /* tt = phi / (pi/2) in [0, 4) is base + g' or base - g' with
    * g' = atan(ay/ax) / (pi/2) (g, or 1 - g when ay > ax) and, by quadrant,
@@ -589,7 +594,7 @@ CG_HD long long cg_pix_checked(const cg_dir *d, int nside, float ein)
     const float ev = CG_FMA(ns, CG_FMA(0.75f, d->ecth, CG_ADD(ef, 2.5e-7f)), 1e-9f);
     const float fa = floorf(A), fb = floorf(B);
     const float da = CG_SUB(A, fa), db = CG_SUB(B, fb);
-    const float dm = cg_fminf(cg_fminf(da, CG_SUB(1.0f, da)), cg_fminf(db, CG_SUB(1.0f, db)));
+    const float dm = cg_min_nn(cg_min_nn(da, CG_SUB(1.0f, da)), cg_min_nn(db, CG_SUB(1.0f, db)));
     if (!(region_ok && dm > ev)) return -1;
     const int jp = nside * d->q + cg_fint(fa), jm = nside * d->q + cg_fint(fb);
     const int ir = nside + 1 + jp - jm;
@@ -628,8 +633,8 @@ CG_HD long long cg_pix_checked(const cg_dir *d, int nside, float ein)
   const float p3 = CG_MUL(d->f, (float)ir);
   const float f3 = floorf(p3), d3 = CG_SUB(p3, f3);
   const float e3 = CG_FMA((float)ir, ef, CG_FMA(2.0f * CG_E24, p3, 2.0f * CG_E24 + 1e-9f));
-  if (!(cg_fminf(d1, CG_SUB(1.0f, d1)) > e1 && cg_fminf(d2, CG_SUB(1.0f, d2)) > e2 &&
-        cg_fminf(d3, CG_SUB(1.0f, d3)) > e3))
+  if (!(cg_min_nn(d1, CG_SUB(1.0f, d1)) > e1 && cg_min_nn(d2, CG_SUB(1.0f, d2)) > e2 &&
+        cg_min_nn(d3, CG_SUB(1.0f, d3)) > e3))
     return -1;
   int ip = d->q * ir + cg_fint(f3);
   const int m = 4 * ir;
@@ -805,7 +810,7 @@ CG_HD float cg_interval_margin(const cg_shells *sh, int k, float r)
 {
   const float below = k >= 0 ? CG_SUB(r, sh->b[k]) : 3.0e38f;
   const float above = k + 1 < sh->nb ? CG_SUB(sh->b[k + 1], r) : 3.0e38f;
-  return cg_fminf(below, above);
+  return cg_min_nn(below, above);
 }
 
 /* Everything a species' cells and samples need, in float and in double. */
