@@ -87,8 +87,10 @@ __device__ __noinline__ int ptrs_float(float lam, float elam, long long cid, uin
  * positive lambda.  The cell loop is not unrolled (unrolled, the kernel ran
  * instruction-fetch bound); the counts are packed in two 64-bit registers.
  * Each warp adds its total to the block's entry (zeroed before the launch),
- * so warps that finish early do not wait for the block's slowest. */
-__global__ void __launch_bounds__(SB, 4) k_pois_count(const float *__restrict__ grid, cg_srcs_params p)
+ * so warps that finish early do not wait for the block's slowest.  Six
+ * blocks per SM (40 registers): the table lookups' latency wants the warps
+ * more than the few spills cost (13.1 -> 12.0 ms at 1024^3 against four). */
+__global__ void __launch_bounds__(SB, 6) k_pois_count(const float *__restrict__ grid, cg_srcs_params p)
 {
   const int N = p.box.N;
   const long long ncell = (long long)N * N * N;
