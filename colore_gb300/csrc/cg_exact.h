@@ -583,26 +583,29 @@ CG_HD long long cg_pix_checked(const cg_dir *d, int nside, float ein)
   if (ctha < c23) {
     /* phi error from the inputs: sqrt(2) ein / sin(theta) with
      * sin(theta) >= sqrt(5)/3 here, times 2/pi */
-    const float ef = CG_FMA(1.21f, ein, d->ef);
     /* temp1 -+ temp2 = ns (q + 0.5 + f -+ 0.75 cth): the integer ns q is
      * split off and ns v is exact (ns a power of two) */
     const float hf = CG_ADD(0.5f, d->f);
     const float A = CG_MUL(ns, CG_FMA(-0.75f, d->cth, hf));
     const float B = CG_MUL(ns, CG_FMA(0.75f, d->cth, hf));
-    /* roundings of 0.5 + f (<= 1.5) and of the fused multiply-add (<= 2.25):
-     * 1.8e-7, taken as 2.5e-7 */
-    const float ev = CG_FMA(ns, CG_FMA(0.75f, d->ecth, CG_ADD(ef, 2.5e-7f)), 1e-9f);
+    /* v's bound: 0.75 ecth, f's bound d->ef plus the inputs' share
+     * 1.21 ein, and the roundings of 0.5 + f (<= 1.5) and of the fused
+     * multiply-add (<= 2.25): 1.8e-7, taken as 2.5e-7 */
+    const float ev = CG_FMA(ns, CG_FMA(0.75f, d->ecth, CG_FMA(1.21f, ein, CG_ADD(d->ef, 2.5e-7f))), 1e-9f);
     const float fa = floorf(A), fb = floorf(B);
     const float da = CG_SUB(A, fa), db = CG_SUB(B, fb);
     const float dm = cg_min_nn(cg_min_nn(da, CG_SUB(1.0f, da)), cg_min_nn(db, CG_SUB(1.0f, db)));
     if (!(region_ok && dm > ev)) return -1;
-    const int jp = nside * d->q + cg_fint(fa), jm = nside * d->q + cg_fint(fb);
-    const int ir = nside + 1 + jp - jm;
+    /* jp = nside q + floor(A), jm = nside q + floor(B): the floors read from
+     * the bits of fa + 1.5 2^23 (cg_fint), whose offsets cancel in jp - jm
+     * and are removed once from jp + jm (in unsigned arithmetic, which wraps) */
+    const unsigned ua = cg_f2u(CG_ADD(fa, 12582912.0f)), ub = cg_f2u(CG_ADD(fb, 12582912.0f));
+    const int ir = nside + 1 + (int)(ua - ub);
     const int kshift = 1 - (ir & 1);
-    int ip = (jp + jm - nside + kshift + 1) >> 1;
     /* ip mod 4 nside: with q in 0..3 and 0 <= A/ns, B/ns < 2.25, jp + jm is
      * in [nside - 1, 2 (3 + 2.25) nside) (each floor loses less than 1), so
      * ip is in [0, 5 nside) and one subtraction is the modulo */
+    int ip = (int)((unsigned)(2 * nside * d->q - nside + kshift + 1) + ua + ub - 2u * 0x4B400000u) >> 1;
     const int m = 4 * nside;
     if (ip >= m) ip -= m;
     return (long long)(nside * (nside - 1) * 2 + (ir - 1) * 4 * nside + ip);
@@ -624,16 +627,19 @@ CG_HD long long cg_pix_checked(const cg_dir *d, int nside, float ein)
   const float ef = CG_FMA(0.91f * ein, isth, d->ef);
   const float tp = d->f;
   const float p1 = CG_MUL(tp, tmp), p2 = CG_MUL(CG_SUB(1.0f, tp), tmp);
-  const float e1 = CG_FMA(tmp, ef, CG_FMA(tp, es, CG_FMA(2.0f * CG_E24, p1, 2.0f * CG_E24 + 1e-9f)));
-  const float e2 = CG_FMA(tmp, CG_ADD(ef, CG_E24), CG_FMA(CG_SUB(1.0f, tp), es, CG_FMA(2.0f * CG_E24, p2, 2.0f * CG_E24 + 1e-9f)));
+  /* p1 = tp tmp: tmp ef + tp es and its rounding; p2 = (1 - tp) tmp: one
+   * more rounding in 1 - tp; with p1, p2 <= tmp and tp, 1 - tp <= 1, one
+   * bound covers both */
+  const float e12 = CG_FMA(tmp, CG_ADD(ef, 3.0f * CG_E24), CG_ADD(es, 2.0f * CG_E24 + 1e-9f));
   const float f1 = floorf(p1), f2 = floorf(p2);
   const float d1 = CG_SUB(p1, f1), d2 = CG_SUB(p2, f2);
   const int jp = cg_fint(f1), jm = cg_fint(f2);
   const int ir = jp + jm + 1;
-  const float p3 = CG_MUL(d->f, (float)ir);
+  const float fir = CG_ADD(CG_ADD(f1, f2), 1.0f); /* ir, exact */
+  const float p3 = CG_MUL(d->f, fir);
   const float f3 = floorf(p3), d3 = CG_SUB(p3, f3);
-  const float e3 = CG_FMA((float)ir, ef, CG_FMA(2.0f * CG_E24, p3, 2.0f * CG_E24 + 1e-9f));
-  if (!(cg_min_nn(d1, CG_SUB(1.0f, d1)) > e1 && cg_min_nn(d2, CG_SUB(1.0f, d2)) > e2 &&
+  const float e3 = CG_FMA(fir, ef, CG_FMA(2.0f * CG_E24, p3, 2.0f * CG_E24 + 1e-9f));
+  if (!(cg_min_nn(cg_min_nn(d1, CG_SUB(1.0f, d1)), cg_min_nn(d2, CG_SUB(1.0f, d2))) > e12 &&
         cg_min_nn(d3, CG_SUB(1.0f, d3)) > e3))
     return -1;
   int ip = d->q * ir + cg_fint(f3);

@@ -85,7 +85,9 @@ CG_HD float cg_u2f(uint32_t u)
 #endif
 }
 
-CG_HD float cg_fabsf(float x) { return cg_u2f(cg_f2u(x) & 0x7fffffffu); }
+/* |x|: the sign bit cleared (fabsf, which the device folds into the
+ * operands of the instructions that use it). */
+CG_HD float cg_fabsf(float x) { return fabsf(x); }
 
 /* floor for |x| < 2^31, exact on both sides (truncation then correction). */
 CG_HD float cg_floorf(float x)
