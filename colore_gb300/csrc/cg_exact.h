@@ -536,7 +536,7 @@ CG_HD cg_dir cg_dir_of(float x, float y, float z, float ein)
   const float ax = cg_fabsf(x), ay = cg_fabsf(y);
   const float mx = cg_max_nn(ax, ay), mn = cg_min_nn(ax, ay);
   const float t = CG_MUL(mn, cg_rcp_fast(cg_max_nn(mx, 1e-30f))); /* atan2(0, 0) = 0 */
-  const float g = CG_MUL(cg_atan01(t), 0.636619772367581343f); /* atan(min/max) / (pi/2) */
+  const float g = cg_atan01_q(t); /* atan(min/max) / (pi/2) */
   /* tt = phi / (pi/2) in [0, 4) is base + g' or base - g' with
    * g' = atan(ay/ax) / (pi/2) (g, or 1 - g when ay > ax) and, by quadrant,
    * (base, sign) = (0, +) x >= 0 y >= 0, (2, -) x < 0 y >= 0, (2, +) x < 0 y < 0,
@@ -556,11 +556,11 @@ CG_HD cg_dir cg_dir_of(float x, float y, float z, float ein)
   /* cos(theta): r^2 (2 roundings), rsqrt (2^-22), product (2^-24); the
    * inputs' error ein (relative to r) moves cos(theta) by at most 2 ein */
   o.ecth = CG_FMA(cg_fabsf(o.cth), 8.0f * CG_E24, CG_MUL(2.0f, ein));
-  /* f: atan01 within 1.3 ulp of atan on [0,1] (7.8e-8 absolute below
-   * pi/4), times 2/pi; the ratio's relative error 2^-22 moves atan by at most
-   * that times t/(1+t^2) <= 1/2 (6e-8); the roundings of g and of 1 - g
-   * (3e-8 each): 1.5e-7 in all, taken as 2.5e-7.  The inputs' share, which
-   * depends on 1/sin(theta), is added by cg_pix_checked. */
+  /* f: cg_atan01_q within 8.2e-8 of atan / (pi/2) on [0,1]; the ratio's
+   * relative error 2^-22 moves atan by at most that times t/(1+t^2) <= 1/2
+   * (6e-8 rad, 3.8e-8 in quarter turns); the rounding of 1 - g (3e-8):
+   * 1.5e-7 in all, taken as 2.5e-7.  The inputs' share, which depends on
+   * 1/sin(theta), is added by cg_pix_checked. */
   o.ef = 2.5e-7f;
   return o;
 }
@@ -1011,8 +1011,9 @@ CG_HD int cg_imap_decide(const cg_imap_args *a, const cg_imap_cell *c, float x, 
                          long long *pix)
 {
   cg_dir dr = cg_dir_of(x, y, z, 0.0f);
-  /* coordinates within 2^-24 (|x| + 2 dx) of the double ones */
-  const float ein = CG_MUL(1.8f * CG_E24, CG_FMA(2.0f * a->dx, dr.rinv, 1.0f));
+  /* coordinates within 2^-24 (|x| + 2 dx) of the double ones: relative to
+   * r, 1.8 2^-24 (1 + 2 dx / r) */
+  const float ein = CG_FMA(CG_MUL(3.6f * CG_E24, a->dx), dr.rinv, 1.8f * CG_E24);
   if (!cg_imap_shell_checked(a, c, CG_MUL(dr.r2, dr.rinv), ein, s)) return 0;
   if (*s < 0 || *s >= a->sh.nr) return 1;
   dr.ecth = CG_FMA(2.0f, ein, dr.ecth);

@@ -194,6 +194,26 @@ CG_HD float cg_atan01(float a)
   return CG_MUL(a, p);
 }
 
+/* atan(a) / (pi/2) on [0, 1]: cg_atan01's coefficients times 2/pi, each
+ * rounded to float, so that the quarter-turn angle costs no extra product;
+ * within 8.2e-8 of the value over every float of [0, 1] (checked
+ * exhaustively against libm's double atan). */
+CG_HD float cg_atan01_q(float a)
+{
+  const float w = CG_MUL(a, a);
+  float p = -0.00111658662f;
+  p = CG_FMA(p, w, 0.00682898518f);
+  p = CG_FMA(p, w, -0.0196108148f);
+  p = CG_FMA(p, w, 0.0366388075f);
+  p = CG_FMA(p, w, -0.0533316508f);
+  p = CG_FMA(p, w, 0.0696591288f);
+  p = CG_FMA(p, w, -0.0907942802f);
+  p = CG_FMA(p, w, 0.127312914f);
+  p = CG_FMA(p, w, -0.212206274f);
+  p = CG_FMA(p, w, 0.636619747f);
+  return CG_MUL(a, p);
+}
+
 /* atan2(y, x) in (-pi, pi]; atan2(0, 0) = 0. */
 CG_HD float cg_atan2f(float y, float x)
 {

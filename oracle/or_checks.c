@@ -19,6 +19,21 @@ void or_vec_sincosf(const float *x, float *s, float *c, long n)
 {
   for (long i = 0; i < n; i++) cg_sincosf(x[i], &s[i], &c[i]);
 }
+/* Largest |cg_atan01_q(t) - atan(t) / (pi/2)| over every float t in [0, 1]
+ * (libm's double atan as the reference). */
+double or_atan_q_maxerr(void)
+{
+  const uint32_t top = 0x3f800000u; /* 1.0f */
+  double mx = 0;
+#pragma omp parallel for reduction(max : mx) schedule(static, 65536)
+  for (long long b = 0; b <= (long long)top; b++) {
+    const float t = cg_u2f((uint32_t)b);
+    const double e = fabs((double)cg_atan01_q(t) - atan((double)t) * 0.63661977236758134308);
+    if (e > mx) mx = e;
+  }
+  return mx;
+}
+
 void or_philox(const uint32_t *ctr, const uint32_t *key, uint32_t *out)
 {
   cg_u32x4 r = cg_philox4x32_10(ctr[0], ctr[1], ctr[2], ctr[3], key[0], key[1]);

@@ -52,6 +52,7 @@ def lib():
             "or_shell_index": [vp, vp, i, vp, vp, vp, C.c_long],
             "or_pix_checked": [C.c_long, vp, C.c_long, f, vp], "or_pix_cgx": [C.c_long, vp, C.c_long, vp],
             "or_pix64": [C.c_long, vp, C.c_long, vp], "or_pix_ff": [C.c_long, vp, vp, C.c_long, vp],
+            "or_atan_q_maxerr": [],
             "or_sht_legendre": [i, i, i, vp, vp, vp, d, vp],
             "or_src_offset_checked": [C.c_long, vp, d, vp, vp, vp, vp],
             "or_ptrs_checked": [C.c_long, vp, vp, vp, vp, C.c_uint32, C.c_uint32, vp, vp],
@@ -64,6 +65,8 @@ def lib():
             fn.argtypes = a
             if k in ("or_imap_samples", "or_poisson_total64"):
                 fn.restype = C.c_longlong
+            elif k == "or_atan_q_maxerr":
+                fn.restype = C.c_double
             elif k.startswith("or_vec") or k in void:
                 fn.restype = None
             else:

@@ -125,6 +125,14 @@ def test_float_float_pixels_never_disagree_with_double(ns):
             assert (orc.pix_checked(ns, v.astype(np.float32)) < 0).mean() > 0.99
 
 
+def test_quarter_turn_atan_exhaustive():
+    """The polynomial behind every float direction's quarter-turn angle
+    (cg_atan01_q) is within 8.2e-8 of atan(t) / (pi/2) for every float t in
+    [0, 1]: the accuracy the pixel margins assume."""
+    import oracle as orc
+    assert orc.lib().or_atan_q_maxerr() < 8.2e-8
+
+
 def _spec(bias_model):
     return dict(n_grid=64, z_min=0.05, z_max=0.6, r_smooth=2.0, seed=11 + bias_model, dens_type=0,
                 bias_model=bias_model,
