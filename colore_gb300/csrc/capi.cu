@@ -2090,7 +2090,13 @@ static int out_catalogs(cg_ctx *c)
 
 /* The beam stage (beaming.c:293-374).  async: inside a captured sequence --
  * source totals stay on the device, no host outputs. */
-static int beam_run(cg_ctx *c, bool async)
+/* The per-source half of the beam stage (beaming.c:293-374): RSD, lensing
+ * and skewers at the sources, then (plain runs) the catalogues to the host.
+ * The reference computes the beam quantities last; the passes are
+ * independent of the maps, so the mock sequence runs them before the
+ * intensity and convergence maps and the catalogues cross the host link
+ * while the maps are computed. */
+static int beam_srcs(cg_ctx *c, bool async)
 {
   if (!async) {
     if (int rc = refresh_counts(c)) return rc;
@@ -2104,9 +2110,6 @@ static int beam_run(cg_ctx *c, bool async)
     out_join(c, 0); /* RSD and lensing columns are rewritten */
     out_join(c, 2);
   }
-  /* The source quantities first (the reference computes them last,
-   * beaming.c:293-374; the passes are independent): the catalogues can then
-   * go to the host while the maps are computed. */
   if (c->cfg.n_srcs > 0) {
     if (!c->have_srcs) return fail(c, CG_ESTATE, "srcs_set_cartesian first");
     for (int ip = 0; ip < c->cfg.n_srcs; ip++) {
@@ -2121,6 +2124,16 @@ static int beam_run(cg_ctx *c, bool async)
     if (!async)
       if (int rc = out_catalogs(c)) return rc;
   }
+  return CG_OK;
+}
+
+/* The map half of the beam stage: convergence (and its host copy), ISW and
+ * custom maps. */
+static int beam_maps(cg_ctx *c, bool async)
+{
+  if (!c->cfg.need_beaming) return CG_OK;
+  if (!c->have_fields) return fail(c, CG_ESTATE, "fields not created");
+  cudaSetDevice(c->device);
   if (c->cfg.do_kappa) {
     if (int rc = kappa_run(c)) return rc;
     if (!async && c->h_kappa) {
@@ -2135,6 +2148,12 @@ static int beam_run(cg_ctx *c, bool async)
   if (c->cfg.n_cstm > 0)
     if (int rc = cstm_run(c)) return rc;
   return CG_OK;
+}
+
+static int beam_run(cg_ctx *c, bool async)
+{
+  if (int rc = beam_srcs(c, async)) return rc;
+  return beam_maps(c, async);
 }
 
 extern "C" int cg_get_beam_properties(cg_ctx *c)
@@ -2192,9 +2211,10 @@ extern "C" int cg_run_mock(cg_ctx *c)
   if ((rc = cg_compute_physical_density_field(c))) return rc;
   if ((rc = cg_compute_density_normalization(c))) return rc;
   if ((rc = cg_srcs_set_cartesian(c, nullptr))) return rc;
+  /* the sources' beam quantities before the maps (beam_srcs) */
+  if ((rc = beam_srcs(c, false))) return rc;
   if ((rc = cg_imap_set_cartesian(c))) return rc;
-  if ((rc = cg_get_beam_properties(c))) return rc;
-  return CG_OK;
+  return beam_maps(c, false);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -2212,8 +2232,9 @@ static int run_mock_async(cg_ctx *c)
   if ((rc = cg_compute_physical_density_field(c))) return rc;
   if ((rc = cg_compute_density_normalization(c))) return rc;
   if ((rc = srcs_run(c, nullptr, false))) return rc;
+  if ((rc = beam_srcs(c, true))) return rc;
   if (c->cfg.n_imap > 0 && (rc = imap_run(c, false))) return rc;
-  return beam_run(c, true);
+  return beam_maps(c, true);
 }
 
 extern "C" int cg_graph_capture(cg_ctx *c)

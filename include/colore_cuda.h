@@ -210,7 +210,11 @@ int cg_get_beam_properties(cg_ctx *ctx);
 int cg_set_host_catalog(cg_ctx *ctx, int ipop, float *src9, long long cap, long long *n_out);
 int cg_set_host_imap(cg_ctx *ctx, int ipop, float *map);
 int cg_set_host_kappa(cg_ctx *ctx, float *map);
-/* Run the whole driver sequence of src/main.c:66-125 in one call. */
+/* Run the whole driver sequence of src/main.c:66-125 in one call.  The
+ * sources' beam quantities (RSD, lensing, skewers) run right after the
+ * sources and before the intensity and convergence maps, on which they do
+ * not depend, so that a registered host catalogue is copied while the maps
+ * are computed; the outputs are those of the reference's order. */
 int cg_run_mock(cg_ctx *ctx);
 
 /* Graph-captured sequence (no counterpart in the reference; the batching
