@@ -83,8 +83,9 @@ __device__ __forceinline__ Sh shells_at(const cg_imap_params &p, unsigned char *
 /* The painting warps' queue stages follow the tables. */
 __host__ __device__ __forceinline__ size_t paint_stage_off(int nr, int nbk) { return (shell_smem(nr, nbk, true) + 15) & ~(size_t)15; }
 __host__ __device__ __forceinline__ size_t paint_smem(int nr, int nbk) { return paint_stage_off(nr, nbk) + (size_t)IW * QB * 8; }
-/* The double pass's per-warp gathers (64 entries) follow its tables. */
-__host__ __device__ __forceinline__ size_t double_stage_off(int nr, int nbk) { return (shell_smem(nr, nbk, false) + 15) & ~(size_t)15; }
+/* The double pass keeps the buckets' bases where the painting keeps its
+ * chunk table; its per-warp gathers (64 entries) follow. */
+__host__ __device__ __forceinline__ size_t double_stage_off(int nr, int nbk) { return (shell_smem(nr, nbk, true) + 15) & ~(size_t)15; }
 
 __device__ __forceinline__ Sh load_shells(const cg_imap_params &p, unsigned char *raw, bool chunks)
 {
@@ -633,8 +634,8 @@ __global__ void __launch_bounds__(IW * 32, 8) k_imap_paint(cg_imap_params p)
  * of each run of one record and handed to the rest of the run, then the
  * sample's shell and pixel (imap.c:210-231). */
 __device__ __forceinline__ void double_batch(const float *__restrict__ phi, const cg_imap_params &p,
-                                             const cg_imap_args &A, const Sh &sh, unsigned long long e, bool valid,
-                                             int lane)
+                                             const cg_imap_args &A, const Sh &sh, const long long *sbase,
+                                             unsigned long long e, bool valid, int lane)
 {
   const long long rec = (long long)(e >> 30);
   const int q = (int)(e & ((1ull << 30) - 1));
@@ -651,7 +652,7 @@ __device__ __forceinline__ void double_batch(const float *__restrict__ phi, cons
     int hi = p.nbk - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
-      if (p.base[mid] <= rec) lo = mid;
+      if (sbase[mid] <= rec) lo = mid;
       else hi = mid - 1;
     }
     int dbl;
@@ -693,6 +694,8 @@ __global__ void __launch_bounds__(DB_WARPS * 32) k_imap_double(const float *__re
 {
   extern __shared__ __align__(16) unsigned char sraw[];
   const Sh sh = load_shells(p, sraw, false);
+  long long *sbase = reinterpret_cast<long long *>(sh.chunk_off); /* the buckets' first records */
+  for (int i = threadIdx.x; i < p.nbk; i += blockDim.x) sbase[i] = p.base[i];
   __syncthreads();
   const cg_imap_args A = args_with(p, sh);
   unsigned long long *db = reinterpret_cast<unsigned long long *>(sraw + double_stage_off(p.nr, p.nbk)) +
@@ -714,7 +717,7 @@ __global__ void __launch_bounds__(DB_WARPS * 32) k_imap_double(const float *__re
       int lo = 0, hi = p.nbk - 1;
       while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (p.base[mid] <= rec) lo = mid;
+        if (sbase[mid] <= rec) lo = mid;
         else hi = mid - 1;
       }
       int ix, iy, iz, dbl;
@@ -741,14 +744,14 @@ __global__ void __launch_bounds__(DB_WARPS * 32) k_imap_double(const float *__re
     ndbl += lane == 0 ? (unsigned long long)__popc(nm) : 0ull;
     __syncwarp();
     if (dn >= 32) {
-      double_batch(phi, p, A, sh, db[lane], true, lane);
+      double_batch(phi, p, A, sh, sbase, db[lane], true, lane);
       __syncwarp();
       if (lane < dn - 32) db[lane] = db[lane + 32];
       dn -= 32;
       __syncwarp();
     }
   }
-  if (dn > 0) double_batch(phi, p, A, sh, lane < dn ? db[lane] : ~0ull, lane < dn, lane);
+  if (dn > 0) double_batch(phi, p, A, sh, sbase, lane < dn ? db[lane] : ~0ull, lane < dn, lane);
   if (ndbl) atomicAdd(p.xstats + 3, ndbl);
 }
 
