@@ -463,14 +463,12 @@ __device__ __forceinline__ void paint_sample(const cg_imap_params &p, const cg_i
   }
 }
 
-/* The G unit groups of one chunk of bucket b (nsub ns, NS when it is known
- * at compile time: whole cells of NS^3 samples, their x offsets computed once
- * per cell and the x loop unrolled).  Each lane walks one unit (a cell, a
- * slab or a line) sample by sample with its row coordinates and the cell's
- * fields held in registers.  Every lane of a warp runs the same sample loop,
+/* The G unit groups of one chunk of bucket b (nsub ns).  Each lane walks one
+ * unit (a cell, a slab or a line) sample by sample with its row coordinates
+ * and the cell's fields held in registers.  Every lane of a warp runs the same sample loop,
  * so the samples that only double can decide are staged per warp in shared
  * memory (qb, qn entries) and queued in batches. */
-template <typename K, int NS>
+template <typename K>
 __device__ __forceinline__ void paint_chunk(const cg_imap_params &p, const cg_imap_args &A, int b, int ns,
                                             unsigned long long u0, int G, unsigned long long nu, float dxs, int lane,
                                             int &qn)
@@ -532,33 +530,18 @@ __device__ __forceinline__ void paint_chunk(const cg_imap_params &p, const cg_im
      * queued after the unit, the rest queued at once */
     int nf = 0, f0 = 0, f1 = 0, f2 = 0, f3 = 0;
     if (valid) {
-      if (NS > 0) {
-        float xs[NS > 0 ? NS : 1];
-#pragma unroll
-        for (int sx = 0; sx < NS; sx++) xs[sx] = CG_ADD(xc, CG_FMA((float)sx + 0.5f, dxs, xl));
-#pragma unroll 1
-        for (int sz = 0; sz < NS; sz++) {
-          const float z = CG_ADD(zc, CG_FMA(CG_ADD((float)sz, 0.5f), dxs, zl));
-#pragma unroll 1
-          for (int sy = 0; sy < NS; sy++) {
-            const float y = CG_ADD(yc, CG_FMA(CG_ADD((float)sy, 0.5f), dxs, yl));
-#pragma unroll
-            for (int sx = 0; sx < NS; sx++)
-              paint_sample<K>(p, A, c, dbl, rec, xs[sx], y, z, sx + NS * (sy + NS * sz), k0, n0, k1, n1, nf, f0,
-                              f1, f2, f3);
-          }
-        }
-      } else {
-        for (int sz = z0; sz < z1; sz++) {
-          const float z = CG_ADD(zc, CG_FMA(CG_ADD((float)sz, 0.5f), dxs, zl));
-          for (int sy = y0; sy < y1; sy++) {
-            const float y = CG_ADD(yc, CG_FMA(CG_ADD((float)sy, 0.5f), dxs, yl));
-            float fsx = 0.5f; /* sx + 1/2, exact, without a conversion per sample */
-#pragma unroll 4
-            for (int sx = 0; sx < ns; sx++, fsx = CG_ADD(fsx, 1.0f))
-              paint_sample<K>(p, A, c, dbl, rec, CG_ADD(xc, CG_FMA(fsx, dxs, xl)), y, z, sx + ns * (sy + ns * sz),
-                              k0, n0, k1, n1, nf, f0, f1, f2, f3);
-          }
+      for (int sz = z0; sz < z1; sz++) {
+        const float z = CG_ADD(zc, CG_FMA(CG_ADD((float)sz, 0.5f), dxs, zl));
+        for (int sy = y0; sy < y1; sy++) {
+          const float y = CG_ADD(yc, CG_FMA(CG_ADD((float)sy, 0.5f), dxs, yl));
+          float fsx = 0.5f; /* sx + 1/2, exact, without a conversion per sample */
+          /* unrolled by 3: half the samples of a 1024^3 run are in cells of
+           * nsub 2 and 3; copies per nsub, or unrolled by 2 or 4, measured
+           * slower (instruction fetch) */
+#pragma unroll 3
+          for (int sx = 0; sx < ns; sx++, fsx = CG_ADD(fsx, 1.0f))
+            paint_sample<K>(p, A, c, dbl, rec, CG_ADD(xc, CG_FMA(fsx, dxs, xl)), y, z, sx + ns * (sy + ns * sz), k0,
+                            n0, k1, n1, nf, f0, f1, f2, f3);
         }
       }
     }
@@ -588,9 +571,7 @@ __device__ __forceinline__ void paint_chunk(const cg_imap_params &p, const cg_im
   }
 }
 
-/* Warps take chunks in bucket order (paint_chunk paints one); buckets of
- * nsub 2 to 4 -- cells of 8 to 64 samples, half the samples of a 1024^3 run
- * -- have their own unrolled copy. */
+/* Warps take chunks in bucket order; paint_chunk paints one. */
 template <typename K>
 __global__ void __launch_bounds__(IW * 32, 8) k_imap_paint(cg_imap_params p)
 {
@@ -621,10 +602,7 @@ __global__ void __launch_bounds__(IW * 32, 8) k_imap_paint(cg_imap_params p)
     const int G = groups_per_chunk(ns);
     const float dxs = sh.dxs[b];
     const unsigned long long u0 = (ck - sh.chunk_off[b]) * 32ull * (unsigned long long)G;
-    if (ns == 2) paint_chunk<K, 2>(p, A, b, ns, u0, G, nu, dxs, lane, qn);
-    else if (ns == 3) paint_chunk<K, 3>(p, A, b, ns, u0, G, nu, dxs, lane, qn);
-    else if (ns == 4) paint_chunk<K, 4>(p, A, b, ns, u0, G, nu, dxs, lane, qn);
-    else paint_chunk<K, 0>(p, A, b, ns, u0, G, nu, dxs, lane, qn);
+    paint_chunk<K>(p, A, b, ns, u0, G, nu, dxs, lane, qn);
   }
   if (qn) queue_flush(p, stage_of(p), qn, lane);
 }
