@@ -121,8 +121,8 @@ MEASURED_DRAM_BYTES_PER_CELL = {"field_fft": 38.5, "lpt_fft": 59.8, "dens_bins":
 # listing kernel per cell in the shells' radial range, the painting kernel per
 # sub-sample.  The stage is bound by instruction issue, not HBM, so its
 # roofline is the issue rate: 4 schedulers x 32 lanes per SM and cycle.
-IMAP_INSTR_PER_CELL = 848.0
-IMAP_INSTR_PER_SAMPLE = 193.5
+IMAP_INSTR_PER_CELL = 688.9
+IMAP_INSTR_PER_SAMPLE = 176.5
 
 
 def issue_roofline(dom, t_step, cfg, m, clocks):
