@@ -1444,7 +1444,9 @@ static int srcs_run(cg_ctx *c, long long *nsrc, bool readback)
   int rc;
   if (c->cfg.n_srcs > 0) {
     if (!c->d_counts && (rc = dalloc(c, &c->d_counts, (size_t)ncell))) return rc;
-    if (!c->d_bsums && (rc = dalloc(c, &c->d_bsums, (size_t)cg_srcs_nblocks(c->N)))) return rc;
+    if (!c->d_bsums && (rc = dalloc(c, &c->d_bsums, (size_t)(cg_srcs_nblocks(c->N) +
+                                                             cg_srcs_scan_room(cg_srcs_nblocks(c->N))))))
+      return rc;
     if (!c->d_total && (rc = dalloc(c, &c->d_total, (size_t)CG_NPOP_MAX))) return rc;
     if (!c->d_ovf_n && ((rc = dalloc(c, &c->d_ovf_cell, (size_t)CG_OVF_CAP)) ||
                         (rc = dalloc(c, &c->d_ovf_cnt, (size_t)CG_OVF_CAP)) || (rc = dalloc(c, &c->d_ovf_n, (size_t)1))))
@@ -1489,7 +1491,7 @@ static int srcs_run(cg_ctx *c, long long *nsrc, bool readback)
       ProfScope ps(c, "srcs_emit");
       CUDA_TRY(c, cg_srcs_emit(c->stream, c->d_npot, &p));
     }
-    c->launches += 3;
+    c->launches += 5; /* count, three scan passes, emission */
   }
   c->have_srcs = 1;
   return CG_OK;

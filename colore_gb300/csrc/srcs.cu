@@ -10,7 +10,7 @@
  *                  as uint16 and the block totals written out.  A cell with
  *                  CG_COUNT_ESC or more sources stores the escape value and
  *                  appends (cell, count) to a short overflow list.
- *   k_scan       : exclusive scan of the block totals (one block).
+ *   k_scan_*     : exclusive scan of the block totals (three coalesced passes).
  *   k_emit       : re-reads the counts, scans them inside the block and writes
  *                  every source at its final catalog index, in cell order (the
  *                  order of the reference run with one thread); the block's
@@ -156,33 +156,78 @@ __global__ void __launch_bounds__(SB, 6) k_pois_count(const float *__restrict__ 
   }
 }
 
-/* Exclusive scan of n block totals in place; total into *total. */
-__global__ void __launch_bounds__(1024) k_scan(long long *v, long long n, long long *total, unsigned int *err)
+/* Exclusive scan of the n block totals in place, their sum into *total, in
+ * three coalesced passes over tiles of SCAN_T values (a thread holds two
+ * neighbours): each tile reduced to its sum (tsum), the tile sums scanned by
+ * one block, then every tile scanned from its offset.  (One block walking
+ * the whole array took 0.87 ms at 1024^3.) */
+constexpr int SCAN_T = 2048;
+
+/* Exclusive scan of x over the block's 1024 threads; *tot = the block sum. */
+__device__ __forceinline__ long long block_scan(long long x, long long *ws, long long *tot)
 {
-  __shared__ long long s[1024];
-  const long long per = (n + 1023) / 1024;
-  const long long b = (long long)threadIdx.x * per, e = (b + per < n) ? b + per : n;
-  long long acc = 0;
-  for (long long i = b; i < e; i++) {
-    const long long x = v[i];
-    if (x > 0x7fffffffLL) atomicOr(err, ERR_COUNT_OVERFLOW); /* k_emit scans a block in int */
-    acc += x;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  long long inc = x;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
   }
-  s[threadIdx.x] = acc;
+  if (lane == 31) ws[w] = inc;
   __syncthreads();
-  for (int o = 1; o < 1024; o <<= 1) {
-    long long t = (int)threadIdx.x >= o ? s[threadIdx.x - o] : 0;
-    __syncthreads();
-    s[threadIdx.x] += t;
-    __syncthreads();
+  if (w == 0) {
+    long long y = ws[lane], yi = y;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long t = __shfl_up_sync(0xffffffffu, yi, o);
+      if (lane >= o) yi += t;
+    }
+    ws[lane] = yi - y;
+    if (lane == 31) ws[32] = yi;
   }
-  long long run = s[threadIdx.x] - acc;
-  for (long long i = b; i < e; i++) {
-    long long x = v[i];
-    v[i] = run;
-    run += x;
+  __syncthreads();
+  const long long ex = ws[w] + inc - x;
+  *tot = ws[32];
+  __syncthreads(); /* ws is reused by the next call */
+  return ex;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_tiles(const long long *__restrict__ v, long long n, long long *tsum,
+                                                     unsigned int *err)
+{
+  __shared__ long long ws[33];
+  const long long i = (long long)blockIdx.x * SCAN_T + 2 * (long long)threadIdx.x;
+  const long long a = i < n ? v[i] : 0, b = i + 1 < n ? v[i + 1] : 0;
+  if (a > 0x7fffffffLL || b > 0x7fffffffLL) atomicOr(err, ERR_COUNT_OVERFLOW); /* k_emit scans a block in int */
+  long long tot;
+  block_scan(a + b, ws, &tot);
+  if (threadIdx.x == 0) tsum[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_top(long long *tsum, long long nt, long long *total)
+{
+  __shared__ long long ws[33];
+  long long carry = 0;
+  for (long long c0 = 0; c0 < nt; c0 += 1024) {
+    const long long i = c0 + threadIdx.x;
+    const long long x = i < nt ? tsum[i] : 0;
+    long long tot;
+    const long long ex = block_scan(x, ws, &tot);
+    if (i < nt) tsum[i] = carry + ex;
+    carry += tot;
   }
-  if (threadIdx.x == 1023) *total = s[1023];
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_apply(long long *v, long long n, const long long *__restrict__ tsum)
+{
+  __shared__ long long ws[33];
+  const long long i = (long long)blockIdx.x * SCAN_T + 2 * (long long)threadIdx.x;
+  const long long a = i < n ? v[i] : 0, b = i + 1 < n ? v[i + 1] : 0;
+  long long tot;
+  const long long off = tsum[blockIdx.x] + block_scan(a + b, ws, &tot);
+  if (i < n) v[i] = off;
+  if (i + 1 < n) v[i + 1] = off + a;
 }
 
 /* Centred potential differences at a cell (get_rvel / get_element VEL). */
@@ -531,6 +576,7 @@ __global__ void __launch_bounds__(256) k_src_skewers(const float *__restrict__ d
 } /* namespace */
 
 long long cg_srcs_nblocks(int N) { return ((long long)N * N * N + CPB - 1) / CPB; }
+long long cg_srcs_scan_room(long long nb) { return (nb + SCAN_T - 1) / SCAN_T; }
 
 cudaError_t cg_srcs_count(cudaStream_t s, const float *grid, const cg_srcs_params *p, long long *total)
 {
@@ -539,7 +585,11 @@ cudaError_t cg_srcs_count(cudaStream_t s, const float *grid, const cg_srcs_param
   if (e == cudaSuccess) e = cudaMemsetAsync(p->block_sums, 0, nb * sizeof(long long), s);
   if (e != cudaSuccess) return e;
   k_pois_count<<<(unsigned)nb, SB, 0, s>>>(grid, *p);
-  k_scan<<<1, 1024, 0, s>>>(p->block_sums, nb, total, p->err);
+  const long long nt = cg_srcs_scan_room(nb);
+  long long *tsum = p->block_sums + nb; /* the tile sums, just past the block totals */
+  k_scan_tiles<<<(unsigned)nt, 1024, 0, s>>>(p->block_sums, nb, tsum, p->err);
+  k_scan_top<<<1, 1024, 0, s>>>(tsum, nt, total);
+  k_scan_apply<<<(unsigned)nt, 1024, 0, s>>>(p->block_sums, nb, tsum);
   return cudaGetLastError();
 }
 

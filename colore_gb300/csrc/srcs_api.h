@@ -30,7 +30,7 @@ struct cg_srcs_params {
   long long *ovf_cell;       /* cells holding CG_COUNT_ESC or more sources ...     */
   int *ovf_cnt;              /* ... and their counts                             */
   int *ovf_n;                /* entries used (zeroed by cg_srcs_count)           */
-  long long *block_sums;     /* per block; exclusive offsets after the scan */
+  long long *block_sums;     /* per block, then the scan's tile sums; exclusive offsets after the scan */
   long long capacity;
   float4 *pos;
   int *ipix;
@@ -77,6 +77,8 @@ struct cg_los_params {
 };
 
 long long cg_srcs_nblocks(int N);
+/* Scan scratch that block_sums needs past its nb entries (the tile sums). */
+long long cg_srcs_scan_room(long long nb);
 cudaError_t cg_srcs_count(cudaStream_t s, const float *grid, const cg_srcs_params *p, long long *total);
 cudaError_t cg_srcs_emit(cudaStream_t s, const float *phi, const cg_srcs_params *p);
 /* nsrc sources, or with nsrc_dev non-NULL min(*nsrc_dev, nsrc) read on the
