@@ -822,12 +822,20 @@ extern "C" int cg_memory_estimate(const cg_config *cfg, unsigned long long *byte
 }
 
 /* write_imap's normalisation (io.c:738-741): data/nadd where nadd > 0. */
+__device__ __forceinline__ float div_nadd(float d, int k) { return k > 0 ? d / (float)k : d; }
+
+/* data/nadd of m pixels (16-byte vectors; the buffers are cudaMalloc'd). */
 __global__ void k_div_nadd(const float *__restrict__ d, const int *__restrict__ n, float *out, long long m)
 {
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x) {
-    int k = n[i];
-    out[i] = k > 0 ? d[i] / (float)k : d[i];
+  const long long m4 = m >> 2, stride = (long long)gridDim.x * blockDim.x;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (long long i = t; i < m4; i += stride) {
+    const float4 a = reinterpret_cast<const float4 *>(d)[i];
+    const int4 k = reinterpret_cast<const int4 *>(n)[i];
+    reinterpret_cast<float4 *>(out)[i] = make_float4(div_nadd(a.x, k.x), div_nadd(a.y, k.y), div_nadd(a.z, k.z),
+                                                     div_nadd(a.w, k.w));
   }
+  for (long long i = 4 * m4 + t; i < m; i += stride) out[i] = div_nadd(d[i], n[i]);
 }
 
 /* ---- host outputs (cg_set_host_*) ---- */
