@@ -8,8 +8,9 @@
  * r + dr_rsd) and a RING pixel, where temp is added and a hit counted.  The
  * shells and pixels are decided as the reference's double arithmetic
  * decides them: in single precision where a bound on the distance to the
- * double value proves the decision, in double otherwise (cg_exact.h), so the
- * hit counts are those of the double arithmetic.
+ * double value proves the decision, in float-float where that bound fails,
+ * and in double only where the float-float bound fails too (cg_exact.h), so
+ * the hit counts are those of the double arithmetic.
  *
  * nsub is fixed by the shell of the cell's corner radius and grows towards
  * the observer (from 2 at high redshift to ~20 for the nearest shells), so
@@ -20,19 +21,22 @@
  *                  one cell (listed or not, its shell, brightness, radial
  *                  shift, and whether all its samples certainly stay in one
  *                  shell, which spares them the radial test) and appends it
- *                  to its bucket with one atomic per bucket and warp.  A cell
- *                  that finds its bucket full is painted by its warp on the
- *                  spot.
+ *                  to its bucket: one atomic per bucket present in the warp,
+ *                  all issued together.  A cell that finds its bucket full is
+ *                  painted by its warp on the spot.
  *   k_imap_chunks  One thread cuts each bucket into chunks of about CHS
  *                  samples: whole cells, or slices of one cell.
  *   k_imap_paint   Warps take chunks in bucket order, so the maps' working
  *                  set at any time is a few shells (25 MB per shell at nside
- *                  512) and the atomics stay in L2.  32 consecutive samples
- *                  per step; runs of equal (cell, shell, pixel) across the
- *                  lanes are added with one float and one integer atomic.
- *                  Samples whose margins fail are queued.
- *   k_imap_double  One thread per queued sample: the cell's radial shift and
- *                  the sample's shell and pixel in double, then its atomics.
+ *                  512) and the atomics stay in L2.  Each lane walks one unit
+ *                  sample by sample, keeping two (key, count) run slots that
+ *                  it evicts with one float and one integer atomic.  Samples
+ *                  whose margins fail are staged per warp in shared memory
+ *                  and queued in batches.
+ *   k_imap_double  The queued samples: first in float-float, then, for the
+ *                  few left, gathered per warp and decided in double 32 at a
+ *                  time, the cell's radial shift computed once per run of
+ *                  one record.
  */
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
