@@ -312,8 +312,9 @@ int cg_set_profiling(cg_ctx *ctx, int on);
  * the reference, which computes in double throughout): Poisson counts,
  * base and count-map pixels and intensity-map hits are decided in single
  * precision where a bound on the distance to the double value proves the
- * decision, and in double otherwise.  With all != 0 every such decision is
- * taken in double (slow; for checking).  cg_exact_stats reads the numbers of
+ * decision, and in double otherwise (intensity-map samples try float-float
+ * arithmetic in between).  With all != 0 every such decision is taken in
+ * double (slow; for checking).  cg_exact_stats reads the numbers of
  * decisions taken in double since the last reset: [0] cells' counts,
  * [1] source pixels, [2] intensity-map cells, [3] intensity-map samples. */
 int cg_set_decisions_in_double(cg_ctx *ctx, int all);
