@@ -370,7 +370,8 @@ def run_ours(args):
         "exact_decisions": {"per_step": {k: v / max(args.steps, 1) for k, v in exact.items()},
                             "note": "decisions taken in double per step (cells' counts, source pixels, "
                                     "intensity-map cells and sub-samples); every other decision in single "
-                                    "precision with a proven margin"},
+                                    "precision with a proven margin, or in float-float for the intensity-map "
+                                    "sub-samples that margin leaves open"},
         "roofline_dominant": issue_roofline(dom, t_step, cfg, m, clk.summary()) if dom else None,
         "clocks": clk.summary(),
     }
