@@ -302,6 +302,9 @@ __global__ void __launch_bounds__(IW * 32) k_imap_list(const float *__restrict__
             }
           }
         }
+        /* nothing to append (a chunk outside the shells' radial range, about
+         * half of them): skip the bucket reservation */
+        if (!__any_sync(FULL, want)) continue;
         /* append to the buckets: one atomic per bucket present in the warp,
          * issued together by each bucket's first lane (one round trip) */
         bool over = false;
