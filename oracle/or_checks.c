@@ -80,6 +80,25 @@ void or_pix_checked(long nside, const float *xyz, long n, float ein, long long *
   }
 }
 
+/* The float-float operations of cg_ff.h on n operand pairs: op 0 sum,
+ * 1 product, 2 quotient, 3 square root of x, 4 product by the float y.h;
+ * x and y as (h, l) pairs in xh/xl, yh/yl, the result in oh/ol. */
+void or_ff_ops(int op, const float *xh, const float *xl, const float *yh, const float *yl, long n, float *oh,
+               float *ol)
+{
+  for (long i = 0; i < n; i++) {
+    const cg_ff x = cg_ff_make(xh[i], xl[i]), y = cg_ff_make(yh[i], yl[i]);
+    cg_ff r;
+    if (op == 0) r = cg_ff_add(x, y);
+    else if (op == 1) r = cg_ff_mul(x, y);
+    else if (op == 2) r = cg_ff_div(x, y);
+    else if (op == 3) r = cg_ff_sqrt(x);
+    else r = cg_ff_mulf(x, y.h);
+    oh[i] = r.h;
+    ol[i] = r.l;
+  }
+}
+
 /* RING pixels of float-float positions (6 floats each: x, its rest, y, ...)
  * by the float-float tier (cg_pix_ff; -1 where it defers to double), each
  * within eP[i] of the double position. */

@@ -52,13 +52,13 @@ def lib():
             "or_shell_index": [vp, vp, i, vp, vp, vp, C.c_long],
             "or_pix_checked": [C.c_long, vp, C.c_long, f, vp], "or_pix_cgx": [C.c_long, vp, C.c_long, vp],
             "or_pix64": [C.c_long, vp, C.c_long, vp], "or_pix_ff": [C.c_long, vp, vp, C.c_long, vp],
-            "or_atan_q_maxerr": [],
+            "or_atan_q_maxerr": [], "or_ff_ops": [i, vp, vp, vp, vp, C.c_long, vp, vp],
             "or_sht_legendre": [i, i, i, vp, vp, vp, d, vp],
             "or_src_offset_checked": [C.c_long, vp, d, vp, vp, vp, vp],
             "or_ptrs_checked": [C.c_long, vp, vp, vp, vp, C.c_uint32, C.c_uint32, vp, vp],
         }
         void = ("or_philox", "or_poisson", "or_ang2pix", "or_nest2ring", "or_ring2nest", "or_pix2vec_nest",
-                "or_shell_index", "or_pix_checked", "or_pix_cgx", "or_pix64", "or_pix_ff", "or_src_offset_checked",
+                "or_shell_index", "or_pix_checked", "or_pix_cgx", "or_pix64", "or_pix_ff", "or_ff_ops", "or_src_offset_checked",
                 "or_ptrs_checked")
         for k, a in sig.items():
             fn = getattr(L, k)
@@ -517,6 +517,17 @@ def pix_ff(nside, xyz, rel=2.0 ** -47):
     out = np.empty(len(a), np.int64)
     lib().or_pix_ff(nside, P(q), P(eP), len(a), P(out))
     return out
+
+
+def ff_ops(op, x, y=None):
+    """cg_ff.h's operation op (0 sum, 1 product, 2 quotient, 3 root of x,
+    4 product by a float) on float-float operands given as (h, l) arrays."""
+    xh, xl = (np.ascontiguousarray(a, np.float32) for a in x)
+    yh, yl = (np.ascontiguousarray(a, np.float32) for a in (y if y is not None else (xh, xl)))
+    oh = np.empty_like(xh)
+    ol = np.empty_like(xh)
+    lib().or_ff_ops(op, P(xh), P(xl), P(yh), P(yl), len(xh), P(oh), P(ol))
+    return oh, ol
 
 
 def pix64(nside, xyz, shared=False):

@@ -125,6 +125,47 @@ def test_float_float_pixels_never_disagree_with_double(ns):
             assert (orc.pix_checked(ns, v.astype(np.float32)) < 0).mean() > 0.99
 
 
+@pytest.mark.parametrize("op,bound", [(0, 4), (1, 5), (2, 16), (3, 4), (4, 2)])
+def test_float_float_operations_within_their_bounds(op, bound):
+    """cg_ff.h's sum, product, quotient, square root and product by a float
+    on random normalised pairs (both signs, magnitudes 1e-3..1e4, so sums
+    cancel) against exact rational arithmetic: the relative error stays
+    within the u^2 = 2^-48 multiples the float-float pixel bounds use."""
+    from decimal import Decimal, getcontext
+    from fractions import Fraction
+    import oracle as orc
+    getcontext().prec = 80
+    r = np.random.default_rng(100 + op)
+
+    def pairs(n):
+        h = (r.choice([-1, 1], n) * 10 ** r.uniform(-3, 4, n)).astype(np.float32)
+        l = (r.uniform(-0.5, 0.5, n) * np.spacing(np.abs(h)).astype(np.float64)).astype(np.float32)
+        return h, l
+
+    n = 4000
+    (xh, xl), (yh, yl) = pairs(n), pairs(n)
+    if op == 3:
+        xl = np.where(xh < 0, -xl, xl).astype(np.float32)
+        xh = np.abs(xh)
+    if op == 4:
+        yl = np.zeros(n, np.float32)
+    oh, ol = orc.ff_ops(op, (xh, xl), (yh, yl))
+    u2 = Fraction(1, 2 ** 48)
+    worst = 0.0
+    for i in range(n):
+        X = Fraction(float(xh[i])) + Fraction(float(xl[i]))
+        Y = Fraction(float(yh[i])) + Fraction(float(yl[i]))
+        R = Fraction(float(oh[i])) + Fraction(float(ol[i]))
+        if op == 3:
+            s = (Decimal(X.numerator) / Decimal(X.denominator)).sqrt()
+            rel = float(abs((Decimal(R.numerator) / Decimal(R.denominator) - s) / s) * Decimal(2 ** 48))
+        else:
+            E = X + Y if op == 0 else (X / Y if op == 2 else X * Y)
+            rel = float(abs((R - E) / E) / u2) if E != 0 else 0.0
+        worst = max(worst, rel)
+    assert worst <= bound, (op, worst)
+
+
 def test_quarter_turn_atan_exhaustive():
     """The polynomial behind every float direction's quarter-turn angle
     (cg_atan01_q) is within 8.2e-8 of atan(t) / (pi/2) for every float t in
