@@ -695,8 +695,17 @@ CG_HD int cg_lambda_checked(const cg_pois_args *a, int ix, int iy, int iz, float
     dn.v = a->norm[a->na];
     dn.e = CG_MUL(cg_fabsf(dn.v), 2.0f * CG_E24);
   }
-  if (!(nd.v > nd.e)) return nd.e == 0.0f ? 0 : 2; /* ndens > 0 (srcs.c:171) */
   const cg_ve bm = cg_bias_ve(d, b.v, b.e, a->bias_model);
+  if (!(nd.v > nd.e)) { /* ndens > 0 (srcs.c:171) not certain */
+    if (nd.e == 0.0f) return 0;
+    /* the double lambda is 0 (ndens <= 0: no source) or lies in
+     * (0, (nd + e_nd) cv (bm + e_bm) (dn + e_dn)]: inversion with lambda 0
+     * and that upper end as its bound (six roundings, taken as 2^-20) */
+    const float lhi = CG_MUL(CG_MUL(CG_MUL(CG_MUL(CG_ADD(nd.v, nd.e), a->cell_vol), CG_ADD(bm.v, bm.e)),
+                                    CG_ADD(dn.v, dn.e)), 1.000001f);
+    *elam = lhi;
+    return lhi < 10.0f ? 1 : 2;
+  }
   const float nc = CG_MUL(nd.v, a->cell_vol);
   const float l = CG_MUL(CG_MUL(nc, bm.v), dn.v);
   const float bmh = CG_ADD(bm.v, bm.e), dnh = CG_ADD(dn.v, dn.e);
@@ -709,7 +718,7 @@ CG_HD int cg_lambda_checked(const cg_pois_args *a, int ix, int iy, int iz, float
   e = CG_FMA(CG_MUL(1.01f, a->cell_vol), e, CG_MUL(l, 8.0f * CG_E24));
   *lam = l;
   *elam = e;
-  if (!(l > 0.0f)) return e == 0.0f ? 0 : 2;
+  if (!(l > 0.0f)) return e == 0.0f ? 0 : (e < 10.0f ? 1 : 2); /* lambda in [0, e]: inversion with lambda 0 */
   if (!(CG_ADD(l, e) < 10.0f)) return CG_SUB(l, e) >= 10.0f ? 3 : 2; /* PTRS, or too close to the switch */
   return 1;
 }

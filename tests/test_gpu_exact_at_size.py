@@ -1,7 +1,8 @@
-"""Integer outputs at a larger size: the c4 configuration at 256^3 (1LPT,
+"""Integer outputs at larger sizes: the c4 configuration at 256^3 (1LPT,
 one population with an nside 512 count map; its 64-shell intensity map at
 nside 64, so that forcing every sub-sample into the double pass fits that
-pass's queue) run twice on the device, once as the kernels decide (single
+pass's queue) and the c2 configuration at 512^3 (lognormal, two
+populations with nside 256 count maps), each run twice on the device, once as the kernels decide (single
 precision with proven margins, float-float for the intensity-map samples
 those margins leave open, double for the rest) and once with every decision
 taken in the device's double arithmetic (cg_set_decisions_in_double).  The
@@ -15,12 +16,21 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _run(tmp_path, double):
+def _spec(name):
+    from colore_gb300 import inputs
+    if name == "c4":
+        spec = inputs.scaled("c4", 256)
+        spec["imap"] = [dict(spec["imap"][0], nside=64)]
+    else:
+        spec = inputs.scaled("c2", 512)
+    spec.pop("kappa", None)
+    return spec
+
+
+def _run(tmp_path, name, double):
     import colore_gb300 as cg
     from colore_gb300 import inputs
-    spec = inputs.scaled("c4", 256)
-    spec.pop("kappa", None)
-    spec["imap"] = [dict(spec["imap"][0], nside=64)]
+    spec = _spec(name)
     m = cg.Mock(cg.Params(inputs.write_inputs(str(tmp_path), spec)))
     m.set_decisions_in_double(double)
     m.create_cartesian_fields()
@@ -28,23 +38,36 @@ def _run(tmp_path, double):
     m.compute_density_normalization()
     m.exact_stats(reset=True)
     nsrc = list(m.srcs_set_cartesian())
-    m.imap_set_cartesian()
+    imap = bool(spec.get("imap"))
+    if imap:
+        m.imap_set_cartesian()
     st = m.exact_stats()
-    cat = m.catalog(0, pos=True, ipix=True, src=False)
-    out = dict(nsrc=nsrc, pos=cat["pos"].copy(), ipix=cat["ipix"].copy(), cmap=m.count_map(0).copy(),
-               nadd=m.imap(0, with_nadd=True)[1].copy(), samples=m.imap_samples(0), stats=st)
+    out = dict(nsrc=nsrc, stats=st, cats=[], cmaps=[])
+    for ip in range(len(nsrc)):
+        cat = m.catalog(ip, pos=True, ipix=True, src=False)
+        out["cats"].append((cat["pos"].copy(), cat["ipix"].copy()))
+        out["cmaps"].append(m.count_map(ip).copy())
+    if imap:
+        out["nadd"] = m.imap(0, with_nadd=True)[1].copy()
+        out["samples"] = m.imap_samples(0)
     m.close()
     return out
 
 
-def test_c4_256_decisions_equal_forced_double(tmp_path_factory):
-    a = _run(tmp_path_factory.mktemp("margins"), False)
-    b = _run(tmp_path_factory.mktemp("double"), True)
-    print("decided in double with the margins:", a["stats"], "forced:", b["stats"])
+@pytest.mark.parametrize("name", ["c4", "c2"])
+def test_decisions_equal_forced_double_at_size(tmp_path_factory, name):
+    a = _run(tmp_path_factory.mktemp("margins"), name, False)
+    b = _run(tmp_path_factory.mktemp("double"), name, True)
+    print(name, "decided in double with the margins:", a["stats"], "forced:", b["stats"])
     assert a["nsrc"] == b["nsrc"] and a["nsrc"][0] > 10 ** 7
-    assert np.array_equal(a["pos"], b["pos"])
-    assert np.array_equal(a["ipix"], b["ipix"])
-    assert np.array_equal(a["cmap"], b["cmap"])
+    for (pa, ia), (pb, ib) in zip(a["cats"], b["cats"]):
+        assert np.array_equal(pa, pb)
+        assert np.array_equal(ia, ib)
+    for ca, cb in zip(a["cmaps"], b["cmaps"]):
+        assert np.array_equal(ca, cb)
+    assert a["stats"]["count_cells"] < 1e-3 * b["stats"]["count_cells"]
+    if "nadd" not in a:
+        return
     assert a["samples"] == b["samples"] and a["samples"] > 10 ** 6
     assert np.array_equal(a["nadd"], b["nadd"]), int((a["nadd"] != b["nadd"]).sum())
     # the forced run took every sample in double; the margins left few
